@@ -1,0 +1,333 @@
+"""ctypes mirror of include/icsfoam_gb300.h.
+
+``Binding`` wraps one shared library that exports the C ABI under a given
+symbol prefix ("ics_" for the CUDA library).  ``CaseHandle`` owns one
+``ics_handle`` plus the numpy arrays whose pointers were handed over.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import mesh as _mesh
+
+ICS_OK = 0
+ICS_ERR_ARG = 1
+ICS_ERR_CUDA = 2
+ICS_ERR_NONFINITE = 3
+ICS_ERR_BREAKDOWN = 4
+ICS_ERR_DIAG = 5
+ICS_ERR_SCHEME = 6
+ICS_ERR_STATE = 7
+ICS_ERR_NOMEM = 8
+ICS_ERR_TIMEOUT = 9
+
+STATUS_NAMES = {
+    0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "non-finite value",
+    4: "Krylov breakdown", 5: "zero diagonal", 6: "unknown scheme",
+    7: "call order", 8: "out of device memory", 9: "device wait timeout",
+}
+
+FLUX = {"AUSMPlusUp": 0, "HLLC": 1, "ROE": 2}
+RECON = {"upwind": 0, "vanLeer": 1, "Minmod": 2, "MUSCLVenkatakrishnan": 3, "MUSCLMinmod": 4}
+DDT = {"steadyState": 0, "Euler": 1, "backward": 2}
+PRECON = {"none": 0, "LUSGS": 1, "Jacobi": 2}
+PRECISION = {"fp64": 0, "mixed": 1}
+
+
+class IcsError(RuntimeError):
+    def __init__(self, status: int, where: str, msg: str = ""):
+        super().__init__(f"{where}: {STATUS_NAMES.get(status, status)} ({status}) {msg}".strip())
+        self.status = status
+
+
+class PatchDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("is_wall", C.c_int32), ("p", C.c_double), ("T", C.c_double),
+                ("U", C.c_double * 3), ("p0", C.c_double), ("T0", C.c_double)]
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [
+        ("n_cells", C.c_int32), ("n_faces", C.c_int32), ("n_bfaces", C.c_int32), ("n_patches", C.c_int32),
+        ("owner", C.c_void_p), ("neighbour", C.c_void_p),
+        ("Sf", C.c_void_p), ("Cf", C.c_void_p), ("weights", C.c_void_p),
+        ("delta_coeffs", C.c_void_p), ("nonorth_delta_coeffs", C.c_void_p),
+        ("C", C.c_void_p), ("V", C.c_void_p),
+        ("b_cell", C.c_void_p), ("b_patch", C.c_void_p), ("b_Sf", C.c_void_p), ("b_Cf", C.c_void_p),
+        ("b_delta_coeffs", C.c_void_p), ("patches", C.POINTER(PatchDesc)),
+        ("solution_d", C.c_int32 * 3),
+    ]
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("R", C.c_double), ("Cp", C.c_double),
+        ("mu", C.c_double), ("Pr", C.c_double), ("As", C.c_double), ("Ts", C.c_double),
+        ("sutherland", C.c_int32), ("viscous", C.c_int32),
+        ("flux_scheme", C.c_int32), ("low_mach_ausm", C.c_int32), ("entropy_fix_coeff", C.c_double),
+        ("recon_rho", C.c_int32), ("recon_U", C.c_int32), ("recon_T", C.c_int32),
+        ("ddt_scheme", C.c_int32), ("delta_t", C.c_double),
+        ("solver", C.c_int32), ("preconditioner", C.c_int32), ("n_directions", C.c_int32),
+        ("max_iter", C.c_int32), ("min_iter", C.c_int32),
+        ("tolerance", C.c_double), ("rel_tol", C.c_double),
+        ("precision", C.c_int32),
+        ("n_pseudo_corr", C.c_int32), ("n_pseudo_corr_min", C.c_int32),
+        ("pseudo_tol", C.c_double), ("pseudo_tol_rel", C.c_double),
+        ("pseudo_co_num", C.c_double), ("pseudo_co_num_min", C.c_double), ("pseudo_co_num_max", C.c_double),
+        ("pseudo_co_max_increase", C.c_double), ("pseudo_co_min_decrease", C.c_double),
+        ("local_timestepping", C.c_int32), ("local_timestepping_bounding", C.c_int32),
+        ("local_timestepping_lower_bound", C.c_double),
+        ("reset_pseudo", C.c_int32),
+        ("rho_min", C.c_double), ("T_min", C.c_double), ("T_max", C.c_double),
+    ]
+
+
+class SolverPerf(C.Structure):
+    _fields_ = [("init_res", C.c_double * 5), ("final_res", C.c_double * 5),
+                ("n_iterations", C.c_int32), ("converged", C.c_int32)]
+
+    def as_dict(self):
+        return {"init_res": list(self.init_res), "final_res": list(self.final_res),
+                "n_iterations": int(self.n_iterations), "converged": bool(self.converged)}
+
+
+class IterStats(C.Structure):
+    _fields_ = [("perf", SolverPerf), ("rho_l2_residual", C.c_double), ("pseudo_co_mean", C.c_double),
+                ("bounded_cells", C.c_int32), ("status", C.c_int32)]
+
+
+# exported functions: name -> (restype, argtypes)
+_P = C.c_void_p
+_FUNCS = {
+    "default_config": (None, [C.POINTER(Config)]),
+    "create": (C.c_int, [C.POINTER(MeshDesc), C.POINTER(Config), C.POINTER(_P)]),
+    "destroy": (C.c_int, [_P]),
+    "set_config": (C.c_int, [_P, C.POINTER(Config)]),
+    "last_error": (C.c_int, [_P, C.c_char_p, C.c_int32]),
+    "set_primitive": (C.c_int, [_P, _P, _P, _P]),
+    "set_boundary_state": (C.c_int, [_P, _P, _P, _P, _P]),
+    "get_boundary_state": (C.c_int, [_P, _P, _P, _P, _P]),
+    "get_state": (C.c_int, [_P, _P, _P, _P, _P]),
+    "set_conservative": (C.c_int, [_P, _P, C.c_int32]),
+    "set_pseudo_co": (C.c_int, [_P, _P]),
+    "get_pseudo_co": (C.c_int, [_P, _P, _P]),
+    "calc_flux": (C.c_int, [_P, _P, _P, _P]),
+    "residual": (C.c_int, [_P, _P]),
+    "assemble_jacobian": (C.c_int, [_P]),
+    "get_jacobian": (C.c_int, [_P, _P, _P, _P]),
+    "matrix_mul": (C.c_int, [_P, _P, _P]),
+    "precondition": (C.c_int, [_P, _P]),
+    "solve_increment": (C.c_int, [_P, C.POINTER(SolverPerf), _P]),
+    "update_fields": (C.c_int, [_P, C.POINTER(IterStats)]),
+    "pseudo_iteration": (C.c_int, [_P, C.POINTER(IterStats)]),
+    "begin_time_step": (C.c_int, [_P]),
+    "pseudo_loop": (C.c_int, [_P, C.POINTER(C.c_int32)]),
+}
+
+EXPORTED = tuple(_FUNCS)
+
+
+class Binding:
+    """Typed access to one library exporting the C ABI with ``prefix``."""
+
+    def __init__(self, lib: C.CDLL, prefix: str):
+        self.lib = lib
+        self.prefix = prefix
+        self.fn = {}
+        for name, (res, args) in _FUNCS.items():
+            f = getattr(lib, prefix + name)
+            f.restype = res
+            f.argtypes = args
+            self.fn[name] = f
+
+    def default_config(self) -> Config:
+        cfg = Config()
+        self.fn["default_config"](C.byref(cfg))
+        return cfg
+
+
+def _ptr(a: Optional[np.ndarray]):
+    if a is None:
+        return None
+    return a.ctypes.data
+
+
+class CaseHandle:
+    """One case (mesh + state) behind the C ABI of ``binding``."""
+
+    def __init__(self, binding: Binding, mesh: _mesh.Mesh, cfg: Config):
+        self.b = binding
+        self.mesh = mesh
+        self.N = mesh.n_cells
+        self.F = mesh.n_faces
+        self.B = mesh.n_bfaces
+        self._keep = []
+        desc = MeshDesc()
+        desc.n_cells, desc.n_faces, desc.n_bfaces = self.N, self.F, self.B
+        desc.n_patches = len(mesh.patches)
+
+        def keep(a, dt):
+            a = np.ascontiguousarray(a, dtype=dt)
+            self._keep.append(a)
+            return a.ctypes.data
+
+        desc.owner = keep(mesh.owner, np.int32)
+        desc.neighbour = keep(mesh.neighbour, np.int32)
+        desc.Sf = keep(mesh.Sf, np.float64)
+        desc.Cf = keep(mesh.Cf, np.float64)
+        desc.weights = keep(mesh.weights, np.float64)
+        desc.delta_coeffs = keep(mesh.delta_coeffs, np.float64)
+        desc.nonorth_delta_coeffs = keep(mesh.nonorth_delta_coeffs, np.float64)
+        desc.C = keep(mesh.C, np.float64)
+        desc.V = keep(mesh.V, np.float64)
+        desc.b_cell = keep(mesh.b_cell, np.int32)
+        desc.b_patch = keep(mesh.b_patch, np.int32)
+        desc.b_Sf = keep(mesh.b_Sf if self.B else np.zeros((0, 3)), np.float64)
+        desc.b_Cf = keep(mesh.b_Cf if self.B else np.zeros((0, 3)), np.float64)
+        desc.b_delta_coeffs = keep(mesh.b_delta_coeffs, np.float64)
+        pats = (PatchDesc * max(1, len(mesh.patches)))()
+        for i, p in enumerate(mesh.patches):
+            pats[i].kind = p.kind
+            pats[i].is_wall = int(p.is_wall)
+            pats[i].p, pats[i].T = p.p, p.T
+            for k in range(3):
+                pats[i].U[k] = p.U[k]
+            pats[i].p0, pats[i].T0 = p.p0, p.T0
+        self._keep.append(pats)
+        desc.patches = pats
+        for k in range(3):
+            desc.solution_d[k] = mesh.solution_d[k]
+        self.cfg = cfg
+        h = C.c_void_p()
+        st = binding.fn["create"](C.byref(desc), C.byref(cfg), C.byref(h))
+        if st != ICS_OK:
+            raise IcsError(st, binding.prefix + "create")
+        self.h = h
+
+    # ---------------------------------------------------------------- utils
+    def _check(self, st: int, where: str, ok=(ICS_OK,)):
+        if st not in ok:
+            buf = C.create_string_buffer(512)
+            if self.h:
+                self.b.fn["last_error"](self.h, buf, 512)
+            raise IcsError(st, self.b.prefix + where, buf.value.decode(errors="replace"))
+        return st
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.b.fn["destroy"](self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---------------------------------------------------------------- state
+    def set_config(self, cfg: Config):
+        self.cfg = cfg
+        self._check(self.b.fn["set_config"](self.h, C.byref(cfg)), "set_config")
+
+    def set_primitive(self, p, U, T):
+        p = np.ascontiguousarray(p, np.float64)
+        U = np.ascontiguousarray(U, np.float64).reshape(self.N, 3)
+        T = np.ascontiguousarray(T, np.float64)
+        self._check(self.b.fn["set_primitive"](self.h, _ptr(p), _ptr(U), _ptr(T)), "set_primitive")
+
+    def set_conservative(self, W, set_old=False):
+        W = np.ascontiguousarray(W, np.float64).reshape(self.N, 5)
+        self._check(self.b.fn["set_conservative"](self.h, _ptr(W), int(set_old)), "set_conservative")
+
+    def get_state(self):
+        W = np.empty((self.N, 5))
+        p = np.empty(self.N)
+        U = np.empty((self.N, 3))
+        T = np.empty(self.N)
+        self._check(self.b.fn["get_state"](self.h, _ptr(W), _ptr(p), _ptr(U), _ptr(T)), "get_state")
+        return {"W": W, "p": p, "U": U, "T": T}
+
+    def get_boundary_state(self):
+        p = np.empty(self.B)
+        U = np.empty((self.B, 3))
+        T = np.empty(self.B)
+        phi = np.empty(self.B)
+        self._check(self.b.fn["get_boundary_state"](self.h, _ptr(p), _ptr(U), _ptr(T), _ptr(phi)),
+                    "get_boundary_state")
+        return {"p": p, "U": U, "T": T, "phi": phi}
+
+    def set_boundary_state(self, p, U, T, phi):
+        arrs = [np.ascontiguousarray(a, np.float64) if a is not None else None for a in (p, U, T, phi)]
+        self._check(self.b.fn["set_boundary_state"](self.h, *[_ptr(a) for a in arrs]), "set_boundary_state")
+
+    def set_pseudo_co(self, co):
+        co = np.ascontiguousarray(np.broadcast_to(co, (self.N,)), np.float64)
+        self._check(self.b.fn["set_pseudo_co"](self.h, _ptr(co)), "set_pseudo_co")
+
+    def get_pseudo_co(self):
+        co = np.empty(self.N)
+        r = np.empty(self.N)
+        self._check(self.b.fn["get_pseudo_co"](self.h, _ptr(co), _ptr(r)), "get_pseudo_co")
+        return co, r
+
+    # ------------------------------------------------------------- hot path
+    def calc_flux(self):
+        n = self.F + self.B
+        phi = np.empty(n)
+        phiU = np.empty((n, 3))
+        phiE = np.empty(n)
+        self._check(self.b.fn["calc_flux"](self.h, _ptr(phi), _ptr(phiU), _ptr(phiE)), "calc_flux")
+        return phi, phiU, phiE
+
+    def residual(self):
+        s = np.empty((self.N, 5))
+        self._check(self.b.fn["residual"](self.h, _ptr(s)), "residual")
+        return s
+
+    def assemble_jacobian(self):
+        self._check(self.b.fn["assemble_jacobian"](self.h), "assemble_jacobian")
+
+    def get_jacobian(self):
+        d = np.empty((self.N, 5, 5))
+        lo = np.empty((self.F, 5, 5))
+        up = np.empty((self.F, 5, 5))
+        self._check(self.b.fn["get_jacobian"](self.h, _ptr(d), _ptr(lo), _ptr(up)), "get_jacobian")
+        return d, lo, up
+
+    def matrix_mul(self, x):
+        x = np.ascontiguousarray(x, np.float64).reshape(self.N, 5)
+        y = np.empty((self.N, 5))
+        self._check(self.b.fn["matrix_mul"](self.h, _ptr(x), _ptr(y)), "matrix_mul")
+        return y
+
+    def precondition(self, r):
+        r = np.array(r, dtype=np.float64, copy=True).reshape(self.N, 5)
+        self._check(self.b.fn["precondition"](self.h, _ptr(r)), "precondition")
+        return r
+
+    def solve_increment(self, allow=(ICS_OK,)):
+        perf = SolverPerf()
+        dW = np.empty((self.N, 5))
+        st = self._check(self.b.fn["solve_increment"](self.h, C.byref(perf), _ptr(dW)), "solve_increment", allow)
+        return perf, dW, st
+
+    def update_fields(self):
+        s = IterStats()
+        self._check(self.b.fn["update_fields"](self.h, C.byref(s)), "update_fields")
+        return s
+
+    def pseudo_iteration(self):
+        s = IterStats()
+        self._check(self.b.fn["pseudo_iteration"](self.h, C.byref(s)), "pseudo_iteration")
+        return s
+
+    def begin_time_step(self):
+        self._check(self.b.fn["begin_time_step"](self.h), "begin_time_step")
+
+    def pseudo_loop(self) -> bool:
+        more = C.c_int32()
+        self._check(self.b.fn["pseudo_loop"](self.h, C.byref(more)), "pseudo_loop")
+        return bool(more.value)

@@ -1,0 +1,151 @@
+"""Synthetic workloads: meshes, patches, initial fields and solver settings.
+
+The reference is quoted on cases that are not shipped with it, so every mesh
+here is generated from fixed seeds:
+
+* ``shock_tube``   - 1D Sod problem, hex cells one thick, empty sides.
+* ``bump_channel`` - 3D inviscid channel with a circular-arc bump on the
+                     lower wall, total-pressure inlet and static-pressure
+                     outlet, slip walls (the transonic circularArcBump layout).
+* ``random_box``   - hex box with randomly displaced interior vertices, cells
+                     randomly permuted then reverse-Cuthill-McKee renumbered.
+
+Sizes are parameters; the headline sizes are 1000 cells, 256x64x64 and 200^3.
+"""
+
+from __future__ import annotations
+
+import dataclasses
+from typing import Dict, Optional
+
+import numpy as np
+
+from . import mesh as M
+from . import ordering
+
+
+@dataclasses.dataclass
+class Workload:
+    name: str
+    mesh: M.Mesh
+    p: np.ndarray
+    U: np.ndarray
+    T: np.ndarray
+    settings: Dict  # ics_config field overrides
+
+
+GAMMA = 1.4
+R_GAS = 287.0
+CP = GAMMA * R_GAS / (GAMMA - 1.0)   # 1004.5
+
+
+def thermo_settings():
+    return {"R": R_GAS, "Cp": CP}
+
+
+def shock_tube(n: int = 1000, x0: float = -5.0, x1: float = 5.0, ordering_mode: str = "natural") -> Workload:
+    """Sod shock tube: left p=1e5 T=348.4, right p=1e4 T=278.7, u=0."""
+    xs = np.linspace(x0, x1, n + 1)
+    g = np.zeros((n + 1, 2, 2, 3))
+    g[..., 0] = xs[:, None, None]
+    g[:, 1, :, 1] = 1.0 * (x1 - x0) / n
+    g[:, :, 1, 2] = 1.0 * (x1 - x0) / n
+    ends = M.Patch("sides", M.PATCH_ZERO_GRADIENT)
+    empty = M.Patch("empty", M.PATCH_EMPTY)
+    sides = {"xmin": ends, "xmax": ends, "ymin": empty, "ymax": empty, "zmin": empty, "zmax": empty}
+    mesh = M.hex_mesh(g, sides)
+    mesh = ordering.apply(mesh, ordering_mode)
+    x = mesh.C[:, 0]
+    left = x < 0.0
+    p = np.where(left, 1.0e5, 1.0e4)
+    T = np.where(left, 348.4, 278.7)
+    U = np.zeros((mesh.n_cells, 3))
+    settings = dict(thermo_settings(), flux_scheme=0, ddt_scheme=2, delta_t=1e-5,
+                    pseudo_co_num=50.0, pseudo_co_num_max=50.0, n_pseudo_corr=10,
+                    pseudo_tol=1e-5, pseudo_tol_rel=1e-5,
+                    n_directions=8, max_iter=20, tolerance=1e-12, rel_tol=1e-4)
+    return Workload("shock_tube_%d" % n, mesh, p, U, T, settings)
+
+
+def bump_points(nx: int, ny: int, nz: int, length=3.0, height=1.0, width=0.5, thickness=0.1) -> np.ndarray:
+    """Grid points of a channel x in [-1, 2] with a circular-arc bump on x in [0, 1]."""
+    xs = np.linspace(-1.0, -1.0 + length, nx + 1)
+    Rb = (0.25 + thickness ** 2) / (2.0 * thickness)
+    yb = np.where((xs > 0.0) & (xs < 1.0), np.sqrt(np.maximum(Rb ** 2 - (xs - 0.5) ** 2, 0.0)) - (Rb - thickness), 0.0)
+    eta = np.linspace(0.0, 1.0, ny + 1)
+    zs = np.linspace(0.0, width, nz + 1)
+    g = np.zeros((nx + 1, ny + 1, nz + 1, 3))
+    g[..., 0] = xs[:, None, None]
+    g[..., 1] = (yb[:, None] + eta[None, :] * (height - yb[:, None]))[:, :, None]
+    g[..., 2] = zs[None, None, :]
+    return g
+
+
+def bump_channel(nx: int = 256, ny: int = 64, nz: int = 64, mach: float = 0.675, p0: float = 1.0e5,
+                 T0: float = 300.0, ordering_mode: str = "colour", second_order: bool = True,
+                 flux: str = "HLLC") -> Workload:
+    """Inviscid transonic channel over a 10% circular-arc bump (M=0.675)."""
+    g = bump_points(nx, ny, nz)
+    fac = 1.0 + 0.5 * (GAMMA - 1.0) * mach ** 2
+    p_static = p0 / fac ** (GAMMA / (GAMMA - 1.0))
+    T_static = T0 / fac
+    inlet = M.Patch("inlet", M.PATCH_TOTAL_INLET, p0=p0, T0=T0)
+    outlet = M.Patch("outlet", M.PATCH_PRESSURE_OUTLET, p=p_static)
+    wall = M.Patch("walls", M.PATCH_SLIP, is_wall=True)
+    sides = {"xmin": inlet, "xmax": outlet, "ymin": wall, "ymax": wall, "zmin": wall, "zmax": wall}
+    mesh = M.hex_mesh(g, sides)
+    mesh = ordering.apply(mesh, ordering_mode)
+    N = mesh.n_cells
+    c = np.sqrt(GAMMA * R_GAS * T_static)
+    p = np.full(N, p_static)
+    T = np.full(N, T_static)
+    U = np.zeros((N, 3))
+    U[:, 0] = mach * c
+    rec = 3 if second_order else 0
+    settings = dict(thermo_settings(), flux_scheme={"AUSMPlusUp": 0, "HLLC": 1, "ROE": 2}[flux],
+                    recon_rho=rec, recon_U=rec, recon_T=rec,
+                    ddt_scheme=0, pseudo_co_num=1.0, pseudo_co_num_max=200.0,
+                    n_directions=8, max_iter=5, tolerance=1e-12, rel_tol=1e-2,
+                    pseudo_tol=1e-30, pseudo_tol_rel=1e-30)
+    return Workload("bump_%dx%dx%d" % (nx, ny, nz), mesh, p, U, T, settings)
+
+
+def random_box(n: int = 200, seed_vertices: int = 0, seed_perm: int = 1, mach: float = 2.0,
+               p: float = 1.0e4, T: float = 220.0, T_wall: float = 300.0, length: float = 1.0,
+               ordering_mode: str = "rcm") -> Workload:
+    """Randomised hex box: interior vertices displaced by U(+-0.2h), cells permuted then RCM."""
+    h = length / n
+    xs = np.linspace(0.0, length, n + 1)
+    g = np.stack(np.meshgrid(xs, xs, xs, indexing="ij"), axis=-1)
+    rng = np.random.default_rng(seed_vertices)
+    disp = rng.uniform(-0.2 * h, 0.2 * h, size=g.shape)
+    interior = np.zeros(g.shape[:3], bool)
+    interior[1:-1, 1:-1, 1:-1] = True
+    g = g + np.where(interior[..., None], disp, 0.0)
+    c = np.sqrt(GAMMA * R_GAS * T)
+    uinf = mach * c
+    inlet = M.Patch("inlet", M.PATCH_FIXED, p=p, T=T, U=(uinf, 0.0, 0.0))
+    outlet = M.Patch("outlet", M.PATCH_ZERO_GRADIENT)
+    wall = M.Patch("wall", M.PATCH_ISOTHERMAL_WALL, is_wall=True, T=T_wall)
+    top = M.Patch("top", M.PATCH_ZERO_GRADIENT)
+    sym = M.Patch("sides", M.PATCH_SLIP)
+    sides = {"xmin": inlet, "xmax": outlet, "ymin": wall, "ymax": top, "zmin": sym, "zmax": sym}
+    mesh = M.hex_mesh(g, sides)
+    perm = np.random.default_rng(seed_perm).permutation(mesh.n_cells)
+    mesh = M.renumber(mesh, perm)
+    mesh = ordering.apply(mesh, ordering_mode)
+    N = mesh.n_cells
+    Uc = np.zeros((N, 3))
+    Uc[:, 0] = uinf
+    settings = dict(thermo_settings(), flux_scheme=0, recon_rho=3, recon_U=3, recon_T=3,
+                    ddt_scheme=0, pseudo_co_num=1.0, pseudo_co_num_max=50.0,
+                    n_directions=8, max_iter=5, rel_tol=1e-2, tolerance=1e-12,
+                    pseudo_tol=1e-30, pseudo_tol_rel=1e-30)
+    return Workload("random_box_%d" % n, mesh, np.full(N, p), Uc, np.full(N, T), settings)
+
+
+def make_config(binding, settings: Dict, **overrides):
+    cfg = binding.default_config()
+    for k, v in dict(settings, **overrides).items():
+        setattr(cfg, k, v)
+    return cfg

@@ -1,0 +1,899 @@
+// C ABI of the GB300 hot path and its host-side driver.
+//
+// ics_create uploads addressing and geometry once and builds, on the host:
+//   - the cell->face CSR in face order (gathers accumulate in the order the
+//     reference's face loops do),
+//   - the sliced-ELL slot structure of the block Jacobian,
+//   - the LU-SGS level schedule of the current cell numbering.
+// Every later call works on device-resident state.  The host keeps only the
+// scalar bookkeeping of the pseudo-time control (residualsIO history, SER,
+// pseudotimeControl counters), mirroring setCoAndDeltaT.H and
+// pseudotimeControl.C.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "ics_internal.cuh"
+
+using namespace ics;
+
+struct ics_handle_s {
+  Handle h;
+};
+
+namespace ics {
+double rho_l2(Handle& h);
+}
+
+namespace {
+
+template <typename T>
+T* dalloc(size_t n) {
+  T* p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+  if (e != cudaSuccess) throw CudaError(e, "cudaMalloc", __FILE__, __LINE__);
+  ICS_CUDA(cudaMemset(p, 0, n * sizeof(T)));
+  return p;
+}
+
+template <typename T>
+T* upload(const std::vector<T>& v) {
+  T* p = dalloc<T>(v.size());
+  if (!v.empty()) ICS_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return p;
+}
+
+void dfree(void* p) {
+  if (p) cudaFree(p);
+}
+
+void free_all(Handle& h) {
+  DevMesh& m = h.m;
+  void* ptrs[] = {m.own, m.nei, m.Sf, m.magSf, m.w, m.nodc, m.dOwn, m.dNei, m.dCC, m.nf, m.bnf, m.C, m.V,
+                  m.bcell, m.bpatch, m.bSf, m.bmagSf, m.bdOwn, m.bdc, m.patches, m.cptr, m.cface, m.bptr,
+                  m.bface, m.slot_base, m.scol, m.sface, m.nlow, m.nslot, m.fl_cells, m.rl_cells, m.fl_lptr,
+                  m.rl_lptr, h.W, h.W0, h.W00, h.Wprev, h.prim, h.pB, h.TB, h.UB, h.phiB, h.pseudoCo, h.rPDT,
+                  h.ddtCoeff, h.q, h.bq, h.clin, h.grad, h.fflux, h.frec, h.flam, h.bjac, h.src, h.blk, h.dg,
+                  h.dginv, h.rD, h.kv, h.kw, h.kx, h.kb, h.kt, h.dW, h.partials, h.counter, h.ks, h.scratch,
+                  h.ibuf};
+  for (void* p : ptrs) dfree(p);
+  if (h.ksHost) cudaFreeHost(h.ksHost);
+  if (h.stream) cudaStreamDestroy(h.stream);
+}
+
+template <typename F>
+int guard(ics_handle hh, F&& f) {
+  if (!hh) return ICS_ERR_ARG;
+  Handle& h = hh->h;
+  try {
+    return f(h);
+  } catch (const CudaError& e) {
+    char buf[512];
+    std::snprintf(buf, sizeof(buf), "%s: %s (%s:%d)", e.what, cudaGetErrorString(e.e), e.file, e.line);
+    h.err = buf;
+    return e.e == cudaErrorMemoryAllocation ? ICS_ERR_NOMEM : ICS_ERR_CUDA;
+  } catch (const std::string& s) {
+    h.err = s;
+    return ICS_ERR_ARG;
+  } catch (const std::bad_alloc&) {
+    h.err = "host allocation failed";
+    return ICS_ERR_NOMEM;
+  }
+}
+
+int validate_config(const ics_config* c, std::string& err) {
+  if (c->flux_scheme < 0 || c->flux_scheme > 2) {
+    err = "Unknown convectiveFluxScheme";
+    return ICS_ERR_SCHEME;
+  }
+  if (c->solver != ICS_SOLVER_GMRES || c->preconditioner < 0 || c->preconditioner > 2) {
+    err = "Unknown solver or preconditioner";
+    return ICS_ERR_SCHEME;
+  }
+  const int rs[3] = {c->recon_rho, c->recon_U, c->recon_T};
+  for (int r : rs)
+    if (r < 0 || r > 4) {
+      err = "Unknown reconstruction scheme";
+      return ICS_ERR_SCHEME;
+    }
+  if (c->ddt_scheme < 0 || c->ddt_scheme > 2) {
+    err = "Unknown ddt scheme";
+    return ICS_ERR_SCHEME;
+  }
+  if (c->n_directions < 1 || c->n_directions > MAX_DIRS) {
+    err = "nDirections out of range";
+    return ICS_ERR_ARG;
+  }
+  if (c->precision != ICS_PREC_FP64 && c->precision != ICS_PREC_MIXED) {
+    err = "unknown precision";
+    return ICS_ERR_ARG;
+  }
+  if (!c->local_timestepping) {
+    err = "global pseudo time stepping is not supported";
+    return ICS_ERR_ARG;
+  }
+  if (!(c->R > 0) || !(c->Cp > c->R)) {
+    err = "invalid thermo constants";
+    return ICS_ERR_ARG;
+  }
+  return ICS_OK;
+}
+
+// Krylov and Jacobian storage sized for the current precision / nDirections
+void ensure_workspace(Handle& h) {
+  const int p = prec(h);
+  const int m = h.cfg.c.n_directions;
+  const size_t eb = p == ICS_PREC_MIXED ? 4 : 8;
+  const size_t n5 = 5ull * h.m.N;
+  if (h.kvPrec != p) {
+    void* ptrs[] = {h.blk, h.dg, h.dginv, h.rD, h.kw, h.kx, h.kb, h.kt, h.kv};
+    for (void* q : ptrs) dfree(q);
+    h.blk = dalloc<char>((size_t)h.m.nslots * 25 * 32 * eb);
+    h.dg = dalloc<char>((size_t)h.m.nslices * 25 * 32 * eb);
+    h.dginv = dalloc<char>((size_t)h.m.nslices * 25 * 32 * eb);
+    h.rD = dalloc<char>((size_t)h.m.N * eb);
+    h.kw = dalloc<char>(n5 * eb);
+    h.kx = dalloc<char>(n5 * eb);
+    h.kb = dalloc<char>(n5 * eb);
+    h.kt = dalloc<char>(n5 * eb);
+    h.kv = dalloc<char>(n5 * eb * m);
+    h.kvDirs = m;
+    h.kvPrec = p;
+    h.haveMatrix = false;
+  } else if (h.kvDirs < m) {
+    dfree(h.kv);
+    h.kv = dalloc<char>(n5 * eb * m);
+    h.kvDirs = m;
+  }
+}
+
+void build_mesh(Handle& h, const ics_mesh_desc* d) {
+  DevMesh& m = h.m;
+  const int N = d->n_cells, F = d->n_faces, B = d->n_bfaces;
+  m.N = N;
+  m.F = F;
+  m.B = B;
+  for (int k = 0; k < 3; ++k) m.solD[k] = d->solution_d[k];
+  for (int f = 0; f < F; ++f) {
+    const int o = d->owner[f], n = d->neighbour[f];
+    if (o < 0 || n >= N || o >= n) throw std::string("faces must satisfy 0 <= owner < neighbour < n_cells");
+    if (f > 0 && (o < d->owner[f - 1] || (o == d->owner[f - 1] && n <= d->neighbour[f - 1])))
+      throw std::string("internal faces must be in upper-triangular order");
+  }
+  for (int b = 0; b < B; ++b)
+    if (d->b_cell[b] < 0 || d->b_cell[b] >= N || d->b_patch[b] < 0 || d->b_patch[b] >= d->n_patches)
+      throw std::string("boundary face addressing out of range");
+  // geometry in SoA with the derived quantities the kernels use
+  std::vector<double> Sf(3 * F), magSf(F), nf(3 * F), dOwn(3 * F), dNei(3 * F), dCC(3 * F);
+  for (int f = 0; f < F; ++f) {
+    const double s[3] = {d->Sf[3 * f], d->Sf[3 * f + 1], d->Sf[3 * f + 2]};
+    const double ms = std::sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
+    magSf[f] = ms;
+    const int o = d->owner[f], n = d->neighbour[f];
+    for (int k = 0; k < 3; ++k) {
+      Sf[k * F + f] = s[k];
+      nf[k * F + f] = s[k] / ms;
+      dOwn[k * F + f] = d->Cf[3 * f + k] - d->C[3 * o + k];
+      dNei[k * F + f] = d->Cf[3 * f + k] - d->C[3 * n + k];
+      dCC[k * F + f] = d->C[3 * n + k] - d->C[3 * o + k];
+    }
+  }
+  std::vector<double> bSf(3 * B), bmag(B), bnf(3 * B), bdOwn(3 * B);
+  for (int b = 0; b < B; ++b) {
+    const double s[3] = {d->b_Sf[3 * b], d->b_Sf[3 * b + 1], d->b_Sf[3 * b + 2]};
+    const double ms = std::sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
+    bmag[b] = ms;
+    for (int k = 0; k < 3; ++k) {
+      bSf[k * B + b] = s[k];
+      bnf[k * B + b] = s[k] / ms;
+      bdOwn[k * B + b] = d->b_Cf[3 * b + k] - d->C[3 * d->b_cell[b] + k];
+    }
+  }
+  std::vector<double> C(3 * N);
+  for (int i = 0; i < N; ++i)
+    for (int k = 0; k < 3; ++k) C[k * N + i] = d->C[3 * i + k];
+  m.own = upload(std::vector<int>(d->owner, d->owner + F));
+  m.nei = upload(std::vector<int>(d->neighbour, d->neighbour + F));
+  m.Sf = upload(Sf);
+  m.magSf = upload(magSf);
+  m.nf = upload(nf);
+  m.w = upload(std::vector<double>(d->weights, d->weights + F));
+  m.nodc = upload(std::vector<double>(d->nonorth_delta_coeffs, d->nonorth_delta_coeffs + F));
+  m.dOwn = upload(dOwn);
+  m.dNei = upload(dNei);
+  m.dCC = upload(dCC);
+  m.C = upload(C);
+  m.V = upload(std::vector<double>(d->V, d->V + N));
+  m.bcell = upload(std::vector<int>(d->b_cell, d->b_cell + B));
+  m.bpatch = upload(std::vector<int>(d->b_patch, d->b_patch + B));
+  m.bSf = upload(bSf);
+  m.bmagSf = upload(bmag);
+  m.bnf = upload(bnf);
+  m.bdOwn = upload(bdOwn);
+  m.bdc = upload(std::vector<double>(d->b_delta_coeffs, d->b_delta_coeffs + B));
+  std::vector<Patch> pts(std::max(1, d->n_patches));
+  for (int p = 0; p < d->n_patches; ++p) {
+    const ics_patch_desc& q = d->patches[p];
+    pts[p].kind = q.kind;
+    pts[p].is_wall = q.is_wall;
+    pts[p].p = q.p;
+    pts[p].T = q.T;
+    for (int k = 0; k < 3; ++k) pts[p].U[k] = q.U[k];
+    pts[p].p0 = q.p0;
+    pts[p].T0 = q.T0;
+    if (q.kind < 0 || q.kind > ICS_PATCH_ISOTHERMAL_WALL) throw std::string("unknown patch kind");
+  }
+  m.patches = upload(pts);
+  m.npatches = d->n_patches;
+  // cell -> faces CSR in face order
+  std::vector<int> cnt(N + 1, 0);
+  for (int f = 0; f < F; ++f) {
+    cnt[d->owner[f] + 1]++;
+    cnt[d->neighbour[f] + 1]++;
+  }
+  for (int i = 0; i < N; ++i) cnt[i + 1] += cnt[i];
+  std::vector<int> cface(cnt[N]);
+  {
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    for (int f = 0; f < F; ++f) {
+      cface[fill[d->owner[f]]++] = f;
+      cface[fill[d->neighbour[f]]++] = ~f;
+    }
+  }
+  m.cptr = upload(cnt);
+  m.cface = upload(cface);
+  std::vector<int> bcnt(N + 1, 0);
+  for (int b = 0; b < B; ++b) bcnt[d->b_cell[b] + 1]++;
+  for (int i = 0; i < N; ++i) bcnt[i + 1] += bcnt[i];
+  std::vector<int> bface(B);
+  {
+    std::vector<int> fill(bcnt.begin(), bcnt.end() - 1);
+    for (int b = 0; b < B; ++b) bface[fill[d->b_cell[b]]++] = b;
+  }
+  m.bptr = upload(bcnt);
+  m.bface = upload(bface);
+  // sliced-ELL: row c slots = its faces in face order (lower part first)
+  const int ns = (N + SLICE - 1) / SLICE;
+  m.nslices = ns;
+  std::vector<int> slot_base(ns + 1, 0), nslot(N), nlow(N);
+  for (int c = 0; c < N; ++c) {
+    nslot[c] = cnt[c + 1] - cnt[c];
+    int nl = 0;
+    for (int e = cnt[c]; e < cnt[c + 1]; ++e) nl += cface[e] < 0;
+    nlow[c] = nl;
+  }
+  for (int s = 0; s < ns; ++s) {
+    int wmax = 0;
+    for (int c = s * SLICE; c < std::min(N, (s + 1) * SLICE); ++c) wmax = std::max(wmax, nslot[c]);
+    slot_base[s + 1] = slot_base[s] + wmax;
+  }
+  m.nslots = slot_base[ns];
+  std::vector<int> scol((size_t)m.nslots * SLICE, -1), sface((size_t)m.nslots * SLICE, 0x7fffffff);
+  for (int c = 0; c < N; ++c) {
+    const int s = c / SLICE, lane = c % SLICE;
+    // face order within a cell: neighbour-side faces (lower, col = owner
+    // ascending) come before owner-side faces (upper, col = neighbour ascending)
+    int t = 0;
+    for (int e = cnt[c]; e < cnt[c + 1]; ++e) {
+      const int code = cface[e];
+      const int f = code >= 0 ? code : ~code;
+      const int col = code >= 0 ? d->neighbour[f] : d->owner[f];
+      const size_t idx = (size_t)(slot_base[s] + t) * SLICE + lane;
+      scol[idx] = col;
+      sface[idx] = code;
+      ++t;
+    }
+  }
+  // verify the slot column order (lower part ascending, then upper ascending)
+  for (int c = 0; c < N; ++c) {
+    const int s = c / SLICE, lane = c % SLICE;
+    int prev = -1;
+    for (int t = 0; t < nslot[c]; ++t) {
+      const int col = scol[(size_t)(slot_base[s] + t) * SLICE + lane];
+      if (col <= prev || (t < nlow[c]) != (col < c)) throw std::string("slot ordering invariant violated");
+      prev = col;
+    }
+  }
+  m.slot_base = upload(slot_base);
+  m.scol = upload(scol);
+  m.sface = upload(sface);
+  m.nslot = upload(nslot);
+  m.nlow = upload(nlow);
+  // LU-SGS levels
+  std::vector<int> lev(N, 0), rlev(N, 0);
+  for (int c = 0; c < N; ++c)
+    for (int e = cnt[c]; e < cnt[c + 1]; ++e)
+      if (cface[e] < 0) lev[c] = std::max(lev[c], lev[d->owner[~cface[e]]] + 1);
+  for (int c = N - 1; c >= 0; --c)
+    for (int e = cnt[c]; e < cnt[c + 1]; ++e)
+      if (cface[e] >= 0) rlev[c] = std::max(rlev[c], rlev[d->neighbour[cface[e]]] + 1);
+  auto group = [&](const std::vector<int>& L, int& nl, std::vector<int>& ptr, std::vector<int>& cells,
+                   std::vector<int>& cstart) {
+    nl = 0;
+    for (int v : L) nl = std::max(nl, v + 1);
+    ptr.assign(nl + 1, 0);
+    for (int v : L) ptr[v + 1]++;
+    for (int l = 0; l < nl; ++l) ptr[l + 1] += ptr[l];
+    cells.assign(N, 0);
+    std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+    for (int c = 0; c < N; ++c) cells[fill[L[c]]++] = c;
+    cstart.assign(nl, -1);
+    for (int l = 0; l < nl; ++l) {
+      bool contig = true;
+      for (int i = ptr[l] + 1; i < ptr[l + 1]; ++i)
+        if (cells[i] != cells[i - 1] + 1) contig = false;
+      if (contig && ptr[l + 1] > ptr[l]) cstart[l] = cells[ptr[l]];
+    }
+  };
+  std::vector<int> fcells, rcells;
+  group(lev, m.nfl, m.fl_ptr, fcells, m.fl_cstart);
+  group(rlev, m.nrl, m.rl_ptr, rcells, m.rl_cstart);
+  m.fl_cells = upload(fcells);
+  m.rl_cells = upload(rcells);
+  m.fl_lptr = upload(m.fl_ptr);
+  m.rl_lptr = upload(m.rl_ptr);
+}
+
+void alloc_state(Handle& h) {
+  const int N = h.m.N, F = h.m.F, B = h.m.B;
+  h.W = dalloc<double>(5ull * N);
+  h.W0 = dalloc<double>(5ull * N);
+  h.W00 = dalloc<double>(5ull * N);
+  h.Wprev = dalloc<double>(5ull * N);
+  h.prim = dalloc<double>(5ull * N);
+  h.pB = dalloc<double>(B);
+  h.TB = dalloc<double>(B);
+  h.UB = dalloc<double>(3ull * B);
+  h.phiB = dalloc<double>(B);
+  h.pseudoCo = dalloc<double>(N);
+  h.rPDT = dalloc<double>(N);
+  h.ddtCoeff = dalloc<double>(N);
+  h.q = dalloc<double>((size_t)NQ * N);
+  h.bq = dalloc<double>((size_t)NQ * B);
+  h.clin = dalloc<double>((size_t)N + B);
+  h.grad = dalloc<double>((size_t)NQ * 3 * N);
+  h.fflux = dalloc<double>(5ull * (F + B));
+  h.frec = dalloc<double>(8ull * F);
+  h.flam = dalloc<double>((size_t)F + B);
+  h.bjac = dalloc<double>(25ull * B);
+  h.src = dalloc<double>(5ull * N);
+  h.dW = dalloc<double>(5ull * N);
+  h.partials = dalloc<double>((size_t)REDUCE_BLOCKS * 16);
+  h.counter = dalloc<unsigned int>(4);
+  h.ks = dalloc<KrylovScalars>(1);
+  ICS_CUDA(cudaMallocHost(&h.ksHost, sizeof(KrylovScalars)));
+  h.scratch = dalloc<double>(5ull * N + 8);
+  h.ibuf = dalloc<int>((size_t)N + 8);
+}
+
+double residual_norm(const ics_solver_perf& r) {
+  return std::sqrt(r.init_res[0] * r.init_res[0] + r.init_res[4] * r.init_res[4] +
+                   (r.init_res[1] * r.init_res[1] + r.init_res[2] * r.init_res[2] + r.init_res[3] * r.init_res[3]));
+}
+
+int do_residual(Handle& h, double* host_src) {
+  // SER (setCoAndDeltaT.H:3-37) from the last two linear-solver initial residuals
+  double ratio = 1.0;
+  bool apply = false;
+  if (h.initResValid) {
+    const bool firstIter = h.corr == 1;
+    if (!firstIter && h.prevResValid) {
+      ratio = residual_norm(h.prevRes) / residual_norm(h.initRes);
+      ratio = std::max(std::min(ratio, h.cfg.c.pseudo_co_max_increase), h.cfg.c.pseudo_co_min_decrease);
+      apply = true;
+    }
+    h.prevRes = h.initRes;
+    h.prevResValid = true;
+  }
+  launch_fields(h);
+  launch_grad(h);
+  launch_face_flux(h);
+  launch_residual(h, ratio, apply);
+  h.haveFlux = true;
+  h.lastRhoL2 = rho_l2(h);
+  if (host_src) {
+    ICS_CUDA(cudaMemcpyAsync(host_src, h.src, 5ull * h.m.N * sizeof(double), cudaMemcpyDeviceToHost, h.stream));
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    for (size_t i = 0; i < 5ull * h.m.N; ++i)
+      if (!std::isfinite(host_src[i])) {
+        h.err = "non-finite residual";
+        return ICS_ERR_NONFINITE;
+      }
+  }
+  if (!std::isfinite(h.lastRhoL2)) {
+    h.err = "non-finite residual";
+    return ICS_ERR_NONFINITE;
+  }
+  return ICS_OK;
+}
+
+int do_jacobian(Handle& h) {
+  if (!h.haveFlux) {
+    h.err = "assemble_jacobian needs a residual evaluation first";
+    return ICS_ERR_STATE;
+  }
+  ensure_workspace(h);
+  ICS_CUDA(cudaMemsetAsync(&h.ks->status, 0, sizeof(int), h.stream));
+  launch_jacobian(h);
+  int st = 0;
+  ICS_CUDA(cudaMemcpyAsync(&st, &h.ks->status, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+  ICS_CUDA(cudaStreamSynchronize(h.stream));
+  h.haveMatrix = true;
+  if (st) {
+    h.err = "All diagonals of coupledMatrix are zero";
+    return ICS_ERR_DIAG;
+  }
+  return ICS_OK;
+}
+
+int do_solve(Handle& h, ics_solver_perf* perf) {
+  if (!h.haveMatrix) {
+    h.err = "solve_increment needs an assembled Jacobian";
+    return ICS_ERR_STATE;
+  }
+  ensure_workspace(h);
+  ICS_CUDA(cudaMemcpyAsync(h.Wprev, h.W, 5ull * h.m.N * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
+  ics_solver_perf p;
+  const int st = gmres_solve(h, &p);
+  h.haveIncrement = true;
+  h.initRes = p;
+  h.initResValid = true;
+  h.residuals_ = p;
+  if (perf) *perf = p;
+  if (st) h.err = st == ICS_ERR_BREAKDOWN ? "zero Krylov norm" : "non-finite Krylov residual";
+  return st;
+}
+
+int do_update(Handle& h, ics_iter_stats* s) {
+  if (!h.haveIncrement) {
+    h.err = "update_fields needs a solved increment";
+    return ICS_ERR_STATE;
+  }
+  launch_bound_local_timestep(h);
+  int* bounded = h.ibuf + h.m.N;
+  ICS_CUDA(cudaMemsetAsync(bounded, 0, sizeof(int), h.stream));
+  launch_update(h, bounded);
+  launch_bc(h);
+  int nb = 0;
+  ICS_CUDA(cudaMemcpyAsync(&nb, bounded, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+  ICS_CUDA(cudaStreamSynchronize(h.stream));
+  h.haveIncrement = false;
+  if (s) {
+    s->bounded_cells = nb;
+    s->rho_l2_residual = h.lastRhoL2;
+  }
+  return ICS_OK;
+}
+
+double max_init(const ics_solver_perf& r) {
+  double m = -VGREAT;
+  for (int k = 0; k < 5; ++k) m = std::max(m, r.init_res[k]);
+  return m;
+}
+
+bool criteria_satisfied(Handle& h) {
+  const ics_config& c = h.cfg.c;
+  const bool finalIter = h.converged_ || (h.corr == c.n_pseudo_corr);
+  if (h.firstIteration_ || h.corr == 1 || finalIter) {
+    h.firstIteration_ = false;
+    return false;
+  }
+  const bool storeIni = h.corr == 2;
+  if (storeIni) h.initResiduals_ = h.residuals_;
+  const bool absCheck = max_init(h.residuals_) < c.pseudo_tol;
+  bool relCheck = false;
+  if (!storeIni) {
+    ics_solver_perf q = h.residuals_;
+    for (int k = 0; k < 5; ++k) q.init_res[k] /= h.initResiduals_.init_res[k] + ROOTVSMALL;
+    relCheck = max_init(q) < c.pseudo_tol_rel;
+  }
+  return (h.corr >= c.n_pseudo_corr_min) && (absCheck || relCheck);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+extern "C" {
+
+void ics_default_config(ics_config* c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->R = 287.0;
+  c->Cp = 1004.5;
+  c->mu = 0;
+  c->Pr = 0.72;
+  c->As = 1.458e-6;
+  c->Ts = 110.4;
+  c->flux_scheme = ICS_FLUX_AUSMPLUSUP;
+  c->low_mach_ausm = 1;
+  c->entropy_fix_coeff = 0.05;
+  c->recon_rho = c->recon_U = c->recon_T = ICS_RECON_UPWIND;
+  c->ddt_scheme = ICS_DDT_STEADY;
+  c->delta_t = 1;
+  c->solver = ICS_SOLVER_GMRES;
+  c->preconditioner = ICS_PC_LUSGS;
+  c->n_directions = 8;
+  c->max_iter = 1000;
+  c->min_iter = 0;
+  c->tolerance = 1e-12;
+  c->rel_tol = 1e-2;
+  c->precision = ICS_PREC_FP64;
+  c->n_pseudo_corr = 20;
+  c->n_pseudo_corr_min = 1;
+  c->pseudo_tol = 1e-5;
+  c->pseudo_tol_rel = 1e-5;
+  c->pseudo_co_num = 1;
+  c->pseudo_co_num_min = 0.1;
+  c->pseudo_co_num_max = 25;
+  c->pseudo_co_max_increase = 1.25;
+  c->pseudo_co_min_decrease = 0.1;
+  c->local_timestepping = 1;
+  c->local_timestepping_bounding = 1;
+  c->local_timestepping_lower_bound = 0.95;
+  c->reset_pseudo = 0;
+  c->rho_min = -GREAT;
+  c->T_min = SMALL;
+  c->T_max = GREAT;
+}
+
+int ics_create(const ics_mesh_desc* mesh, const ics_config* cfg, ics_handle* out) {
+  if (!mesh || !cfg || !out || mesh->n_cells <= 0 || mesh->n_faces < 0 || mesh->n_bfaces < 0 ||
+      mesh->n_patches < 0 || (mesh->n_faces && (!mesh->owner || !mesh->neighbour || !mesh->Sf || !mesh->Cf)) ||
+      !mesh->C || !mesh->V)
+    return ICS_ERR_ARG;
+  *out = nullptr;
+  ics_handle hh = new (std::nothrow) ics_handle_s();
+  if (!hh) return ICS_ERR_NOMEM;
+  std::string err;
+  int st = validate_config(cfg, err);
+  if (st) {
+    delete hh;
+    return st;
+  }
+  Handle& h = hh->h;
+  h.cfg.c = *cfg;
+  h.cfg.Cv = cfg->Cp - cfg->R;
+  h.cfg.gamma = cfg->Cp / h.cfg.Cv;
+  st = guard(hh, [&](Handle& hd) {
+    ICS_CUDA(cudaStreamCreateWithFlags(&hd.stream, cudaStreamNonBlocking));
+    build_mesh(hd, mesh);
+    alloc_state(hd);
+    ensure_workspace(hd);
+    std::vector<double> co(hd.m.N, cfg->pseudo_co_num);
+    ICS_CUDA(cudaMemcpy(hd.pseudoCo, co.data(), co.size() * sizeof(double), cudaMemcpyHostToDevice));
+    return ICS_OK;
+  });
+  if (st) {
+    free_all(h);
+    delete hh;
+    return st;
+  }
+  *out = hh;
+  return ICS_OK;
+}
+
+int ics_destroy(ics_handle hh) {
+  if (!hh) return ICS_ERR_ARG;
+  free_all(hh->h);
+  delete hh;
+  return ICS_OK;
+}
+
+int ics_set_config(ics_handle hh, const ics_config* cfg) {
+  if (!hh || !cfg) return ICS_ERR_ARG;
+  std::string err;
+  const int st = validate_config(cfg, err);
+  if (st) {
+    hh->h.err = err;
+    return st;
+  }
+  return guard(hh, [&](Handle& h) {
+    const bool structural = cfg->precision != h.cfg.c.precision || cfg->n_directions != h.cfg.c.n_directions;
+    h.cfg.c = *cfg;
+    h.cfg.Cv = cfg->Cp - cfg->R;
+    h.cfg.gamma = cfg->Cp / h.cfg.Cv;
+    if (structural) ensure_workspace(h);
+    return ICS_OK;
+  });
+}
+
+int ics_last_error(ics_handle hh, char* buf, int32_t len) {
+  if (!hh || !buf || len <= 0) return ICS_ERR_ARG;
+  std::snprintf(buf, len, "%s", hh->h.err.c_str());
+  return ICS_OK;
+}
+
+int ics_set_primitive(ics_handle hh, const double* p, const double* U, const double* T) {
+  if (!p || !U || !T) return ICS_ERR_ARG;
+  return guard(hh, [&](Handle& h) {
+    const size_t N = h.m.N;
+    ICS_CUDA(cudaMemcpyAsync(h.scratch, p, N * sizeof(double), cudaMemcpyHostToDevice, h.stream));
+    ICS_CUDA(cudaMemcpyAsync(h.scratch + N, U, 3 * N * sizeof(double), cudaMemcpyHostToDevice, h.stream));
+    ICS_CUDA(cudaMemcpyAsync(h.scratch + 4 * N, T, N * sizeof(double), cudaMemcpyHostToDevice, h.stream));
+    launch_set_primitive(h);
+    ICS_CUDA(cudaMemcpyAsync(h.W0, h.W, 5 * N * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
+    ICS_CUDA(cudaMemcpyAsync(h.W00, h.W, 5 * N * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    h.timeIndex = 0;
+    h.haveFlux = h.haveMatrix = h.haveIncrement = false;
+    return ICS_OK;
+  });
+}
+
+int ics_set_boundary_state(ics_handle hh, const double* pb, const double* Ub, const double* Tb, const double* phib) {
+  return guard(hh, [&](Handle& h) {
+    const size_t B = h.m.B;
+    if (pb) ICS_CUDA(cudaMemcpy(h.pB, pb, B * sizeof(double), cudaMemcpyHostToDevice));
+    if (Tb) ICS_CUDA(cudaMemcpy(h.TB, Tb, B * sizeof(double), cudaMemcpyHostToDevice));
+    if (phib) ICS_CUDA(cudaMemcpy(h.phiB, phib, B * sizeof(double), cudaMemcpyHostToDevice));
+    if (Ub) {
+      std::vector<double> t(3 * B);
+      for (size_t b = 0; b < B; ++b)
+        for (int k = 0; k < 3; ++k) t[k * B + b] = Ub[3 * b + k];
+      ICS_CUDA(cudaMemcpy(h.UB, t.data(), 3 * B * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    return ICS_OK;
+  });
+}
+
+int ics_get_boundary_state(ics_handle hh, double* pb, double* Ub, double* Tb, double* phib) {
+  return guard(hh, [&](Handle& h) {
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    const size_t B = h.m.B;
+    if (pb) ICS_CUDA(cudaMemcpy(pb, h.pB, B * sizeof(double), cudaMemcpyDeviceToHost));
+    if (Tb) ICS_CUDA(cudaMemcpy(Tb, h.TB, B * sizeof(double), cudaMemcpyDeviceToHost));
+    if (phib) ICS_CUDA(cudaMemcpy(phib, h.phiB, B * sizeof(double), cudaMemcpyDeviceToHost));
+    if (Ub) {
+      std::vector<double> t(3 * B);
+      ICS_CUDA(cudaMemcpy(t.data(), h.UB, 3 * B * sizeof(double), cudaMemcpyDeviceToHost));
+      for (size_t b = 0; b < B; ++b)
+        for (int k = 0; k < 3; ++k) Ub[3 * b + k] = t[k * B + b];
+    }
+    return ICS_OK;
+  });
+}
+
+int ics_get_state(ics_handle hh, double* W, double* p, double* U, double* T) {
+  return guard(hh, [&](Handle& h) {
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    const size_t N = h.m.N;
+    if (W) ICS_CUDA(cudaMemcpy(W, h.W, 5 * N * sizeof(double), cudaMemcpyDeviceToHost));
+    if (p || U || T) {
+      std::vector<double> pr(5 * N);
+      ICS_CUDA(cudaMemcpy(pr.data(), h.prim, 5 * N * sizeof(double), cudaMemcpyDeviceToHost));
+      for (size_t i = 0; i < N; ++i) {
+        if (p) p[i] = pr[i];
+        if (T) T[i] = pr[N + i];
+        if (U)
+          for (int k = 0; k < 3; ++k) U[3 * i + k] = pr[(2 + k) * N + i];
+      }
+    }
+    return ICS_OK;
+  });
+}
+
+int ics_set_conservative(ics_handle hh, const double* W, int32_t set_old) {
+  if (!W) return ICS_ERR_ARG;
+  return guard(hh, [&](Handle& h) {
+    const size_t N = h.m.N;
+    ICS_CUDA(cudaMemcpyAsync(h.W, W, 5 * N * sizeof(double), cudaMemcpyHostToDevice, h.stream));
+    launch_derive_primitive(h);
+    if (set_old) {
+      ICS_CUDA(cudaMemcpyAsync(h.W0, h.W, 5 * N * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
+      ICS_CUDA(cudaMemcpyAsync(h.W00, h.W, 5 * N * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
+    }
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    return ICS_OK;
+  });
+}
+
+int ics_set_pseudo_co(ics_handle hh, const double* co) {
+  if (!co) return ICS_ERR_ARG;
+  return guard(hh, [&](Handle& h) {
+    ICS_CUDA(cudaMemcpy(h.pseudoCo, co, h.m.N * sizeof(double), cudaMemcpyHostToDevice));
+    return ICS_OK;
+  });
+}
+
+int ics_get_pseudo_co(ics_handle hh, double* co, double* rdt) {
+  return guard(hh, [&](Handle& h) {
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    if (co) ICS_CUDA(cudaMemcpy(co, h.pseudoCo, h.m.N * sizeof(double), cudaMemcpyDeviceToHost));
+    if (rdt) ICS_CUDA(cudaMemcpy(rdt, h.rPDT, h.m.N * sizeof(double), cudaMemcpyDeviceToHost));
+    return ICS_OK;
+  });
+}
+
+int ics_calc_flux(ics_handle hh, double* phi, double* phiU, double* phiE) {
+  return guard(hh, [&](Handle& h) {
+    launch_fields(h);
+    launch_grad(h);
+    launch_face_flux(h);
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    const size_t FB = (size_t)h.m.F + h.m.B;
+    std::vector<double> t(5 * FB);
+    ICS_CUDA(cudaMemcpy(t.data(), h.fflux, 5 * FB * sizeof(double), cudaMemcpyDeviceToHost));
+    for (size_t f = 0; f < FB; ++f) {
+      if (phi) phi[f] = t[f];
+      if (phiU)
+        for (int k = 0; k < 3; ++k) phiU[3 * f + k] = t[(1 + k) * FB + f];
+      if (phiE) phiE[f] = t[4 * FB + f];
+    }
+    return ICS_OK;
+  });
+}
+
+int ics_residual(ics_handle hh, double* source) {
+  return guard(hh, [&](Handle& h) { return do_residual(h, source); });
+}
+
+int ics_assemble_jacobian(ics_handle hh) {
+  return guard(hh, [&](Handle& h) { return do_jacobian(h); });
+}
+
+int ics_get_jacobian(ics_handle hh, double* diag, double* lower, double* upper) {
+  return guard(hh, [&](Handle& h) {
+    if (!h.haveMatrix) {
+      h.err = "no assembled Jacobian";
+      return ICS_ERR_STATE;
+    }
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    const DevMesh& m = h.m;
+    const bool mixed = h.jacPrecision == ICS_PREC_MIXED;
+    const size_t eb = mixed ? 4 : 8;
+    std::vector<char> blk((size_t)m.nslots * 25 * 32 * eb), dg((size_t)m.nslices * 25 * 32 * eb);
+    ICS_CUDA(cudaMemcpy(blk.data(), h.blk, blk.size(), cudaMemcpyDeviceToHost));
+    ICS_CUDA(cudaMemcpy(dg.data(), h.dg, dg.size(), cudaMemcpyDeviceToHost));
+    std::vector<int> sb(m.nslices + 1), sface((size_t)m.nslots * 32), nsl(m.N);
+    ICS_CUDA(cudaMemcpy(sb.data(), m.slot_base, sb.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    ICS_CUDA(cudaMemcpy(sface.data(), m.sface, sface.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    ICS_CUDA(cudaMemcpy(nsl.data(), m.nslot, nsl.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    auto get = [&](const std::vector<char>& a, size_t idx) {
+      return mixed ? (double)((const float*)a.data())[idx] : ((const double*)a.data())[idx];
+    };
+    for (int c = 0; c < m.N; ++c) {
+      const int s = c / 32, lane = c % 32;
+      if (diag)
+        for (int k = 0; k < 25; ++k) diag[25 * c + k] = get(dg, ((size_t)s * 25 + k) * 32 + lane);
+      for (int t = 0; t < nsl[c]; ++t) {
+        const int code = sface[(size_t)(sb[s] + t) * 32 + lane];
+        const int f = code >= 0 ? code : ~code;
+        double* dst = code >= 0 ? upper : lower;  // owner row holds upper_f
+        if (!dst) continue;
+        for (int k = 0; k < 25; ++k) dst[25 * f + k] = get(blk, ((size_t)(sb[s] + t) * 25 + k) * 32 + lane);
+      }
+    }
+    return ICS_OK;
+  });
+}
+
+int ics_matrix_mul(ics_handle hh, const double* x, double* y) {
+  if (!x || !y) return ICS_ERR_ARG;
+  return guard(hh, [&](Handle& h) {
+    if (!h.haveMatrix) {
+      h.err = "no assembled Jacobian";
+      return ICS_ERR_STATE;
+    }
+    const size_t n5 = 5ull * h.m.N;
+    ICS_CUDA(cudaMemcpyAsync(h.scratch, x, n5 * sizeof(double), cudaMemcpyHostToDevice, h.stream));
+    to_vec(h, h.scratch, h.kw);
+    spmv(h, h.kw, h.kt);
+    from_vec(h, h.kt, h.scratch);
+    ICS_CUDA(cudaMemcpyAsync(y, h.scratch, n5 * sizeof(double), cudaMemcpyDeviceToHost, h.stream));
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    return ICS_OK;
+  });
+}
+
+int ics_precondition(ics_handle hh, double* r) {
+  if (!r) return ICS_ERR_ARG;
+  return guard(hh, [&](Handle& h) {
+    if (!h.haveMatrix) {
+      h.err = "no assembled Jacobian";
+      return ICS_ERR_STATE;
+    }
+    const size_t n5 = 5ull * h.m.N;
+    ICS_CUDA(cudaMemcpyAsync(h.scratch, r, n5 * sizeof(double), cudaMemcpyHostToDevice, h.stream));
+    to_vec(h, h.scratch, h.kw);
+    precondition(h, h.kw);
+    from_vec(h, h.kw, h.scratch);
+    ICS_CUDA(cudaMemcpyAsync(r, h.scratch, n5 * sizeof(double), cudaMemcpyDeviceToHost, h.stream));
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    return ICS_OK;
+  });
+}
+
+int ics_solve_increment(ics_handle hh, ics_solver_perf* perf, double* dW) {
+  return guard(hh, [&](Handle& h) {
+    const int st = do_solve(h, perf);
+    if (dW) {
+      ICS_CUDA(cudaMemcpyAsync(dW, h.dW, 5ull * h.m.N * sizeof(double), cudaMemcpyDeviceToHost, h.stream));
+      ICS_CUDA(cudaStreamSynchronize(h.stream));
+    }
+    return st;
+  });
+}
+
+int ics_update_fields(ics_handle hh, ics_iter_stats* stats) {
+  return guard(hh, [&](Handle& h) { return do_update(h, stats); });
+}
+
+int ics_pseudo_iteration(ics_handle hh, ics_iter_stats* stats) {
+  return guard(hh, [&](Handle& h) {
+    ics_iter_stats s;
+    std::memset(&s, 0, sizeof(s));
+    int r = do_residual(h, nullptr);
+    if (r) return r;
+    r = do_jacobian(h);
+    if (r) return r;
+    const int sv = do_solve(h, &s.perf);
+    if (sv && sv != ICS_ERR_BREAKDOWN) return sv;
+    const int u = do_update(h, &s);
+    std::vector<double> co(h.m.N);
+    ICS_CUDA(cudaMemcpy(co.data(), h.pseudoCo, h.m.N * sizeof(double), cudaMemcpyDeviceToHost));
+    double m = 0;
+    for (double v : co) m += v;
+    s.pseudo_co_mean = m / h.m.N;
+    s.rho_l2_residual = h.lastRhoL2;
+    s.status = sv ? sv : u;
+    if (stats) *stats = s;
+    return u;
+  });
+}
+
+int ics_begin_time_step(ics_handle hh) {
+  return guard(hh, [&](Handle& h) {
+    const size_t n5 = 5ull * h.m.N;
+    const bool steady = h.cfg.c.ddt_scheme == ICS_DDT_STEADY;
+    if (h.timeIndex == 0) {
+      ICS_CUDA(cudaMemcpyAsync(h.W0, h.W, n5 * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
+      ICS_CUDA(cudaMemcpyAsync(h.W00, h.W, n5 * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
+    } else {
+      ICS_CUDA(cudaMemcpyAsync(h.W00, h.W0, n5 * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
+      ICS_CUDA(cudaMemcpyAsync(h.W0, h.W, n5 * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
+    }
+    h.timeIndex++;
+    if (!steady) {
+      h.initResValid = false;
+      h.prevResValid = false;
+    }
+    if (h.cfg.c.reset_pseudo) {
+      std::vector<double> co(h.m.N, h.cfg.c.pseudo_co_num);
+      ICS_CUDA(cudaMemcpyAsync(h.pseudoCo, co.data(), co.size() * sizeof(double), cudaMemcpyHostToDevice, h.stream));
+    }
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    return ICS_OK;
+  });
+}
+
+int ics_pseudo_loop(ics_handle hh, int32_t* more) {
+  if (!more) return ICS_ERR_ARG;
+  return guard(hh, [&](Handle& h) {
+    const bool steady = h.cfg.c.ddt_scheme == ICS_DDT_STEADY;
+    h.corr++;
+    if (!steady && h.corr == h.cfg.c.n_pseudo_corr + 1) {
+      h.corr = 0;
+      *more = 0;
+      return ICS_OK;
+    }
+    bool completed = false;
+    if (h.converged_ || criteria_satisfied(h)) {
+      if (h.converged_) {
+        h.corr = 0;
+        h.converged_ = false;
+        completed = true;
+      } else {
+        h.converged_ = true;
+      }
+    }
+    *more = completed ? 0 : 1;
+    return ICS_OK;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,213 @@
+// Internal declarations of the GB300 hot path.
+//
+// Device data layout (all resident for the life of a handle):
+//   * cell 5-vectors  [N][5]  AoS (rho, rhoUx, rhoUy, rhoUz, rhoE): one
+//     gather of a neighbour's state is one 40-byte (FP64) or 20-byte (FP32)
+//     contiguous read.
+//   * reconstructed scalars and their gradients: SoA [k][N] and [k][3][N],
+//     coalesced for the cell- and face-parallel kernels.
+//   * face arrays: SoA [F] per component, face-parallel kernels read them
+//     with unit stride.
+//   * Jacobian: sliced-ELL with slice height 32 (one warp) of 5x5 blocks.
+//     Row = cell, one slot per internal face of that cell, slots sorted by
+//     column (lower part first).  Block entry k of slot t of slice s for lane
+//     l lives at ((slot_base[s] + t) * 25 + k) * 32 + l, so a warp reading
+//     one entry of its 32 rows touches one contiguous 256 B (FP64) line.
+//     The diagonal block of cell c lives at ((c/32) * 25 + k) * 32 + c%32.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "icsfoam_gb300.h"
+
+namespace ics {
+
+constexpr double SMALL = 1e-15;
+constexpr double VSMALL = 1e-300;
+constexpr double ROOTVSMALL = 1e-150;
+constexpr double GREAT = 1e15;
+constexpr double VGREAT = 1e300;
+
+// reconstructed scalar fields (slots of q[][N])
+enum { Q_RHO = 0, Q_P = 1, Q_UX = 2, Q_UY = 3, Q_UZ = 4, Q_E = 5, Q_H = 6, Q_C = 7, NQ = 8 };
+
+constexpr int SLICE = 32;
+constexpr int REDUCE_BLOCKS = 608;  // 4 x 152 SMs
+constexpr int MAX_DIRS = 64;
+
+// Scalars living in device memory for the Krylov cycle (one per handle).
+struct KrylovScalars {
+  double H[MAX_DIRS * MAX_DIRS];
+  double c[MAX_DIRS], s[MAX_DIRS], bh[MAX_DIRS + 1], y[MAX_DIRS];
+  double beta;            // norm used to scale the next Krylov vector
+  double red[16];         // reduction results
+  double avg[5];
+  double nf[3];           // norm factors (rho, rhoE, rhoU)
+  double res[5];          // L1 residuals (unnormalised sums)
+  double l2;              // rho L2 partial result
+  int status;             // breakdown / non-finite flags
+};
+
+struct Patch {
+  int kind, is_wall;
+  double p, T, U[3], p0, T0;
+};
+
+struct DevMesh {
+  int N = 0, F = 0, B = 0, nslices = 0, nslots = 0;
+  int solD[3] = {1, 1, 1};
+  int* own = nullptr;
+  int* nei = nullptr;
+  double* Sf = nullptr;      // [3][F] SoA
+  double* magSf = nullptr;   // [F]
+  double* w = nullptr;       // [F]
+  double* nodc = nullptr;    // [F]
+  double* dOwn = nullptr;    // [3][F] Cf - C[own]
+  double* dNei = nullptr;    // [3][F] Cf - C[nei]
+  double* dCC = nullptr;     // [3][F] C[nei] - C[own]
+  double* nf = nullptr;      // [3][F] Sf/magSf
+  double* bnf = nullptr;     // [3][B] Sf/magSf
+  double* C = nullptr;       // [3][N]
+  double* V = nullptr;       // [N]
+  int* bcell = nullptr;      // [B]
+  int* bpatch = nullptr;     // [B]
+  double* bSf = nullptr;     // [3][B]
+  double* bmagSf = nullptr;  // [B]
+  double* bdOwn = nullptr;   // [3][B] Cf - C
+  double* bdc = nullptr;     // [B]
+  Patch* patches = nullptr;
+  int npatches = 0;
+  // cell -> internal faces CSR in increasing face order (code f: owner side, ~f: neighbour side)
+  int* cptr = nullptr;
+  int* cface = nullptr;
+  // cell -> boundary faces CSR
+  int* bptr = nullptr;
+  int* bface = nullptr;
+  // sliced-ELL structure
+  int* slot_base = nullptr;  // [nslices+1]
+  int* scol = nullptr;       // [nslots*32] column or -1
+  int* sface = nullptr;      // [nslots*32] face code or 0x7fffffff
+  int* nlow = nullptr;       // [N] number of lower slots
+  int* nslot = nullptr;      // [N] number of slots
+  // LU-SGS level schedule
+  int nfl = 0, nrl = 0;              // number of forward / reverse levels
+  std::vector<int> fl_ptr, rl_ptr;   // host copies of level pointers
+  std::vector<int> fl_cstart, rl_cstart;  // first cell when a level is a contiguous range, else -1
+  int* fl_cells = nullptr;           // cells by forward level
+  int* rl_cells = nullptr;           // cells by reverse level
+  int* fl_lptr = nullptr;            // device copies of the level pointers
+  int* rl_lptr = nullptr;
+};
+
+struct Cfg {
+  ics_config c;
+  double Cv, gamma;
+};
+
+struct Handle {
+  DevMesh m;
+  Cfg cfg;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // state
+  double* W = nullptr;      // [N][5]
+  double* W0 = nullptr;
+  double* W00 = nullptr;
+  double* Wprev = nullptr;
+  double* prim = nullptr;   // [5][N]: p, T, Ux, Uy, Uz
+  double* pB = nullptr;     // [B]
+  double* TB = nullptr;
+  double* UB = nullptr;     // [3][B]
+  double* phiB = nullptr;
+  double* pseudoCo = nullptr;
+  double* rPDT = nullptr;
+  double* ddtCoeff = nullptr;
+  int timeIndex = 0;
+  // residual pipeline
+  double* q = nullptr;      // [NQ][N]
+  double* bq = nullptr;     // [NQ][B]
+  double* clin = nullptr;   // [N] sqrt(gamma/psi)
+  double* grad = nullptr;   // [NQ][3][N]
+  double* fflux = nullptr;  // [5][F+B]
+  double* frec = nullptr;   // [8][F]: ULx,ULy,ULz,URx,URy,URz,EL,ER
+  double* flam = nullptr;   // [F+B]
+  double* bjac = nullptr;   // [25][B] boundary Jacobian diag contribution
+  double* src = nullptr;    // [N][5] source = R*V
+  // Jacobian (FP64 or FP32 storage by precision)
+  void* blk = nullptr;      // [nslots*25*32]
+  void* dg = nullptr;       // [nslices*25*32]
+  void* dginv = nullptr;    // Jacobi inverse, same layout as dg
+  void* rD = nullptr;       // [N]
+  bool haveMatrix = false, haveIncrement = false, haveFlux = false;
+  int jacPrecision = ICS_PREC_FP64;
+  // Krylov workspace (element type by precision)
+  void* kv = nullptr;       // [m][N][5]
+  void* kw = nullptr;       // [N][5]
+  void* kx = nullptr;       // [N][5]
+  void* kb = nullptr;       // [N][5]
+  void* kt = nullptr;       // [N][5]
+  double* dW = nullptr;     // [N][5]
+  int kvDirs = 0, kvPrec = -1;
+  // reductions
+  double* partials = nullptr;   // [REDUCE_BLOCKS * 16]
+  unsigned int* counter = nullptr;
+  KrylovScalars* ks = nullptr;  // device
+  KrylovScalars* ksHost = nullptr;  // pinned mirror
+  // host-side residual bookkeeping (setCoAndDeltaT.H, pseudotimeControl)
+  bool initResValid = false, prevResValid = false;
+  ics_solver_perf initRes{}, prevRes{};
+  int corr = 0;
+  bool converged_ = false, firstIteration_ = true;
+  ics_solver_perf residuals_{}, initResiduals_{};
+  double lastRhoL2 = 0;
+  // scratch
+  double* scratch = nullptr;  // generic [N*5] doubles
+  int* ibuf = nullptr;        // [N] flags
+};
+
+// ------------------------------------------------------------------ kernels
+void launch_fields(Handle& h);
+void launch_grad(Handle& h);
+void launch_face_flux(Handle& h);
+void launch_residual(Handle& h, double serRatio, bool applySer);
+void launch_jacobian(Handle& h);
+void launch_update(Handle& h, int* boundedDev);
+void launch_bc(Handle& h);
+void launch_set_primitive(Handle& h);
+void launch_derive_primitive(Handle& h);
+void launch_bound_local_timestep(Handle& h);
+
+// linear algebra: precision-dispatched (mixed = FP32 blocks and vectors)
+void spmv(Handle& h, const void* x, void* y);
+int precondition(Handle& h, void* r);
+int gmres_solve(Handle& h, ics_solver_perf* perf);
+void to_vec(Handle& h, const double* src, void* dst);   // FP64 -> Krylov type
+void from_vec(Handle& h, const void* src, double* dst); // Krylov type -> FP64
+
+inline int prec(const Handle& h) { return h.cfg.c.precision; }
+inline size_t vbytes(const Handle& h) { return prec(h) == ICS_PREC_MIXED ? 4 : 8; }
+
+#define ICS_CUDA(call)                                                    \
+  do {                                                                    \
+    cudaError_t e_ = (call);                                              \
+    if (e_ != cudaSuccess) throw ::ics::CudaError(e_, #call, __FILE__, __LINE__); \
+  } while (0)
+
+struct CudaError {
+  cudaError_t e;
+  const char* what;
+  const char* file;
+  int line;
+  CudaError(cudaError_t e_, const char* w, const char* f, int l) : e(e_), what(w), file(f), line(l) {}
+};
+
+inline int grid_for(long n, int bs) {
+  long g = (n + bs - 1) / bs;
+  return (int)(g < 1 ? 1 : g);
+}
+
+}  // namespace ics

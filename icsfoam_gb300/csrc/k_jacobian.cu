@@ -1,0 +1,302 @@
+// Jacobian assembly into the sliced-ELL block matrix.
+//
+// Row-parallel: the thread of cell c writes its whole row (diagonal block and
+// one block per internal face), so every store is coalesced across the warp
+// and no atomics are needed.  For face f the reference inserts
+//     upper_f = 0.5|S| A(W_R) - 0.5|S| lambda I   (row own, column nei)
+//     lower_f = -0.5|S| A(W_L) - 0.5|S| lambda I  (row nei, column own)
+// and the diagonal is the negative column sum of the off-diagonal blocks
+// (LduMatrix::negSumDiag), plus the boundary dissipation, the boundary
+// Jacobian and the temporal term.  Each cell therefore evaluates A(W_L) and
+// A(W_R) of its faces (both sides of a face evaluate both Jacobians); in
+// mixed precision this block arithmetic runs in FP32.
+//
+// Reference: convectiveFluxScheme::addFluxTerms (convectiveFluxScheme.C:374-484),
+// addDissipationJacobian (:487-534), addBoundaryTerms with boundaryJacobian
+// (:47-120, :219-355), addTemporalTerms (:358-369); blockFvMatrix::insertBlock
+// and insertDissipationBlock (blockFvMatrix.C:211-326); LU-SGS scalar
+// diagonal (lusgs.C:50-127).
+#include "flux.cuh"
+#include "ics_internal.cuh"
+
+namespace ics {
+
+// Euler flux Jacobian entry (row i, column j) of state (U, E) for normal n.
+template <typename T>
+struct EulerJ {
+  T U[3], n[3], theta, a1, a2, projU, g;
+  __device__ __forceinline__ void init(T gamma, const T* u, T E, const T* nn) {
+    g = gamma;
+    for (int k = 0; k < 3; ++k) {
+      U[k] = u[k];
+      n[k] = nn[k];
+    }
+    theta = T(0.5) * (g - T(1)) * (U[0] * U[0] + U[1] * U[1] + U[2] * U[2]);
+    a1 = g * E - theta;
+    a2 = g - T(1);
+    projU = U[0] * n[0] + U[1] * n[1] + U[2] * n[2];
+  }
+  __device__ __forceinline__ T entry(int i, int j) const {
+    if (i == 0) return j == 0 ? T(0) : (j == 4 ? T(0) : n[j - 1]);
+    if (i == 4) {
+      if (j == 0) return projU * (theta - a1);
+      if (j == 4) return g * projU;
+      return n[j - 1] * a1 - a2 * U[j - 1] * projU;
+    }
+    const int r = i - 1;
+    if (j == 0) return n[r] * theta - U[r] * projU;
+    if (j == 4) return n[r] * a2;
+    const int cc = j - 1;
+    return U[r] * n[cc] - a2 * n[r] * U[cc] + (r == cc ? projU : T(0));
+  }
+};
+
+// Boundary diagonal contribution of one boundary face (addBoundaryTerms and
+// the boundary part of insertDissipationBlock), FP64, [25][B].
+__global__ void k_jac_boundary(DevMesh m, double R, double Cv, double gamma, const double* __restrict__ W,
+                               const double* __restrict__ prim, const double* __restrict__ pB,
+                               const double* __restrict__ TB, const double* __restrict__ UBv,
+                               const double* __restrict__ phiB, const double* __restrict__ flam,
+                               double* __restrict__ bjac) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= m.B) return;
+  const int B = m.B, N = m.N;
+  const Patch pt = m.patches[m.bpatch[b]];
+  const int ci = m.bcell[b];
+  const double bm = m.bmagSf[b];
+  const double SfB[3] = {m.bSf[b], m.bSf[B + b], m.bSf[2 * B + b]};
+  const double nf[3] = {SfB[0] / bm, SfB[1] / bm, SfB[2] / bm};
+  double pV = 1, tV = 1, uV[3] = {1, 1, 1};
+  switch (pt.kind) {
+    case ICS_PATCH_SLIP:
+      for (int k = 0; k < 3; ++k) uV[k] = 1 - fabs(nf[k]);
+      break;
+    case ICS_PATCH_FIXED:
+      pV = 0;
+      tV = 0;
+      uV[0] = uV[1] = uV[2] = 0;
+      break;
+    case ICS_PATCH_PRESSURE_OUTLET: pV = 0; break;
+    case ICS_PATCH_TOTAL_INLET:
+      pV = 0;
+      tV = 0;
+      if (phiB[b] < 0)
+        for (int k = 0; k < 3; ++k) uV[k] = nf[k] * nf[k];
+      break;
+    case ICS_PATCH_ISOTHERMAL_WALL:
+      tV = 0;
+      uV[0] = uV[1] = uV[2] = 0;
+      break;
+    default: break;
+  }
+  const double TBb = TB[b], pBb = pB[b];
+  const double rhoB = (1.0 / (R * TBb)) * pBb;
+  const double UB[3] = {UBv[b], UBv[B + b], UBv[2 * B + b]};
+  const double UrelBdotSf = dot3(UB, SfB) - 0.0 * bm;
+  const double rhoEB = rhoB * (Cv * TBb + 0.5 * dot3(UB, UB));
+  double SuV[3], dCdU[3], dMdp[3], dMdT[3], dEdU[3], dMdUDiag[3];
+  double dMdU[3][3];
+  const double dCdp = rhoB / pBb * UrelBdotSf * pV;
+  const double dCdT = -rhoB / TBb * UrelBdotSf * tV;
+  for (int k = 0; k < 3; ++k) {
+    SuV[k] = SfB[k] * uV[k];
+    dCdU[k] = rhoB * SuV[k];
+    dMdp[k] = (rhoB / pBb * UB[k] * UrelBdotSf + SfB[k]) * pV;
+    dMdUDiag[k] = rhoB * UrelBdotSf * uV[k];
+    dMdT[k] = -rhoB / TBb * UB[k] * UrelBdotSf * tV;
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) dMdU[i][j] = (rhoB * UB[i]) * SuV[j];
+  for (int i = 0; i < 3; ++i) dMdU[i][i] += dMdUDiag[i];
+  const double dEdp = (rhoEB / pBb * UrelBdotSf + dot3(UB, SfB)) * pV;
+  for (int k = 0; k < 3; ++k) dEdU[k] = SuV[k] * (rhoEB + pBb) + rhoB * UrelBdotSf * (UB[k] * uV[k]);
+  const double dEdT = UrelBdotSf * (rhoB * Cv - rhoEB / TBb) * tV;
+  // interior derivatives
+  const double rhoI = W[5 * ci], rhoEI = W[5 * ci + 4];
+  const double UI[3] = {prim[2 * N + ci], prim[3 * N + ci], prim[4 * N + ci]};
+  const double magU2 = dot3(UI, UI);
+  const double dPdRho = 0.5 * (gamma - 1) * magU2;
+  double dUdRho[3], dPdRhoU[3], dTdRhoU[3];
+  for (int k = 0; k < 3; ++k) {
+    dUdRho[k] = -1.0 * UI[k] / rhoI;
+    dPdRhoU[k] = -(gamma - 1) * UI[k];
+    dTdRhoU[k] = -1.0 * UI[k] / (Cv * rhoI);
+  }
+  const double dTdRho = -1.0 / (Cv * rhoI) * (rhoEI / rhoI - magU2);
+  const double dUdRhoU = 1.0 / rhoI;
+  const double dPdRhoE = gamma - 1;
+  const double dTdRhoE = 1.0 / (Cv * rhoI);
+  double D[25];
+  for (int k = 0; k < 25; ++k) D[k] = 0.0;
+  D[0] = dCdp * dPdRho + dot3(dCdU, dUdRho) + dCdT * dTdRho;
+  for (int j = 0; j < 3; ++j) D[1 + j] = dCdp * dPdRhoU[j] + dCdU[j] * dUdRhoU + dCdT * dTdRhoU[j];
+  D[4] = dCdp * dPdRhoE + 0.0 + dCdT * dTdRhoE;
+  for (int i = 0; i < 3; ++i) {
+    D[5 * (1 + i)] = dMdp[i] * dPdRho + (dMdU[i][0] * dUdRho[0] + dMdU[i][1] * dUdRho[1] + dMdU[i][2] * dUdRho[2]) +
+                     dMdT[i] * dTdRho;
+    for (int j = 0; j < 3; ++j)
+      D[5 * (1 + i) + 1 + j] = dMdp[i] * dPdRhoU[j] + dMdU[i][j] * dUdRhoU + dMdT[i] * dTdRhoU[j];
+    D[5 * (1 + i) + 4] = dMdp[i] * dPdRhoE + 0.0 + dMdT[i] * dTdRhoE;
+  }
+  D[20] = dEdp * dPdRho + dot3(dEdU, dUdRho) + dEdT * dTdRho;
+  for (int j = 0; j < 3; ++j) D[21 + j] = dEdp * dPdRhoU[j] + dEdU[j] * dUdRhoU + dEdT * dTdRhoU[j];
+  D[24] = dEdp * dPdRhoE + 0.0 + dEdT * dTdRhoE;
+  // boundary dissipation 0.5 |S_b| lambda_b on the diagonal entries
+  const double d = 0.5 * bm * flam[m.F + b];
+  for (int q = 0; q < 5; ++q) D[6 * q] += d;
+  for (int k = 0; k < 25; ++k) bjac[k * B + b] = D[k];
+}
+
+// Row assembly.  T = block storage/compute type.
+template <typename T>
+__global__ void __launch_bounds__(128) k_jac_rows(DevMesh m, double gamma, const double* __restrict__ frec,
+                                                  const double* __restrict__ flam, const double* __restrict__ bjac,
+                                                  const double* __restrict__ ddtCoeff, T* __restrict__ blk,
+                                                  T* __restrict__ dg, T* __restrict__ rD, int* __restrict__ status) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.N) return;
+  const int F = m.F, B = m.B;
+  const int s = c >> 5, lane = c & 31;
+  T diag[25];
+#pragma unroll
+  for (int k = 0; k < 25; ++k) diag[k] = T(0);
+  const T g = T(gamma);
+  const int base = m.slot_base[s];
+  const int width = m.slot_base[s + 1] - base;
+  const int ns = m.nslot[c];
+  for (int t = 0; t < width; ++t) {
+    const int idx = (base + t) * 32 + lane;
+    T* out = blk + (size_t)(base + t) * 25 * 32 + lane;
+    if (t >= ns) {
+#pragma unroll
+      for (int k = 0; k < 25; ++k) out[k * 32] = T(0);
+      continue;
+    }
+    const int code = m.sface[idx];
+    const bool isOwn = code >= 0;
+    const int f = isOwn ? code : ~code;
+    const T nn[3] = {T(m.nf[f]), T(m.nf[F + f]), T(m.nf[2 * F + f])};
+    const T UL[3] = {T(frec[f]), T(frec[F + f]), T(frec[2 * F + f])};
+    const T UR[3] = {T(frec[3 * F + f]), T(frec[4 * F + f]), T(frec[5 * F + f])};
+    EulerJ<T> AL, AR;
+    AL.init(g, UL, T(frec[6 * F + f]), nn);
+    AR.init(g, UR, T(frec[7 * F + f]), nn);
+    const T magS = T(m.magSf[f]);
+    const T hs = T(0.5) * magS;
+    const T mhs = T(-0.5) * magS;
+    const T d = T(0.5) * magS * T(flam[f]);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+#pragma unroll
+      for (int j = 0; j < 5; ++j) {
+        const int k = 5 * i + j;
+        const T lo = mhs * AL.entry(i, j);
+        const T up = hs * AR.entry(i, j);
+        T off;
+        if (isOwn) {
+          // row own: this slot is upper_f; diagonal gains -lower_f
+          off = up;
+          diag[k] -= lo;
+        } else {
+          off = lo;
+          diag[k] -= up;
+        }
+        if (i == j) {
+          off -= d;
+          diag[k] += d;
+        }
+        out[k * 32] = off;
+      }
+    }
+  }
+  const int b0 = m.bptr[c], b1 = m.bptr[c + 1];
+  for (int e = b0; e < b1; ++e) {
+    const int b = m.bface[e];
+#pragma unroll
+    for (int k = 0; k < 25; ++k) diag[k] += T(bjac[k * B + b]);
+  }
+  const T dc = T(ddtCoeff[c] * m.V[c]);
+#pragma unroll
+  for (int q = 0; q < 5; ++q) diag[6 * q] += dc;
+  T* dout = dg + (size_t)s * 25 * 32 + lane;
+#pragma unroll
+  for (int k = 0; k < 25; ++k) dout[k * 32] = diag[k];
+  // LU-SGS scalar diagonal: rD = 1/max over the five diagonal entries
+  double r = GREAT;
+  const int order[5] = {0, 24, 6, 12, 18};
+#pragma unroll
+  for (int q = 0; q < 5; ++q) r = 1.0 / fmax(1.0 / r, fabs((double)diag[order[q]]));
+  if (!(r >= VSMALL)) atomicOr(status, 1);
+  rD[c] = T(r);
+}
+
+// 5x5 block inverses for the Jacobi preconditioner (Jacobi.C:55-135 with
+// JacobiSmoother::calcInvDiag); Gauss-Jordan with partial pivoting.
+template <typename T>
+__global__ void k_jacobi_inverse(int N, const T* __restrict__ dg, T* __restrict__ inv, int* __restrict__ status) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= N) return;
+  const int s = c >> 5, lane = c & 31;
+  double a[5][10];
+  const T* src = dg + (size_t)s * 25 * 32 + lane;
+  for (int i = 0; i < 5; ++i)
+    for (int j = 0; j < 5; ++j) {
+      a[i][j] = (double)src[(5 * i + j) * 32];
+      a[i][5 + j] = i == j ? 1.0 : 0.0;
+    }
+  for (int k = 0; k < 5; ++k) {
+    int p = k;
+    double mx = fabs(a[k][k]);
+    for (int i = k + 1; i < 5; ++i)
+      if (fabs(a[i][k]) > mx) {
+        mx = fabs(a[i][k]);
+        p = i;
+      }
+    if (mx == 0.0) {
+      atomicOr(status, 1);
+      return;
+    }
+    if (p != k)
+      for (int j = 0; j < 10; ++j) {
+        double t = a[k][j];
+        a[k][j] = a[p][j];
+        a[p][j] = t;
+      }
+    const double piv = a[k][k];
+    for (int j = 0; j < 10; ++j) a[k][j] /= piv;
+    for (int i = 0; i < 5; ++i) {
+      if (i == k) continue;
+      const double fct = a[i][k];
+      for (int j = 0; j < 10; ++j) a[i][j] -= fct * a[k][j];
+    }
+  }
+  T* dst = inv + (size_t)s * 25 * 32 + lane;
+  for (int i = 0; i < 5; ++i)
+    for (int j = 0; j < 5; ++j) dst[(5 * i + j) * 32] = T(a[i][5 + j]);
+}
+
+void launch_jacobian(Handle& h) {
+  if (h.m.B > 0)
+    k_jac_boundary<<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, h.cfg.c.R, h.cfg.Cv, h.cfg.gamma, h.W, h.prim,
+                                                                h.pB, h.TB, h.UB, h.phiB, h.flam, h.bjac);
+  int* status = &h.ks->status;
+  if (prec(h) == ICS_PREC_MIXED) {
+    k_jac_rows<float><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, h.cfg.gamma, h.frec, h.flam, h.bjac,
+                                                                   h.ddtCoeff, (float*)h.blk, (float*)h.dg,
+                                                                   (float*)h.rD, status);
+    if (h.cfg.c.preconditioner == ICS_PC_JACOBI)
+      k_jacobi_inverse<float><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m.N, (float*)h.dg, (float*)h.dginv,
+                                                                          status);
+  } else {
+    k_jac_rows<double><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, h.cfg.gamma, h.frec, h.flam, h.bjac,
+                                                                    h.ddtCoeff, (double*)h.blk, (double*)h.dg,
+                                                                    (double*)h.rD, status);
+    if (h.cfg.c.preconditioner == ICS_PC_JACOBI)
+      k_jacobi_inverse<double><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m.N, (double*)h.dg, (double*)h.dginv,
+                                                                           status);
+  }
+  ICS_CUDA(cudaGetLastError());
+  h.jacPrecision = prec(h);
+}
+
+}  // namespace ics

@@ -1,0 +1,582 @@
+// Block linear algebra on the sliced-ELL Jacobian and the Krylov solver.
+//
+//   spmv      y = A x, thread per row; diagonal + one 5x5 block per face slot,
+//             slots in column order (= face order, the order Amul adds them)
+//   lusgs     (D_s + L) D_s^-1 (D_s + U) z = r with the scalar diagonal D_s,
+//             level-scheduled: a level holds rows whose lower (forward) or
+//             upper (reverse) neighbours all lie in earlier levels.  Within a
+//             row the neighbour contributions are subtracted in the order the
+//             sequential sweep of lusgs.C:233-384 applies them.
+//   jacobi    z = D^-1 r with precomputed 5x5 inverses (Jacobi.C:55-135)
+//   gmres     left-preconditioned restarted GMRES with modified Gram-Schmidt
+//             and Givens rotations (gmres.C:772-1107).  All vectors and the
+//             Hessenberg matrix stay on the device; dot products use a fixed
+//             grid and a last-block-done tree, so results are reproducible
+//             run to run.  One host synchronisation per restart cycle reads
+//             the L1 residuals for the stop test (coupledMatrixSolver.C:198-221).
+#include <cmath>
+
+#include "ics_internal.cuh"
+
+namespace ics {
+
+// ------------------------------------------------------------------ reduce
+template <int NV>
+__device__ __forceinline__ void reduce_finish(double (&v)[NV], double* __restrict__ partials,
+                                              unsigned int* __restrict__ counter, double* __restrict__ out) {
+  __shared__ double sm[32][NV];
+  __shared__ bool amLast;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double x = v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sm[warp][k] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = blockDim.x >> 5;
+    for (int k = 0; k < NV; ++k) {
+      double s = 0;
+      for (int w = 0; w < nw; ++w) s += sm[w][k];
+      partials[blockIdx.x * NV + k] = s;
+    }
+    __threadfence();
+    const unsigned t = atomicAdd(counter, 1u);
+    amLast = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (amLast && threadIdx.x < NV) {
+    __threadfence();
+    const int k = threadIdx.x;
+    double s = 0;
+    const volatile double* vp = partials;
+    for (int b = 0; b < (int)gridDim.x; ++b) s += vp[b * NV + k];
+    out[k] = s;
+  }
+  if (amLast && threadIdx.x == 0) *counter = 0;
+}
+
+constexpr int RB = 256;  // threads per reduction block
+
+// ------------------------------------------------------------------- spmv
+template <typename TB, typename TV>
+__global__ void __launch_bounds__(128) k_spmv(DevMesh m, const TB* __restrict__ blk, const TB* __restrict__ dg,
+                                              const TV* __restrict__ x, TV* __restrict__ y) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.N) return;
+  const int s = c >> 5, lane = c & 31;
+  TV xc[5], acc[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) xc[k] = x[5 * c + k];
+  const TB* D = dg + (size_t)s * 25 * 32 + lane;
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    TV a = TV(0);
+#pragma unroll
+    for (int j = 0; j < 5; ++j) a += TV(D[(5 * i + j) * 32]) * xc[j];
+    acc[i] = a;
+  }
+  const int base = m.slot_base[s];
+  const int ns = m.nslot[c];
+  for (int t = 0; t < ns; ++t) {
+    const int col = m.scol[(base + t) * 32 + lane];
+    TV xj[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) xj[k] = x[5 * col + k];
+    const TB* Bk = blk + (size_t)(base + t) * 25 * 32 + lane;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      TV a = TV(0);
+#pragma unroll
+      for (int j = 0; j < 5; ++j) a += TV(Bk[(5 * i + j) * 32]) * xj[j];
+      acc[i] += a;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) y[5 * c + k] = acc[k];
+}
+
+// ------------------------------------------------------------------ LU-SGS
+template <typename TB, typename TV>
+__device__ __forceinline__ void lusgs_fwd_row(const DevMesh& m, const TB* __restrict__ blk, const TB* __restrict__ rD,
+                                              TV* __restrict__ r, int c) {
+  const int s = c >> 5, lane = c & 31;
+  const int base = m.slot_base[s];
+  const int nl = m.nlow[c];
+  TV acc[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) acc[k] = r[5 * c + k];
+  for (int t = 0; t < nl; ++t) {
+    const int col = m.scol[(base + t) * 32 + lane];
+    const TV rj = TV(rD[col]);
+    TV dj[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) dj[k] = rj * r[5 * col + k];
+    const TB* Bk = blk + (size_t)(base + t) * 25 * 32 + lane;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      TV a = TV(0);
+#pragma unroll
+      for (int j = 0; j < 5; ++j) a += TV(Bk[(5 * i + j) * 32]) * dj[j];
+      acc[i] -= a;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) r[5 * c + k] = acc[k];
+}
+
+template <typename TB, typename TV>
+__device__ __forceinline__ void lusgs_rev_row(const DevMesh& m, const TB* __restrict__ blk, const TB* __restrict__ rD,
+                                              TV* __restrict__ r, int c) {
+  const int s = c >> 5, lane = c & 31;
+  const int base = m.slot_base[s];
+  const int nl = m.nlow[c], ns = m.nslot[c];
+  TV acc[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) acc[k] = r[5 * c + k];
+  for (int t = ns - 1; t >= nl; --t) {
+    const int col = m.scol[(base + t) * 32 + lane];
+    TV dj[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) dj[k] = r[5 * col + k];
+    const TB* Bk = blk + (size_t)(base + t) * 25 * 32 + lane;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      TV a = TV(0);
+#pragma unroll
+      for (int j = 0; j < 5; ++j) a += TV(Bk[(5 * i + j) * 32]) * dj[j];
+      acc[i] -= a;
+    }
+  }
+  const TV rc = TV(rD[c]);
+#pragma unroll
+  for (int k = 0; k < 5; ++k) r[5 * c + k] = rc * acc[k];
+}
+
+// one launch per level: cells = level list (nullptr when the level is the
+// contiguous range [start, start+count))
+template <typename TB, typename TV, bool FWD>
+__global__ void __launch_bounds__(128) k_lusgs_level(DevMesh m, const TB* __restrict__ blk,
+                                                     const TB* __restrict__ rD, TV* __restrict__ r,
+                                                     const int* __restrict__ cells, int start, int count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const int c = cells ? cells[start + i] : start + i;
+  if (FWD)
+    lusgs_fwd_row<TB, TV>(m, blk, rD, r, c);
+  else
+    lusgs_rev_row<TB, TV>(m, blk, rD, r, c);
+}
+
+// one CTA walks every level (small meshes / many tiny levels)
+template <typename TB, typename TV, bool FWD>
+__global__ void __launch_bounds__(1024) k_lusgs_block(DevMesh m, const TB* __restrict__ blk,
+                                                      const TB* __restrict__ rD, TV* __restrict__ r,
+                                                      const int* __restrict__ cells, const int* __restrict__ lptr,
+                                                      int nlev) {
+  for (int l = 0; l < nlev; ++l) {
+    const int a = lptr[l], b = lptr[l + 1];
+    for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
+      const int c = cells[i];
+      if (FWD)
+        lusgs_fwd_row<TB, TV>(m, blk, rD, r, c);
+      else
+        lusgs_rev_row<TB, TV>(m, blk, rD, r, c);
+    }
+    __syncthreads();
+  }
+}
+
+template <typename TB, typename TV>
+__global__ void k_jacobi_apply(int N, const TB* __restrict__ inv, TV* __restrict__ r) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= N) return;
+  const int s = c >> 5, lane = c & 31;
+  const TB* D = inv + (size_t)s * 25 * 32 + lane;
+  TV x[5], z[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) x[k] = r[5 * c + k];
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    TV a = TV(0);
+#pragma unroll
+    for (int j = 0; j < 5; ++j) a += TV(D[(5 * i + j) * 32]) * x[j];
+    z[i] = a;
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) r[5 * c + k] = z[k];
+}
+
+// ------------------------------------------------------------ vector kernels
+template <typename TS, typename TD>
+__global__ void k_cast(long n, const TS* __restrict__ a, TD* __restrict__ b) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) b[i] = TD(a[i]);
+}
+
+// w -= hprev * vprev (when vprev), then sum w.vnext (or w.w) -> out
+template <typename TV>
+__global__ void __launch_bounds__(RB) k_mgs(long n, TV* __restrict__ w, const TV* __restrict__ vprev,
+                                            const double* __restrict__ hprev, const TV* __restrict__ vnext,
+                                            const int* __restrict__ status, double* __restrict__ partials,
+                                            unsigned int* __restrict__ counter, double* __restrict__ out) {
+  double acc[1] = {0.0};
+  if (*status == 0) {
+    const TV h = vprev ? TV(*hprev) : TV(0);
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+      TV x = w[i];
+      if (vprev) {
+        x = x - h * vprev[i];
+        w[i] = x;
+      }
+      const TV o = vnext ? vnext[i] : x;
+      acc[0] += double(x * o);
+    }
+  }
+  reduce_finish<1>(acc, partials, counter, out);
+}
+
+template <typename TV>
+__global__ void k_scale(long n, const TV* __restrict__ w, TV* __restrict__ v, const KrylovScalars* __restrict__ ks) {
+  if (ks->status) return;
+  const TV beta = TV(ks->beta);
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    v[i] = w[i] / beta;
+}
+
+// start of a cycle: beta = sqrt(sum), bh = (beta, 0...)
+__global__ void k_beta0(KrylovScalars* ks, int m) {
+  const double beta = sqrt(ks->red[0]);
+  ks->beta = beta;
+  for (int i = 0; i <= m; ++i) ks->bh[i] = 0.0;
+  ks->bh[0] = beta;
+  if (!(beta > 0.0)) ks->status = isfinite(beta) ? 2 : 4;
+}
+
+__device__ __forceinline__ void givens(double h, double beta, double& c, double& s) {
+  if (beta == 0) {
+    c = 1;
+    s = 0;
+  } else if (fabs(beta) > fabs(h)) {
+    const double tau = -h / beta;
+    s = 1.0 / sqrt(1.0 + tau * tau);
+    c = s * tau;
+  } else {
+    const double tau = -beta / h;
+    c = 1.0 / sqrt(1.0 + tau * tau);
+    s = c * tau;
+  }
+}
+
+// after MGS of direction i: H[j][i] for j <= i are in H (written by k_mgs),
+// red[1] holds |w|^2
+__global__ void k_hess(KrylovScalars* ks, int i, int m) {
+  if (ks->status) return;
+  double* H = ks->H;
+  const double beta = sqrt(ks->red[1]);
+  for (int j = 0; j < i; ++j) {
+    const double Hji = H[j * m + i];
+    H[j * m + i] = ks->c[j] * Hji - ks->s[j] * H[(j + 1) * m + i];
+    H[(j + 1) * m + i] = ks->s[j] * Hji + ks->c[j] * H[(j + 1) * m + i];
+  }
+  givens(H[i * m + i], beta, ks->c[i], ks->s[i]);
+  const double bhi = ks->bh[i];
+  ks->bh[i] = ks->c[i] * bhi - ks->s[i] * ks->bh[i + 1];
+  ks->bh[i + 1] = ks->s[i] * bhi + ks->c[i] * ks->bh[i + 1];
+  H[i * m + i] = ks->c[i] * H[i * m + i] - ks->s[i] * beta;
+  ks->beta = beta;
+}
+
+__global__ void k_backsub(KrylovScalars* ks, int m) {
+  if (ks->status) return;
+  for (int i = m - 1; i >= 0; --i) {
+    double sum = ks->bh[i];
+    for (int j = i + 1; j < m; ++j) sum -= ks->H[i * m + j] * ks->y[j];
+    const double hii = ks->H[i * m + i];
+    const double st = hii >= 0 ? hii + VSMALL : hii - VSMALL;
+    ks->y[i] = sum / st;
+  }
+}
+
+template <typename TV>
+__global__ void k_xupdate(long n, TV* __restrict__ x, const TV* __restrict__ V, const KrylovScalars* __restrict__ ks,
+                          int m) {
+  if (ks->status) return;
+  for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+    TV a = x[q];
+    for (int i = 0; i < m; ++i) a += TV(ks->y[i]) * V[(size_t)i * n + q];
+    x[q] = a;
+  }
+}
+
+// r = b - t, per-equation L1 sums of r (rho, rhoUx, rhoUy, rhoUz, rhoE)
+template <typename TV>
+__global__ void __launch_bounds__(RB) k_resid(int N, const double* __restrict__ b, const TV* __restrict__ t,
+                                              TV* __restrict__ r, double* __restrict__ partials,
+                                              unsigned int* __restrict__ counter, double* __restrict__ out) {
+  double acc[5] = {0, 0, 0, 0, 0};
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      const TV v = TV(b[5 * c + k]) - t[5 * c + k];
+      r[5 * c + k] = v;
+      acc[k] += fabs(double(v));
+    }
+  }
+  reduce_finish<5>(acc, partials, counter, out);
+}
+
+// sums of |b_k| (initial residual) and the norm factors
+template <typename TV>
+__global__ void __launch_bounds__(RB) k_normfac(int N, const double* __restrict__ b, const TV* __restrict__ t,
+                                                double* __restrict__ partials, unsigned int* __restrict__ counter,
+                                                double* __restrict__ out) {
+  // out: nf_rho, nf_rhoE, nf_rhoU, |b| rho, Ux, Uy, Uz, rhoE
+  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+    const double t0 = double(t[5 * c]), t4 = double(t[5 * c + 4]);
+    const double t1 = double(t[5 * c + 1]), t2 = double(t[5 * c + 2]), t3 = double(t[5 * c + 3]);
+    const double b0 = b[5 * c], b1 = b[5 * c + 1], b2 = b[5 * c + 2], b3 = b[5 * c + 3], b4 = b[5 * c + 4];
+    acc[0] += fabs(t0) + fabs(b0);
+    acc[1] += fabs(t4) + fabs(b4);
+    acc[2] += sqrt(t1 * t1 + t2 * t2 + t3 * t3) + sqrt(b1 * b1 + b2 * b2 + b3 * b3);
+    acc[3] += fabs(b0);
+    acc[4] += fabs(b1);
+    acc[5] += fabs(b2);
+    acc[6] += fabs(b3);
+    acc[7] += fabs(b4);
+  }
+  reduce_finish<8>(acc, partials, counter, out);
+}
+
+__global__ void __launch_bounds__(RB) k_wsum(int N, const double* __restrict__ W, double* __restrict__ partials,
+                                             unsigned int* __restrict__ counter, double* __restrict__ out) {
+  double acc[5] = {0, 0, 0, 0, 0};
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x)
+#pragma unroll
+    for (int k = 0; k < 5; ++k) acc[k] += W[5 * c + k];
+  reduce_finish<5>(acc, partials, counter, out);
+}
+
+template <typename TV>
+__global__ void k_wmavg(int N, const double* __restrict__ W, const KrylovScalars* __restrict__ ks,
+                        TV* __restrict__ out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= N) return;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) out[5 * c + k] = TV(W[5 * c + k] - ks->avg[k]);
+}
+
+__global__ void k_avg(KrylovScalars* ks, int N) {
+  for (int k = 0; k < 5; ++k) ks->avg[k] = ks->red[k] / N;
+}
+
+template <typename TV>
+__global__ void k_to_dW(int N, const TV* __restrict__ x, double* __restrict__ dW, int s0, int s1, int s2) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= N) return;
+  dW[5 * c] = double(x[5 * c]);
+  dW[5 * c + 1] = s0 == -1 ? 0.0 : double(x[5 * c + 1]);
+  dW[5 * c + 2] = s1 == -1 ? 0.0 : double(x[5 * c + 2]);
+  dW[5 * c + 3] = s2 == -1 ? 0.0 : double(x[5 * c + 3]);
+  dW[5 * c + 4] = double(x[5 * c + 4]);
+}
+
+__global__ void __launch_bounds__(RB) k_sumsq(int N, const double* __restrict__ a, double* __restrict__ partials,
+                                              unsigned int* __restrict__ counter, double* __restrict__ out) {
+  double acc[1] = {0.0};
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) acc[0] += a[c];
+  reduce_finish<1>(acc, partials, counter, out);
+}
+
+// -------------------------------------------------------------- dispatch
+template <typename TB, typename TV>
+static void spmv_t(Handle& h, const TV* x, TV* y) {
+  k_spmv<TB, TV><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, (const TB*)h.blk, (const TB*)h.dg, x, y);
+}
+
+
+template <typename TB, typename TV>
+static void lusgs_t(Handle& h, TV* r) {
+  const DevMesh& m = h.m;
+  const TB* blk = (const TB*)h.blk;
+  const TB* rD = (const TB*)h.rD;
+  // forward sweep, then reverse sweep; many small levels run in one CTA
+  if ((long)m.N < 2048L * m.nfl) {
+    k_lusgs_block<TB, TV, true><<<1, 1024, 0, h.stream>>>(m, blk, rD, r, m.fl_cells, m.fl_lptr, m.nfl);
+  } else {
+    for (int l = 0; l < m.nfl; ++l) {
+      const int a = m.fl_ptr[l], cnt = m.fl_ptr[l + 1] - a;
+      const bool contig = m.fl_cstart[l] >= 0;
+      k_lusgs_level<TB, TV, true><<<grid_for(cnt, 128), 128, 0, h.stream>>>(
+          m, blk, rD, r, contig ? nullptr : m.fl_cells, contig ? m.fl_cstart[l] : a, cnt);
+    }
+  }
+  if ((long)m.N < 2048L * m.nrl) {
+    k_lusgs_block<TB, TV, false><<<1, 1024, 0, h.stream>>>(m, blk, rD, r, m.rl_cells, m.rl_lptr, m.nrl);
+  } else {
+    for (int l = 0; l < m.nrl; ++l) {
+      const int a = m.rl_ptr[l], cnt = m.rl_ptr[l + 1] - a;
+      const bool contig = m.rl_cstart[l] >= 0;
+      k_lusgs_level<TB, TV, false><<<grid_for(cnt, 128), 128, 0, h.stream>>>(
+          m, blk, rD, r, contig ? nullptr : m.rl_cells, contig ? m.rl_cstart[l] : a, cnt);
+    }
+  }
+}
+
+template <typename TB, typename TV>
+static void precondition_t(Handle& h, TV* r) {
+  if (h.cfg.c.preconditioner == ICS_PC_LUSGS)
+    lusgs_t<TB, TV>(h, r);
+  else if (h.cfg.c.preconditioner == ICS_PC_JACOBI)
+    k_jacobi_apply<TB, TV><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m.N, (const TB*)h.dginv, r);
+}
+
+void spmv(Handle& h, const void* x, void* y) {
+  if (prec(h) == ICS_PREC_MIXED)
+    spmv_t<float, float>(h, (const float*)x, (float*)y);
+  else
+    spmv_t<double, double>(h, (const double*)x, (double*)y);
+  ICS_CUDA(cudaGetLastError());
+}
+
+int precondition(Handle& h, void* r) {
+  if (prec(h) == ICS_PREC_MIXED)
+    precondition_t<float, float>(h, (float*)r);
+  else
+    precondition_t<double, double>(h, (double*)r);
+  ICS_CUDA(cudaGetLastError());
+  return ICS_OK;
+}
+
+void to_vec(Handle& h, const double* src, void* dst) {
+  const long n = 5L * h.m.N;
+  if (prec(h) == ICS_PREC_MIXED)
+    k_cast<double, float><<<REDUCE_BLOCKS, RB, 0, h.stream>>>(n, src, (float*)dst);
+  else
+    ICS_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
+}
+
+void from_vec(Handle& h, const void* src, double* dst) {
+  const long n = 5L * h.m.N;
+  if (prec(h) == ICS_PREC_MIXED)
+    k_cast<float, double><<<REDUCE_BLOCKS, RB, 0, h.stream>>>(n, (const float*)src, dst);
+  else
+    ICS_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
+}
+
+// ----------------------------------------------------------------- GMRES
+static bool stop_test(const Handle& h, const ics_solver_perf& p) {
+  const ics_config& c = h.cfg.c;
+  if (p.n_iterations < c.min_iter) return false;
+  double mx = -VGREAT, mrel = -VGREAT;
+  for (int k = 0; k < 5; ++k) mx = fmax(mx, p.final_res[k]);
+  mrel = fmax(mrel, p.final_res[0] / (p.init_res[0] + ROOTVSMALL));
+  mrel = fmax(mrel, p.final_res[4] / (p.init_res[4] + ROOTVSMALL));
+  for (int k = 0; k < 3; ++k)
+    if (h.m.solD[k] == 1) mrel = fmax(mrel, p.final_res[1 + k] / (p.init_res[1 + k] + ROOTVSMALL));
+  return p.n_iterations >= c.max_iter || mx < c.tolerance || mrel < c.rel_tol;
+}
+
+template <typename TB, typename TV>
+static int gmres_t(Handle& h, ics_solver_perf* perf) {
+  const int N = h.m.N, m = h.cfg.c.n_directions;
+  const long n5 = 5L * N;
+  cudaStream_t st = h.stream;
+  KrylovScalars* ks = h.ks;
+  TV* V = (TV*)h.kv;
+  TV* w = (TV*)h.kw;
+  TV* x = (TV*)h.kx;
+  TV* t = (TV*)h.kt;
+  double* red = ks->red;
+  ICS_CUDA(cudaMemsetAsync(&ks->status, 0, sizeof(int), st));
+  // norm factors: A (W - avg(W))
+  k_wsum<<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.W, h.partials, h.counter, red);
+  k_avg<<<1, 1, 0, st>>>(ks, N);
+  k_wmavg<TV><<<grid_for(N, 256), 256, 0, st>>>(N, h.W, ks, w);
+  spmv_t<TB, TV>(h, w, t);
+  k_normfac<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.src, t, h.partials, h.counter, red);
+  ICS_CUDA(cudaMemcpyAsync(h.ksHost->red, red, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  ICS_CUDA(cudaStreamSynchronize(st));
+  double nf[3];
+  for (int k = 0; k < 3; ++k) nf[k] = h.ksHost->red[k] + VSMALL;
+  ics_solver_perf p;
+  memset(&p, 0, sizeof(p));
+  p.init_res[0] = h.ksHost->red[3] / nf[0];
+  p.init_res[1] = h.ksHost->red[4] / nf[2];
+  p.init_res[2] = h.ksHost->red[5] / nf[2];
+  p.init_res[3] = h.ksHost->red[6] / nf[2];
+  p.init_res[4] = h.ksHost->red[7] / nf[1];
+  for (int k = 0; k < 5; ++k) p.final_res[k] = p.init_res[k];
+  // r = b, x = 0
+  ICS_CUDA(cudaMemsetAsync(x, 0, n5 * sizeof(TV), st));
+  to_vec(h, h.src, w);
+  int status = ICS_OK;
+  do {
+    precondition_t<TB, TV>(h, w);
+    k_mgs<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, w, nullptr, nullptr, nullptr, &ks->status, h.partials, h.counter,
+                                            red);
+    k_beta0<<<1, 1, 0, st>>>(ks, m);
+    for (int i = 0; i < m; ++i) {
+      TV* vi = V + (size_t)i * n5;
+      k_scale<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, w, vi, ks);
+      spmv_t<TB, TV>(h, vi, w);
+      precondition_t<TB, TV>(h, w);
+      for (int j = 0; j <= i; ++j) {
+        const TV* vprev = j > 0 ? V + (size_t)(j - 1) * n5 : nullptr;
+        const double* hprev = j > 0 ? &ks->H[(j - 1) * m + i] : nullptr;
+        k_mgs<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, w, vprev, hprev, V + (size_t)j * n5, &ks->status, h.partials,
+                                                h.counter, &ks->H[j * m + i]);
+      }
+      k_mgs<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, w, vi, &ks->H[i * m + i], nullptr, &ks->status, h.partials,
+                                              h.counter, &red[1]);
+      k_hess<<<1, 1, 0, st>>>(ks, i, m);
+    }
+    k_backsub<<<1, 1, 0, st>>>(ks, m);
+    k_xupdate<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, x, V, ks, m);
+    spmv_t<TB, TV>(h, x, t);
+    k_resid<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.src, t, w, h.partials, h.counter, ks->res);
+    ICS_CUDA(cudaGetLastError());
+    ICS_CUDA(cudaMemcpyAsync(h.ksHost->res, ks->res, 5 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    ICS_CUDA(cudaMemcpyAsync(&h.ksHost->status, &ks->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ICS_CUDA(cudaStreamSynchronize(st));
+    if (h.ksHost->status) {
+      status = (h.ksHost->status & 4) ? ICS_ERR_NONFINITE : ICS_ERR_BREAKDOWN;
+      p.n_iterations++;
+      break;
+    }
+    const double* rs = h.ksHost->res;
+    p.final_res[0] = rs[0] / nf[0];
+    p.final_res[4] = rs[4] / nf[1];
+    for (int k = 0; k < 3; ++k) p.final_res[1 + k] = h.m.solD[k] == -1 ? 0.0 : rs[1 + k] / nf[2];
+    p.n_iterations++;
+    bool finite = true;
+    for (int k = 0; k < 5; ++k) finite = finite && std::isfinite(p.final_res[k]);
+    if (!finite) {
+      status = ICS_ERR_NONFINITE;
+      break;
+    }
+  } while (!stop_test(h, p));
+  p.converged = status == ICS_OK;
+  k_to_dW<TV><<<grid_for(N, 256), 256, 0, st>>>(N, x, h.dW, h.m.solD[0], h.m.solD[1], h.m.solD[2]);
+  ICS_CUDA(cudaGetLastError());
+  *perf = p;
+  return status;
+}
+
+int gmres_solve(Handle& h, ics_solver_perf* perf) {
+  if (prec(h) == ICS_PREC_MIXED) return gmres_t<float, float>(h, perf);
+  return gmres_t<double, double>(h, perf);
+}
+
+// rho L2 residual: sqrt(sum (div(phi) V)^2) from the per-cell squares
+double rho_l2(Handle& h) {
+  k_sumsq<<<REDUCE_BLOCKS, RB, 0, h.stream>>>(h.m.N, h.scratch, h.partials, h.counter, &h.ks->l2);
+  double v = 0;
+  ICS_CUDA(cudaMemcpyAsync(&v, &h.ks->l2, sizeof(double), cudaMemcpyDeviceToHost, h.stream));
+  ICS_CUDA(cudaStreamSynchronize(h.stream));
+  return std::sqrt(v);
+}
+
+}  // namespace ics

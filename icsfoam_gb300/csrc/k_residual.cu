@@ -1,0 +1,514 @@
+// Residual pipeline: reconstructed fields -> gradients (+ limiter) ->
+// face fluxes -> cell residual, local pseudo time step and ddtCoeff.
+//
+//   fields   (cell / boundary face)  q = rho, p, U, E, H, c          [NQ][N]
+//   grad     (cell, face-ordered gather) Gauss linear gradient of each
+//            reconstructed scalar; for MUSCL the cellLimited limiter is
+//            fused in (it needs only the cell's own gradient and its
+//            neighbours' values)                                       [NQ][3][N]
+//   face     (internal face) left/right reconstruction + flux scheme,
+//            linear-interpolated wave speed, reconstructed (U, E) kept
+//            for the Jacobian                                          [5][F]
+//   bface    (boundary face) L = R = boundary value
+//   cellres  (cell, face-ordered gather) div of the fluxes, dual-time ddt,
+//            source = R*V, SER update of the pseudo Courant number,
+//            rPseudoDeltaT and ddtCoeff (setCoAndDeltaT.H)
+//
+// Reference: ausmPlusUpFluxScheme.C:73-299, hllcFluxScheme.C:70-240,
+// roeFluxScheme.C:276-409, residualsUpdate.H:1-83, setCoAndDeltaT.H:39-141,
+// dualTimeDdtScheme.C:111-126.  Reconstruction restates OpenFOAM's
+// limitedScheme (NVD/TVD r with vanLeer or Minmod), linearUpwind and
+// cellLimited<Venkatakrishnan|minmod> Gauss linear gradients.
+#include "flux.cuh"
+#include "ics_internal.cuh"
+
+namespace ics {
+
+struct ResParams {
+  double R, Cv, gamma, cstarFac;
+  int scheme, reconRho, reconU, reconT, lowMach;
+  double entropyFix;
+};
+
+__device__ __forceinline__ int recon_of(const ResParams& P, int q) {
+  if (q == Q_RHO || q == Q_P) return P.reconRho;
+  if (q == Q_UX || q == Q_UY || q == Q_UZ) return P.reconU;
+  return P.reconT;
+}
+
+// ------------------------------------------------------------------ fields
+__global__ void k_fields(int N, int B, const double* __restrict__ W, const double* __restrict__ prim,
+                         const double* __restrict__ pB, const double* __restrict__ TB,
+                         const double* __restrict__ UB, ResParams P, double* __restrict__ q,
+                         double* __restrict__ bq, double* __restrict__ clin, double* __restrict__ bclin) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) {
+    const double rho = W[5 * i];
+    const double p = prim[i], T = prim[N + i];
+    const double U0 = prim[2 * N + i], U1 = prim[3 * N + i], U2 = prim[4 * N + i];
+    const double E = P.Cv * T + 0.5 * (U0 * U0 + U1 * U1 + U2 * U2);
+    const double H = fmax(E, SMALL) + fmax(p / rho, SMALL);
+    const double psi = 1.0 / (P.R * T);
+    const double cl = sqrt(P.gamma / psi);
+    q[Q_RHO * N + i] = rho;
+    q[Q_P * N + i] = p;
+    q[Q_UX * N + i] = U0;
+    q[Q_UY * N + i] = U1;
+    q[Q_UZ * N + i] = U2;
+    q[Q_E * N + i] = E;
+    q[Q_H * N + i] = H;
+    q[Q_C * N + i] = P.scheme == ICS_FLUX_AUSMPLUSUP ? sqrt(P.cstarFac * H) : fmax(cl, VSMALL);
+    clin[i] = cl;
+  }
+  if (i < B) {
+    const double p = pB[i], T = TB[i];
+    const double U0 = UB[i], U1 = UB[B + i], U2 = UB[2 * B + i];
+    const double psi = 1.0 / (P.R * T);
+    const double rho = psi * p;
+    const double E = P.Cv * T + 0.5 * (U0 * U0 + U1 * U1 + U2 * U2);
+    const double H = fmax(E, SMALL) + fmax(p / rho, SMALL);
+    const double cl = sqrt(P.gamma / psi);
+    bq[Q_RHO * B + i] = rho;
+    bq[Q_P * B + i] = p;
+    bq[Q_UX * B + i] = U0;
+    bq[Q_UY * B + i] = U1;
+    bq[Q_UZ * B + i] = U2;
+    bq[Q_E * B + i] = E;
+    bq[Q_H * B + i] = H;
+    bq[Q_C * B + i] = P.scheme == ICS_FLUX_AUSMPLUSUP ? sqrt(P.cstarFac * H) : fmax(cl, VSMALL);
+    bclin[i] = cl;
+  }
+}
+
+// --------------------------------------------------------------- gradients
+// One thread per cell; faces visited in increasing face index (the order the
+// face-loop gradient accumulates them).  mask selects the fields, limited
+// selects cellLimited (1 = minmod, 2 = Venkatakrishnan).
+template <int LIMITED>
+__global__ void __launch_bounds__(128) k_grad(DevMesh m, const double* __restrict__ q, const double* __restrict__ bq,
+                                              unsigned mask, double* __restrict__ grad) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.N) return;
+  const int N = m.N, F = m.F, B = m.B;
+  double g[NQ][3];
+  double qc[NQ], qmax[NQ], qmin[NQ];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    g[k][0] = g[k][1] = g[k][2] = 0.0;
+    qc[k] = (mask >> k) & 1 ? q[k * N + c] : 0.0;
+    qmax[k] = qmin[k] = qc[k];
+  }
+  const int e0 = m.cptr[c], e1 = m.cptr[c + 1];
+  for (int e = e0; e < e1; ++e) {
+    const int code = m.cface[e];
+    const bool isOwn = code >= 0;
+    const int f = isOwn ? code : ~code;
+    const int o = m.own[f], nb = m.nei[f];
+    const int other = isOwn ? nb : o;
+    const double wf = m.w[f];
+    const double S0 = m.Sf[f], S1 = m.Sf[F + f], S2 = m.Sf[2 * F + f];
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+      if (!((mask >> k) & 1)) continue;
+      const double qo = q[k * N + other];
+      const double qown = isOwn ? qc[k] : qo, qnei = isOwn ? qo : qc[k];
+      const double sf = wf * (qown - qnei) + qnei;
+      if (isOwn) {
+        g[k][0] = g[k][0] + S0 * sf;
+        g[k][1] = g[k][1] + S1 * sf;
+        g[k][2] = g[k][2] + S2 * sf;
+      } else {
+        g[k][0] = g[k][0] - S0 * sf;
+        g[k][1] = g[k][1] - S1 * sf;
+        g[k][2] = g[k][2] - S2 * sf;
+      }
+      if (LIMITED) {
+        qmax[k] = fmax(qmax[k], qo);
+        qmin[k] = fmin(qmin[k], qo);
+      }
+    }
+  }
+  const int b0 = m.bptr[c], b1 = m.bptr[c + 1];
+  for (int e = b0; e < b1; ++e) {
+    const int b = m.bface[e];
+    const double S0 = m.bSf[b], S1 = m.bSf[B + b], S2 = m.bSf[2 * B + b];
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+      if (!((mask >> k) & 1)) continue;
+      const double v = bq[k * B + b];
+      g[k][0] = g[k][0] + S0 * v;
+      g[k][1] = g[k][1] + S1 * v;
+      g[k][2] = g[k][2] + S2 * v;
+      if (LIMITED) {
+        qmax[k] = fmax(qmax[k], v);
+        qmin[k] = fmin(qmin[k], v);
+      }
+    }
+  }
+  const double Vc = m.V[c];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    g[k][0] = g[k][0] / Vc;
+    g[k][1] = g[k][1] / Vc;
+    g[k][2] = g[k][2] / Vc;
+  }
+  if (LIMITED) {
+    double lim[NQ];
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+      lim[k] = 1.0;
+      qmax[k] -= qc[k];
+      qmin[k] -= qc[k];
+    }
+    auto limitFace = [&](int k, double extrap) {
+      double r = 1;
+      if (extrap > SMALL)
+        r = qmax[k] / extrap;
+      else if (extrap < -SMALL)
+        r = qmin[k] / extrap;
+      const double lr = LIMITED == 2 ? (r * r + 2 * r) / (r * r + r + 2) : fmin(r, 1.0);
+      lim[k] = fmin(lim[k], lr);
+    };
+    for (int e = e0; e < e1; ++e) {
+      const int code = m.cface[e];
+      const bool isOwn = code >= 0;
+      const int f = isOwn ? code : ~code;
+      const double* d = isOwn ? m.dOwn : m.dNei;
+      const double d0 = d[f], d1 = d[F + f], d2 = d[2 * F + f];
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) {
+        if (!((mask >> k) & 1)) continue;
+        limitFace(k, d0 * g[k][0] + d1 * g[k][1] + d2 * g[k][2]);
+      }
+    }
+    for (int e = b0; e < b1; ++e) {
+      const int b = m.bface[e];
+      const double d0 = m.bdOwn[b], d1 = m.bdOwn[B + b], d2 = m.bdOwn[2 * B + b];
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) {
+        if (!((mask >> k) & 1)) continue;
+        limitFace(k, d0 * g[k][0] + d1 * g[k][1] + d2 * g[k][2]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+      g[k][0] = g[k][0] * lim[k];
+      g[k][1] = g[k][1] * lim[k];
+      g[k][2] = g[k][2] * lim[k];
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    if (!((mask >> k) & 1)) continue;
+    grad[(3 * k + 0) * N + c] = g[k][0];
+    grad[(3 * k + 1) * N + c] = g[k][1];
+    grad[(3 * k + 2) * N + c] = g[k][2];
+  }
+}
+
+// ------------------------------------------------------------ face fluxes
+// reconstruct field k on face f for direction dir (+1 owner side, -1 neighbour side)
+__device__ __forceinline__ double reconstruct(const DevMesh& m, int scheme, int k, int f, int o, int nb, double qo,
+                                              double qn, const double* __restrict__ grad, double dir) {
+  const int N = m.N, F = m.F;
+  const double wUp = dir > 0 ? 1.0 : 0.0;
+  if (scheme == ICS_RECON_UPWIND) return wUp * (qo - qn) + qn;
+  if (scheme == ICS_RECON_VANLEER || scheme == ICS_RECON_MINMOD) {
+    const int c = dir > 0 ? o : nb;
+    const double d0 = m.dCC[f], d1 = m.dCC[F + f], d2 = m.dCC[2 * F + f];
+    const double gradf = qn - qo;
+    const double gradcf = d0 * grad[(3 * k) * N + c] + d1 * grad[(3 * k + 1) * N + c] + d2 * grad[(3 * k + 2) * N + c];
+    double r;
+    if (fabs(gradcf) >= 1000 * fabs(gradf))
+      r = 2 * 1000 * (gradcf >= 0 ? 1.0 : -1.0) * (gradf >= 0 ? 1.0 : -1.0) - 1;
+    else
+      r = 2 * (gradcf / gradf) - 1;
+    double lim;
+    if (scheme == ICS_RECON_VANLEER)
+      lim = (r + fabs(r)) / (1 + fabs(r));
+    else
+      lim = fmax(fmin(fmin(r, 1.0), 2.0), 0.0);
+    const double wgt = lim * m.w[f] + (1.0 - lim) * wUp;
+    return wgt * (qo - qn) + qn;
+  }
+  // MUSCL: upwind value + limited-gradient extrapolation
+  const int c = dir > 0 ? o : nb;
+  const double* d = dir > 0 ? m.dOwn : m.dNei;
+  const double base = wUp * (qo - qn) + qn;
+  return base + (d[f] * grad[(3 * k) * N + c] + d[F + f] * grad[(3 * k + 1) * N + c] +
+                 d[2 * F + f] * grad[(3 * k + 2) * N + c]);
+}
+
+__global__ void __launch_bounds__(128) k_face(DevMesh m, ResParams P, const double* __restrict__ q,
+                                              const double* __restrict__ grad, const double* __restrict__ clin,
+                                              const double* __restrict__ nf, double* __restrict__ fflux,
+                                              double* __restrict__ frec, double* __restrict__ flam, int FB) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.F) return;
+  const int N = m.N, F = m.F;
+  const int o = m.own[f], nb = m.nei[f];
+  double qL[NQ], qR[NQ];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    if (P.scheme == ICS_FLUX_ROE && k == Q_C) {
+      qL[k] = qR[k] = 0.0;
+      continue;
+    }
+    const double qo = q[k * N + o], qn = q[k * N + nb];
+    const int sch = recon_of(P, k);
+    qL[k] = reconstruct(m, sch, k, f, o, nb, qo, qn, grad, +1.0);
+    qR[k] = reconstruct(m, sch, k, f, o, nb, qo, qn, grad, -1.0);
+  }
+  FState L{qL[Q_RHO], qL[Q_P], {qL[Q_UX], qL[Q_UY], qL[Q_UZ]}, qL[Q_E], qL[Q_H], qL[Q_C]};
+  FState R{qR[Q_RHO], qR[Q_P], {qR[Q_UX], qR[Q_UY], qR[Q_UZ]}, qR[Q_E], qR[Q_H], qR[Q_C]};
+  const double S[3] = {m.Sf[f], m.Sf[F + f], m.Sf[2 * F + f]};
+  const double n[3] = {nf[f], nf[F + f], nf[2 * F + f]};
+  const double magS = m.magSf[f];
+  double out[5];
+  if (P.scheme == ICS_FLUX_AUSMPLUSUP)
+    flux_ausm(L, R, S, magS, P.lowMach, out);
+  else if (P.scheme == ICS_FLUX_HLLC)
+    flux_hllc(L, R, n, magS, P.gamma, out);
+  else
+    flux_roe(L, R, n, magS, P.gamma, P.entropyFix, out);
+#pragma unroll
+  for (int k = 0; k < 5; ++k) fflux[k * FB + f] = out[k];
+  frec[0 * F + f] = qL[Q_UX];
+  frec[1 * F + f] = qL[Q_UY];
+  frec[2 * F + f] = qL[Q_UZ];
+  frec[3 * F + f] = qR[Q_UX];
+  frec[4 * F + f] = qR[Q_UY];
+  frec[5 * F + f] = qR[Q_UZ];
+  frec[6 * F + f] = qL[Q_E];
+  frec[7 * F + f] = qR[Q_E];
+  // wave speed with linear interpolation (setCoAndDeltaT.H:52-54)
+  const double wf = m.w[f];
+  const double ci = wf * (clin[o] - clin[nb]) + clin[nb];
+  double ui[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double a = q[(Q_UX + k) * N + o], b = q[(Q_UX + k) * N + nb];
+    ui[k] = wf * (a - b) + b;
+  }
+  flam[f] = ci + fabs(dot3(ui, n) - 0.0);
+}
+
+__global__ void k_bface(DevMesh m, ResParams P, const double* __restrict__ bq, const double* __restrict__ bclin,
+                        const double* __restrict__ bnf, double* __restrict__ fflux, double* __restrict__ flam,
+                        double* __restrict__ phiB, int FB) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= m.B) return;
+  const int B = m.B, F = m.F;
+  double qb[NQ];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) qb[k] = bq[k * B + b];
+  FState L{qb[Q_RHO], qb[Q_P], {qb[Q_UX], qb[Q_UY], qb[Q_UZ]}, qb[Q_E], qb[Q_H], qb[Q_C]};
+  const double S[3] = {m.bSf[b], m.bSf[B + b], m.bSf[2 * B + b]};
+  const double n[3] = {bnf[b], bnf[B + b], bnf[2 * B + b]};
+  const double magS = m.bmagSf[b];
+  double out[5];
+  if (P.scheme == ICS_FLUX_AUSMPLUSUP)
+    flux_ausm(L, L, S, magS, P.lowMach, out);
+  else if (P.scheme == ICS_FLUX_HLLC)
+    flux_hllc(L, L, n, magS, P.gamma, out);
+  else
+    flux_roe(L, L, n, magS, P.gamma, P.entropyFix, out);
+#pragma unroll
+  for (int k = 0; k < 5; ++k) fflux[k * FB + F + b] = out[k];
+  phiB[b] = out[0];
+  flam[F + b] = bclin[b] + fabs(dot3(L.U, n) - 0.0);
+}
+
+// ------------------------------------------------------------ cell residual
+struct CellResParams {
+  int ddt;            // ICS_DDT_*
+  double rDeltaT, coefft, coefft0, coefft00;
+  double serRatio;    // SER factor (setCoAndDeltaT.H:18-26)
+  int applySer;
+  double coMin, coMax;
+};
+
+__device__ __forceinline__ void ddt_matrix(const CellResParams& D, double Vc, double rpdt, double W, double W0,
+                                           double W00, double& dg, double& s) {
+  if (D.ddt == ICS_DDT_STEADY) {
+    dg = 0;
+    s = 0;
+  } else if (D.ddt == ICS_DDT_EULER) {
+    dg = D.rDeltaT * Vc;
+    s = D.rDeltaT * W0 * Vc;
+  } else {
+    dg = (D.coefft * D.rDeltaT) * Vc;
+    s = D.rDeltaT * Vc * (D.coefft0 * W0 - D.coefft00 * W00);
+  }
+  dg += rpdt * Vc;
+  s += rpdt * W * Vc;
+}
+
+__global__ void __launch_bounds__(128) k_cellres(DevMesh m, CellResParams D, const double* __restrict__ fflux, int FB,
+                                                 const double* __restrict__ flam, const double* __restrict__ W,
+                                                 const double* __restrict__ W0, const double* __restrict__ W00,
+                                                 const double* __restrict__ prim, const double* __restrict__ clin,
+                                                 double* __restrict__ pseudoCo, double* __restrict__ rPDT,
+                                                 double* __restrict__ ddtCoeff, double* __restrict__ src,
+                                                 double* __restrict__ l2cell) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.N) return;
+  const int N = m.N, F = m.F, B = m.B;
+  double dv[5] = {0, 0, 0, 0, 0};
+  double rmax = 0.0;
+  const int e0 = m.cptr[c], e1 = m.cptr[c + 1];
+  for (int e = e0; e < e1; ++e) {
+    const int code = m.cface[e];
+    const int f = code >= 0 ? code : ~code;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      const double v = fflux[k * FB + f];
+      dv[k] = code >= 0 ? dv[k] + v : dv[k] - v;
+    }
+    rmax = fmax(rmax, m.nodc[f] * flam[f]);
+  }
+  const int b0 = m.bptr[c], b1 = m.bptr[c + 1];
+  for (int e = b0; e < b1; ++e) {
+    const int b = m.bface[e];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) dv[k] += fflux[k * FB + F + b];
+    if (m.patches[m.bpatch[b]].is_wall) {
+      const double U0 = prim[2 * N + c], U1 = prim[3 * N + c], U2 = prim[4 * N + c];
+      const double bm = m.bmagSf[b];
+      const double un = U0 * (m.bSf[b] / bm) + U1 * (m.bSf[B + b] / bm) + U2 * (m.bSf[2 * B + b] / bm);
+      const double pl = 0.5 * m.bdc[b] * (clin[c] + fabs(un - 0.0));
+      rmax = fmax(rmax, pl);
+    }
+  }
+  const double Vc = m.V[c];
+  double r[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) r[k] = -(dv[k] / Vc);
+  const double dV0 = (dv[0] / Vc) * Vc;
+  l2cell[c] = dV0 * dV0;
+  const double rpOld = rPDT[c];
+  if (D.ddt != ICS_DDT_STEADY) {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      double dg, s;
+      const double w = W[5 * c + k];
+      ddt_matrix(D, Vc, rpOld, w, W0[5 * c + k], W00[5 * c + k], dg, s);
+      r[k] -= (dg * w - s) / Vc;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) src[5 * c + k] = r[k] * Vc;
+  double co = pseudoCo[c];
+  if (D.applySer) {
+    co *= D.serRatio;
+    co = fmax(fmin(co, D.coMax), D.coMin);
+    pseudoCo[c] = co;
+  }
+  const double rp = rmax / co;
+  rPDT[c] = rp;
+  double dg, s;
+  ddt_matrix(D, Vc, rp, 0.0, 0.0, 0.0, dg, s);
+  ddtCoeff[c] = dg / Vc;
+}
+
+// ------------------------------------------------------------------ launch
+static ResParams res_params(const Handle& h) {
+  ResParams P;
+  P.R = h.cfg.c.R;
+  P.Cv = h.cfg.Cv;
+  P.gamma = h.cfg.gamma;
+  P.cstarFac = 2.0 * (P.gamma - 1.0) / (P.gamma + 1.0);
+  P.scheme = h.cfg.c.flux_scheme;
+  P.reconRho = h.cfg.c.recon_rho;
+  P.reconU = h.cfg.c.recon_U;
+  P.reconT = h.cfg.c.recon_T;
+  P.lowMach = h.cfg.c.low_mach_ausm;
+  P.entropyFix = h.cfg.c.entropy_fix_coeff;
+  return P;
+}
+
+void launch_fields(Handle& h) {
+  const int n = h.m.N > h.m.B ? h.m.N : h.m.B;
+  k_fields<<<grid_for(n, 256), 256, 0, h.stream>>>(h.m.N, h.m.B, h.W, h.prim, h.pB, h.TB, h.UB, res_params(h), h.q,
+                                                   h.bq, h.clin, h.clin + h.m.N);
+  ICS_CUDA(cudaGetLastError());
+}
+
+static unsigned grad_mask(const Handle& h, int* limited) {
+  unsigned mask = 0;
+  int lim = 0;
+  const int rs[3] = {h.cfg.c.recon_rho, h.cfg.c.recon_U, h.cfg.c.recon_T};
+  const unsigned groups[3] = {(1u << Q_RHO) | (1u << Q_P), (1u << Q_UX) | (1u << Q_UY) | (1u << Q_UZ),
+                              (1u << Q_E) | (1u << Q_H) | (1u << Q_C)};
+  for (int g = 0; g < 3; ++g) {
+    if (rs[g] == ICS_RECON_UPWIND) continue;
+    mask |= groups[g];
+    if (rs[g] == ICS_RECON_MUSCL_VENKATAKRISHNAN) lim = 2;
+    if (rs[g] == ICS_RECON_MUSCL_MINMOD) lim = lim ? lim : 1;
+  }
+  if (h.cfg.c.flux_scheme == ICS_FLUX_ROE) mask &= ~(1u << Q_C);
+  *limited = lim;
+  return mask;
+}
+
+void launch_grad(Handle& h) {
+  int limited = 0;
+  const unsigned mask = grad_mask(h, &limited);
+  if (!mask) return;
+  // groups mixing limited and unlimited schemes are not supported: all
+  // reconstructed groups use the same gradient kind
+  const int rs[3] = {h.cfg.c.recon_rho, h.cfg.c.recon_U, h.cfg.c.recon_T};
+  for (int g = 0; g < 3; ++g) {
+    const bool isMuscl = rs[g] == ICS_RECON_MUSCL_VENKATAKRISHNAN || rs[g] == ICS_RECON_MUSCL_MINMOD;
+    if (rs[g] != ICS_RECON_UPWIND && (isMuscl != (limited != 0)))
+      throw std::string("reconstruction groups must all be TVD or all MUSCL");
+    if (isMuscl && rs[g] != (limited == 2 ? ICS_RECON_MUSCL_VENKATAKRISHNAN : ICS_RECON_MUSCL_MINMOD))
+      throw std::string("MUSCL groups must share one gradient limiter");
+  }
+  const int bs = 128;
+  if (limited == 2)
+    k_grad<2><<<grid_for(h.m.N, bs), bs, 0, h.stream>>>(h.m, h.q, h.bq, mask, h.grad);
+  else if (limited == 1)
+    k_grad<1><<<grid_for(h.m.N, bs), bs, 0, h.stream>>>(h.m, h.q, h.bq, mask, h.grad);
+  else
+    k_grad<0><<<grid_for(h.m.N, bs), bs, 0, h.stream>>>(h.m, h.q, h.bq, mask, h.grad);
+  ICS_CUDA(cudaGetLastError());
+}
+
+void launch_face_flux(Handle& h) {
+  const int FB = h.m.F + h.m.B;
+  const ResParams P = res_params(h);
+  if (h.m.F > 0)
+    k_face<<<grid_for(h.m.F, 128), 128, 0, h.stream>>>(h.m, P, h.q, h.grad, h.clin, h.m.nf, h.fflux,
+                                                        h.frec, h.flam, FB);
+  if (h.m.B > 0)
+    k_bface<<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, P, h.bq, h.clin + h.m.N, h.m.bnf, h.fflux,
+                                                         h.flam, h.phiB, FB);
+  ICS_CUDA(cudaGetLastError());
+}
+
+void launch_residual(Handle& h, double serRatio, bool applySer) {
+  CellResParams D;
+  D.ddt = h.cfg.c.ddt_scheme;
+  D.rDeltaT = D.coefft = D.coefft0 = D.coefft00 = 0;
+  if (D.ddt != ICS_DDT_STEADY) {
+    D.rDeltaT = 1.0 / h.cfg.c.delta_t;
+    if (D.ddt == ICS_DDT_BACKWARD) {
+      const double dt = h.cfg.c.delta_t;
+      const double dt0 = h.timeIndex <= 1 ? GREAT : dt;
+      D.coefft = 1 + dt / (dt + dt0);
+      D.coefft00 = dt * dt / (dt0 * (dt + dt0));
+      D.coefft0 = D.coefft + D.coefft00;
+    }
+  }
+  D.serRatio = serRatio;
+  D.applySer = applySer ? 1 : 0;
+  D.coMin = h.cfg.c.pseudo_co_num_min;
+  D.coMax = h.cfg.c.pseudo_co_num_max;
+  const int FB = h.m.F + h.m.B;
+  k_cellres<<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, D, h.fflux, FB, h.flam, h.W, h.W0, h.W00, h.prim,
+                                                         h.clin, h.pseudoCo, h.rPDT, h.ddtCoeff, h.src, h.scratch);
+  ICS_CUDA(cudaGetLastError());
+}
+
+}  // namespace ics

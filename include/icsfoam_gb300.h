@@ -1,0 +1,226 @@
+/*
+ * icsfoam_gb300.h - C ABI of the GB300 implicit coupled pseudo-time solver.
+ *
+ * One handle owns one finite-volume case resident on the current CUDA
+ * device: mesh addressing and geometry are uploaded once by ics_create(),
+ * the conservative state, boundary values, Jacobian and Krylov workspace
+ * stay in device memory for the life of the handle.  Host arrays passed in
+ * are only read during the call; nothing keeps a pointer to them.
+ *
+ * Conventions
+ *  - Every function returns an ICS_* status; 0 is success.  A failed call
+ *    leaves a message retrievable with ics_last_error().  Nothing aborts the
+ *    process (the reference raises FatalError instead).
+ *  - Cell 5-vectors are stored cell-major [n_cells][5] in the order
+ *    (rho, rhoUx, rhoUy, rhoUz, rhoE).  5x5 blocks are row-major with the
+ *    same order: block[i][j] = d(equation i)/d(variable j).
+ *  - Face arrays list the internal faces first, then the non-empty
+ *    boundary faces in patch order, exactly like an OpenFOAM surface field.
+ *  - A handle is not thread-safe; several handles may coexist.
+ *
+ * The oracle library (test infrastructure) exports the same functions with
+ * the prefix "icsref_" and the same structs, so one test harness drives both.
+ */
+#ifndef ICSFOAM_GB300_H
+#define ICSFOAM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define ICS_OK             0
+#define ICS_ERR_ARG        1  /* invalid argument / size                       */
+#define ICS_ERR_CUDA       2  /* CUDA runtime error                            */
+#define ICS_ERR_NONFINITE  3  /* NaN/Inf in residual or state                  */
+#define ICS_ERR_BREAKDOWN  4  /* zero Krylov norm at the start of a cycle      */
+#define ICS_ERR_DIAG       5  /* all-zero diagonal for LU-SGS (lusgs.C:117-121) */
+#define ICS_ERR_SCHEME     6  /* unknown scheme/solver name                    */
+#define ICS_ERR_STATE      7  /* call made in the wrong order                  */
+#define ICS_ERR_NOMEM      8  /* device allocation failed                      */
+#define ICS_ERR_TIMEOUT    9  /* bounded device wait gave up                   */
+
+/* ---- selectors (runtime-selection table keys of the reference) ------------ */
+/* fvSchemes/convectiveFluxScheme/fluxScheme (newConvectiveFluxScheme.C:50)     */
+enum { ICS_FLUX_AUSMPLUSUP = 0, ICS_FLUX_HLLC = 1, ICS_FLUX_ROE = 2 };
+/* fvSchemes/interpolationSchemes reconstruct(rho|U|T) (convectiveFluxScheme.C:387-400) */
+enum {
+  ICS_RECON_UPWIND = 0,              /* first order                                 */
+  ICS_RECON_VANLEER = 1,             /* TVD limitedScheme, Gauss linear gradient    */
+  ICS_RECON_MINMOD = 2,              /* TVD limitedScheme, Gauss linear gradient    */
+  ICS_RECON_MUSCL_VENKATAKRISHNAN = 3, /* linearUpwind + cellLimited<Venkatakrishnan> */
+  ICS_RECON_MUSCL_MINMOD = 4         /* linearUpwind + cellLimited<minmod>          */
+};
+/* ddtSchemes default dualTime rPseudoDeltaT <scheme> (dualTimeDdtScheme.H:109-118) */
+enum { ICS_DDT_STEADY = 0, ICS_DDT_EULER = 1, ICS_DDT_BACKWARD = 2 };
+/* flowSolver/solver (coupledMatrixSolver.C:41-67)                               */
+enum { ICS_SOLVER_GMRES = 0 };
+/* flowSolver/<solver>/preconditioner (coupledMatrix.H:296-369)                  */
+enum { ICS_PC_NONE = 0, ICS_PC_LUSGS = 1, ICS_PC_JACOBI = 2 };
+/* precision of the linear solve: FP64 everywhere, or FP32 Jacobian blocks,
+ * preconditioner and Krylov basis under an FP64 residual/update            */
+enum { ICS_PREC_FP64 = 0, ICS_PREC_MIXED = 1 };
+
+/* boundary patch kinds */
+enum {
+  ICS_PATCH_EMPTY = 0,
+  ICS_PATCH_ZERO_GRADIENT = 1,   /* U, p, T zeroGradient                             */
+  ICS_PATCH_SLIP = 2,            /* U slip, p, T zeroGradient                        */
+  ICS_PATCH_FIXED = 3,           /* U, p, T fixedValue                               */
+  ICS_PATCH_PRESSURE_OUTLET = 4, /* p fixedValue, U, T zeroGradient                  */
+  ICS_PATCH_TOTAL_INLET = 5,     /* totalPressure, totalTemperature,
+                                    pressureInletOutletVelocity                      */
+  ICS_PATCH_ISOTHERMAL_WALL = 6  /* U = 0, T fixed, p zeroGradient                   */
+};
+
+typedef struct {
+  int32_t kind;     /* ICS_PATCH_*                                         */
+  int32_t is_wall;  /* OpenFOAM "wall" patch type (setCoAndDeltaT.H:88-90) */
+  double p, T;      /* fixed static pressure / temperature                 */
+  double U[3];      /* fixed velocity                                      */
+  double p0, T0;    /* total pressure / temperature (ICS_PATCH_TOTAL_INLET) */
+} ics_patch_desc;
+
+/* Mesh in OpenFOAM LDU convention (owner < neighbour, upper-triangular
+ * internal faces).  Vectors are [n][3].  Empty patches are not listed.     */
+typedef struct {
+  int32_t n_cells, n_faces, n_bfaces, n_patches;
+  const int32_t* owner;
+  const int32_t* neighbour;
+  const double* Sf;                   /* [n_faces][3] area vectors          */
+  const double* Cf;                   /* [n_faces][3] face centres          */
+  const double* weights;              /* [n_faces] linear weights           */
+  const double* delta_coeffs;         /* [n_faces]                          */
+  const double* nonorth_delta_coeffs; /* [n_faces]                          */
+  const double* C;                    /* [n_cells][3] cell centres          */
+  const double* V;                    /* [n_cells] volumes                  */
+  const int32_t* b_cell;              /* [n_bfaces] adjacent cell           */
+  const int32_t* b_patch;             /* [n_bfaces] patch index             */
+  const double* b_Sf;                 /* [n_bfaces][3]                      */
+  const double* b_Cf;                 /* [n_bfaces][3]                      */
+  const double* b_delta_coeffs;       /* [n_bfaces]                         */
+  const ics_patch_desc* patches;      /* [n_patches]                        */
+  int32_t solution_d[3];              /* +1 solved, -1 empty direction      */
+} ics_mesh_desc;
+
+/* Dictionary entries of fvSchemes / fvSolution / thermophysicalProperties
+ * the hot path reads.  Defaults are those of the reference (ics_default_config). */
+typedef struct {
+  /* thermo: perfectGas, hConst, sensibleInternalEnergy with Tref = 0      */
+  double R, Cp;
+  /* transport: const (mu) or sutherland (As, Ts); Prandtl number         */
+  double mu, Pr, As, Ts;
+  int32_t sutherland;
+  int32_t viscous;                 /* add viscous residual and Jacobian   */
+  /* convectiveFluxScheme                                                  */
+  int32_t flux_scheme;             /* ICS_FLUX_*                          */
+  int32_t low_mach_ausm;           /* lowMachAusm (ausmPlusUpFluxScheme.C:61)      */
+  double entropy_fix_coeff;        /* entropyFixCoeff (roeFluxScheme.C:255)        */
+  int32_t recon_rho, recon_U, recon_T; /* ICS_RECON_* per reconstruct() group      */
+  /* ddtSchemes                                                            */
+  int32_t ddt_scheme;              /* ICS_DDT_*                           */
+  double delta_t;                  /* physical time step                  */
+  /* flowSolver                                                            */
+  int32_t solver, preconditioner, n_directions, max_iter, min_iter;
+  double tolerance, rel_tol;
+  int32_t precision;               /* ICS_PREC_*                          */
+  /* pseudoTime                                                            */
+  int32_t n_pseudo_corr, n_pseudo_corr_min;
+  double pseudo_tol, pseudo_tol_rel;
+  double pseudo_co_num, pseudo_co_num_min, pseudo_co_num_max;
+  double pseudo_co_max_increase, pseudo_co_min_decrease;
+  int32_t local_timestepping, local_timestepping_bounding;
+  double local_timestepping_lower_bound;
+  int32_t reset_pseudo;
+  double rho_min, T_min, T_max;
+} ics_config;
+
+/* residualsIO (residualsIO.H:54-315): L1 residuals normalised per equation. */
+typedef struct {
+  double init_res[5];   /* rho, rhoUx, rhoUy, rhoUz, rhoE */
+  double final_res[5];
+  int32_t n_iterations; /* restart cycles */
+  int32_t converged;
+} ics_solver_perf;
+
+typedef struct {
+  ics_solver_perf perf;
+  double rho_l2_residual;   /* sqrt(sum((div(phi)*V)^2)), dbnsFoam.C:136-138 */
+  double pseudo_co_mean;
+  int32_t bounded_cells;    /* cells touched by T/rho bounding           */
+  int32_t status;
+} ics_iter_stats;
+
+typedef struct ics_handle_s* ics_handle;
+
+/* ---- lifecycle ----------------------------------------------------------- */
+/* Defaults of the reference dictionaries (pseudotimeControl.C:49-57,
+ * beginTimeStep.H:15-44, initialise.H:39-70, coupledMatrixSolver.C:81-84). */
+void ics_default_config(ics_config* cfg);
+/* Replaces: fvMesh construction + createFields.H:160-190 (flux scheme and
+ * solver objects).  Uploads addressing and geometry once.                   */
+int ics_create(const ics_mesh_desc* mesh, const ics_config* cfg, ics_handle* out);
+int ics_destroy(ics_handle h);
+int ics_set_config(ics_handle h, const ics_config* cfg);
+int ics_last_error(ics_handle h, char* buf, int32_t len);
+
+/* ---- state --------------------------------------------------------------- */
+/* Initial fields from primitive variables (0/p, 0/U, 0/T); boundary values
+ * are evaluated from the patch kinds.  U is [n_cells][3].                   */
+int ics_set_primitive(ics_handle h, const double* p, const double* U, const double* T);
+/* Overwrite boundary values (p, U[3], T) and the boundary mass flux used by
+ * inlet/outlet switching, all [n_bfaces] / [n_bfaces][3].                   */
+int ics_set_boundary_state(ics_handle h, const double* p_b, const double* U_b,
+                           const double* T_b, const double* phi_b);
+int ics_get_boundary_state(ics_handle h, double* p_b, double* U_b, double* T_b, double* phi_b);
+/* Any output may be NULL.  W is [n_cells][5].                               */
+int ics_get_state(ics_handle h, double* W, double* p, double* U, double* T);
+/* Overwrite the conservative state (also the old time levels when
+ * set_old != 0) and re-derive primitives without touching boundary values. */
+int ics_set_conservative(ics_handle h, const double* W, int32_t set_old);
+/* Per-cell pseudo Courant number field (createFields.H:212-235).           */
+int ics_set_pseudo_co(ics_handle h, const double* co);
+int ics_get_pseudo_co(ics_handle h, double* co, double* rPseudoDeltaT);
+
+/* ---- the hot path, one reference virtual per entry point ---------------- */
+/* convectiveFluxScheme::calcFlux(phi, phiUp, phiEp)
+ * (convectiveFluxScheme.H:219-224; ausmPlusUpFluxScheme.C:73-299,
+ *  hllcFluxScheme.C:70-240, roeFluxScheme.C:276-409).  Outputs are
+ * [n_faces+n_bfaces] (phiU: [..][3]); any may be NULL.                      */
+int ics_calc_flux(ics_handle h, double* phi, double* phiU, double* phiE);
+/* residualsUpdate.H:1-83 then setCoAndDeltaT.H:1-173: matrix source
+ * R*V ([n_cells][5]) and the new local rPseudoDeltaT.  Calls calc_flux.     */
+int ics_residual(ics_handle h, double* source);
+/* convectiveFluxScheme::createConvectiveJacobian(coupledMatrix&, ddtCoeff)
+ * (convectiveFluxScheme.C:537-546) + viscousFluxScheme::createViscousJacobian
+ * (viscousFluxScheme.C:265-273).  Uses the state of the last ics_residual.  */
+int ics_assemble_jacobian(ics_handle h);
+/* Export the assembled blocks in LDU form: diag [n_cells][25],
+ * lower/upper [n_faces][25] (blockFvMatrix.H:68-222 storage).               */
+int ics_get_jacobian(ics_handle h, double* diag, double* lower, double* upper);
+/* coupledMatrix::matrixMul (coupledMatrix.C:66-123): y = A x, [n_cells][5]. */
+int ics_matrix_mul(ics_handle h, const double* x, double* y);
+/* coupledMatrix::preconditioner::precondition (lusgs.C:220-385,
+ * Jacobi.C:55-135): r <- P^-1 r in place.                                    */
+int ics_precondition(ics_handle h, double* r);
+/* coupledMatrix::solveForIncr -> solver::solveDelta (coupledMatrix.C:297-385,
+ * gmres.C:772-1107).  Solves for the increment of the last assembly; dW
+ * ([n_cells][5]) may be NULL.                                               */
+int ics_solve_increment(ics_handle h, ics_solver_perf* perf, double* dW);
+/* updateFields.H:1-105 (+ boundLocalTimeStep.H:1-97) with the increment of
+ * the last solve.                                                            */
+int ics_update_fields(ics_handle h, ics_iter_stats* stats);
+/* One pseudo-time iteration: outerLoop.H:1-99 then updateFields.H.          */
+int ics_pseudo_iteration(ics_handle h, ics_iter_stats* stats);
+/* Start a physical time step: shift old time levels, beginTimeStep.H:1-45.  */
+int ics_begin_time_step(ics_handle h);
+/* pseudotimeControl::loop() (pseudotimeControl.C:159-241): returns 1 in
+ * *more while the pseudo loop should run another iteration.                 */
+int ics_pseudo_loop(ics_handle h, int32_t* more);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ICSFOAM_GB300_H */

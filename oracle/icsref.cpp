@@ -1,0 +1,1830 @@
+// icsref - CPU FP64 oracle for the implicit coupled pseudo-time iteration.
+//
+// TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
+// cpu_baseline / reference arm of bench.py may load this library, and only as
+// the checker or the timed CPU baseline - never as part of the product path.
+//
+// A sequential restatement, written field-by-field in the style of the
+// reference, of ICSFoam's dbnsFoam pseudo-time iteration:
+//   fluxes          ausmPlusUpFluxScheme.C:73-299, hllcFluxScheme.C:70-240,
+//                   roeFluxScheme.C:41-409, cellFaceFunctions.H:491-661
+//   residual        applications/solvers/dbnsFoam/residualsUpdate.H:1-83
+//   local dtau, SER setCoAndDeltaT.H:1-173
+//   Jacobian        convectiveFluxScheme.C:47-546, blockFvMatrix.C:211-326
+//   linear algebra  blockFvMatrix.C:329-601, coupledMatrix.C:66-385,
+//                   coupledMatrixSolver.C:99-221, gmres.C:44-1107,
+//                   lusgs.C:50-385, Jacobi.C:55-135, JacobiSmoother.C:42-205
+//   update          boundLocalTimeStep.H:1-97, updateFields.H:1-105
+//   control         pseudotimeControl.C:42-241, pseudotimeControlI.H:42-69
+//   dual time       dualTimeDdtScheme.C:111-185
+// The OpenFOAM v2112 pieces these call (limitedScheme/linearUpwind
+// interpolation, Gauss gradients, cellLimited gradient limiting, Euler and
+// backward ddt, boundary conditions, perfect-gas thermo, LUscalarMatrix) are
+// restated from their documented mathematics; OpenFOAM itself is absent.
+//
+// Parity against the reference binary is unpinned: the reference has no
+// tests or golden data and cannot be built without OpenFOAM.  The oracle is
+// pinned instead by analytic known-answer tests (tests/test_oracle_*.py).
+//
+// Built with -ffp-contract=off so x86 and Arm produce identical bits.
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+#include "../include/icsfoam_gb300.h"
+
+namespace {
+
+constexpr double SMALL = 1e-15;
+constexpr double VSMALL = 1e-300;
+constexpr double ROOTVSMALL = 1e-150;
+constexpr double GREAT = 1e15;
+constexpr double VGREAT = 1e300;
+
+struct V3 {
+  double x = 0, y = 0, z = 0;
+  V3() = default;
+  V3(double a, double b, double c) : x(a), y(b), z(c) {}
+  double& operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
+  double operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+};
+inline V3 operator+(const V3& a, const V3& b) { return V3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline V3 operator-(const V3& a, const V3& b) { return V3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline V3 operator*(double s, const V3& a) { return V3(s * a.x, s * a.y, s * a.z); }
+inline V3 operator*(const V3& a, double s) { return V3(a.x * s, a.y * s, a.z * s); }
+inline V3 operator/(const V3& a, double s) { return V3(a.x / s, a.y / s, a.z / s); }
+inline double dot(const V3& a, const V3& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline double magSqr(const V3& a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
+inline double mag(const V3& a) { return std::sqrt(magSqr(a)); }
+inline double pos0(double s) { return s >= 0 ? 1.0 : 0.0; }
+inline double neg(double s) { return s < 0 ? 1.0 : 0.0; }
+inline double sgn(double s) { return s >= 0 ? 1.0 : -1.0; }
+inline double sqr(double s) { return s * s; }
+
+// 3x3 tensor, row-major T[i][j]
+struct T33 {
+  double a[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+};
+inline T33 outer(const V3& u, const V3& v) {
+  T33 t;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) t.a[i][j] = u[i] * v[j];
+  return t;
+}
+
+// 5x5 block in variable order (rho, rhoUx, rhoUy, rhoUz, rhoE)
+struct B5 {
+  double a[25];
+  B5() { std::memset(a, 0, sizeof(a)); }
+  double& operator()(int i, int j) { return a[i * 5 + j]; }
+  double operator()(int i, int j) const { return a[i * 5 + j]; }
+};
+
+struct Patch {
+  int kind, is_wall;
+  double p, T, U[3], p0, T0;
+};
+
+struct Case {
+  // mesh
+  int N = 0, F = 0, B = 0;
+  std::vector<int> own, nei, bcell, bpatch;
+  std::vector<V3> Sf, Cf, C, bSf, bCf;
+  std::vector<double> magSf, bmagSf, w, dc, nodc, V, bdc;
+  std::vector<Patch> patches;
+  int solD[3] = {1, 1, 1};
+  std::vector<std::vector<int>> cellFaces;  // OpenFOAM cells(): owner faces then neighbour faces
+  ics_config cfg{};
+  double Cv = 0, gamma = 0;
+
+  // state (internal)
+  std::vector<double> rho, rhoE, p, T, e;
+  std::vector<V3> rhoU, U;
+  // boundary values
+  std::vector<double> pB, TB, phiB;
+  std::vector<V3> UB;
+  // old time levels
+  std::vector<double> rho0, rhoE0, rho00, rhoE00;
+  std::vector<V3> rhoU0, rhoU00;
+  int timeIndex = 0;  // number of begun physical time steps
+  // pseudo time
+  std::vector<double> pseudoCo, rPseudoDeltaT, ddtCoeff;
+  // fluxes of the last calcFlux (F+B)
+  std::vector<double> phi, phiE;
+  std::vector<V3> phiU;
+  double lastRhoL2 = 0;
+  // matrix: LDU of 5x5 blocks + source
+  std::vector<B5> diag, lower, upper;
+  std::vector<double> src;  // N*5
+  bool haveMatrix = false;
+  // previous-iteration state and increment
+  std::vector<double> Wprev, dW;  // N*5
+  bool haveIncrement = false;
+  // residual bookkeeping (setCoAndDeltaT.H, pseudotimeControl)
+  bool initResValid = false, prevResValid = false;
+  ics_solver_perf initRes{}, prevRes{};
+  // pseudotimeControl state
+  int corr = 0;
+  bool converged_ = false, firstIteration_ = true;
+  ics_solver_perf residuals_{}, initResiduals_{};
+  std::string err;
+};
+
+// ---------------------------------------------------------------------------
+// Thermo: perfectGas + hConst + sensibleInternalEnergy, Tref = 0
+// ---------------------------------------------------------------------------
+inline double psiOf(const Case& c, double T) { return 1.0 / (c.cfg.R * T); }
+inline double heOf(const Case& c, double T) { return c.Cv * T; }
+
+// ---------------------------------------------------------------------------
+// Field helpers: a vol field = internal values + boundary-face values
+// ---------------------------------------------------------------------------
+struct VolS {
+  std::vector<double> in, bf;
+};
+
+// Gauss linear gradient (OpenFOAM gaussGrad with linear interpolation)
+void gaussGrad(const Case& c, const VolS& f, std::vector<V3>& g) {
+  g.assign(c.N, V3());
+  for (int fi = 0; fi < c.F; ++fi) {
+    const int o = c.own[fi], n = c.nei[fi];
+    const double sf = c.w[fi] * (f.in[o] - f.in[n]) + f.in[n];
+    const V3 Ssf = c.Sf[fi] * sf;
+    g[o] = g[o] + Ssf;
+    g[n] = g[n] - Ssf;
+  }
+  for (int b = 0; b < c.B; ++b) {
+    const int o = c.bcell[b];
+    g[o] = g[o] + c.bSf[b] * f.bf[b];
+  }
+  for (int i = 0; i < c.N; ++i) g[i] = g[i] / c.V[i];
+}
+
+// cellLimited<limiter> Gauss linear 1 (cellLimitedGrad): minmod or Venkatakrishnan
+void cellLimitedGrad(const Case& c, const VolS& f, bool venkat, std::vector<V3>& g) {
+  gaussGrad(c, f, g);
+  std::vector<double> maxV(f.in), minV(f.in);
+  for (int fi = 0; fi < c.F; ++fi) {
+    const int o = c.own[fi], n = c.nei[fi];
+    maxV[o] = std::max(maxV[o], f.in[n]);
+    minV[o] = std::min(minV[o], f.in[n]);
+    maxV[n] = std::max(maxV[n], f.in[o]);
+    minV[n] = std::min(minV[n], f.in[o]);
+  }
+  for (int b = 0; b < c.B; ++b) {
+    const int o = c.bcell[b];
+    maxV[o] = std::max(maxV[o], f.bf[b]);
+    minV[o] = std::min(minV[o], f.bf[b]);
+  }
+  for (int i = 0; i < c.N; ++i) {
+    maxV[i] -= f.in[i];
+    minV[i] -= f.in[i];
+  }
+  std::vector<double> lim(c.N, 1.0);
+  auto limitFace = [&](double& l, double maxD, double minD, double extrap) {
+    double r = 1;
+    if (extrap > SMALL)
+      r = maxD / extrap;
+    else if (extrap < -SMALL)
+      r = minD / extrap;
+    double lr = venkat ? (sqr(r) + 2 * r) / (sqr(r) + r + 2) : std::min(r, 1.0);
+    l = std::min(l, lr);
+  };
+  for (int fi = 0; fi < c.F; ++fi) {
+    const int o = c.own[fi], n = c.nei[fi];
+    limitFace(lim[o], maxV[o], minV[o], dot(c.Cf[fi] - c.C[o], g[o]));
+    limitFace(lim[n], maxV[n], minV[n], dot(c.Cf[fi] - c.C[n], g[n]));
+  }
+  for (int b = 0; b < c.B; ++b) {
+    const int o = c.bcell[b];
+    limitFace(lim[o], maxV[o], minV[o], dot(c.bCf[b] - c.C[o], g[o]));
+  }
+  for (int i = 0; i < c.N; ++i) g[i] = g[i] * lim[i];
+}
+
+// linear interpolation (internal + boundary values)
+void interpLinear(const Case& c, const VolS& f, std::vector<double>& out) {
+  out.resize(c.F + c.B);
+  for (int fi = 0; fi < c.F; ++fi) {
+    const int o = c.own[fi], n = c.nei[fi];
+    out[fi] = c.w[fi] * (f.in[o] - f.in[n]) + f.in[n];
+  }
+  for (int b = 0; b < c.B; ++b) out[c.F + b] = f.bf[b];
+}
+
+// fvc::interpolate(vf, dir, "reconstruct(..)") for the configured scheme.
+void reconstruct(const Case& c, const VolS& f, double dir, int scheme, std::vector<double>& out) {
+  out.resize(c.F + c.B);
+  const double wUp = pos0(dir);
+  if (scheme == ICS_RECON_UPWIND) {
+    for (int fi = 0; fi < c.F; ++fi) {
+      const int o = c.own[fi], n = c.nei[fi];
+      out[fi] = wUp * (f.in[o] - f.in[n]) + f.in[n];
+    }
+  } else if (scheme == ICS_RECON_VANLEER || scheme == ICS_RECON_MINMOD) {
+    std::vector<V3> g;
+    gaussGrad(c, f, g);
+    for (int fi = 0; fi < c.F; ++fi) {
+      const int o = c.own[fi], n = c.nei[fi];
+      const double phiP = f.in[o], phiN = f.in[n];
+      const V3 d = c.C[n] - c.C[o];
+      const double gradf = phiN - phiP;
+      const double gradcf = dir > 0 ? dot(d, g[o]) : dot(d, g[n]);
+      double r;
+      if (std::fabs(gradcf) >= 1000 * std::fabs(gradf))
+        r = 2 * 1000 * sgn(gradcf) * sgn(gradf) - 1;
+      else
+        r = 2 * (gradcf / gradf) - 1;
+      double lim;
+      if (scheme == ICS_RECON_VANLEER)
+        lim = (r + std::fabs(r)) / (1 + std::fabs(r));
+      else
+        lim = std::max(std::min(std::min(r, 1.0), 2.0), 0.0);
+      const double wgt = lim * c.w[fi] + (1.0 - lim) * wUp;
+      out[fi] = wgt * (phiP - phiN) + phiN;
+    }
+  } else {  // MUSCL: linearUpwind + cellLimited gradient
+    std::vector<V3> g;
+    cellLimitedGrad(c, f, scheme == ICS_RECON_MUSCL_VENKATAKRISHNAN, g);
+    for (int fi = 0; fi < c.F; ++fi) {
+      const int o = c.own[fi], n = c.nei[fi];
+      const int up = dir > 0 ? o : n;
+      const double base = wUp * (f.in[o] - f.in[n]) + f.in[n];
+      out[fi] = base + dot(c.Cf[fi] - c.C[up], g[up]);
+    }
+  }
+  for (int b = 0; b < c.B; ++b) out[c.F + b] = f.bf[b];
+}
+
+// component fields of U (internal + boundary)
+VolS Ucmpt(const Case& c, int k) {
+  VolS f;
+  f.in.resize(c.N);
+  f.bf.resize(c.B);
+  for (int i = 0; i < c.N; ++i) f.in[i] = c.U[i][k];
+  for (int b = 0; b < c.B; ++b) f.bf[b] = c.UB[b][k];
+  return f;
+}
+
+void reconstructU(const Case& c, double dir, std::vector<V3>& out) {
+  out.assign(c.F + c.B, V3());
+  std::vector<double> tmp;
+  for (int k = 0; k < 3; ++k) {
+    reconstruct(c, Ucmpt(c, k), dir, c.cfg.recon_U, tmp);
+    for (int fi = 0; fi < c.F + c.B; ++fi) out[fi][k] = tmp[fi];
+  }
+}
+
+inline const V3& SfOf(const Case& c, int fi) { return fi < c.F ? c.Sf[fi] : c.bSf[fi - c.F]; }
+inline double magSfOf(const Case& c, int fi) { return fi < c.F ? c.magSf[fi] : c.bmagSf[fi - c.F]; }
+
+// E = he(p,T) + 0.5|U|^2 and boundary values
+VolS fieldE(const Case& c) {
+  VolS E;
+  E.in.resize(c.N);
+  E.bf.resize(c.B);
+  for (int i = 0; i < c.N; ++i) E.in[i] = heOf(c, c.T[i]) + 0.5 * magSqr(c.U[i]);
+  for (int b = 0; b < c.B; ++b) E.bf[b] = heOf(c, c.TB[b]) + 0.5 * magSqr(c.UB[b]);
+  return E;
+}
+double rhoBof(const Case& c, int b) { return psiOf(c, c.TB[b]) * c.pB[b]; }
+
+VolS fieldH(const Case& c, const VolS& E) {
+  VolS H;
+  H.in.resize(c.N);
+  H.bf.resize(c.B);
+  for (int i = 0; i < c.N; ++i) H.in[i] = std::max(E.in[i], SMALL) + std::max(c.p[i] / c.rho[i], SMALL);
+  for (int b = 0; b < c.B; ++b) H.bf[b] = std::max(E.bf[b], SMALL) + std::max(c.pB[b] / rhoBof(c, b), SMALL);
+  return H;
+}
+VolS fieldRho(const Case& c) {
+  VolS r;
+  r.in = c.rho;
+  r.bf.resize(c.B);
+  for (int b = 0; b < c.B; ++b) r.bf[b] = rhoBof(c, b);
+  return r;
+}
+VolS fieldP(const Case& c) {
+  VolS r;
+  r.in = c.p;
+  r.bf = c.pB;
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// Flux schemes
+// ---------------------------------------------------------------------------
+void calcFluxAUSM(Case& c) {
+  const int NF = c.F + c.B;
+  std::vector<V3> U_L, U_R;
+  reconstructU(c, +1, U_L);
+  reconstructU(c, -1, U_R);
+  std::vector<double> un_L(NF), un_R(NF);
+  for (int fi = 0; fi < NF; ++fi) {
+    un_L[fi] = dot(U_L[fi], SfOf(c, fi)) / magSfOf(c, fi);
+    un_R[fi] = dot(U_R[fi], SfOf(c, fi)) / magSfOf(c, fi);
+    un_L[fi] -= 0.0;  // MRF face velocity (zero without MRF zones)
+    un_R[fi] -= 0.0;
+  }
+  VolS E = fieldE(c);
+  VolS H = fieldH(c, E);
+  VolS cs;
+  cs.in.resize(c.N);
+  cs.bf.resize(c.B);
+  const double g = c.gamma;
+  for (int i = 0; i < c.N; ++i) cs.in[i] = std::sqrt(2.0 * (g - 1.0) / (g + 1.0) * H.in[i]);
+  for (int b = 0; b < c.B; ++b) cs.bf[b] = std::sqrt(2.0 * (g - 1.0) / (g + 1.0) * H.bf[b]);
+  std::vector<double> c_L, c_R;
+  reconstruct(c, cs, +1, c.cfg.recon_T, c_L);
+  reconstruct(c, cs, -1, c.cfg.recon_T, c_R);
+  std::vector<double> c_face(NF);
+  for (int fi = 0; fi < NF; ++fi) {
+    const double cl = sqr(c_L[fi]) / std::max(c_L[fi], un_L[fi]);
+    const double cr = sqr(c_R[fi]) / std::max(c_R[fi], -un_R[fi]);
+    c_face[fi] = std::min(cl, cr);
+  }
+  std::vector<double> p_L, p_R, rho_L, rho_R, H_L, H_R;
+  VolS P = fieldP(c), RHO = fieldRho(c);
+  reconstruct(c, P, +1, c.cfg.recon_rho, p_L);
+  reconstruct(c, P, -1, c.cfg.recon_rho, p_R);
+  reconstruct(c, RHO, +1, c.cfg.recon_rho, rho_L);
+  reconstruct(c, RHO, -1, c.cfg.recon_rho, rho_R);
+  reconstruct(c, H, +1, c.cfg.recon_T, H_L);
+  reconstruct(c, H, -1, c.cfg.recon_T, H_R);
+  for (int fi = 0; fi < NF; ++fi) {
+    const double cf = c_face[fi];
+    const double ML = un_L[fi] / cf;
+    double Mplus, pplus;
+    if (std::fabs(ML) < 1.0) {
+      const double ML2p = 0.25 * sqr(ML + 1);
+      const double ML2m = -0.25 * sqr(ML - 1);
+      Mplus = ML2p * (1 - 2 * ML2m);
+      pplus = ML2p * (2 - ML - 3 * ML * ML2m);
+    } else {
+      Mplus = std::max(ML, 0.0);
+      pplus = ML > 0 ? 1.0 : 0.0;
+    }
+    const double MR = un_R[fi] / cf;
+    double Mminus, pminus;
+    if (std::fabs(MR) < 1.0) {
+      const double MR2m = -0.25 * sqr(MR - 1);
+      const double MR2p = 0.25 * sqr(MR + 1);
+      Mminus = MR2m * (1 + 2 * MR2p);
+      pminus = MR2m * (-2 - MR + 3 * MR * MR2p);
+    } else {
+      Mminus = std::min(MR, 0.0);
+      pminus = MR < 0 ? 1.0 : 0.0;
+    }
+    double M12 = Mplus + Mminus;
+    double p12 = pplus * p_L[fi] + pminus * p_R[fi];
+    const double Mmean = 0.5 * (sqr(un_L[fi]) + sqr(un_R[fi])) / sqr(cf);
+    const double MDiff =
+        -0.25 * std::max((1.0 - Mmean), 0.0) * (p_R[fi] - p_L[fi]) / (0.5 * (rho_L[fi] + rho_R[fi]) * sqr(cf));
+    if ((M12 > 0.0 && M12 + MDiff <= 0.0) || (M12 < 0.0 && M12 + MDiff >= 0.0))
+      M12 += 0.2 * MDiff;
+    else
+      M12 += MDiff;
+    if (c.cfg.low_mach_ausm) {
+      const double pDiff = -0.25 * pplus * pminus * (rho_L[fi] + rho_R[fi]) * cf * (un_R[fi] - un_L[fi]);
+      p12 += pDiff;
+    }
+    const bool left = M12 >= 0;
+    const V3 Uf = left ? U_L[fi] : U_R[fi];
+    const double rhoa = M12 * cf * (left ? rho_L[fi] : rho_R[fi]);
+    const V3 rhoaU = rhoa * Uf;
+    const double rhoah = rhoa * (left ? H_L[fi] : H_R[fi]);
+    const double ms = magSfOf(c, fi);
+    c.phi[fi] = rhoa * ms;
+    c.phiU[fi] = rhoaU * ms + p12 * SfOf(c, fi);
+    c.phiE[fi] = rhoah * ms + p12 * 0.0 * ms;
+  }
+}
+
+void calcFluxHLLC(Case& c) {
+  const int NF = c.F + c.B;
+  std::vector<double> rho_l, rho_r, p_l, p_r, c_l, c_r, E_l, E_r, H_l, H_r;
+  VolS P = fieldP(c), RHO = fieldRho(c);
+  reconstruct(c, RHO, +1, c.cfg.recon_rho, rho_l);
+  reconstruct(c, RHO, -1, c.cfg.recon_rho, rho_r);
+  reconstruct(c, P, +1, c.cfg.recon_rho, p_l);
+  reconstruct(c, P, -1, c.cfg.recon_rho, p_r);
+  std::vector<V3> U_l, U_r;
+  reconstructU(c, +1, U_l);
+  reconstructU(c, -1, U_r);
+  VolS cs;
+  cs.in.resize(c.N);
+  cs.bf.resize(c.B);
+  for (int i = 0; i < c.N; ++i) cs.in[i] = std::max(std::sqrt(c.gamma / psiOf(c, c.T[i])), VSMALL);
+  for (int b = 0; b < c.B; ++b) cs.bf[b] = std::max(std::sqrt(c.gamma / psiOf(c, c.TB[b])), VSMALL);
+  reconstruct(c, cs, +1, c.cfg.recon_T, c_l);
+  reconstruct(c, cs, -1, c.cfg.recon_T, c_r);
+  VolS E = fieldE(c);
+  reconstruct(c, E, +1, c.cfg.recon_T, E_l);
+  reconstruct(c, E, -1, c.cfg.recon_T, E_r);
+  VolS H = fieldH(c, E);
+  reconstruct(c, H, +1, c.cfg.recon_T, H_l);
+  reconstruct(c, H, -1, c.cfg.recon_T, H_r);
+  const double gInterp = c.gamma;  // linear interpolation of a uniform gamma
+  for (int fi = 0; fi < NF; ++fi) {
+    const double ms = magSfOf(c, fi);
+    const V3 n = SfOf(c, fi) / ms;
+    const double coefR = std::sqrt(std::max(VSMALL, rho_r[fi]) / std::max(VSMALL, rho_l[fi]));
+    const V3 uAvg = (coefR * U_r[fi] + U_l[fi]) / (coefR + 1.0);
+    const double HAvg = (coefR * H_r[fi] + H_l[fi]) / (coefR + 1.0);
+    const double cAvg = std::sqrt(std::fabs((gInterp - 1.0) * (HAvg - 0.5 * magSqr(uAvg))));
+    const double uMag_l = dot(U_l[fi], n) - 0.0;
+    const double uMag_r = dot(U_r[fi], n) - 0.0;
+    const double uMagAvg = dot(uAvg, n) - 0.0;
+    const double Sl = std::min(uMag_l - c_l[fi], uMagAvg - cAvg);
+    const double Sr = std::max(uMag_r + c_r[fi], uMagAvg + cAvg);
+    const double rl = rho_l[fi], rr = rho_r[fi], pl = p_l[fi], pr = p_r[fi];
+    const double Sm = (rr * uMag_r * (Sr - uMag_r) - rl * uMag_l * (Sl - uMag_l) + pl - pr) /
+                      (rr * (Sr - uMag_r) - rl * (Sl - uMag_l));
+    const double coefSl = pos0(Sl);
+    const double coefSr = neg(Sr);
+    const double coefSm = pos0(Sm);
+    const double coefSlm = (1.0 - coefSl) * coefSm;
+    const double coefSmr = (1.0 - coefSm) * (1.0 - coefSr);
+    const double fluxRhoStar_l = Sm / (Sl - Sm) * ((Sl - uMag_l) * rl);
+    const double fluxRhoStar_r = Sm / (Sr - Sm) * ((Sr - uMag_r) * rr);
+    c.phi[fi] = (coefSl * rl * uMag_l + coefSlm * fluxRhoStar_l + coefSmr * fluxRhoStar_r + coefSr * rr * uMag_r) * ms;
+    const double pStar_l = rl * (uMag_l - Sl) * (uMag_l - Sm) + pl;
+    const double pStar_r = rr * (uMag_r - Sr) * (uMag_r - Sm) + pr;
+    const V3 rhoUStar_l = 1.0 / (Sl - Sm) * ((Sl - uMag_l) * rl * U_l[fi] + (pStar_l - pl) * n);
+    const V3 rhoUStar_r = 1.0 / (Sr - Sm) * ((Sr - uMag_r) * rr * U_r[fi] + (pStar_r - pr) * n);
+    const V3 fluxRhoUStar_l = Sm * rhoUStar_l + pStar_l * n;
+    const V3 fluxRhoUStar_r = Sm * rhoUStar_r + pStar_r * n;
+    c.phiU[fi] = (coefSl * (rl * uMag_l * U_l[fi] + pl * n) + coefSlm * fluxRhoUStar_l + coefSmr * fluxRhoUStar_r +
+                  coefSr * (rr * uMag_r * U_r[fi] + pr * n)) *
+                 ms;
+    const double rhoEStar_l = 1.0 / (Sl - Sm) * ((Sl - uMag_l) * (rl * E_l[fi]) - pl * uMag_l + pStar_l * Sm);
+    const double rhoEStar_r = 1.0 / (Sr - Sm) * ((Sr - uMag_r) * (rr * E_r[fi]) - pr * uMag_r + pStar_r * Sm);
+    const double fluxRhoEStar_l = Sm * (rhoEStar_l + pStar_l) + pStar_l * 0.0;
+    const double fluxRhoEStar_r = Sm * (rhoEStar_r + pStar_r) + pStar_r * 0.0;
+    c.phiE[fi] = (coefSl * rl * H_l[fi] * uMag_l + coefSlm * fluxRhoEStar_l + coefSmr * fluxRhoEStar_r +
+                  coefSr * rr * H_r[fi] * uMag_r) *
+                 ms;
+  }
+}
+
+void calcFluxRoe(Case& c) {
+  const int NF = c.F + c.B;
+  std::vector<double> rho_l, rho_r, p_l, p_r, E_l, E_r, H_l, H_r;
+  VolS P = fieldP(c), RHO = fieldRho(c);
+  reconstruct(c, RHO, +1, c.cfg.recon_rho, rho_l);
+  reconstruct(c, RHO, -1, c.cfg.recon_rho, rho_r);
+  reconstruct(c, P, +1, c.cfg.recon_rho, p_l);
+  reconstruct(c, P, -1, c.cfg.recon_rho, p_r);
+  std::vector<V3> U_l, U_r;
+  reconstructU(c, +1, U_l);
+  reconstructU(c, -1, U_r);
+  VolS E = fieldE(c);
+  reconstruct(c, E, +1, c.cfg.recon_T, E_l);
+  reconstruct(c, E, -1, c.cfg.recon_T, E_r);
+  VolS H = fieldH(c, E);
+  reconstruct(c, H, +1, c.cfg.recon_T, H_l);
+  reconstruct(c, H, -1, c.cfg.recon_T, H_r);
+  const double gI = c.gamma;
+  const double eps = c.cfg.entropy_fix_coeff;
+  for (int fi = 0; fi < NF; ++fi) {
+    const double ms = magSfOf(c, fi);
+    const V3 n = SfOf(c, fi) / ms;
+    const double coefR = std::sqrt(std::max(VSMALL, rho_r[fi]) / std::max(VSMALL, rho_l[fi]));
+    const double rD = coefR * rho_l[fi];
+    const V3 rU = (coefR * U_r[fi] + U_l[fi]) / (coefR + 1.0);
+    const double rH = (coefR * H_r[fi] + H_l[fi]) / (coefR + 1.0);
+    const double rC = std::sqrt(std::fabs((gI - 1.0) * (rH - 0.5 * magSqr(rU))));
+    const double uMag_l = dot(U_l[fi], n), uMag_r = dot(U_r[fi], n);
+    const double uProj = dot(rU, n) - 0.0;
+    const V3 rhoU_l = rho_l[fi] * U_l[fi], rhoU_r = rho_r[fi] * U_r[fi];
+    const double rhoE_l = rho_l[fi] * E_l[fi], rhoE_r = rho_r[fi] * E_r[fi];
+    // getRoeDissipation: P |Lambda| P^-1 assembled in conservative variables
+    const double a1 = gI - 1;
+    const double theta = 0.5 * a1 * magSqr(rU);
+    const double c2 = sqr(rC);
+    const double a2 = 1 / (rD * rC * std::sqrt(2.0));
+    const double a3 = rD / (rC * std::sqrt(2.0));
+    const double a4 = (theta + c2) / a1;
+    const double a5 = 1 - theta / c2;
+    const double a6 = theta / a1;
+    auto cross = [](const V3& a, const V3& b) {
+      return V3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+    };
+    // inverse P: rows 1 (vector, 3 rows), 2, 3; columns rho | rhoU | rhoE
+    V3 invP11 = (n * a5) - cross(rU, n) / rD;
+    T33 invP12 = outer(a1 / c2 * n, rU);
+    invP12.a[0][1] += n.z / rD;
+    invP12.a[0][2] -= n.y / rD;
+    invP12.a[1][0] -= n.z / rD;
+    invP12.a[1][2] += n.x / rD;
+    invP12.a[2][0] += n.y / rD;
+    invP12.a[2][1] -= n.x / rD;
+    V3 invP13 = -a1 / c2 * n;
+    const double invP21 = a2 * (theta - rC * uProj);
+    const V3 invP22 = -a2 * (a1 * rU - rC * n);
+    const double invP23 = a1 * a2;
+    const double invP31 = a2 * (theta + rC * uProj);
+    const V3 invP32 = -a2 * (a1 * rU + rC * n);
+    const double invP33 = a1 * a2;
+    double L1 = std::fabs(uProj), L2 = std::fabs(uProj + rC), L3 = std::fabs(uProj - rC);
+    const double epsilon = eps * std::max(L2, L3);
+    if (L1 < epsilon) L1 = (sqr(L1) + sqr(epsilon)) / (2.0 * epsilon);
+    if (L2 < epsilon) L2 = (sqr(L2) + sqr(epsilon)) / (2.0 * epsilon);
+    if (L3 < epsilon) L3 = (sqr(L3) + sqr(epsilon)) / (2.0 * epsilon);
+    const V3 P11 = n;
+    const double P12 = a3, P13 = a3;
+    T33 P21 = outer(rU, n);
+    P21.a[0][1] -= n.z * rD;
+    P21.a[0][2] += n.y * rD;
+    P21.a[1][0] += n.z * rD;
+    P21.a[1][2] -= n.x * rD;
+    P21.a[2][0] -= n.y * rD;
+    P21.a[2][1] += n.x * rD;
+    const V3 P22 = a3 * (rU + rC * n);
+    const V3 P23 = a3 * (rU - rC * n);
+    const V3 P31 = n * a6 + rD * cross(rU, n);
+    const double P32 = a3 * (a4 + rC * uProj);
+    const double P33 = a3 * (a4 - rC * uProj);
+    // dissipation blocks
+    const V3 P11L = P11 * L1;
+    const double dCR = dot(P11L, invP11) + (L2 * P12 * invP21) + (L3 * P13 * invP31);
+    V3 dCU;  // (P11*L1) & invP12 : vector & tensor = row vector
+    for (int j = 0; j < 3; ++j) dCU[j] = P11L.x * invP12.a[0][j] + P11L.y * invP12.a[1][j] + P11L.z * invP12.a[2][j];
+    dCU = dCU + (L2 * P12 * invP22) + (L3 * P13 * invP32);
+    const double dCE = dot(P11L, invP13) + (L2 * P12 * invP23) + (L3 * P13 * invP33);
+    // momentum rows: (P21*L1) & invP11 -> tensor & vector
+    T33 P21L;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) P21L.a[i][j] = P21.a[i][j] * L1;
+    V3 dMR, dME;
+    T33 dMU;
+    for (int i = 0; i < 3; ++i) {
+      dMR[i] = P21L.a[i][0] * invP11.x + P21L.a[i][1] * invP11.y + P21L.a[i][2] * invP11.z;
+      dME[i] = P21L.a[i][0] * invP13.x + P21L.a[i][1] * invP13.y + P21L.a[i][2] * invP13.z;
+      for (int j = 0; j < 3; ++j)
+        dMU.a[i][j] = P21L.a[i][0] * invP12.a[0][j] + P21L.a[i][1] * invP12.a[1][j] + P21L.a[i][2] * invP12.a[2][j];
+    }
+    dMR = dMR + (L2 * invP21 * P22) + (L3 * invP31 * P23);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) dMU.a[i][j] += (L2 * P22[i] * invP22[j]) + (L3 * P23[i] * invP32[j]);
+    dME = dME + (L2 * invP23 * P22) + (L3 * invP33 * P23);
+    const V3 P31L = P31 * L1;
+    const double dER = dot(P31L, invP11) + (L2 * P32 * invP21) + (L3 * P33 * invP31);
+    V3 dEU;
+    for (int j = 0; j < 3; ++j) dEU[j] = P31L.x * invP12.a[0][j] + P31L.y * invP12.a[1][j] + P31L.z * invP12.a[2][j];
+    dEU = dEU + (L2 * P32 * invP22) + (L3 * P33 * invP32);
+    const double dEE = dot(P31L, invP13) + (L2 * P32 * invP23) + (L3 * P33 * invP33);
+
+    const double dRho = rho_r[fi] - rho_l[fi];
+    const V3 dRhoU = rhoU_r - rhoU_l;
+    const double dRhoE = rhoE_r - rhoE_l;
+    double ph = -0.5 * ms * (dCR * dRho + dot(dCU, dRhoU) + dCE * dRhoE);
+    V3 tU;
+    for (int i = 0; i < 3; ++i)
+      tU[i] = dMR[i] * dRho + (dMU.a[i][0] * dRhoU.x + dMU.a[i][1] * dRhoU.y + dMU.a[i][2] * dRhoU.z) + dME[i] * dRhoE;
+    V3 pU = -0.5 * ms * tU;
+    double pE = -0.5 * ms * (dER * dRho + dot(dEU, dRhoU) + dEE * dRhoE);
+    const double rn_l = rho_l[fi] * uMag_l, rn_r = rho_r[fi] * uMag_r;
+    ph += 0.5 * ms * (rn_l + rn_r);
+    pU = pU + 0.5 * ms * (rn_l * U_l[fi] + rn_r * U_r[fi] + n * (p_l[fi] + p_r[fi]));
+    pE += 0.5 * ms * (rn_l * H_l[fi] + rn_r * H_r[fi]);
+    ph -= 0.5 * ms * 0.0 * (rho_l[fi] + rho_r[fi]);
+    c.phi[fi] = ph;
+    c.phiU[fi] = pU;
+    c.phiE[fi] = pE;
+  }
+}
+
+void calcFlux(Case& c) {
+  const int NF = c.F + c.B;
+  c.phi.assign(NF, 0.0);
+  c.phiE.assign(NF, 0.0);
+  c.phiU.assign(NF, V3());
+  if (c.cfg.flux_scheme == ICS_FLUX_AUSMPLUSUP)
+    calcFluxAUSM(c);
+  else if (c.cfg.flux_scheme == ICS_FLUX_HLLC)
+    calcFluxHLLC(c);
+  else
+    calcFluxRoe(c);
+  for (int b = 0; b < c.B; ++b) c.phiB[b] = c.phi[c.F + b];
+}
+
+// ---------------------------------------------------------------------------
+// Dual-time ddt (dualTimeDdtScheme.C:111-126 around Euler/backward/steady)
+// ---------------------------------------------------------------------------
+struct DdtCoeffs {
+  double rDeltaT = 0, coefft = 0, coefft0 = 0, coefft00 = 0;
+};
+DdtCoeffs ddtCoeffs(const Case& c) {
+  DdtCoeffs d;
+  if (c.cfg.ddt_scheme == ICS_DDT_STEADY) return d;
+  d.rDeltaT = 1.0 / c.cfg.delta_t;
+  if (c.cfg.ddt_scheme == ICS_DDT_BACKWARD) {
+    const double dt = c.cfg.delta_t;
+    const double dt0 = c.timeIndex <= 1 ? GREAT : dt;  // no old-old level on the first step
+    d.coefft = 1 + dt / (dt + dt0);
+    d.coefft00 = dt * dt / (dt0 * (dt + dt0));
+    d.coefft0 = d.coefft + d.coefft00;
+  }
+  return d;
+}
+// diag and source of fvm::ddt(W) for one cell and one scalar component
+inline void ddtMatrix(const Case& c, const DdtCoeffs& d, int i, double W, double W0, double W00, double& diag,
+                      double& source) {
+  const double Vc = c.V[i];
+  if (c.cfg.ddt_scheme == ICS_DDT_STEADY) {
+    diag = 0;
+    source = 0;
+  } else if (c.cfg.ddt_scheme == ICS_DDT_EULER) {
+    diag = d.rDeltaT * Vc;
+    source = d.rDeltaT * W0 * Vc;
+  } else {
+    diag = (d.coefft * d.rDeltaT) * Vc;
+    source = d.rDeltaT * Vc * (d.coefft0 * W0 - d.coefft00 * W00);
+  }
+  diag += c.rPseudoDeltaT[i] * Vc;
+  source += c.rPseudoDeltaT[i] * W * Vc;
+}
+
+// residualsUpdate.H: source = R*V with R = -div(fluxes) - ddt_phys
+void residualSource(Case& c) {
+  std::vector<double> divR(c.N, 0.0), divE(c.N, 0.0);
+  std::vector<V3> divU(c.N);
+  for (int fi = 0; fi < c.F; ++fi) {
+    const int o = c.own[fi], n = c.nei[fi];
+    divR[o] += c.phi[fi];
+    divR[n] -= c.phi[fi];
+    divU[o] = divU[o] + c.phiU[fi];
+    divU[n] = divU[n] - c.phiU[fi];
+    divE[o] += c.phiE[fi];
+    divE[n] -= c.phiE[fi];
+  }
+  for (int b = 0; b < c.B; ++b) {
+    const int o = c.bcell[b];
+    divR[o] += c.phi[c.F + b];
+    divU[o] = divU[o] + c.phiU[c.F + b];
+    divE[o] += c.phiE[c.F + b];
+  }
+  double l2 = 0;
+  c.src.assign(5 * c.N, 0.0);
+  const DdtCoeffs d = ddtCoeffs(c);
+  const bool steady = c.cfg.ddt_scheme == ICS_DDT_STEADY;
+  for (int i = 0; i < c.N; ++i) {
+    const double Vc = c.V[i];
+    double rR = -(divR[i] / Vc);
+    V3 rU = -1.0 * (divU[i] / Vc);
+    double rE = -(divE[i] / Vc);
+    l2 += sqr((divR[i] / Vc) * Vc);
+    if (!steady) {
+      double dg, s;
+      ddtMatrix(c, d, i, c.rho[i], c.rho0[i], c.rho00[i], dg, s);
+      rR -= (dg * c.rho[i] - s) / Vc;
+      for (int k = 0; k < 3; ++k) {
+        ddtMatrix(c, d, i, c.rhoU[i][k], c.rhoU0[i][k], c.rhoU00[i][k], dg, s);
+        rU[k] -= (dg * c.rhoU[i][k] - s) / Vc;
+      }
+      ddtMatrix(c, d, i, c.rhoE[i], c.rhoE0[i], c.rhoE00[i], dg, s);
+      rE -= (dg * c.rhoE[i] - s) / Vc;
+    }
+    c.src[5 * i + 0] = rR * Vc;
+    c.src[5 * i + 1] = rU.x * Vc;
+    c.src[5 * i + 2] = rU.y * Vc;
+    c.src[5 * i + 3] = rU.z * Vc;
+    c.src[5 * i + 4] = rE * Vc;
+  }
+  c.lastRhoL2 = std::sqrt(l2);
+}
+
+// face wave speed lambda = interp(c) + |interp(U) . n| (setCoAndDeltaT.H:52-54)
+void waveSpeed(const Case& c, std::vector<double>& lam) {
+  VolS cs;
+  cs.in.resize(c.N);
+  cs.bf.resize(c.B);
+  for (int i = 0; i < c.N; ++i) cs.in[i] = std::sqrt(c.gamma / psiOf(c, c.T[i]));
+  for (int b = 0; b < c.B; ++b) cs.bf[b] = std::sqrt(c.gamma / psiOf(c, c.TB[b]));
+  std::vector<double> ci;
+  interpLinear(c, cs, ci);
+  std::vector<double> ui[3];
+  for (int k = 0; k < 3; ++k) interpLinear(c, Ucmpt(c, k), ui[k]);
+  lam.resize(c.F + c.B);
+  for (int fi = 0; fi < c.F + c.B; ++fi) {
+    const V3 n = SfOf(c, fi) / magSfOf(c, fi);
+    const V3 uf(ui[0][fi], ui[1][fi], ui[2][fi]);
+    lam[fi] = ci[fi] + std::fabs(dot(uf, n) - 0.0);
+  }
+}
+
+double residualNorm(const ics_solver_perf& r) {
+  // sqrt(|s0|^2 + |s1|^2 + |v0|^2) with scalars rho, rhoE and vector rhoU
+  return std::sqrt(sqr(r.init_res[0]) + sqr(r.init_res[4]) +
+                   (sqr(r.init_res[1]) + sqr(r.init_res[2]) + sqr(r.init_res[3])));
+}
+
+// setCoAndDeltaT.H
+void setCoAndDeltaT(Case& c) {
+  if (c.initResValid) {
+    const bool firstIter = c.corr == 1;
+    if (!firstIter && c.prevResValid) {
+      const double normInit = residualNorm(c.initRes);
+      const double normPrev = residualNorm(c.prevRes);
+      double ratio = normPrev / normInit;
+      ratio = std::max(std::min(ratio, c.cfg.pseudo_co_max_increase), c.cfg.pseudo_co_min_decrease);
+      for (int i = 0; i < c.N; ++i) {
+        c.pseudoCo[i] *= ratio;
+        c.pseudoCo[i] = std::max(std::min(c.pseudoCo[i], c.cfg.pseudo_co_num_max), c.cfg.pseudo_co_num_min);
+      }
+    }
+    c.prevRes = c.initRes;
+    c.prevResValid = true;
+  }
+  std::vector<double> lam;
+  waveSpeed(c, lam);
+  std::fill(c.rPseudoDeltaT.begin(), c.rPseudoDeltaT.end(), 0.0);
+  for (int fi = 0; fi < c.F; ++fi) {
+    const double frdt = c.nodc[fi] * lam[fi];
+    c.rPseudoDeltaT[c.own[fi]] = std::max(c.rPseudoDeltaT[c.own[fi]], frdt);
+    c.rPseudoDeltaT[c.nei[fi]] = std::max(c.rPseudoDeltaT[c.nei[fi]], frdt);
+  }
+  for (int b = 0; b < c.B; ++b) {
+    const Patch& pt = c.patches[c.bpatch[b]];
+    if (!pt.is_wall) continue;
+    const int o = c.bcell[b];
+    const double cc = std::sqrt(c.gamma / psiOf(c, c.T[o]));
+    const double pl = 0.5 * c.bdc[b] * (cc + std::fabs(dot(c.U[o], c.bSf[b] / c.bmagSf[b]) - 0.0));
+    c.rPseudoDeltaT[o] = std::max(c.rPseudoDeltaT[o], pl);
+  }
+  for (int i = 0; i < c.N; ++i) c.rPseudoDeltaT[i] /= c.pseudoCo[i];
+  // ddtCoeff = max diag(fvm::ddt(rho|rhoU|rhoE)) / V
+  const DdtCoeffs d = ddtCoeffs(c);
+  for (int i = 0; i < c.N; ++i) {
+    double dg, s;
+    ddtMatrix(c, d, i, 0, 0, 0, dg, s);
+    c.ddtCoeff[i] = dg / c.V[i];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Jacobian (convectiveFluxScheme::createConvectiveJacobian)
+// ---------------------------------------------------------------------------
+// Euler flux Jacobian at state (U, E) for unit normal n (addFluxTerms:432-464)
+B5 eulerJacobian(double g, const V3& U, double E, const V3& n) {
+  B5 A;
+  const double theta = 0.5 * (g - 1) * magSqr(U);
+  const double a1 = g * E - theta;
+  const double a2 = g - 1;
+  const double projU = dot(U, n);
+  // d(cont)/d(rhoU) = n
+  A(0, 1) = n.x;
+  A(0, 2) = n.y;
+  A(0, 3) = n.z;
+  // d(mom)/d(rho) = n theta - U projU
+  for (int i = 0; i < 3; ++i) A(1 + i, 0) = n[i] * theta - U[i] * projU;
+  // d(mom)/d(rhoU) = U n - a2 n U + projU I
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) A(1 + i, 1 + j) = U[i] * n[j] - a2 * n[i] * U[j] + (i == j ? projU : 0.0);
+  // d(mom)/d(rhoE) = n a2
+  for (int i = 0; i < 3; ++i) A(1 + i, 4) = n[i] * a2;
+  A(4, 0) = projU * (theta - a1);
+  for (int j = 0; j < 3; ++j) A(4, 1 + j) = n[j] * a1 - a2 * U[j] * projU;
+  A(4, 4) = g * projU;
+  return A;
+}
+
+const int diagIdx[5] = {0, 6, 12, 18, 24};
+
+void assembleJacobian(Case& c) {
+  const int NF = c.F + c.B;
+  c.diag.assign(c.N, B5());
+  c.lower.assign(c.F, B5());
+  c.upper.assign(c.F, B5());
+  std::vector<V3> U_l, U_r;
+  reconstructU(c, +1, U_l);
+  reconstructU(c, -1, U_r);
+  VolS E = fieldE(c);
+  std::vector<double> E_l, E_r;
+  reconstruct(c, E, +1, c.cfg.recon_T, E_l);
+  reconstruct(c, E, -1, c.cfg.recon_T, E_r);
+  const double g = c.gamma;
+  // insertBlock: upper = 0.5|S| A_R, lower = -0.5|S| A_L, negSumDiag
+  for (int fi = 0; fi < c.F; ++fi) {
+    const V3 n = c.Sf[fi] / c.magSf[fi];
+    const B5 AL = eulerJacobian(g, U_l[fi], E_l[fi], n);
+    const B5 AR = eulerJacobian(g, U_r[fi], E_r[fi], n);
+    const double hs = 0.5 * c.magSf[fi];
+    for (int k = 0; k < 25; ++k) {
+      const double up = hs * AR.a[k];
+      const double lo = -0.5 * c.magSf[fi] * AL.a[k];
+      c.upper[fi].a[k] += up;
+      c.lower[fi].a[k] += lo;
+      c.diag[c.own[fi]].a[k] -= lo;
+      c.diag[c.nei[fi]].a[k] -= up;
+    }
+  }
+  // addDissipationJacobian: lambda = interp(c) + |interp(U).n|, subtracted
+  std::vector<double> lam;
+  waveSpeed(c, lam);
+  for (int fi = 0; fi < c.F; ++fi) {
+    const double d = 0.5 * c.magSf[fi] * lam[fi];
+    for (int q = 0; q < 5; ++q) {
+      const int k = diagIdx[q];
+      c.upper[fi].a[k] -= d;
+      c.lower[fi].a[k] -= d;
+      c.diag[c.own[fi]].a[k] += d;
+      c.diag[c.nei[fi]].a[k] += d;
+    }
+  }
+  for (int b = 0; b < c.B; ++b) {
+    const double d = 0.5 * c.bmagSf[b] * lam[c.F + b];
+    for (int q = 0; q < 5; ++q) c.diag[c.bcell[b]].a[diagIdx[q]] += d;
+  }
+  // addBoundaryTerms (boundaryJacobian :47-120, :219-355)
+  for (int b = 0; b < c.B; ++b) {
+    const Patch& pt = c.patches[c.bpatch[b]];
+    const int ci = c.bcell[b];
+    // valueInternalCoeffs
+    double pV = 1, tV = 1;
+    V3 uV(1, 1, 1);
+    const V3 nf = c.bSf[b] / c.bmagSf[b];
+    switch (pt.kind) {
+      case ICS_PATCH_ZERO_GRADIENT: break;
+      case ICS_PATCH_SLIP: uV = V3(1 - std::fabs(nf.x), 1 - std::fabs(nf.y), 1 - std::fabs(nf.z)); break;
+      case ICS_PATCH_FIXED: pV = 0; tV = 0; uV = V3(0, 0, 0); break;
+      case ICS_PATCH_PRESSURE_OUTLET: pV = 0; break;
+      case ICS_PATCH_TOTAL_INLET:
+        pV = 0;
+        tV = 0;
+        if (c.phiB[b] < 0) uV = V3(nf.x * nf.x, nf.y * nf.y, nf.z * nf.z);
+        break;
+      case ICS_PATCH_ISOTHERMAL_WALL: tV = 0; uV = V3(0, 0, 0); break;
+    }
+    const V3 SfB = c.bSf[b];
+    const double rhoB = rhoBof(c, b);
+    const V3 UB = c.UB[b];
+    const double UrelBdotSf = dot(UB, SfB) - 0.0 * c.bmagSf[b];
+    const double pB = c.pB[b], TB = c.TB[b];
+    const double rhoEB = rhoB * (heOf(c, TB) + 0.5 * magSqr(UB));
+    const double cvB = c.Cv;
+    const V3 SuV(SfB.x * uV.x, SfB.y * uV.y, SfB.z * uV.z);
+    const double dCdp = rhoB / pB * UrelBdotSf * pV;
+    const V3 dCdU = rhoB * SuV;
+    const double dCdT = -rhoB / TB * UrelBdotSf * tV;
+    const V3 dMdp = (rhoB / pB * UB * UrelBdotSf + SfB) * pV;
+    T33 dMdU = outer(rhoB * UB, SuV);
+    const V3 dMdUDiag = rhoB * UrelBdotSf * uV;
+    const V3 dMdT = -rhoB / TB * UB * UrelBdotSf * tV;
+    const double dEdp = (rhoEB / pB * UrelBdotSf + dot(UB, SfB)) * pV;
+    const V3 dEdU = SuV * (rhoEB + pB) + rhoB * UrelBdotSf * V3(UB.x * uV.x, UB.y * uV.y, UB.z * uV.z);
+    const double dEdT = UrelBdotSf * (rhoB * cvB - rhoEB / TB) * tV;
+    for (int i = 0; i < 3; ++i) dMdU.a[i][i] += dMdUDiag[i];
+    // derivatives of primitives w.r.t. conservative variables of the interior cell
+    const double rhoI = c.rho[ci];
+    const V3 UI = c.U[ci];
+    const double rhoEI = c.rhoE[ci];
+    const double gI = c.gamma, cvI = c.Cv;
+    const double dPdRho = 0.5 * (gI - 1) * magSqr(UI);
+    const V3 dUdRho = -1.0 * UI / rhoI;
+    const double dTdRho = -1.0 / (cvI * rhoI) * (rhoEI / rhoI - magSqr(UI));
+    const V3 dPdRhoU = -(gI - 1) * UI;
+    const double dUdRhoU = 1.0 / rhoI;  // spherical tensor
+    const V3 dTdRhoU = -1.0 * UI / (cvI * rhoI);
+    const double dPdRhoE = gI - 1;
+    const double dTdRhoE = 1.0 / (cvI * rhoI);
+    B5& D = c.diag[ci];
+    // continuity row
+    D(0, 0) += dCdp * dPdRho;
+    D(0, 0) += dot(dCdU, dUdRho);
+    D(0, 0) += dCdT * dTdRho;
+    for (int j = 0; j < 3; ++j) {
+      D(0, 1 + j) += dCdp * dPdRhoU[j];
+      D(0, 1 + j) += dCdU[j] * dUdRhoU;
+      D(0, 1 + j) += dCdT * dTdRhoU[j];
+    }
+    D(0, 4) += dCdp * dPdRhoE;
+    D(0, 4) += 0.0;
+    D(0, 4) += dCdT * dTdRhoE;
+    // momentum rows
+    for (int i = 0; i < 3; ++i) {
+      D(1 + i, 0) += dMdp[i] * dPdRho;
+      D(1 + i, 0) += dMdU.a[i][0] * dUdRho.x + dMdU.a[i][1] * dUdRho.y + dMdU.a[i][2] * dUdRho.z;
+      D(1 + i, 0) += dMdT[i] * dTdRho;
+      for (int j = 0; j < 3; ++j) {
+        D(1 + i, 1 + j) += dMdp[i] * dPdRhoU[j];
+        D(1 + i, 1 + j) += dMdU.a[i][j] * dUdRhoU;
+        D(1 + i, 1 + j) += dMdT[i] * dTdRhoU[j];
+      }
+      D(1 + i, 4) += dMdp[i] * dPdRhoE;
+      D(1 + i, 4) += 0.0;
+      D(1 + i, 4) += dMdT[i] * dTdRhoE;
+    }
+    // energy row
+    D(4, 0) += dEdp * dPdRho;
+    D(4, 0) += dot(dEdU, dUdRho);
+    D(4, 0) += dEdT * dTdRho;
+    for (int j = 0; j < 3; ++j) {
+      D(4, 1 + j) += dEdp * dPdRhoU[j];
+      D(4, 1 + j) += dEdU[j] * dUdRhoU;
+      D(4, 1 + j) += dEdT * dTdRhoU[j];
+    }
+    D(4, 4) += dEdp * dPdRhoE;
+    D(4, 4) += 0.0;
+    D(4, 4) += dEdT * dTdRhoE;
+  }
+  // addTemporalTerms
+  for (int i = 0; i < c.N; ++i) {
+    const double dc = c.ddtCoeff[i] * c.V[i];
+    for (int q = 0; q < 5; ++q) c.diag[i].a[diagIdx[q]] += dc;
+  }
+  (void)NF;
+  c.haveMatrix = true;
+}
+
+// ---------------------------------------------------------------------------
+// Linear algebra
+// ---------------------------------------------------------------------------
+inline void bmv(const B5& A, const double* x, double* y, double sign) {
+  for (int i = 0; i < 5; ++i) {
+    double s = 0;
+    for (int j = 0; j < 5; ++j) s += A(i, j) * x[j];
+    y[i] += sign * s;
+  }
+}
+
+// coupledMatrix::matrixMul -> blockFvMatrix::Amul (face loop in face order)
+void matrixMul(const Case& c, const double* x, double* y) {
+  for (int i = 0; i < c.N; ++i) {
+    for (int k = 0; k < 5; ++k) y[5 * i + k] = 0;
+    bmv(c.diag[i], x + 5 * i, y + 5 * i, 1.0);
+  }
+  for (int fi = 0; fi < c.F; ++fi) {
+    const int l = c.own[fi], u = c.nei[fi];
+    bmv(c.lower[fi], x + 5 * l, y + 5 * u, 1.0);
+    bmv(c.upper[fi], x + 5 * u, y + 5 * l, 1.0);
+  }
+}
+
+// lusgs.C:50-127 scalar diagonal
+bool lusgsDiag(const Case& c, std::vector<double>& rD) {
+  // scalars (rho, rhoE) first, then the vector diagonal xx, yy, zz
+  const int order[5] = {0, 24, 6, 12, 18};
+  rD.assign(c.N, GREAT);
+  for (int i = 0; i < c.N; ++i) {
+    for (int q = 0; q < 5; ++q) rD[i] = 1.0 / std::max(1.0 / rD[i], std::fabs(c.diag[i].a[order[q]]));
+    if (rD[i] < VSMALL) return false;
+  }
+  return true;
+}
+
+// lusgs::precondition (lusgs.C:220-385), sequential in cell order
+void lusgsPrecondition(const Case& c, const std::vector<double>& rD, double* r) {
+  for (int ci = 0; ci < c.N; ++ci) {
+    double d[5];
+    for (int k = 0; k < 5; ++k) d[k] = rD[ci] * r[5 * ci + k];
+    for (int fi : c.cellFaces[ci]) {
+      if (c.own[fi] == ci && c.nei[fi] > ci) bmv(c.lower[fi], d, r + 5 * c.nei[fi], -1.0);
+    }
+  }
+  for (int ci = c.N - 1; ci >= 0; --ci) {
+    double d[5];
+    for (int k = 0; k < 5; ++k) d[k] = rD[ci] * r[5 * ci + k];
+    for (int k = 0; k < 5; ++k) r[5 * ci + k] = d[k];
+    for (int fi : c.cellFaces[ci]) {
+      if (c.nei[fi] == ci && c.own[fi] < ci) bmv(c.upper[fi], d, r + 5 * c.own[fi], -1.0);
+    }
+  }
+}
+
+// 5x5 inverse by LU with partial pivoting (LUscalarMatrix restated)
+bool inv5(const B5& A, B5& Ainv) {
+  double a[5][5];
+  int piv[5];
+  for (int i = 0; i < 5; ++i)
+    for (int j = 0; j < 5; ++j) a[i][j] = A(i, j);
+  for (int k = 0; k < 5; ++k) {
+    int p = k;
+    double m = std::fabs(a[k][k]);
+    for (int i = k + 1; i < 5; ++i)
+      if (std::fabs(a[i][k]) > m) {
+        m = std::fabs(a[i][k]);
+        p = i;
+      }
+    piv[k] = p;
+    if (m == 0) return false;
+    if (p != k)
+      for (int j = 0; j < 5; ++j) std::swap(a[k][j], a[p][j]);
+    for (int i = k + 1; i < 5; ++i) {
+      a[i][k] /= a[k][k];
+      for (int j = k + 1; j < 5; ++j) a[i][j] -= a[i][k] * a[k][j];
+    }
+  }
+  for (int col = 0; col < 5; ++col) {
+    double b[5] = {0, 0, 0, 0, 0};
+    b[col] = 1;
+    for (int k = 0; k < 5; ++k)
+      if (piv[k] != k) std::swap(b[k], b[piv[k]]);
+    for (int i = 1; i < 5; ++i)
+      for (int j = 0; j < i; ++j) b[i] -= a[i][j] * b[j];
+    for (int i = 4; i >= 0; --i) {
+      for (int j = i + 1; j < 5; ++j) b[i] -= a[i][j] * b[j];
+      b[i] /= a[i][i];
+    }
+    for (int i = 0; i < 5; ++i) Ainv(i, col) = b[i];
+  }
+  return true;
+}
+
+void jacobiPrecondition(const Case& c, double* r) {
+  for (int i = 0; i < c.N; ++i) {
+    B5 inv;
+    inv5(c.diag[i], inv);
+    double z[5] = {0, 0, 0, 0, 0};
+    bmv(inv, r + 5 * i, z, 1.0);
+    for (int k = 0; k < 5; ++k) r[5 * i + k] = z[k];
+  }
+}
+
+int precondition(const Case& c, const std::vector<double>& rD, double* r) {
+  if (c.cfg.preconditioner == ICS_PC_LUSGS)
+    lusgsPrecondition(c, rD, r);
+  else if (c.cfg.preconditioner == ICS_PC_JACOBI)
+    jacobiPrecondition(c, r);
+  return ICS_OK;
+}
+
+// residualsIO helpers: per-equation L1 with scalar (rho, rhoE) and vector (rhoU) norm factors
+void l1Residual(const Case& c, const double* r, const double nf[3], double out[5]) {
+  double s0 = 0, s1 = 0, vx = 0, vy = 0, vz = 0;
+  for (int i = 0; i < c.N; ++i) {
+    s0 += std::fabs(r[5 * i + 0]);
+    vx += std::fabs(r[5 * i + 1]);
+    vy += std::fabs(r[5 * i + 2]);
+    vz += std::fabs(r[5 * i + 3]);
+    s1 += std::fabs(r[5 * i + 4]);
+  }
+  out[0] = s0 / nf[0];
+  out[4] = s1 / nf[1];
+  out[1] = vx / nf[2];
+  out[2] = vy / nf[2];
+  out[3] = vz / nf[2];
+}
+
+bool stopTest(const Case& c, const ics_solver_perf& perf) {
+  if (perf.n_iterations < c.cfg.min_iter) return false;
+  double mx = -VGREAT, mrel = -VGREAT;
+  for (int k = 0; k < 5; ++k) mx = std::max(mx, perf.final_res[k]);
+  mrel = std::max(mrel, perf.final_res[0] / (perf.init_res[0] + ROOTVSMALL));
+  mrel = std::max(mrel, perf.final_res[4] / (perf.init_res[4] + ROOTVSMALL));
+  for (int k = 0; k < 3; ++k)
+    if (c.solD[k] == 1) mrel = std::max(mrel, perf.final_res[1 + k] / (perf.init_res[1 + k] + ROOTVSMALL));
+  return perf.n_iterations >= c.cfg.max_iter || mx < c.cfg.tolerance || mrel < c.cfg.rel_tol;
+}
+
+// gmres::solveDelta (gmres.C:772-1107)
+int gmresSolveDelta(Case& c, const std::vector<double>& W, ics_solver_perf& perf, std::vector<double>& dx) {
+  const int N = c.N, m = c.cfg.n_directions;
+  const int n5 = 5 * N;
+  const double* b = c.src.data();
+  std::memset(&perf, 0, sizeof(perf));
+  // norm factors from A (W - avg)
+  double avg[5] = {0, 0, 0, 0, 0};
+  for (int i = 0; i < N; ++i)
+    for (int k = 0; k < 5; ++k) avg[k] += W[5 * i + k];
+  for (int k = 0; k < 5; ++k) avg[k] /= N;
+  std::vector<double> wmr(n5), tmp(n5);
+  for (int i = 0; i < N; ++i)
+    for (int k = 0; k < 5; ++k) wmr[5 * i + k] = W[5 * i + k] - avg[k];
+  matrixMul(c, wmr.data(), tmp.data());
+  double nf[3] = {0, 0, 0};
+  for (int i = 0; i < N; ++i) {
+    nf[0] += std::fabs(tmp[5 * i]) + std::fabs(b[5 * i]);
+    nf[1] += std::fabs(tmp[5 * i + 4]) + std::fabs(b[5 * i + 4]);
+    const V3 t(tmp[5 * i + 1], tmp[5 * i + 2], tmp[5 * i + 3]);
+    const V3 s(b[5 * i + 1], b[5 * i + 2], b[5 * i + 3]);
+    nf[2] += mag(t) + mag(s);
+  }
+  for (int k = 0; k < 3; ++k) nf[k] += VSMALL;
+  l1Residual(c, b, nf, perf.init_res);
+  std::memcpy(perf.final_res, perf.init_res, sizeof(perf.init_res));
+
+  std::vector<double> rD;
+  if (c.cfg.preconditioner == ICS_PC_LUSGS && !lusgsDiag(c, rD)) {
+    c.err = "All diagonals of coupledMatrix are zero";
+    return ICS_ERR_DIAG;
+  }
+  dx.assign(n5, 0.0);
+  std::vector<double> r(b, b + n5);
+  std::vector<std::vector<double>> Vk(m, std::vector<double>(n5));
+  std::vector<double> H(m * m, 0.0), yh(m, 0.0), bh(m + 1, 0.0), cs(m, 0.0), sn(m, 0.0);
+  auto givens = [](double h, double beta, double& cc, double& ss) {
+    if (beta == 0) {
+      cc = 1;
+      ss = 0;
+    } else if (std::fabs(beta) > std::fabs(h)) {
+      double tau = -h / beta;
+      ss = 1.0 / std::sqrt(1.0 + sqr(tau));
+      cc = ss * tau;
+    } else {
+      double tau = -beta / h;
+      cc = 1.0 / std::sqrt(1.0 + sqr(tau));
+      ss = cc * tau;
+    }
+  };
+  int status = ICS_OK;
+  do {
+    precondition(c, rD, r.data());
+    double beta = 0;
+    for (int i = 0; i < N; ++i) beta += sqr(r[5 * i]);
+    for (int i = 0; i < N; ++i) beta += sqr(r[5 * i + 4]);
+    for (int i = 0; i < N; ++i) beta += sqr(r[5 * i + 1]) + sqr(r[5 * i + 2]) + sqr(r[5 * i + 3]);
+    beta = std::sqrt(beta);
+    if (!(beta > 0) || !std::isfinite(beta)) {
+      // the reference divides by beta and produces NaN; stop with a status
+      status = std::isfinite(beta) ? ICS_ERR_BREAKDOWN : ICS_ERR_NONFINITE;
+      perf.n_iterations++;
+      break;
+    }
+    std::fill(bh.begin(), bh.end(), 0.0);
+    bh[0] = beta;
+    for (int i = 0; i < m; ++i) {
+      for (int q = 0; q < n5; ++q) Vk[i][q] = r[q] / beta;
+      matrixMul(c, Vk[i].data(), r.data());
+      precondition(c, rD, r.data());
+      for (int j = 0; j <= i; ++j) {
+        double s = 0;
+        for (int q = 0; q < N; ++q) s += r[5 * q] * Vk[j][5 * q];
+        for (int q = 0; q < N; ++q) s += r[5 * q + 4] * Vk[j][5 * q + 4];
+        for (int q = 0; q < N; ++q)
+          s += r[5 * q + 1] * Vk[j][5 * q + 1] + r[5 * q + 2] * Vk[j][5 * q + 2] + r[5 * q + 3] * Vk[j][5 * q + 3];
+        H[j * m + i] = s;
+        for (int q = 0; q < n5; ++q) r[q] -= H[j * m + i] * Vk[j][q];
+      }
+      beta = 0;
+      for (int q = 0; q < N; ++q) beta += sqr(r[5 * q]);
+      for (int q = 0; q < N; ++q) beta += sqr(r[5 * q + 4]);
+      for (int q = 0; q < N; ++q) beta += sqr(r[5 * q + 1]) + sqr(r[5 * q + 2]) + sqr(r[5 * q + 3]);
+      beta = std::sqrt(beta);
+      for (int j = 0; j < i; ++j) {
+        const double Hji = H[j * m + i];
+        H[j * m + i] = cs[j] * Hji - sn[j] * H[(j + 1) * m + i];
+        H[(j + 1) * m + i] = sn[j] * Hji + cs[j] * H[(j + 1) * m + i];
+      }
+      givens(H[i * m + i], beta, cs[i], sn[i]);
+      const double bhi = bh[i];
+      bh[i] = cs[i] * bhi - sn[i] * bh[i + 1];
+      bh[i + 1] = sn[i] * bhi + cs[i] * bh[i + 1];
+      H[i * m + i] = cs[i] * H[i * m + i] - sn[i] * beta;
+    }
+    for (int i = m - 1; i >= 0; --i) {
+      double sum = bh[i];
+      for (int j = i + 1; j < m; ++j) sum -= H[i * m + j] * yh[j];
+      double hii = H[i * m + i];
+      // stabilise(H_ii, VSMALL)
+      double st = hii >= 0 ? hii + VSMALL : hii - VSMALL;
+      yh[i] = sum / st;
+    }
+    for (int i = 0; i < m; ++i)
+      for (int q = 0; q < n5; ++q) dx[q] += yh[i] * Vk[i][q];
+    matrixMul(c, dx.data(), r.data());
+    for (int q = 0; q < n5; ++q) r[q] = b[q] - r[q];
+    l1Residual(c, r.data(), nf, perf.final_res);
+    for (int k = 0; k < 3; ++k)
+      if (c.solD[k] == -1) perf.final_res[1 + k] = 0.0;
+    perf.n_iterations++;
+  } while (!stopTest(c, perf));
+  perf.converged = status == ICS_OK;
+  // zero increments in empty directions (coupledMatrix.C:370-381)
+  for (int k = 0; k < 3; ++k)
+    if (c.solD[k] == -1)
+      for (int i = 0; i < N; ++i) dx[5 * i + 1 + k] = 0.0;
+  return status;
+}
+
+// ---------------------------------------------------------------------------
+// Boundary conditions and field update (updateFields.H)
+// ---------------------------------------------------------------------------
+void correctBoundaryConditions(Case& c, const std::vector<double>& psiB) {
+  const double g = c.gamma;
+  // p
+  for (int b = 0; b < c.B; ++b) {
+    const Patch& pt = c.patches[c.bpatch[b]];
+    const int ci = c.bcell[b];
+    switch (pt.kind) {
+      case ICS_PATCH_ZERO_GRADIENT:
+      case ICS_PATCH_SLIP:
+      case ICS_PATCH_ISOTHERMAL_WALL: c.pB[b] = c.p[ci]; break;
+      case ICS_PATCH_FIXED:
+      case ICS_PATCH_PRESSURE_OUTLET: c.pB[b] = pt.p; break;
+      case ICS_PATCH_TOTAL_INLET: {
+        const double gM1ByG = (g - 1.0) / g;
+        c.pB[b] = pt.p0 / std::pow((1.0 + 0.5 * psiB[b] * gM1ByG * (1.0 - pos0(c.phiB[b])) * magSqr(c.UB[b])),
+                                   1.0 / gM1ByG);
+        break;
+      }
+    }
+  }
+  // U
+  for (int b = 0; b < c.B; ++b) {
+    const Patch& pt = c.patches[c.bpatch[b]];
+    const int ci = c.bcell[b];
+    const V3 n = c.bSf[b] / c.bmagSf[b];
+    switch (pt.kind) {
+      case ICS_PATCH_ZERO_GRADIENT:
+      case ICS_PATCH_PRESSURE_OUTLET: c.UB[b] = c.U[ci]; break;
+      case ICS_PATCH_SLIP: c.UB[b] = c.U[ci] - n * dot(n, c.U[ci]); break;
+      case ICS_PATCH_FIXED: c.UB[b] = V3(pt.U[0], pt.U[1], pt.U[2]); break;
+      case ICS_PATCH_ISOTHERMAL_WALL: c.UB[b] = V3(0, 0, 0); break;
+      case ICS_PATCH_TOTAL_INLET: {
+        // directionMixed with valueFraction = neg(phi)(I - nn), refValue = 0
+        const double vf = neg(c.phiB[b]);
+        V3 out;
+        for (int i = 0; i < 3; ++i) {
+          double s = 0;
+          for (int j = 0; j < 3; ++j) {
+            const double Iij = (i == j ? 1.0 : 0.0);
+            const double vfij = vf * (Iij - n[i] * n[j]);
+            s += (Iij - vfij) * c.U[ci][j];
+          }
+          out[i] = 0.0 + s;
+        }
+        c.UB[b] = out;
+        break;
+      }
+    }
+  }
+  // T
+  for (int b = 0; b < c.B; ++b) {
+    const Patch& pt = c.patches[c.bpatch[b]];
+    const int ci = c.bcell[b];
+    switch (pt.kind) {
+      case ICS_PATCH_ZERO_GRADIENT:
+      case ICS_PATCH_SLIP:
+      case ICS_PATCH_PRESSURE_OUTLET: c.TB[b] = c.T[ci]; break;
+      case ICS_PATCH_FIXED:
+      case ICS_PATCH_ISOTHERMAL_WALL: c.TB[b] = pt.T; break;
+      case ICS_PATCH_TOTAL_INLET: {
+        const double gM1ByG = (g - 1.0) / g;
+        c.TB[b] = pt.T0 / (1.0 + 0.5 * psiB[b] * gM1ByG * (1.0 - pos0(c.phiB[b])) * magSqr(c.UB[b]));
+        break;
+      }
+    }
+    c.TB[b] = std::max(c.TB[b], c.cfg.T_min);
+    if (c.cfg.T_max < GREAT) c.TB[b] = std::max(c.TB[b], c.cfg.T_max);  // updateFields.H:86-89 as written
+  }
+}
+
+// updateFields.H: W += dW, bounding, thermo, primitives, BCs
+int updateFields(Case& c, const std::vector<double>& dW, int& bounded) {
+  bounded = 0;
+  for (int i = 0; i < c.N; ++i) {
+    c.rho[i] += dW[5 * i];
+    c.rhoU[i] = c.rhoU[i] + V3(dW[5 * i + 1], dW[5 * i + 2], dW[5 * i + 3]);
+    c.rhoE[i] += dW[5 * i + 4];
+  }
+  bool anyLow = false;
+  for (int i = 0; i < c.N; ++i)
+    if (c.rho[i] < c.cfg.rho_min) anyLow = true;
+  if (anyLow)
+    for (int i = 0; i < c.N; ++i) c.rho[i] = std::max(c.rho[i], c.cfg.rho_min);
+  const double eMin = heOf(c, c.cfg.T_min);
+  const double eMax = heOf(c, c.cfg.T_max);
+  for (int i = 0; i < c.N; ++i) {
+    c.U[i] = c.rhoU[i] / c.rho[i];
+    c.e[i] = c.rhoE[i] / c.rho[i] - 0.5 * magSqr(c.U[i]);
+    if (c.e[i] < eMin) {
+      c.e[i] = eMin;
+      bounded++;
+    }
+    if (c.cfg.T_max < GREAT && c.e[i] > eMax) {
+      c.e[i] = eMax;
+      bounded++;
+    }
+  }
+  // thermo.correct(): T from e, psi; boundary psi from the current boundary T
+  std::vector<double> psiB(c.B);
+  for (int i = 0; i < c.N; ++i) c.T[i] = c.e[i] / c.Cv;
+  for (int b = 0; b < c.B; ++b) psiB[b] = psiOf(c, c.TB[b]);
+  for (int i = 0; i < c.N; ++i) {
+    c.p[i] = c.rho[i] / psiOf(c, c.T[i]);
+    c.rhoU[i] = c.rho[i] * c.U[i];
+    c.rhoE[i] = c.rho[i] * (c.e[i] + 0.5 * magSqr(c.U[i]));
+  }
+  correctBoundaryConditions(c, psiB);
+  bool finite = true;
+  for (int i = 0; i < c.N; ++i)
+    if (!std::isfinite(c.rho[i]) || !std::isfinite(c.rhoE[i])) finite = false;
+  return finite ? ICS_OK : ICS_ERR_NONFINITE;
+}
+
+// boundLocalTimeStep.H (inert unless W_prev produces sub-bound values)
+void boundLocalTimeStep(Case& c) {
+  if (!c.cfg.local_timestepping || !c.cfg.local_timestepping_bounding) return;
+  const double lb = c.cfg.local_timestepping_lower_bound;
+  std::vector<double> rhoMin(c.N), eMin(c.N), eT(c.N), factor(c.N, 1.0);
+  for (int i = 0; i < c.N; ++i) {
+    const double rp = c.Wprev[5 * i], rEp = c.Wprev[5 * i + 4];
+    const V3 rUp(c.Wprev[5 * i + 1], c.Wprev[5 * i + 2], c.Wprev[5 * i + 3]);
+    rhoMin[i] = lb * rp;
+    eMin[i] = lb * (rEp / rp - 0.5 * magSqr(rUp / rp));
+    eT[i] = c.rhoE[i] / c.rho[i] - 0.5 * magSqr(c.rhoU[i] / c.rho[i]);
+  }
+  auto bad = [&](int i) { return c.rho[i] < rhoMin[i] || eT[i] < eMin[i] || eT[i] < SMALL; };
+  for (int fi = 0; fi < c.F; ++fi) {
+    const int o = c.own[fi], n = c.nei[fi];
+    if (bad(o)) {
+      factor[o] = std::min(0.5, factor[o]);
+      factor[n] = std::min(0.75, factor[n]);
+    }
+    if (bad(n)) {
+      factor[n] = std::min(0.5, factor[n]);
+      factor[o] = std::min(0.75, factor[o]);
+    }
+  }
+  for (int i = 0; i < c.N; ++i) c.pseudoCo[i] *= factor[i];
+}
+
+void storeW(const Case& c, std::vector<double>& W) {
+  W.resize(5 * c.N);
+  for (int i = 0; i < c.N; ++i) {
+    W[5 * i] = c.rho[i];
+    W[5 * i + 1] = c.rhoU[i].x;
+    W[5 * i + 2] = c.rhoU[i].y;
+    W[5 * i + 3] = c.rhoU[i].z;
+    W[5 * i + 4] = c.rhoE[i];
+  }
+}
+
+// pseudotimeControl::criteriaSatisfied / loop
+double maxInit(const ics_solver_perf& r) {
+  double m = -VGREAT;
+  for (int k = 0; k < 5; ++k) m = std::max(m, r.init_res[k]);
+  return m;
+}
+bool criteriaSatisfied(Case& c) {
+  const bool finalIter = c.converged_ || (c.corr == c.cfg.n_pseudo_corr);
+  if (c.firstIteration_ || c.corr == 1 || finalIter) {
+    c.firstIteration_ = false;
+    return false;
+  }
+  const bool storeIni = c.corr == 2;
+  if (storeIni) c.initResiduals_ = c.residuals_;
+  const bool absCheck = maxInit(c.residuals_) < c.cfg.pseudo_tol;
+  bool relCheck = false;
+  if (!storeIni) {
+    ics_solver_perf q = c.residuals_;
+    for (int k = 0; k < 5; ++k) q.init_res[k] /= c.initResiduals_.init_res[k] + ROOTVSMALL;
+    relCheck = maxInit(q) < c.cfg.pseudo_tol_rel;
+  }
+  return (c.corr >= c.cfg.n_pseudo_corr_min) && (absCheck || relCheck);
+}
+bool pseudoLoop(Case& c) {
+  const bool steady = c.cfg.ddt_scheme == ICS_DDT_STEADY;
+  c.corr++;
+  if (!steady && c.corr == c.cfg.n_pseudo_corr + 1) {
+    c.corr = 0;
+    return false;
+  }
+  bool completed = false;
+  if (c.converged_ || criteriaSatisfied(c)) {
+    if (c.converged_) {
+      c.corr = 0;
+      c.converged_ = false;
+      completed = true;
+    } else {
+      c.converged_ = true;
+    }
+  } else {
+    completed = false;
+  }
+  return !completed;
+}
+
+}  // namespace
+
+struct ics_handle_s : Case {};
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+void icsref_default_config(ics_config* c) {
+  std::memset(c, 0, sizeof(*c));
+  c->R = 287.0;
+  c->Cp = 1004.5;
+  c->mu = 0;
+  c->Pr = 0.72;
+  c->As = 1.458e-6;
+  c->Ts = 110.4;
+  c->flux_scheme = ICS_FLUX_AUSMPLUSUP;
+  c->low_mach_ausm = 1;
+  c->entropy_fix_coeff = 0.05;
+  c->recon_rho = c->recon_U = c->recon_T = ICS_RECON_UPWIND;
+  c->ddt_scheme = ICS_DDT_STEADY;
+  c->delta_t = 1;
+  c->solver = ICS_SOLVER_GMRES;
+  c->preconditioner = ICS_PC_LUSGS;
+  c->n_directions = 8;
+  c->max_iter = 1000;
+  c->min_iter = 0;
+  c->tolerance = 1e-12;
+  c->rel_tol = 1e-2;
+  c->precision = ICS_PREC_FP64;
+  c->n_pseudo_corr = 20;
+  c->n_pseudo_corr_min = 1;
+  c->pseudo_tol = 1e-5;
+  c->pseudo_tol_rel = 1e-5;
+  c->pseudo_co_num = 1;
+  c->pseudo_co_num_min = 0.1;
+  c->pseudo_co_num_max = 25;
+  c->pseudo_co_max_increase = 1.25;
+  c->pseudo_co_min_decrease = 0.1;
+  c->local_timestepping = 1;
+  c->local_timestepping_bounding = 1;
+  c->local_timestepping_lower_bound = 0.95;
+  c->reset_pseudo = 0;
+  c->rho_min = -GREAT;
+  c->T_min = SMALL;
+  c->T_max = GREAT;
+}
+
+int icsref_set_config(ics_handle h, const ics_config* cfg) {
+  if (!h || !cfg) return ICS_ERR_ARG;
+  if (cfg->flux_scheme < 0 || cfg->flux_scheme > 2) {
+    h->err = "Unknown convectiveFluxScheme";
+    return ICS_ERR_SCHEME;
+  }
+  if (cfg->preconditioner < 0 || cfg->preconditioner > 2 || cfg->solver != ICS_SOLVER_GMRES) {
+    h->err = "Unknown solver or preconditioner";
+    return ICS_ERR_SCHEME;
+  }
+  if (cfg->n_directions < 1 || cfg->n_directions > 64) return ICS_ERR_ARG;
+  h->cfg = *cfg;
+  h->Cv = cfg->Cp - cfg->R;
+  h->gamma = cfg->Cp / h->Cv;
+  if (!cfg->local_timestepping) {
+    h->err = "global pseudo time stepping is not supported";
+    return ICS_ERR_ARG;
+  }
+  return ICS_OK;
+}
+
+int icsref_create(const ics_mesh_desc* m, const ics_config* cfg, ics_handle* out) {
+  if (!m || !cfg || !out || m->n_cells <= 0 || m->n_faces < 0 || m->n_bfaces < 0) return ICS_ERR_ARG;
+  ics_handle h = new ics_handle_s();
+  Case& c = *h;
+  c.N = m->n_cells;
+  c.F = m->n_faces;
+  c.B = m->n_bfaces;
+  c.own.assign(m->owner, m->owner + c.F);
+  c.nei.assign(m->neighbour, m->neighbour + c.F);
+  for (int f = 0; f < c.F; ++f) {
+    if (c.own[f] < 0 || c.nei[f] >= c.N || c.own[f] >= c.nei[f]) {
+      delete h;
+      return ICS_ERR_ARG;
+    }
+  }
+  c.Sf.resize(c.F);
+  c.Cf.resize(c.F);
+  c.magSf.resize(c.F);
+  for (int f = 0; f < c.F; ++f) {
+    c.Sf[f] = V3(m->Sf[3 * f], m->Sf[3 * f + 1], m->Sf[3 * f + 2]);
+    c.Cf[f] = V3(m->Cf[3 * f], m->Cf[3 * f + 1], m->Cf[3 * f + 2]);
+    c.magSf[f] = mag(c.Sf[f]);
+  }
+  c.w.assign(m->weights, m->weights + c.F);
+  c.dc.assign(m->delta_coeffs, m->delta_coeffs + c.F);
+  c.nodc.assign(m->nonorth_delta_coeffs, m->nonorth_delta_coeffs + c.F);
+  c.C.resize(c.N);
+  for (int i = 0; i < c.N; ++i) c.C[i] = V3(m->C[3 * i], m->C[3 * i + 1], m->C[3 * i + 2]);
+  c.V.assign(m->V, m->V + c.N);
+  c.bcell.assign(m->b_cell, m->b_cell + c.B);
+  c.bpatch.assign(m->b_patch, m->b_patch + c.B);
+  c.bSf.resize(c.B);
+  c.bCf.resize(c.B);
+  c.bmagSf.resize(c.B);
+  for (int b = 0; b < c.B; ++b) {
+    if (c.bcell[b] < 0 || c.bcell[b] >= c.N || c.bpatch[b] < 0 || c.bpatch[b] >= m->n_patches) {
+      delete h;
+      return ICS_ERR_ARG;
+    }
+    c.bSf[b] = V3(m->b_Sf[3 * b], m->b_Sf[3 * b + 1], m->b_Sf[3 * b + 2]);
+    c.bCf[b] = V3(m->b_Cf[3 * b], m->b_Cf[3 * b + 1], m->b_Cf[3 * b + 2]);
+    c.bmagSf[b] = mag(c.bSf[b]);
+  }
+  c.bdc.assign(m->b_delta_coeffs, m->b_delta_coeffs + c.B);
+  for (int p = 0; p < m->n_patches; ++p) {
+    const ics_patch_desc& d = m->patches[p];
+    Patch q;
+    q.kind = d.kind;
+    q.is_wall = d.is_wall;
+    q.p = d.p;
+    q.T = d.T;
+    for (int k = 0; k < 3; ++k) q.U[k] = d.U[k];
+    q.p0 = d.p0;
+    q.T0 = d.T0;
+    c.patches.push_back(q);
+  }
+  for (int k = 0; k < 3; ++k) c.solD[k] = m->solution_d[k];
+  c.cellFaces.assign(c.N, {});
+  for (int f = 0; f < c.F; ++f) c.cellFaces[c.own[f]].push_back(f);
+  for (int f = 0; f < c.F; ++f) c.cellFaces[c.nei[f]].push_back(f);
+  int st = icsref_set_config(h, cfg);
+  if (st) {
+    delete h;
+    return st;
+  }
+  const int N = c.N;
+  c.rho.assign(N, 0);
+  c.rhoE.assign(N, 0);
+  c.p.assign(N, 0);
+  c.T.assign(N, 0);
+  c.e.assign(N, 0);
+  c.rhoU.assign(N, V3());
+  c.U.assign(N, V3());
+  c.pB.assign(c.B, 0);
+  c.TB.assign(c.B, 0);
+  c.phiB.assign(c.B, 0);
+  c.UB.assign(c.B, V3());
+  c.pseudoCo.assign(N, cfg->pseudo_co_num);
+  c.rPseudoDeltaT.assign(N, 0.0);
+  c.ddtCoeff.assign(N, 0.0);
+  *out = h;
+  return ICS_OK;
+}
+
+int icsref_destroy(ics_handle h) {
+  delete h;
+  return ICS_OK;
+}
+
+int icsref_last_error(ics_handle h, char* buf, int32_t len) {
+  if (!h || !buf || len <= 0) return ICS_ERR_ARG;
+  std::snprintf(buf, len, "%s", h->err.c_str());
+  return ICS_OK;
+}
+
+static void copyOld(Case& c) {
+  c.rho0 = c.rho;
+  c.rhoE0 = c.rhoE;
+  c.rhoU0 = c.rhoU;
+  c.rho00 = c.rho;
+  c.rhoE00 = c.rhoE;
+  c.rhoU00 = c.rhoU;
+}
+
+int icsref_set_primitive(ics_handle h, const double* p, const double* U, const double* T) {
+  if (!h || !p || !U || !T) return ICS_ERR_ARG;
+  Case& c = *h;
+  for (int i = 0; i < c.N; ++i) {
+    c.p[i] = p[i];
+    c.T[i] = T[i];
+    c.U[i] = V3(U[3 * i], U[3 * i + 1], U[3 * i + 2]);
+    c.e[i] = heOf(c, c.T[i]);
+    c.rho[i] = psiOf(c, c.T[i]) * c.p[i];
+    c.rhoU[i] = c.rho[i] * c.U[i];
+    c.rhoE[i] = c.rho[i] * (c.e[i] + 0.5 * magSqr(c.U[i]));
+  }
+  // boundary initial guess: interior values, then one BC evaluation
+  std::vector<double> psiB(c.B);
+  for (int b = 0; b < c.B; ++b) {
+    const int ci = c.bcell[b];
+    c.pB[b] = c.p[ci];
+    c.TB[b] = c.T[ci];
+    c.UB[b] = c.U[ci];
+    c.phiB[b] = psiOf(c, c.TB[b]) * c.pB[b] * dot(c.UB[b], c.bSf[b]);
+    psiB[b] = psiOf(c, c.TB[b]);
+  }
+  correctBoundaryConditions(c, psiB);
+  copyOld(c);
+  c.timeIndex = 0;
+  return ICS_OK;
+}
+
+int icsref_set_boundary_state(ics_handle h, const double* pb, const double* Ub, const double* Tb, const double* phib) {
+  if (!h) return ICS_ERR_ARG;
+  Case& c = *h;
+  for (int b = 0; b < c.B; ++b) {
+    if (pb) c.pB[b] = pb[b];
+    if (Tb) c.TB[b] = Tb[b];
+    if (Ub) c.UB[b] = V3(Ub[3 * b], Ub[3 * b + 1], Ub[3 * b + 2]);
+    if (phib) c.phiB[b] = phib[b];
+  }
+  return ICS_OK;
+}
+
+int icsref_get_boundary_state(ics_handle h, double* pb, double* Ub, double* Tb, double* phib) {
+  if (!h) return ICS_ERR_ARG;
+  Case& c = *h;
+  for (int b = 0; b < c.B; ++b) {
+    if (pb) pb[b] = c.pB[b];
+    if (Tb) Tb[b] = c.TB[b];
+    if (Ub)
+      for (int k = 0; k < 3; ++k) Ub[3 * b + k] = c.UB[b][k];
+    if (phib) phib[b] = c.phiB[b];
+  }
+  return ICS_OK;
+}
+
+int icsref_get_state(ics_handle h, double* W, double* p, double* U, double* T) {
+  if (!h) return ICS_ERR_ARG;
+  Case& c = *h;
+  for (int i = 0; i < c.N; ++i) {
+    if (W) {
+      W[5 * i] = c.rho[i];
+      W[5 * i + 1] = c.rhoU[i].x;
+      W[5 * i + 2] = c.rhoU[i].y;
+      W[5 * i + 3] = c.rhoU[i].z;
+      W[5 * i + 4] = c.rhoE[i];
+    }
+    if (p) p[i] = c.p[i];
+    if (T) T[i] = c.T[i];
+    if (U)
+      for (int k = 0; k < 3; ++k) U[3 * i + k] = c.U[i][k];
+  }
+  return ICS_OK;
+}
+
+int icsref_set_conservative(ics_handle h, const double* W, int32_t set_old) {
+  if (!h || !W) return ICS_ERR_ARG;
+  Case& c = *h;
+  for (int i = 0; i < c.N; ++i) {
+    c.rho[i] = W[5 * i];
+    c.rhoU[i] = V3(W[5 * i + 1], W[5 * i + 2], W[5 * i + 3]);
+    c.rhoE[i] = W[5 * i + 4];
+    c.U[i] = c.rhoU[i] / c.rho[i];
+    c.e[i] = c.rhoE[i] / c.rho[i] - 0.5 * magSqr(c.U[i]);
+    c.T[i] = c.e[i] / c.Cv;
+    c.p[i] = c.rho[i] / psiOf(c, c.T[i]);
+  }
+  if (set_old) copyOld(c);
+  return ICS_OK;
+}
+
+int icsref_set_pseudo_co(ics_handle h, const double* co) {
+  if (!h || !co) return ICS_ERR_ARG;
+  h->pseudoCo.assign(co, co + h->N);
+  return ICS_OK;
+}
+
+int icsref_get_pseudo_co(ics_handle h, double* co, double* rdt) {
+  if (!h) return ICS_ERR_ARG;
+  for (int i = 0; i < h->N; ++i) {
+    if (co) co[i] = h->pseudoCo[i];
+    if (rdt) rdt[i] = h->rPseudoDeltaT[i];
+  }
+  return ICS_OK;
+}
+
+int icsref_calc_flux(ics_handle h, double* phi, double* phiU, double* phiE) {
+  if (!h) return ICS_ERR_ARG;
+  Case& c = *h;
+  calcFlux(c);
+  const int NF = c.F + c.B;
+  for (int f = 0; f < NF; ++f) {
+    if (phi) phi[f] = c.phi[f];
+    if (phiE) phiE[f] = c.phiE[f];
+    if (phiU)
+      for (int k = 0; k < 3; ++k) phiU[3 * f + k] = c.phiU[f][k];
+  }
+  return ICS_OK;
+}
+
+int icsref_residual(ics_handle h, double* source) {
+  if (!h) return ICS_ERR_ARG;
+  Case& c = *h;
+  calcFlux(c);
+  residualSource(c);
+  setCoAndDeltaT(c);
+  if (source) std::memcpy(source, c.src.data(), sizeof(double) * 5 * c.N);
+  for (double v : c.src)
+    if (!std::isfinite(v)) {
+      c.err = "non-finite residual";
+      return ICS_ERR_NONFINITE;
+    }
+  return ICS_OK;
+}
+
+int icsref_assemble_jacobian(ics_handle h) {
+  if (!h) return ICS_ERR_ARG;
+  assembleJacobian(*h);
+  return ICS_OK;
+}
+
+int icsref_get_jacobian(ics_handle h, double* diag, double* lower, double* upper) {
+  if (!h) return ICS_ERR_ARG;
+  Case& c = *h;
+  if (!c.haveMatrix) return ICS_ERR_STATE;
+  for (int i = 0; i < c.N; ++i)
+    if (diag) std::memcpy(diag + 25 * i, c.diag[i].a, sizeof(double) * 25);
+  for (int f = 0; f < c.F; ++f) {
+    if (lower) std::memcpy(lower + 25 * f, c.lower[f].a, sizeof(double) * 25);
+    if (upper) std::memcpy(upper + 25 * f, c.upper[f].a, sizeof(double) * 25);
+  }
+  return ICS_OK;
+}
+
+int icsref_matrix_mul(ics_handle h, const double* x, double* y) {
+  if (!h || !x || !y) return ICS_ERR_ARG;
+  if (!h->haveMatrix) return ICS_ERR_STATE;
+  matrixMul(*h, x, y);
+  return ICS_OK;
+}
+
+int icsref_precondition(ics_handle h, double* r) {
+  if (!h || !r) return ICS_ERR_ARG;
+  Case& c = *h;
+  if (!c.haveMatrix) return ICS_ERR_STATE;
+  std::vector<double> rD;
+  if (c.cfg.preconditioner == ICS_PC_LUSGS && !lusgsDiag(c, rD)) return ICS_ERR_DIAG;
+  return precondition(c, rD, r);
+}
+
+int icsref_solve_increment(ics_handle h, ics_solver_perf* perf, double* dW) {
+  if (!h) return ICS_ERR_ARG;
+  Case& c = *h;
+  if (!c.haveMatrix) return ICS_ERR_STATE;
+  storeW(c, c.Wprev);
+  ics_solver_perf pf;
+  int st = gmresSolveDelta(c, c.Wprev, pf, c.dW);
+  c.haveIncrement = true;
+  if (perf) *perf = pf;
+  if (dW) std::memcpy(dW, c.dW.data(), sizeof(double) * 5 * c.N);
+  c.initRes = pf;
+  c.initResValid = true;
+  c.residuals_ = pf;
+  return st;
+}
+
+int icsref_update_fields(ics_handle h, ics_iter_stats* st) {
+  if (!h) return ICS_ERR_ARG;
+  Case& c = *h;
+  if (!c.haveIncrement) return ICS_ERR_STATE;
+  boundLocalTimeStep(c);
+  int bounded = 0;
+  int s = updateFields(c, c.dW, bounded);
+  c.haveIncrement = false;
+  if (st) {
+    st->bounded_cells = bounded;
+    st->rho_l2_residual = c.lastRhoL2;
+  }
+  return s;
+}
+
+int icsref_pseudo_iteration(ics_handle h, ics_iter_stats* st) {
+  if (!h) return ICS_ERR_ARG;
+  Case& c = *h;
+  ics_iter_stats s{};
+  int r = icsref_residual(h, nullptr);
+  if (r) return r;
+  assembleJacobian(c);
+  r = icsref_solve_increment(h, &s.perf, nullptr);
+  if (r && r != ICS_ERR_BREAKDOWN) return r;
+  int bounded = 0;
+  boundLocalTimeStep(c);
+  int u = updateFields(c, c.dW, bounded);
+  c.haveIncrement = false;
+  s.bounded_cells = bounded;
+  s.rho_l2_residual = c.lastRhoL2;
+  double m = 0;
+  for (int i = 0; i < c.N; ++i) m += c.pseudoCo[i];
+  s.pseudo_co_mean = m / c.N;
+  s.status = r ? r : u;
+  if (st) *st = s;
+  return u;
+}
+
+int icsref_begin_time_step(ics_handle h) {
+  if (!h) return ICS_ERR_ARG;
+  Case& c = *h;
+  const bool steady = c.cfg.ddt_scheme == ICS_DDT_STEADY;
+  // runTime++: old-old <- old <- current
+  c.rho00 = c.rho0;
+  c.rhoU00 = c.rhoU0;
+  c.rhoE00 = c.rhoE0;
+  c.rho0 = c.rho;
+  c.rhoU0 = c.rhoU;
+  c.rhoE0 = c.rhoE;
+  if (c.timeIndex == 0) {
+    c.rho00 = c.rho0;
+    c.rhoU00 = c.rhoU0;
+    c.rhoE00 = c.rhoE0;
+  }
+  c.timeIndex++;
+  if (!steady) {
+    c.initResValid = false;
+    c.prevResValid = false;
+  }
+  if (c.cfg.reset_pseudo) std::fill(c.pseudoCo.begin(), c.pseudoCo.end(), c.cfg.pseudo_co_num);
+  return ICS_OK;
+}
+
+int icsref_pseudo_loop(ics_handle h, int32_t* more) {
+  if (!h || !more) return ICS_ERR_ARG;
+  *more = pseudoLoop(*h) ? 1 : 0;
+  return ICS_OK;
+}
+
+}  // extern "C"

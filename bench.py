@@ -1,0 +1,425 @@
+#!/usr/bin/env python
+"""Benchmark of the implicit coupled pseudo-time iteration on one GB300.
+
+Workload: inviscid transonic bump channel, 256x64x64 hex cells (1,048,576),
+HLLC with MUSCL / Venkatakrishnan reconstruction, steady local time stepping
+with the SER CFL ramp 1 -> 200, GMRES(8) + LU-SGS on the colour-blocked cell
+numbering.  Synthetic mesh and uniform initial state (generated, seeded).
+
+A step is one pseudo-time (Newton) iteration: residual, local time step,
+Jacobian assembly, GMRES solve, state update.  ``value`` is cell-iterations
+per second of the mixed-precision path (FP64 residual and update, FP32
+Jacobian, preconditioner and Krylov basis) with all state resident in HBM;
+the FP64 path is timed the same way beside it.  The working set (state,
+Jacobian, Krylov basis: several GB) is far larger than the 129 MB L2, so no
+L2 flush is needed between steps.
+
+Other legs in the JSON line: iterations and seconds to a 1e-8 drop of the
+density residual (mixed and FP64), the end-to-end rate through the C ABI with
+host buffers, the roofline of the dominant kernel, SM clocks sampled during
+the timed region, and the CPU oracle timed on a bounded sample.
+
+``--impl reference`` times the CPU oracle (the reference algorithm restated
+in C++) on a 64x16x16 sample of the same workload.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-iters/s to 1e-8 residual drop, mixed vs FP64 on GB300; flux+SpMV HBM GB/s"
+UNIT = "cell-iters/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nx", type=int, default=256)
+    ap.add_argument("--ny", type=int, default=64)
+    ap.add_argument("--nz", type=int, default=64)
+    ap.add_argument("--to-solution", type=int, default=1, help="also run to the 1e-8 drop")
+    ap.add_argument("--solution-cap-s", type=float, default=60.0)
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--profile", type=int, default=1, help="per-kernel CUDA events in the timed region")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ ranks
+class Dist:
+    def __init__(self, n):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+
+            td.init_process_group("gloo")
+            self.td = td
+            self.pg = True
+
+    def barrier(self):
+        if self.pg:
+            self.td.barrier()
+
+    def max(self, v):
+        if not self.pg:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.td.destroy_process_group()
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.rows = []
+        self.p = None
+        self.index = index
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 8:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        sm, mx, reasons = [], [], set()
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                mx.append(float(r[1]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if r[4 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------- algorithmic bytes
+def kernel_bytes(kind, N, F, B, nslots, mixed, nlev):
+    """Compulsory DRAM bytes of one launch of a kernel class (each array once)."""
+    pb = 4 if mixed else 8   # block entries
+    pv = 4 if mixed else 8   # Krylov vectors
+    if kind == "face":       # MUSCL face flux: gathered cell fields + face geometry + outputs
+        return 264 * N + 232 * F
+    if kind == "grad":
+        return 268 * N + 96 * F
+    if kind == "cellres":
+        return 136 * N + 64 * F
+    if kind == "jac_rows":
+        return (112 + 50 * pb) * F + (25 * pb + 16 + pb) * N
+    if kind == "spmv":
+        return 25 * pb * N + 50 * pb * F + 8 * F + 10 * pv * N
+    if kind in ("lusgs_fwd", "lusgs_rev"):  # one level; sweep total split evenly over levels
+        return (25 * pb * F + pb * N + 10 * pv * N + 4 * F) / max(1, nlev)
+    if kind == "mgs":
+        return 20 * pv * N
+    return None
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def load_traffic():
+    """Per-launch DRAM bytes of kernel classes from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "ncu_dram_traffic.txt")
+    out = {}
+    try:
+        with open(p) as f:
+            for line in f:
+                if line.startswith("#") or not line.strip():
+                    continue
+                kind, cells, prec, byts = line.split()[:4]
+                out[(kind, prec)] = (int(cells), float(byts))
+    except OSError:
+        pass
+    return out
+
+
+# ------------------------------------------------------------------ legs
+def run_timed(w, prec, steps, warmup, dist, profile):
+    from icsfoam_gb300 import cases, gpu
+
+    b = gpu.binding()
+    h = gpu.open_case(w.mesh, cases.make_config(b, w.settings, precision=prec))
+    h.set_primitive(w.p, w.U, w.T)
+    for _ in range(warmup):
+        h.pseudo_loop()
+        h.pseudo_iteration()
+    clocks = ClockSampler(0)
+    clocks.start()
+    dist.barrier()
+    l0 = h.launch_count()
+    if profile:
+        h.profile(True)
+    h.timer_start()
+    last = None
+    for _ in range(steps):
+        h.pseudo_loop()
+        last = h.pseudo_iteration()
+    ms = h.timer_stop()
+    launches = h.launch_count() - l0
+    kern = None
+    if profile:
+        h.profile(False)
+        kern = h.profile_read()
+    ck = clocks.stop()
+    ms = dist.max(ms)
+    h.close()
+    return {"ms": ms, "launches": launches, "kernels": kern, "clocks": ck,
+            "last_rho_l2": last.rho_l2_residual if last else None}
+
+
+def run_to_solution(w, prec, cap_s, target=1e-8, max_iters=20000):
+    from icsfoam_gb300 import cases, gpu
+
+    b = gpu.binding()
+    h = gpu.open_case(w.mesh, cases.make_config(b, w.settings, precision=prec))
+    h.set_primitive(w.p, w.U, w.T)
+    t0 = time.perf_counter()
+    r0 = None
+    it = 0
+    drop = 1.0
+    hist = []
+    while it < max_iters:
+        h.pseudo_loop()
+        s = h.pseudo_iteration()
+        it += 1
+        r0 = r0 or s.rho_l2_residual
+        drop = s.rho_l2_residual / r0
+        if it % 50 == 0:
+            hist.append((it, drop))
+        if drop <= target or time.perf_counter() - t0 > cap_s:
+            break
+    dt = time.perf_counter() - t0
+    state = h.get_state()["W"]
+    h.close()
+    return {"iterations": it, "seconds": dt, "drop": drop, "reached": drop <= target,
+            "cell_iters_per_s": w.mesh.n_cells * it / dt, "history": hist[-6:]}, state
+
+
+def run_e2e(w, steps):
+    """Through the C ABI with host buffers: state H2D, one pseudo iteration, state D2H per step."""
+    import numpy as np
+
+    from icsfoam_gb300 import cases, gpu
+
+    b = gpu.binding()
+    h = gpu.open_case(w.mesh, cases.make_config(b, w.settings, precision=1))
+    h.set_primitive(w.p, w.U, w.T)
+    W = h.get_state()["W"]
+    for _ in range(2):
+        h.set_conservative(W)
+        h.pseudo_loop()
+        h.pseudo_iteration()
+        W = h.get_state()["W"]
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        h.set_conservative(W)
+        h.pseudo_loop()
+        s = h.pseudo_iteration()
+        W = h.get_state()["W"]
+    dt = time.perf_counter() - t0
+    h.close()
+    n = w.mesh.n_cells
+    return {"value": n * steps / dt, "unit": UNIT, "h2d_bytes_per_step": int(W.nbytes),
+            "d2h_bytes_per_step": int(W.nbytes + 8 * np.dtype("float64").itemsize)}
+
+
+def cpu_sample(seconds, warm=1):
+    """The oracle (reference algorithm, FP64, sequential) on a 64x16x16 sample."""
+    import oracle
+    from icsfoam_gb300 import cases
+
+    w = cases.bump_channel(64, 16, 16, ordering_mode="colour")
+    h = oracle.open_case(w.mesh, cases.make_config(oracle.binding(), w.settings))
+    h.set_primitive(w.p, w.U, w.T)
+    for _ in range(warm):
+        h.pseudo_loop()
+        h.pseudo_iteration()
+    t0 = time.perf_counter()
+    it = 0
+    while True:
+        h.pseudo_loop()
+        h.pseudo_iteration()
+        it += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": w.mesh.n_cells * it / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "bump channel 64x16x16 (16,384 cells), same schemes/settings, %d pseudo iterations "
+                      "after %d warm-up, FP64 oracle, 1 thread" % (it, warm)}
+
+
+def reference_arm(args, dist):
+    if dist.rank != 0:
+        return
+    import oracle
+    from icsfoam_gb300 import cases
+
+    w = cases.bump_channel(64, 16, 16, ordering_mode="colour")
+    h = oracle.open_case(w.mesh, cases.make_config(oracle.binding(), w.settings))
+    h.set_primitive(w.p, w.U, w.T)
+    for _ in range(args.warmup):
+        h.pseudo_loop()
+        h.pseudo_iteration()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        h.pseudo_loop()
+        h.pseudo_iteration()
+    dt = time.perf_counter() - t0
+    v = w.mesh.n_cells * args.steps / dt
+    sample = ("bump channel 64x16x16 (16,384 cells) standing in for 256x64x64; HLLC MUSCL/Venkatakrishnan, "
+              "GMRES(8)+LU-SGS; FP64 oracle, 1 thread")
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "bump_channel_64x16x16_sample_of_256x64x64", "cells": w.mesh.n_cells},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    dist = Dist(args.gpus)
+    if args.impl == "reference":
+        reference_arm(args, dist)
+        dist.close()
+        return
+    if dist.world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(dist.local)
+    from icsfoam_gb300 import cases
+
+    t0 = time.time()
+    w = cases.bump_channel(args.nx, args.ny, args.nz, ordering_mode="colour")
+    mesh_s = time.time() - t0
+    N, F, B = w.mesh.n_cells, w.mesh.n_faces, w.mesh.n_bfaces
+    mixed = run_timed(w, 1, args.steps, args.warmup, dist, args.profile)
+    fp64 = run_timed(w, 0, args.steps, args.warmup, dist, args.profile)
+    value = N * args.steps * dist.world / (mixed["ms"] / 1000.0)
+    value64 = N * args.steps * dist.world / (fp64["ms"] / 1000.0)
+    extra = {}
+    if dist.rank == 0 and args.to_solution:
+        import numpy as np
+
+        sm, Wm = run_to_solution(w, 1, args.solution_cap_s)
+        sd, Wd = run_to_solution(w, 0, args.solution_cap_s)
+        scale = np.abs(Wd).max(axis=0)
+        scale[1:4] = scale[1:4].max()
+        extra["to_solution"] = {"mixed": sm, "fp64": sd,
+                                "mixed_vs_fp64_field_max_rel_diff": float((np.abs(Wm - Wd) / scale).max())}
+    e2e = run_e2e(w, args.e2e_steps) if dist.rank == 0 else None
+    # roofline of the dominant kernel class of the mixed leg
+    from icsfoam_gb300 import ordering  # noqa: F401
+
+    nslots = None
+    roof = None
+    kern_table = {}
+    if mixed["kernels"]:
+        peak, peak_kind = load_peaks()
+        traffic = load_traffic()
+        nlev = 2
+        tot = sum(v[0] for v in mixed["kernels"].values())
+        dom = max(mixed["kernels"].items(), key=lambda kv: kv[1][0])
+        for k, (ms, n) in mixed["kernels"].items():
+            if n:
+                kern_table[k] = {"ms_total": round(ms, 3), "launches": n, "share": round(ms / tot, 4),
+                                 "ms_per_launch": round(ms / n, 5)}
+                byts = kernel_bytes(k, N, F, B, nslots, True, nlev)
+                if byts:
+                    kern_table[k]["GBps"] = round(byts / (ms / n / 1000.0) / 1e9, 1)
+        name, (ms, n) = dom
+        byts = kernel_bytes(name, N, F, B, nslots, True, nlev)
+        if byts:
+            ach = byts / (ms / n / 1000.0) / 1e9
+            tr = traffic.get((name, "mixed"))
+            roof = {"kernel": name, "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                    "frac": round(ach / peak, 4), "peak_source": peak_kind,
+                    "algorithmic_bytes_per_launch": int(byts),
+                    "traffic": (tr[1] * N / tr[0]) if tr else None}
+    fp64_table = {}
+    if fp64["kernels"]:
+        for k, (ms, n) in fp64["kernels"].items():
+            if n:
+                fp64_table[k] = {"ms_total": round(ms, 3), "launches": n}
+                byts = kernel_bytes(k, N, F, B, nslots, False, 2)
+                if byts:
+                    fp64_table[k]["GBps"] = round(byts / (ms / n / 1000.0) / 1e9, 1)
+    cpu = cpu_sample(args.cpu_seconds) if dist.rank == 0 else None
+    if dist.rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": mixed["ms"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64 residual/update + f32 Jacobian/Krylov",
+            "data": "synthetic (generated bump-channel mesh, uniform M=0.675 initial state)",
+            "config": {"workload": "bump_channel_%dx%dx%d" % (args.nx, args.ny, args.nz), "cells": N,
+                       "internal_faces": F, "boundary_faces": B, "flux": "HLLC",
+                       "reconstruction": "MUSCL + cellLimited<Venkatakrishnan>", "solver": "GMRES(8)+LU-SGS",
+                       "ordering": "colour-blocked", "parallelism": "replicas" if dist.world > 1 else "1 GPU",
+                       "l2": "working set >> 129 MB L2; no flush needed"},
+            "fp64": {"value": value64, "unit": UNIT, "ms_per_step": fp64["ms"] / args.steps,
+                     "kernels": fp64_table},
+            "mixed_over_fp64": value / value64,
+            "kernels": kern_table, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": mixed["launches"], "clocks": mixed["clocks"], "mesh_build_s": round(mesh_s, 1),
+        }
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

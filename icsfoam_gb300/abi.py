@@ -127,7 +127,19 @@ _FUNCS = {
     "pseudo_loop": (C.c_int, [_P, C.POINTER(C.c_int32)]),
 }
 
-EXPORTED = tuple(_FUNCS)
+# measurement entry points (CUDA library only)
+_MEASURE = {
+    "profile": (C.c_int, [_P, C.c_int32]),
+    "profile_read": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
+    "launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "timer_start": (C.c_int, [_P]),
+    "timer_stop": (C.c_int, [_P, C.POINTER(C.c_double)]),
+}
+
+KERNEL_CLASSES = ("fields", "grad", "face", "bface", "cellres", "jac_boundary", "jac_rows", "jacobi_inv", "spmv",
+                  "lusgs_fwd", "lusgs_rev", "jacobi", "mgs", "vector", "scalar", "update", "bc", "bound")
+
+EXPORTED = tuple(_FUNCS) + tuple(_MEASURE)
 
 
 class Binding:
@@ -142,6 +154,12 @@ class Binding:
             f.restype = res
             f.argtypes = args
             self.fn[name] = f
+        for name, (res, args) in _MEASURE.items():
+            f = getattr(lib, prefix + name, None)
+            if f is not None:
+                f.restype = res
+                f.argtypes = args
+                self.fn[name] = f
 
     def default_config(self) -> Config:
         cfg = Config()
@@ -331,3 +349,29 @@ class CaseHandle:
         more = C.c_int32()
         self._check(self.b.fn["pseudo_loop"](self.h, C.byref(more)), "pseudo_loop")
         return bool(more.value)
+
+    # ---------------------------------------------------------- measurement
+    def profile(self, enable: bool):
+        self._check(self.b.fn["profile"](self.h, int(enable)), "profile")
+
+    def profile_read(self):
+        out = {}
+        for k, name in enumerate(KERNEL_CLASSES):
+            ms = C.c_double()
+            n = C.c_int64()
+            self._check(self.b.fn["profile_read"](self.h, k, C.byref(ms), C.byref(n)), "profile_read")
+            out[name] = (float(ms.value), int(n.value))
+        return out
+
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        self._check(self.b.fn["launch_count"](self.h, C.byref(n)), "launch_count")
+        return int(n.value)
+
+    def timer_start(self):
+        self._check(self.b.fn["timer_start"](self.h), "timer_start")
+
+    def timer_stop(self) -> float:
+        ms = C.c_double()
+        self._check(self.b.fn["timer_stop"](self.h, C.byref(ms)), "timer_stop")
+        return float(ms.value)

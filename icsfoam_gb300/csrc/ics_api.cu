@@ -27,7 +27,41 @@ struct ics_handle_s {
 
 namespace ics {
 double rho_l2(Handle& h);
+
+constexpr size_t EV_POOL = 8192;  // events; folded into the totals when full
+
+// fold recorded event pairs into per-class totals (synchronises the stream)
+static void prof_fold(Handle& h) {
+  if (h.evUsed == 0) return;
+  ICS_CUDA(cudaStreamSynchronize(h.stream));
+  for (size_t p = 0; p < h.evKind.size(); ++p) {
+    float t = 0;
+    ICS_CUDA(cudaEventElapsedTime(&t, h.evPool[2 * p], h.evPool[2 * p + 1]));
+    h.profMs[h.evKind[p]] += t;
+    h.profN[h.evKind[p]] += 1;
+  }
+  h.evUsed = 0;
+  h.evKind.clear();
 }
+
+Launch::Launch(Handle& hh, int k) : h(hh), kind(k) {
+  h.launches++;
+  if (!h.prof) return;
+  if (h.evPool.empty()) {
+    h.evPool.resize(EV_POOL);
+    for (auto& e : h.evPool) ICS_CUDA(cudaEventCreate(&e));
+  }
+  if (h.evUsed + 2 > h.evPool.size()) prof_fold(h);
+  ICS_CUDA(cudaEventRecord(h.evPool[h.evUsed], h.stream));
+  stop = h.evPool[h.evUsed + 1];
+  h.evKind.push_back(k);
+  h.evUsed += 2;
+}
+
+Launch::~Launch() {
+  if (stop) cudaEventRecord(stop, h.stream);
+}
+}  // namespace ics
 
 namespace {
 
@@ -62,6 +96,9 @@ void free_all(Handle& h) {
                   h.dginv, h.rD, h.kv, h.kw, h.kx, h.kb, h.kt, h.dW, h.partials, h.counter, h.ks, h.scratch,
                   h.ibuf};
   for (void* p : ptrs) dfree(p);
+  for (cudaEvent_t e : h.evPool) cudaEventDestroy(e);
+  if (h.tStart) cudaEventDestroy(h.tStart);
+  if (h.tStop) cudaEventDestroy(h.tStop);
   if (h.ksHost) cudaFreeHost(h.ksHost);
   if (h.stream) cudaStreamDestroy(h.stream);
 }
@@ -867,6 +904,67 @@ int ics_begin_time_step(ics_handle hh) {
       ICS_CUDA(cudaMemcpyAsync(h.pseudoCo, co.data(), co.size() * sizeof(double), cudaMemcpyHostToDevice, h.stream));
     }
     ICS_CUDA(cudaStreamSynchronize(h.stream));
+    return ICS_OK;
+  });
+}
+
+int ics_profile(ics_handle hh, int32_t enable) {
+  return guard(hh, [&](Handle& h) {
+    if (enable) {
+      ICS_CUDA(cudaStreamSynchronize(h.stream));
+      h.evUsed = 0;
+      h.evKind.clear();
+      for (int k = 0; k < ICS_K_COUNT; ++k) {
+        h.profMs[k] = 0;
+        h.profN[k] = 0;
+      }
+      h.prof = true;
+    } else {
+      h.prof = false;
+      prof_fold(h);
+    }
+    return ICS_OK;
+  });
+}
+
+int ics_profile_read(ics_handle hh, int32_t kind, double* ms, int64_t* launches) {
+  if (kind < 0 || kind >= ICS_K_COUNT) return ICS_ERR_ARG;
+  return guard(hh, [&](Handle& h) {
+    prof_fold(h);
+    if (ms) *ms = h.profMs[kind];
+    if (launches) *launches = h.profN[kind];
+    return ICS_OK;
+  });
+}
+
+int ics_launch_count(ics_handle hh, int64_t* launches) {
+  if (!launches) return ICS_ERR_ARG;
+  return guard(hh, [&](Handle& h) {
+    *launches = h.launches;
+    return ICS_OK;
+  });
+}
+
+int ics_timer_start(ics_handle hh) {
+  return guard(hh, [&](Handle& h) {
+    if (!h.tStart) {
+      ICS_CUDA(cudaEventCreate(&h.tStart));
+      ICS_CUDA(cudaEventCreate(&h.tStop));
+    }
+    ICS_CUDA(cudaEventRecord(h.tStart, h.stream));
+    return ICS_OK;
+  });
+}
+
+int ics_timer_stop(ics_handle hh, double* ms) {
+  if (!ms) return ICS_ERR_ARG;
+  return guard(hh, [&](Handle& h) {
+    if (!h.tStart) return ICS_ERR_STATE;
+    ICS_CUDA(cudaEventRecord(h.tStop, h.stream));
+    ICS_CUDA(cudaEventSynchronize(h.tStop));
+    float t = 0;
+    ICS_CUDA(cudaEventElapsedTime(&t, h.tStart, h.tStop));
+    *ms = t;
     return ICS_OK;
   });
 }

@@ -167,6 +167,24 @@ struct Handle {
   // scratch
   double* scratch = nullptr;  // generic [N*5] doubles
   int* ibuf = nullptr;        // [N] flags
+  // measurement
+  long long launches = 0;
+  bool prof = false;
+  std::vector<cudaEvent_t> evPool;
+  size_t evUsed = 0;
+  std::vector<int> evKind;  // kind of each recorded pair
+  double profMs[ICS_K_COUNT] = {};
+  long long profN[ICS_K_COUNT] = {};
+  cudaEvent_t tStart = nullptr, tStop = nullptr;
+};
+
+// Times one kernel launch of class `kind` when profiling is on; counts it always.
+struct Launch {
+  Handle& h;
+  int kind;
+  cudaEvent_t stop = nullptr;
+  Launch(Handle& hh, int k);
+  ~Launch();
 };
 
 // ------------------------------------------------------------------ kernels
@@ -204,6 +222,13 @@ struct CudaError {
   int line;
   CudaError(cudaError_t e_, const char* w, const char* f, int l) : e(e_), what(w), file(f), line(l) {}
 };
+
+// launch a kernel as class `kind` (timed when profiling is on)
+#define ICS_LAUNCH(hnd, kind, ...)    \
+  do {                                \
+    ::ics::Launch ics_l_((hnd), kind); \
+    __VA_ARGS__;                      \
+  } while (0)
 
 inline int grid_for(long n, int bs) {
   long g = (n + bs - 1) / bs;

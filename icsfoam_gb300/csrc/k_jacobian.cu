@@ -277,23 +277,23 @@ __global__ void k_jacobi_inverse(int N, const T* __restrict__ dg, T* __restrict_
 
 void launch_jacobian(Handle& h) {
   if (h.m.B > 0)
-    k_jac_boundary<<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, h.cfg.c.R, h.cfg.Cv, h.cfg.gamma, h.W, h.prim,
-                                                                h.pB, h.TB, h.UB, h.phiB, h.flam, h.bjac);
+    ICS_LAUNCH(h, ICS_K_JAC_BOUNDARY, k_jac_boundary<<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, h.cfg.c.R, h.cfg.Cv, h.cfg.gamma, h.W, h.prim,
+                                                                h.pB, h.TB, h.UB, h.phiB, h.flam, h.bjac));
   int* status = &h.ks->status;
   if (prec(h) == ICS_PREC_MIXED) {
-    k_jac_rows<float><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, h.cfg.gamma, h.frec, h.flam, h.bjac,
+    ICS_LAUNCH(h, ICS_K_JAC_ROWS, k_jac_rows<float><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, h.cfg.gamma, h.frec, h.flam, h.bjac,
                                                                    h.ddtCoeff, (float*)h.blk, (float*)h.dg,
-                                                                   (float*)h.rD, status);
+                                                                   (float*)h.rD, status));
     if (h.cfg.c.preconditioner == ICS_PC_JACOBI)
-      k_jacobi_inverse<float><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m.N, (float*)h.dg, (float*)h.dginv,
-                                                                          status);
+      ICS_LAUNCH(h, ICS_K_JACOBI_INV, k_jacobi_inverse<float><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m.N, (float*)h.dg, (float*)h.dginv,
+                                                                          status));
   } else {
-    k_jac_rows<double><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, h.cfg.gamma, h.frec, h.flam, h.bjac,
+    ICS_LAUNCH(h, ICS_K_JAC_ROWS, k_jac_rows<double><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, h.cfg.gamma, h.frec, h.flam, h.bjac,
                                                                     h.ddtCoeff, (double*)h.blk, (double*)h.dg,
-                                                                    (double*)h.rD, status);
+                                                                    (double*)h.rD, status));
     if (h.cfg.c.preconditioner == ICS_PC_JACOBI)
-      k_jacobi_inverse<double><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m.N, (double*)h.dg, (double*)h.dginv,
-                                                                           status);
+      ICS_LAUNCH(h, ICS_K_JACOBI_INV, k_jacobi_inverse<double><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m.N, (double*)h.dg, (double*)h.dginv,
+                                                                           status));
   }
   ICS_CUDA(cudaGetLastError());
   h.jacPrecision = prec(h);

@@ -393,7 +393,7 @@ __global__ void __launch_bounds__(RB) k_sumsq(int N, const double* __restrict__ 
 // -------------------------------------------------------------- dispatch
 template <typename TB, typename TV>
 static void spmv_t(Handle& h, const TV* x, TV* y) {
-  k_spmv<TB, TV><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, (const TB*)h.blk, (const TB*)h.dg, x, y);
+  ICS_LAUNCH(h, ICS_K_SPMV, k_spmv<TB, TV><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, (const TB*)h.blk, (const TB*)h.dg, x, y));
 }
 
 
@@ -404,23 +404,23 @@ static void lusgs_t(Handle& h, TV* r) {
   const TB* rD = (const TB*)h.rD;
   // forward sweep, then reverse sweep; many small levels run in one CTA
   if ((long)m.N < 2048L * m.nfl) {
-    k_lusgs_block<TB, TV, true><<<1, 1024, 0, h.stream>>>(m, blk, rD, r, m.fl_cells, m.fl_lptr, m.nfl);
+    ICS_LAUNCH(h, ICS_K_LUSGS_FWD, k_lusgs_block<TB, TV, true><<<1, 1024, 0, h.stream>>>(m, blk, rD, r, m.fl_cells, m.fl_lptr, m.nfl));
   } else {
     for (int l = 0; l < m.nfl; ++l) {
       const int a = m.fl_ptr[l], cnt = m.fl_ptr[l + 1] - a;
       const bool contig = m.fl_cstart[l] >= 0;
-      k_lusgs_level<TB, TV, true><<<grid_for(cnt, 128), 128, 0, h.stream>>>(
-          m, blk, rD, r, contig ? nullptr : m.fl_cells, contig ? m.fl_cstart[l] : a, cnt);
+      ICS_LAUNCH(h, ICS_K_LUSGS_FWD, k_lusgs_level<TB, TV, true><<<grid_for(cnt, 128), 128, 0, h.stream>>>(
+          m, blk, rD, r, contig ? nullptr : m.fl_cells, contig ? m.fl_cstart[l] : a, cnt));
     }
   }
   if ((long)m.N < 2048L * m.nrl) {
-    k_lusgs_block<TB, TV, false><<<1, 1024, 0, h.stream>>>(m, blk, rD, r, m.rl_cells, m.rl_lptr, m.nrl);
+    ICS_LAUNCH(h, ICS_K_LUSGS_REV, k_lusgs_block<TB, TV, false><<<1, 1024, 0, h.stream>>>(m, blk, rD, r, m.rl_cells, m.rl_lptr, m.nrl));
   } else {
     for (int l = 0; l < m.nrl; ++l) {
       const int a = m.rl_ptr[l], cnt = m.rl_ptr[l + 1] - a;
       const bool contig = m.rl_cstart[l] >= 0;
-      k_lusgs_level<TB, TV, false><<<grid_for(cnt, 128), 128, 0, h.stream>>>(
-          m, blk, rD, r, contig ? nullptr : m.rl_cells, contig ? m.rl_cstart[l] : a, cnt);
+      ICS_LAUNCH(h, ICS_K_LUSGS_REV, k_lusgs_level<TB, TV, false><<<grid_for(cnt, 128), 128, 0, h.stream>>>(
+          m, blk, rD, r, contig ? nullptr : m.rl_cells, contig ? m.rl_cstart[l] : a, cnt));
     }
   }
 }
@@ -430,7 +430,7 @@ static void precondition_t(Handle& h, TV* r) {
   if (h.cfg.c.preconditioner == ICS_PC_LUSGS)
     lusgs_t<TB, TV>(h, r);
   else if (h.cfg.c.preconditioner == ICS_PC_JACOBI)
-    k_jacobi_apply<TB, TV><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m.N, (const TB*)h.dginv, r);
+    ICS_LAUNCH(h, ICS_K_JACOBI, k_jacobi_apply<TB, TV><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m.N, (const TB*)h.dginv, r));
 }
 
 void spmv(Handle& h, const void* x, void* y) {
@@ -453,7 +453,7 @@ int precondition(Handle& h, void* r) {
 void to_vec(Handle& h, const double* src, void* dst) {
   const long n = 5L * h.m.N;
   if (prec(h) == ICS_PREC_MIXED)
-    k_cast<double, float><<<REDUCE_BLOCKS, RB, 0, h.stream>>>(n, src, (float*)dst);
+    ICS_LAUNCH(h, ICS_K_VECTOR, k_cast<double, float><<<REDUCE_BLOCKS, RB, 0, h.stream>>>(n, src, (float*)dst));
   else
     ICS_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
 }
@@ -461,7 +461,7 @@ void to_vec(Handle& h, const double* src, void* dst) {
 void from_vec(Handle& h, const void* src, double* dst) {
   const long n = 5L * h.m.N;
   if (prec(h) == ICS_PREC_MIXED)
-    k_cast<float, double><<<REDUCE_BLOCKS, RB, 0, h.stream>>>(n, (const float*)src, dst);
+    ICS_LAUNCH(h, ICS_K_VECTOR, k_cast<float, double><<<REDUCE_BLOCKS, RB, 0, h.stream>>>(n, (const float*)src, dst));
   else
     ICS_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
 }
@@ -492,11 +492,11 @@ static int gmres_t(Handle& h, ics_solver_perf* perf) {
   double* red = ks->red;
   ICS_CUDA(cudaMemsetAsync(&ks->status, 0, sizeof(int), st));
   // norm factors: A (W - avg(W))
-  k_wsum<<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.W, h.partials, h.counter, red);
-  k_avg<<<1, 1, 0, st>>>(ks, N);
-  k_wmavg<TV><<<grid_for(N, 256), 256, 0, st>>>(N, h.W, ks, w);
+  ICS_LAUNCH(h, ICS_K_VECTOR, k_wsum<<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.W, h.partials, h.counter, red));
+  ICS_LAUNCH(h, ICS_K_SCALAR, k_avg<<<1, 1, 0, st>>>(ks, N));
+  ICS_LAUNCH(h, ICS_K_VECTOR, k_wmavg<TV><<<grid_for(N, 256), 256, 0, st>>>(N, h.W, ks, w));
   spmv_t<TB, TV>(h, w, t);
-  k_normfac<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.src, t, h.partials, h.counter, red);
+  ICS_LAUNCH(h, ICS_K_VECTOR, k_normfac<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.src, t, h.partials, h.counter, red));
   ICS_CUDA(cudaMemcpyAsync(h.ksHost->red, red, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
   ICS_CUDA(cudaStreamSynchronize(st));
   double nf[3];
@@ -515,28 +515,28 @@ static int gmres_t(Handle& h, ics_solver_perf* perf) {
   int status = ICS_OK;
   do {
     precondition_t<TB, TV>(h, w);
-    k_mgs<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, w, nullptr, nullptr, nullptr, &ks->status, h.partials, h.counter,
-                                            red);
-    k_beta0<<<1, 1, 0, st>>>(ks, m);
+    ICS_LAUNCH(h, ICS_K_MGS, k_mgs<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, w, nullptr, nullptr, nullptr, &ks->status, h.partials, h.counter,
+                                            red));
+    ICS_LAUNCH(h, ICS_K_SCALAR, k_beta0<<<1, 1, 0, st>>>(ks, m));
     for (int i = 0; i < m; ++i) {
       TV* vi = V + (size_t)i * n5;
-      k_scale<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, w, vi, ks);
+      ICS_LAUNCH(h, ICS_K_VECTOR, k_scale<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, w, vi, ks));
       spmv_t<TB, TV>(h, vi, w);
       precondition_t<TB, TV>(h, w);
       for (int j = 0; j <= i; ++j) {
         const TV* vprev = j > 0 ? V + (size_t)(j - 1) * n5 : nullptr;
         const double* hprev = j > 0 ? &ks->H[(j - 1) * m + i] : nullptr;
-        k_mgs<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, w, vprev, hprev, V + (size_t)j * n5, &ks->status, h.partials,
-                                                h.counter, &ks->H[j * m + i]);
+        ICS_LAUNCH(h, ICS_K_MGS, k_mgs<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, w, vprev, hprev, V + (size_t)j * n5, &ks->status, h.partials,
+                                                h.counter, &ks->H[j * m + i]));
       }
-      k_mgs<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, w, vi, &ks->H[i * m + i], nullptr, &ks->status, h.partials,
-                                              h.counter, &red[1]);
-      k_hess<<<1, 1, 0, st>>>(ks, i, m);
+      ICS_LAUNCH(h, ICS_K_MGS, k_mgs<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, w, vi, &ks->H[i * m + i], nullptr, &ks->status, h.partials,
+                                              h.counter, &red[1]));
+      ICS_LAUNCH(h, ICS_K_SCALAR, k_hess<<<1, 1, 0, st>>>(ks, i, m));
     }
-    k_backsub<<<1, 1, 0, st>>>(ks, m);
-    k_xupdate<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, x, V, ks, m);
+    ICS_LAUNCH(h, ICS_K_SCALAR, k_backsub<<<1, 1, 0, st>>>(ks, m));
+    ICS_LAUNCH(h, ICS_K_VECTOR, k_xupdate<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, x, V, ks, m));
     spmv_t<TB, TV>(h, x, t);
-    k_resid<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.src, t, w, h.partials, h.counter, ks->res);
+    ICS_LAUNCH(h, ICS_K_VECTOR, k_resid<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.src, t, w, h.partials, h.counter, ks->res));
     ICS_CUDA(cudaGetLastError());
     ICS_CUDA(cudaMemcpyAsync(h.ksHost->res, ks->res, 5 * sizeof(double), cudaMemcpyDeviceToHost, st));
     ICS_CUDA(cudaMemcpyAsync(&h.ksHost->status, &ks->status, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -559,7 +559,7 @@ static int gmres_t(Handle& h, ics_solver_perf* perf) {
     }
   } while (!stop_test(h, p));
   p.converged = status == ICS_OK;
-  k_to_dW<TV><<<grid_for(N, 256), 256, 0, st>>>(N, x, h.dW, h.m.solD[0], h.m.solD[1], h.m.solD[2]);
+  ICS_LAUNCH(h, ICS_K_VECTOR, k_to_dW<TV><<<grid_for(N, 256), 256, 0, st>>>(N, x, h.dW, h.m.solD[0], h.m.solD[1], h.m.solD[2]));
   ICS_CUDA(cudaGetLastError());
   *perf = p;
   return status;
@@ -572,7 +572,7 @@ int gmres_solve(Handle& h, ics_solver_perf* perf) {
 
 // rho L2 residual: sqrt(sum (div(phi) V)^2) from the per-cell squares
 double rho_l2(Handle& h) {
-  k_sumsq<<<REDUCE_BLOCKS, RB, 0, h.stream>>>(h.m.N, h.scratch, h.partials, h.counter, &h.ks->l2);
+  ICS_LAUNCH(h, ICS_K_VECTOR, k_sumsq<<<REDUCE_BLOCKS, RB, 0, h.stream>>>(h.m.N, h.scratch, h.partials, h.counter, &h.ks->l2));
   double v = 0;
   ICS_CUDA(cudaMemcpyAsync(&v, &h.ks->l2, sizeof(double), cudaMemcpyDeviceToHost, h.stream));
   ICS_CUDA(cudaStreamSynchronize(h.stream));

@@ -429,8 +429,8 @@ static ResParams res_params(const Handle& h) {
 
 void launch_fields(Handle& h) {
   const int n = h.m.N > h.m.B ? h.m.N : h.m.B;
-  k_fields<<<grid_for(n, 256), 256, 0, h.stream>>>(h.m.N, h.m.B, h.W, h.prim, h.pB, h.TB, h.UB, res_params(h), h.q,
-                                                   h.bq, h.clin, h.clin + h.m.N);
+  ICS_LAUNCH(h, ICS_K_FIELDS, k_fields<<<grid_for(n, 256), 256, 0, h.stream>>>(h.m.N, h.m.B, h.W, h.prim, h.pB, h.TB, h.UB, res_params(h), h.q,
+                                                   h.bq, h.clin, h.clin + h.m.N));
   ICS_CUDA(cudaGetLastError());
 }
 
@@ -467,11 +467,11 @@ void launch_grad(Handle& h) {
   }
   const int bs = 128;
   if (limited == 2)
-    k_grad<2><<<grid_for(h.m.N, bs), bs, 0, h.stream>>>(h.m, h.q, h.bq, mask, h.grad);
+    ICS_LAUNCH(h, ICS_K_GRAD, k_grad<2><<<grid_for(h.m.N, bs), bs, 0, h.stream>>>(h.m, h.q, h.bq, mask, h.grad));
   else if (limited == 1)
-    k_grad<1><<<grid_for(h.m.N, bs), bs, 0, h.stream>>>(h.m, h.q, h.bq, mask, h.grad);
+    ICS_LAUNCH(h, ICS_K_GRAD, k_grad<1><<<grid_for(h.m.N, bs), bs, 0, h.stream>>>(h.m, h.q, h.bq, mask, h.grad));
   else
-    k_grad<0><<<grid_for(h.m.N, bs), bs, 0, h.stream>>>(h.m, h.q, h.bq, mask, h.grad);
+    ICS_LAUNCH(h, ICS_K_GRAD, k_grad<0><<<grid_for(h.m.N, bs), bs, 0, h.stream>>>(h.m, h.q, h.bq, mask, h.grad));
   ICS_CUDA(cudaGetLastError());
 }
 
@@ -479,11 +479,11 @@ void launch_face_flux(Handle& h) {
   const int FB = h.m.F + h.m.B;
   const ResParams P = res_params(h);
   if (h.m.F > 0)
-    k_face<<<grid_for(h.m.F, 128), 128, 0, h.stream>>>(h.m, P, h.q, h.grad, h.clin, h.m.nf, h.fflux,
-                                                        h.frec, h.flam, FB);
+    ICS_LAUNCH(h, ICS_K_FACE, k_face<<<grid_for(h.m.F, 128), 128, 0, h.stream>>>(h.m, P, h.q, h.grad, h.clin, h.m.nf, h.fflux,
+                                                        h.frec, h.flam, FB));
   if (h.m.B > 0)
-    k_bface<<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, P, h.bq, h.clin + h.m.N, h.m.bnf, h.fflux,
-                                                         h.flam, h.phiB, FB);
+    ICS_LAUNCH(h, ICS_K_BFACE, k_bface<<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, P, h.bq, h.clin + h.m.N, h.m.bnf, h.fflux,
+                                                         h.flam, h.phiB, FB));
   ICS_CUDA(cudaGetLastError());
 }
 
@@ -506,8 +506,8 @@ void launch_residual(Handle& h, double serRatio, bool applySer) {
   D.coMin = h.cfg.c.pseudo_co_num_min;
   D.coMax = h.cfg.c.pseudo_co_num_max;
   const int FB = h.m.F + h.m.B;
-  k_cellres<<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, D, h.fflux, FB, h.flam, h.W, h.W0, h.W00, h.prim,
-                                                         h.clin, h.pseudoCo, h.rPDT, h.ddtCoeff, h.src, h.scratch);
+  ICS_LAUNCH(h, ICS_K_CELLRES, k_cellres<<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, D, h.fflux, FB, h.flam, h.W, h.W0, h.W00, h.prim,
+                                                         h.clin, h.pseudoCo, h.rPDT, h.ddtCoeff, h.src, h.scratch));
   ICS_CUDA(cudaGetLastError());
 }
 

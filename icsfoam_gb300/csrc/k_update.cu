@@ -218,40 +218,40 @@ void launch_update(Handle& h, int* boundedDev) {
   const double eMin = h.cfg.Cv * c.T_min;
   const double eMax = h.cfg.Cv * c.T_max;
   const int useTMax = c.T_max < GREAT ? 1 : 0;
-  k_update<<<grid_for(h.m.N, 256), 256, 0, h.stream>>>(h.m.N, h.W, h.dW, h.prim, c.R, h.cfg.Cv, c.rho_min, eMin, eMax,
-                                                        useTMax, boundedDev);
+  ICS_LAUNCH(h, ICS_K_UPDATE, k_update<<<grid_for(h.m.N, 256), 256, 0, h.stream>>>(h.m.N, h.W, h.dW, h.prim, c.R, h.cfg.Cv, c.rho_min, eMin, eMax,
+                                                        useTMax, boundedDev));
   ICS_CUDA(cudaGetLastError());
 }
 
 void launch_bc(Handle& h) {
   if (!h.m.B) return;
   const ics_config& c = h.cfg.c;
-  k_bc<<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, h.prim, h.pB, h.TB, h.UB, h.phiB, c.R, h.cfg.gamma, c.T_min,
-                                                    c.T_max, c.T_max < GREAT ? 1 : 0);
+  ICS_LAUNCH(h, ICS_K_BC, k_bc<<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, h.prim, h.pB, h.TB, h.UB, h.phiB, c.R, h.cfg.gamma, c.T_min,
+                                                    c.T_max, c.T_max < GREAT ? 1 : 0));
   ICS_CUDA(cudaGetLastError());
 }
 
 void launch_set_primitive(Handle& h) {
   // staged inputs: scratch holds p (N), U (3N), T (N)
   const int N = h.m.N;
-  k_set_primitive<<<grid_for(N, 256), 256, 0, h.stream>>>(N, h.cfg.c.R, h.cfg.Cv, h.scratch, h.scratch + N,
-                                                           h.scratch + 4 * N, h.W, h.prim);
+  ICS_LAUNCH(h, ICS_K_UPDATE, k_set_primitive<<<grid_for(N, 256), 256, 0, h.stream>>>(N, h.cfg.c.R, h.cfg.Cv, h.scratch, h.scratch + N,
+                                                           h.scratch + 4 * N, h.W, h.prim));
   if (h.m.B)
-    k_bc_init<<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, h.prim, h.cfg.c.R, h.pB, h.TB, h.UB, h.phiB);
+    ICS_LAUNCH(h, ICS_K_BC, k_bc_init<<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, h.prim, h.cfg.c.R, h.pB, h.TB, h.UB, h.phiB));
   ICS_CUDA(cudaGetLastError());
   launch_bc(h);
 }
 
 void launch_derive_primitive(Handle& h) {
-  k_derive<<<grid_for(h.m.N, 256), 256, 0, h.stream>>>(h.m.N, h.W, h.prim, h.cfg.c.R, h.cfg.Cv);
+  ICS_LAUNCH(h, ICS_K_UPDATE, k_derive<<<grid_for(h.m.N, 256), 256, 0, h.stream>>>(h.m.N, h.W, h.prim, h.cfg.c.R, h.cfg.Cv));
   ICS_CUDA(cudaGetLastError());
 }
 
 void launch_bound_local_timestep(Handle& h) {
   const ics_config& c = h.cfg.c;
   if (!c.local_timestepping || !c.local_timestepping_bounding) return;
-  k_bad<<<grid_for(h.m.N, 256), 256, 0, h.stream>>>(h.m.N, h.W, h.Wprev, c.local_timestepping_lower_bound, h.ibuf);
-  k_bound_factor<<<grid_for(h.m.N, 256), 256, 0, h.stream>>>(h.m, h.ibuf, h.pseudoCo);
+  ICS_LAUNCH(h, ICS_K_BOUND, k_bad<<<grid_for(h.m.N, 256), 256, 0, h.stream>>>(h.m.N, h.W, h.Wprev, c.local_timestepping_lower_bound, h.ibuf));
+  ICS_LAUNCH(h, ICS_K_BOUND, k_bound_factor<<<grid_for(h.m.N, 256), 256, 0, h.stream>>>(h.m, h.ibuf, h.pseudoCo));
   ICS_CUDA(cudaGetLastError());
 }
 

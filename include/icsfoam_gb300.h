@@ -220,6 +220,25 @@ int ics_begin_time_step(ics_handle h);
  * *more while the pseudo loop should run another iteration.                 */
 int ics_pseudo_loop(ics_handle h, int32_t* more);
 
+/* ---- measurement (no counterpart in the reference, which has only Info logs) */
+/* kernel classes timed by ics_profile_read                                  */
+enum {
+  ICS_K_FIELDS = 0, ICS_K_GRAD, ICS_K_FACE, ICS_K_BFACE, ICS_K_CELLRES, ICS_K_JAC_BOUNDARY, ICS_K_JAC_ROWS,
+  ICS_K_JACOBI_INV, ICS_K_SPMV, ICS_K_LUSGS_FWD, ICS_K_LUSGS_REV, ICS_K_JACOBI, ICS_K_MGS, ICS_K_VECTOR,
+  ICS_K_SCALAR, ICS_K_UPDATE, ICS_K_BC, ICS_K_BOUND, ICS_K_COUNT
+};
+/* Start (enable=1) or stop (0) recording a CUDA event pair around every
+ * kernel launch on the handle's stream; starting clears previous records.  */
+int ics_profile(ics_handle h, int32_t enable);
+/* Accumulated device time (ms) and launch count of one kernel class.        */
+int ics_profile_read(ics_handle h, int32_t kind, double* ms, int64_t* launches);
+/* Total kernels launched by the handle since creation.                      */
+int ics_launch_count(ics_handle h, int64_t* launches);
+/* Device timer on the handle's stream: start records an event, stop records
+ * a second one, synchronises and returns the elapsed milliseconds.          */
+int ics_timer_start(ics_handle h);
+int ics_timer_stop(ics_handle h, double* ms);
+
 #ifdef __cplusplus
 }
 #endif

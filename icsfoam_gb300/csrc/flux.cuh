@@ -80,9 +80,10 @@ __device__ __forceinline__ void flux_ausm(const FState& L, const FState& R, cons
 __device__ __forceinline__ void flux_hllc(const FState& L, const FState& R, const double n[3], double magS,
                                           double gInterp, double out[5]) {
   const double coefR = sqrt(fmax(VSMALL, R.rho) / fmax(VSMALL, L.rho));
+  const double icr = 1.0 / (coefR + 1.0);  // one FP64 reciprocal for the four Roe averages
   double uAvg[3];
-  for (int k = 0; k < 3; ++k) uAvg[k] = (coefR * R.U[k] + L.U[k]) / (coefR + 1.0);
-  const double HAvg = (coefR * R.H + L.H) / (coefR + 1.0);
+  for (int k = 0; k < 3; ++k) uAvg[k] = (coefR * R.U[k] + L.U[k]) * icr;
+  const double HAvg = (coefR * R.H + L.H) * icr;
   const double cAvg = sqrt(fabs((gInterp - 1.0) * (HAvg - 0.5 * dot3(uAvg, uAvg))));
   const double uMag_l = dot3(L.U, n) - 0.0;
   const double uMag_r = dot3(R.U, n) - 0.0;
@@ -130,8 +131,9 @@ __device__ __forceinline__ void flux_roe(const FState& L, const FState& R, const
   const double coefR = sqrt(fmax(VSMALL, R.rho) / fmax(VSMALL, L.rho));
   const double rD = coefR * L.rho;
   double rU[3];
-  for (int k = 0; k < 3; ++k) rU[k] = (coefR * R.U[k] + L.U[k]) / (coefR + 1.0);
-  const double rH = (coefR * R.H + L.H) / (coefR + 1.0);
+  const double icr = 1.0 / (coefR + 1.0);
+  for (int k = 0; k < 3; ++k) rU[k] = (coefR * R.U[k] + L.U[k]) * icr;
+  const double rH = (coefR * R.H + L.H) * icr;
   const double rC = sqrt(fabs((gI - 1.0) * (rH - 0.5 * dot3(rU, rU))));
   const double uMag_l = dot3(L.U, n), uMag_r = dot3(R.U, n);
   const double uProj = dot3(rU, n) - 0.0;

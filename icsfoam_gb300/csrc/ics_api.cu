@@ -163,6 +163,7 @@ int validate_config(const ics_config* c, std::string& err) {
 
 // Krylov and Jacobian storage sized for the current precision / nDirections
 void ensure_workspace(Handle& h) {
+  // Krylov vectors start on 256-byte boundaries (vectorised 16-byte access)
   const int p = prec(h);
   const int m = h.cfg.c.n_directions;
   const size_t eb = p == ICS_PREC_MIXED ? 4 : 8;
@@ -178,13 +179,13 @@ void ensure_workspace(Handle& h) {
     h.kx = dalloc<char>(n5 * eb);
     h.kb = dalloc<char>(n5 * eb);
     h.kt = dalloc<char>(n5 * eb);
-    h.kv = dalloc<char>(n5 * eb * m);
+    h.kv = dalloc<char>(kstride(h) * eb * m);
     h.kvDirs = m;
     h.kvPrec = p;
     h.haveMatrix = false;
   } else if (h.kvDirs < m) {
     dfree(h.kv);
-    h.kv = dalloc<char>(n5 * eb * m);
+    h.kv = dalloc<char>(kstride(h) * eb * m);
     h.kvDirs = m;
   }
 }

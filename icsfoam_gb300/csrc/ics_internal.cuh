@@ -36,7 +36,7 @@ constexpr double VGREAT = 1e300;
 enum { Q_RHO = 0, Q_P = 1, Q_UX = 2, Q_UY = 3, Q_UZ = 4, Q_E = 5, Q_H = 6, Q_C = 7, NQ = 8 };
 
 constexpr int SLICE = 32;
-constexpr int REDUCE_BLOCKS = 608;  // 4 x 152 SMs
+constexpr int REDUCE_BLOCKS = 1216;  // 8 x 152 SMs
 constexpr int MAX_DIRS = 64;
 
 // Scalars living in device memory for the Krylov cycle (one per handle).
@@ -207,6 +207,8 @@ void to_vec(Handle& h, const double* src, void* dst);   // FP64 -> Krylov type
 void from_vec(Handle& h, const void* src, double* dst); // Krylov type -> FP64
 
 inline int prec(const Handle& h) { return h.cfg.c.precision; }
+// element stride between consecutive Krylov basis vectors (5N rounded up to 64)
+inline size_t kstride(const Handle& h) { return ((5ull * h.m.N + 63) / 64) * 64; }
 inline size_t vbytes(const Handle& h) { return prec(h) == ICS_PREC_MIXED ? 4 : 8; }
 
 #define ICS_CUDA(call)                                                    \

@@ -21,8 +21,9 @@
 namespace ics {
 
 // ------------------------------------------------------------------ reduce
+// Returns true on the one thread (thread 0 of the last block) that wrote out[].
 template <int NV>
-__device__ __forceinline__ void reduce_finish(double (&v)[NV], double* __restrict__ partials,
+__device__ __forceinline__ bool reduce_finish(double (&v)[NV], double* __restrict__ partials,
                                               unsigned int* __restrict__ counter, double* __restrict__ out) {
   __shared__ double sm[32][NV];
   __shared__ bool amLast;
@@ -47,18 +48,69 @@ __device__ __forceinline__ void reduce_finish(double (&v)[NV], double* __restric
     amLast = (t == gridDim.x - 1);
   }
   __syncthreads();
-  if (amLast && threadIdx.x < NV) {
+  if (amLast) {  // block-uniform: the last block folds all partials in a fixed order
     __threadfence();
-    const int k = threadIdx.x;
-    double s = 0;
     const volatile double* vp = partials;
-    for (int b = 0; b < (int)gridDim.x; ++b) s += vp[b * NV + k];
-    out[k] = s;
+    double acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+#pragma unroll
+      for (int k = 0; k < NV; ++k) acc[k] += vp[b * NV + k];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double x = acc[k];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      if (lane == 0) sm[warp][k] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int nw = blockDim.x >> 5;
+      for (int k = 0; k < NV; ++k) {
+        double s = 0;
+        for (int w = 0; w < nw; ++w) s += sm[w][k];
+        out[k] = s;
+      }
+      *counter = 0;
+      return true;
+    }
   }
-  if (amLast && threadIdx.x == 0) *counter = 0;
+  return false;
 }
 
 constexpr int RB = 256;  // threads per reduction block
+
+// 16-byte vector of the Krylov element type
+template <typename TV>
+struct V16;
+template <>
+struct V16<float> {
+  using T = float4;
+  static constexpr int n = 4;
+  __device__ static float get(const T& v, int k) { return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w; }
+};
+template <>
+struct V16<double> {
+  using T = double2;
+  static constexpr int n = 2;
+  __device__ static double get(const T& v, int k) { return k == 0 ? v.x : v.y; }
+};
+
+__device__ __forceinline__ void axpy16(float4& x, float h, const float4& p) {
+  x.x -= h * p.x;
+  x.y -= h * p.y;
+  x.z -= h * p.z;
+  x.w -= h * p.w;
+}
+__device__ __forceinline__ void axpy16(double2& x, double h, const double2& p) {
+  x.x -= h * p.x;
+  x.y -= h * p.y;
+}
+__device__ __forceinline__ double dot16(const float4& a, const float4& b) {
+  return double(a.x * b.x) + double(a.y * b.y) + double(a.z * b.z) + double(a.w * b.w);
+}
+__device__ __forceinline__ double dot16(const double2& a, const double2& b) { return a.x * b.x + a.y * b.y; }
 
 // ------------------------------------------------------------------- spmv
 template <typename TB, typename TV>
@@ -215,38 +267,8 @@ __global__ void k_cast(long n, const TS* __restrict__ a, TD* __restrict__ b) {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) b[i] = TD(a[i]);
 }
 
-// w -= hprev * vprev (when vprev), then sum w.vnext (or w.w) -> out
-template <typename TV>
-__global__ void __launch_bounds__(RB) k_mgs(long n, TV* __restrict__ w, const TV* __restrict__ vprev,
-                                            const double* __restrict__ hprev, const TV* __restrict__ vnext,
-                                            const int* __restrict__ status, double* __restrict__ partials,
-                                            unsigned int* __restrict__ counter, double* __restrict__ out) {
-  double acc[1] = {0.0};
-  if (*status == 0) {
-    const TV h = vprev ? TV(*hprev) : TV(0);
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-      TV x = w[i];
-      if (vprev) {
-        x = x - h * vprev[i];
-        w[i] = x;
-      }
-      const TV o = vnext ? vnext[i] : x;
-      acc[0] += double(x * o);
-    }
-  }
-  reduce_finish<1>(acc, partials, counter, out);
-}
-
-template <typename TV>
-__global__ void k_scale(long n, const TV* __restrict__ w, TV* __restrict__ v, const KrylovScalars* __restrict__ ks) {
-  if (ks->status) return;
-  const TV beta = TV(ks->beta);
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-    v[i] = w[i] / beta;
-}
-
 // start of a cycle: beta = sqrt(sum), bh = (beta, 0...)
-__global__ void k_beta0(KrylovScalars* ks, int m) {
+__device__ __forceinline__ void dev_beta0(KrylovScalars* ks, int m) {
   const double beta = sqrt(ks->red[0]);
   ks->beta = beta;
   for (int i = 0; i <= m; ++i) ks->bh[i] = 0.0;
@@ -269,9 +291,10 @@ __device__ __forceinline__ void givens(double h, double beta, double& c, double&
   }
 }
 
-// after MGS of direction i: H[j][i] for j <= i are in H (written by k_mgs),
-// red[1] holds |w|^2
-__global__ void k_hess(KrylovScalars* ks, int i, int m) {
+// after MGS of direction i: H[j][i] for j <= i are in H, red[1] holds |w|^2;
+// rotate column i with the previous Givens rotations and make a new one
+// (gmres.C:1013-1027, rotation gmres.C:44-69)
+__device__ __forceinline__ void dev_hess(KrylovScalars* ks, int i, int m) {
   if (ks->status) return;
   double* H = ks->H;
   const double beta = sqrt(ks->red[1]);
@@ -288,6 +311,81 @@ __global__ void k_hess(KrylovScalars* ks, int i, int m) {
   ks->beta = beta;
 }
 
+// w -= hprev * vprev (when vprev), then sum w.vnext (or w.w) -> out.
+// post = 1: the finishing thread also starts the cycle (dev_beta0);
+// post = 2: it also performs the Hessenberg update of direction i.
+template <typename TV>
+__global__ void __launch_bounds__(RB) k_mgs(long n, TV* __restrict__ w, const TV* __restrict__ vprev,
+                                            const double* __restrict__ hprev, const TV* __restrict__ vnext,
+                                            const int* __restrict__ status, double* __restrict__ partials,
+                                            unsigned int* __restrict__ counter, double* __restrict__ out,
+                                            KrylovScalars* __restrict__ ks, int post, int dir, int m) {
+  double acc[1] = {0.0};
+  if (*status == 0) {
+    const TV h = vprev ? TV(*hprev) : TV(0);
+    using VT = typename V16<TV>::T;
+    constexpr int L = V16<TV>::n;
+    const long nv = n / L;  // 16-byte chunks (vectors start 256-byte aligned)
+    VT* w4 = reinterpret_cast<VT*>(w);
+    const VT* p4 = reinterpret_cast<const VT*>(vprev);
+    const VT* o4 = reinterpret_cast<const VT*>(vnext);
+    const long stride = (long)gridDim.x * blockDim.x;
+#pragma unroll 4
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nv; i += stride) {
+      VT x = w4[i];
+      if (vprev) {
+        axpy16(x, h, p4[i]);
+        w4[i] = x;
+      }
+      acc[0] += dot16(x, vnext ? o4[i] : x);
+    }
+    for (long i = nv * L + blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += stride) {
+      TV x = w[i];
+      if (vprev) {
+        x = x - h * vprev[i];
+        w[i] = x;
+      }
+      const TV o = vnext ? vnext[i] : x;
+      acc[0] += double(x * o);
+    }
+  }
+  if (reduce_finish<1>(acc, partials, counter, out)) {
+    if (post == 1)
+      dev_beta0(ks, m);
+    else if (post == 2)
+      dev_hess(ks, dir, m);
+  }
+}
+
+__device__ __forceinline__ float4 div16(float4 x, float b) { return make_float4(x.x / b, x.y / b, x.z / b, x.w / b); }
+__device__ __forceinline__ double2 div16(double2 x, double b) { return make_double2(x.x / b, x.y / b); }
+__device__ __forceinline__ void addmul16(float4& a, float y, const float4& v) {
+  a.x += y * v.x;
+  a.y += y * v.y;
+  a.z += y * v.z;
+  a.w += y * v.w;
+}
+__device__ __forceinline__ void addmul16(double2& a, double y, const double2& v) {
+  a.x += y * v.x;
+  a.y += y * v.y;
+}
+
+// v = w / beta (gmres.C: sV = sTmp/beta)
+template <typename TV>
+__global__ void k_scale(long n, const TV* __restrict__ w, TV* __restrict__ v, const KrylovScalars* __restrict__ ks) {
+  if (ks->status) return;
+  const TV beta = TV(ks->beta);
+  using VT = typename V16<TV>::T;
+  constexpr int L = V16<TV>::n;
+  const long nv = n / L;
+  const long stride = (long)gridDim.x * blockDim.x;
+  const VT* w4 = reinterpret_cast<const VT*>(w);
+  VT* v4 = reinterpret_cast<VT*>(v);
+#pragma unroll 4
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nv; i += stride) v4[i] = div16(w4[i], beta);
+  for (long i = nv * L + blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += stride) v[i] = w[i] / beta;
+}
+
 __global__ void k_backsub(KrylovScalars* ks, int m) {
   if (ks->status) return;
   for (int i = m - 1; i >= 0; --i) {
@@ -301,11 +399,22 @@ __global__ void k_backsub(KrylovScalars* ks, int m) {
 
 template <typename TV>
 __global__ void k_xupdate(long n, TV* __restrict__ x, const TV* __restrict__ V, const KrylovScalars* __restrict__ ks,
-                          int m) {
+                          int m, long vstride) {
   if (ks->status) return;
-  for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+  using VT = typename V16<TV>::T;
+  constexpr int L = V16<TV>::n;
+  const long nv = n / L;
+  const long stride = (long)gridDim.x * blockDim.x;
+  VT* x4 = reinterpret_cast<VT*>(x);
+  for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nv; q += stride) {
+    VT a = x4[q];
+    for (int i = 0; i < m; ++i)
+      addmul16(a, TV(ks->y[i]), reinterpret_cast<const VT*>(V + (size_t)i * vstride)[q]);
+    x4[q] = a;
+  }
+  for (long q = nv * L + blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += stride) {
     TV a = x[q];
-    for (int i = 0; i < m; ++i) a += TV(ks->y[i]) * V[(size_t)i * n + q];
+    for (int i = 0; i < m; ++i) a += TV(ks->y[i]) * V[(size_t)i * vstride + q];
     x[q] = a;
   }
 }
@@ -483,6 +592,7 @@ template <typename TB, typename TV>
 static int gmres_t(Handle& h, ics_solver_perf* perf) {
   const int N = h.m.N, m = h.cfg.c.n_directions;
   const long n5 = 5L * N;
+  const long vs = (long)kstride(h);
   cudaStream_t st = h.stream;
   KrylovScalars* ks = h.ks;
   TV* V = (TV*)h.kv;
@@ -515,26 +625,27 @@ static int gmres_t(Handle& h, ics_solver_perf* perf) {
   int status = ICS_OK;
   do {
     precondition_t<TB, TV>(h, w);
-    ICS_LAUNCH(h, ICS_K_MGS, k_mgs<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, w, nullptr, nullptr, nullptr, &ks->status, h.partials, h.counter,
-                                            red));
-    ICS_LAUNCH(h, ICS_K_SCALAR, k_beta0<<<1, 1, 0, st>>>(ks, m));
+    ICS_LAUNCH(h, ICS_K_MGS,
+               k_mgs<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, w, nullptr, nullptr, nullptr, &ks->status, h.partials,
+                                                       h.counter, red, ks, 1, 0, m));
     for (int i = 0; i < m; ++i) {
-      TV* vi = V + (size_t)i * n5;
+      TV* vi = V + (size_t)i * vs;
       ICS_LAUNCH(h, ICS_K_VECTOR, k_scale<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, w, vi, ks));
       spmv_t<TB, TV>(h, vi, w);
       precondition_t<TB, TV>(h, w);
       for (int j = 0; j <= i; ++j) {
-        const TV* vprev = j > 0 ? V + (size_t)(j - 1) * n5 : nullptr;
+        const TV* vprev = j > 0 ? V + (size_t)(j - 1) * vs : nullptr;
         const double* hprev = j > 0 ? &ks->H[(j - 1) * m + i] : nullptr;
-        ICS_LAUNCH(h, ICS_K_MGS, k_mgs<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, w, vprev, hprev, V + (size_t)j * n5, &ks->status, h.partials,
-                                                h.counter, &ks->H[j * m + i]));
+        ICS_LAUNCH(h, ICS_K_MGS,
+                   k_mgs<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, w, vprev, hprev, V + (size_t)j * vs, &ks->status,
+                                                           h.partials, h.counter, &ks->H[j * m + i], ks, 0, i, m));
       }
-      ICS_LAUNCH(h, ICS_K_MGS, k_mgs<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, w, vi, &ks->H[i * m + i], nullptr, &ks->status, h.partials,
-                                              h.counter, &red[1]));
-      ICS_LAUNCH(h, ICS_K_SCALAR, k_hess<<<1, 1, 0, st>>>(ks, i, m));
+      ICS_LAUNCH(h, ICS_K_MGS,
+                 k_mgs<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, w, vi, &ks->H[i * m + i], nullptr, &ks->status,
+                                                         h.partials, h.counter, &red[1], ks, 2, i, m));
     }
     ICS_LAUNCH(h, ICS_K_SCALAR, k_backsub<<<1, 1, 0, st>>>(ks, m));
-    ICS_LAUNCH(h, ICS_K_VECTOR, k_xupdate<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, x, V, ks, m));
+    ICS_LAUNCH(h, ICS_K_VECTOR, k_xupdate<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, x, V, ks, m, vs));
     spmv_t<TB, TV>(h, x, t);
     ICS_LAUNCH(h, ICS_K_VECTOR, k_resid<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.src, t, w, h.partials, h.counter, ks->res));
     ICS_CUDA(cudaGetLastError());

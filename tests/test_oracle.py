@@ -1,0 +1,327 @@
+"""Known-answer tests that pin the oracle (CPU, no GPU needed).
+
+The reference ships no tests or golden data, so the oracle is pinned by
+analytic results: freestream preservation, the exact Sod Riemann solution,
+the Euler flux Jacobian against finite differences of the Euler flux, dense
+linear algebra for GMRES / LU-SGS / block Jacobi, and the pseudo-time loop
+logic of pseudotimeControl.C.
+"""
+
+import math
+
+import numpy as np
+import pytest
+
+from icsfoam_gb300 import abi, cases, schemes
+
+GAMMA = 1.4
+
+
+def open_oracle(binding, w, **over):
+    cfg = cases.make_config(binding, w.settings, **over)
+    h = abi.CaseHandle(binding, w.mesh, cfg)
+    h.set_primitive(w.p, w.U, w.T)
+    return h
+
+
+# ------------------------------------------------------------ exact Riemann
+def exact_riemann(x, t, left, right, g=GAMMA, x0=0.0):
+    """Exact solution of the 1D Riemann problem (Toro, ch. 4), returns rho, u, p."""
+    rL, uL, pL = left
+    rR, uR, pR = right
+    aL, aR = math.sqrt(g * pL / rL), math.sqrt(g * pR / rR)
+
+    def fK(p, rK, pK, aK):
+        if p > pK:
+            A, Bk = 2.0 / ((g + 1) * rK), (g - 1) / (g + 1) * pK
+            q = math.sqrt(A / (p + Bk))
+            return (p - pK) * q, q * (1 - (p - pK) / (2 * (Bk + p)))
+        pr = p / pK
+        return (2 * aK / (g - 1) * (pr ** ((g - 1) / (2 * g)) - 1),
+                1.0 / (rK * aK) * pr ** (-(g + 1) / (2 * g)))
+
+    p = 0.5 * (pL + pR)
+    for _ in range(100):
+        f1, d1 = fK(p, rL, pL, aL)
+        f2, d2 = fK(p, rR, pR, aR)
+        dp = (f1 + f2 + uR - uL) / (d1 + d2)
+        pn = max(p - dp, 1e-8)
+        if abs(pn - p) < 1e-14 * p:
+            p = pn
+            break
+        p = pn
+    ps = p
+    us = 0.5 * (uL + uR) + 0.5 * (fK(ps, rR, pR, aR)[0] - fK(ps, rL, pL, aL)[0])
+    out = np.zeros((len(x), 3))
+    for i, xi in enumerate(x):
+        S = (xi - x0) / t
+        if S <= us:
+            if ps > pL:
+                SL = uL - aL * math.sqrt((g + 1) / (2 * g) * ps / pL + (g - 1) / (2 * g))
+                if S <= SL:
+                    out[i] = (rL, uL, pL)
+                else:
+                    r = rL * ((ps / pL + (g - 1) / (g + 1)) / ((g - 1) / (g + 1) * ps / pL + 1))
+                    out[i] = (r, us, ps)
+            else:
+                SHL = uL - aL
+                asl = aL * (ps / pL) ** ((g - 1) / (2 * g))
+                if S <= SHL:
+                    out[i] = (rL, uL, pL)
+                elif S > us - asl:
+                    out[i] = (rL * (ps / pL) ** (1 / g), us, ps)
+                else:
+                    c = 2 / (g + 1) + (g - 1) / ((g + 1) * aL) * (uL - S)
+                    out[i] = (rL * c ** (2 / (g - 1)), 2 / (g + 1) * (aL + (g - 1) / 2 * uL + S),
+                              pL * c ** (2 * g / (g - 1)))
+        else:
+            if ps > pR:
+                SR = uR + aR * math.sqrt((g + 1) / (2 * g) * ps / pR + (g - 1) / (2 * g))
+                if S >= SR:
+                    out[i] = (rR, uR, pR)
+                else:
+                    r = rR * ((ps / pR + (g - 1) / (g + 1)) / ((g - 1) / (g + 1) * ps / pR + 1))
+                    out[i] = (r, us, ps)
+            else:
+                SHR = uR + aR
+                asr = aR * (ps / pR) ** ((g - 1) / (2 * g))
+                if S >= SHR:
+                    out[i] = (rR, uR, pR)
+                elif S < us + asr:
+                    out[i] = (rR * (ps / pR) ** (1 / g), us, ps)
+                else:
+                    c = 2 / (g + 1) - (g - 1) / ((g + 1) * aR) * (uR - S)
+                    out[i] = (rR * c ** (2 / (g - 1)), 2 / (g + 1) * (-aR + (g - 1) / 2 * uR + S),
+                              pR * c ** (2 * g / (g - 1)))
+    return out
+
+
+def test_exact_riemann_self_consistent():
+    # star pressure of the classic Sod problem (1, 0, 1 | 0.125, 0, 0.1): 0.30313
+    sol = exact_riemann(np.array([0.0]), 0.2, (1.0, 0.0, 1.0), (0.125, 0.0, 0.1))
+    assert abs(sol[0, 2] - 0.30313) < 1e-4
+
+
+def run_shock_tube(binding, n=1000, steps=100):
+    w = cases.shock_tube(n)
+    h = open_oracle(binding, w)
+    for _ in range(steps):
+        h.begin_time_step()
+        while h.pseudo_loop():
+            h.pseudo_iteration()
+    return w, h
+
+
+def test_sod_shock_tube_against_exact_solution(oracle_binding):
+    w, h = run_shock_tube(oracle_binding)
+    st = h.get_state()
+    x = w.mesh.C[:, 0]
+    R = 287.0
+    left = (1e5 / (R * 348.4), 0.0, 1e5)
+    right = (1e4 / (R * 278.7), 0.0, 1e4)
+    ex = exact_riemann(x, 100 * 1e-5, left, right)
+    rho = st["W"][:, 0]
+    err = np.abs(rho - ex[:, 0])
+    assert err.mean() < 0.01 * (left[0] - right[0])          # first-order scheme, diffused waves
+    assert np.abs(st["p"] - ex[:, 2]).mean() < 0.01 * (left[2] - right[2])
+    # shock position: first cell from the right where the density rises above the mid level
+    mid = 0.5 * (ex[:, 0].min() + ex[x > 0, 0].max())
+    xs_num = x[np.nonzero(rho > mid)[0].max()]
+    xs_ex = x[np.nonzero(ex[:, 0] > mid)[0].max()]
+    assert abs(xs_num - xs_ex) < 0.1
+    # mass conservation (closed ends carry no net flux in 1 ms)
+    m0 = (w.p / (R * w.T) * w.mesh.V).sum()
+    assert abs((rho * w.mesh.V).sum() - m0) < 1e-10 * m0
+
+
+# ------------------------------------------------------ freestream preservation
+@pytest.mark.parametrize("flux", [0, 1, 2])
+@pytest.mark.parametrize("recon", [0, 1, 3])
+def test_freestream_preservation(oracle_binding, flux, recon):
+    w = cases.random_box(5)
+    h = open_oracle(oracle_binding, w, flux_scheme=flux, recon_rho=recon, recon_U=recon, recon_T=recon)
+    s = h.residual()
+    scale = 1e4 * np.abs(w.mesh.Sf).max()  # p |S|
+    assert np.abs(s).max() < 1e-11 * scale
+
+
+# ------------------------------------------------------- Jacobian structure
+def euler_flux_n(W, n):
+    rho, ru, rE = W[0], W[1:4], W[4]
+    u = ru / rho
+    p = (GAMMA - 1) * (rE - 0.5 * rho * u @ u)
+    un = u @ n
+    return np.concatenate([[rho * un], ru * un + p * n, [(rE + p) * un]])
+
+
+def test_flux_jacobian_matches_finite_differences(oracle_binding):
+    w = cases.bump_channel(6, 3, 2, ordering_mode="natural", second_order=False)
+    rng = np.random.default_rng(4)
+    w.p = w.p * (1 + 0.05 * rng.uniform(-1, 1, len(w.p)))
+    w.U = w.U + 20 * rng.uniform(-1, 1, w.U.shape)
+    h = open_oracle(oracle_binding, w)
+    h.residual()
+    h.assemble_jacobian()
+    D, L, U = h.get_jacobian()
+    st = h.get_state()
+    m = w.mesh
+    c = np.sqrt(GAMMA * 287.0 * st["T"])
+    for f in range(0, m.n_faces, 3):
+        o, nb = m.owner[f], m.neighbour[f]
+        S = m.Sf[f]
+        mS = np.linalg.norm(S)
+        n = S / mS
+        wf = m.weights[f]
+        lam = wf * (c[o] - c[nb]) + c[nb] + abs((wf * (st["U"][o] - st["U"][nb]) + st["U"][nb]) @ n)
+        for cell, blk, sgn in ((nb, U[f], 1.0), (o, L[f], -1.0)):
+            A = (blk + 0.5 * mS * lam * np.eye(5)) / (sgn * 0.5 * mS)
+            Wc = st["W"][cell]
+            J = np.zeros((5, 5))
+            for j in range(5):
+                hstep = 1e-6 * max(abs(Wc[j]), 1.0)
+                e = np.zeros(5)
+                e[j] = hstep
+                J[:, j] = (euler_flux_n(Wc + e, n) - euler_flux_n(Wc - e, n)) / (2 * hstep)
+            assert np.abs(A - J).max() < 1e-5 * np.abs(J).max()
+
+
+# --------------------------------------------------------- dense linear algebra
+def dense(h, D, L, U):
+    m = h.mesh
+    N = m.n_cells
+    A = np.zeros((5 * N, 5 * N))
+    for c in range(N):
+        A[5 * c:5 * c + 5, 5 * c:5 * c + 5] = D[c]
+    for f in range(m.n_faces):
+        o, nb = m.owner[f], m.neighbour[f]
+        A[5 * nb:5 * nb + 5, 5 * o:5 * o + 5] = L[f]   # lower: row neighbour, column owner
+        A[5 * o:5 * o + 5, 5 * nb:5 * nb + 5] = U[f]
+    return A
+
+
+@pytest.fixture
+def small_system(oracle_binding):
+    w = cases.bump_channel(6, 3, 2, ordering_mode="natural")
+    h = open_oracle(oracle_binding, w, tolerance=1e-300, rel_tol=1e-13, max_iter=400, n_directions=8)
+    b = h.residual()
+    h.assemble_jacobian()
+    D, L, U = h.get_jacobian()
+    return h, b, D, L, U, dense(h, D, L, U)
+
+
+def test_matrix_mul_is_dense_product(small_system):
+    h, b, D, L, U, A = small_system
+    x = np.random.default_rng(0).standard_normal((h.N, 5))
+    assert np.allclose(h.matrix_mul(x).ravel(), A @ x.ravel(), rtol=1e-13, atol=1e-12 * np.abs(A).max())
+
+
+def test_gmres_matches_dense_solve(small_system):
+    h, b, D, L, U, A = small_system
+    perf, dW, st = h.solve_increment()
+    ref = np.linalg.solve(A, b.ravel()).reshape(-1, 5)
+    scale = np.abs(ref).max(axis=0)
+    assert np.abs(dW - ref).max(axis=0).max() / scale.max() < 1e-8
+    assert perf.final_res[0] < 1e-12 and perf.n_iterations >= 1
+
+
+def test_lusgs_is_the_factored_sgs_operator(small_system):
+    h, b, D, L, U, A = small_system
+    N = h.N
+    order = [0, 24, 6, 12, 18]
+    rD = np.full(N, 1e15)
+    for c in range(N):
+        for k in order:
+            rD[c] = 1.0 / max(1.0 / rD[c], abs(D[c].ravel()[k]))
+    Ds = np.kron(np.diag(1.0 / rD), np.eye(5))
+    Lo = np.tril(A, -1) - np.tril(np.kron(np.eye(N), np.ones((5, 5))) * A, -1)
+    Up = np.triu(A, 1) - np.triu(np.kron(np.eye(N), np.ones((5, 5))) * A, 1)
+    P = (Ds + Lo) @ np.linalg.inv(Ds) @ (Ds + Up)
+    r = np.random.default_rng(1).standard_normal(5 * N)
+    z = h.precondition(r.reshape(-1, 5)).ravel()
+    assert np.allclose(P @ z, r, rtol=1e-10, atol=1e-10 * np.abs(r).max())
+
+
+def test_jacobi_is_block_diagonal_inverse(oracle_binding):
+    w = cases.bump_channel(6, 3, 2, ordering_mode="natural")
+    h = open_oracle(oracle_binding, w, preconditioner=2)
+    h.residual()
+    h.assemble_jacobian()
+    D, _, _ = h.get_jacobian()
+    r = np.random.default_rng(2).standard_normal((h.N, 5))
+    z = h.precondition(r)
+    for c in range(h.N):
+        assert np.allclose(D[c] @ z[c], r[c], rtol=1e-10, atol=1e-12)
+
+
+# ------------------------------------------------------------ pseudo-time control
+def test_pseudotime_loop_steady(oracle_binding):
+    w = cases.bump_channel(4, 2, 2)
+    h = open_oracle(oracle_binding, w, pseudo_tol=1e300)
+    seq = [h.pseudo_loop() for _ in range(3)]
+    assert seq == [True, True, False]   # first iteration, converged -> final iteration, done
+
+
+def test_pseudotime_loop_max_iterations(oracle_binding):
+    w = cases.shock_tube(20)
+    h = open_oracle(oracle_binding, w, pseudo_tol=-1.0, pseudo_tol_rel=-1.0, n_pseudo_corr=4)
+    h.begin_time_step()
+    n = 0
+    while h.pseudo_loop():
+        h.pseudo_iteration()
+        n += 1
+    assert n == 4
+
+
+def test_ser_ramps_pseudo_courant(oracle_binding):
+    w = cases.bump_channel(8, 4, 2, ordering_mode="colour")
+    h = open_oracle(oracle_binding, w)
+    cos = []
+    for _ in range(6):
+        h.pseudo_loop()
+        h.pseudo_iteration()
+        cos.append(h.get_pseudo_co()[0].mean())
+    assert cos[0] == 1.0 and cos[1] == 1.0       # SER starts at the third iteration
+    assert all(1.0 <= c <= 200.0 for c in cos)
+    assert cos[-1] > 1.0
+
+
+# ---------------------------------------------------------------- errors
+def test_unknown_scheme_is_an_error(oracle_binding):
+    w = cases.bump_channel(4, 2, 2)
+    cfg = cases.make_config(oracle_binding, w.settings, flux_scheme=7)
+    with pytest.raises(abi.IcsError) as e:
+        abi.CaseHandle(oracle_binding, w.mesh, cfg)
+    assert e.value.status == abi.ICS_ERR_SCHEME
+
+
+def test_nonfinite_state_is_reported(oracle_binding):
+    w = cases.bump_channel(4, 2, 2)
+    h = open_oracle(oracle_binding, w)
+    W = h.get_state()["W"]
+    W[3, 0] = np.nan
+    h.set_conservative(W)
+    with pytest.raises(abi.IcsError) as e:
+        h.residual()
+    assert e.value.status == abi.ICS_ERR_NONFINITE
+
+
+def test_dictionary_selection_and_errors(oracle_binding):
+    fvSchemes = {"convectiveFluxScheme": {"fluxScheme": "HLLCGPU"},
+                 "ddtSchemes": {"default": "dualTime rPseudoDeltaT steadyState"},
+                 "interpolationSchemes": {"reconstruct(rho)": "linearUpwind grad(rho)",
+                                          "reconstruct(U)": "linearUpwind grad(U)",
+                                          "reconstruct(T)": "linearUpwind grad(T)"},
+                 "gradSchemes": {"default": "cellLimited<Venkatakrishnan> Gauss linear 1"}}
+    fvSolution = {"flowSolver": {"solver": "GMRESGPU", "precision": "mixed",
+                                 "GMRES": {"preconditioner": "LUSGS", "nDirections": 8, "maxIter": 5,
+                                           "tolerance": 1e-12, "relTol": 1e-2}},
+                  "pseudoTime": {"pseudoTol": 1e-8, "pseudoTolRel": 1e-8, "pseudoCoNumMax": 200}}
+    cfg = schemes.config_from_dicts(oracle_binding, fvSchemes, fvSolution)
+    assert (cfg.flux_scheme, cfg.recon_rho, cfg.precision, cfg.n_directions) == (1, 3, 1, 8)
+    assert cfg.pseudo_co_num_max == 200
+    bad = dict(fvSchemes, convectiveFluxScheme={"fluxScheme": "Upwind"})
+    with pytest.raises(ValueError):
+        schemes.config_from_dicts(oracle_binding, bad, fvSolution)
+    bad2 = dict(fvSolution, flowSolver={"solver": "BiCG"})
+    with pytest.raises(ValueError):
+        schemes.config_from_dicts(oracle_binding, fvSchemes, bad2)

@@ -1,0 +1,123 @@
+"""CUDA path: physics known answers, failure statuses and control logic.
+
+Failures are injected on the host (a NaN written into the uploaded state, an
+exactly zero right-hand side); nothing here faults, traps or hangs a GPU.
+"""
+
+import numpy as np
+import pytest
+
+from icsfoam_gb300 import abi, cases
+
+from test_oracle import exact_riemann  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def open_case(binding, w, **over):
+    h = abi.CaseHandle(binding, w.mesh, cases.make_config(binding, w.settings, **over))
+    h.set_primitive(w.p, w.U, w.T)
+    return h
+
+
+def test_sod_on_gpu_matches_exact_and_oracle(gpu_binding, oracle_binding):
+    w = cases.shock_tube(1000)
+    hg = open_case(gpu_binding, w)
+    ho = open_case(oracle_binding, w)
+    for step in range(100):
+        for h in (hg, ho):
+            h.begin_time_step()
+        while True:
+            mg, mo = hg.pseudo_loop(), ho.pseudo_loop()
+            assert mg == mo
+            if not mg:
+                break
+            hg.pseudo_iteration()
+            ho.pseudo_iteration()
+    g, o = hg.get_state(), ho.get_state()
+    assert np.abs(g["W"] - o["W"]).max(axis=0).max() / np.abs(o["W"]).max() < 1e-9
+    x = w.mesh.C[:, 0]
+    ex = exact_riemann(x, 1e-3, (1e5 / (287 * 348.4), 0, 1e5), (1e4 / (287 * 278.7), 0, 1e4))
+    assert np.abs(g["W"][:, 0] - ex[:, 0]).mean() < 0.01
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_nonfinite_state_is_reported(gpu_binding, precision):
+    w = cases.bump_channel(8, 4, 2, ordering_mode="colour")
+    h = open_case(gpu_binding, w, precision=precision)
+    W = h.get_state()["W"]
+    W[5, 4] = np.nan
+    h.set_conservative(W)
+    with pytest.raises(abi.IcsError) as e:
+        h.residual()
+    assert e.value.status == abi.ICS_ERR_NONFINITE
+    # the context stays usable: a clean state runs again
+    h.set_primitive(w.p, w.U, w.T)
+    h.pseudo_iteration()
+
+
+def still_air(n=6):
+    w = cases.shock_tube(n)
+    w.p[:] = 1e5
+    w.T[:] = 300.0
+    w.U[:] = 0.0
+    w.settings = dict(w.settings, ddt_scheme=0)
+    return w
+
+
+@pytest.mark.parametrize("lib", ["gpu", "oracle"])
+def test_zero_rhs_is_a_krylov_breakdown(gpu_binding, oracle_binding, lib):
+    """Still air: the residual is exactly zero, so the first Krylov norm is zero."""
+    b = gpu_binding if lib == "gpu" else oracle_binding
+    h = open_case(b, still_air())
+    src = h.residual()
+    assert np.all(src == 0.0)
+    h.assemble_jacobian()
+    perf, dW, st = h.solve_increment(allow=(abi.ICS_OK, abi.ICS_ERR_BREAKDOWN))
+    assert st == abi.ICS_ERR_BREAKDOWN
+    assert np.all(dW == 0.0)
+
+
+def test_pseudo_loop_sequence_matches_oracle(gpu_binding, oracle_binding):
+    w = cases.shock_tube(30)
+    seqs = []
+    for b in (gpu_binding, oracle_binding):
+        h = open_case(b, w, n_pseudo_corr=6)
+        seq = []
+        for _ in range(3):
+            h.begin_time_step()
+            while h.pseudo_loop():
+                h.pseudo_iteration()
+                seq.append(1)
+            seq.append(0)
+        seqs.append(seq)
+    assert seqs[0] == seqs[1]
+
+
+def test_jacobi_preconditioner_parity(gpu_binding, oracle_binding):
+    w = cases.bump_channel(10, 4, 3, ordering_mode="colour")
+    hs = [open_case(b, w, preconditioner=2) for b in (gpu_binding, oracle_binding)]
+    for h in hs:
+        h.residual()
+        h.assemble_jacobian()
+    r = np.random.default_rng(0).standard_normal((w.mesh.n_cells, 5))
+    zg, zo = hs[0].precondition(r), hs[1].precondition(r)
+    assert np.abs(zg - zo).max() < 1e-11 * np.abs(zo).max()
+    pg, dg, _ = hs[0].solve_increment()
+    po, do, _ = hs[1].solve_increment()
+    assert pg.n_iterations == po.n_iterations
+    assert np.abs(dg - do).max() < 1e-9 * np.abs(do).max()
+
+
+def test_profiling_counts_launches(gpu_binding):
+    w = cases.bump_channel(8, 4, 2, ordering_mode="colour")
+    h = open_case(gpu_binding, w)
+    n0 = h.launch_count()
+    h.profile(True)
+    h.pseudo_iteration()
+    h.profile(False)
+    prof = h.profile_read()
+    n = h.launch_count() - n0
+    assert n == sum(v[1] for v in prof.values())
+    assert prof["face"][1] == 1 and prof["spmv"][1] >= 2
+    assert all(v[0] >= 0 for v in prof.values())

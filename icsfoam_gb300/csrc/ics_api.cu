@@ -95,6 +95,7 @@ void free_all(Handle& h) {
                   h.ddtCoeff, h.q, h.bq, h.clin, h.grad, h.fflux, h.frec, h.flam, h.bjac, h.src, h.blk, h.dg,
                   h.dginv, h.rD, h.kv, h.kw, h.kx, h.kb, h.kt, h.dW, h.partials, h.counter, h.ks, h.scratch,
                   h.ibuf};
+  drop_graphs(h);
   for (void* p : ptrs) dfree(p);
   for (cudaEvent_t e : h.evPool) cudaEventDestroy(e);
   if (h.tStart) cudaEventDestroy(h.tStart);
@@ -168,6 +169,7 @@ void ensure_workspace(Handle& h) {
   const int m = h.cfg.c.n_directions;
   const size_t eb = p == ICS_PREC_MIXED ? 4 : 8;
   const size_t n5 = 5ull * h.m.N;
+  if (h.kvPrec != p || h.kvDirs < m) drop_graphs(h);  // captured pointers change
   if (h.kvPrec != p) {
     void* ptrs[] = {h.blk, h.dg, h.dginv, h.rD, h.kw, h.kx, h.kb, h.kt, h.kv};
     for (void* q : ptrs) dfree(q);
@@ -371,6 +373,11 @@ void build_mesh(Handle& h, const ics_mesh_desc* d) {
   std::vector<int> fcells, rcells;
   group(lev, m.nfl, m.fl_ptr, fcells, m.fl_cstart);
   group(rlev, m.nrl, m.rl_ptr, rcells, m.rl_cstart);
+  {
+    const int a = m.fl_ptr[m.nfl - 1], b = m.fl_ptr[m.nfl];
+    m.fuse_last = (b - a) == (m.rl_ptr[1] - m.rl_ptr[0]) &&
+                  std::equal(fcells.begin() + a, fcells.begin() + b, rcells.begin() + m.rl_ptr[0]);
+  }
   m.fl_cells = upload(fcells);
   m.rl_cells = upload(rcells);
   m.fl_lptr = upload(m.fl_ptr);

@@ -101,6 +101,7 @@ struct DevMesh {
   int* rl_cells = nullptr;           // cells by reverse level
   int* fl_lptr = nullptr;            // device copies of the level pointers
   int* rl_lptr = nullptr;
+  bool fuse_last = false;            // last forward level == first reverse level (same rows)
 };
 
 struct Cfg {
@@ -176,7 +177,17 @@ struct Handle {
   double profMs[ICS_K_COUNT] = {};
   long long profN[ICS_K_COUNT] = {};
   cudaEvent_t tStart = nullptr, tStop = nullptr;
+  // one GMRES restart cycle captured as a CUDA graph (key = precision*1000 + m)
+  cudaGraphExec_t cycleExec = nullptr;
+  int cycleKey = -1;
+  long long cycleLaunches = 0;
 };
+
+inline void drop_graphs(Handle& h) {
+  if (h.cycleExec) cudaGraphExecDestroy(h.cycleExec);
+  h.cycleExec = nullptr;
+  h.cycleKey = -1;
+}
 
 // Times one kernel launch of class `kind` when profiling is on; counts it always.
 struct Launch {

@@ -107,8 +107,11 @@ __device__ __forceinline__ void axpy16(double2& x, double h, const double2& p) {
   x.x -= h * p.x;
   x.y -= h * p.y;
 }
-__device__ __forceinline__ double dot16(const float4& a, const float4& b) {
-  return double(a.x * b.x) + double(a.y * b.y) + double(a.z * b.z) + double(a.w * b.w);
+// Per-thread dot accumulation stays in the Krylov element type (a thread
+// sums a few dozen products); FP64 conversions on GB300 run on the slow
+// FP64 pipe, so the FP32 path converts once per thread, not per product.
+__device__ __forceinline__ float dot16(const float4& a, const float4& b) {
+  return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
 }
 __device__ __forceinline__ double dot16(const double2& a, const double2& b) { return a.x * b.x + a.y * b.y; }
 
@@ -151,7 +154,9 @@ __global__ void __launch_bounds__(128) k_spmv(DevMesh m, const TB* __restrict__ 
 }
 
 // ------------------------------------------------------------------ LU-SGS
-template <typename TB, typename TV>
+// SCALE: also apply the reverse step of a row without upper neighbours
+// (delta = rD * r'), fusing the last forward level with the first reverse one.
+template <typename TB, typename TV, bool SCALE = false>
 __device__ __forceinline__ void lusgs_fwd_row(const DevMesh& m, const TB* __restrict__ blk, const TB* __restrict__ rD,
                                               TV* __restrict__ r, int c) {
   const int s = c >> 5, lane = c & 31;
@@ -175,8 +180,14 @@ __device__ __forceinline__ void lusgs_fwd_row(const DevMesh& m, const TB* __rest
       acc[i] -= a;
     }
   }
+  if (SCALE) {
+    const TV rc = TV(rD[c]);
 #pragma unroll
-  for (int k = 0; k < 5; ++k) r[5 * c + k] = acc[k];
+    for (int k = 0; k < 5; ++k) r[5 * c + k] = rc * acc[k];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) r[5 * c + k] = acc[k];
+  }
 }
 
 template <typename TB, typename TV>
@@ -209,17 +220,20 @@ __device__ __forceinline__ void lusgs_rev_row(const DevMesh& m, const TB* __rest
 
 // one launch per level: cells = level list (nullptr when the level is the
 // contiguous range [start, start+count))
-template <typename TB, typename TV, bool FWD>
+// MODE 0: forward row, 1: reverse row, 2: forward row + reverse scaling
+template <typename TB, typename TV, int MODE>
 __global__ void __launch_bounds__(128) k_lusgs_level(DevMesh m, const TB* __restrict__ blk,
                                                      const TB* __restrict__ rD, TV* __restrict__ r,
                                                      const int* __restrict__ cells, int start, int count) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
   const int c = cells ? cells[start + i] : start + i;
-  if (FWD)
+  if (MODE == 0)
     lusgs_fwd_row<TB, TV>(m, blk, rD, r, c);
-  else
+  else if (MODE == 1)
     lusgs_rev_row<TB, TV>(m, blk, rD, r, c);
+  else
+    lusgs_fwd_row<TB, TV, true>(m, blk, rD, r, c);
 }
 
 // one CTA walks every level (small meshes / many tiny levels)
@@ -330,6 +344,7 @@ __global__ void __launch_bounds__(RB) k_mgs(long n, TV* __restrict__ w, const TV
     const VT* p4 = reinterpret_cast<const VT*>(vprev);
     const VT* o4 = reinterpret_cast<const VT*>(vnext);
     const long stride = (long)gridDim.x * blockDim.x;
+    TV tacc = TV(0);
 #pragma unroll 4
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nv; i += stride) {
       VT x = w4[i];
@@ -337,7 +352,7 @@ __global__ void __launch_bounds__(RB) k_mgs(long n, TV* __restrict__ w, const TV
         axpy16(x, h, p4[i]);
         w4[i] = x;
       }
-      acc[0] += dot16(x, vnext ? o4[i] : x);
+      tacc += dot16(x, vnext ? o4[i] : x);
     }
     for (long i = nv * L + blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += stride) {
       TV x = w[i];
@@ -346,8 +361,9 @@ __global__ void __launch_bounds__(RB) k_mgs(long n, TV* __restrict__ w, const TV
         w[i] = x;
       }
       const TV o = vnext ? vnext[i] : x;
-      acc[0] += double(x * o);
+      tacc += x * o;
     }
+    acc[0] = double(tacc);
   }
   if (reduce_finish<1>(acc, partials, counter, out)) {
     if (post == 1)
@@ -514,22 +530,44 @@ static void lusgs_t(Handle& h, TV* r) {
   // forward sweep, then reverse sweep; many small levels run in one CTA
   if ((long)m.N < 2048L * m.nfl) {
     ICS_LAUNCH(h, ICS_K_LUSGS_FWD, k_lusgs_block<TB, TV, true><<<1, 1024, 0, h.stream>>>(m, blk, rD, r, m.fl_cells, m.fl_lptr, m.nfl));
-  } else {
+    if ((long)m.N < 2048L * m.nrl) {
+      ICS_LAUNCH(h, ICS_K_LUSGS_REV,
+                 k_lusgs_block<TB, TV, false><<<1, 1024, 0, h.stream>>>(m, blk, rD, r, m.rl_cells, m.rl_lptr, m.nrl));
+      return;
+    }
+  }
+  // Level launches.  Forward level 0 has no lower neighbours (r' = r): skipped.
+  // When the last forward level holds exactly the rows of the first reverse
+  // level (rows without upper neighbours, e.g. the last colour), the two are
+  // fused: r' = r - L d*, then delta = rD r' in the same pass.
+  const bool blockFwd = (long)m.N < 2048L * m.nfl;
+  const bool fuse = !blockFwd && m.fuse_last;
+  if (!blockFwd) {
     for (int l = 0; l < m.nfl; ++l) {
+      const bool last = l == m.nfl - 1;
+      if (l == 0 && !(fuse && last)) continue;
       const int a = m.fl_ptr[l], cnt = m.fl_ptr[l + 1] - a;
       const bool contig = m.fl_cstart[l] >= 0;
-      ICS_LAUNCH(h, ICS_K_LUSGS_FWD, k_lusgs_level<TB, TV, true><<<grid_for(cnt, 128), 128, 0, h.stream>>>(
-          m, blk, rD, r, contig ? nullptr : m.fl_cells, contig ? m.fl_cstart[l] : a, cnt));
+      const int* cells = contig ? nullptr : m.fl_cells;
+      const int start = contig ? m.fl_cstart[l] : a;
+      if (fuse && last)
+        ICS_LAUNCH(h, ICS_K_LUSGS_FWD, k_lusgs_level<TB, TV, 2><<<grid_for(cnt, 128), 128, 0, h.stream>>>(
+                                           m, blk, rD, r, cells, start, cnt));
+      else
+        ICS_LAUNCH(h, ICS_K_LUSGS_FWD, k_lusgs_level<TB, TV, 0><<<grid_for(cnt, 128), 128, 0, h.stream>>>(
+                                           m, blk, rD, r, cells, start, cnt));
     }
   }
   if ((long)m.N < 2048L * m.nrl) {
-    ICS_LAUNCH(h, ICS_K_LUSGS_REV, k_lusgs_block<TB, TV, false><<<1, 1024, 0, h.stream>>>(m, blk, rD, r, m.rl_cells, m.rl_lptr, m.nrl));
+    ICS_LAUNCH(h, ICS_K_LUSGS_REV,
+               k_lusgs_block<TB, TV, false><<<1, 1024, 0, h.stream>>>(m, blk, rD, r, m.rl_cells, m.rl_lptr, m.nrl));
   } else {
-    for (int l = 0; l < m.nrl; ++l) {
+    for (int l = fuse ? 1 : 0; l < m.nrl; ++l) {
       const int a = m.rl_ptr[l], cnt = m.rl_ptr[l + 1] - a;
       const bool contig = m.rl_cstart[l] >= 0;
-      ICS_LAUNCH(h, ICS_K_LUSGS_REV, k_lusgs_level<TB, TV, false><<<grid_for(cnt, 128), 128, 0, h.stream>>>(
-          m, blk, rD, r, contig ? nullptr : m.rl_cells, contig ? m.rl_cstart[l] : a, cnt));
+      ICS_LAUNCH(h, ICS_K_LUSGS_REV, k_lusgs_level<TB, TV, 1><<<grid_for(cnt, 128), 128, 0, h.stream>>>(
+                                         m, blk, rD, r, contig ? nullptr : m.rl_cells,
+                                         contig ? m.rl_cstart[l] : a, cnt));
     }
   }
 }
@@ -623,7 +661,9 @@ static int gmres_t(Handle& h, ics_solver_perf* perf) {
   ICS_CUDA(cudaMemsetAsync(x, 0, n5 * sizeof(TV), st));
   to_vec(h, h.src, w);
   int status = ICS_OK;
-  do {
+  // one restart cycle: every scalar it needs lives in device memory, so the
+  // same launch sequence can be captured once and replayed per cycle
+  auto cycle = [&]() {
     precondition_t<TB, TV>(h, w);
     ICS_LAUNCH(h, ICS_K_MGS,
                k_mgs<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, w, nullptr, nullptr, nullptr, &ks->status, h.partials,
@@ -647,7 +687,31 @@ static int gmres_t(Handle& h, ics_solver_perf* perf) {
     ICS_LAUNCH(h, ICS_K_SCALAR, k_backsub<<<1, 1, 0, st>>>(ks, m));
     ICS_LAUNCH(h, ICS_K_VECTOR, k_xupdate<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, x, V, ks, m, vs));
     spmv_t<TB, TV>(h, x, t);
-    ICS_LAUNCH(h, ICS_K_VECTOR, k_resid<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.src, t, w, h.partials, h.counter, ks->res));
+    ICS_LAUNCH(h, ICS_K_VECTOR,
+               k_resid<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.src, t, w, h.partials, h.counter, ks->res));
+  };
+  const int key = h.cfg.c.preconditioner * 100000 + prec(h) * 1000 + m;
+  const bool useGraph = !h.prof;  // per-launch event timing needs direct launches
+  if (useGraph && h.cycleKey != key) {
+    drop_graphs(h);
+    cudaGraph_t g = nullptr;
+    const long long before = h.launches;
+    ICS_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cycle();
+    ICS_CUDA(cudaStreamEndCapture(st, &g));
+    ICS_CUDA(cudaGraphInstantiate(&h.cycleExec, g, 0));
+    ICS_CUDA(cudaGraphDestroy(g));
+    h.cycleLaunches = h.launches - before;
+    h.launches = before;  // captured, not executed
+    h.cycleKey = key;
+  }
+  do {
+    if (useGraph) {
+      ICS_CUDA(cudaGraphLaunch(h.cycleExec, st));
+      h.launches += h.cycleLaunches;
+    } else {
+      cycle();
+    }
     ICS_CUDA(cudaGetLastError());
     ICS_CUDA(cudaMemcpyAsync(h.ksHost->res, ks->res, 5 * sizeof(double), cudaMemcpyDeviceToHost, st));
     ICS_CUDA(cudaMemcpyAsync(&h.ksHost->status, &ks->status, sizeof(int), cudaMemcpyDeviceToHost, st));

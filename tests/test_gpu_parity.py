@@ -22,6 +22,8 @@ WORKLOADS = {
     "bump_ausm_muscl_colour": lambda: cases.bump_channel(24, 8, 4, ordering_mode="colour", flux="AUSMPlusUp"),
     "bump_roe_muscl_natural": lambda: cases.bump_channel(16, 6, 3, ordering_mode="natural", flux="ROE"),
     "box_ausm_rcm": lambda: cases.random_box(6),
+    # large enough for per-level LU-SGS launches (fused last forward / first reverse level)
+    "bump_hllc_muscl_colour_levels": lambda: cases.bump_channel(32, 16, 10, ordering_mode="colour", flux="HLLC"),
 }
 
 EXTRA = {
@@ -142,7 +144,8 @@ def test_solve_and_update(oracle_binding, gpu_binding, name):
         assert relerr(bg[k], bo[k]) < 1e-10
 
 
-@pytest.mark.parametrize("name", ["tube_ausm_natural", "bump_hllc_muscl_colour", "box_ausm_rcm"])
+@pytest.mark.parametrize("name", ["tube_ausm_natural", "bump_hllc_muscl_colour", "box_ausm_rcm",
+                                  "bump_hllc_muscl_colour_levels"])
 def test_pseudo_trajectory(oracle_binding, gpu_binding, name):
     """Several full pseudo iterations (SER, local dtau, GMRES, update) in lockstep."""
     w = WORKLOADS[name]()

@@ -210,31 +210,41 @@ def run_timed(w, prec, steps, warmup, dist, profile):
     launches = h.launch_count() - l0
     ck = clocks.stop()
     ms = dist.max(ms)
+    h.close()
     kern = None
     if profile:
-        # the same number of further iterations with a CUDA event pair around
-        # every launch on the handle's stream: per-kernel-class device time
+        # replay the same iterations on a fresh handle with a CUDA event pair
+        # around every launch on the handle's stream: per-kernel-class device
+        # time of exactly the timed work (direct launches instead of the
+        # captured GMRES cycle graph)
+        h = gpu.open_case(w.mesh, cases.make_config(b, w.settings, precision=prec))
+        h.set_primitive(w.p, w.U, w.T)
+        for _ in range(warmup):
+            h.pseudo_loop()
+            h.pseudo_iteration()
         h.profile(True)
         for _ in range(steps):
             h.pseudo_loop()
             h.pseudo_iteration()
         h.profile(False)
         kern = h.profile_read()
-    h.close()
+        h.close()
     return {"ms": ms, "launches": launches, "kernels": kern, "clocks": ck,
             "last_rho_l2": last.rho_l2_residual if last else None}
 
 
-def run_to_solution(w, prec, cap_s, target=1e-8, max_iters=20000):
+def run_to_solution(w, prec, cap_s, target=1e-8, max_iters=20000, **over):
+    """Iterate until the rho L2 residual drops by `target` (or the time cap)."""
     from icsfoam_gb300 import cases, gpu
 
     b = gpu.binding()
-    h = gpu.open_case(w.mesh, cases.make_config(b, w.settings, precision=prec))
+    h = gpu.open_case(w.mesh, cases.make_config(b, w.settings, precision=prec, **over))
     h.set_primitive(w.p, w.U, w.T)
     t0 = time.perf_counter()
     r0 = None
     it = 0
     drop = 1.0
+    best = 1.0
     hist = []
     while it < max_iters:
         h.pseudo_loop()
@@ -242,15 +252,16 @@ def run_to_solution(w, prec, cap_s, target=1e-8, max_iters=20000):
         it += 1
         r0 = r0 or s.rho_l2_residual
         drop = s.rho_l2_residual / r0
-        if it % 50 == 0:
-            hist.append((it, drop))
+        best = min(best, drop)
+        if it % 100 == 0:
+            hist.append((it, round(time.perf_counter() - t0, 2), drop))
         if drop <= target or time.perf_counter() - t0 > cap_s:
             break
     dt = time.perf_counter() - t0
     state = h.get_state()["W"]
     h.close()
-    return {"iterations": it, "seconds": dt, "drop": drop, "reached": drop <= target,
-            "cell_iters_per_s": w.mesh.n_cells * it / dt, "history": hist[-6:]}, state
+    return {"iterations": it, "seconds": dt, "drop": drop, "min_drop": best, "reached": drop <= target,
+            "cell_iters_per_s": w.mesh.n_cells * it / dt, "history": hist[-5:]}, state
 
 
 def run_e2e(w, steps, warmup):
@@ -365,10 +376,15 @@ def main():
 
         sm, Wm = run_to_solution(w, 1, args.solution_cap_s)
         sd, Wd = run_to_solution(w, 0, args.solution_cap_s)
+        # first-order reconstruction converges without limiter chatter
+        s1, W1m = run_to_solution(w, 1, args.solution_cap_s / 2, recon_rho=0, recon_U=0, recon_T=0)
         scale = np.abs(Wd).max(axis=0)
         scale[1:4] = scale[1:4].max()
-        extra["to_solution"] = {"mixed": sm, "fp64": sd,
-                                "mixed_vs_fp64_field_max_rel_diff": float((np.abs(Wm - Wd) / scale).max())}
+        extra["to_solution"] = {
+            "mixed": sm, "fp64": sd, "mixed_first_order": s1,
+            "mixed_vs_fp64_field_max_rel_diff_at_cap": float((np.abs(Wm - Wd) / scale).max()),
+            "note": "second-order MUSCL with OpenFOAM's cellLimited<Venkatakrishnan> (no smoothing) stalls "
+                    "at a 1e-6..1e-5 drop on this case (limiter chatter); min_drop records the plateau"}
     e2e = run_e2e(w, args.steps, args.warmup) if dist.rank == 0 else None
     # roofline of the dominant kernel class of the mixed leg
     from icsfoam_gb300 import ordering  # noqa: F401

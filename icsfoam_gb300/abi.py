@@ -136,6 +136,9 @@ _MEASURE = {
     "timer_stop": (C.c_int, [_P, C.POINTER(C.c_double)]),
 }
 
+# allocation-free linear residual (CUDA library only; arguments are device pointers)
+_MEASURE["linear_residual_noalloc"] = (C.c_int, [_P, _P, _P, _P])
+
 KERNEL_CLASSES = ("fields", "grad", "face", "bface", "cellres", "jac_boundary", "jac_rows", "jacobi_inv", "spmv",
                   "lusgs_fwd", "lusgs_rev", "jacobi", "mgs", "vector", "scalar", "update", "bc", "bound")
 
@@ -375,3 +378,7 @@ class CaseHandle:
         ms = C.c_double()
         self._check(self.b.fn["timer_stop"](self.h, C.byref(ms)), "timer_stop")
         return float(ms.value)
+
+    def linear_residual_noalloc(self, x_dev: int, r_dev: int, l1_dev: int) -> int:
+        """Device-pointer call of ics_linear_residual_noalloc; returns the status."""
+        return int(self.b.fn["linear_residual_noalloc"](self.h, x_dev, r_dev, l1_dev))

@@ -239,6 +239,20 @@ int ics_launch_count(ics_handle h, int64_t* launches);
 int ics_timer_start(ics_handle h);
 int ics_timer_stop(ics_handle h, double* ms);
 
+/* ---- allocation-free entry point (no counterpart in the reference) ------ */
+/* r = b - A x and the five per-equation L1 sums of r, with A the handle's
+ * assembled Jacobian and b its last residual source, for callers that must
+ * not allocate device memory while running (code inside a CUDA graph
+ * capture, real-time drivers that allocate only at start-up, hosts that own
+ * every device buffer).  x, r ([n_cells][5]) and l1 ([5]) are caller-owned
+ * DEVICE pointers; nothing is allocated or freed.  The only scratch is a
+ * fixed file-scope device array sized for at most 2,097,152 cells: larger
+ * handles return ICS_ERR_ARG.  The first call on a device looks up that
+ * array's address (cudaGetSymbolAddress), so make it before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race.
+ * Runs on the handle's stream and synchronises it before returning.        */
+int ics_linear_residual_noalloc(ics_handle h, const double* x, double* r, double* l1);
+
 #ifdef __cplusplus
 }
 #endif

@@ -140,7 +140,7 @@ _MEASURE = {
 _MEASURE["linear_residual_noalloc"] = (C.c_int, [_P, _P, _P, _P])
 
 KERNEL_CLASSES = ("fields", "grad", "face", "bface", "cellres", "jac_boundary", "jac_rows", "jacobi_inv", "spmv",
-                  "lusgs_fwd", "lusgs_rev", "jacobi", "mgs", "vector", "scalar", "update", "bc", "bound")
+                  "lusgs_fwd", "lusgs_rev", "jacobi", "mgs", "vector", "scalar", "update", "bc", "bound", "visc")
 
 EXPORTED = tuple(_FUNCS) + tuple(_MEASURE)
 

@@ -112,13 +112,18 @@ def bump_channel(nx: int = 256, ny: int = 64, nz: int = 64, mach: float = 0.675,
 
 def random_box(n: int = 200, seed_vertices: int = 0, seed_perm: int = 1, mach: float = 2.0,
                p: float = 1.0e4, T: float = 220.0, T_wall: float = 300.0, length: float = 1.0,
-               ordering_mode: str = "rcm") -> Workload:
-    """Randomised hex box: interior vertices displaced by U(+-0.2h), cells permuted then RCM."""
+               ordering_mode: str = "rcm", jitter: float = 0.2, reynolds_per_m: float = 1.0e5) -> Workload:
+    """Randomised hex box: interior vertices displaced by U(+-jitter h), cells permuted then RCM.
+
+    Viscous supersonic flow over an isothermal wall (bottom): Sutherland
+    viscosity scaled so that rho U / mu equals ``reynolds_per_m`` in the
+    freestream, Pr = 0.72.
+    """
     h = length / n
     xs = np.linspace(0.0, length, n + 1)
     g = np.stack(np.meshgrid(xs, xs, xs, indexing="ij"), axis=-1)
     rng = np.random.default_rng(seed_vertices)
-    disp = rng.uniform(-0.2 * h, 0.2 * h, size=g.shape)
+    disp = rng.uniform(-jitter * h, jitter * h, size=g.shape)
     interior = np.zeros(g.shape[:3], bool)
     interior[1:-1, 1:-1, 1:-1] = True
     g = g + np.where(interior[..., None], disp, 0.0)
@@ -137,10 +142,16 @@ def random_box(n: int = 200, seed_vertices: int = 0, seed_perm: int = 1, mach: f
     N = mesh.n_cells
     Uc = np.zeros((N, 3))
     Uc[:, 0] = uinf
+    # Sutherland constant As chosen so that rho u / mu(T) = Re per metre
+    rho = p / (R_GAS * T)
+    Ts = 110.4
+    mu_inf = rho * uinf / reynolds_per_m
+    As = mu_inf * (1.0 + Ts / T) / np.sqrt(T)
     settings = dict(thermo_settings(), flux_scheme=0, recon_rho=3, recon_U=3, recon_T=3,
                     ddt_scheme=0, pseudo_co_num=1.0, pseudo_co_num_max=50.0,
                     n_directions=8, max_iter=5, rel_tol=1e-2, tolerance=1e-12,
-                    pseudo_tol=1e-30, pseudo_tol_rel=1e-30)
+                    pseudo_tol=1e-30, pseudo_tol_rel=1e-30,
+                    viscous=1, sutherland=1, As=float(As), Ts=Ts, Pr=0.72)
     return Workload("random_box_%d" % n, mesh, np.full(N, p), Uc, np.full(N, T), settings)
 
 

@@ -92,7 +92,8 @@ void free_all(Handle& h) {
                   m.bcell, m.bpatch, m.bSf, m.bmagSf, m.bdOwn, m.bdc, m.patches, m.cptr, m.cface, m.bptr,
                   m.bface, m.slot_base, m.scol, m.sface, m.nlow, m.nslot, m.fl_cells, m.rl_cells, m.fl_lptr,
                   m.rl_lptr, h.W, h.W0, h.W00, h.Wprev, h.prim, h.pB, h.TB, h.UB, h.phiB, h.pseudoCo, h.rPDT,
-                  h.ddtCoeff, h.q, h.bq, h.clin, h.grad, h.fflux, h.frec, h.flam, h.bjac, h.src, h.blk, h.dg,
+                  h.ddtCoeff, h.q, h.bq, h.clin, h.grad, h.fflux, h.frec, h.flam, h.bjac, h.src, h.vcell,
+                  h.fvisc, h.vsf2, m.dc, h.blk, h.dg,
                   h.dginv, h.rD, h.kv, h.kw, h.kx, h.kb, h.kt, h.dW, h.partials, h.counter, h.ks, h.scratch,
                   h.ibuf};
   drop_graphs(h);
@@ -244,6 +245,7 @@ void build_mesh(Handle& h, const ics_mesh_desc* d) {
   m.nf = upload(nf);
   m.w = upload(std::vector<double>(d->weights, d->weights + F));
   m.nodc = upload(std::vector<double>(d->nonorth_delta_coeffs, d->nonorth_delta_coeffs + F));
+  m.dc = upload(std::vector<double>(d->delta_coeffs, d->delta_coeffs + F));
   m.dOwn = upload(dOwn);
   m.dNei = upload(dNei);
   m.dCC = upload(dCC);
@@ -438,6 +440,14 @@ int do_residual(Handle& h, double* host_src) {
   launch_fields(h);
   launch_grad(h);
   launch_face_flux(h);
+  if (h.cfg.c.viscous) {
+    if (!h.vcell) {
+      h.vcell = dalloc<double>(24ull * h.m.N);
+      h.fvisc = dalloc<double>(8ull * (h.m.F + h.m.B));
+      h.vsf2 = dalloc<double>((size_t)h.m.F);
+    }
+    launch_viscous(h);
+  }
   launch_residual(h, ratio, apply);
   h.haveFlux = true;
   h.lastRhoL2 = rho_l2(h);

@@ -66,6 +66,7 @@ struct DevMesh {
   double* magSf = nullptr;   // [F]
   double* w = nullptr;       // [F]
   double* nodc = nullptr;    // [F]
+  double* dc = nullptr;      // [F] deltaCoeffs 1/|C_nei - C_own|
   double* dOwn = nullptr;    // [3][F] Cf - C[own]
   double* dNei = nullptr;    // [3][F] Cf - C[nei]
   double* dCC = nullptr;     // [3][F] C[nei] - C[own]
@@ -138,6 +139,10 @@ struct Handle {
   double* flam = nullptr;   // [F+B]
   double* bjac = nullptr;   // [25][B] boundary Jacobian diag contribution
   double* src = nullptr;    // [N][5] source = R*V
+  // viscous terms (allocated when the case is viscous)
+  double* vcell = nullptr;  // [24][N] grad U, grad e, tauMC, mu, alphaEff, e
+  double* fvisc = nullptr;  // [8][F+B] lapU, divTau, divSig, lapE face terms
+  double* vsf2 = nullptr;   // [F] LF viscous Jacobian coefficient
   // Jacobian (FP64 or FP32 storage by precision)
   void* blk = nullptr;      // [nslots*25*32]
   void* dg = nullptr;       // [nslices*25*32]
@@ -209,6 +214,7 @@ void launch_bc(Handle& h);
 void launch_set_primitive(Handle& h);
 void launch_derive_primitive(Handle& h);
 void launch_bound_local_timestep(Handle& h);
+void launch_viscous(Handle& h);
 
 // linear algebra: precision-dispatched (mixed = FP32 blocks and vectors)
 void spmv(Handle& h, const void* x, void* y);

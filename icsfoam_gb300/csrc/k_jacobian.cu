@@ -152,7 +152,11 @@ template <typename T>
 __global__ void __launch_bounds__(128) k_jac_rows(DevMesh m, double gamma, const double* __restrict__ frec,
                                                   const double* __restrict__ flam, const double* __restrict__ bjac,
                                                   const double* __restrict__ ddtCoeff, T* __restrict__ blk,
-                                                  T* __restrict__ dg, T* __restrict__ rD, int* __restrict__ status) {
+                                                  T* __restrict__ dg, T* __restrict__ rD, int* __restrict__ status,
+                                                  const double* __restrict__ vsf2) {
+  // vsf2 (viscous cases): LF viscous coefficient 0.5 lambda_v |S| deltaCoeffs,
+  // subtracted from the off-diagonal and added to the diagonal entries
+  // (viscousFluxScheme.C:234-247); nullptr for inviscid cases
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.N) return;
   const int F = m.F, B = m.B;
@@ -185,6 +189,7 @@ __global__ void __launch_bounds__(128) k_jac_rows(DevMesh m, double gamma, const
     const T hs = T(0.5) * magS;
     const T mhs = T(-0.5) * magS;
     const T d = T(0.5) * magS * T(flam[f]);
+    const T sv = vsf2 ? T(vsf2[f]) : T(0);
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
 #pragma unroll
@@ -204,6 +209,8 @@ __global__ void __launch_bounds__(128) k_jac_rows(DevMesh m, double gamma, const
         if (i == j) {
           off -= d;
           diag[k] += d;
+          off -= sv;
+          diag[k] += sv;
         }
         out[k * 32] = off;
       }
@@ -283,14 +290,14 @@ void launch_jacobian(Handle& h) {
   if (prec(h) == ICS_PREC_MIXED) {
     ICS_LAUNCH(h, ICS_K_JAC_ROWS, k_jac_rows<float><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, h.cfg.gamma, h.frec, h.flam, h.bjac,
                                                                    h.ddtCoeff, (float*)h.blk, (float*)h.dg,
-                                                                   (float*)h.rD, status));
+                                                                   (float*)h.rD, status, h.cfg.c.viscous ? h.vsf2 : nullptr));
     if (h.cfg.c.preconditioner == ICS_PC_JACOBI)
       ICS_LAUNCH(h, ICS_K_JACOBI_INV, k_jacobi_inverse<float><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m.N, (float*)h.dg, (float*)h.dginv,
                                                                           status));
   } else {
     ICS_LAUNCH(h, ICS_K_JAC_ROWS, k_jac_rows<double><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, h.cfg.gamma, h.frec, h.flam, h.bjac,
                                                                     h.ddtCoeff, (double*)h.blk, (double*)h.dg,
-                                                                    (double*)h.rD, status));
+                                                                    (double*)h.rD, status, h.cfg.c.viscous ? h.vsf2 : nullptr));
     if (h.cfg.c.preconditioner == ICS_PC_JACOBI)
       ICS_LAUNCH(h, ICS_K_JACOBI_INV, k_jacobi_inverse<double><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m.N, (double*)h.dg, (double*)h.dginv,
                                                                            status));

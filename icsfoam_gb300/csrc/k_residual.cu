@@ -365,10 +365,29 @@ __global__ void __launch_bounds__(128) k_cellres(DevMesh m, CellResParams D, con
                                                  const double* __restrict__ prim, const double* __restrict__ clin,
                                                  double* __restrict__ pseudoCo, double* __restrict__ rPDT,
                                                  double* __restrict__ ddtCoeff, double* __restrict__ src,
-                                                 double* __restrict__ l2cell) {
+                                                 double* __restrict__ l2cell, const double* __restrict__ fvisc) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.N) return;
   const int N = m.N, F = m.F, B = m.B;
+  // viscous terms: laplacian(mu,U), div(tauMC), div(sigmaDotU.S), laplacian(alpha,e),
+  // each summed over the faces and divided by V on its own (residualsUpdate.H:24-42)
+  double vt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (fvisc) {
+    for (int e = m.cptr[c]; e < m.cptr[c + 1]; ++e) {
+      const int code = m.cface[e];
+      const int f = code >= 0 ? code : ~code;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const double v = fvisc[k * FB + f];
+        vt[k] = code >= 0 ? vt[k] + v : vt[k] - v;
+      }
+    }
+    for (int e = m.bptr[c]; e < m.bptr[c + 1]; ++e) {
+      const int b = m.bface[e];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) vt[k] += fvisc[k * FB + F + b];
+    }
+  }
   double dv[5] = {0, 0, 0, 0, 0};
   double rmax = 0.0;
   const int e0 = m.cptr[c], e1 = m.cptr[c + 1];
@@ -401,6 +420,14 @@ __global__ void __launch_bounds__(128) k_cellres(DevMesh m, CellResParams D, con
   for (int k = 0; k < 5; ++k) r[k] = -(dv[k] / Vc);
   const double dV0 = (dv[0] / Vc) * Vc;
   l2cell[c] = dV0 * dV0;
+  if (fvisc) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r[1 + k] = r[1 + k] + vt[k] / Vc;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r[1 + k] = r[1 + k] + vt[3 + k] / Vc;
+    r[4] += vt[6] / Vc;
+    r[4] += vt[7] / Vc;
+  }
   const double rpOld = rPDT[c];
   if (D.ddt != ICS_DDT_STEADY) {
 #pragma unroll
@@ -522,7 +549,8 @@ void launch_residual(Handle& h, double serRatio, bool applySer) {
   D.coMax = h.cfg.c.pseudo_co_num_max;
   const int FB = h.m.F + h.m.B;
   ICS_LAUNCH(h, ICS_K_CELLRES, k_cellres<<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, D, h.fflux, FB, h.flam, h.W, h.W0, h.W00, h.prim,
-                                                         h.clin, h.pseudoCo, h.rPDT, h.ddtCoeff, h.src, h.scratch));
+                                                         h.clin, h.pseudoCo, h.rPDT, h.ddtCoeff, h.src, h.scratch,
+                                                         h.cfg.c.viscous ? h.fvisc : nullptr));
   ICS_CUDA(cudaGetLastError());
 }
 

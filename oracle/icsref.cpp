@@ -113,6 +113,8 @@ struct Case {
   int timeIndex = 0;  // number of begun physical time steps
   // pseudo time
   std::vector<double> pseudoCo, rPseudoDeltaT, ddtCoeff;
+  // LF viscous Jacobian coefficient per internal face (from the last residual)
+  std::vector<double> viscSf2;
   // fluxes of the last calcFlux (F+B)
   std::vector<double> phi, phiE;
   std::vector<V3> phiU;
@@ -614,6 +616,161 @@ void calcFlux(Case& c) {
 }
 
 // ---------------------------------------------------------------------------
+// Viscous terms (residualsUpdate.H:16-43): laminar muEff = mu(T) (constant or
+// Sutherland As sqrt(T)/(1 + Ts/T)), alphaEff = (Cp/Cv) kappa/Cp with
+// kappa = Cp mu / Pr; Gauss linear gradients; Laplacians "Gauss linear
+// corrected" (non-orthogonal correction with linearly interpolated
+// gradients); boundary snGrad = (psi_b - psi_P) deltaCoeffs_b; boundary
+// gradient values corrected to that snGrad (gaussGrad boundary correction).
+// ---------------------------------------------------------------------------
+struct T9 {
+  double a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // row-major, a[3*i+j]
+};
+
+inline double muOf(const Case& c, double T) {
+  if (c.cfg.sutherland) return c.cfg.As * std::sqrt(T) / (1.0 + c.cfg.Ts / T);
+  return c.cfg.mu;
+}
+inline double alphaEffOf(const Case& c, double mu) { return c.cfg.Cp / c.Cv * (mu / c.cfg.Pr); }
+
+// fvc::grad(U) (tensor, (grad U)_ij = d U_j / d x_i) and fvc::grad(e), Gauss linear
+void gaussGradVec(const Case& c, const std::vector<V3>& in, const std::vector<V3>& bf, std::vector<T9>& g) {
+  g.assign(c.N, T9());
+  for (int fi = 0; fi < c.F; ++fi) {
+    const int o = c.own[fi], n = c.nei[fi];
+    for (int j = 0; j < 3; ++j) {
+      const double sf = c.w[fi] * (in[o][j] - in[n][j]) + in[n][j];
+      for (int i = 0; i < 3; ++i) {
+        g[o].a[3 * i + j] += c.Sf[fi][i] * sf;
+        g[n].a[3 * i + j] -= c.Sf[fi][i] * sf;
+      }
+    }
+  }
+  for (int b = 0; b < c.B; ++b)
+    for (int j = 0; j < 3; ++j)
+      for (int i = 0; i < 3; ++i) g[c.bcell[b]].a[3 * i + j] += c.bSf[b][i] * bf[b][j];
+  for (int k = 0; k < c.N; ++k)
+    for (int q = 0; q < 9; ++q) g[k].a[q] /= c.V[k];
+}
+
+struct Viscous {
+  std::vector<double> mu, al, e, muB, alB, eB;
+  std::vector<T9> gU, tau;  // cell values
+  std::vector<V3> ge;
+};
+
+inline T9 devTwoT(const T9& g, double mu) {  // mu dev2(T(g))
+  T9 t;
+  const double tr = g.a[0] + g.a[4] + g.a[8];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) t.a[3 * i + j] = mu * (g.a[3 * j + i] - (i == j ? (2.0 / 3.0) * tr : 0.0));
+  return t;
+}
+
+void viscousFields(const Case& c, Viscous& v) {
+  v.mu.resize(c.N);
+  v.al.resize(c.N);
+  v.e.resize(c.N);
+  v.muB.resize(c.B);
+  v.alB.resize(c.B);
+  v.eB.resize(c.B);
+  for (int i = 0; i < c.N; ++i) {
+    v.mu[i] = muOf(c, c.T[i]);
+    v.al[i] = alphaEffOf(c, v.mu[i]);
+    v.e[i] = c.rhoE[i] / c.rho[i] - 0.5 * magSqr(c.U[i]);
+  }
+  for (int b = 0; b < c.B; ++b) {
+    v.muB[b] = muOf(c, c.TB[b]);
+    v.alB[b] = alphaEffOf(c, v.muB[b]);
+    v.eB[b] = heOf(c, c.TB[b]);
+  }
+  gaussGradVec(c, c.U, c.UB, v.gU);
+  v.tau.resize(c.N);
+  for (int i = 0; i < c.N; ++i) v.tau[i] = devTwoT(v.gU[i], v.mu[i]);
+  VolS E;
+  E.in = v.e;
+  E.bf = v.eB;
+  gaussGrad(c, E, v.ge);
+}
+
+// Viscous face fluxes out of the owner: momentum (laplacian(mu,U) + div(tauMC))
+// and energy (div(sigmaDotU . S) + laplacian(alphaEff, e)), each term kept
+// separate as in residualsUpdate.H, plus the LF viscous Jacobian coefficient
+// sf2 = 0.5 lambda_v |S| deltaCoeffs (viscousFluxScheme.C:234-247).
+void viscousFluxes(const Case& c, const Viscous& v, std::vector<V3>& lapU, std::vector<V3>& divTau,
+                   std::vector<double>& divSig, std::vector<double>& lapE, std::vector<double>& sf2) {
+  const int NF = c.F + c.B;
+  lapU.assign(NF, V3());
+  divTau.assign(NF, V3());
+  divSig.assign(NF, 0.0);
+  lapE.assign(NF, 0.0);
+  sf2.assign(c.F, 0.0);
+  for (int fi = 0; fi < c.F; ++fi) {
+    const int o = c.own[fi], n = c.nei[fi];
+    const double wf = c.w[fi];
+    auto lin = [&](double a, double b) { return wf * (a - b) + b; };
+    const double muf = lin(v.mu[o], v.mu[n]), alf = lin(v.al[o], v.al[n]);
+    const double ms = c.magSf[fi];
+    const V3 d = c.C[n] - c.C[o];
+    const V3 unit = c.Sf[fi] / ms;
+    const V3 kcor = unit - d * c.nodc[fi];  // non-orthogonal correction vector
+    T9 gUf, tf;
+    for (int q = 0; q < 9; ++q) {
+      gUf.a[q] = lin(v.gU[o].a[q], v.gU[n].a[q]);
+      tf.a[q] = lin(v.tau[o].a[q], v.tau[n].a[q]);
+    }
+    V3 Uf, snU;
+    for (int j = 0; j < 3; ++j) {
+      Uf[j] = lin(c.U[o][j], c.U[n][j]);
+      const double corr = kcor.x * gUf.a[j] + kcor.y * gUf.a[3 + j] + kcor.z * gUf.a[6 + j];
+      snU[j] = c.nodc[fi] * (c.U[n][j] - c.U[o][j]) + corr;
+    }
+    lapU[fi] = (muf * ms) * snU;
+    for (int j = 0; j < 3; ++j)
+      divTau[fi][j] = c.Sf[fi].x * tf.a[j] + c.Sf[fi].y * tf.a[3 + j] + c.Sf[fi].z * tf.a[6 + j];
+    V3 sig;
+    for (int i = 0; i < 3; ++i) {
+      double s = 0;
+      for (int j = 0; j < 3; ++j) s += (muf * gUf.a[3 * i + j] + tf.a[3 * i + j]) * Uf[j];
+      sig[i] = s;
+    }
+    divSig[fi] = dot(sig, c.Sf[fi]);
+    const V3 gef(lin(v.ge[o].x, v.ge[n].x), lin(v.ge[o].y, v.ge[n].y), lin(v.ge[o].z, v.ge[n].z));
+    const double snE = c.nodc[fi] * (v.e[n] - v.e[o]) + dot(kcor, gef);
+    lapE[fi] = (alf * ms) * snE;
+    const double rhof = lin(c.rho[o], c.rho[n]);
+    const double lamv = (muf + alf) / rhof;
+    sf2[fi] = 0.5 * lamv * ms * c.dc[fi];
+  }
+  for (int b = 0; b < c.B; ++b) {
+    const int o = c.bcell[b];
+    const double ms = c.bmagSf[b];
+    const V3 n = c.bSf[b] / ms;
+    V3 snU;
+    for (int j = 0; j < 3; ++j) snU[j] = (c.UB[b][j] - c.U[o][j]) * c.bdc[b];
+    const double snE = (v.eB[b] - v.e[o]) * c.bdc[b];
+    // boundary gradient: cell gradient with its normal part replaced by snGrad
+    T9 gUb = v.gU[o];
+    for (int j = 0; j < 3; ++j) {
+      const double ng = n.x * v.gU[o].a[j] + n.y * v.gU[o].a[3 + j] + n.z * v.gU[o].a[6 + j];
+      for (int i = 0; i < 3; ++i) gUb.a[3 * i + j] += n[i] * (snU[j] - ng);
+    }
+    const T9 tb = devTwoT(gUb, v.muB[b]);
+    lapU[c.F + b] = (v.muB[b] * ms) * snU;
+    for (int j = 0; j < 3; ++j)
+      divTau[c.F + b][j] = c.bSf[b].x * tb.a[j] + c.bSf[b].y * tb.a[3 + j] + c.bSf[b].z * tb.a[6 + j];
+    V3 sig;
+    for (int i = 0; i < 3; ++i) {
+      double s = 0;
+      for (int j = 0; j < 3; ++j) s += (v.muB[b] * gUb.a[3 * i + j] + tb.a[3 * i + j]) * c.UB[b][j];
+      sig[i] = s;
+    }
+    divSig[c.F + b] = dot(sig, c.bSf[b]);
+    lapE[c.F + b] = (v.alB[b] * ms) * snE;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Dual-time ddt (dualTimeDdtScheme.C:111-126 around Euler/backward/steady)
 // ---------------------------------------------------------------------------
 struct DdtCoeffs {
@@ -669,6 +826,38 @@ void residualSource(Case& c) {
     divU[o] = divU[o] + c.phiU[c.F + b];
     divE[o] += c.phiE[c.F + b];
   }
+  // viscous divergences, one per fvc term of residualsUpdate.H:24-42
+  std::vector<V3> dLapU, dTau;
+  std::vector<double> dSig, dLapE;
+  if (c.cfg.viscous) {
+    Viscous v;
+    viscousFields(c, v);
+    std::vector<V3> lapU, divTau;
+    std::vector<double> divSig, lapE;
+    viscousFluxes(c, v, lapU, divTau, divSig, lapE, c.viscSf2);
+    dLapU.assign(c.N, V3());
+    dTau.assign(c.N, V3());
+    dSig.assign(c.N, 0.0);
+    dLapE.assign(c.N, 0.0);
+    for (int fi = 0; fi < c.F; ++fi) {
+      const int o = c.own[fi], n = c.nei[fi];
+      dLapU[o] = dLapU[o] + lapU[fi];
+      dLapU[n] = dLapU[n] - lapU[fi];
+      dTau[o] = dTau[o] + divTau[fi];
+      dTau[n] = dTau[n] - divTau[fi];
+      dSig[o] += divSig[fi];
+      dSig[n] -= divSig[fi];
+      dLapE[o] += lapE[fi];
+      dLapE[n] -= lapE[fi];
+    }
+    for (int b = 0; b < c.B; ++b) {
+      const int o = c.bcell[b];
+      dLapU[o] = dLapU[o] + lapU[c.F + b];
+      dTau[o] = dTau[o] + divTau[c.F + b];
+      dSig[o] += divSig[c.F + b];
+      dLapE[o] += lapE[c.F + b];
+    }
+  }
   double l2 = 0;
   c.src.assign(5 * c.N, 0.0);
   const DdtCoeffs d = ddtCoeffs(c);
@@ -679,6 +868,12 @@ void residualSource(Case& c) {
     V3 rU = -1.0 * (divU[i] / Vc);
     double rE = -(divE[i] / Vc);
     l2 += sqr((divR[i] / Vc) * Vc);
+    if (c.cfg.viscous) {
+      rU = rU + dLapU[i] / Vc;
+      rU = rU + dTau[i] / Vc;
+      rE += dSig[i] / Vc;
+      rE += dLapE[i] / Vc;
+    }
     if (!steady) {
       double dg, s;
       ddtMatrix(c, d, i, c.rho[i], c.rho0[i], c.rho00[i], dg, s);
@@ -937,6 +1132,20 @@ void assembleJacobian(Case& c) {
   for (int i = 0; i < c.N; ++i) {
     const double dc = c.ddtCoeff[i] * c.V[i];
     for (int q = 0; q < 5; ++q) c.diag[i].a[diagIdx[q]] += dc;
+  }
+  // viscousFluxScheme::createViscousJacobian, LaxFriedrichJacobian:
+  // minus laplacian(0.5 lambda_v, 1) on rho, rhoU (x I), rhoE (viscousFluxScheme.C:234-247)
+  if (c.cfg.viscous && (int)c.viscSf2.size() == c.F) {
+    for (int fi = 0; fi < c.F; ++fi) {
+      const double s = c.viscSf2[fi];
+      for (int q = 0; q < 5; ++q) {
+        const int k = diagIdx[q];
+        c.upper[fi].a[k] -= s;
+        c.lower[fi].a[k] -= s;
+        c.diag[c.own[fi]].a[k] += s;
+        c.diag[c.nei[fi]].a[k] += s;
+      }
+    }
   }
   (void)NF;
   c.haveMatrix = true;

@@ -139,10 +139,47 @@ def test_sod_shock_tube_against_exact_solution(oracle_binding):
 @pytest.mark.parametrize("recon", [0, 1, 3])
 def test_freestream_preservation(oracle_binding, flux, recon):
     w = cases.random_box(5)
-    h = open_oracle(oracle_binding, w, flux_scheme=flux, recon_rho=recon, recon_U=recon, recon_T=recon)
+    h = open_oracle(oracle_binding, w, flux_scheme=flux, recon_rho=recon, recon_U=recon, recon_T=recon, viscous=0)
     s = h.residual()
     scale = 1e4 * np.abs(w.mesh.Sf).max()  # p |S|
     assert np.abs(s).max() < 1e-11 * scale
+
+
+# ------------------------------------------------------------ viscous terms
+def test_viscous_shear_flow_known_answer(oracle_binding):
+    """U = (a y, 0, 0), uniform p and T, constant mu on an orthogonal box.
+
+    Interior cells: the viscous momentum source vanishes (the velocity is
+    linear and divergence free) and the viscous energy source equals the
+    dissipation mu a^2 per unit volume (div of sigma.U).
+    """
+    n, a, mu = 8, 300.0, 1.8e-3
+    w = cases.random_box(n, jitter=0.0, ordering_mode="natural")
+    y = w.mesh.C[:, 1]
+    w.U = np.zeros((w.mesh.n_cells, 3))
+    w.U[:, 0] = a * y
+    w.p[:] = 1e5
+    w.T[:] = 300.0
+    res = {}
+    for visc in (0, 1):
+        h = open_oracle(oracle_binding, w, viscous=visc, sutherland=0, mu=mu, recon_rho=0, recon_U=0, recon_T=0)
+        res[visc] = h.residual()
+    dv = (res[1] - res[0]) / w.mesh.V[:, None]
+    ijk = w.mesh.cell_ijk
+    inner = np.all((ijk >= 2) & (ijk <= n - 3), axis=1)
+    assert inner.sum() > 0
+    assert np.abs(dv[inner, 1:4]).max() < 1e-9 * mu * a * n   # momentum: zero to round-off
+    assert np.allclose(dv[inner, 4], mu * a * a, rtol=1e-9)
+
+
+def test_sutherland_viscosity(oracle_binding):
+    w = cases.random_box(4)
+    s = w.settings
+    T = 220.0
+    mu = s["As"] * np.sqrt(T) / (1 + s["Ts"] / T)
+    rho = 1e4 / (287.0 * T)
+    u = 2.0 * np.sqrt(1.4 * 287.0 * T)
+    assert abs(rho * u / mu - 1e5) < 1e-6 * 1e5
 
 
 # ------------------------------------------------------- Jacobian structure

@@ -35,6 +35,7 @@ FLUX = {"AUSMPlusUp": 0, "HLLC": 1, "ROE": 2}
 RECON = {"upwind": 0, "vanLeer": 1, "Minmod": 2, "MUSCLVenkatakrishnan": 3, "MUSCLMinmod": 4}
 DDT = {"steadyState": 0, "Euler": 1, "backward": 2}
 PRECON = {"none": 0, "LUSGS": 1, "Jacobi": 2}
+SOLVER = {"GMRES": 0, "smoothSolverCoupled": 1}
 PRECISION = {"fp64": 0, "mixed": 1}
 
 
@@ -82,6 +83,7 @@ class Config(C.Structure):
         ("local_timestepping_lower_bound", C.c_double),
         ("reset_pseudo", C.c_int32),
         ("rho_min", C.c_double), ("T_min", C.c_double), ("T_max", C.c_double),
+        ("n_sweeps", C.c_int32),
     ]
 
 

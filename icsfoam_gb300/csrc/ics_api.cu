@@ -130,7 +130,8 @@ int validate_config(const ics_config* c, std::string& err) {
     err = "Unknown convectiveFluxScheme";
     return ICS_ERR_SCHEME;
   }
-  if (c->solver != ICS_SOLVER_GMRES || c->preconditioner < 0 || c->preconditioner > 2) {
+  if ((c->solver != ICS_SOLVER_GMRES && c->solver != ICS_SOLVER_SMOOTH) || c->preconditioner < 0 ||
+      c->preconditioner > 2 || c->n_sweeps < 1) {
     err = "Unknown solver or preconditioner";
     return ICS_ERR_SCHEME;
   }
@@ -594,6 +595,7 @@ void ics_default_config(ics_config* c) {
   c->rho_min = -GREAT;
   c->T_min = SMALL;
   c->T_max = GREAT;
+  c->n_sweeps = 1;
 }
 
 int ics_create(const ics_mesh_desc* mesh, const ics_config* cfg, ics_handle* out) {

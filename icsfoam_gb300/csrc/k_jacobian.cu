@@ -291,14 +291,14 @@ void launch_jacobian(Handle& h) {
     ICS_LAUNCH(h, ICS_K_JAC_ROWS, k_jac_rows<float><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, h.cfg.gamma, h.frec, h.flam, h.bjac,
                                                                    h.ddtCoeff, (float*)h.blk, (float*)h.dg,
                                                                    (float*)h.rD, status, h.cfg.c.viscous ? h.vsf2 : nullptr));
-    if (h.cfg.c.preconditioner == ICS_PC_JACOBI)
+    if (h.cfg.c.preconditioner == ICS_PC_JACOBI || h.cfg.c.solver == ICS_SOLVER_SMOOTH)
       ICS_LAUNCH(h, ICS_K_JACOBI_INV, k_jacobi_inverse<float><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m.N, (float*)h.dg, (float*)h.dginv,
                                                                           status));
   } else {
     ICS_LAUNCH(h, ICS_K_JAC_ROWS, k_jac_rows<double><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, h.cfg.gamma, h.frec, h.flam, h.bjac,
                                                                     h.ddtCoeff, (double*)h.blk, (double*)h.dg,
                                                                     (double*)h.rD, status, h.cfg.c.viscous ? h.vsf2 : nullptr));
-    if (h.cfg.c.preconditioner == ICS_PC_JACOBI)
+    if (h.cfg.c.preconditioner == ICS_PC_JACOBI || h.cfg.c.solver == ICS_SOLVER_SMOOTH)
       ICS_LAUNCH(h, ICS_K_JACOBI_INV, k_jacobi_inverse<double><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m.N, (double*)h.dg, (double*)h.dginv,
                                                                            status));
   }

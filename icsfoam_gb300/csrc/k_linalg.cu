@@ -626,6 +626,118 @@ static bool stop_test(const Handle& h, const ics_solver_perf& p) {
   return p.n_iterations >= c.max_iter || mx < c.tolerance || mrel < c.rel_tol;
 }
 
+// Norm factors of coupledMatrixSolver (gmres.C:812-850): sum |A (W - avg W)| +
+// |b| per equation (vector magnitude for rhoU), and the initial L1 residuals.
+template <typename TB, typename TV>
+static void norm_factors_t(Handle& h, double nf[3], ics_solver_perf& p) {
+  const int N = h.m.N;
+  cudaStream_t st = h.stream;
+  KrylovScalars* ks = h.ks;
+  TV* w = (TV*)h.kw;
+  TV* t = (TV*)h.kt;
+  double* red = ks->red;
+  ICS_CUDA(cudaMemsetAsync(&ks->status, 0, sizeof(int), st));
+  ICS_LAUNCH(h, ICS_K_VECTOR, k_wsum<<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.W, h.partials, h.counter, red));
+  ICS_LAUNCH(h, ICS_K_SCALAR, k_avg<<<1, 1, 0, st>>>(ks, N));
+  ICS_LAUNCH(h, ICS_K_VECTOR, k_wmavg<TV><<<grid_for(N, 256), 256, 0, st>>>(N, h.W, ks, w));
+  spmv_t<TB, TV>(h, w, t);
+  ICS_LAUNCH(h, ICS_K_VECTOR,
+             k_normfac<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.src, t, h.partials, h.counter, red));
+  ICS_CUDA(cudaMemcpyAsync(h.ksHost->red, red, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  ICS_CUDA(cudaStreamSynchronize(st));
+  for (int k = 0; k < 3; ++k) nf[k] = h.ksHost->red[k] + VSMALL;
+  memset(&p, 0, sizeof(p));
+  p.init_res[0] = h.ksHost->red[3] / nf[0];
+  p.init_res[1] = h.ksHost->red[4] / nf[2];
+  p.init_res[2] = h.ksHost->red[5] / nf[2];
+  p.init_res[3] = h.ksHost->red[6] / nf[2];
+  p.init_res[4] = h.ksHost->red[7] / nf[1];
+  for (int k = 0; k < 5; ++k) p.final_res[k] = p.init_res[k];
+}
+
+// x_new = D^-1 (b - (A - D) x_old): one block-Jacobi sweep (JacobiSmoother::smooth)
+template <typename TB, typename TV>
+__global__ void __launch_bounds__(128) k_jacobi_sweep(DevMesh m, const TB* __restrict__ blk,
+                                                      const TB* __restrict__ inv, const double* __restrict__ b,
+                                                      const TV* __restrict__ xo, TV* __restrict__ xn) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.N) return;
+  const int s = c >> 5, lane = c & 31;
+  TV acc[5] = {TV(0), TV(0), TV(0), TV(0), TV(0)};
+  const int base = m.slot_base[s];
+  for (int t = 0; t < m.nslot[c]; ++t) {
+    const int col = m.scol[(base + t) * 32 + lane];
+    const TB* Bk = blk + (size_t)(base + t) * 25 * 32 + lane;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      TV a = TV(0);
+#pragma unroll
+      for (int j = 0; j < 5; ++j) a += TV(Bk[(5 * i + j) * 32]) * xo[5 * col + j];
+      acc[i] += a;
+    }
+  }
+  TV r[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) r[k] = -(acc[k] - TV(b[5 * c + k]));
+  const TB* D = inv + (size_t)s * 25 * 32 + lane;
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    TV a = TV(0);
+#pragma unroll
+    for (int j = 0; j < 5; ++j) a += TV(D[(5 * i + j) * 32]) * r[j];
+    xn[5 * c + i] = a;
+  }
+}
+
+// smoothSolverCoupled::solveDelta (smoothSolverCoupled.C:369-515)
+template <typename TB, typename TV>
+static int smooth_t(Handle& h, ics_solver_perf* perf) {
+  const int N = h.m.N;
+  const long n5 = 5L * N;
+  cudaStream_t st = h.stream;
+  KrylovScalars* ks = h.ks;
+  double nf[3];
+  ics_solver_perf p;
+  norm_factors_t<TB, TV>(h, nf, p);
+  TV* x = (TV*)h.kx;
+  TV* y = (TV*)h.kb;
+  TV* t = (TV*)h.kt;
+  TV* r = (TV*)h.kw;
+  ICS_CUDA(cudaMemsetAsync(x, 0, n5 * sizeof(TV), st));
+  do {
+    for (int s = 0; s < h.cfg.c.n_sweeps; ++s) {
+      ICS_LAUNCH(h, ICS_K_JACOBI,
+                 k_jacobi_sweep<TB, TV><<<grid_for(N, 128), 128, 0, st>>>(h.m, (const TB*)h.blk, (const TB*)h.dginv,
+                                                                          h.src, x, y));
+      TV* tmp = x;
+      x = y;
+      y = tmp;
+    }
+    spmv_t<TB, TV>(h, x, t);
+    ICS_LAUNCH(h, ICS_K_VECTOR,
+               k_resid<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.src, t, r, h.partials, h.counter, ks->res));
+    ICS_CUDA(cudaGetLastError());
+    ICS_CUDA(cudaMemcpyAsync(h.ksHost->res, ks->res, 5 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    ICS_CUDA(cudaStreamSynchronize(st));
+    const double* rs = h.ksHost->res;
+    p.final_res[0] = rs[0] / nf[0];
+    p.final_res[4] = rs[4] / nf[1];
+    for (int k = 0; k < 3; ++k) p.final_res[1 + k] = h.m.solD[k] == -1 ? 0.0 : rs[1 + k] / nf[2];
+    p.n_iterations += h.cfg.c.n_sweeps;
+    bool finite = true;
+    for (int k = 0; k < 5; ++k) finite = finite && std::isfinite(p.final_res[k]);
+    if (!finite) break;
+  } while (!stop_test(h, p));
+  bool finite = true;
+  for (int k = 0; k < 5; ++k) finite = finite && std::isfinite(p.final_res[k]);
+  p.converged = finite;
+  ICS_LAUNCH(h, ICS_K_VECTOR,
+             k_to_dW<TV><<<grid_for(N, 256), 256, 0, st>>>(N, x, h.dW, h.m.solD[0], h.m.solD[1], h.m.solD[2]));
+  ICS_CUDA(cudaGetLastError());
+  *perf = p;
+  return finite ? ICS_OK : ICS_ERR_NONFINITE;
+}
+
 template <typename TB, typename TV>
 static int gmres_t(Handle& h, ics_solver_perf* perf) {
   const int N = h.m.N, m = h.cfg.c.n_directions;
@@ -638,25 +750,9 @@ static int gmres_t(Handle& h, ics_solver_perf* perf) {
   TV* x = (TV*)h.kx;
   TV* t = (TV*)h.kt;
   double* red = ks->red;
-  ICS_CUDA(cudaMemsetAsync(&ks->status, 0, sizeof(int), st));
-  // norm factors: A (W - avg(W))
-  ICS_LAUNCH(h, ICS_K_VECTOR, k_wsum<<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.W, h.partials, h.counter, red));
-  ICS_LAUNCH(h, ICS_K_SCALAR, k_avg<<<1, 1, 0, st>>>(ks, N));
-  ICS_LAUNCH(h, ICS_K_VECTOR, k_wmavg<TV><<<grid_for(N, 256), 256, 0, st>>>(N, h.W, ks, w));
-  spmv_t<TB, TV>(h, w, t);
-  ICS_LAUNCH(h, ICS_K_VECTOR, k_normfac<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.src, t, h.partials, h.counter, red));
-  ICS_CUDA(cudaMemcpyAsync(h.ksHost->red, red, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
-  ICS_CUDA(cudaStreamSynchronize(st));
   double nf[3];
-  for (int k = 0; k < 3; ++k) nf[k] = h.ksHost->red[k] + VSMALL;
   ics_solver_perf p;
-  memset(&p, 0, sizeof(p));
-  p.init_res[0] = h.ksHost->red[3] / nf[0];
-  p.init_res[1] = h.ksHost->red[4] / nf[2];
-  p.init_res[2] = h.ksHost->red[5] / nf[2];
-  p.init_res[3] = h.ksHost->red[6] / nf[2];
-  p.init_res[4] = h.ksHost->red[7] / nf[1];
-  for (int k = 0; k < 5; ++k) p.final_res[k] = p.init_res[k];
+  norm_factors_t<TB, TV>(h, nf, p);
   // r = b, x = 0
   ICS_CUDA(cudaMemsetAsync(x, 0, n5 * sizeof(TV), st));
   to_vec(h, h.src, w);
@@ -741,6 +837,10 @@ static int gmres_t(Handle& h, ics_solver_perf* perf) {
 }
 
 int gmres_solve(Handle& h, ics_solver_perf* perf) {
+  if (h.cfg.c.solver == ICS_SOLVER_SMOOTH) {
+    if (prec(h) == ICS_PREC_MIXED) return smooth_t<float, float>(h, perf);
+    return smooth_t<double, double>(h, perf);
+  }
   if (prec(h) == ICS_PREC_MIXED) return gmres_t<float, float>(h, perf);
   return gmres_t<double, double>(h, perf);
 }

@@ -88,14 +88,20 @@ def config_from_dicts(binding: abi.Binding, fvSchemes: Dict, fvSolution: Dict, t
         setattr(cfg, attr, reconstruction_scheme(entry, gentry))
     fs = fvSolution.get("flowSolver", {})
     sname = _strip_gpu(fs.get("solver", "GMRES"))
-    if sname != "GMRES":
-        raise ValueError("Unknown solver type %s; valid types: [GMRES]" % sname)
+    if sname not in abi.SOLVER:
+        raise ValueError("Unknown solver type %s; valid types: %s" % (sname, sorted(abi.SOLVER)))
+    cfg.solver = abi.SOLVER[sname]
     sd = fs.get(sname, fs.get(sname + "GPU", {}))
-    pc = sd.get("preconditioner", "LUSGS")
-    if pc not in abi.PRECON:
-        raise ValueError("Unknown preconditioner %s" % pc)
-    cfg.preconditioner = abi.PRECON[pc]
-    cfg.n_directions = int(sd["nDirections"])
+    if sname == "smoothSolverCoupled":
+        if sd.get("smoother", "Jacobi") != "Jacobi":
+            raise ValueError("Unknown smoother %s; valid types: [Jacobi]" % sd.get("smoother"))
+        cfg.n_sweeps = int(sd.get("nSweeps", 1))
+    else:
+        pc = sd.get("preconditioner", "LUSGS")
+        if pc not in abi.PRECON:
+            raise ValueError("Unknown preconditioner %s" % pc)
+        cfg.preconditioner = abi.PRECON[pc]
+        cfg.n_directions = int(sd["nDirections"])
     cfg.max_iter = int(sd.get("maxIter", 1000))
     cfg.min_iter = int(sd.get("minIter", 0))
     cfg.tolerance = float(sd["tolerance"])

@@ -55,8 +55,9 @@ enum {
 };
 /* ddtSchemes default dualTime rPseudoDeltaT <scheme> (dualTimeDdtScheme.H:109-118) */
 enum { ICS_DDT_STEADY = 0, ICS_DDT_EULER = 1, ICS_DDT_BACKWARD = 2 };
-/* flowSolver/solver (coupledMatrixSolver.C:41-67)                               */
-enum { ICS_SOLVER_GMRES = 0 };
+/* flowSolver/solver (coupledMatrixSolver.C:41-67): GMRES (gmres.C) or
+ * smoothSolverCoupled (smoothSolverCoupled.C:369-515, block-Jacobi sweeps)      */
+enum { ICS_SOLVER_GMRES = 0, ICS_SOLVER_SMOOTH = 1 };
 /* flowSolver/<solver>/preconditioner (coupledMatrix.H:296-369)                  */
 enum { ICS_PC_NONE = 0, ICS_PC_LUSGS = 1, ICS_PC_JACOBI = 2 };
 /* precision of the linear solve: FP64 everywhere, or FP32 Jacobian blocks,
@@ -135,6 +136,8 @@ typedef struct {
   double local_timestepping_lower_bound;
   int32_t reset_pseudo;
   double rho_min, T_min, T_max;
+  /* smoothSolverCoupled: Jacobi sweeps per stop test (nSweeps)            */
+  int32_t n_sweeps;
 } ics_config;
 
 /* residualsIO (residualsIO.H:54-315): L1 residuals normalised per equation. */

@@ -1411,6 +1411,71 @@ int gmresSolveDelta(Case& c, const std::vector<double>& W, ics_solver_perf& perf
   return status;
 }
 
+// smoothSolverCoupled::solveDelta (smoothSolverCoupled.C:369-515) with the
+// Jacobi smoother (JacobiSmoother.C:42-205): same norm factors as GMRES, then
+// nSweeps sweeps x <- D^-1 (b - (A - D) x) between stop tests.
+int smoothSolveDelta(Case& c, const std::vector<double>& W, ics_solver_perf& perf, std::vector<double>& dx) {
+  const int N = c.N, n5 = 5 * N;
+  const double* b = c.src.data();
+  std::memset(&perf, 0, sizeof(perf));
+  double avg[5] = {0, 0, 0, 0, 0};
+  for (int i = 0; i < N; ++i)
+    for (int k = 0; k < 5; ++k) avg[k] += W[5 * i + k];
+  for (int k = 0; k < 5; ++k) avg[k] /= N;
+  std::vector<double> wmr(n5), tmp(n5);
+  for (int i = 0; i < N; ++i)
+    for (int k = 0; k < 5; ++k) wmr[5 * i + k] = W[5 * i + k] - avg[k];
+  matrixMul(c, wmr.data(), tmp.data());
+  double nf[3] = {0, 0, 0};
+  for (int i = 0; i < N; ++i) {
+    nf[0] += std::fabs(tmp[5 * i]) + std::fabs(b[5 * i]);
+    nf[1] += std::fabs(tmp[5 * i + 4]) + std::fabs(b[5 * i + 4]);
+    const V3 t(tmp[5 * i + 1], tmp[5 * i + 2], tmp[5 * i + 3]);
+    const V3 s(b[5 * i + 1], b[5 * i + 2], b[5 * i + 3]);
+    nf[2] += mag(t) + mag(s);
+  }
+  for (int k = 0; k < 3; ++k) nf[k] += VSMALL;
+  l1Residual(c, b, nf, perf.init_res);
+  std::memcpy(perf.final_res, perf.init_res, sizeof(perf.init_res));
+  std::vector<B5> inv(N);
+  for (int i = 0; i < N; ++i)
+    if (!inv5(c.diag[i], inv[i])) {
+      c.err = "singular diagonal block";
+      return ICS_ERR_DIAG;
+    }
+  dx.assign(n5, 0.0);
+  std::vector<double> r(n5);
+  do {
+    for (int s = 0; s < c.cfg.n_sweeps; ++s) {
+      // t = (A - D) x  (matrixMulNoDiag), then x = D^-1 (b - t)
+      std::fill(tmp.begin(), tmp.end(), 0.0);
+      for (int fi = 0; fi < c.F; ++fi) {
+        const int l = c.own[fi], u = c.nei[fi];
+        bmv(c.lower[fi], dx.data() + 5 * l, tmp.data() + 5 * u, 1.0);
+        bmv(c.upper[fi], dx.data() + 5 * u, tmp.data() + 5 * l, 1.0);
+      }
+      for (int i = 0; i < N; ++i) {
+        double t[5];
+        for (int k = 0; k < 5; ++k) t[k] = -(tmp[5 * i + k] - b[5 * i + k]);
+        double z[5] = {0, 0, 0, 0, 0};
+        bmv(inv[i], t, z, 1.0);
+        for (int k = 0; k < 5; ++k) dx[5 * i + k] = z[k];
+      }
+    }
+    matrixMul(c, dx.data(), r.data());
+    for (int q = 0; q < n5; ++q) r[q] = b[q] - r[q];
+    l1Residual(c, r.data(), nf, perf.final_res);
+    for (int k = 0; k < 3; ++k)
+      if (c.solD[k] == -1) perf.final_res[1 + k] = 0.0;
+    perf.n_iterations += c.cfg.n_sweeps;
+  } while (!stopTest(c, perf));
+  perf.converged = 1;
+  for (int k = 0; k < 3; ++k)
+    if (c.solD[k] == -1)
+      for (int i = 0; i < N; ++i) dx[5 * i + 1 + k] = 0.0;
+  return ICS_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Boundary conditions and field update (updateFields.H)
 // ---------------------------------------------------------------------------
@@ -1657,6 +1722,7 @@ void icsref_default_config(ics_config* c) {
   c->rho_min = -GREAT;
   c->T_min = SMALL;
   c->T_max = GREAT;
+  c->n_sweeps = 1;
 }
 
 int icsref_set_config(ics_handle h, const ics_config* cfg) {
@@ -1665,7 +1731,8 @@ int icsref_set_config(ics_handle h, const ics_config* cfg) {
     h->err = "Unknown convectiveFluxScheme";
     return ICS_ERR_SCHEME;
   }
-  if (cfg->preconditioner < 0 || cfg->preconditioner > 2 || cfg->solver != ICS_SOLVER_GMRES) {
+  if (cfg->preconditioner < 0 || cfg->preconditioner > 2 ||
+      (cfg->solver != ICS_SOLVER_GMRES && cfg->solver != ICS_SOLVER_SMOOTH) || cfg->n_sweeps < 1) {
     h->err = "Unknown solver or preconditioner";
     return ICS_ERR_SCHEME;
   }
@@ -1957,7 +2024,8 @@ int icsref_solve_increment(ics_handle h, ics_solver_perf* perf, double* dW) {
   if (!c.haveMatrix) return ICS_ERR_STATE;
   storeW(c, c.Wprev);
   ics_solver_perf pf;
-  int st = gmresSolveDelta(c, c.Wprev, pf, c.dW);
+  int st = c.cfg.solver == ICS_SOLVER_SMOOTH ? smoothSolveDelta(c, c.Wprev, pf, c.dW)
+                                             : gmresSolveDelta(c, c.Wprev, pf, c.dW);
   c.haveIncrement = true;
   if (perf) *perf = pf;
   if (dW) std::memcpy(dW, c.dW.data(), sizeof(double) * 5 * c.N);

@@ -109,6 +109,22 @@ def test_jacobi_preconditioner_parity(gpu_binding, oracle_binding):
     assert np.abs(dg - do).max() < 1e-9 * np.abs(do).max()
 
 
+@pytest.mark.parametrize("precision,tol", [(0, 1e-10), (1, 1e-4)])
+def test_smooth_solver_parity(gpu_binding, oracle_binding, precision, tol):
+    """smoothSolverCoupled (block-Jacobi sweeps) against the oracle."""
+    w = cases.bump_channel(10, 4, 3, ordering_mode="colour")
+    over = dict(solver=1, n_sweeps=2, max_iter=12, rel_tol=1e-6)
+    hg = open_case(gpu_binding, w, precision=precision, **over)
+    ho = open_case(oracle_binding, w, **over)
+    for h in (hg, ho):
+        h.residual()
+        h.assemble_jacobian()
+    pg, dg, _ = hg.solve_increment()
+    po, do, _ = ho.solve_increment()
+    assert pg.n_iterations == po.n_iterations
+    assert np.abs(dg - do).max() < tol * np.abs(do).max()
+
+
 def test_profiling_counts_launches(gpu_binding):
     w = cases.bump_channel(8, 4, 2, ordering_mode="colour")
     h = open_case(gpu_binding, w)

@@ -278,6 +278,20 @@ def test_lusgs_is_the_factored_sgs_operator(small_system):
     assert np.allclose(P @ z, r, rtol=1e-10, atol=1e-10 * np.abs(r).max())
 
 
+def test_smooth_solver_converges_to_dense_solve(oracle_binding):
+    w = cases.bump_channel(6, 3, 2, ordering_mode="natural")
+    # absolute stop test: the z-momentum initial residual is ~0 here, so the
+    # reference's relative test (final/initial per component) cannot fire
+    h = open_oracle(oracle_binding, w, solver=1, n_sweeps=3, tolerance=1e-13, rel_tol=1e-300, max_iter=3000)
+    b = h.residual()
+    h.assemble_jacobian()
+    A = dense(h, *h.get_jacobian())
+    perf, dW, st = h.solve_increment()
+    ref = np.linalg.solve(A, b.ravel()).reshape(-1, 5)
+    assert perf.n_iterations % 3 == 0 and perf.n_iterations < 3000
+    assert np.abs(dW - ref).max() < 1e-8 * np.abs(ref).max()
+
+
 def test_jacobi_is_block_diagonal_inverse(oracle_binding):
     w = cases.bump_channel(6, 3, 2, ordering_mode="natural")
     h = open_oracle(oracle_binding, w, preconditioner=2)

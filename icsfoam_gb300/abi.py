@@ -127,6 +127,7 @@ _FUNCS = {
     "pseudo_iteration": (C.c_int, [_P, C.POINTER(IterStats)]),
     "begin_time_step": (C.c_int, [_P]),
     "pseudo_loop": (C.c_int, [_P, C.POINTER(C.c_int32)]),
+    "set_hb": (C.c_int, [_P, C.c_int32, _P]),
 }
 
 # measurement entry points (CUDA library only)
@@ -349,6 +350,10 @@ class CaseHandle:
 
     def begin_time_step(self):
         self._check(self.b.fn["begin_time_step"](self.h), "begin_time_step")
+
+    def set_hb(self, n_instances: int, D):
+        D = np.ascontiguousarray(D, np.float64).reshape(n_instances, n_instances)
+        self._check(self.b.fn["set_hb"](self.h, int(n_instances), _ptr(D)), "set_hb")
 
     def pseudo_loop(self) -> bool:
         more = C.c_int32()

@@ -9,6 +9,9 @@ here is generated from fixed seeds:
                      outlet, slip walls (the transonic circularArcBump layout).
 * ``random_box``   - hex box with randomly displaced interior vertices, cells
                      randomly permuted then reverse-Cuthill-McKee renumbered.
+* ``hb_bump_channel`` - Harmonic Balance version of the bump channel: a
+                     time-periodic outlet static pressure, 2H+1 stacked
+                     instances and the spectral operator D.
 
 Sizes are parameters; the headline sizes are 1000 cells, 256x64x64 and 200^3.
 """
@@ -32,6 +35,7 @@ class Workload:
     U: np.ndarray
     T: np.ndarray
     settings: Dict  # ics_config field overrides
+    hb: Optional[tuple] = None  # Harmonic Balance (n_instances, D) or None
 
 
 GAMMA = 1.4
@@ -153,6 +157,32 @@ def random_box(n: int = 200, seed_vertices: int = 0, seed_perm: int = 1, mach: f
                     pseudo_tol=1e-30, pseudo_tol_rel=1e-30,
                     viscous=1, sutherland=1, As=float(As), Ts=Ts, Pr=0.72)
     return Workload("random_box_%d" % n, mesh, np.full(N, p), Uc, np.full(N, T), settings)
+
+
+def hb_bump_channel(nx: int = 64, ny: int = 16, nz: int = 4, frequency: float = 50.0, harmonics: int = 1,
+                    amplitude: float = 0.05, selected_period: Optional[float] = None, **kw) -> Workload:
+    """Bump channel under an oscillating back pressure p_out (1 + a sin(w t)).
+
+    Instance J is the flow at instant t_J: its outlet patch carries
+    p_out(t_J); the instants are equispaced over ``selected_period`` or, when
+    None, over the period of smallest condition number (HBZoneList::setInstants).
+    """
+    from . import hb as HB
+    w = bump_channel(nx, ny, nz, **kw)
+    omegas = HB.omega_list([2.0 * np.pi * frequency], [harmonics])
+    n = 2 * harmonics + 1
+    t = HB.select_instants(omegas, n, selected_period)
+    D = HB.hb_operator(omegas, t)
+    p_out = next(p.p for p in w.mesh.patches if p.kind == M.PATCH_PRESSURE_OUTLET)
+
+    def patch_for(q, J):
+        if q.kind == M.PATCH_PRESSURE_OUTLET:
+            q.p = p_out * (1.0 + amplitude * np.sin(omegas[1] * t[J]))
+        return q
+
+    st = HB.stack_instances(w.mesh, n, patch_for)
+    rep = lambda a: np.concatenate([a] * n)
+    return Workload("hb%d_%s" % (n, w.name), st, rep(w.p), rep(w.U), rep(w.T), dict(w.settings), hb=(n, D))
 
 
 def make_config(binding, settings: Dict, **overrides):

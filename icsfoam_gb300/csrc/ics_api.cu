@@ -93,7 +93,7 @@ void free_all(Handle& h) {
                   m.bface, m.slot_base, m.scol, m.sface, m.nlow, m.nslot, m.fl_cells, m.rl_cells, m.fl_lptr,
                   m.rl_lptr, h.W, h.W0, h.W00, h.Wprev, h.prim, h.pB, h.TB, h.UB, h.phiB, h.pseudoCo, h.rPDT,
                   h.ddtCoeff, h.q, h.bq, h.clin, h.grad, h.fflux, h.frec, h.flam, h.bjac, h.src, h.vcell,
-                  h.fvisc, h.vsf2, m.dc, h.blk, h.dg,
+                  h.fvisc, h.vsf2, m.dc, m.Dhb, h.blk, h.dg,
                   h.dginv, h.rD, h.kv, h.kw, h.kx, h.kb, h.kt, h.dW, h.partials, h.counter, h.ks, h.scratch,
                   h.ibuf};
   drop_graphs(h);
@@ -198,6 +198,7 @@ void build_mesh(Handle& h, const ics_mesh_desc* d) {
   DevMesh& m = h.m;
   const int N = d->n_cells, F = d->n_faces, B = d->n_bfaces;
   m.N = N;
+  m.Nc = N;
   m.F = F;
   m.B = B;
   for (int k = 0; k < 3; ++k) m.solD[k] = d->solution_d[k];
@@ -412,16 +413,22 @@ void alloc_state(Handle& h) {
   h.src = dalloc<double>(5ull * N);
   h.dW = dalloc<double>(5ull * N);
   h.partials = dalloc<double>((size_t)REDUCE_BLOCKS * 16);
-  h.counter = dalloc<unsigned int>(4);
+  h.counter = dalloc<unsigned int>(MAX_INST + 4);
   h.ks = dalloc<KrylovScalars>(1);
   ICS_CUDA(cudaMallocHost(&h.ksHost, sizeof(KrylovScalars)));
   h.scratch = dalloc<double>(5ull * N + 8);
   h.ibuf = dalloc<int>((size_t)N + 8);
 }
 
-double residual_norm(const ics_solver_perf& r) {
-  return std::sqrt(r.init_res[0] * r.init_res[0] + r.init_res[4] * r.init_res[4] +
-                   (r.init_res[1] * r.init_res[1] + r.init_res[2] * r.init_res[2] + r.init_res[3] * r.init_res[3]));
+// sqrt(sum over instances of |s0|^2 + |s1|^2 + |v0|^2), scalars rho, rhoE and
+// vector rhoU (setCoAndDeltaT.H:10-16; HB outerLoop.H:34-56)
+double residual_norm(const std::vector<double>& r) {
+  double s = 0;
+  for (size_t J = 0; J < r.size() / 5; ++J) {
+    const double* q = &r[5 * J];
+    s += q[0] * q[0] + q[4] * q[4] + (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  }
+  return std::sqrt(s);
 }
 
 int do_residual(Handle& h, double* host_src) {
@@ -429,7 +436,7 @@ int do_residual(Handle& h, double* host_src) {
   double ratio = 1.0;
   bool apply = false;
   if (h.initResValid) {
-    const bool firstIter = h.corr == 1;
+    const bool firstIter = h.ctl[0].corr == 1;
     if (!firstIter && h.prevResValid) {
       ratio = residual_norm(h.prevRes) / residual_norm(h.initRes);
       ratio = std::max(std::min(ratio, h.cfg.c.pseudo_co_max_increase), h.cfg.c.pseudo_co_min_decrease);
@@ -495,11 +502,10 @@ int do_solve(Handle& h, ics_solver_perf* perf) {
   ensure_workspace(h);
   ICS_CUDA(cudaMemcpyAsync(h.Wprev, h.W, 5ull * h.m.N * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
   ics_solver_perf p;
-  const int st = gmres_solve(h, &p);
+  const int st = gmres_solve(h, &p, h.initRes);
   h.haveIncrement = true;
-  h.initRes = p;
   h.initResValid = true;
-  h.residuals_ = p;
+  for (int J = 0; J < h.m.nInst; ++J) std::memcpy(h.ctl[J].residuals, &h.initRes[5 * J], 5 * sizeof(double));
   if (perf) *perf = p;
   if (st) h.err = st == ICS_ERR_BREAKDOWN ? "zero Krylov norm" : "non-finite Krylov residual";
   return st;
@@ -526,29 +532,46 @@ int do_update(Handle& h, ics_iter_stats* s) {
   return ICS_OK;
 }
 
-double max_init(const ics_solver_perf& r) {
-  double m = -VGREAT;
-  for (int k = 0; k < 5; ++k) m = std::max(m, r.init_res[k]);
-  return m;
-}
-
-bool criteria_satisfied(Handle& h) {
+// pseudotimeControl::criteriaSatisfied (pseudotimeControl.C), the residuals
+// being the initial residuals of the last linear solve
+bool criteria_satisfied(const Handle& h, Handle::Control& q) {
   const ics_config& c = h.cfg.c;
-  const bool finalIter = h.converged_ || (h.corr == c.n_pseudo_corr);
-  if (h.firstIteration_ || h.corr == 1 || finalIter) {
-    h.firstIteration_ = false;
+  const bool finalIter = q.converged || (q.corr == c.n_pseudo_corr);
+  if (q.firstIteration || q.corr == 1 || finalIter) {
+    q.firstIteration = false;
     return false;
   }
-  const bool storeIni = h.corr == 2;
-  if (storeIni) h.initResiduals_ = h.residuals_;
-  const bool absCheck = max_init(h.residuals_) < c.pseudo_tol;
-  bool relCheck = false;
-  if (!storeIni) {
-    ics_solver_perf q = h.residuals_;
-    for (int k = 0; k < 5; ++k) q.init_res[k] /= h.initResiduals_.init_res[k] + ROOTVSMALL;
-    relCheck = max_init(q) < c.pseudo_tol_rel;
+  const bool storeIni = q.corr == 2;
+  if (storeIni) std::memcpy(q.initResiduals, q.residuals, sizeof(q.residuals));
+  double mx = -VGREAT, mrel = -VGREAT;
+  for (int k = 0; k < 5; ++k) {
+    mx = std::max(mx, q.residuals[k]);
+    mrel = std::max(mrel, q.residuals[k] / (q.initResiduals[k] + ROOTVSMALL));
   }
-  return (h.corr >= c.n_pseudo_corr_min) && (absCheck || relCheck);
+  const bool absCheck = mx < c.pseudo_tol;
+  const bool relCheck = !storeIni && mrel < c.pseudo_tol_rel;
+  return (q.corr >= c.n_pseudo_corr_min) && (absCheck || relCheck);
+}
+
+// pseudotimeControl::loop (pseudotimeControl.C:159-241) for one control
+bool pseudo_loop_one(const Handle& h, Handle::Control& q) {
+  const bool steady = h.cfg.c.ddt_scheme == ICS_DDT_STEADY;
+  q.corr++;
+  if (!steady && q.corr == h.cfg.c.n_pseudo_corr + 1) {
+    q.corr = 0;
+    return false;
+  }
+  bool completed = false;
+  if (q.converged || criteria_satisfied(h, q)) {
+    if (q.converged) {
+      q.corr = 0;
+      q.converged = false;
+      completed = true;
+    } else {
+      q.converged = true;
+    }
+  }
+  return !completed;
 }
 
 }  // namespace
@@ -648,6 +671,10 @@ int ics_set_config(ics_handle hh, const ics_config* cfg) {
   if (st) {
     hh->h.err = err;
     return st;
+  }
+  if (hh->h.m.nInst > 1 && (cfg->ddt_scheme != ICS_DDT_STEADY || cfg->solver != ICS_SOLVER_GMRES)) {
+    hh->h.err = "Harmonic Balance needs steadyState ddt and the GMRES solver";
+    return ICS_ERR_ARG;
   }
   return guard(hh, [&](Handle& h) {
     const bool structural = cfg->precision != h.cfg.c.precision || cfg->n_directions != h.cfg.c.n_directions;
@@ -992,24 +1019,48 @@ int ics_timer_stop(ics_handle hh, double* ms) {
 int ics_pseudo_loop(ics_handle hh, int32_t* more) {
   if (!more) return ICS_ERR_ARG;
   return guard(hh, [&](Handle& h) {
-    const bool steady = h.cfg.c.ddt_scheme == ICS_DDT_STEADY;
-    h.corr++;
-    if (!steady && h.corr == h.cfg.c.n_pseudo_corr + 1) {
-      h.corr = 0;
-      *more = 0;
-      return ICS_OK;
+    // every instance's control advances (no short cut); more while any runs
+    bool any = false;
+    for (auto& q : h.ctl) any = pseudo_loop_one(h, q) || any;
+    *more = any ? 1 : 0;
+    return ICS_OK;
+  });
+}
+
+int ics_set_hb(ics_handle hh, int32_t n, const double* D) {
+  if (!hh) return ICS_ERR_ARG;
+  Handle& h0 = hh->h;
+  if (n < 1 || n > MAX_INST || (n > 1 && !D)) {
+    h0.err = "n_instances must be in [1, ICS_MAX_INSTANCES] with an operator";
+    return ICS_ERR_ARG;
+  }
+  if (h0.m.N % n != 0) {
+    h0.err = "cell count is not a multiple of the number of instances";
+    return ICS_ERR_ARG;
+  }
+  if (n > 1 && (h0.cfg.c.ddt_scheme != ICS_DDT_STEADY || h0.cfg.c.solver != ICS_SOLVER_GMRES)) {
+    h0.err = "Harmonic Balance needs steadyState ddt and the GMRES solver";
+    return ICS_ERR_ARG;
+  }
+  for (int q = 0; n > 1 && q < n * n; ++q)
+    if (!std::isfinite(D[q])) {
+      h0.err = "non-finite Harmonic Balance operator";
+      return ICS_ERR_ARG;
     }
-    bool completed = false;
-    if (h.converged_ || criteria_satisfied(h)) {
-      if (h.converged_) {
-        h.corr = 0;
-        h.converged_ = false;
-        completed = true;
-      } else {
-        h.converged_ = true;
-      }
+  return guard(hh, [&](Handle& h) {
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    if (h.m.Dhb) ICS_CUDA(cudaFree(h.m.Dhb));
+    h.m.Dhb = nullptr;
+    if (n > 1) {
+      h.m.Dhb = dalloc<double>((size_t)n * n);
+      ICS_CUDA(cudaMemcpy(h.m.Dhb, D, sizeof(double) * n * n, cudaMemcpyHostToDevice));
     }
-    *more = completed ? 0 : 1;
+    h.m.nInst = n;
+    h.m.Nc = h.m.N / n;
+    h.ctl.assign(n, Handle::Control());
+    h.initResValid = h.prevResValid = false;
+    h.haveMatrix = h.haveIncrement = false;
+    drop_graphs(h);  // the captured cycle's reduction grids depend on n
     return ICS_OK;
   });
 }

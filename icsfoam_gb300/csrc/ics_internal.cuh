@@ -38,6 +38,7 @@ enum { Q_RHO = 0, Q_P = 1, Q_UX = 2, Q_UY = 3, Q_UZ = 4, Q_E = 5, Q_H = 6, Q_C =
 constexpr int SLICE = 32;
 constexpr int REDUCE_BLOCKS = 1216;  // 8 x 152 SMs
 constexpr int MAX_DIRS = 64;
+constexpr int MAX_INST = ICS_MAX_INSTANCES;  // Harmonic Balance instances
 
 // Scalars living in device memory for the Krylov cycle (one per handle).
 struct KrylovScalars {
@@ -45,9 +46,9 @@ struct KrylovScalars {
   double c[MAX_DIRS], s[MAX_DIRS], bh[MAX_DIRS + 1], y[MAX_DIRS];
   double beta;            // norm used to scale the next Krylov vector
   double red[16];         // reduction results
-  double avg[5];
-  double nf[3];           // norm factors (rho, rhoE, rhoU)
-  double res[5];          // L1 residuals (unnormalised sums)
+  double avg[5 * MAX_INST];  // per-instance field averages of W
+  double nfr[8 * MAX_INST];  // per instance: norm-factor sums (rho, rhoE, rhoU), |b| per equation
+  double res[5 * MAX_INST];  // per-instance L1 residuals (unnormalised sums)
   double l2;              // rho L2 partial result
   int status;             // breakdown / non-finite flags
 };
@@ -103,6 +104,10 @@ struct DevMesh {
   int* fl_lptr = nullptr;            // device copies of the level pointers
   int* rl_lptr = nullptr;
   bool fuse_last = false;            // last forward level == first reverse level (same rows)
+  // Harmonic Balance: nInst stacked instances of Nc cells (instance-major),
+  // coupled through the spectral operator Dhb [nInst][nInst]
+  int nInst = 1, Nc = 0;
+  double* Dhb = nullptr;
 };
 
 struct Cfg {
@@ -163,12 +168,17 @@ struct Handle {
   unsigned int* counter = nullptr;
   KrylovScalars* ks = nullptr;  // device
   KrylovScalars* ksHost = nullptr;  // pinned mirror
-  // host-side residual bookkeeping (setCoAndDeltaT.H, pseudotimeControl)
+  // host-side residual bookkeeping (setCoAndDeltaT.H, pseudotimeControl):
+  // linear-solver initial residuals per instance and equation, [5*J + k]
   bool initResValid = false, prevResValid = false;
-  ics_solver_perf initRes{}, prevRes{};
-  int corr = 0;
-  bool converged_ = false, firstIteration_ = true;
-  ics_solver_perf residuals_{}, initResiduals_{};
+  std::vector<double> initRes, prevRes;
+  // one pseudotimeControl per instance (the HB solver loops while any runs)
+  struct Control {
+    int corr = 0;
+    bool converged = false, firstIteration = true;
+    double residuals[5] = {0, 0, 0, 0, 0}, initResiduals[5] = {0, 0, 0, 0, 0};
+  };
+  std::vector<Control> ctl = std::vector<Control>(1);
   double lastRhoL2 = 0;
   // scratch
   double* scratch = nullptr;  // generic [N*5] doubles
@@ -219,7 +229,8 @@ void launch_viscous(Handle& h);
 // linear algebra: precision-dispatched (mixed = FP32 blocks and vectors)
 void spmv(Handle& h, const void* x, void* y);
 int precondition(Handle& h, void* r);
-int gmres_solve(Handle& h, ics_solver_perf* perf);
+// fills *perf (maximum over instances) and initRes (per instance, [5*J + k])
+int gmres_solve(Handle& h, ics_solver_perf* perf, std::vector<double>& initRes);
 void to_vec(Handle& h, const double* src, void* dst);   // FP64 -> Krylov type
 void from_vec(Handle& h, const void* src, double* dst); // Krylov type -> FP64
 

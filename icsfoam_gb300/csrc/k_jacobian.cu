@@ -225,6 +225,13 @@ __global__ void __launch_bounds__(128) k_jac_rows(DevMesh m, double gamma, const
   const T dc = T(ddtCoeff[c] * m.V[c]);
 #pragma unroll
   for (int q = 0; q < 5; ++q) diag[6 * q] += dc;
+  if (m.nInst > 1) {
+    // Harmonic Balance diagonal V D_JJ on every equation (HBZone.C:435-518)
+    const int J = c / m.Nc;
+    const T hd = T(m.V[c] * m.Dhb[J * m.nInst + J]);
+#pragma unroll
+    for (int q = 0; q < 5; ++q) diag[6 * q] += hd;
+  }
   T* dout = dg + (size_t)s * 25 * 32 + lane;
 #pragma unroll
   for (int k = 0; k < 25; ++k) dout[k * 32] = diag[k];

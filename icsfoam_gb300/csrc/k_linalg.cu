@@ -149,6 +149,18 @@ __global__ void __launch_bounds__(128) k_spmv(DevMesh m, const TB* __restrict__ 
       acc[i] += a;
     }
   }
+  if (m.nInst > 1) {
+    // Harmonic Balance coupling blocks V D_JK I with the other instances
+    const int J = c / m.Nc, cl = c - J * m.Nc;
+    const double Vc = m.V[c];
+    for (int K = 0; K < m.nInst; ++K) {
+      if (K == J) continue;
+      const TV d = TV(Vc * m.Dhb[J * m.nInst + K]);
+      const TV* xk = x + 5 * ((size_t)K * m.Nc + cl);
+#pragma unroll
+      for (int k = 0; k < 5; ++k) acc[k] += d * xk[k];
+    }
+  }
 #pragma unroll
   for (int k = 0; k < 5; ++k) y[5 * c + k] = acc[k];
 }
@@ -435,13 +447,24 @@ __global__ void k_xupdate(long n, TV* __restrict__ x, const TV* __restrict__ V, 
   }
 }
 
+// Per-instance reductions: blockIdx.y is the instance, whose Nc cells start at
+// y*Nc; each instance folds its own partials and counter into out + y*NV.
+#define ICS_INSTANCE_RANGE(Nc)                                     \
+  const int inst_ = blockIdx.y;                                    \
+  const int cend_ = (inst_ + 1) * (Nc);                            \
+  partials += (size_t)inst_ * gridDim.x * NV_;                     \
+  counter += inst_;                                                \
+  out += inst_ * NV_;
+
 // r = b - t, per-equation L1 sums of r (rho, rhoUx, rhoUy, rhoUz, rhoE)
 template <typename TV>
-__global__ void __launch_bounds__(RB) k_resid(int N, const double* __restrict__ b, const TV* __restrict__ t,
+__global__ void __launch_bounds__(RB) k_resid(int Nc, const double* __restrict__ b, const TV* __restrict__ t,
                                               TV* __restrict__ r, double* __restrict__ partials,
                                               unsigned int* __restrict__ counter, double* __restrict__ out) {
+  constexpr int NV_ = 5;
+  ICS_INSTANCE_RANGE(Nc)
   double acc[5] = {0, 0, 0, 0, 0};
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+  for (int c = inst_ * Nc + blockIdx.x * blockDim.x + threadIdx.x; c < cend_; c += gridDim.x * blockDim.x) {
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
       const TV v = TV(b[5 * c + k]) - t[5 * c + k];
@@ -454,12 +477,14 @@ __global__ void __launch_bounds__(RB) k_resid(int N, const double* __restrict__ 
 
 // sums of |b_k| (initial residual) and the norm factors
 template <typename TV>
-__global__ void __launch_bounds__(RB) k_normfac(int N, const double* __restrict__ b, const TV* __restrict__ t,
+__global__ void __launch_bounds__(RB) k_normfac(int Nc, const double* __restrict__ b, const TV* __restrict__ t,
                                                 double* __restrict__ partials, unsigned int* __restrict__ counter,
                                                 double* __restrict__ out) {
-  // out: nf_rho, nf_rhoE, nf_rhoU, |b| rho, Ux, Uy, Uz, rhoE
+  // out per instance: nf_rho, nf_rhoE, nf_rhoU, |b| rho, Ux, Uy, Uz, rhoE
+  constexpr int NV_ = 8;
+  ICS_INSTANCE_RANGE(Nc)
   double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+  for (int c = inst_ * Nc + blockIdx.x * blockDim.x + threadIdx.x; c < cend_; c += gridDim.x * blockDim.x) {
     const double t0 = double(t[5 * c]), t4 = double(t[5 * c + 4]);
     const double t1 = double(t[5 * c + 1]), t2 = double(t[5 * c + 2]), t3 = double(t[5 * c + 3]);
     const double b0 = b[5 * c], b1 = b[5 * c + 1], b2 = b[5 * c + 2], b3 = b[5 * c + 3], b4 = b[5 * c + 4];
@@ -475,26 +500,30 @@ __global__ void __launch_bounds__(RB) k_normfac(int N, const double* __restrict_
   reduce_finish<8>(acc, partials, counter, out);
 }
 
-__global__ void __launch_bounds__(RB) k_wsum(int N, const double* __restrict__ W, double* __restrict__ partials,
+__global__ void __launch_bounds__(RB) k_wsum(int Nc, const double* __restrict__ W, double* __restrict__ partials,
                                              unsigned int* __restrict__ counter, double* __restrict__ out) {
+  constexpr int NV_ = 5;
+  ICS_INSTANCE_RANGE(Nc)
   double acc[5] = {0, 0, 0, 0, 0};
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x)
+  for (int c = inst_ * Nc + blockIdx.x * blockDim.x + threadIdx.x; c < cend_; c += gridDim.x * blockDim.x)
 #pragma unroll
     for (int k = 0; k < 5; ++k) acc[k] += W[5 * c + k];
   reduce_finish<5>(acc, partials, counter, out);
 }
 
 template <typename TV>
-__global__ void k_wmavg(int N, const double* __restrict__ W, const KrylovScalars* __restrict__ ks,
+__global__ void k_wmavg(int N, int Nc, const double* __restrict__ W, const KrylovScalars* __restrict__ ks,
                         TV* __restrict__ out) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= N) return;
+  const double* avg = ks->avg + 5 * (c / Nc);
 #pragma unroll
-  for (int k = 0; k < 5; ++k) out[5 * c + k] = TV(W[5 * c + k] - ks->avg[k]);
+  for (int k = 0; k < 5; ++k) out[5 * c + k] = TV(W[5 * c + k] - avg[k]);
 }
 
-__global__ void k_avg(KrylovScalars* ks, int N) {
-  for (int k = 0; k < 5; ++k) ks->avg[k] = ks->red[k] / N;
+// instance averages (gAverage per field) from the instance sums
+__global__ void k_avg(KrylovScalars* ks, int Nc, int nInst) {
+  for (int k = 0; k < 5 * nInst; ++k) ks->avg[k] = ks->avg[k] / Nc;
 }
 
 template <typename TV>
@@ -614,45 +643,84 @@ void from_vec(Handle& h, const void* src, double* dst) {
 }
 
 // ----------------------------------------------------------------- GMRES
-static bool stop_test(const Handle& h, const ics_solver_perf& p) {
+// residualsIO of the coupled system: initial and final L1 residuals per
+// instance and equation, [5*J + k]
+struct ResIO {
+  std::vector<double> init, fin;
+  int nIter = 0;
+};
+
+// coupledMatrix::solver::stop (coupledMatrixSolver.C:198-221) over every entry
+static bool stop_test(const Handle& h, const ResIO& r) {
   const ics_config& c = h.cfg.c;
-  if (p.n_iterations < c.min_iter) return false;
+  if (r.nIter < c.min_iter) return false;
   double mx = -VGREAT, mrel = -VGREAT;
-  for (int k = 0; k < 5; ++k) mx = fmax(mx, p.final_res[k]);
-  mrel = fmax(mrel, p.final_res[0] / (p.init_res[0] + ROOTVSMALL));
-  mrel = fmax(mrel, p.final_res[4] / (p.init_res[4] + ROOTVSMALL));
-  for (int k = 0; k < 3; ++k)
-    if (h.m.solD[k] == 1) mrel = fmax(mrel, p.final_res[1 + k] / (p.init_res[1 + k] + ROOTVSMALL));
-  return p.n_iterations >= c.max_iter || mx < c.tolerance || mrel < c.rel_tol;
+  for (double v : r.fin) mx = fmax(mx, v);
+  for (int J = 0; J < h.m.nInst; ++J) {
+    const double* in = &r.init[5 * J];
+    const double* fi = &r.fin[5 * J];
+    mrel = fmax(mrel, fi[0] / (in[0] + ROOTVSMALL));
+    mrel = fmax(mrel, fi[4] / (in[4] + ROOTVSMALL));
+    for (int k = 0; k < 3; ++k)
+      if (h.m.solD[k] == 1) mrel = fmax(mrel, fi[1 + k] / (in[1 + k] + ROOTVSMALL));
+  }
+  return r.nIter >= c.max_iter || mx < c.tolerance || mrel < c.rel_tol;
+}
+
+// grid of the per-instance reductions: the instances share REDUCE_BLOCKS
+static dim3 inst_grid(const Handle& h) {
+  const int bx = REDUCE_BLOCKS / h.m.nInst;
+  return dim3(bx < 1 ? 1 : bx, h.m.nInst);
+}
+
+// final L1 residuals from the per-instance sums in h.ksHost->res; false when
+// any is not finite
+static bool final_residuals(const Handle& h, const std::vector<double>& nf, ResIO& r) {
+  bool finite = true;
+  for (int J = 0; J < h.m.nInst; ++J) {
+    const double* rs = h.ksHost->res + 5 * J;
+    double* fi = &r.fin[5 * J];
+    fi[0] = rs[0] / nf[3 * J];
+    fi[4] = rs[4] / nf[3 * J + 1];
+    for (int k = 0; k < 3; ++k) fi[1 + k] = h.m.solD[k] == -1 ? 0.0 : rs[1 + k] / nf[3 * J + 2];
+    for (int k = 0; k < 5; ++k) finite = finite && std::isfinite(fi[k]);
+  }
+  return finite;
 }
 
 // Norm factors of coupledMatrixSolver (gmres.C:812-850): sum |A (W - avg W)| +
-// |b| per equation (vector magnitude for rhoU), and the initial L1 residuals.
+// |b| per equation (vector magnitude for rhoU), and the initial L1 residuals,
+// each per instance (gAverage and gSum per field).
 template <typename TB, typename TV>
-static void norm_factors_t(Handle& h, double nf[3], ics_solver_perf& p) {
-  const int N = h.m.N;
+static void norm_factors_t(Handle& h, std::vector<double>& nf, ResIO& r) {
+  const int N = h.m.N, Nc = h.m.Nc, nI = h.m.nInst;
   cudaStream_t st = h.stream;
   KrylovScalars* ks = h.ks;
   TV* w = (TV*)h.kw;
   TV* t = (TV*)h.kt;
-  double* red = ks->red;
+  const dim3 g = inst_grid(h);
   ICS_CUDA(cudaMemsetAsync(&ks->status, 0, sizeof(int), st));
-  ICS_LAUNCH(h, ICS_K_VECTOR, k_wsum<<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.W, h.partials, h.counter, red));
-  ICS_LAUNCH(h, ICS_K_SCALAR, k_avg<<<1, 1, 0, st>>>(ks, N));
-  ICS_LAUNCH(h, ICS_K_VECTOR, k_wmavg<TV><<<grid_for(N, 256), 256, 0, st>>>(N, h.W, ks, w));
+  ICS_LAUNCH(h, ICS_K_VECTOR, k_wsum<<<g, RB, 0, st>>>(Nc, h.W, h.partials, h.counter, ks->avg));
+  ICS_LAUNCH(h, ICS_K_SCALAR, k_avg<<<1, 1, 0, st>>>(ks, Nc, nI));
+  ICS_LAUNCH(h, ICS_K_VECTOR, k_wmavg<TV><<<grid_for(N, 256), 256, 0, st>>>(N, Nc, h.W, ks, w));
   spmv_t<TB, TV>(h, w, t);
-  ICS_LAUNCH(h, ICS_K_VECTOR,
-             k_normfac<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.src, t, h.partials, h.counter, red));
-  ICS_CUDA(cudaMemcpyAsync(h.ksHost->red, red, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  ICS_LAUNCH(h, ICS_K_VECTOR, k_normfac<TV><<<g, RB, 0, st>>>(Nc, h.src, t, h.partials, h.counter, ks->nfr));
+  ICS_CUDA(cudaMemcpyAsync(h.ksHost->nfr, ks->nfr, 8 * nI * sizeof(double), cudaMemcpyDeviceToHost, st));
   ICS_CUDA(cudaStreamSynchronize(st));
-  for (int k = 0; k < 3; ++k) nf[k] = h.ksHost->red[k] + VSMALL;
-  memset(&p, 0, sizeof(p));
-  p.init_res[0] = h.ksHost->red[3] / nf[0];
-  p.init_res[1] = h.ksHost->red[4] / nf[2];
-  p.init_res[2] = h.ksHost->red[5] / nf[2];
-  p.init_res[3] = h.ksHost->red[6] / nf[2];
-  p.init_res[4] = h.ksHost->red[7] / nf[1];
-  for (int k = 0; k < 5; ++k) p.final_res[k] = p.init_res[k];
+  nf.assign(3 * nI, 0.0);
+  r.init.assign(5 * nI, 0.0);
+  r.nIter = 0;
+  for (int J = 0; J < nI; ++J) {
+    const double* q = h.ksHost->nfr + 8 * J;
+    for (int k = 0; k < 3; ++k) nf[3 * J + k] = q[k] + VSMALL;
+    double* in = &r.init[5 * J];
+    in[0] = q[3] / nf[3 * J];
+    in[1] = q[4] / nf[3 * J + 2];
+    in[2] = q[5] / nf[3 * J + 2];
+    in[3] = q[6] / nf[3 * J + 2];
+    in[4] = q[7] / nf[3 * J + 1];
+  }
+  r.fin = r.init;
 }
 
 // x_new = D^-1 (b - (A - D) x_old): one block-Jacobi sweep (JacobiSmoother::smooth)
@@ -691,19 +759,19 @@ __global__ void __launch_bounds__(128) k_jacobi_sweep(DevMesh m, const TB* __res
 
 // smoothSolverCoupled::solveDelta (smoothSolverCoupled.C:369-515)
 template <typename TB, typename TV>
-static int smooth_t(Handle& h, ics_solver_perf* perf) {
+static int smooth_t(Handle& h, ResIO& p) {
   const int N = h.m.N;
   const long n5 = 5L * N;
   cudaStream_t st = h.stream;
   KrylovScalars* ks = h.ks;
-  double nf[3];
-  ics_solver_perf p;
+  std::vector<double> nf;
   norm_factors_t<TB, TV>(h, nf, p);
   TV* x = (TV*)h.kx;
   TV* y = (TV*)h.kb;
   TV* t = (TV*)h.kt;
   TV* r = (TV*)h.kw;
   ICS_CUDA(cudaMemsetAsync(x, 0, n5 * sizeof(TV), st));
+  bool finite = true;
   do {
     for (int s = 0; s < h.cfg.c.n_sweeps; ++s) {
       ICS_LAUNCH(h, ICS_K_JACOBI,
@@ -715,31 +783,22 @@ static int smooth_t(Handle& h, ics_solver_perf* perf) {
     }
     spmv_t<TB, TV>(h, x, t);
     ICS_LAUNCH(h, ICS_K_VECTOR,
-               k_resid<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.src, t, r, h.partials, h.counter, ks->res));
+               k_resid<TV><<<inst_grid(h), RB, 0, st>>>(h.m.Nc, h.src, t, r, h.partials, h.counter, ks->res));
     ICS_CUDA(cudaGetLastError());
-    ICS_CUDA(cudaMemcpyAsync(h.ksHost->res, ks->res, 5 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    ICS_CUDA(cudaMemcpyAsync(h.ksHost->res, ks->res, 5 * h.m.nInst * sizeof(double), cudaMemcpyDeviceToHost, st));
     ICS_CUDA(cudaStreamSynchronize(st));
-    const double* rs = h.ksHost->res;
-    p.final_res[0] = rs[0] / nf[0];
-    p.final_res[4] = rs[4] / nf[1];
-    for (int k = 0; k < 3; ++k) p.final_res[1 + k] = h.m.solD[k] == -1 ? 0.0 : rs[1 + k] / nf[2];
-    p.n_iterations += h.cfg.c.n_sweeps;
-    bool finite = true;
-    for (int k = 0; k < 5; ++k) finite = finite && std::isfinite(p.final_res[k]);
+    finite = final_residuals(h, nf, p);
+    p.nIter += h.cfg.c.n_sweeps;
     if (!finite) break;
   } while (!stop_test(h, p));
-  bool finite = true;
-  for (int k = 0; k < 5; ++k) finite = finite && std::isfinite(p.final_res[k]);
-  p.converged = finite;
   ICS_LAUNCH(h, ICS_K_VECTOR,
              k_to_dW<TV><<<grid_for(N, 256), 256, 0, st>>>(N, x, h.dW, h.m.solD[0], h.m.solD[1], h.m.solD[2]));
   ICS_CUDA(cudaGetLastError());
-  *perf = p;
   return finite ? ICS_OK : ICS_ERR_NONFINITE;
 }
 
 template <typename TB, typename TV>
-static int gmres_t(Handle& h, ics_solver_perf* perf) {
+static int gmres_t(Handle& h, ResIO& p) {
   const int N = h.m.N, m = h.cfg.c.n_directions;
   const long n5 = 5L * N;
   const long vs = (long)kstride(h);
@@ -750,8 +809,7 @@ static int gmres_t(Handle& h, ics_solver_perf* perf) {
   TV* x = (TV*)h.kx;
   TV* t = (TV*)h.kt;
   double* red = ks->red;
-  double nf[3];
-  ics_solver_perf p;
+  std::vector<double> nf;
   norm_factors_t<TB, TV>(h, nf, p);
   // r = b, x = 0
   ICS_CUDA(cudaMemsetAsync(x, 0, n5 * sizeof(TV), st));
@@ -784,7 +842,7 @@ static int gmres_t(Handle& h, ics_solver_perf* perf) {
     ICS_LAUNCH(h, ICS_K_VECTOR, k_xupdate<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, x, V, ks, m, vs));
     spmv_t<TB, TV>(h, x, t);
     ICS_LAUNCH(h, ICS_K_VECTOR,
-               k_resid<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.src, t, w, h.partials, h.counter, ks->res));
+               k_resid<TV><<<inst_grid(h), RB, 0, st>>>(h.m.Nc, h.src, t, w, h.partials, h.counter, ks->res));
   };
   const int key = h.cfg.c.preconditioner * 100000 + prec(h) * 1000 + m;
   const bool useGraph = !h.prof;  // per-launch event timing needs direct launches
@@ -809,40 +867,47 @@ static int gmres_t(Handle& h, ics_solver_perf* perf) {
       cycle();
     }
     ICS_CUDA(cudaGetLastError());
-    ICS_CUDA(cudaMemcpyAsync(h.ksHost->res, ks->res, 5 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    ICS_CUDA(cudaMemcpyAsync(h.ksHost->res, ks->res, 5 * h.m.nInst * sizeof(double), cudaMemcpyDeviceToHost, st));
     ICS_CUDA(cudaMemcpyAsync(&h.ksHost->status, &ks->status, sizeof(int), cudaMemcpyDeviceToHost, st));
     ICS_CUDA(cudaStreamSynchronize(st));
     if (h.ksHost->status) {
       status = (h.ksHost->status & 4) ? ICS_ERR_NONFINITE : ICS_ERR_BREAKDOWN;
-      p.n_iterations++;
+      p.nIter++;
       break;
     }
-    const double* rs = h.ksHost->res;
-    p.final_res[0] = rs[0] / nf[0];
-    p.final_res[4] = rs[4] / nf[1];
-    for (int k = 0; k < 3; ++k) p.final_res[1 + k] = h.m.solD[k] == -1 ? 0.0 : rs[1 + k] / nf[2];
-    p.n_iterations++;
-    bool finite = true;
-    for (int k = 0; k < 5; ++k) finite = finite && std::isfinite(p.final_res[k]);
+    const bool finite = final_residuals(h, nf, p);
+    p.nIter++;
     if (!finite) {
       status = ICS_ERR_NONFINITE;
       break;
     }
   } while (!stop_test(h, p));
-  p.converged = status == ICS_OK;
   ICS_LAUNCH(h, ICS_K_VECTOR, k_to_dW<TV><<<grid_for(N, 256), 256, 0, st>>>(N, x, h.dW, h.m.solD[0], h.m.solD[1], h.m.solD[2]));
   ICS_CUDA(cudaGetLastError());
-  *perf = p;
   return status;
 }
 
-int gmres_solve(Handle& h, ics_solver_perf* perf) {
-  if (h.cfg.c.solver == ICS_SOLVER_SMOOTH) {
-    if (prec(h) == ICS_PREC_MIXED) return smooth_t<float, float>(h, perf);
-    return smooth_t<double, double>(h, perf);
+int gmres_solve(Handle& h, ics_solver_perf* perf, std::vector<double>& initRes) {
+  ResIO r;
+  int st;
+  if (h.cfg.c.solver == ICS_SOLVER_SMOOTH)
+    st = prec(h) == ICS_PREC_MIXED ? smooth_t<float, float>(h, r) : smooth_t<double, double>(h, r);
+  else
+    st = prec(h) == ICS_PREC_MIXED ? gmres_t<float, float>(h, r) : gmres_t<double, double>(h, r);
+  // the C ABI's summary: maximum over instances per equation
+  memset(perf, 0, sizeof(*perf));
+  for (int k = 0; k < 5; ++k) {
+    perf->init_res[k] = -VGREAT;
+    perf->final_res[k] = -VGREAT;
+    for (int J = 0; J < h.m.nInst; ++J) {
+      perf->init_res[k] = fmax(perf->init_res[k], r.init[5 * J + k]);
+      perf->final_res[k] = fmax(perf->final_res[k], r.fin[5 * J + k]);
+    }
   }
-  if (prec(h) == ICS_PREC_MIXED) return gmres_t<float, float>(h, perf);
-  return gmres_t<double, double>(h, perf);
+  perf->n_iterations = r.nIter;
+  perf->converged = st == ICS_OK;
+  initRes = r.init;
+  return st;
 }
 
 // rho L2 residual: sqrt(sum (div(phi) V)^2) from the per-cell squares

@@ -438,8 +438,23 @@ __global__ void __launch_bounds__(128) k_cellres(DevMesh m, CellResParams D, con
       r[k] -= (dg * w - s) / Vc;
     }
   }
+  if (m.nInst > 1) {
+    // Harmonic Balance source -V sum_K D_JK W_K of this cell's instance J
+    // (HBZoneTemplates.C:39-92), added to R*V (HB residualsUpdate.H:72-74)
+    const int J = c / m.Nc, cl = c - J * m.Nc;
+    double hb[5] = {0, 0, 0, 0, 0};
+    for (int K = 0; K < m.nInst; ++K) {
+      const double d = m.Dhb[J * m.nInst + K];
+      const double* wk = W + 5 * ((size_t)K * m.Nc + cl);
 #pragma unroll
-  for (int k = 0; k < 5; ++k) src[5 * c + k] = r[k] * Vc;
+      for (int k = 0; k < 5; ++k) hb[k] -= Vc * d * wk[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) src[5 * c + k] = r[k] * Vc + hb[k];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 5; ++k) src[5 * c + k] = r[k] * Vc;
+  }
   double co = pseudoCo[c];
   if (D.applySer) {
     co *= D.serRatio;

@@ -28,8 +28,7 @@ __device__ __forceinline__ double mu_of(const ViscParams& P, double T) {
 }
 __device__ __forceinline__ double alpha_of(const ViscParams& P, double mu) { return P.Cp / P.Cv * (mu / P.Pr); }
 
-// vc layout [VC][N]: 0-8 grad U (3i+j), 9-11 grad e, 12-20 tau (3i+j), 21 mu, 22 alpha, 23 e
-constexpr int VC = 24;
+// vc layout [24][N]: 0-8 grad U (3i+j), 9-11 grad e, 12-20 tau (3i+j), 21 mu, 22 alpha, 23 e
 
 __global__ void __launch_bounds__(128) k_visc_cell(DevMesh m, ViscParams P, const double* __restrict__ W,
                                                    const double* __restrict__ prim, const double* __restrict__ TB,

@@ -219,6 +219,19 @@ int ics_update_fields(ics_handle h, ics_iter_stats* stats);
 int ics_pseudo_iteration(ics_handle h, ics_iter_stats* stats);
 /* Start a physical time step: shift old time levels, beginTimeStep.H:1-45.  */
 int ics_begin_time_step(ics_handle h);
+/* Harmonic Balance (dbnsFullyImplicitHBFoam outerLoop.H:1-230, HBZone.C:359-519):
+ * the mesh given to ics_create holds n_instances stacked copies (instance J
+ * owns cells [J*n, (J+1)*n), n = n_cells/n_instances).  D is the row-major
+ * n_instances x n_instances spectral operator (HBZone::updateHBOperators).
+ * Adds -V sum_K D_JK W_K to each instance's residual source, V D_JJ to the
+ * diagonal and V D_JK I couplings to the Jacobian action; norm factors and
+ * L1 residuals become per instance (solver_perf reports the maximum over
+ * instances) and every instance keeps its own pseudotimeControl state
+ * (ics_pseudo_loop answers 1 while any instance is not finished).  Needs
+ * steadyState ddt and the GMRES solver; n_instances = 1 switches HB off.
+ * Rotating-frame (cylindrical) momentum sources are not provided.          */
+#define ICS_MAX_INSTANCES 16
+int ics_set_hb(ics_handle h, int32_t n_instances, const double* D);
 /* pseudotimeControl::loop() (pseudotimeControl.C:159-241): returns 1 in
  * *more while the pseudo loop should run another iteration.                 */
 int ics_pseudo_loop(ics_handle h, int32_t* more);
@@ -250,7 +263,8 @@ int ics_timer_stop(ics_handle h, double* ms);
  * every device buffer).  x, r ([n_cells][5]) and l1 ([5]) are caller-owned
  * DEVICE pointers; nothing is allocated or freed.  The only scratch is a
  * fixed file-scope device array sized for at most 2,097,152 cells: larger
- * handles return ICS_ERR_ARG.  The first call on a device looks up that
+ * handles return ICS_ERR_ARG, and so do Harmonic Balance handles (A here
+ * has no instance coupling).  The first call on a device looks up that
  * array's address (cudaGetSymbolAddress), so make it before any stream
  * capture.  All calls share the array: calls that overlap on the GPU race.
  * Runs on the handle's stream and synchronises it before returning.        */

@@ -126,13 +126,21 @@ struct Case {
   // previous-iteration state and increment
   std::vector<double> Wprev, dW;  // N*5
   bool haveIncrement = false;
-  // residual bookkeeping (setCoAndDeltaT.H, pseudotimeControl)
+  // Harmonic Balance: nInst stacked instances of Nc cells, operator Dhb
+  int nInst = 1, Nc = 0;
+  std::vector<double> Dhb;
+  // residual bookkeeping (setCoAndDeltaT.H, pseudotimeControl), one entry per
+  // equation and instance: [5*J + k], k = rho, rhoUx, rhoUy, rhoUz, rhoE
   bool initResValid = false, prevResValid = false;
-  ics_solver_perf initRes{}, prevRes{};
-  // pseudotimeControl state
-  int corr = 0;
-  bool converged_ = false, firstIteration_ = true;
-  ics_solver_perf residuals_{}, initResiduals_{};
+  std::vector<double> initRes, prevRes;
+  // pseudotimeControl state, one per instance (the HB solver keeps one
+  // control per sub-time mesh and loops while any of them is not finished)
+  struct Control {
+    int corr = 0;
+    bool converged = false, firstIteration = true;
+    double residuals[5] = {0, 0, 0, 0, 0}, initResiduals[5] = {0, 0, 0, 0, 0};
+  };
+  std::vector<Control> ctl = std::vector<Control>(1);
   std::string err;
 };
 
@@ -890,6 +898,18 @@ void residualSource(Case& c) {
     c.src[5 * i + 2] = rU.y * Vc;
     c.src[5 * i + 3] = rU.z * Vc;
     c.src[5 * i + 4] = rE * Vc;
+    if (c.nInst > 1) {
+      // Harmonic Balance source -V sum_K D_JK W_K (HBZoneTemplates.C:39-92),
+      // added to R*V (HB residualsUpdate.H:72-74)
+      const int J = i / c.Nc, cl = i % c.Nc;
+      double hb[5] = {0, 0, 0, 0, 0};
+      for (int K = 0; K < c.nInst; ++K) {
+        const int j = K * c.Nc + cl;
+        const double wv[5] = {c.rho[j], c.rhoU[j].x, c.rhoU[j].y, c.rhoU[j].z, c.rhoE[j]};
+        for (int k = 0; k < 5; ++k) hb[k] -= Vc * c.Dhb[J * c.nInst + K] * wv[k];
+      }
+      for (int k = 0; k < 5; ++k) c.src[5 * i + k] = c.src[5 * i + k] + hb[k];
+    }
   }
   c.lastRhoL2 = std::sqrt(l2);
 }
@@ -913,16 +933,21 @@ void waveSpeed(const Case& c, std::vector<double>& lam) {
   }
 }
 
-double residualNorm(const ics_solver_perf& r) {
-  // sqrt(|s0|^2 + |s1|^2 + |v0|^2) with scalars rho, rhoE and vector rhoU
-  return std::sqrt(sqr(r.init_res[0]) + sqr(r.init_res[4]) +
-                   (sqr(r.init_res[1]) + sqr(r.init_res[2]) + sqr(r.init_res[3])));
+// sqrt(sum over instances of |s0|^2 + |s1|^2 + |v0|^2), scalars rho, rhoE and
+// vector rhoU (setCoAndDeltaT.H:10-16; HB outerLoop.H:34-56)
+double residualNorm(const std::vector<double>& r) {
+  double s = 0;
+  for (size_t J = 0; J < r.size() / 5; ++J) {
+    const double* q = &r[5 * J];
+    s += sqr(q[0]) + sqr(q[4]) + (sqr(q[1]) + sqr(q[2]) + sqr(q[3]));
+  }
+  return std::sqrt(s);
 }
 
 // setCoAndDeltaT.H
 void setCoAndDeltaT(Case& c) {
   if (c.initResValid) {
-    const bool firstIter = c.corr == 1;
+    const bool firstIter = c.ctl[0].corr == 1;
     if (!firstIter && c.prevResValid) {
       const double normInit = residualNorm(c.initRes);
       const double normPrev = residualNorm(c.prevRes);
@@ -1147,6 +1172,14 @@ void assembleJacobian(Case& c) {
       }
     }
   }
+  // Harmonic Balance diagonal V D_JJ on every equation (HBZone.C:435-518)
+  if (c.nInst > 1) {
+    for (int i = 0; i < c.N; ++i) {
+      const int J = i / c.Nc;
+      const double d = c.V[i] * c.Dhb[J * c.nInst + J];
+      for (int q = 0; q < 5; ++q) c.diag[i].a[diagIdx[q]] += d;
+    }
+  }
   (void)NF;
   c.haveMatrix = true;
 }
@@ -1172,6 +1205,19 @@ void matrixMul(const Case& c, const double* x, double* y) {
     const int l = c.own[fi], u = c.nei[fi];
     bmv(c.lower[fi], x + 5 * l, y + 5 * u, 1.0);
     bmv(c.upper[fi], x + 5 * u, y + 5 * l, 1.0);
+  }
+  // Harmonic Balance coupling blocks (J, K != J): V D_JK times the identity
+  // on every equation (dbnsFullyImplicitHBFoam outerLoop.H, HB.addBlock)
+  if (c.nInst > 1) {
+    for (int i = 0; i < c.N; ++i) {
+      const int J = i / c.Nc, cl = i % c.Nc;
+      for (int K = 0; K < c.nInst; ++K) {
+        if (K == J) continue;
+        const double d = c.V[i] * c.Dhb[J * c.nInst + K];
+        const double* xk = x + 5 * (K * c.Nc + cl);
+        for (int k = 0; k < 5; ++k) y[5 * i + k] += d * xk[k];
+      }
+    }
   }
 }
 
@@ -1264,59 +1310,110 @@ int precondition(const Case& c, const std::vector<double>& rD, double* r) {
 }
 
 // residualsIO helpers: per-equation L1 with scalar (rho, rhoE) and vector (rhoU) norm factors
-void l1Residual(const Case& c, const double* r, const double nf[3], double out[5]) {
-  double s0 = 0, s1 = 0, vx = 0, vy = 0, vz = 0;
-  for (int i = 0; i < c.N; ++i) {
-    s0 += std::fabs(r[5 * i + 0]);
-    vx += std::fabs(r[5 * i + 1]);
-    vy += std::fabs(r[5 * i + 2]);
-    vz += std::fabs(r[5 * i + 3]);
-    s1 += std::fabs(r[5 * i + 4]);
+// residualsIO of the coupled system: one entry per equation and instance,
+// [5*J + k] (the reference's 2 nO scalars and nO vectors)
+struct ResIO {
+  std::vector<double> init, fin;
+  int nIter = 0;
+};
+
+// L1 residuals per instance: scalars rho, rhoE normalised by their own
+// factor, the three rhoU components by the vector factor (residualsIO.H)
+void l1ResidualIO(const Case& c, const double* r, const std::vector<double>& nf, std::vector<double>& out) {
+  out.assign(5 * c.nInst, 0.0);
+  for (int J = 0; J < c.nInst; ++J) {
+    double s0 = 0, s1 = 0, vx = 0, vy = 0, vz = 0;
+    for (int i = J * c.Nc; i < (J + 1) * c.Nc; ++i) {
+      s0 += std::fabs(r[5 * i + 0]);
+      vx += std::fabs(r[5 * i + 1]);
+      vy += std::fabs(r[5 * i + 2]);
+      vz += std::fabs(r[5 * i + 3]);
+      s1 += std::fabs(r[5 * i + 4]);
+    }
+    double* o = &out[5 * J];
+    o[0] = s0 / nf[3 * J];
+    o[4] = s1 / nf[3 * J + 1];
+    o[1] = vx / nf[3 * J + 2];
+    o[2] = vy / nf[3 * J + 2];
+    o[3] = vz / nf[3 * J + 2];
   }
-  out[0] = s0 / nf[0];
-  out[4] = s1 / nf[1];
-  out[1] = vx / nf[2];
-  out[2] = vy / nf[2];
-  out[3] = vz / nf[2];
 }
 
-bool stopTest(const Case& c, const ics_solver_perf& perf) {
-  if (perf.n_iterations < c.cfg.min_iter) return false;
+// norm factors sum |A (W - avg W)| + |b| per instance (gmres.C:812-850;
+// gAverage per field, i.e. per instance) and the initial residuals
+void normFactorsIO(const Case& c, const std::vector<double>& W, std::vector<double>& nf, ResIO& res) {
+  const int n5 = 5 * c.N;
+  const double* b = c.src.data();
+  std::vector<double> wmr(n5), tmp(n5);
+  for (int J = 0; J < c.nInst; ++J) {
+    double avg[5] = {0, 0, 0, 0, 0};
+    for (int i = J * c.Nc; i < (J + 1) * c.Nc; ++i)
+      for (int k = 0; k < 5; ++k) avg[k] += W[5 * i + k];
+    for (int k = 0; k < 5; ++k) avg[k] /= c.Nc;
+    for (int i = J * c.Nc; i < (J + 1) * c.Nc; ++i)
+      for (int k = 0; k < 5; ++k) wmr[5 * i + k] = W[5 * i + k] - avg[k];
+  }
+  matrixMul(c, wmr.data(), tmp.data());
+  nf.assign(3 * c.nInst, 0.0);
+  for (int J = 0; J < c.nInst; ++J) {
+    double* f = &nf[3 * J];
+    for (int i = J * c.Nc; i < (J + 1) * c.Nc; ++i) {
+      f[0] += std::fabs(tmp[5 * i]) + std::fabs(b[5 * i]);
+      f[1] += std::fabs(tmp[5 * i + 4]) + std::fabs(b[5 * i + 4]);
+      const V3 t(tmp[5 * i + 1], tmp[5 * i + 2], tmp[5 * i + 3]);
+      const V3 s(b[5 * i + 1], b[5 * i + 2], b[5 * i + 3]);
+      f[2] += mag(t) + mag(s);
+    }
+    for (int k = 0; k < 3; ++k) f[k] += VSMALL;
+  }
+  l1ResidualIO(c, b, nf, res.init);
+  res.fin = res.init;
+  res.nIter = 0;
+}
+
+void zeroEmpty(const Case& c, std::vector<double>& r) {
+  for (int J = 0; J < c.nInst; ++J)
+    for (int k = 0; k < 3; ++k)
+      if (c.solD[k] == -1) r[5 * J + 1 + k] = 0.0;
+}
+
+// coupledMatrix::solver::stop (coupledMatrixSolver.C:198-221) over all entries
+bool stopTest(const Case& c, const ResIO& r) {
+  if (r.nIter < c.cfg.min_iter) return false;
   double mx = -VGREAT, mrel = -VGREAT;
-  for (int k = 0; k < 5; ++k) mx = std::max(mx, perf.final_res[k]);
-  mrel = std::max(mrel, perf.final_res[0] / (perf.init_res[0] + ROOTVSMALL));
-  mrel = std::max(mrel, perf.final_res[4] / (perf.init_res[4] + ROOTVSMALL));
-  for (int k = 0; k < 3; ++k)
-    if (c.solD[k] == 1) mrel = std::max(mrel, perf.final_res[1 + k] / (perf.init_res[1 + k] + ROOTVSMALL));
-  return perf.n_iterations >= c.cfg.max_iter || mx < c.cfg.tolerance || mrel < c.cfg.rel_tol;
+  for (double v : r.fin) mx = std::max(mx, v);
+  for (int J = 0; J < c.nInst; ++J) {
+    const double* in = &r.init[5 * J];
+    const double* fi = &r.fin[5 * J];
+    mrel = std::max(mrel, fi[0] / (in[0] + ROOTVSMALL));
+    mrel = std::max(mrel, fi[4] / (in[4] + ROOTVSMALL));
+    for (int k = 0; k < 3; ++k)
+      if (c.solD[k] == 1) mrel = std::max(mrel, fi[1 + k] / (in[1 + k] + ROOTVSMALL));
+  }
+  return r.nIter >= c.cfg.max_iter || mx < c.cfg.tolerance || mrel < c.cfg.rel_tol;
+}
+
+// the C ABI's 5-entry summary: maximum over instances per equation
+void toPerf(const ResIO& r, ics_solver_perf& p) {
+  std::memset(&p, 0, sizeof(p));
+  for (int k = 0; k < 5; ++k) {
+    p.init_res[k] = -VGREAT;
+    p.final_res[k] = -VGREAT;
+    for (size_t J = 0; J < r.init.size() / 5; ++J) {
+      p.init_res[k] = std::max(p.init_res[k], r.init[5 * J + k]);
+      p.final_res[k] = std::max(p.final_res[k], r.fin[5 * J + k]);
+    }
+  }
+  p.n_iterations = r.nIter;
 }
 
 // gmres::solveDelta (gmres.C:772-1107)
-int gmresSolveDelta(Case& c, const std::vector<double>& W, ics_solver_perf& perf, std::vector<double>& dx) {
+int gmresSolveDelta(Case& c, const std::vector<double>& W, ResIO& perf, std::vector<double>& dx) {
   const int N = c.N, m = c.cfg.n_directions;
   const int n5 = 5 * N;
   const double* b = c.src.data();
-  std::memset(&perf, 0, sizeof(perf));
-  // norm factors from A (W - avg)
-  double avg[5] = {0, 0, 0, 0, 0};
-  for (int i = 0; i < N; ++i)
-    for (int k = 0; k < 5; ++k) avg[k] += W[5 * i + k];
-  for (int k = 0; k < 5; ++k) avg[k] /= N;
-  std::vector<double> wmr(n5), tmp(n5);
-  for (int i = 0; i < N; ++i)
-    for (int k = 0; k < 5; ++k) wmr[5 * i + k] = W[5 * i + k] - avg[k];
-  matrixMul(c, wmr.data(), tmp.data());
-  double nf[3] = {0, 0, 0};
-  for (int i = 0; i < N; ++i) {
-    nf[0] += std::fabs(tmp[5 * i]) + std::fabs(b[5 * i]);
-    nf[1] += std::fabs(tmp[5 * i + 4]) + std::fabs(b[5 * i + 4]);
-    const V3 t(tmp[5 * i + 1], tmp[5 * i + 2], tmp[5 * i + 3]);
-    const V3 s(b[5 * i + 1], b[5 * i + 2], b[5 * i + 3]);
-    nf[2] += mag(t) + mag(s);
-  }
-  for (int k = 0; k < 3; ++k) nf[k] += VSMALL;
-  l1Residual(c, b, nf, perf.init_res);
-  std::memcpy(perf.final_res, perf.init_res, sizeof(perf.init_res));
+  std::vector<double> nf;
+  normFactorsIO(c, W, nf, perf);
 
   std::vector<double> rD;
   if (c.cfg.preconditioner == ICS_PC_LUSGS && !lusgsDiag(c, rD)) {
@@ -1352,7 +1449,7 @@ int gmresSolveDelta(Case& c, const std::vector<double>& W, ics_solver_perf& perf
     if (!(beta > 0) || !std::isfinite(beta)) {
       // the reference divides by beta and produces NaN; stop with a status
       status = std::isfinite(beta) ? ICS_ERR_BREAKDOWN : ICS_ERR_NONFINITE;
-      perf.n_iterations++;
+      perf.nIter++;
       break;
     }
     std::fill(bh.begin(), bh.end(), 0.0);
@@ -1398,12 +1495,10 @@ int gmresSolveDelta(Case& c, const std::vector<double>& W, ics_solver_perf& perf
       for (int q = 0; q < n5; ++q) dx[q] += yh[i] * Vk[i][q];
     matrixMul(c, dx.data(), r.data());
     for (int q = 0; q < n5; ++q) r[q] = b[q] - r[q];
-    l1Residual(c, r.data(), nf, perf.final_res);
-    for (int k = 0; k < 3; ++k)
-      if (c.solD[k] == -1) perf.final_res[1 + k] = 0.0;
-    perf.n_iterations++;
+    l1ResidualIO(c, r.data(), nf, perf.fin);
+    zeroEmpty(c, perf.fin);
+    perf.nIter++;
   } while (!stopTest(c, perf));
-  perf.converged = status == ICS_OK;
   // zero increments in empty directions (coupledMatrix.C:370-381)
   for (int k = 0; k < 3; ++k)
     if (c.solD[k] == -1)
@@ -1414,29 +1509,12 @@ int gmresSolveDelta(Case& c, const std::vector<double>& W, ics_solver_perf& perf
 // smoothSolverCoupled::solveDelta (smoothSolverCoupled.C:369-515) with the
 // Jacobi smoother (JacobiSmoother.C:42-205): same norm factors as GMRES, then
 // nSweeps sweeps x <- D^-1 (b - (A - D) x) between stop tests.
-int smoothSolveDelta(Case& c, const std::vector<double>& W, ics_solver_perf& perf, std::vector<double>& dx) {
+int smoothSolveDelta(Case& c, const std::vector<double>& W, ResIO& perf, std::vector<double>& dx) {
   const int N = c.N, n5 = 5 * N;
   const double* b = c.src.data();
-  std::memset(&perf, 0, sizeof(perf));
-  double avg[5] = {0, 0, 0, 0, 0};
-  for (int i = 0; i < N; ++i)
-    for (int k = 0; k < 5; ++k) avg[k] += W[5 * i + k];
-  for (int k = 0; k < 5; ++k) avg[k] /= N;
-  std::vector<double> wmr(n5), tmp(n5);
-  for (int i = 0; i < N; ++i)
-    for (int k = 0; k < 5; ++k) wmr[5 * i + k] = W[5 * i + k] - avg[k];
-  matrixMul(c, wmr.data(), tmp.data());
-  double nf[3] = {0, 0, 0};
-  for (int i = 0; i < N; ++i) {
-    nf[0] += std::fabs(tmp[5 * i]) + std::fabs(b[5 * i]);
-    nf[1] += std::fabs(tmp[5 * i + 4]) + std::fabs(b[5 * i + 4]);
-    const V3 t(tmp[5 * i + 1], tmp[5 * i + 2], tmp[5 * i + 3]);
-    const V3 s(b[5 * i + 1], b[5 * i + 2], b[5 * i + 3]);
-    nf[2] += mag(t) + mag(s);
-  }
-  for (int k = 0; k < 3; ++k) nf[k] += VSMALL;
-  l1Residual(c, b, nf, perf.init_res);
-  std::memcpy(perf.final_res, perf.init_res, sizeof(perf.init_res));
+  std::vector<double> nf;
+  normFactorsIO(c, W, nf, perf);
+  std::vector<double> tmp(n5);
   std::vector<B5> inv(N);
   for (int i = 0; i < N; ++i)
     if (!inv5(c.diag[i], inv[i])) {
@@ -1464,12 +1542,10 @@ int smoothSolveDelta(Case& c, const std::vector<double>& W, ics_solver_perf& per
     }
     matrixMul(c, dx.data(), r.data());
     for (int q = 0; q < n5; ++q) r[q] = b[q] - r[q];
-    l1Residual(c, r.data(), nf, perf.final_res);
-    for (int k = 0; k < 3; ++k)
-      if (c.solD[k] == -1) perf.final_res[1 + k] = 0.0;
-    perf.n_iterations += c.cfg.n_sweeps;
+    l1ResidualIO(c, r.data(), nf, perf.fin);
+    zeroEmpty(c, perf.fin);
+    perf.nIter += c.cfg.n_sweeps;
   } while (!stopTest(c, perf));
-  perf.converged = 1;
   for (int k = 0; k < 3; ++k)
     if (c.solD[k] == -1)
       for (int i = 0; i < N; ++i) dx[5 * i + 1 + k] = 0.0;
@@ -1630,49 +1706,51 @@ void storeW(const Case& c, std::vector<double>& W) {
   }
 }
 
-// pseudotimeControl::criteriaSatisfied / loop
-double maxInit(const ics_solver_perf& r) {
-  double m = -VGREAT;
-  for (int k = 0; k < 5; ++k) m = std::max(m, r.init_res[k]);
-  return m;
-}
-bool criteriaSatisfied(Case& c) {
-  const bool finalIter = c.converged_ || (c.corr == c.cfg.n_pseudo_corr);
-  if (c.firstIteration_ || c.corr == 1 || finalIter) {
-    c.firstIteration_ = false;
+// pseudotimeControl::criteriaSatisfied / loop (pseudotimeControl.C), the
+// residuals being the initial residuals of the last linear solve
+bool criteriaSatisfied(const Case& c, Case::Control& q) {
+  const bool finalIter = q.converged || (q.corr == c.cfg.n_pseudo_corr);
+  if (q.firstIteration || q.corr == 1 || finalIter) {
+    q.firstIteration = false;
     return false;
   }
-  const bool storeIni = c.corr == 2;
-  if (storeIni) c.initResiduals_ = c.residuals_;
-  const bool absCheck = maxInit(c.residuals_) < c.cfg.pseudo_tol;
-  bool relCheck = false;
-  if (!storeIni) {
-    ics_solver_perf q = c.residuals_;
-    for (int k = 0; k < 5; ++k) q.init_res[k] /= c.initResiduals_.init_res[k] + ROOTVSMALL;
-    relCheck = maxInit(q) < c.cfg.pseudo_tol_rel;
+  const bool storeIni = q.corr == 2;
+  if (storeIni) std::memcpy(q.initResiduals, q.residuals, sizeof(q.residuals));
+  double mx = -VGREAT, mrel = -VGREAT;
+  for (int k = 0; k < 5; ++k) {
+    mx = std::max(mx, q.residuals[k]);
+    mrel = std::max(mrel, q.residuals[k] / (q.initResiduals[k] + ROOTVSMALL));
   }
-  return (c.corr >= c.cfg.n_pseudo_corr_min) && (absCheck || relCheck);
+  const bool absCheck = mx < c.cfg.pseudo_tol;
+  const bool relCheck = !storeIni && mrel < c.cfg.pseudo_tol_rel;
+  return (q.corr >= c.cfg.n_pseudo_corr_min) && (absCheck || relCheck);
 }
-bool pseudoLoop(Case& c) {
+bool pseudoLoopOne(const Case& c, Case::Control& q) {
   const bool steady = c.cfg.ddt_scheme == ICS_DDT_STEADY;
-  c.corr++;
-  if (!steady && c.corr == c.cfg.n_pseudo_corr + 1) {
-    c.corr = 0;
+  q.corr++;
+  if (!steady && q.corr == c.cfg.n_pseudo_corr + 1) {
+    q.corr = 0;
     return false;
   }
   bool completed = false;
-  if (c.converged_ || criteriaSatisfied(c)) {
-    if (c.converged_) {
-      c.corr = 0;
-      c.converged_ = false;
+  if (q.converged || criteriaSatisfied(c, q)) {
+    if (q.converged) {
+      q.corr = 0;
+      q.converged = false;
       completed = true;
     } else {
-      c.converged_ = true;
+      q.converged = true;
     }
   } else {
     completed = false;
   }
   return !completed;
+}
+// every instance's control is advanced (no short cut); more while any is
+bool pseudoLoop(Case& c) {
+  bool more = false;
+  for (auto& q : c.ctl) more = pseudoLoopOne(c, q) || more;
+  return more;
 }
 
 }  // namespace
@@ -1737,6 +1815,10 @@ int icsref_set_config(ics_handle h, const ics_config* cfg) {
     return ICS_ERR_SCHEME;
   }
   if (cfg->n_directions < 1 || cfg->n_directions > 64) return ICS_ERR_ARG;
+  if (h->nInst > 1 && (cfg->ddt_scheme != ICS_DDT_STEADY || cfg->solver != ICS_SOLVER_GMRES)) {
+    h->err = "Harmonic Balance needs steadyState ddt and the GMRES solver";
+    return ICS_ERR_ARG;
+  }
   h->cfg = *cfg;
   h->Cv = cfg->Cp - cfg->R;
   h->gamma = cfg->Cp / h->Cv;
@@ -1752,6 +1834,7 @@ int icsref_create(const ics_mesh_desc* m, const ics_config* cfg, ics_handle* out
   ics_handle h = new ics_handle_s();
   Case& c = *h;
   c.N = m->n_cells;
+  c.Nc = c.N;
   c.F = m->n_faces;
   c.B = m->n_bfaces;
   c.own.assign(m->owner, m->owner + c.F);
@@ -2023,15 +2106,18 @@ int icsref_solve_increment(ics_handle h, ics_solver_perf* perf, double* dW) {
   Case& c = *h;
   if (!c.haveMatrix) return ICS_ERR_STATE;
   storeW(c, c.Wprev);
-  ics_solver_perf pf;
-  int st = c.cfg.solver == ICS_SOLVER_SMOOTH ? smoothSolveDelta(c, c.Wprev, pf, c.dW)
-                                             : gmresSolveDelta(c, c.Wprev, pf, c.dW);
+  ResIO rio;
+  int st = c.cfg.solver == ICS_SOLVER_SMOOTH ? smoothSolveDelta(c, c.Wprev, rio, c.dW)
+                                             : gmresSolveDelta(c, c.Wprev, rio, c.dW);
   c.haveIncrement = true;
+  ics_solver_perf pf;
+  toPerf(rio, pf);
+  pf.converged = st == ICS_OK;
   if (perf) *perf = pf;
   if (dW) std::memcpy(dW, c.dW.data(), sizeof(double) * 5 * c.N);
-  c.initRes = pf;
+  c.initRes = rio.init;
   c.initResValid = true;
-  c.residuals_ = pf;
+  for (int J = 0; J < c.nInst; ++J) std::memcpy(c.ctl[J].residuals, &rio.init[5 * J], 5 * sizeof(double));
   return st;
 }
 
@@ -2095,6 +2181,30 @@ int icsref_begin_time_step(ics_handle h) {
     c.prevResValid = false;
   }
   if (c.cfg.reset_pseudo) std::fill(c.pseudoCo.begin(), c.pseudoCo.end(), c.cfg.pseudo_co_num);
+  return ICS_OK;
+}
+
+// Harmonic Balance: the handle's cells are n_instances stacked copies of one
+// mesh (instance-major); D is the row-major n x n spectral operator
+int icsref_set_hb(ics_handle h, int32_t n, const double* D) {
+  if (!h || n < 1 || n > ICS_MAX_INSTANCES || (n > 1 && !D)) return ICS_ERR_ARG;
+  Case& c = *h;
+  if (c.N % n != 0) {
+    c.err = "cell count is not a multiple of the number of instances";
+    return ICS_ERR_ARG;
+  }
+  if (n > 1 && (c.cfg.ddt_scheme != ICS_DDT_STEADY || c.cfg.solver != ICS_SOLVER_GMRES)) {
+    c.err = "Harmonic Balance needs steadyState ddt and the GMRES solver";
+    return ICS_ERR_ARG;
+  }
+  for (int q = 0; q < n * n && n > 1; ++q)
+    if (!std::isfinite(D[q])) return ICS_ERR_ARG;
+  c.nInst = n;
+  c.Nc = c.N / n;
+  c.Dhb.assign(n > 1 ? D : nullptr, n > 1 ? D + n * n : nullptr);
+  c.ctl.assign(n, Case::Control());
+  c.initResValid = c.prevResValid = false;
+  c.haveMatrix = c.haveIncrement = false;
   return ICS_OK;
 }
 

@@ -1,0 +1,79 @@
+"""Harmonic Balance on the CUDA path against the oracle.
+
+Same stacked case (3 instances, oscillating back pressure) in both
+libraries: residual source with the -V D W term, Jacobian action with the
+V D couplings, the per-instance norm factors / residuals of the solve, and a
+run of pseudo iterations with the per-instance pseudotimeControl sequence.
+Tolerances as in the other parity tests (FP64: 1e-12 for single kernels,
+1e-10 for solves and trajectories; mixed precision looser).
+"""
+
+import numpy as np
+import pytest
+
+from icsfoam_gb300 import abi, cases
+
+from test_gpu_parity import relerr  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def open_case(b, w, **over):
+    h = abi.CaseHandle(b, w.mesh, cases.make_config(b, w.settings, **over))
+    h.set_hb(*w.hb)
+    h.set_primitive(w.p, w.U, w.T)
+    return h
+
+
+@pytest.fixture(scope="module")
+def hbcase():
+    return cases.hb_bump_channel(16, 6, 3, amplitude=0.1)
+
+
+def test_hb_residual_and_matrix_action(gpu_binding, oracle_binding, hbcase):
+    hg, ho = open_case(gpu_binding, hbcase), open_case(oracle_binding, hbcase)
+    assert relerr(hg.residual(), ho.residual()) < 1e-12
+    hg.assemble_jacobian()
+    ho.assemble_jacobian()
+    x = np.random.default_rng(1).standard_normal((hbcase.mesh.n_cells, 5))
+    assert relerr(hg.matrix_mul(x), ho.matrix_mul(x)) < 1e-12
+    assert relerr(hg.precondition(x), ho.precondition(x)) < 1e-12
+
+
+def test_hb_solve_increment(gpu_binding, oracle_binding, hbcase):
+    hg, ho = open_case(gpu_binding, hbcase), open_case(oracle_binding, hbcase)
+    for h in (hg, ho):
+        h.residual()
+        h.assemble_jacobian()
+    pg, dg, _ = hg.solve_increment()
+    po, do, _ = ho.solve_increment()
+    assert pg.n_iterations == po.n_iterations
+    assert np.allclose(pg.init_res[:], po.init_res[:], rtol=1e-10, atol=0)
+    assert relerr(dg, do) < 1e-10
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-10), (1, 1e-5)])
+def test_hb_pseudo_iterations_and_loop(gpu_binding, oracle_binding, hbcase, precision, tol):
+    over = dict(n_pseudo_corr_min=2, pseudo_tol=1e-30, pseudo_tol_rel=0.3)
+    hg = open_case(gpu_binding, hbcase, precision=precision, **over)
+    ho = open_case(oracle_binding, hbcase, **over)
+    seq = []
+    for _ in range(12):
+        mg, mo = hg.pseudo_loop(), ho.pseudo_loop()
+        assert mg == mo
+        seq.append(mg)
+        hg.pseudo_iteration()
+        ho.pseudo_iteration()
+    assert relerr(hg.get_state()["W"], ho.get_state()["W"]) < tol
+
+
+def test_hb_rejects_noalloc_entry(gpu_binding, hbcase):
+    import torch
+
+    h = open_case(gpu_binding, hbcase)
+    h.residual()
+    h.assemble_jacobian()
+    x = torch.zeros((hbcase.mesh.n_cells, 5), dtype=torch.float64, device="cuda")
+    r = torch.zeros_like(x)
+    l1 = torch.zeros(5, dtype=torch.float64, device="cuda")
+    assert h.linear_residual_noalloc(x.data_ptr(), r.data_ptr(), l1.data_ptr()) == abi.ICS_ERR_ARG

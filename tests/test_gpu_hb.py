@@ -52,11 +52,20 @@ def test_hb_solve_increment(gpu_binding, oracle_binding, hbcase):
     assert relerr(dg, do) < 1e-10
 
 
-@pytest.mark.parametrize("precision,tol", [(0, 1e-10), (1, 1e-5)])
-def test_hb_pseudo_iterations_and_loop(gpu_binding, oracle_binding, hbcase, precision, tol):
-    over = dict(n_pseudo_corr_min=2, pseudo_tol=1e-30, pseudo_tol_rel=0.3)
-    hg = open_case(gpu_binding, hbcase, precision=precision, **over)
-    ho = open_case(oracle_binding, hbcase, **over)
+@pytest.mark.parametrize("precision,tol", [(0, 1e-10), (1, 1e-4)])
+def test_hb_pseudo_iterations_and_loop(gpu_binding, oracle_binding, precision, tol):
+    """Lockstep pseudo iterations; the loop completes and restarts (steady).
+
+    24x8x4 instances: on this mesh the oracle's own trajectory moves by
+    ~1e-14 under a 1e-14 perturbation of the initial state.  (Meshes such
+    as 16x6x3 are ill-conditioned: a cell at a local extremum whose face
+    extrapolation is round-off decides between limiter 0 and 1, and a 1e-14
+    perturbation moves the oracle's own state by 5e-4 in one iteration.)
+    """
+    w = cases.hb_bump_channel(24, 8, 4, amplitude=0.1)
+    over = dict(n_pseudo_corr_min=2, pseudo_tol=0.3, pseudo_tol_rel=1e-30)
+    hg = open_case(gpu_binding, w, precision=precision, **over)
+    ho = open_case(oracle_binding, w, **over)
     seq = []
     for _ in range(12):
         mg, mo = hg.pseudo_loop(), ho.pseudo_loop()
@@ -64,7 +73,8 @@ def test_hb_pseudo_iterations_and_loop(gpu_binding, oracle_binding, hbcase, prec
         seq.append(mg)
         hg.pseudo_iteration()
         ho.pseudo_iteration()
-    assert relerr(hg.get_state()["W"], ho.get_state()["W"]) < tol
+        assert relerr(hg.get_state()["W"], ho.get_state()["W"]) < tol
+    assert not all(seq)
 
 
 def test_hb_rejects_noalloc_entry(gpu_binding, hbcase):

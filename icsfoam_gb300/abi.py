@@ -142,8 +142,15 @@ _MEASURE = {
 # allocation-free linear residual (CUDA library only; arguments are device pointers)
 _MEASURE["linear_residual_noalloc"] = (C.c_int, [_P, _P, _P, _P])
 
+# differentiation of the residual (CUDA library only)
+_MEASURE["jvp"] = (C.c_int, [_P, _P, _P, C.c_int32])
+_MEASURE["vjp"] = (C.c_int, [_P, _P, _P, C.c_int32])
+_MEASURE["assemble_exact_jacobian"] = (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int32)])
+_MEASURE["get_exact_jacobian"] = (C.c_int, [_P, _P, _P, _P])
+
 KERNEL_CLASSES = ("fields", "grad", "face", "bface", "cellres", "jac_boundary", "jac_rows", "jacobi_inv", "spmv",
-                  "lusgs_fwd", "lusgs_rev", "jacobi", "mgs", "vector", "scalar", "update", "bc", "bound", "visc")
+                  "lusgs_fwd", "lusgs_rev", "jacobi", "mgs", "vector", "scalar", "update", "bc", "bound", "visc",
+                  "tangent", "exact")
 
 EXPORTED = tuple(_FUNCS) + tuple(_MEASURE)
 
@@ -385,6 +392,49 @@ class CaseHandle:
         ms = C.c_double()
         self._check(self.b.fn["timer_stop"](self.h, C.byref(ms)), "timer_stop")
         return float(ms.value)
+
+    # ------------------------------------------------------ differentiation
+    def jvp(self, v: np.ndarray) -> np.ndarray:
+        """d(R V)/dW v at the current state (boundary values fixed)."""
+        v = np.ascontiguousarray(v, np.float64).reshape(self.N, 5)
+        out = np.empty((self.N, 5))
+        self._check(self.b.fn["jvp"](self.h, _ptr(v), _ptr(out), 0), "jvp")
+        return out
+
+    def vjp(self, u: np.ndarray) -> np.ndarray:
+        """(d(R V)/dW)^T u with the exact Jacobian."""
+        u = np.ascontiguousarray(u, np.float64).reshape(self.N, 5)
+        out = np.empty((self.N, 5))
+        self._check(self.b.fn["vjp"](self.h, _ptr(u), _ptr(out), 0), "vjp")
+        return out
+
+    def jvp_device(self, v_dev: int, out_dev: int):
+        self._check(self.b.fn["jvp"](self.h, v_dev, out_dev, 1), "jvp")
+
+    def vjp_device(self, u_dev: int, out_dev: int):
+        self._check(self.b.fn["vjp"](self.h, u_dev, out_dev, 1), "vjp")
+
+    def assemble_exact_jacobian(self):
+        nnz = C.c_int64()
+        ncol = C.c_int32()
+        self._check(self.b.fn["assemble_exact_jacobian"](self.h, C.byref(nnz), C.byref(ncol)),
+                    "assemble_exact_jacobian")
+        return int(nnz.value), int(ncol.value)
+
+    def get_exact_jacobian(self):
+        """(row_ptr, cols, blocks[nnz, 5, 5]) of the assembled exact Jacobian."""
+        nnz, _ = self._exact_size()
+        ptr = np.empty(self.N + 1, np.int32)
+        cols = np.empty(nnz, np.int32)
+        blocks = np.empty((nnz, 5, 5))
+        self._check(self.b.fn["get_exact_jacobian"](self.h, _ptr(ptr), _ptr(cols), _ptr(blocks)),
+                    "get_exact_jacobian")
+        return ptr, cols, blocks
+
+    def _exact_size(self):
+        ptr = np.empty(self.N + 1, np.int32)
+        self._check(self.b.fn["get_exact_jacobian"](self.h, _ptr(ptr), None, None), "get_exact_jacobian")
+        return int(ptr[-1]), ptr
 
     def linear_residual_noalloc(self, x_dev: int, r_dev: int, l1_dev: int) -> int:
         """Device-pointer call of ics_linear_residual_noalloc; returns the status."""

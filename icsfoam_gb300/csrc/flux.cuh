@@ -13,63 +13,78 @@
 // explicit "- 0.0" only where it changes nothing.
 #pragma once
 
+#include "dual.cuh"
 #include "ics_internal.cuh"
 
 namespace ics {
 
-struct FState {
-  double rho, p, U[3], E, H, c;
+// Face state; Real = double for the residual, Dual for its tangent
+template <typename Real>
+struct FStateT {
+  Real rho, p, U[3], E, H, c;
 };
+using FState = FStateT<double>;
 
-__device__ __forceinline__ double sq(double x) { return x * x; }
-__device__ __forceinline__ double dot3(const double* a, const double* b) {
+template <typename Real>
+__device__ __forceinline__ Real sq(const Real& x) {
+  return x * x;
+}
+template <typename A, typename B>
+__device__ __forceinline__ auto dot3(const A* a, const B* b) {
   return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
 }
-__device__ __forceinline__ double pos0d(double s) { return s >= 0 ? 1.0 : 0.0; }
-__device__ __forceinline__ double negd(double s) { return s < 0 ? 1.0 : 0.0; }
+template <typename Real>
+__device__ __forceinline__ double pos0d(const Real& s) {
+  return val(s) >= 0 ? 1.0 : 0.0;
+}
+template <typename Real>
+__device__ __forceinline__ double negd(const Real& s) {
+  return val(s) < 0 ? 1.0 : 0.0;
+}
 
 // out: phi, phiUx, phiUy, phiUz, phiE
-__device__ __forceinline__ void flux_ausm(const FState& L, const FState& R, const double S[3], double magS,
-                                          int lowMach, double out[5]) {
-  const double unL = dot3(L.U, S) / magS;
-  const double unR = dot3(R.U, S) / magS;
-  const double cl = sq(L.c) / fmax(L.c, unL);
-  const double cr = sq(R.c) / fmax(R.c, -unR);
-  const double cf = fmin(cl, cr);
-  const double ML = unL / cf;
-  double Mplus, pplus;
+template <typename Real>
+__device__ __forceinline__ void flux_ausm(const FStateT<Real>& L, const FStateT<Real>& R, const double S[3],
+                                          double magS, int lowMach, Real out[5]) {
+  const Real unL = dot3(L.U, S) / magS;
+  const Real unR = dot3(R.U, S) / magS;
+  const Real cl = sq(L.c) / fmax(L.c, unL);
+  const Real cr = sq(R.c) / fmax(R.c, -unR);
+  const Real cf = fmin(cl, cr);
+  const Real ML = unL / cf;
+  Real Mplus, pplus;
   if (fabs(ML) < 1.0) {
-    const double ML2p = 0.25 * sq(ML + 1);
-    const double ML2m = -0.25 * sq(ML - 1);
+    const Real ML2p = 0.25 * sq(ML + 1);
+    const Real ML2m = -0.25 * sq(ML - 1);
     Mplus = ML2p * (1 - 2 * ML2m);
     pplus = ML2p * (2 - ML - 3 * ML * ML2m);
   } else {
     Mplus = fmax(ML, 0.0);
     pplus = ML > 0 ? 1.0 : 0.0;
   }
-  const double MR = unR / cf;
-  double Mminus, pminus;
+  const Real MR = unR / cf;
+  Real Mminus, pminus;
   if (fabs(MR) < 1.0) {
-    const double MR2m = -0.25 * sq(MR - 1);
-    const double MR2p = 0.25 * sq(MR + 1);
+    const Real MR2m = -0.25 * sq(MR - 1);
+    const Real MR2p = 0.25 * sq(MR + 1);
     Mminus = MR2m * (1 + 2 * MR2p);
     pminus = MR2m * (-2 - MR + 3 * MR * MR2p);
   } else {
     Mminus = fmin(MR, 0.0);
     pminus = MR < 0 ? 1.0 : 0.0;
   }
-  double M12 = Mplus + Mminus;
-  double p12 = pplus * L.p + pminus * R.p;
-  const double Mmean = 0.5 * (sq(unL) + sq(unR)) / sq(cf);
-  const double MDiff = -0.25 * fmax((1.0 - Mmean), 0.0) * (R.p - L.p) / (0.5 * (L.rho + R.rho) * sq(cf));
+  Real M12 = Mplus + Mminus;
+  Real p12 = pplus * L.p + pminus * R.p;
+  const Real Mmean = 0.5 * (sq(unL) + sq(unR)) / sq(cf);
+  const Real MDiff = -0.25 * fmax((1.0 - Mmean), 0.0) * (R.p - L.p) / (0.5 * (L.rho + R.rho) * sq(cf));
   if ((M12 > 0.0 && M12 + MDiff <= 0.0) || (M12 < 0.0 && M12 + MDiff >= 0.0))
     M12 += 0.2 * MDiff;
   else
     M12 += MDiff;
   if (lowMach) p12 += -0.25 * pplus * pminus * (L.rho + R.rho) * cf * (unR - unL);
   const bool left = M12 >= 0;
-  const FState& up = left ? L : R;
-  const double rhoa = M12 * cf * up.rho;
+  const FStateT<Real>& up = left ? L : R;
+  const Real rhoa = M12 * cf * up.rho;
   out[0] = rhoa * magS;
   out[1] = rhoa * up.U[0] * magS + p12 * S[0];
   out[2] = rhoa * up.U[1] * magS + p12 * S[1];
@@ -77,78 +92,81 @@ __device__ __forceinline__ void flux_ausm(const FState& L, const FState& R, cons
   out[4] = rhoa * up.H * magS + p12 * 0.0 * magS;
 }
 
-__device__ __forceinline__ void flux_hllc(const FState& L, const FState& R, const double n[3], double magS,
-                                          double gInterp, double out[5]) {
-  const double coefR = sqrt(fmax(VSMALL, R.rho) / fmax(VSMALL, L.rho));
-  const double icr = 1.0 / (coefR + 1.0);  // one FP64 reciprocal for the four Roe averages
-  double uAvg[3];
+template <typename Real>
+__device__ __forceinline__ void flux_hllc(const FStateT<Real>& L, const FStateT<Real>& R, const double n[3],
+                                          double magS, double gInterp, Real out[5]) {
+  const Real coefR = sqrt(fmax(VSMALL, R.rho) / fmax(VSMALL, L.rho));
+  const Real icr = 1.0 / (coefR + 1.0);  // one FP64 reciprocal for the four Roe averages
+  Real uAvg[3];
   for (int k = 0; k < 3; ++k) uAvg[k] = (coefR * R.U[k] + L.U[k]) * icr;
-  const double HAvg = (coefR * R.H + L.H) * icr;
-  const double cAvg = sqrt(fabs((gInterp - 1.0) * (HAvg - 0.5 * dot3(uAvg, uAvg))));
-  const double uMag_l = dot3(L.U, n) - 0.0;
-  const double uMag_r = dot3(R.U, n) - 0.0;
-  const double uMagAvg = dot3(uAvg, n) - 0.0;
-  const double Sl = fmin(uMag_l - L.c, uMagAvg - cAvg);
-  const double Sr = fmax(uMag_r + R.c, uMagAvg + cAvg);
-  const double rl = L.rho, rr = R.rho, pl = L.p, pr = R.p;
-  const double Sm = (rr * uMag_r * (Sr - uMag_r) - rl * uMag_l * (Sl - uMag_l) + pl - pr) /
+  const Real HAvg = (coefR * R.H + L.H) * icr;
+  const Real cAvg = sqrt(fabs((gInterp - 1.0) * (HAvg - 0.5 * dot3(uAvg, uAvg))));
+  const Real uMag_l = dot3(L.U, n) - 0.0;
+  const Real uMag_r = dot3(R.U, n) - 0.0;
+  const Real uMagAvg = dot3(uAvg, n) - 0.0;
+  const Real Sl = fmin(uMag_l - L.c, uMagAvg - cAvg);
+  const Real Sr = fmax(uMag_r + R.c, uMagAvg + cAvg);
+  const Real rl = L.rho, rr = R.rho, pl = L.p, pr = R.p;
+  const Real Sm = (rr * uMag_r * (Sr - uMag_r) - rl * uMag_l * (Sl - uMag_l) + pl - pr) /
                     (rr * (Sr - uMag_r) - rl * (Sl - uMag_l));
   const double coefSl = pos0d(Sl);
   const double coefSr = negd(Sr);
   const double coefSm = pos0d(Sm);
   const double coefSlm = (1.0 - coefSl) * coefSm;
   const double coefSmr = (1.0 - coefSm) * (1.0 - coefSr);
-  const double fluxRhoStar_l = Sm / (Sl - Sm) * ((Sl - uMag_l) * rl);
-  const double fluxRhoStar_r = Sm / (Sr - Sm) * ((Sr - uMag_r) * rr);
+  const Real fluxRhoStar_l = Sm / (Sl - Sm) * ((Sl - uMag_l) * rl);
+  const Real fluxRhoStar_r = Sm / (Sr - Sm) * ((Sr - uMag_r) * rr);
   out[0] = (coefSl * rl * uMag_l + coefSlm * fluxRhoStar_l + coefSmr * fluxRhoStar_r + coefSr * rr * uMag_r) * magS;
-  const double pStar_l = rl * (uMag_l - Sl) * (uMag_l - Sm) + pl;
-  const double pStar_r = rr * (uMag_r - Sr) * (uMag_r - Sm) + pr;
-  const double il = 1.0 / (Sl - Sm), ir = 1.0 / (Sr - Sm);
+  const Real pStar_l = rl * (uMag_l - Sl) * (uMag_l - Sm) + pl;
+  const Real pStar_r = rr * (uMag_r - Sr) * (uMag_r - Sm) + pr;
+  const Real il = 1.0 / (Sl - Sm), ir = 1.0 / (Sr - Sm);
   for (int k = 0; k < 3; ++k) {
-    const double rusl = il * ((Sl - uMag_l) * rl * L.U[k] + (pStar_l - pl) * n[k]);
-    const double rusr = ir * ((Sr - uMag_r) * rr * R.U[k] + (pStar_r - pr) * n[k]);
-    const double fl = Sm * rusl + pStar_l * n[k];
-    const double fr = Sm * rusr + pStar_r * n[k];
+    const Real rusl = il * ((Sl - uMag_l) * rl * L.U[k] + (pStar_l - pl) * n[k]);
+    const Real rusr = ir * ((Sr - uMag_r) * rr * R.U[k] + (pStar_r - pr) * n[k]);
+    const Real fl = Sm * rusl + pStar_l * n[k];
+    const Real fr = Sm * rusr + pStar_r * n[k];
     out[1 + k] = (coefSl * (rl * uMag_l * L.U[k] + pl * n[k]) + coefSlm * fl + coefSmr * fr +
                   coefSr * (rr * uMag_r * R.U[k] + pr * n[k])) *
                  magS;
   }
-  const double rhoEStar_l = il * ((Sl - uMag_l) * (rl * L.E) - pl * uMag_l + pStar_l * Sm);
-  const double rhoEStar_r = ir * ((Sr - uMag_r) * (rr * R.E) - pr * uMag_r + pStar_r * Sm);
-  const double fEl = Sm * (rhoEStar_l + pStar_l) + pStar_l * 0.0;
-  const double fEr = Sm * (rhoEStar_r + pStar_r) + pStar_r * 0.0;
+  const Real rhoEStar_l = il * ((Sl - uMag_l) * (rl * L.E) - pl * uMag_l + pStar_l * Sm);
+  const Real rhoEStar_r = ir * ((Sr - uMag_r) * (rr * R.E) - pr * uMag_r + pStar_r * Sm);
+  const Real fEl = Sm * (rhoEStar_l + pStar_l) + pStar_l * 0.0;
+  const Real fEr = Sm * (rhoEStar_r + pStar_r) + pStar_r * 0.0;
   out[4] = (coefSl * rl * L.H * uMag_l + coefSlm * fEl + coefSmr * fEr + coefSr * rr * R.H * uMag_r) * magS;
 }
 
-__device__ __forceinline__ void cross3(const double* a, const double* b, double* c) {
+template <typename A, typename B, typename C>
+__device__ __forceinline__ void cross3(const A* a, const B* b, C* c) {
   c[0] = a[1] * b[2] - a[2] * b[1];
   c[1] = a[2] * b[0] - a[0] * b[2];
   c[2] = a[0] * b[1] - a[1] * b[0];
 }
 
-__device__ __forceinline__ void flux_roe(const FState& L, const FState& R, const double n[3], double magS,
-                                         double gI, double eps, double out[5]) {
-  const double coefR = sqrt(fmax(VSMALL, R.rho) / fmax(VSMALL, L.rho));
-  const double rD = coefR * L.rho;
-  double rU[3];
-  const double icr = 1.0 / (coefR + 1.0);
+template <typename Real>
+__device__ __forceinline__ void flux_roe(const FStateT<Real>& L, const FStateT<Real>& R, const double n[3],
+                                         double magS, double gI, double eps, Real out[5]) {
+  const Real coefR = sqrt(fmax(VSMALL, R.rho) / fmax(VSMALL, L.rho));
+  const Real rD = coefR * L.rho;
+  Real rU[3];
+  const Real icr = 1.0 / (coefR + 1.0);
   for (int k = 0; k < 3; ++k) rU[k] = (coefR * R.U[k] + L.U[k]) * icr;
-  const double rH = (coefR * R.H + L.H) * icr;
-  const double rC = sqrt(fabs((gI - 1.0) * (rH - 0.5 * dot3(rU, rU))));
-  const double uMag_l = dot3(L.U, n), uMag_r = dot3(R.U, n);
-  const double uProj = dot3(rU, n) - 0.0;
+  const Real rH = (coefR * R.H + L.H) * icr;
+  const Real rC = sqrt(fabs((gI - 1.0) * (rH - 0.5 * dot3(rU, rU))));
+  const Real uMag_l = dot3(L.U, n), uMag_r = dot3(R.U, n);
+  const Real uProj = dot3(rU, n) - 0.0;
   const double a1 = gI - 1;
-  const double theta = 0.5 * a1 * dot3(rU, rU);
-  const double c2 = sq(rC);
-  const double a2 = 1 / (rD * rC * sqrt(2.0));
-  const double a3 = rD / (rC * sqrt(2.0));
-  const double a4 = (theta + c2) / a1;
-  const double a5 = 1 - theta / c2;
-  const double a6 = theta / a1;
-  double cUn[3];
+  const Real theta = 0.5 * a1 * dot3(rU, rU);
+  const Real c2 = sq(rC);
+  const Real a2 = 1 / (rD * rC * sqrt(2.0));
+  const Real a3 = rD / (rC * sqrt(2.0));
+  const Real a4 = (theta + c2) / a1;
+  const Real a5 = 1 - theta / c2;
+  const Real a6 = theta / a1;
+  Real cUn[3];
   cross3(rU, n, cUn);
-  double invP11[3], invP13[3], invP22[3], invP32[3];
-  double invP12[3][3];
+  Real invP11[3], invP13[3], invP22[3], invP32[3];
+  Real invP12[3][3];
   for (int i = 0; i < 3; ++i) {
     invP11[i] = (n[i] * a5) - cUn[i] / rD;
     invP13[i] = -a1 / c2 * n[i];
@@ -162,16 +180,16 @@ __device__ __forceinline__ void flux_roe(const FState& L, const FState& R, const
   invP12[1][2] += n[0] / rD;
   invP12[2][0] += n[1] / rD;
   invP12[2][1] -= n[0] / rD;
-  const double invP21 = a2 * (theta - rC * uProj);
-  const double invP23 = a1 * a2;
-  const double invP31 = a2 * (theta + rC * uProj);
-  const double invP33 = a1 * a2;
-  double L1 = fabs(uProj), L2 = fabs(uProj + rC), L3 = fabs(uProj - rC);
-  const double epsilon = eps * fmax(L2, L3);
+  const Real invP21 = a2 * (theta - rC * uProj);
+  const Real invP23 = a1 * a2;
+  const Real invP31 = a2 * (theta + rC * uProj);
+  const Real invP33 = a1 * a2;
+  Real L1 = fabs(uProj), L2 = fabs(uProj + rC), L3 = fabs(uProj - rC);
+  const Real epsilon = eps * fmax(L2, L3);
   if (L1 < epsilon) L1 = (sq(L1) + sq(epsilon)) / (2.0 * epsilon);
   if (L2 < epsilon) L2 = (sq(L2) + sq(epsilon)) / (2.0 * epsilon);
   if (L3 < epsilon) L3 = (sq(L3) + sq(epsilon)) / (2.0 * epsilon);
-  double P21[3][3];
+  Real P21[3][3];
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) P21[i][j] = rU[i] * n[j];
   P21[0][1] -= n[2] * rD;
@@ -180,54 +198,54 @@ __device__ __forceinline__ void flux_roe(const FState& L, const FState& R, const
   P21[1][2] -= n[0] * rD;
   P21[2][0] -= n[1] * rD;
   P21[2][1] += n[0] * rD;
-  double P22[3], P23[3], P31[3];
+  Real P22[3], P23[3], P31[3];
   for (int i = 0; i < 3; ++i) {
     P22[i] = a3 * (rU[i] + rC * n[i]);
     P23[i] = a3 * (rU[i] - rC * n[i]);
     P31[i] = n[i] * a6 + rD * cUn[i];
   }
-  const double P12 = a3, P13 = a3;
-  const double P32 = a3 * (a4 + rC * uProj);
-  const double P33 = a3 * (a4 - rC * uProj);
+  const Real P12 = a3, P13 = a3;
+  const Real P32 = a3 * (a4 + rC * uProj);
+  const Real P33 = a3 * (a4 - rC * uProj);
   // differences of conservative states
-  const double dRho = R.rho - L.rho;
-  double dRhoU[3];
+  const Real dRho = R.rho - L.rho;
+  Real dRhoU[3];
   for (int k = 0; k < 3; ++k) dRhoU[k] = R.rho * R.U[k] - L.rho * L.U[k];
-  const double dRhoE = R.rho * R.E - L.rho * L.E;
+  const Real dRhoE = R.rho * R.E - L.rho * L.E;
   // continuity row
-  double P11L[3] = {n[0] * L1, n[1] * L1, n[2] * L1};
-  const double dCR = dot3(P11L, invP11) + (L2 * P12 * invP21) + (L3 * P13 * invP31);
-  double dCU[3];
+  Real P11L[3] = {n[0] * L1, n[1] * L1, n[2] * L1};
+  const Real dCR = dot3(P11L, invP11) + (L2 * P12 * invP21) + (L3 * P13 * invP31);
+  Real dCU[3];
   for (int j = 0; j < 3; ++j)
     dCU[j] = (P11L[0] * invP12[0][j] + P11L[1] * invP12[1][j] + P11L[2] * invP12[2][j]) + (L2 * P12 * invP22[j]) +
              (L3 * P13 * invP32[j]);
-  const double dCE = dot3(P11L, invP13) + (L2 * P12 * invP23) + (L3 * P13 * invP33);
-  double ph = -0.5 * magS * (dCR * dRho + dot3(dCU, dRhoU) + dCE * dRhoE);
+  const Real dCE = dot3(P11L, invP13) + (L2 * P12 * invP23) + (L3 * P13 * invP33);
+  Real ph = -0.5 * magS * (dCR * dRho + dot3(dCU, dRhoU) + dCE * dRhoE);
   // momentum rows
-  double pU[3];
+  Real pU[3];
   for (int i = 0; i < 3; ++i) {
-    double Pl[3] = {P21[i][0] * L1, P21[i][1] * L1, P21[i][2] * L1};
-    const double dMR = (Pl[0] * invP11[0] + Pl[1] * invP11[1] + Pl[2] * invP11[2]) + (L2 * invP21 * P22[i]) +
+    Real Pl[3] = {P21[i][0] * L1, P21[i][1] * L1, P21[i][2] * L1};
+    const Real dMR = (Pl[0] * invP11[0] + Pl[1] * invP11[1] + Pl[2] * invP11[2]) + (L2 * invP21 * P22[i]) +
                        (L3 * invP31 * P23[i]);
-    const double dME = (Pl[0] * invP13[0] + Pl[1] * invP13[1] + Pl[2] * invP13[2]) + (L2 * invP23 * P22[i]) +
+    const Real dME = (Pl[0] * invP13[0] + Pl[1] * invP13[1] + Pl[2] * invP13[2]) + (L2 * invP23 * P22[i]) +
                        (L3 * invP33 * P23[i]);
-    double dMUdot = 0;
+    Real dMUdot = 0;
     for (int j = 0; j < 3; ++j) {
-      const double dMU = (Pl[0] * invP12[0][j] + Pl[1] * invP12[1][j] + Pl[2] * invP12[2][j]) +
+      const Real dMU = (Pl[0] * invP12[0][j] + Pl[1] * invP12[1][j] + Pl[2] * invP12[2][j]) +
                          (L2 * P22[i] * invP22[j]) + (L3 * P23[i] * invP32[j]);
       dMUdot += dMU * dRhoU[j];
     }
     pU[i] = -0.5 * magS * (dMR * dRho + dMUdot + dME * dRhoE);
   }
-  double P31L[3] = {P31[0] * L1, P31[1] * L1, P31[2] * L1};
-  const double dER = dot3(P31L, invP11) + (L2 * P32 * invP21) + (L3 * P33 * invP31);
-  double dEU[3];
+  Real P31L[3] = {P31[0] * L1, P31[1] * L1, P31[2] * L1};
+  const Real dER = dot3(P31L, invP11) + (L2 * P32 * invP21) + (L3 * P33 * invP31);
+  Real dEU[3];
   for (int j = 0; j < 3; ++j)
     dEU[j] = (P31L[0] * invP12[0][j] + P31L[1] * invP12[1][j] + P31L[2] * invP12[2][j]) + (L2 * P32 * invP22[j]) +
              (L3 * P33 * invP32[j]);
-  const double dEE = dot3(P31L, invP13) + (L2 * P32 * invP23) + (L3 * P33 * invP33);
-  double pE = -0.5 * magS * (dER * dRho + dot3(dEU, dRhoU) + dEE * dRhoE);
-  const double rn_l = L.rho * uMag_l, rn_r = R.rho * uMag_r;
+  const Real dEE = dot3(P31L, invP13) + (L2 * P32 * invP23) + (L3 * P33 * invP33);
+  Real pE = -0.5 * magS * (dER * dRho + dot3(dEU, dRhoU) + dEE * dRhoE);
+  const Real rn_l = L.rho * uMag_l, rn_r = R.rho * uMag_r;
   ph += 0.5 * magS * (rn_l + rn_r);
   for (int k = 0; k < 3; ++k) pU[k] += 0.5 * magS * (rn_l * L.U[k] + rn_r * R.U[k] + n[k] * (L.p + R.p));
   pE += 0.5 * magS * (rn_l * L.H + rn_r * R.H);

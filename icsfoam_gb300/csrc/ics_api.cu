@@ -93,10 +93,12 @@ void free_all(Handle& h) {
                   m.bface, m.slot_base, m.scol, m.sface, m.nlow, m.nslot, m.fl_cells, m.rl_cells, m.fl_lptr,
                   m.rl_lptr, h.W, h.W0, h.W00, h.Wprev, h.prim, h.pB, h.TB, h.UB, h.phiB, h.pseudoCo, h.rPDT,
                   h.ddtCoeff, h.q, h.bq, h.clin, h.grad, h.fflux, h.frec, h.flam, h.bjac, h.src, h.vcell,
-                  h.fvisc, h.vsf2, m.dc, m.Dhb, h.blk, h.dg,
+                  h.fvisc, h.vsf2, m.dc, m.Dhb, h.tW, h.tprim, h.tq, h.tgrad, h.tflux, h.tvc, h.tfv, h.tv,
+                  h.blk, h.dg,
                   h.dginv, h.rD, h.kv, h.kw, h.kx, h.kb, h.kt, h.dW, h.partials, h.counter, h.ks, h.scratch,
                   h.ibuf};
   drop_graphs(h);
+  free_exact(h);
   for (void* p : ptrs) dfree(p);
   for (cudaEvent_t e : h.evPool) cudaEventDestroy(e);
   if (h.tStart) cudaEventDestroy(h.tStart);
@@ -517,6 +519,7 @@ int do_update(Handle& h, ics_iter_stats* s) {
     return ICS_ERR_STATE;
   }
   launch_bound_local_timestep(h);
+  h.haveExact = false;
   int* bounded = h.ibuf + h.m.N;
   ICS_CUDA(cudaMemsetAsync(bounded, 0, sizeof(int), h.stream));
   launch_update(h, bounded);
@@ -681,6 +684,7 @@ int ics_set_config(ics_handle hh, const ics_config* cfg) {
     h.cfg.c = *cfg;
     h.cfg.Cv = cfg->Cp - cfg->R;
     h.cfg.gamma = cfg->Cp / h.cfg.Cv;
+    h.haveExact = false;
     if (structural) ensure_workspace(h);
     return ICS_OK;
   });
@@ -704,7 +708,7 @@ int ics_set_primitive(ics_handle hh, const double* p, const double* U, const dou
     ICS_CUDA(cudaMemcpyAsync(h.W00, h.W, 5 * N * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
     ICS_CUDA(cudaStreamSynchronize(h.stream));
     h.timeIndex = 0;
-    h.haveFlux = h.haveMatrix = h.haveIncrement = false;
+    h.haveFlux = h.haveMatrix = h.haveIncrement = h.haveExact = false;
     return ICS_OK;
   });
 }
@@ -712,6 +716,7 @@ int ics_set_primitive(ics_handle hh, const double* p, const double* U, const dou
 int ics_set_boundary_state(ics_handle hh, const double* pb, const double* Ub, const double* Tb, const double* phib) {
   return guard(hh, [&](Handle& h) {
     const size_t B = h.m.B;
+    h.haveExact = false;
     if (pb) ICS_CUDA(cudaMemcpy(h.pB, pb, B * sizeof(double), cudaMemcpyHostToDevice));
     if (Tb) ICS_CUDA(cudaMemcpy(h.TB, Tb, B * sizeof(double), cudaMemcpyHostToDevice));
     if (phib) ICS_CUDA(cudaMemcpy(h.phiB, phib, B * sizeof(double), cudaMemcpyHostToDevice));
@@ -767,6 +772,7 @@ int ics_set_conservative(ics_handle hh, const double* W, int32_t set_old) {
     const size_t N = h.m.N;
     ICS_CUDA(cudaMemcpyAsync(h.W, W, 5 * N * sizeof(double), cudaMemcpyHostToDevice, h.stream));
     launch_derive_primitive(h);
+    h.haveExact = false;
     if (set_old) {
       ICS_CUDA(cudaMemcpyAsync(h.W0, h.W, 5 * N * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
       ICS_CUDA(cudaMemcpyAsync(h.W00, h.W, 5 * N * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
@@ -942,6 +948,7 @@ int ics_begin_time_step(ics_handle hh) {
       ICS_CUDA(cudaMemcpyAsync(h.W0, h.W, n5 * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
     }
     h.timeIndex++;
+    h.haveExact = false;
     if (!steady) {
       h.initResValid = false;
       h.prevResValid = false;
@@ -1016,6 +1023,91 @@ int ics_timer_stop(ics_handle hh, double* ms) {
   });
 }
 
+// Jacobian-vector products of the residual source ------------------------
+namespace {
+void ensure_tangent(Handle& h) {
+  if (h.tW) return;
+  const size_t N = h.m.N, FB = (size_t)h.m.F + h.m.B, D = 2 * sizeof(double);
+  auto dal = [&](size_t bytes) {
+    void* p = nullptr;
+    const cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
+    if (e != cudaSuccess) throw CudaError(e, "cudaMalloc", __FILE__, __LINE__);
+    return p;
+  };
+  h.tW = dal(5 * N * D);
+  h.tprim = dal(5 * N * D);
+  h.tq = dal(NQ * N * D);
+  h.tgrad = dal(3 * NQ * N * D);
+  h.tflux = dal(5 * FB * D);
+  h.tvc = dal(24 * N * D);
+  h.tfv = dal(8 * FB * D);
+  h.tv = (double*)dal(10 * N * sizeof(double));
+}
+
+// stage a [N][5] input into dst (device) from a host or device pointer
+void stage_in(Handle& h, const double* src, double* dst, int device) {
+  ICS_CUDA(cudaMemcpyAsync(dst, src, 5ull * h.m.N * sizeof(double),
+                           device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h.stream));
+}
+void stage_out(Handle& h, const double* src, double* dst, int device) {
+  ICS_CUDA(cudaMemcpyAsync(dst, src, 5ull * h.m.N * sizeof(double),
+                           device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h.stream));
+  ICS_CUDA(cudaStreamSynchronize(h.stream));
+}
+}  // namespace
+
+int ics_jvp(ics_handle hh, const double* v, double* Jv, int32_t device) {
+  if (!v || !Jv) return ICS_ERR_ARG;
+  return guard(hh, [&](Handle& h) {
+    ensure_tangent(h);
+    double* tv = h.tv;
+    double* out = h.tv + 5ull * h.m.N;
+    stage_in(h, v, tv, device);
+    launch_residual_tangent(h, tv, out);
+    stage_out(h, out, Jv, device);
+    return ICS_OK;
+  });
+}
+
+int ics_assemble_exact_jacobian(ics_handle hh, int64_t* nnz_blocks, int32_t* n_colours) {
+  return guard(hh, [&](Handle& h) {
+    ensure_tangent(h);
+    assemble_exact(h);
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    if (nnz_blocks) *nnz_blocks = h.xnnz;
+    if (n_colours) *n_colours = h.xncol;
+    return ICS_OK;
+  });
+}
+
+int ics_get_exact_jacobian(ics_handle hh, int32_t* row_ptr, int32_t* cols, double* blocks) {
+  return guard(hh, [&](Handle& h) {
+    if (!h.haveExact) {
+      h.err = "get_exact_jacobian needs ics_assemble_exact_jacobian at the current state";
+      return ICS_ERR_STATE;
+    }
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    if (row_ptr) ICS_CUDA(cudaMemcpy(row_ptr, h.xptr, (h.m.N + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+    if (cols) ICS_CUDA(cudaMemcpy(cols, h.xcol, h.xnnz * sizeof(int), cudaMemcpyDeviceToHost));
+    if (blocks) ICS_CUDA(cudaMemcpy(blocks, h.xblk, h.xnnz * 25 * sizeof(double), cudaMemcpyDeviceToHost));
+    return ICS_OK;
+  });
+}
+
+int ics_vjp(ics_handle hh, const double* u, double* JTu, int32_t device) {
+  if (!u || !JTu) return ICS_ERR_ARG;
+  return guard(hh, [&](Handle& h) {
+    ensure_tangent(h);
+    if (!h.haveExact) assemble_exact(h);
+    double* tu = h.tv;
+    double* out = h.tv + 5ull * h.m.N;
+    stage_in(h, u, tu, device);
+    exact_vjp(h, tu, out);
+    stage_out(h, out, JTu, device);
+    return ICS_OK;
+  });
+}
+
 int ics_pseudo_loop(ics_handle hh, int32_t* more) {
   if (!more) return ICS_ERR_ARG;
   return guard(hh, [&](Handle& h) {
@@ -1060,6 +1152,7 @@ int ics_set_hb(ics_handle hh, int32_t n, const double* D) {
     h.ctl.assign(n, Handle::Control());
     h.initResValid = h.prevResValid = false;
     h.haveMatrix = h.haveIncrement = false;
+    free_exact(h);   // the stencil gains the instance partners
     drop_graphs(h);  // the captured cycle's reduction grids depend on n
     return ICS_OK;
   });

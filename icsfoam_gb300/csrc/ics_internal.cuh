@@ -180,6 +180,28 @@ struct Handle {
   };
   std::vector<Control> ctl = std::vector<Control>(1);
   double lastRhoL2 = 0;
+  // residual tangent (Jacobian-vector product) workspace of dual numbers
+  // (value, derivative), allocated on first use: W, prim [5N], q [NQ N],
+  // grad [3 NQ N], face fluxes [5 (F+B)], viscous cell terms [24 N] and
+  // viscous face terms [8 (F+B)]
+  void* tW = nullptr;
+  void* tprim = nullptr;
+  void* tq = nullptr;
+  void* tgrad = nullptr;
+  void* tflux = nullptr;
+  void* tvc = nullptr;
+  void* tfv = nullptr;
+  double* tv = nullptr;   // [10N] direction and product staging
+  // exact Jacobian of the residual source: stencil CSR (two face hops plus
+  // Harmonic Balance partners), transpose positions, colouring, blocks
+  int* xptr = nullptr;
+  int* xcol = nullptr;
+  int* xtpos = nullptr;
+  int* xcolour = nullptr;
+  double* xblk = nullptr;  // [nnz][25]
+  long long xnnz = 0;
+  int xncol = 0;
+  bool haveExact = false;
   // scratch
   double* scratch = nullptr;  // generic [N*5] doubles
   int* ibuf = nullptr;        // [N] flags
@@ -225,6 +247,15 @@ void launch_set_primitive(Handle& h);
 void launch_derive_primitive(Handle& h);
 void launch_bound_local_timestep(Handle& h);
 void launch_viscous(Handle& h);
+// Jacobian-vector product of the residual source: out = d(R V)/dW v at the
+// current state with the boundary values held fixed (v, out device [N][5])
+void launch_residual_tangent(Handle& h, const double* v, double* out);
+// exact Jacobian by coloured tangents; products with it and its transpose
+void build_exact_pattern(Handle& h);
+void free_exact(Handle& h);
+void assemble_exact(Handle& h);
+void exact_vjp(Handle& h, const double* u, double* y);
+void exact_jvp(Handle& h, const double* x, double* y);
 
 // linear algebra: precision-dispatched (mixed = FP32 blocks and vectors)
 void spmv(Handle& h, const void* x, void* y);

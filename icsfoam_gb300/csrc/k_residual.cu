@@ -19,10 +19,15 @@
 // dualTimeDdtScheme.C:111-126.  Reconstruction restates OpenFOAM's
 // limitedScheme (NVD/TVD r with vanLeer or Minmod), linearUpwind and
 // cellLimited<Venkatakrishnan|minmod> Gauss linear gradients.
+#include <type_traits>
+
 #include "flux.cuh"
 #include "ics_internal.cuh"
 
 namespace ics {
+
+template <typename Real>
+constexpr bool is_fp64 = std::is_same<Real, double>::value;
 
 struct ResParams {
   double R, Cv, gamma, cstarFac;
@@ -37,19 +42,22 @@ __device__ __forceinline__ int recon_of(const ResParams& P, int q) {
 }
 
 // ------------------------------------------------------------------ fields
-__global__ void k_fields(int N, int B, const double* __restrict__ W, const double* __restrict__ prim,
+// Real = double: cells and boundary faces; Real = Dual: the cells' tangents
+// (boundary values are held fixed, their tangent is zero).
+template <typename Real>
+__global__ void k_fields(int N, int B, const Real* __restrict__ W, const Real* __restrict__ prim,
                          const double* __restrict__ pB, const double* __restrict__ TB,
-                         const double* __restrict__ UB, ResParams P, double* __restrict__ q,
+                         const double* __restrict__ UB, ResParams P, Real* __restrict__ q,
                          double* __restrict__ bq, double* __restrict__ clin, double* __restrict__ bclin) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < N) {
-    const double rho = W[5 * i];
-    const double p = prim[i], T = prim[N + i];
-    const double U0 = prim[2 * N + i], U1 = prim[3 * N + i], U2 = prim[4 * N + i];
-    const double E = P.Cv * T + 0.5 * (U0 * U0 + U1 * U1 + U2 * U2);
-    const double H = fmax(E, SMALL) + fmax(p / rho, SMALL);
-    const double psi = 1.0 / (P.R * T);
-    const double cl = sqrt(P.gamma / psi);
+    const Real rho = W[5 * i];
+    const Real p = prim[i], T = prim[N + i];
+    const Real U0 = prim[2 * N + i], U1 = prim[3 * N + i], U2 = prim[4 * N + i];
+    const Real E = P.Cv * T + 0.5 * (U0 * U0 + U1 * U1 + U2 * U2);
+    const Real H = fmax(E, SMALL) + fmax(p / rho, SMALL);
+    const Real psi = 1.0 / (P.R * T);
+    const Real cl = sqrt(P.gamma / psi);
     q[Q_RHO * N + i] = rho;
     q[Q_P * N + i] = p;
     q[Q_UX * N + i] = U0;
@@ -58,25 +66,27 @@ __global__ void k_fields(int N, int B, const double* __restrict__ W, const doubl
     q[Q_E * N + i] = E;
     q[Q_H * N + i] = H;
     q[Q_C * N + i] = P.scheme == ICS_FLUX_AUSMPLUSUP ? sqrt(P.cstarFac * H) : fmax(cl, VSMALL);
-    clin[i] = cl;
+    if constexpr (is_fp64<Real>) clin[i] = cl;
   }
-  if (i < B) {
-    const double p = pB[i], T = TB[i];
-    const double U0 = UB[i], U1 = UB[B + i], U2 = UB[2 * B + i];
-    const double psi = 1.0 / (P.R * T);
-    const double rho = psi * p;
-    const double E = P.Cv * T + 0.5 * (U0 * U0 + U1 * U1 + U2 * U2);
-    const double H = fmax(E, SMALL) + fmax(p / rho, SMALL);
-    const double cl = sqrt(P.gamma / psi);
-    bq[Q_RHO * B + i] = rho;
-    bq[Q_P * B + i] = p;
-    bq[Q_UX * B + i] = U0;
-    bq[Q_UY * B + i] = U1;
-    bq[Q_UZ * B + i] = U2;
-    bq[Q_E * B + i] = E;
-    bq[Q_H * B + i] = H;
-    bq[Q_C * B + i] = P.scheme == ICS_FLUX_AUSMPLUSUP ? sqrt(P.cstarFac * H) : fmax(cl, VSMALL);
-    bclin[i] = cl;
+  if constexpr (is_fp64<Real>) {
+    if (i < B) {
+      const double p = pB[i], T = TB[i];
+      const double U0 = UB[i], U1 = UB[B + i], U2 = UB[2 * B + i];
+      const double psi = 1.0 / (P.R * T);
+      const double rho = psi * p;
+      const double E = P.Cv * T + 0.5 * (U0 * U0 + U1 * U1 + U2 * U2);
+      const double H = fmax(E, SMALL) + fmax(p / rho, SMALL);
+      const double cl = sqrt(P.gamma / psi);
+      bq[Q_RHO * B + i] = rho;
+      bq[Q_P * B + i] = p;
+      bq[Q_UX * B + i] = U0;
+      bq[Q_UY * B + i] = U1;
+      bq[Q_UZ * B + i] = U2;
+      bq[Q_E * B + i] = E;
+      bq[Q_H * B + i] = H;
+      bq[Q_C * B + i] = P.scheme == ICS_FLUX_AUSMPLUSUP ? sqrt(P.cstarFac * H) : fmax(cl, VSMALL);
+      bclin[i] = cl;
+    }
   }
 }
 
@@ -84,18 +94,18 @@ __global__ void k_fields(int N, int B, const double* __restrict__ W, const doubl
 // One thread per cell; faces visited in increasing face index (the order the
 // face-loop gradient accumulates them).  mask selects the fields, limited
 // selects cellLimited (1 = minmod, 2 = Venkatakrishnan).
-template <int LIMITED>
-__global__ void __launch_bounds__(128) k_grad(DevMesh m, const double* __restrict__ q, const double* __restrict__ bq,
-                                              unsigned mask, double* __restrict__ grad) {
+template <int LIMITED, typename Real = double>
+__global__ void __launch_bounds__(128) k_grad(DevMesh m, const Real* __restrict__ q, const double* __restrict__ bq,
+                                              unsigned mask, Real* __restrict__ grad) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.N) return;
   const int N = m.N, F = m.F, B = m.B;
-  double g[NQ][3];
-  double qc[NQ], qmax[NQ], qmin[NQ];
+  Real g[NQ][3];
+  Real qc[NQ], qmax[NQ], qmin[NQ];
 #pragma unroll
   for (int k = 0; k < NQ; ++k) {
     g[k][0] = g[k][1] = g[k][2] = 0.0;
-    qc[k] = (mask >> k) & 1 ? q[k * N + c] : 0.0;
+    qc[k] = (mask >> k) & 1 ? q[k * N + c] : Real(0.0);
     qmax[k] = qmin[k] = qc[k];
   }
   const int e0 = m.cptr[c], e1 = m.cptr[c + 1];
@@ -110,9 +120,9 @@ __global__ void __launch_bounds__(128) k_grad(DevMesh m, const double* __restric
 #pragma unroll
     for (int k = 0; k < NQ; ++k) {
       if (!((mask >> k) & 1)) continue;
-      const double qo = q[k * N + other];
-      const double qown = isOwn ? qc[k] : qo, qnei = isOwn ? qo : qc[k];
-      const double sf = wf * (qown - qnei) + qnei;
+      const Real qo = q[k * N + other];
+      const Real qown = isOwn ? qc[k] : qo, qnei = isOwn ? qo : qc[k];
+      const Real sf = wf * (qown - qnei) + qnei;
       if (isOwn) {
         g[k][0] = g[k][0] + S0 * sf;
         g[k][1] = g[k][1] + S1 * sf;
@@ -159,7 +169,7 @@ __global__ void __launch_bounds__(128) k_grad(DevMesh m, const double* __restric
     // non-decreasing in r >= 0 for both limiters, so the minimum is L of the
     // smallest r, and the smallest r comes from the largest |e_f| of each
     // sign: two divisions per field per cell instead of two per face.
-    double epos[NQ], eneg[NQ];
+    Real epos[NQ], eneg[NQ];
     unsigned small = 0;
 #pragma unroll
     for (int k = 0; k < NQ; ++k) {
@@ -168,7 +178,7 @@ __global__ void __launch_bounds__(128) k_grad(DevMesh m, const double* __restric
       qmax[k] -= qc[k];
       qmin[k] -= qc[k];
     }
-    auto faceExtrap = [&](int k, double ex) {
+    auto faceExtrap = [&](int k, const Real& ex) {
       if (ex > SMALL)
         epos[k] = fmax(epos[k], ex);
       else if (ex < -SMALL)
@@ -201,12 +211,12 @@ __global__ void __launch_bounds__(128) k_grad(DevMesh m, const double* __restric
 #pragma unroll
     for (int k = 0; k < NQ; ++k) {
       if (!((mask >> k) & 1) || !anyFace) continue;
-      double r = VGREAT;
+      Real r = VGREAT;
       if (epos[k] > 0.0) r = fmin(r, qmax[k] / epos[k]);
       if (eneg[k] < 0.0) r = fmin(r, qmin[k] / eneg[k]);
       if ((small >> k) & 1) r = fmin(r, 1.0);
-      const double lr = LIMITED == 2 ? (r * r + 2 * r) / (r * r + r + 2) : fmin(r, 1.0);
-      const double lim = r >= VGREAT ? 1.0 : fmin(1.0, lr);
+      const Real lr = LIMITED == 2 ? (r * r + 2 * r) / (r * r + r + 2) : fmin(r, 1.0);
+      const Real lim = r >= VGREAT ? Real(1.0) : fmin(1.0, lr);
       g[k][0] = g[k][0] * lim;
       g[k][1] = g[k][1] * lim;
       g[k][2] = g[k][2] * lim;
@@ -223,63 +233,65 @@ __global__ void __launch_bounds__(128) k_grad(DevMesh m, const double* __restric
 
 // ------------------------------------------------------------ face fluxes
 // reconstruct field k on face f for direction dir (+1 owner side, -1 neighbour side)
-__device__ __forceinline__ double reconstruct(const DevMesh& m, int scheme, int k, int f, int o, int nb, double qo,
-                                              double qn, const double* __restrict__ grad, double dir) {
+template <typename Real>
+__device__ __forceinline__ Real reconstruct(const DevMesh& m, int scheme, int k, int f, int o, int nb, const Real& qo,
+                                            const Real& qn, const Real* __restrict__ grad, double dir) {
   const int N = m.N, F = m.F;
   const double wUp = dir > 0 ? 1.0 : 0.0;
   if (scheme == ICS_RECON_UPWIND) return wUp * (qo - qn) + qn;
   if (scheme == ICS_RECON_VANLEER || scheme == ICS_RECON_MINMOD) {
     const int c = dir > 0 ? o : nb;
     const double d0 = m.dCC[f], d1 = m.dCC[F + f], d2 = m.dCC[2 * F + f];
-    const double gradf = qn - qo;
-    const double gradcf = d0 * grad[(3 * k) * N + c] + d1 * grad[(3 * k + 1) * N + c] + d2 * grad[(3 * k + 2) * N + c];
-    double r;
+    const Real gradf = qn - qo;
+    const Real gradcf = d0 * grad[(3 * k) * N + c] + d1 * grad[(3 * k + 1) * N + c] + d2 * grad[(3 * k + 2) * N + c];
+    Real r;
     if (fabs(gradcf) >= 1000 * fabs(gradf))
-      r = 2 * 1000 * (gradcf >= 0 ? 1.0 : -1.0) * (gradf >= 0 ? 1.0 : -1.0) - 1;
+      r = 2 * 1000 * (gradcf >= 0 ? 1.0 : -1.0) * (gradf >= 0 ? 1.0 : -1.0) - 1.0;
     else
       r = 2 * (gradcf / gradf) - 1;
-    double lim;
+    Real lim;
     if (scheme == ICS_RECON_VANLEER)
       lim = (r + fabs(r)) / (1 + fabs(r));
     else
       lim = fmax(fmin(fmin(r, 1.0), 2.0), 0.0);
-    const double wgt = lim * m.w[f] + (1.0 - lim) * wUp;
+    const Real wgt = lim * m.w[f] + (1.0 - lim) * wUp;
     return wgt * (qo - qn) + qn;
   }
   // MUSCL: upwind value + limited-gradient extrapolation
   const int c = dir > 0 ? o : nb;
   const double* d = dir > 0 ? m.dOwn : m.dNei;
-  const double base = wUp * (qo - qn) + qn;
+  const Real base = wUp * (qo - qn) + qn;
   return base + (d[f] * grad[(3 * k) * N + c] + d[F + f] * grad[(3 * k + 1) * N + c] +
                  d[2 * F + f] * grad[(3 * k + 2) * N + c]);
 }
 
-__global__ void __launch_bounds__(128) k_face(DevMesh m, ResParams P, const double* __restrict__ q,
-                                              const double* __restrict__ grad, const double* __restrict__ clin,
-                                              const double* __restrict__ nf, double* __restrict__ fflux,
+template <typename Real = double>
+__global__ void __launch_bounds__(128) k_face(DevMesh m, ResParams P, const Real* __restrict__ q,
+                                              const Real* __restrict__ grad, const double* __restrict__ clin,
+                                              const double* __restrict__ nf, Real* __restrict__ fflux,
                                               double* __restrict__ frec, double* __restrict__ flam, int FB) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.F) return;
   const int N = m.N, F = m.F;
   const int o = m.own[f], nb = m.nei[f];
-  double qL[NQ], qR[NQ];
+  Real qL[NQ], qR[NQ];
 #pragma unroll
   for (int k = 0; k < NQ; ++k) {
     if (P.scheme == ICS_FLUX_ROE && k == Q_C) {
       qL[k] = qR[k] = 0.0;
       continue;
     }
-    const double qo = q[k * N + o], qn = q[k * N + nb];
+    const Real qo = q[k * N + o], qn = q[k * N + nb];
     const int sch = recon_of(P, k);
     qL[k] = reconstruct(m, sch, k, f, o, nb, qo, qn, grad, +1.0);
     qR[k] = reconstruct(m, sch, k, f, o, nb, qo, qn, grad, -1.0);
   }
-  FState L{qL[Q_RHO], qL[Q_P], {qL[Q_UX], qL[Q_UY], qL[Q_UZ]}, qL[Q_E], qL[Q_H], qL[Q_C]};
-  FState R{qR[Q_RHO], qR[Q_P], {qR[Q_UX], qR[Q_UY], qR[Q_UZ]}, qR[Q_E], qR[Q_H], qR[Q_C]};
+  FStateT<Real> L{qL[Q_RHO], qL[Q_P], {qL[Q_UX], qL[Q_UY], qL[Q_UZ]}, qL[Q_E], qL[Q_H], qL[Q_C]};
+  FStateT<Real> R{qR[Q_RHO], qR[Q_P], {qR[Q_UX], qR[Q_UY], qR[Q_UZ]}, qR[Q_E], qR[Q_H], qR[Q_C]};
   const double S[3] = {m.Sf[f], m.Sf[F + f], m.Sf[2 * F + f]};
   const double n[3] = {nf[f], nf[F + f], nf[2 * F + f]};
   const double magS = m.magSf[f];
-  double out[5];
+  Real out[5];
   if (P.scheme == ICS_FLUX_AUSMPLUSUP)
     flux_ausm(L, R, S, magS, P.lowMach, out);
   else if (P.scheme == ICS_FLUX_HLLC)
@@ -288,24 +300,26 @@ __global__ void __launch_bounds__(128) k_face(DevMesh m, ResParams P, const doub
     flux_roe(L, R, n, magS, P.gamma, P.entropyFix, out);
 #pragma unroll
   for (int k = 0; k < 5; ++k) fflux[k * FB + f] = out[k];
-  frec[0 * F + f] = qL[Q_UX];
-  frec[1 * F + f] = qL[Q_UY];
-  frec[2 * F + f] = qL[Q_UZ];
-  frec[3 * F + f] = qR[Q_UX];
-  frec[4 * F + f] = qR[Q_UY];
-  frec[5 * F + f] = qR[Q_UZ];
-  frec[6 * F + f] = qL[Q_E];
-  frec[7 * F + f] = qR[Q_E];
-  // wave speed with linear interpolation (setCoAndDeltaT.H:52-54)
-  const double wf = m.w[f];
-  const double ci = wf * (clin[o] - clin[nb]) + clin[nb];
-  double ui[3];
+  if constexpr (is_fp64<Real>) {  // the tangent needs only the fluxes
+    frec[0 * F + f] = qL[Q_UX];
+    frec[1 * F + f] = qL[Q_UY];
+    frec[2 * F + f] = qL[Q_UZ];
+    frec[3 * F + f] = qR[Q_UX];
+    frec[4 * F + f] = qR[Q_UY];
+    frec[5 * F + f] = qR[Q_UZ];
+    frec[6 * F + f] = qL[Q_E];
+    frec[7 * F + f] = qR[Q_E];
+    // wave speed with linear interpolation (setCoAndDeltaT.H:52-54)
+    const double wf = m.w[f];
+    const double ci = wf * (clin[o] - clin[nb]) + clin[nb];
+    double ui[3];
 #pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const double a = q[(Q_UX + k) * N + o], b = q[(Q_UX + k) * N + nb];
-    ui[k] = wf * (a - b) + b;
+    for (int k = 0; k < 3; ++k) {
+      const double a = q[(Q_UX + k) * N + o], b = q[(Q_UX + k) * N + nb];
+      ui[k] = wf * (a - b) + b;
+    }
+    flam[f] = ci + fabs(dot3(ui, n) - 0.0);
   }
-  flam[f] = ci + fabs(dot3(ui, n) - 0.0);
 }
 
 __global__ void k_bface(DevMesh m, ResParams P, const double* __restrict__ bq, const double* __restrict__ bclin,
@@ -508,7 +522,8 @@ static unsigned grad_mask(const Handle& h, int* limited) {
   return mask;
 }
 
-void launch_grad(Handle& h) {
+template <typename Real>
+static void launch_grad_t(Handle& h, const Real* q, Real* grad, int kind) {
   int limited = 0;
   const unsigned mask = grad_mask(h, &limited);
   if (!mask) return;
@@ -524,13 +539,15 @@ void launch_grad(Handle& h) {
   }
   const int bs = 128;
   if (limited == 2)
-    ICS_LAUNCH(h, ICS_K_GRAD, k_grad<2><<<grid_for(h.m.N, bs), bs, 0, h.stream>>>(h.m, h.q, h.bq, mask, h.grad));
+    ICS_LAUNCH(h, kind, k_grad<2, Real><<<grid_for(h.m.N, bs), bs, 0, h.stream>>>(h.m, q, h.bq, mask, grad));
   else if (limited == 1)
-    ICS_LAUNCH(h, ICS_K_GRAD, k_grad<1><<<grid_for(h.m.N, bs), bs, 0, h.stream>>>(h.m, h.q, h.bq, mask, h.grad));
+    ICS_LAUNCH(h, kind, k_grad<1, Real><<<grid_for(h.m.N, bs), bs, 0, h.stream>>>(h.m, q, h.bq, mask, grad));
   else
-    ICS_LAUNCH(h, ICS_K_GRAD, k_grad<0><<<grid_for(h.m.N, bs), bs, 0, h.stream>>>(h.m, h.q, h.bq, mask, h.grad));
+    ICS_LAUNCH(h, kind, k_grad<0, Real><<<grid_for(h.m.N, bs), bs, 0, h.stream>>>(h.m, q, h.bq, mask, grad));
   ICS_CUDA(cudaGetLastError());
 }
+
+void launch_grad(Handle& h) { launch_grad_t<double>(h, h.q, h.grad, ICS_K_GRAD); }
 
 void launch_face_flux(Handle& h) {
   const int FB = h.m.F + h.m.B;
@@ -566,6 +583,115 @@ void launch_residual(Handle& h, double serRatio, bool applySer) {
   ICS_LAUNCH(h, ICS_K_CELLRES, k_cellres<<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, D, h.fflux, FB, h.flam, h.W, h.W0, h.W00, h.prim,
                                                          h.clin, h.pseudoCo, h.rPDT, h.ddtCoeff, h.src, h.scratch,
                                                          h.cfg.c.viscous ? h.fvisc : nullptr));
+  ICS_CUDA(cudaGetLastError());
+}
+
+// ------------------------------------------------------------ tangent
+// Jacobian-vector product of the residual source src = R V with respect to
+// the conservative state, by forward-mode dual numbers through the same
+// kernels (derive primitives -> fields -> limited gradients -> face fluxes,
+// viscous terms), then the tangent of the cell assembly of k_cellres.  The
+// boundary values are held fixed: the boundary-face inviscid fluxes have no
+// tangent, the viscous boundary-face terms do (through the interior cell).
+
+__global__ void k_seed(long n, const double* __restrict__ W, const double* __restrict__ v, Dual* __restrict__ tW) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) tW[i] = Dual(W[i], v[i]);
+}
+
+// d(src)_c = -sum_f +-d(flux_f) + d(viscous face terms) - dgPhys V_c v_c
+//            - V_c sum_K D_JK v_(K,c)   (the pseudo-time terms cancel in R)
+__global__ void __launch_bounds__(128) k_src_tangent(DevMesh m, double dgPhys, const Dual* __restrict__ fflux,
+                                                     const Dual* __restrict__ fvisc, int FB,
+                                                     const double* __restrict__ v, double* __restrict__ out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.N) return;
+  double dv[5] = {0, 0, 0, 0, 0};
+  for (int e = m.cptr[c]; e < m.cptr[c + 1]; ++e) {
+    const int code = m.cface[e];
+    const int f = code >= 0 ? code : ~code;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      const double t = fflux[k * FB + f].d;
+      dv[k] = code >= 0 ? dv[k] + t : dv[k] - t;
+    }
+  }
+  double r[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) r[k] = -dv[k];
+  if (fvisc) {
+    double vt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int e = m.cptr[c]; e < m.cptr[c + 1]; ++e) {
+      const int code = m.cface[e];
+      const int f = code >= 0 ? code : ~code;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const double t = fvisc[k * FB + f].d;
+        vt[k] = code >= 0 ? vt[k] + t : vt[k] - t;
+      }
+    }
+    for (int e = m.bptr[c]; e < m.bptr[c + 1]; ++e) {
+      const int b = m.bface[e];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) vt[k] += fvisc[k * FB + m.F + b].d;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r[1 + k] += vt[k] + vt[3 + k];
+    r[4] += vt[6] + vt[7];
+  }
+  const double Vc = m.V[c];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) r[k] -= dgPhys * Vc * v[5 * c + k];
+  if (m.nInst > 1) {
+    const int J = c / m.Nc, cl = c - J * m.Nc;
+    for (int K = 0; K < m.nInst; ++K) {
+      const double d = Vc * m.Dhb[J * m.nInst + K];
+      const double* vk = v + 5 * ((size_t)K * m.Nc + cl);
+#pragma unroll
+      for (int k = 0; k < 5; ++k) r[k] -= d * vk[k];
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) out[5 * c + k] = r[k];
+}
+
+void launch_derive_tangent(Handle& h, const Dual* W, Dual* prim);
+void launch_viscous_tangent(Handle& h, const Dual* W, const Dual* prim, Dual* vc, Dual* fv);
+
+void launch_residual_tangent(Handle& h, const double* v, double* out) {
+  const int N = h.m.N, FB = h.m.F + h.m.B;
+  Dual* tW = (Dual*)h.tW;
+  Dual* tprim = (Dual*)h.tprim;
+  Dual* tq = (Dual*)h.tq;
+  Dual* tgrad = (Dual*)h.tgrad;
+  Dual* tflux = (Dual*)h.tflux;
+  const ResParams P = res_params(h);
+  // the boundary field values (bq) of the current boundary state
+  launch_fields(h);
+  ICS_LAUNCH(h, ICS_K_TANGENT, k_seed<<<grid_for(5L * N, 256), 256, 0, h.stream>>>(5L * N, h.W, v, tW));
+  launch_derive_tangent(h, tW, tprim);
+  ICS_LAUNCH(h, ICS_K_TANGENT, k_fields<Dual><<<grid_for(N, 256), 256, 0, h.stream>>>(N, 0, tW, tprim, nullptr, nullptr,
+                                                                                      nullptr, P, tq, nullptr, nullptr,
+                                                                                      nullptr));
+  launch_grad_t<Dual>(h, tq, tgrad, ICS_K_TANGENT);
+  if (h.m.F > 0)
+    ICS_LAUNCH(h, ICS_K_TANGENT, k_face<Dual><<<grid_for(h.m.F, 128), 128, 0, h.stream>>>(h.m, P, tq, tgrad, nullptr,
+                                                                                          h.m.nf, tflux, nullptr,
+                                                                                          nullptr, FB));
+  Dual* tfv = nullptr;
+  if (h.cfg.c.viscous) {
+    tfv = (Dual*)h.tfv;
+    launch_viscous_tangent(h, tW, tprim, (Dual*)h.tvc, tfv);
+  }
+  double dgPhys = 0.0;
+  if (h.cfg.c.ddt_scheme == ICS_DDT_EULER) dgPhys = 1.0 / h.cfg.c.delta_t;
+  if (h.cfg.c.ddt_scheme == ICS_DDT_BACKWARD) {
+    const double dt = h.cfg.c.delta_t;
+    const double dt0 = h.timeIndex <= 1 ? GREAT : dt;
+    dgPhys = (1 + dt / (dt + dt0)) / dt;
+  }
+  ICS_LAUNCH(h, ICS_K_TANGENT, k_src_tangent<<<grid_for(N, 128), 128, 0, h.stream>>>(h.m, dgPhys, tflux, tfv, FB, v,
+                                                                                     out));
   ICS_CUDA(cudaGetLastError());
 }
 

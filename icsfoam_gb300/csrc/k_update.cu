@@ -169,14 +169,15 @@ __global__ void k_bc_init(DevMesh m, const double* __restrict__ prim, double R, 
   phiB[b] = (1.0 / (R * T)) * p * dot3(U, S);
 }
 
-// primitives from W (set_conservative)
-__global__ void k_derive(int N, const double* __restrict__ W, double* __restrict__ prim, double R, double Cv) {
+// primitives from W (set_conservative); Real = Dual for the tangent
+template <typename Real>
+__global__ void k_derive(int N, const Real* __restrict__ W, Real* __restrict__ prim, double R, double Cv) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
-  const double rho = W[5 * i];
-  const double U[3] = {W[5 * i + 1] / rho, W[5 * i + 2] / rho, W[5 * i + 3] / rho};
-  const double e = W[5 * i + 4] / rho - 0.5 * dot3(U, U);
-  const double T = e / Cv;
+  const Real rho = W[5 * i];
+  const Real U[3] = {W[5 * i + 1] / rho, W[5 * i + 2] / rho, W[5 * i + 3] / rho};
+  const Real e = W[5 * i + 4] / rho - 0.5 * dot3(U, U);
+  const Real T = e / Cv;
   prim[i] = rho / (1.0 / (R * T));
   prim[N + i] = T;
   prim[2 * N + i] = U[0];
@@ -244,6 +245,12 @@ void launch_set_primitive(Handle& h) {
 
 void launch_derive_primitive(Handle& h) {
   ICS_LAUNCH(h, ICS_K_UPDATE, k_derive<<<grid_for(h.m.N, 256), 256, 0, h.stream>>>(h.m.N, h.W, h.prim, h.cfg.c.R, h.cfg.Cv));
+  ICS_CUDA(cudaGetLastError());
+}
+
+void launch_derive_tangent(Handle& h, const Dual* W, Dual* prim) {
+  ICS_LAUNCH(h, ICS_K_TANGENT, k_derive<Dual><<<grid_for(h.m.N, 256), 256, 0, h.stream>>>(h.m.N, W, prim, h.cfg.c.R,
+                                                                                          h.cfg.Cv));
   ICS_CUDA(cudaGetLastError());
 }
 

@@ -13,6 +13,8 @@
 //                             patch snGrad (psi_b - psi_P) deltaCoeffs_b
 // Reference: residualsUpdate.H:16-43 (terms kept separate, each divided by V),
 // viscousFluxScheme.C:234-247 (LaxFriedrichJacobian).
+#include <type_traits>
+
 #include "flux.cuh"
 #include "ics_internal.cuh"
 
@@ -23,22 +25,27 @@ struct ViscParams {
   int sutherland;
 };
 
-__device__ __forceinline__ double mu_of(const ViscParams& P, double T) {
-  return P.sutherland ? P.As * sqrt(T) / (1.0 + P.Ts / T) : P.mu;
+template <typename Real>
+__device__ __forceinline__ Real mu_of(const ViscParams& P, const Real& T) {
+  return P.sutherland ? P.As * sqrt(T) / (1.0 + P.Ts / T) : Real(P.mu);
 }
-__device__ __forceinline__ double alpha_of(const ViscParams& P, double mu) { return P.Cp / P.Cv * (mu / P.Pr); }
+template <typename Real>
+__device__ __forceinline__ Real alpha_of(const ViscParams& P, const Real& mu) {
+  return P.Cp / P.Cv * (mu / P.Pr);
+}
 
 // vc layout [24][N]: 0-8 grad U (3i+j), 9-11 grad e, 12-20 tau (3i+j), 21 mu, 22 alpha, 23 e
 
-__global__ void __launch_bounds__(128) k_visc_cell(DevMesh m, ViscParams P, const double* __restrict__ W,
-                                                   const double* __restrict__ prim, const double* __restrict__ TB,
-                                                   const double* __restrict__ UB, double* __restrict__ vc) {
+template <typename Real = double>
+__global__ void __launch_bounds__(128) k_visc_cell(DevMesh m, ViscParams P, const Real* __restrict__ W,
+                                                   const Real* __restrict__ prim, const double* __restrict__ TB,
+                                                   const double* __restrict__ UB, Real* __restrict__ vc) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.N) return;
   const int N = m.N, F = m.F, B = m.B;
-  double Uc[3] = {prim[2 * N + c], prim[3 * N + c], prim[4 * N + c]};
-  const double ec = W[5 * c + 4] / W[5 * c] - 0.5 * dot3(Uc, Uc);
-  double g[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, ge[3] = {0, 0, 0};
+  Real Uc[3] = {prim[2 * N + c], prim[3 * N + c], prim[4 * N + c]};
+  const Real ec = W[5 * c + 4] / W[5 * c] - 0.5 * dot3(Uc, Uc);
+  Real g[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, ge[3] = {0, 0, 0};
   for (int e = m.cptr[c]; e < m.cptr[c + 1]; ++e) {
     const int code = m.cface[e];
     const bool isOwn = code >= 0;
@@ -46,15 +53,15 @@ __global__ void __launch_bounds__(128) k_visc_cell(DevMesh m, ViscParams P, cons
     const int other = isOwn ? m.nei[f] : m.own[f];
     const double wf = m.w[f];
     const double S[3] = {m.Sf[f], m.Sf[F + f], m.Sf[2 * F + f]};
-    const double Uo[3] = {prim[2 * N + other], prim[3 * N + other], prim[4 * N + other]};
-    const double eo = W[5 * other + 4] / W[5 * other] - 0.5 * dot3(Uo, Uo);
+    const Real Uo[3] = {prim[2 * N + other], prim[3 * N + other], prim[4 * N + other]};
+    const Real eo = W[5 * other + 4] / W[5 * other] - 0.5 * dot3(Uo, Uo);
     for (int j = 0; j < 3; ++j) {
-      const double a = isOwn ? Uc[j] : Uo[j], b = isOwn ? Uo[j] : Uc[j];
-      const double sf = wf * (a - b) + b;
+      const Real a = isOwn ? Uc[j] : Uo[j], b = isOwn ? Uo[j] : Uc[j];
+      const Real sf = wf * (a - b) + b;
       for (int i = 0; i < 3; ++i) g[3 * i + j] = isOwn ? g[3 * i + j] + S[i] * sf : g[3 * i + j] - S[i] * sf;
     }
-    const double a = isOwn ? ec : eo, b = isOwn ? eo : ec;
-    const double sf = wf * (a - b) + b;
+    const Real a = isOwn ? ec : eo, b = isOwn ? eo : ec;
+    const Real sf = wf * (a - b) + b;
     for (int i = 0; i < 3; ++i) ge[i] = isOwn ? ge[i] + S[i] * sf : ge[i] - S[i] * sf;
   }
   for (int e = m.bptr[c]; e < m.bptr[c + 1]; ++e) {
@@ -69,65 +76,69 @@ __global__ void __launch_bounds__(128) k_visc_cell(DevMesh m, ViscParams P, cons
   const double Vc = m.V[c];
   for (int q = 0; q < 9; ++q) g[q] /= Vc;
   for (int q = 0; q < 3; ++q) ge[q] /= Vc;
-  const double mu = mu_of(P, prim[N + c]);
-  const double tr = g[0] + g[4] + g[8];
+  const Real mu = mu_of(P, prim[N + c]);
+  const Real tr = g[0] + g[4] + g[8];
   for (int q = 0; q < 9; ++q) vc[q * N + c] = g[q];
   for (int q = 0; q < 3; ++q) vc[(9 + q) * N + c] = ge[q];
   for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) vc[(12 + 3 * i + j) * N + c] = mu * (g[3 * j + i] - (i == j ? (2.0 / 3.0) * tr : 0.0));
+    for (int j = 0; j < 3; ++j) vc[(12 + 3 * i + j) * N + c] = mu * (g[3 * j + i] - (i == j ? (2.0 / 3.0) * tr : Real(0.0)));
   vc[21 * N + c] = mu;
   vc[22 * N + c] = alpha_of(P, mu);
   vc[23 * N + c] = ec;
 }
 
 // fv layout [8][F+B]: lapU(3), divTau(3), divSig, lapE
-__global__ void __launch_bounds__(128) k_visc_face(DevMesh m, const double* __restrict__ vc,
-                                                   const double* __restrict__ W, const double* __restrict__ prim,
-                                                   double* __restrict__ fv, double* __restrict__ sf2, int FB) {
+template <typename Real = double>
+__global__ void __launch_bounds__(128) k_visc_face(DevMesh m, const Real* __restrict__ vc,
+                                                   const Real* __restrict__ W, const Real* __restrict__ prim,
+                                                   Real* __restrict__ fv, double* __restrict__ sf2, int FB) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.F) return;
   const int N = m.N, F = m.F;
   const int o = m.own[f], n = m.nei[f];
   const double wf = m.w[f];
   auto lin = [&](int q) { return wf * (vc[q * N + o] - vc[q * N + n]) + vc[q * N + n]; };
-  const double muf = lin(21), alf = lin(22);
+  const Real muf = lin(21), alf = lin(22);
   const double ms = m.magSf[f];
   const double S[3] = {m.Sf[f], m.Sf[F + f], m.Sf[2 * F + f]};
   const double nodc = m.nodc[f];
   double k[3];
   for (int i = 0; i < 3; ++i) k[i] = m.nf[i * F + f] - m.dCC[i * F + f] * nodc;
-  double gUf[9], tf[9];
+  Real gUf[9], tf[9];
   for (int q = 0; q < 9; ++q) {
     gUf[q] = lin(q);
     tf[q] = lin(12 + q);
   }
-  double Uf[3], snU[3];
+  Real Uf[3], snU[3];
   for (int j = 0; j < 3; ++j) {
-    const double a = prim[(2 + j) * N + o], b = prim[(2 + j) * N + n];
+    const Real a = prim[(2 + j) * N + o], b = prim[(2 + j) * N + n];
     Uf[j] = wf * (a - b) + b;
-    const double corr = k[0] * gUf[j] + k[1] * gUf[3 + j] + k[2] * gUf[6 + j];
+    const Real corr = k[0] * gUf[j] + k[1] * gUf[3 + j] + k[2] * gUf[6 + j];
     snU[j] = nodc * (b - a) + corr;
   }
-  const double ml = muf * ms;
+  const Real ml = muf * ms;
   for (int j = 0; j < 3; ++j) fv[j * FB + f] = ml * snU[j];
   for (int j = 0; j < 3; ++j) fv[(3 + j) * FB + f] = S[0] * tf[j] + S[1] * tf[3 + j] + S[2] * tf[6 + j];
-  double sig[3];
+  Real sig[3];
   for (int i = 0; i < 3; ++i) {
-    double s = 0;
+    Real s = 0;
     for (int j = 0; j < 3; ++j) s += (muf * gUf[3 * i + j] + tf[3 * i + j]) * Uf[j];
     sig[i] = s;
   }
   fv[6 * FB + f] = dot3(sig, S);
-  const double gef[3] = {lin(9), lin(10), lin(11)};
-  const double snE = nodc * (vc[23 * N + n] - vc[23 * N + o]) + dot3(k, gef);
+  const Real gef[3] = {lin(9), lin(10), lin(11)};
+  const Real snE = nodc * (vc[23 * N + n] - vc[23 * N + o]) + dot3(k, gef);
   fv[7 * FB + f] = (alf * ms) * snE;
-  const double rhof = wf * (W[5 * o] - W[5 * n]) + W[5 * n];
-  const double lamv = (muf + alf) / rhof;
-  sf2[f] = 0.5 * lamv * ms * m.dc[f];
+  if constexpr (std::is_same<Real, double>::value) {  // Jacobian coefficient: not part of the tangent
+    const double rhof = wf * (W[5 * o] - W[5 * n]) + W[5 * n];
+    const double lamv = (muf + alf) / rhof;
+    sf2[f] = 0.5 * lamv * ms * m.dc[f];
+  }
 }
 
-__global__ void k_visc_bface(DevMesh m, ViscParams P, const double* __restrict__ vc, const double* __restrict__ prim,
-                             const double* __restrict__ TB, const double* __restrict__ UBv, double* __restrict__ fv,
+template <typename Real = double>
+__global__ void k_visc_bface(DevMesh m, ViscParams P, const Real* __restrict__ vc, const Real* __restrict__ prim,
+                             const double* __restrict__ TB, const double* __restrict__ UBv, Real* __restrict__ fv,
                              int FB) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= m.B) return;
@@ -141,25 +152,25 @@ __global__ void k_visc_bface(DevMesh m, ViscParams P, const double* __restrict__
   const double alB = alpha_of(P, muB);
   const double eB = P.Cv * TB[b];
   const double dcb = m.bdc[b];
-  double snU[3];
+  Real snU[3];
   for (int j = 0; j < 3; ++j) snU[j] = (UB[j] - prim[(2 + j) * N + o]) * dcb;
-  const double snE = (eB - vc[23 * N + o]) * dcb;
-  double g[9];
+  const Real snE = (eB - vc[23 * N + o]) * dcb;
+  Real g[9];
   for (int q = 0; q < 9; ++q) g[q] = vc[q * N + o];
   for (int j = 0; j < 3; ++j) {
-    const double ng = n[0] * vc[j * N + o] + n[1] * vc[(3 + j) * N + o] + n[2] * vc[(6 + j) * N + o];
+    const Real ng = n[0] * vc[j * N + o] + n[1] * vc[(3 + j) * N + o] + n[2] * vc[(6 + j) * N + o];
     for (int i = 0; i < 3; ++i) g[3 * i + j] += n[i] * (snU[j] - ng);
   }
-  const double tr = g[0] + g[4] + g[8];
-  double tb[9];
+  const Real tr = g[0] + g[4] + g[8];
+  Real tb[9];
   for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) tb[3 * i + j] = muB * (g[3 * j + i] - (i == j ? (2.0 / 3.0) * tr : 0.0));
+    for (int j = 0; j < 3; ++j) tb[3 * i + j] = muB * (g[3 * j + i] - (i == j ? (2.0 / 3.0) * tr : Real(0.0)));
   const double ml = muB * ms;
   for (int j = 0; j < 3; ++j) fv[j * FB + F + b] = ml * snU[j];
   for (int j = 0; j < 3; ++j) fv[(3 + j) * FB + F + b] = S[0] * tb[j] + S[1] * tb[3 + j] + S[2] * tb[6 + j];
-  double sig[3];
+  Real sig[3];
   for (int i = 0; i < 3; ++i) {
-    double s = 0;
+    Real s = 0;
     for (int j = 0; j < 3; ++j) s += (muB * g[3 * i + j] + tb[3 * i + j]) * UB[j];
     sig[i] = s;
   }
@@ -188,6 +199,30 @@ void launch_viscous(Handle& h) {
   if (h.m.B)
     ICS_LAUNCH(h, ICS_K_VISC, k_visc_bface<<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, P, h.vcell, h.prim, h.TB,
                                                                                         h.UB, h.fvisc, FB));
+  ICS_CUDA(cudaGetLastError());
+}
+
+// tangent of the viscous face terms for the tangent state (W, prim) in tW, tprim
+void launch_viscous_tangent(Handle& h, const Dual* W, const Dual* prim, Dual* vc, Dual* fv) {
+  ViscParams P;
+  P.R = h.cfg.c.R;
+  P.Cv = h.cfg.Cv;
+  P.Cp = h.cfg.c.Cp;
+  P.gamma = h.cfg.gamma;
+  P.mu = h.cfg.c.mu;
+  P.Pr = h.cfg.c.Pr;
+  P.As = h.cfg.c.As;
+  P.Ts = h.cfg.c.Ts;
+  P.sutherland = h.cfg.c.sutherland;
+  const int FB = h.m.F + h.m.B;
+  ICS_LAUNCH(h, ICS_K_TANGENT, k_visc_cell<Dual><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, P, W, prim, h.TB,
+                                                                                             h.UB, vc));
+  if (h.m.F)
+    ICS_LAUNCH(h, ICS_K_TANGENT, k_visc_face<Dual><<<grid_for(h.m.F, 128), 128, 0, h.stream>>>(h.m, vc, W, prim, fv,
+                                                                                               nullptr, FB));
+  if (h.m.B)
+    ICS_LAUNCH(h, ICS_K_TANGENT, k_visc_bface<Dual><<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, P, vc, prim, h.TB,
+                                                                                                h.UB, fv, FB));
   ICS_CUDA(cudaGetLastError());
 }
 

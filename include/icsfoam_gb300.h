@@ -232,6 +232,30 @@ int ics_begin_time_step(ics_handle h);
  * Rotating-frame (cylindrical) momentum sources are not provided.          */
 #define ICS_MAX_INSTANCES 16
 int ics_set_hb(ics_handle h, int32_t n_instances, const double* D);
+/* ---- differentiation of the residual (no counterpart in the reference,
+ * whose Jacobian is the approximate one of ics_assemble_jacobian) --------- */
+/* Jacobian-vector product of the residual source R V (the vector
+ * ics_residual returns) with respect to the conservative state, at the
+ * current state with the boundary values held fixed: Jv = d(R V)/dW v, by
+ * forward-mode dual numbers through the residual kernels (the exact
+ * derivative of the discrete residual, branch by branch).  v and Jv are
+ * [n_cells][5]; device = 1 when both are device pointers on the handle's
+ * device (inputs ready, outputs written before return), 0 for host arrays. */
+int ics_jvp(ics_handle h, const double* v, double* Jv, int32_t device);
+/* Assemble that exact Jacobian as 5x5 blocks over each cell's stencil (two
+ * face hops, plus the other Harmonic Balance instances of the cell) by
+ * coloured Jacobian-vector products.  Returns the number of blocks and of
+ * colours (products = 5 x colours).  Valid until the state, the boundary
+ * values or the configuration change.                                        */
+int ics_assemble_exact_jacobian(ics_handle h, int64_t* nnz_blocks, int32_t* n_colours);
+/* The assembled exact Jacobian in CSR form (host arrays): row_ptr
+ * [n_cells+1], cols [nnz] increasing within a row, blocks [nnz][5][5] with
+ * blocks[j][i][k] = d(R V)_i of the row cell / d(W_k) of cols[j].  Any
+ * pointer may be NULL.  ICS_ERR_STATE when not assembled at this state.    */
+int ics_get_exact_jacobian(ics_handle h, int32_t* row_ptr, int32_t* cols, double* blocks);
+/* Vector-Jacobian product JTu = (d(R V)/dW)^T u with the exact Jacobian,
+ * assembled first when the state changed.  Pointers as in ics_jvp.         */
+int ics_vjp(ics_handle h, const double* u, double* JTu, int32_t device);
 /* pseudotimeControl::loop() (pseudotimeControl.C:159-241): returns 1 in
  * *more while the pseudo loop should run another iteration.                 */
 int ics_pseudo_loop(ics_handle h, int32_t* more);
@@ -241,7 +265,7 @@ int ics_pseudo_loop(ics_handle h, int32_t* more);
 enum {
   ICS_K_FIELDS = 0, ICS_K_GRAD, ICS_K_FACE, ICS_K_BFACE, ICS_K_CELLRES, ICS_K_JAC_BOUNDARY, ICS_K_JAC_ROWS,
   ICS_K_JACOBI_INV, ICS_K_SPMV, ICS_K_LUSGS_FWD, ICS_K_LUSGS_REV, ICS_K_JACOBI, ICS_K_MGS, ICS_K_VECTOR,
-  ICS_K_SCALAR, ICS_K_UPDATE, ICS_K_BC, ICS_K_BOUND, ICS_K_VISC, ICS_K_COUNT
+  ICS_K_SCALAR, ICS_K_UPDATE, ICS_K_BC, ICS_K_BOUND, ICS_K_VISC, ICS_K_TANGENT, ICS_K_EXACT, ICS_K_COUNT
 };
 /* Start (enable=1) or stop (0) recording a CUDA event pair around every
  * kernel launch on the handle's stream; starting clears previous records.  */

@@ -65,7 +65,7 @@ def build_gpu(force: bool = False, extra_flags=None) -> str:
     if failed:
         raise RuntimeError("nvcc failed on: " + ", ".join(failed))
     tmp = GPU_LIB + ".tmp"
-    subprocess.check_call([NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart_static"])
+    subprocess.check_call([NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart_static", "-lpthread"])
     os.replace(tmp, GPU_LIB)
     return GPU_LIB
 

@@ -142,6 +142,9 @@ _MEASURE = {
 # allocation-free linear residual (CUDA library only; arguments are device pointers)
 _MEASURE["linear_residual_noalloc"] = (C.c_int, [_P, _P, _P, _P])
 
+# independent cases iterated concurrently (CUDA library only)
+_MEASURE["pseudo_iteration_batch"] = (C.c_int, [_P, C.c_int32, _P, _P])
+
 # differentiation of the residual (CUDA library only)
 _MEASURE["jvp"] = (C.c_int, [_P, _P, _P, C.c_int32])
 _MEASURE["vjp"] = (C.c_int, [_P, _P, _P, C.c_int32])
@@ -184,6 +187,27 @@ def _ptr(a: Optional[np.ndarray]):
     if a is None:
         return None
     return a.ctypes.data
+
+
+def pseudo_iteration_batch(handles):
+    """One pseudo iteration on each of several independent handles at once.
+
+    Returns (stats list, status list); raises on the first failing handle.
+    """
+    if not handles:
+        return [], []
+    b = handles[0].b
+    n = len(handles)
+    arr = (C.c_void_p * n)(*[h.h.value for h in handles])
+    stats = (IterStats * n)()
+    status = (C.c_int32 * n)()
+    st = b.fn["pseudo_iteration_batch"](arr, n, stats, status)
+    if st != ICS_OK:
+        bad = [k for k in range(n) if status[k] != ICS_OK]
+        if not bad:  # rejected before any handle ran
+            raise IcsError(st, b.prefix + "pseudo_iteration_batch")
+        handles[bad[0]]._check(status[bad[0]], "pseudo_iteration_batch")
+    return list(stats), list(status)
 
 
 class CaseHandle:

@@ -9,6 +9,8 @@ here is generated from fixed seeds:
                      outlet, slip walls (the transonic circularArcBump layout).
 * ``random_box``   - hex box with randomly displaced interior vertices, cells
                      randomly permuted then reverse-Cuthill-McKee renumbered.
+* ``swept_bump``   - transonic channel over a 30-degree swept 8% bump at
+                     3 degrees incidence (the differentiation workload).
 * ``hb_bump_channel`` - Harmonic Balance version of the bump channel: a
                      time-periodic outlet static pressure, 2H+1 stacked
                      instances and the spectral operator D.
@@ -157,6 +159,50 @@ def random_box(n: int = 200, seed_vertices: int = 0, seed_perm: int = 1, mach: f
                     pseudo_tol=1e-30, pseudo_tol_rel=1e-30,
                     viscous=1, sutherland=1, As=float(As), Ts=Ts, Pr=0.72)
     return Workload("random_box_%d" % n, mesh, np.full(N, p), Uc, np.full(N, T), settings)
+
+
+def swept_bump(nx: int = 240, ny: int = 128, nz: int = 128, thickness: float = 0.08, sweep_deg: float = 30.0,
+               mach: float = 0.84, alpha_deg: float = 3.0, p0: float = 1.0e5, T0: float = 300.0,
+               ordering_mode: str = "colour", flux: str = "HLLC") -> Workload:
+    """Transonic channel over a swept circular-arc bump (the differentiation case).
+
+    The 8% arc spans x in [s, s+1] with s = z tan(sweep), so its crest line is
+    swept by ``sweep_deg`` across the span; the initial flow is uniform at
+    M = 0.84 inclined by ``alpha_deg`` in the x-y plane.
+    """
+    length, height, width = 3.0, 1.0, 1.0
+    xs = np.linspace(-1.0, -1.0 + length, nx + 1)
+    eta = np.linspace(0.0, 1.0, ny + 1)
+    zs = np.linspace(0.0, width, nz + 1)
+    Rb = (0.25 + thickness ** 2) / (2.0 * thickness)
+    shift = zs * np.tan(np.radians(sweep_deg))
+    xl = xs[:, None] - shift[None, :]
+    yb = np.where((xl > 0.0) & (xl < 1.0), np.sqrt(np.maximum(Rb ** 2 - (xl - 0.5) ** 2, 0.0)) - (Rb - thickness), 0.0)
+    g = np.zeros((nx + 1, ny + 1, nz + 1, 3))
+    g[..., 0] = xs[:, None, None]
+    g[..., 1] = yb[:, None, :] + eta[None, :, None] * (height - yb[:, None, :])
+    g[..., 2] = zs[None, None, :]
+    fac = 1.0 + 0.5 * (GAMMA - 1.0) * mach ** 2
+    p_static = p0 / fac ** (GAMMA / (GAMMA - 1.0))
+    T_static = T0 / fac
+    inlet = M.Patch("inlet", M.PATCH_TOTAL_INLET, p0=p0, T0=T0)
+    outlet = M.Patch("outlet", M.PATCH_PRESSURE_OUTLET, p=p_static)
+    wall = M.Patch("walls", M.PATCH_SLIP, is_wall=True)
+    sides = {"xmin": inlet, "xmax": outlet, "ymin": wall, "ymax": wall, "zmin": wall, "zmax": wall}
+    mesh = M.hex_mesh(g, sides)
+    mesh = ordering.apply(mesh, ordering_mode)
+    N = mesh.n_cells
+    c = np.sqrt(GAMMA * R_GAS * T_static)
+    a = np.radians(alpha_deg)
+    U = np.zeros((N, 3))
+    U[:, 0] = mach * c * np.cos(a)
+    U[:, 1] = mach * c * np.sin(a)
+    settings = dict(thermo_settings(), flux_scheme={"AUSMPlusUp": 0, "HLLC": 1, "ROE": 2}[flux],
+                    recon_rho=3, recon_U=3, recon_T=3, ddt_scheme=0, pseudo_co_num=1.0,
+                    pseudo_co_num_max=200.0, n_directions=8, max_iter=5, tolerance=1e-12, rel_tol=1e-2,
+                    pseudo_tol=1e-30, pseudo_tol_rel=1e-30)
+    return Workload("swept_bump_%dx%dx%d" % (nx, ny, nz), mesh, np.full(N, p_static), U, np.full(N, T_static),
+                    settings)
 
 
 def hb_bump_channel(nx: int = 64, ny: int = 16, nz: int = 4, frequency: float = 50.0, harmonics: int = 1,

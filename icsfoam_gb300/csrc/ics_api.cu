@@ -14,7 +14,9 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <atomic>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "ics_internal.cuh"
@@ -27,6 +29,7 @@ struct ics_handle_s {
 
 namespace ics {
 double rho_l2(Handle& h);
+double device_sum(Handle& h, const double* a, int n);
 
 constexpr size_t EV_POOL = 8192;  // events; folded into the totals when full
 
@@ -924,16 +927,36 @@ int ics_pseudo_iteration(ics_handle hh, ics_iter_stats* stats) {
     const int sv = do_solve(h, &s.perf);
     if (sv && sv != ICS_ERR_BREAKDOWN) return sv;
     const int u = do_update(h, &s);
-    std::vector<double> co(h.m.N);
-    ICS_CUDA(cudaMemcpy(co.data(), h.pseudoCo, h.m.N * sizeof(double), cudaMemcpyDeviceToHost));
-    double m = 0;
-    for (double v : co) m += v;
-    s.pseudo_co_mean = m / h.m.N;
+    s.pseudo_co_mean = device_sum(h, h.pseudoCo, h.m.N) / h.m.N;
     s.rho_l2_residual = h.lastRhoL2;
     s.status = sv ? sv : u;
     if (stats) *stats = s;
     return u;
   });
+}
+
+int ics_pseudo_iteration_batch(ics_handle* hs, int32_t n, ics_iter_stats* stats, int32_t* status) {
+  if (!hs || n < 0) return ICS_ERR_ARG;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < i; ++j)
+      if (!hs[i] || hs[i] == hs[j]) return ICS_ERR_ARG;  // one thread per handle: no repeats
+  std::atomic<int> next(0);
+  std::vector<int> st(n, ICS_OK);
+  auto work = [&]() {
+    for (int i = next++; i < n; i = next++) st[i] = ics_pseudo_iteration(hs[i], stats ? &stats[i] : nullptr);
+  };
+  unsigned nt = std::thread::hardware_concurrency();
+  nt = std::max(1u, std::min<unsigned>(nt ? nt : 4, (unsigned)n));
+  std::vector<std::thread> pool;
+  for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work);
+  work();
+  for (auto& t : pool) t.join();
+  int first = ICS_OK;
+  for (int i = 0; i < n; ++i) {
+    if (status) status[i] = st[i];
+    if (first == ICS_OK && st[i] != ICS_OK) first = st[i];
+  }
+  return first;
 }
 
 int ics_begin_time_step(ics_handle hh) {

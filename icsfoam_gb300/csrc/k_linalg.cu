@@ -910,6 +910,15 @@ int gmres_solve(Handle& h, ics_solver_perf* perf, std::vector<double>& initRes) 
   return st;
 }
 
+// sum of a device array (deterministic fixed-order reduction)
+double device_sum(Handle& h, const double* a, int n) {
+  ICS_LAUNCH(h, ICS_K_VECTOR, k_sumsq<<<REDUCE_BLOCKS, RB, 0, h.stream>>>(n, a, h.partials, h.counter, &h.ks->red[8]));
+  double v = 0;
+  ICS_CUDA(cudaMemcpyAsync(&v, &h.ks->red[8], sizeof(double), cudaMemcpyDeviceToHost, h.stream));
+  ICS_CUDA(cudaStreamSynchronize(h.stream));
+  return v;
+}
+
 // rho L2 residual: sqrt(sum (div(phi) V)^2) from the per-cell squares
 double rho_l2(Handle& h) {
   ICS_LAUNCH(h, ICS_K_VECTOR, k_sumsq<<<REDUCE_BLOCKS, RB, 0, h.stream>>>(h.m.N, h.scratch, h.partials, h.counter, &h.ks->l2));

@@ -217,6 +217,14 @@ int ics_solve_increment(ics_handle h, ics_solver_perf* perf, double* dW);
 int ics_update_fields(ics_handle h, ics_iter_stats* stats);
 /* One pseudo-time iteration: outerLoop.H:1-99 then updateFields.H.          */
 int ics_pseudo_iteration(ics_handle h, ics_iter_stats* stats);
+/* One pseudo-time iteration on each of n independent handles at once (a
+ * batch of small cases): host threads drive the handles, whose kernels
+ * overlap on their own streams; each handle keeps its own Krylov space and
+ * controls, so every result equals that of ics_pseudo_iteration.  status[i]
+ * (optional) receives each handle's status; the return value is the first
+ * non-OK one.  The handles must be distinct.  (The reference runs such cases
+ * one after another.)                                                        */
+int ics_pseudo_iteration_batch(ics_handle* handles, int32_t n, ics_iter_stats* stats, int32_t* status);
 /* Start a physical time step: shift old time levels, beginTimeStep.H:1-45.  */
 int ics_begin_time_step(ics_handle h);
 /* Harmonic Balance (dbnsFullyImplicitHBFoam outerLoop.H:1-230, HBZone.C:359-519):

@@ -134,3 +134,36 @@ def test_exact_jacobian_invalidated_by_state_change(gpu_binding):
     u = np.random.default_rng(3).standard_normal(W.shape)
     v = direction(W, 4)
     assert abs(np.sum(u * h.jvp(v)) - np.sum(h.vjp(u) * v)) < 1e-10 * np.abs(u * h.jvp(v)).sum()
+
+
+def test_swept_bump_32_directions(gpu_binding, oracle_binding):
+    """The differentiation workload (30-degree swept 8% bump, M 0.84, 3 degrees
+    incidence, HLLC + MUSCL/Venkatakrishnan) at a small size: JVP along 32
+    seeded directions against the oracle's central differences."""
+    w = perturb(cases.swept_bump(12, 6, 4))
+    hg, ho = open_case(gpu_binding, w), open_case(oracle_binding, w)
+    W = hg.get_state()["W"]
+    worst = 0.0
+    for s in range(32):
+        v = direction(W, 100 + s)
+        worst = max(worst, relerr(hg.jvp(v), fd_jvp(ho, W, v)))
+    assert worst < 1e-5
+
+
+def test_torch_autograd_backward_is_the_exact_vjp(gpu_binding):
+    import torch
+
+    from icsfoam_gb300 import autograd
+
+    w = perturb(WORKLOADS["bump_hllc_muscl"]())
+    h = open_case(gpu_binding, w)
+    W0 = h.get_state()["W"]
+    W = torch.tensor(W0, device="cuda", requires_grad=True)
+    g = torch.randn(W.shape, dtype=torch.float64, device="cuda", generator=torch.Generator("cuda").manual_seed(0))
+    R = autograd.residual(h, W)
+    assert relerr(R.detach().cpu().numpy(), h.residual()) < 1e-14
+    (R * g).sum().backward()
+    expect = h.vjp(g.cpu().numpy())
+    assert relerr(W.grad.cpu().numpy(), expect) < 1e-13
+    v = torch.tensor(direction(W0, 3), device="cuda")
+    assert relerr(autograd.jvp(h, W.detach(), v).cpu().numpy(), h.jvp(v.cpu().numpy())) < 1e-13

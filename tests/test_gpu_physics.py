@@ -137,3 +137,23 @@ def test_profiling_counts_launches(gpu_binding):
     assert n == sum(v[1] for v in prof.values())
     assert prof["face"][1] == 1 and prof["spmv"][1] >= 2
     assert all(v[0] >= 0 for v in prof.values())
+
+
+def test_batch_of_independent_cases_equals_sequential_runs(gpu_binding):
+    """ics_pseudo_iteration_batch: concurrent handles give bit-identical results."""
+    ws = [cases.bump_channel(6 + 2 * k, 4, 2 + k % 2, ordering_mode="colour") for k in range(5)]
+    ws.append(cases.shock_tube(50))
+    seq = [open_case(gpu_binding, w) for w in ws]
+    bat = [open_case(gpu_binding, w) for w in ws]
+    for _ in range(4):
+        for h in seq:
+            h.pseudo_loop()
+            h.pseudo_iteration()
+        for h in bat:
+            h.pseudo_loop()
+        stats, status = abi.pseudo_iteration_batch(bat)
+        assert status == [abi.ICS_OK] * len(ws)
+    for a, b in zip(seq, bat):
+        assert np.array_equal(a.get_state()["W"], b.get_state()["W"])
+    with pytest.raises(abi.IcsError):
+        abi.pseudo_iteration_batch([bat[0], bat[0]])

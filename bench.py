@@ -157,8 +157,11 @@ def kernel_bytes(kind, N, F, B, nslots, mixed, nlev):
         return (112 + 50 * pb) * F + (25 * pb + 16 + pb) * N
     if kind == "spmv":
         return 25 * pb * N + 50 * pb * F + 8 * F + 10 * pv * N
-    if kind in ("lusgs_fwd", "lusgs_rev"):  # one level; sweep total split evenly over levels
-        return (25 * pb * F + pb * N + 10 * pv * N + 4 * F) / max(1, nlev)
+    if kind in ("lusgs_fwd", "lusgs_rev"):
+        # colour-blocked 2-level schedule: one launch per sweep (forward level 0 has no lower
+        # neighbours; the last forward level is fused with the first reverse one), reading all F
+        # blocks of its triangle, rD and r of its N/2 rows, the neighbours' deltas, writing deltas
+        return 25 * pb * F + pb * N / 2 + 3 * 5 * pv * N / 2 + 4 * F
     if kind == "mgs":
         return 20 * pv * N
     return None

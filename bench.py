@@ -162,6 +162,10 @@ def kernel_bytes(kind, N, F, B, nslots, mixed, nlev):
         # neighbours; the last forward level is fused with the first reverse one), reading all F
         # blocks of its triangle, rD and r of its N/2 rows, the neighbours' deltas, writing deltas
         return 25 * pb * F + pb * N / 2 + 3 * 5 * pv * N / 2 + 4 * F
+    if kind == "op0":   # fused operator, pass 1: (A x) on the level-0 half of the rows
+        return 25 * pb * N / 2 + 25 * pb * F + 5 * pv * N + 5 * pv * N / 2 + 4 * F
+    if kind == "op1":   # pass 2: (A x) + forward sweep + first reverse on the other half
+        return 25 * pb * N / 2 + 25 * pb * F + 10 * pv * N + pb * N + 4 * F
     if kind == "mgs":
         return 20 * pv * N
     return None

@@ -153,7 +153,7 @@ _MEASURE["get_exact_jacobian"] = (C.c_int, [_P, _P, _P, _P])
 
 KERNEL_CLASSES = ("fields", "grad", "face", "bface", "cellres", "jac_boundary", "jac_rows", "jacobi_inv", "spmv",
                   "lusgs_fwd", "lusgs_rev", "jacobi", "mgs", "vector", "scalar", "update", "bc", "bound", "visc",
-                  "tangent", "exact")
+                  "tangent", "exact", "op0", "op1")
 
 EXPORTED = tuple(_FUNCS) + tuple(_MEASURE)
 

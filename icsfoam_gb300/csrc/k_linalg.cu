@@ -165,6 +165,131 @@ __global__ void __launch_bounds__(128) k_spmv(DevMesh m, const TB* __restrict__ 
   for (int k = 0; k < 5; ++k) y[5 * c + k] = acc[k];
 }
 
+// ------------------------------------- fused A x + LU-SGS (two-level schedule)
+// On a schedule of two levels where the first holds the rows without lower
+// neighbours and the second the rows without upper neighbours (the
+// colour-blocked numbering of a bipartite mesh), z = M^-1 A x takes three
+// passes instead of SpMV + two sweeps, and the second-level rows read their
+// (lower) blocks once for both the product and the forward sweep:
+//   pass 1 (level-0 rows): w = (A x)_c
+//   pass 2 (level-1 rows): y = (A x)_c; r' = y - sum_lower L (rD w)_j;
+//                          w_c = rD_c r'   (forward + fused first reverse)
+//   pass 3 (level-0 rows): the reverse sweep, as k_lusgs_level MODE 1.
+// Same arithmetic as the separate kernels up to the order of the sums.
+template <typename TB, typename TV>
+__global__ void __launch_bounds__(128) k_op_level0(DevMesh m, const TB* __restrict__ blk, const TB* __restrict__ dg,
+                                                   const TV* __restrict__ x, TV* __restrict__ w,
+                                                   const int* __restrict__ cells, int start, int count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const int c = cells ? cells[start + i] : start + i;
+  const int s = c >> 5, lane = c & 31;
+  TV xc[5], acc[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) xc[k] = x[5 * c + k];
+  const TB* D = dg + (size_t)s * 25 * 32 + lane;
+#pragma unroll
+  for (int r = 0; r < 5; ++r) {
+    TV a = TV(0);
+#pragma unroll
+    for (int j = 0; j < 5; ++j) a += TV(D[(5 * r + j) * 32]) * xc[j];
+    acc[r] = a;
+  }
+  const int base = m.slot_base[s];
+  const int ns = m.nslot[c];
+  for (int t = 0; t < ns; ++t) {
+    const int col = m.scol[(base + t) * 32 + lane];
+    TV xj[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) xj[k] = x[5 * col + k];
+    const TB* Bk = blk + (size_t)(base + t) * 25 * 32 + lane;
+#pragma unroll
+    for (int r = 0; r < 5; ++r) {
+      TV a = TV(0);
+#pragma unroll
+      for (int j = 0; j < 5; ++j) a += TV(Bk[(5 * r + j) * 32]) * xj[j];
+      acc[r] += a;
+    }
+  }
+  if (m.nInst > 1) {
+    const int J = c / m.Nc, cl = c - J * m.Nc;
+    const double Vc = m.V[c];
+    for (int K = 0; K < m.nInst; ++K) {
+      if (K == J) continue;
+      const TV d = TV(Vc * m.Dhb[J * m.nInst + K]);
+      const TV* xk = x + 5 * ((size_t)K * m.Nc + cl);
+#pragma unroll
+      for (int k = 0; k < 5; ++k) acc[k] += d * xk[k];
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) w[5 * c + k] = acc[k];
+}
+
+template <typename TB, typename TV>
+__global__ void __launch_bounds__(128) k_op_level1(DevMesh m, const TB* __restrict__ blk, const TB* __restrict__ dg,
+                                                   const TB* __restrict__ rD, const TV* __restrict__ x,
+                                                   TV* __restrict__ w, const int* __restrict__ cells, int start,
+                                                   int count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const int c = cells ? cells[start + i] : start + i;
+  const int s = c >> 5, lane = c & 31;
+  TV xc[5], acc[5], fw[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    xc[k] = x[5 * c + k];
+    fw[k] = TV(0);
+  }
+  const TB* D = dg + (size_t)s * 25 * 32 + lane;
+#pragma unroll
+  for (int r = 0; r < 5; ++r) {
+    TV a = TV(0);
+#pragma unroll
+    for (int j = 0; j < 5; ++j) a += TV(D[(5 * r + j) * 32]) * xc[j];
+    acc[r] = a;
+  }
+  const int base = m.slot_base[s];
+  const int ns = m.nslot[c];  // all lower: these rows have no upper neighbours
+  for (int t = 0; t < ns; ++t) {
+    const int col = m.scol[(base + t) * 32 + lane];
+    const TV rj = TV(rD[col]);
+    TV xj[5], dj[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      xj[k] = x[5 * col + k];
+      dj[k] = rj * w[5 * col + k];
+    }
+    const TB* Bk = blk + (size_t)(base + t) * 25 * 32 + lane;
+#pragma unroll
+    for (int r = 0; r < 5; ++r) {
+      TV a = TV(0), b = TV(0);
+#pragma unroll
+      for (int j = 0; j < 5; ++j) {
+        const TV e = TV(Bk[(5 * r + j) * 32]);
+        a += e * xj[j];
+        b += e * dj[j];
+      }
+      acc[r] += a;
+      fw[r] += b;
+    }
+  }
+  if (m.nInst > 1) {
+    const int J = c / m.Nc, cl = c - J * m.Nc;
+    const double Vc = m.V[c];
+    for (int K = 0; K < m.nInst; ++K) {
+      if (K == J) continue;
+      const TV d = TV(Vc * m.Dhb[J * m.nInst + K]);
+      const TV* xk = x + 5 * ((size_t)K * m.Nc + cl);
+#pragma unroll
+      for (int k = 0; k < 5; ++k) acc[k] += d * xk[k];
+    }
+  }
+  const TV rc = TV(rD[c]);
+#pragma unroll
+  for (int k = 0; k < 5; ++k) w[5 * c + k] = rc * (acc[k] - fw[k]);
+}
+
 // ------------------------------------------------------------------ LU-SGS
 // SCALE: also apply the reverse step of a row without upper neighbours
 // (delta = rD * r'), fusing the last forward level with the first reverse one.
@@ -601,6 +726,43 @@ static void lusgs_t(Handle& h, TV* r) {
   }
 }
 
+// w = M^-1 A x with M the LU-SGS preconditioner; true when the fused
+// three-pass form applies (two levels, the second without upper neighbours,
+// level launches rather than the single-CTA walk)
+template <typename TB, typename TV>
+static bool fused_op_t(Handle& h, const TV* x, TV* w) {
+  const DevMesh& m = h.m;
+  if (h.cfg.c.preconditioner != ICS_PC_LUSGS || m.nfl != 2 || m.nrl != 2 || !m.fuse_last) return false;
+  if ((long)m.N < 2048L * m.nfl) return false;
+  const TB* blk = (const TB*)h.blk;
+  const TB* dg = (const TB*)h.dg;
+  const TB* rD = (const TB*)h.rD;
+  auto level = [&](int l, const int** cells, int* start, int* cnt) {
+    const int a = m.fl_ptr[l];
+    *cnt = m.fl_ptr[l + 1] - a;
+    const bool contig = m.fl_cstart[l] >= 0;
+    *cells = contig ? nullptr : m.fl_cells;
+    *start = contig ? m.fl_cstart[l] : a;
+  };
+  const int* c0;
+  const int* c1;
+  int s0, n0, s1, n1;
+  level(0, &c0, &s0, &n0);
+  level(1, &c1, &s1, &n1);
+  if (n0)
+    ICS_LAUNCH(h, ICS_K_OP0, k_op_level0<TB, TV><<<grid_for(n0, 128), 128, 0, h.stream>>>(m, blk, dg, x, w, c0, s0, n0));
+  if (n1)
+    ICS_LAUNCH(h, ICS_K_OP1,
+               k_op_level1<TB, TV><<<grid_for(n1, 128), 128, 0, h.stream>>>(m, blk, dg, rD, x, w, c1, s1, n1));
+  // reverse level 1 = forward level 0 rows
+  const int a = m.rl_ptr[1], cnt = m.rl_ptr[2] - a;
+  const bool contig = m.rl_cstart[1] >= 0;
+  if (cnt)
+    ICS_LAUNCH(h, ICS_K_LUSGS_REV, k_lusgs_level<TB, TV, 1><<<grid_for(cnt, 128), 128, 0, h.stream>>>(
+                                       m, blk, rD, w, contig ? nullptr : m.rl_cells, contig ? m.rl_cstart[1] : a, cnt));
+  return true;
+}
+
 template <typename TB, typename TV>
 static void precondition_t(Handle& h, TV* r) {
   if (h.cfg.c.preconditioner == ICS_PC_LUSGS)
@@ -825,8 +987,10 @@ static int gmres_t(Handle& h, ResIO& p) {
     for (int i = 0; i < m; ++i) {
       TV* vi = V + (size_t)i * vs;
       ICS_LAUNCH(h, ICS_K_VECTOR, k_scale<TV><<<REDUCE_BLOCKS, RB, 0, st>>>(n5, w, vi, ks));
-      spmv_t<TB, TV>(h, vi, w);
-      precondition_t<TB, TV>(h, w);
+      if (!fused_op_t<TB, TV>(h, vi, w)) {
+        spmv_t<TB, TV>(h, vi, w);
+        precondition_t<TB, TV>(h, w);
+      }
       for (int j = 0; j <= i; ++j) {
         const TV* vprev = j > 0 ? V + (size_t)(j - 1) * vs : nullptr;
         const double* hprev = j > 0 ? &ks->H[(j - 1) * m + i] : nullptr;

@@ -273,7 +273,8 @@ int ics_pseudo_loop(ics_handle h, int32_t* more);
 enum {
   ICS_K_FIELDS = 0, ICS_K_GRAD, ICS_K_FACE, ICS_K_BFACE, ICS_K_CELLRES, ICS_K_JAC_BOUNDARY, ICS_K_JAC_ROWS,
   ICS_K_JACOBI_INV, ICS_K_SPMV, ICS_K_LUSGS_FWD, ICS_K_LUSGS_REV, ICS_K_JACOBI, ICS_K_MGS, ICS_K_VECTOR,
-  ICS_K_SCALAR, ICS_K_UPDATE, ICS_K_BC, ICS_K_BOUND, ICS_K_VISC, ICS_K_TANGENT, ICS_K_EXACT, ICS_K_COUNT
+  ICS_K_SCALAR, ICS_K_UPDATE, ICS_K_BC, ICS_K_BOUND, ICS_K_VISC, ICS_K_TANGENT, ICS_K_EXACT, ICS_K_OP0,
+  ICS_K_OP1, ICS_K_COUNT
 };
 /* Start (enable=1) or stop (0) recording a CUDA event pair around every
  * kernel launch on the handle's stream; starting clears previous records.  */

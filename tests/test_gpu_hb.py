@@ -87,3 +87,20 @@ def test_hb_rejects_noalloc_entry(gpu_binding, hbcase):
     r = torch.zeros_like(x)
     l1 = torch.zeros(5, dtype=torch.float64, device="cuda")
     assert h.linear_residual_noalloc(x.data_ptr(), r.data_ptr(), l1.data_ptr()) == abi.ICS_ERR_ARG
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-10), (1, 5e-3)])
+def test_hb_solve_with_fused_operator(gpu_binding, oracle_binding, precision, tol):
+    """6,144 cells on the two-level colour schedule: the GMRES cycle applies
+    M^-1 A in the fused three-pass form (with the instance couplings)."""
+    w = cases.hb_bump_channel(32, 16, 4, amplitude=0.1)
+    hg = open_case(gpu_binding, w, precision=precision)
+    ho = open_case(oracle_binding, w)
+    for h in (hg, ho):
+        h.residual()
+        h.assemble_jacobian()
+    pg, dg, _ = hg.solve_increment()
+    po, do, _ = ho.solve_increment()
+    if precision == 0:
+        assert pg.n_iterations == po.n_iterations
+    assert relerr(dg, do) < tol

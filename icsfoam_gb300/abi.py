@@ -305,6 +305,13 @@ class CaseHandle:
         self._check(self.b.fn["get_state"](self.h, _ptr(W), _ptr(p), _ptr(U), _ptr(T)), "get_state")
         return {"W": W, "p": p, "U": U, "T": T}
 
+    def get_conservative(self, out: np.ndarray) -> np.ndarray:
+        """Copy the conservative state into ``out`` ([N, 5] float64, C-contiguous, e.g. pinned)."""
+        if out.shape != (self.N, 5) or out.dtype != np.float64 or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float64 [N, 5] array")
+        self._check(self.b.fn["get_state"](self.h, _ptr(out), None, None, None), "get_state")
+        return out
+
     def get_boundary_state(self):
         p = np.empty(self.B)
         U = np.empty((self.B, 3))

@@ -114,12 +114,13 @@ __device__ __forceinline__ void flux_hllc(const FStateT<Real>& L, const FStateT<
   const double coefSm = pos0d(Sm);
   const double coefSlm = (1.0 - coefSl) * coefSm;
   const double coefSmr = (1.0 - coefSm) * (1.0 - coefSr);
-  const Real fluxRhoStar_l = Sm / (Sl - Sm) * ((Sl - uMag_l) * rl);
-  const Real fluxRhoStar_r = Sm / (Sr - Sm) * ((Sr - uMag_r) * rr);
+  // one reciprocal per wave pair, shared by the mass, momentum and energy star fluxes
+  const Real il = 1.0 / (Sl - Sm), ir = 1.0 / (Sr - Sm);
+  const Real fluxRhoStar_l = Sm * il * ((Sl - uMag_l) * rl);
+  const Real fluxRhoStar_r = Sm * ir * ((Sr - uMag_r) * rr);
   out[0] = (coefSl * rl * uMag_l + coefSlm * fluxRhoStar_l + coefSmr * fluxRhoStar_r + coefSr * rr * uMag_r) * magS;
   const Real pStar_l = rl * (uMag_l - Sl) * (uMag_l - Sm) + pl;
   const Real pStar_r = rr * (uMag_r - Sr) * (uMag_r - Sm) + pr;
-  const Real il = 1.0 / (Sl - Sm), ir = 1.0 / (Sr - Sm);
   for (int k = 0; k < 3; ++k) {
     const Real rusl = il * ((Sl - uMag_l) * rl * L.U[k] + (pStar_l - pl) * n[k]);
     const Real rusr = ir * ((Sr - uMag_r) * rr * R.U[k] + (pStar_r - pr) * n[k]);

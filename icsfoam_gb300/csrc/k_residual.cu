@@ -211,12 +211,33 @@ __global__ void __launch_bounds__(128) k_grad(DevMesh m, const Real* __restrict_
 #pragma unroll
     for (int k = 0; k < NQ; ++k) {
       if (!((mask >> k) & 1) || !anyFace) continue;
-      Real r = VGREAT;
-      if (epos[k] > 0.0) r = fmin(r, qmax[k] / epos[k]);
-      if (eneg[k] < 0.0) r = fmin(r, qmin[k] / eneg[k]);
-      if ((small >> k) & 1) r = fmin(r, 1.0);
-      const Real lr = LIMITED == 2 ? (r * r + 2 * r) / (r * r + r + 2) : fmin(r, 1.0);
-      const Real lim = r >= VGREAT ? Real(1.0) : fmin(1.0, lr);
+      // r = ra / rb (rb > 0): the smaller of maxD/e+ and minD/e- found by
+      // cross-multiplication, then one division for the limiter itself
+      bool have = false;
+      Real ra = 1.0, rb = 1.0;
+      if (epos[k] > 0.0) {
+        ra = qmax[k];
+        rb = epos[k];
+        have = true;
+      }
+      if (eneg[k] < 0.0) {
+        const Real a2 = -qmin[k], b2 = -eneg[k];
+        if (!have || a2 * rb < ra * b2) {
+          ra = a2;
+          rb = b2;
+        }
+        have = true;
+      }
+      if ((small >> k) & 1) {
+        if (!have || ra > rb) {
+          ra = 1.0;
+          rb = 1.0;
+        }
+        have = true;
+      }
+      // Venkatakrishnan (r^2 + 2r)/(r^2 + r + 2) and minmod min(r, 1), capped at 1
+      const Real lr = LIMITED == 2 ? (ra * ra + 2 * ra * rb) / (ra * ra + ra * rb + 2 * rb * rb) : ra / rb;
+      const Real lim = !have ? Real(1.0) : fmin(1.0, lr);
       g[k][0] = g[k][0] * lim;
       g[k][1] = g[k][1] * lim;
       g[k][2] = g[k][2] * lim;

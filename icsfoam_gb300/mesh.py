@@ -119,14 +119,25 @@ class Mesh:
 # Geometry (restated from OpenFOAM primitiveMesh / surfaceInterpolation)
 # --------------------------------------------------------------------------
 
-def face_centres_and_areas(points: np.ndarray, fp: np.ndarray) -> Tuple[np.ndarray, np.ndarray]:
-    """Face centres and area vectors of quads by triangle decomposition.
+def face_centres_and_areas(points: np.ndarray, fp) -> Tuple[np.ndarray, np.ndarray]:
+    """Face centres and area vectors by triangle decomposition.
 
     Each polygon is split into triangles about its average point; the area
     vector is half the sum of the triangle normals and the centre is the
-    area-weighted mean of the triangle centroids.
+    area-weighted mean of the triangle centroids.  ``fp`` is an (n, k) array
+    of point labels, or an object array of label arrays of mixed sizes.
     """
-    P = points[fp]                       # (nF, 4, 3)
+    if fp.dtype == object:
+        Cf = np.zeros((len(fp), 3))
+        Sf = np.zeros((len(fp), 3))
+        sizes = np.array([len(f) for f in fp])
+        for k in np.unique(sizes):
+            idx = np.nonzero(sizes == k)[0]
+            c, s = face_centres_and_areas(points, np.stack([fp[i] for i in idx]).astype(np.int64))
+            Cf[idx] = c
+            Sf[idx] = s
+        return Cf, Sf
+    P = points[fp]                       # (nF, k, 3)
     fc = P.mean(axis=1)                  # average point
     sumN = np.zeros_like(fc)
     sumA = np.zeros(fc.shape[0])
@@ -368,7 +379,11 @@ def renumber(mesh: Mesh, new_to_old: np.ndarray) -> Mesh:
     nei = old_to_new[mesh.neighbour.astype(np.int64)]
     fp = mesh.face_points.copy()
     flip = own > nei
-    fp[flip] = fp[flip][:, ::-1]
+    if fp.dtype == object:
+        for i in np.nonzero(flip)[0]:
+            fp[i] = fp[i][::-1]
+    else:
+        fp[flip] = fp[flip][:, ::-1]
     o2 = np.where(flip, nei, own)
     n2 = np.where(flip, own, nei)
     entries = []

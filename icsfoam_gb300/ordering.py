@@ -60,6 +60,20 @@ def colour_blocked(mesh: M.Mesh) -> np.ndarray:
     return np.lexsort((np.arange(mesh.n_cells), col)).astype(np.int64)
 
 
+def permutation(mesh: M.Mesh, mode: str) -> np.ndarray:
+    """new_to_old cell permutation of an ordering mode (identity for natural)."""
+    if mode == "natural":
+        return np.arange(mesh.n_cells)
+    if mode == "rcm":
+        return rcm(mesh)
+    if mode == "colour":
+        return colour_blocked(mesh)
+    if mode == "rcm+colour":
+        p1 = rcm(mesh)
+        return p1[colour_blocked(M.renumber(mesh, p1))]
+    raise ValueError("unknown ordering " + mode)
+
+
 def apply(mesh: M.Mesh, mode: str) -> M.Mesh:
     if mode == "natural":
         return mesh

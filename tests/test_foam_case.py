@@ -139,7 +139,7 @@ def test_reads_a_reference_tutorial_case(oracle_binding):
 @pytest.mark.gpu
 def test_case_read_from_disk_runs_on_the_gpu(tmp_path, gpu_binding, oracle_binding):
     """A case written to disk and read back: GPU and oracle agree on it."""
-    w = cases.bump_channel(16, 8, 4, ordering_mode="natural")
+    w = cases.bump_channel(24, 8, 4, ordering_mode="natural")
     foam_case.write_case(str(tmp_path), w.mesh, w.p, w.U, w.T)
     write_dicts(str(tmp_path))
     mesh, fields, settings, _ = foam_case.load_case(str(tmp_path), ordering_mode="colour")

@@ -14,6 +14,8 @@ Restates (host side, tiny dense linear algebra):
 * ``hb_operator``     HBZone::updateHBOperators (HBZone.C:270-356):
   E^-1_nk = exp(i omega_k t_n), E = pinv(E^-1), A = diag(omega),
   D = -(Im(E^-1) A Re(E) + Re(E^-1) A Im(E)).
+* ``reconstruct``     HBZone::reconstruct (HBZoneTemplates.C:327-405): the
+  time history at any t from the instance snapshots (reconstructHBFoam).
 
 The instances become one stacked mesh (``stack_instances``): instance J owns
 cells [J N, (J+1) N) and its own copy of every patch, so time-varying inlet
@@ -87,6 +89,22 @@ def hb_operator(omegas: np.ndarray, instants: np.ndarray) -> np.ndarray:
     A = np.diag(omegas)
     D = -(E1.imag @ A @ E.real + E1.real @ A @ E.imag)
     return np.ascontiguousarray(D)
+
+
+def reconstruction_weights(omegas: np.ndarray, instants: np.ndarray, t: float) -> np.ndarray:
+    """Weights w_J with f(t) = sum_J w_J f(t_J) for fields band-limited to the
+    omega list (HBZone::reconstruct, HBZoneTemplates.C:327-405):
+    w = Re(E^-1(t) E) with E^-1(t)_k = exp(i omega_k t) and E = pinv(E^-1)."""
+    E = np.linalg.pinv(e_inverse(omegas, instants))
+    e1 = np.exp(1j * omegas * t)
+    return (e1 @ E).real
+
+
+def reconstruct(omegas: np.ndarray, instants: np.ndarray, fields: np.ndarray, t: float) -> np.ndarray:
+    """A field at time t from its n instance snapshots ``fields`` [n, ...]
+    (the reconstructHBFoam post-processing step, one time value)."""
+    w = reconstruction_weights(omegas, instants, t)
+    return np.tensordot(w, np.asarray(fields), axes=(0, 0))
 
 
 def stack_instances(mesh: M.Mesh, n: int, patch_for: Callable[[M.Patch, int], M.Patch] = None) -> M.Mesh:

@@ -150,3 +150,22 @@ def test_errors(oracle_binding):
     assert e.value.status == abi.ICS_ERR_ARG
     with pytest.raises(abi.IcsError):
         h.set_hb(17, np.zeros((17, 17)))
+
+
+@pytest.mark.parametrize("H,selected", [(1, True), (2, False)])
+def test_reconstruction_recovers_band_limited_history(H, selected):
+    """reconstructHBFoam: the snapshots of a band-limited history give it back at any time."""
+    w0 = 2 * np.pi * 3.0
+    om = HB.omega_list([w0], [H])
+    t = HB.select_instants(om, 2 * H + 1, 2 * np.pi / w0 if selected else None)
+    rng = np.random.default_rng(5)
+    a, b = rng.standard_normal((H + 1, 4)), rng.standard_normal((H + 1, 4))
+
+    def f(tt):
+        return a[0] + sum(a[k] * np.cos(k * w0 * tt) + b[k] * np.sin(k * w0 * tt) for k in range(1, H + 1))
+
+    snaps = np.stack([f(tj) for tj in t])
+    for tt in (0.0137, 0.2, 1.7):
+        assert np.allclose(HB.reconstruct(om, t, snaps, tt), f(tt), atol=1e-10)
+    # at an instant the weights select that snapshot
+    assert np.allclose(HB.reconstruction_weights(om, t, t[1]), np.eye(2 * H + 1)[1], atol=1e-10)

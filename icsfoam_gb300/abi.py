@@ -128,6 +128,9 @@ _FUNCS = {
     "begin_time_step": (C.c_int, [_P]),
     "pseudo_loop": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "set_hb": (C.c_int, [_P, C.c_int32, _P]),
+    "scalar_enable": (C.c_int, [_P, _P, _P, _P, C.c_double, C.c_int32]),
+    "scalar_transport": (C.c_int, [_P, C.c_int32, C.POINTER(SolverPerf)]),
+    "get_scalar": (C.c_int, [_P, _P, _P]),
 }
 
 # measurement entry points (CUDA library only)
@@ -153,7 +156,7 @@ _MEASURE["get_exact_jacobian"] = (C.c_int, [_P, _P, _P, _P])
 
 KERNEL_CLASSES = ("fields", "grad", "face", "bface", "cellres", "jac_boundary", "jac_rows", "jacobi_inv", "spmv",
                   "lusgs_fwd", "lusgs_rev", "jacobi", "mgs", "vector", "scalar", "update", "bc", "bound", "visc",
-                  "tangent", "exact", "op0", "op1")
+                  "tangent", "exact", "op0", "op1", "passive")
 
 EXPORTED = tuple(_FUNCS) + tuple(_MEASURE)
 
@@ -423,6 +426,26 @@ class CaseHandle:
         ms = C.c_double()
         self._check(self.b.fn["timer_stop"](self.h, C.byref(ms)), "timer_stop")
         return float(ms.value)
+
+    # ------------------------------------------------------ passive scalar
+    def scalar_enable(self, s, patch_fixed=None, patch_value=None, D=0.0, recon=0):
+        s = np.ascontiguousarray(np.broadcast_to(s, (self.N,)), np.float64)
+        P = len(self.mesh.patches)
+        pf = np.ascontiguousarray(np.zeros(P) if patch_fixed is None else patch_fixed, np.int32)
+        pv = np.ascontiguousarray(np.zeros(P) if patch_value is None else patch_value, np.float64)
+        self._check(self.b.fn["scalar_enable"](self.h, _ptr(s), _ptr(pf), _ptr(pv), float(D), int(recon)),
+                    "scalar_enable")
+
+    def scalar_transport(self, n_iterations=1):
+        perf = SolverPerf()
+        self._check(self.b.fn["scalar_transport"](self.h, int(n_iterations), C.byref(perf)), "scalar_transport")
+        return perf
+
+    def get_scalar(self):
+        s = np.empty(self.N)
+        rs = np.empty(self.N)
+        self._check(self.b.fn["get_scalar"](self.h, _ptr(s), _ptr(rs)), "get_scalar")
+        return s, rs
 
     # ------------------------------------------------------ differentiation
     def jvp(self, v: np.ndarray) -> np.ndarray:

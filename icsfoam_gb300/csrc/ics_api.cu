@@ -97,6 +97,8 @@ void free_all(Handle& h) {
                   m.rl_lptr, h.W, h.W0, h.W00, h.Wprev, h.prim, h.pB, h.TB, h.UB, h.phiB, h.pseudoCo, h.rPDT,
                   h.ddtCoeff, h.q, h.bq, h.clin, h.grad, h.fflux, h.frec, h.flam, h.bjac, h.src, h.vcell,
                   h.fvisc, h.vsf2, m.dc, m.Dhb, h.tW, h.tprim, h.tq, h.tgrad, h.tflux, h.tvc, h.tfv, h.tv,
+                  h.ss, h.ssB, h.srhoS, h.srhoS0, h.srhoS00, h.sgrad, h.sgradL, h.sface, h.sblk, h.sdg, h.srD,
+                  h.ssrc, h.sFixed, h.sValue,
                   h.blk, h.dg,
                   h.dginv, h.rD, h.kv, h.kw, h.kx, h.kb, h.kt, h.dW, h.partials, h.counter, h.ks, h.scratch,
                   h.ibuf};
@@ -970,6 +972,12 @@ int ics_begin_time_step(ics_handle hh) {
       ICS_CUDA(cudaMemcpyAsync(h.W00, h.W0, n5 * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
       ICS_CUDA(cudaMemcpyAsync(h.W0, h.W, n5 * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
     }
+    if (h.scalarOn) {
+      const size_t N = h.m.N;
+      ICS_CUDA(cudaMemcpyAsync(h.srhoS00, h.timeIndex == 0 ? h.srhoS : h.srhoS0, N * sizeof(double),
+                               cudaMemcpyDeviceToDevice, h.stream));
+      ICS_CUDA(cudaMemcpyAsync(h.srhoS0, h.srhoS, N * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
+    }
     h.timeIndex++;
     h.haveExact = false;
     if (!steady) {
@@ -1042,6 +1050,107 @@ int ics_timer_stop(ics_handle hh, double* ms) {
     float t = 0;
     ICS_CUDA(cudaEventElapsedTime(&t, h.tStart, h.tStop));
     *ms = t;
+    return ICS_OK;
+  });
+}
+
+// passive scalar transport ---------------------------------------------------
+__global__ void k_scalar_init(int N, const double* __restrict__ s, const double* __restrict__ W,
+                              double* __restrict__ rhoS) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < N) rhoS[c] = W[5 * c] * s[c];
+}
+
+int ics_scalar_enable(ics_handle hh, const double* s, const int32_t* patch_fixed, const double* patch_value,
+                      double D, int32_t recon) {
+  if (!hh || !s || recon < 0 || recon > ICS_RECON_MUSCL_MINMOD || !(D >= 0)) return ICS_ERR_ARG;
+  if (hh->h.m.nInst > 1) {
+    hh->h.err = "scalar transport is not provided for Harmonic Balance handles";
+    return ICS_ERR_ARG;
+  }
+  return guard(hh, [&](Handle& h) {
+    const size_t N = h.m.N, F = h.m.F, B = h.m.B, P = h.m.npatches;
+    if (!h.ss) {
+      h.ss = dalloc<double>(N);
+      h.ssB = dalloc<double>(B);
+      h.srhoS = dalloc<double>(N);
+      h.srhoS0 = dalloc<double>(N);
+      h.srhoS00 = dalloc<double>(N);
+      h.sgrad = dalloc<double>(3 * N);
+      h.sgradL = dalloc<double>(3 * N);
+      h.sface = dalloc<double>(5 * (F + B));
+      h.sblk = dalloc<double>((size_t)h.m.nslots * 32);
+      h.sdg = dalloc<double>(N);
+      h.srD = dalloc<double>(N);
+      h.ssrc = dalloc<double>(N);
+      h.sFixed = dalloc<int>(P ? P : 1);
+      h.sValue = dalloc<double>(P ? P : 1);
+    }
+    std::vector<int> fx(P, 0);
+    std::vector<double> val(P, 0.0);
+    for (size_t p = 0; p < P; ++p) {
+      fx[p] = patch_fixed ? (patch_fixed[p] != 0) : 0;
+      val[p] = patch_value ? patch_value[p] : 0.0;
+    }
+    if (P) {
+      ICS_CUDA(cudaMemcpy(h.sFixed, fx.data(), P * sizeof(int), cudaMemcpyHostToDevice));
+      ICS_CUDA(cudaMemcpy(h.sValue, val.data(), P * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    ICS_CUDA(cudaMemcpyAsync(h.ss, s, N * sizeof(double), cudaMemcpyHostToDevice, h.stream));
+    k_scalar_init<<<grid_for(N, 256), 256, 0, h.stream>>>((int)N, h.ss, h.W, h.srhoS);
+    ICS_CUDA(cudaGetLastError());
+    h.launches++;
+    ICS_CUDA(cudaMemcpyAsync(h.srhoS0, h.srhoS, N * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
+    ICS_CUDA(cudaMemcpyAsync(h.srhoS00, h.srhoS, N * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
+    h.Ds = D;
+    h.reconS = recon;
+    h.scalarOn = true;
+    launch_scalar_bc(h);
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    return ICS_OK;
+  });
+}
+
+int ics_scalar_transport(ics_handle hh, int32_t n_iterations, ics_solver_perf* perf) {
+  if (!hh || n_iterations < 0) return ICS_ERR_ARG;
+  return guard(hh, [&](Handle& h) {
+    if (!h.scalarOn) {
+      h.err = "scalar transport is not enabled";
+      return ICS_ERR_STATE;
+    }
+    ensure_workspace(h);
+    ics_solver_perf pf;
+    std::memset(&pf, 0, sizeof(pf));
+    double* dx = (double*)h.kx;
+    for (int it = 0; it < n_iterations; ++it) {
+      ICS_CUDA(cudaMemsetAsync(&h.ks->status, 0, sizeof(int), h.stream));
+      launch_scalar_assembly(h);
+      int stt = 0;
+      ICS_CUDA(cudaMemcpyAsync(&stt, &h.ks->status, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+      ICS_CUDA(cudaStreamSynchronize(h.stream));
+      if (stt) {
+        h.err = "All diagonals of the scalar matrix are zero";
+        return ICS_ERR_DIAG;
+      }
+      const int st = scalar_gmres(h, dx, &pf);
+      if (st && st != ICS_ERR_BREAKDOWN) {
+        h.err = "non-finite scalar Krylov residual";
+        return st;
+      }
+      launch_scalar_update(h, dx);
+    }
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    if (perf) *perf = pf;
+    return ICS_OK;
+  });
+}
+
+int ics_get_scalar(ics_handle hh, double* s, double* rhoS) {
+  return guard(hh, [&](Handle& h) {
+    if (!h.scalarOn) return ICS_ERR_STATE;
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    if (s) ICS_CUDA(cudaMemcpy(s, h.ss, h.m.N * sizeof(double), cudaMemcpyDeviceToHost));
+    if (rhoS) ICS_CUDA(cudaMemcpy(rhoS, h.srhoS, h.m.N * sizeof(double), cudaMemcpyDeviceToHost));
     return ICS_OK;
   });
 }

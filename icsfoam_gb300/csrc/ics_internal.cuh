@@ -202,6 +202,25 @@ struct Handle {
   long long xnnz = 0;
   int xncol = 0;
   bool haveExact = false;
+  // passive scalar transport: s, rhoS (+ old levels) [N], boundary s [B],
+  // per-patch BC (fixed flag, value), face terms and the 1x1-block matrix
+  bool scalarOn = false;
+  double Ds = 0;
+  int reconS = 0;
+  double* ss = nullptr;
+  double* ssB = nullptr;
+  double* srhoS = nullptr;
+  double* srhoS0 = nullptr;
+  double* srhoS00 = nullptr;
+  double* sgrad = nullptr;    // [3][N] reconstruction gradient of s
+  double* sgradL = nullptr;   // [3][N] Gauss gradient of s (laplacian correction)
+  double* sface = nullptr;    // [5][F+B]: flux - laplacian, upper, lower, owner diag, neighbour diag
+  double* sblk = nullptr;     // [nslots*32]
+  double* sdg = nullptr;      // [N]
+  double* srD = nullptr;      // [N]
+  double* ssrc = nullptr;     // [N]
+  int* sFixed = nullptr;      // [npatches]
+  double* sValue = nullptr;   // [npatches]
   // scratch
   double* scratch = nullptr;  // generic [N*5] doubles
   int* ibuf = nullptr;        // [N] flags
@@ -250,6 +269,12 @@ void launch_viscous(Handle& h);
 // Jacobian-vector product of the residual source: out = d(R V)/dW v at the
 // current state with the boundary values held fixed (v, out device [N][5])
 void launch_residual_tangent(Handle& h, const double* v, double* out);
+// passive scalar: face terms + matrix rows at the current flow state, the
+// scalar GMRES solve (increment in dx, device [N]) and the state update
+void launch_scalar_assembly(Handle& h);
+int scalar_gmres(Handle& h, double* dx, ics_solver_perf* perf);
+void launch_scalar_update(Handle& h, const double* dx);
+void launch_scalar_bc(Handle& h);
 // exact Jacobian by coloured tangents; products with it and its transpose
 void build_exact_pattern(Handle& h);
 void free_exact(Handle& h);

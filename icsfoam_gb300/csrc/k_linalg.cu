@@ -1156,4 +1156,232 @@ double rho_l2(Handle& h) {
   return std::sqrt(v);
 }
 
+// ------------------------------------------------------ passive scalar
+// The 1x0 coupled system of the scalar transport (same GMRES, LU-SGS and
+// norm factors as the flow's, one equation): 1x1 sliced-ELL blocks, FP64.
+__global__ void __launch_bounds__(128) k_s_spmv(DevMesh m, const double* __restrict__ blk,
+                                                const double* __restrict__ dg, const double* __restrict__ x,
+                                                double* __restrict__ y) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.N) return;
+  const int s = c >> 5, lane = c & 31;
+  double acc = dg[c] * x[c];
+  const int base = m.slot_base[s];
+  for (int t = 0; t < m.nslot[c]; ++t) {
+    const int col = m.scol[(base + t) * 32 + lane];
+    acc += blk[(size_t)(base + t) * 32 + lane] * x[col];
+  }
+  y[c] = acc;
+}
+
+__device__ __forceinline__ void s_fwd_row(const DevMesh& m, const double* __restrict__ blk,
+                                          const double* __restrict__ rD, double* __restrict__ r, int c, bool scale) {
+  const int s = c >> 5, lane = c & 31;
+  const int base = m.slot_base[s];
+  double acc = r[c];
+  for (int t = 0; t < m.nlow[c]; ++t) {
+    const int col = m.scol[(base + t) * 32 + lane];
+    acc -= blk[(size_t)(base + t) * 32 + lane] * (rD[col] * r[col]);
+  }
+  r[c] = scale ? rD[c] * acc : acc;
+}
+
+__device__ __forceinline__ void s_rev_row(const DevMesh& m, const double* __restrict__ blk,
+                                          const double* __restrict__ rD, double* __restrict__ r, int c) {
+  const int s = c >> 5, lane = c & 31;
+  const int base = m.slot_base[s];
+  double acc = r[c];
+  for (int t = m.nslot[c] - 1; t >= m.nlow[c]; --t) {
+    const int col = m.scol[(base + t) * 32 + lane];
+    acc -= blk[(size_t)(base + t) * 32 + lane] * r[col];
+  }
+  r[c] = rD[c] * acc;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(128) k_s_lusgs_level(DevMesh m, const double* __restrict__ blk,
+                                                       const double* __restrict__ rD, double* __restrict__ r,
+                                                       const int* __restrict__ cells, int start, int count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const int c = cells ? cells[start + i] : start + i;
+  if (MODE == 1)
+    s_rev_row(m, blk, rD, r, c);
+  else
+    s_fwd_row(m, blk, rD, r, c, MODE == 2);
+}
+
+template <bool FWD>
+__global__ void __launch_bounds__(1024) k_s_lusgs_block(DevMesh m, const double* __restrict__ blk,
+                                                        const double* __restrict__ rD, double* __restrict__ r,
+                                                        const int* __restrict__ cells, const int* __restrict__ lptr,
+                                                        int nlev) {
+  for (int l = 0; l < nlev; ++l) {
+    for (int i = lptr[l] + threadIdx.x; i < lptr[l + 1]; i += blockDim.x) {
+      if (FWD)
+        s_fwd_row(m, blk, rD, r, cells[i], false);
+      else
+        s_rev_row(m, blk, rD, r, cells[i]);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_s_jacobi(int N, const double* __restrict__ dg, double* __restrict__ r) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < N) r[c] /= dg[c];
+}
+
+// out[0] = sum w
+__global__ void __launch_bounds__(RB) k_s_sum(int N, const double* __restrict__ w, double* __restrict__ partials,
+                                              unsigned int* __restrict__ counter, double* __restrict__ out) {
+  double acc[1] = {0.0};
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) acc[0] += w[c];
+  reduce_finish<1>(acc, partials, counter, out);
+}
+
+__global__ void k_s_wmavg(int N, const double* __restrict__ w, const double* __restrict__ sum,
+                          double* __restrict__ out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < N) out[c] = w[c] - sum[0] / N;
+}
+
+// out[0] = sum |t| + |b|, out[1] = sum |b|
+__global__ void __launch_bounds__(RB) k_s_normfac(int N, const double* __restrict__ b, const double* __restrict__ t,
+                                                  double* __restrict__ partials, unsigned int* __restrict__ counter,
+                                                  double* __restrict__ out) {
+  double acc[2] = {0.0, 0.0};
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+    acc[0] += fabs(t[c]) + fabs(b[c]);
+    acc[1] += fabs(b[c]);
+  }
+  reduce_finish<2>(acc, partials, counter, out);
+}
+
+// r = b - t, out[0] = sum |r|
+__global__ void __launch_bounds__(RB) k_s_resid(int N, const double* __restrict__ b, const double* __restrict__ t,
+                                                double* __restrict__ r, double* __restrict__ partials,
+                                                unsigned int* __restrict__ counter, double* __restrict__ out) {
+  double acc[1] = {0.0};
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < N; c += gridDim.x * blockDim.x) {
+    const double v = b[c] - t[c];
+    r[c] = v;
+    acc[0] += fabs(v);
+  }
+  reduce_finish<1>(acc, partials, counter, out);
+}
+
+static void s_spmv(Handle& h, const double* x, double* y) {
+  ICS_LAUNCH(h, ICS_K_PASSIVE, k_s_spmv<<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, h.sblk, h.sdg, x, y));
+}
+
+static void s_precondition(Handle& h, double* r) {
+  const DevMesh& m = h.m;
+  const int pc = h.cfg.c.preconditioner;
+  if (pc == ICS_PC_JACOBI) {
+    ICS_LAUNCH(h, ICS_K_PASSIVE, k_s_jacobi<<<grid_for(m.N, 256), 256, 0, h.stream>>>(m.N, h.sdg, r));
+    return;
+  }
+  if (pc != ICS_PC_LUSGS) return;
+  if ((long)m.N < 2048L * m.nfl) {
+    ICS_LAUNCH(h, ICS_K_PASSIVE, k_s_lusgs_block<true><<<1, 1024, 0, h.stream>>>(m, h.sblk, h.srD, r, m.fl_cells,
+                                                                                  m.fl_lptr, m.nfl));
+  } else {
+    for (int l = 1; l < m.nfl; ++l) {  // level 0 has no lower neighbours
+      const int a = m.fl_ptr[l], cnt = m.fl_ptr[l + 1] - a;
+      const bool contig = m.fl_cstart[l] >= 0;
+      ICS_LAUNCH(h, ICS_K_PASSIVE, k_s_lusgs_level<0><<<grid_for(cnt, 128), 128, 0, h.stream>>>(
+                                       m, h.sblk, h.srD, r, contig ? nullptr : m.fl_cells,
+                                       contig ? m.fl_cstart[l] : a, cnt));
+    }
+  }
+  if ((long)m.N < 2048L * m.nrl) {
+    ICS_LAUNCH(h, ICS_K_PASSIVE, k_s_lusgs_block<false><<<1, 1024, 0, h.stream>>>(m, h.sblk, h.srD, r, m.rl_cells,
+                                                                                   m.rl_lptr, m.nrl));
+  } else {
+    for (int l = 0; l < m.nrl; ++l) {
+      const int a = m.rl_ptr[l], cnt = m.rl_ptr[l + 1] - a;
+      const bool contig = m.rl_cstart[l] >= 0;
+      ICS_LAUNCH(h, ICS_K_PASSIVE, k_s_lusgs_level<1><<<grid_for(cnt, 128), 128, 0, h.stream>>>(
+                                       m, h.sblk, h.srD, r, contig ? nullptr : m.rl_cells,
+                                       contig ? m.rl_cstart[l] : a, cnt));
+    }
+  }
+}
+
+// gmres::solveDelta on the scalar system: b = h.ssrc, norm factors from the
+// previous-iteration rhoS, increment in dx
+int scalar_gmres(Handle& h, double* dx, ics_solver_perf* perf) {
+  const int N = h.m.N, m = h.cfg.c.n_directions;
+  cudaStream_t st = h.stream;
+  KrylovScalars* ks = h.ks;
+  const long vs = ((long)N + 63) / 64 * 64;
+  double* V = (double*)h.kv;
+  double* w = (double*)h.kw;
+  double* t = (double*)h.kt;
+  double* red = ks->red;
+  ICS_CUDA(cudaMemsetAsync(&ks->status, 0, sizeof(int), st));
+  ICS_LAUNCH(h, ICS_K_PASSIVE, k_s_sum<<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.srhoS, h.partials, h.counter, &red[2]));
+  ICS_LAUNCH(h, ICS_K_PASSIVE, k_s_wmavg<<<grid_for(N, 256), 256, 0, st>>>(N, h.srhoS, &red[2], w));
+  s_spmv(h, w, t);
+  ICS_LAUNCH(h, ICS_K_PASSIVE, k_s_normfac<<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.ssrc, t, h.partials, h.counter, &red[3]));
+  double hv[2];
+  ICS_CUDA(cudaMemcpyAsync(hv, &red[3], 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  ICS_CUDA(cudaStreamSynchronize(st));
+  const double nf = hv[0] + VSMALL;
+  memset(perf, 0, sizeof(*perf));
+  perf->init_res[0] = perf->final_res[0] = hv[1] / nf;
+  ICS_CUDA(cudaMemsetAsync(dx, 0, N * sizeof(double), st));
+  ICS_CUDA(cudaMemcpyAsync(w, h.ssrc, N * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  const ics_config& cf = h.cfg.c;
+  int status = ICS_OK;
+  while (true) {
+    s_precondition(h, w);
+    ICS_LAUNCH(h, ICS_K_MGS, k_mgs<double><<<MGS_BLOCKS, RB, 0, st>>>(N, w, nullptr, nullptr, nullptr, &ks->status,
+                                                                       h.partials, h.counter, red, ks, 1, 0, m));
+    for (int i = 0; i < m; ++i) {
+      double* vi = V + (size_t)i * vs;
+      ICS_LAUNCH(h, ICS_K_VECTOR, k_scale<double><<<REDUCE_BLOCKS, RB, 0, st>>>(N, w, vi, ks));
+      s_spmv(h, vi, w);
+      s_precondition(h, w);
+      for (int j = 0; j <= i; ++j) {
+        const double* vprev = j > 0 ? V + (size_t)(j - 1) * vs : nullptr;
+        const double* hprev = j > 0 ? &ks->H[(j - 1) * m + i] : nullptr;
+        ICS_LAUNCH(h, ICS_K_MGS,
+                   k_mgs<double><<<MGS_BLOCKS, RB, 0, st>>>(N, w, vprev, hprev, V + (size_t)j * vs, &ks->status,
+                                                            h.partials, h.counter, &ks->H[j * m + i], ks, 0, i, m));
+      }
+      ICS_LAUNCH(h, ICS_K_MGS, k_mgs<double><<<MGS_BLOCKS, RB, 0, st>>>(N, w, vi, &ks->H[i * m + i], nullptr,
+                                                                         &ks->status, h.partials, h.counter, &red[1],
+                                                                         ks, 2, i, m));
+    }
+    ICS_LAUNCH(h, ICS_K_SCALAR, k_backsub<<<1, 1, 0, st>>>(ks, m));
+    ICS_LAUNCH(h, ICS_K_VECTOR, k_xupdate<double><<<REDUCE_BLOCKS, RB, 0, st>>>(N, dx, V, ks, m, vs));
+    s_spmv(h, dx, t);
+    ICS_LAUNCH(h, ICS_K_PASSIVE, k_s_resid<<<REDUCE_BLOCKS, RB, 0, st>>>(N, h.ssrc, t, w, h.partials, h.counter,
+                                                                         &red[5]));
+    double rs = 0;
+    int stt = 0;
+    ICS_CUDA(cudaMemcpyAsync(&rs, &red[5], sizeof(double), cudaMemcpyDeviceToHost, st));
+    ICS_CUDA(cudaMemcpyAsync(&stt, &ks->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ICS_CUDA(cudaStreamSynchronize(st));
+    perf->n_iterations++;
+    if (stt) {
+      status = (stt & 4) ? ICS_ERR_NONFINITE : ICS_ERR_BREAKDOWN;
+      break;
+    }
+    perf->final_res[0] = rs / nf;
+    if (!std::isfinite(perf->final_res[0])) {
+      status = ICS_ERR_NONFINITE;
+      break;
+    }
+    if (perf->n_iterations < cf.min_iter) continue;
+    const double rel = perf->final_res[0] / (perf->init_res[0] + ROOTVSMALL);
+    if (perf->n_iterations >= cf.max_iter || perf->final_res[0] < cf.tolerance || rel < cf.rel_tol) break;
+  }
+  perf->converged = status == ICS_OK;
+  ICS_CUDA(cudaGetLastError());
+  return status;
+}
+
 }  // namespace ics

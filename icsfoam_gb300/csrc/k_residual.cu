@@ -716,4 +716,237 @@ void launch_residual_tangent(Handle& h, const double* v, double* out) {
   ICS_CUDA(cudaGetLastError());
 }
 
+// ------------------------------------------------------- passive scalar
+// calculateScalarTransport.H: rho s advected with a Roe-averaged upwind flux
+// (Harten's fix), laplacian(D, s) for viscous cases, and the 1x1-block
+// matrix: convective blocks from the reconstructed normal velocities, LF
+// dissipation |interpolate(U).n|, geometric-boundary diagonal, viscous
+// stabilisation 0.5 D/rho_f |S| deltaCoeffs, dual-time diagonal.
+// sface layout [5][F+B]: 0 flux - laplacian, 1 upper, 2 lower, 3 owner diag,
+// 4 neighbour diag (boundary faces: 0 and 3 only).
+__global__ void __launch_bounds__(128) k_scalar_face(DevMesh m, ResParams P, int reconS, double Ds, int viscous,
+                                                     const double* __restrict__ q, const double* __restrict__ grad,
+                                                     const double* __restrict__ s, const double* __restrict__ sgrad,
+                                                     const double* __restrict__ sgradL, double* __restrict__ out,
+                                                     int FB) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= m.F) return;
+  const int N = m.N, F = m.F;
+  const int o = m.own[f], nb = m.nei[f];
+  const double sl = reconstruct(m, reconS, 0, f, o, nb, s[o], s[nb], sgrad, +1.0);
+  const double sr = reconstruct(m, reconS, 0, f, o, nb, s[o], s[nb], sgrad, -1.0);
+  const double rl = reconstruct(m, P.reconRho, Q_RHO, f, o, nb, q[Q_RHO * N + o], q[Q_RHO * N + nb], grad, +1.0);
+  const double rr = reconstruct(m, P.reconRho, Q_RHO, f, o, nb, q[Q_RHO * N + o], q[Q_RHO * N + nb], grad, -1.0);
+  double Ul[3], Ur[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int qk = Q_UX + k;
+    Ul[k] = reconstruct(m, P.reconU, qk, f, o, nb, q[qk * N + o], q[qk * N + nb], grad, +1.0);
+    Ur[k] = reconstruct(m, P.reconU, qk, f, o, nb, q[qk * N + o], q[qk * N + nb], grad, -1.0);
+  }
+  const double ms = m.magSf[f];
+  const double n[3] = {m.nf[f], m.nf[F + f], m.nf[2 * F + f]};
+  const double rSl = rl * sl, rSr = rr * sr;
+  const double coefR = sqrt(fmax(VSMALL, rr) / fmax(VSMALL, rl));
+  double roeU[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) roeU[k] = (coefR * Ur[k] + Ul[k]) / (coefR + 1.0);
+  const double uProj = dot3(roeU, n) - 0.0;
+  double lam = fabs(uProj);
+  const double eps = 0.05 * lam;
+  if (lam < eps) lam = (lam * lam + eps * eps) / (2.0 * eps);
+  const double unl = dot3(Ul, n), unr = dot3(Ur, n);
+  double ph = -0.5 * ms * lam * (rSr - rSl);
+  ph += 0.5 * ms * (rl * unl * sl + rr * unr * sr);
+  ph -= 0.5 * ms * 0.0 * (rSl + rSr);
+  const double wf = m.w[f];
+  // LF dissipation with the linearly interpolated cell velocity
+  double Uf[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double a = q[(Q_UX + k) * N + o], b = q[(Q_UX + k) * N + nb];
+    Uf[k] = wf * (a - b) + b;
+  }
+  const double d = 0.5 * ms * fabs(dot3(Uf, n) - 0.0);
+  double stab = 0.0, lap = 0.0;
+  if (viscous) {
+    const double nodc = m.nodc[f];
+    double kc[3], gf[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      kc[k] = n[k] - m.dCC[k * F + f] * nodc;
+      gf[k] = wf * (sgradL[k * N + o] - sgradL[k * N + nb]) + sgradL[k * N + nb];
+    }
+    lap = (Ds * ms) * (nodc * (s[nb] - s[o]) + dot3(kc, gf));
+    const double rhof = wf * (q[Q_RHO * N + o] - q[Q_RHO * N + nb]) + q[Q_RHO * N + nb];
+    stab = 0.5 * (Ds / rhof) * ms * m.dc[f];
+  }
+  const double up = 0.5 * ms * unr, lo = -0.5 * ms * unl;
+  out[f] = ph - lap;
+  out[FB + f] = up - d - stab;
+  out[2 * FB + f] = lo - d - stab;
+  out[3 * FB + f] = -lo + d + stab;
+  out[4 * FB + f] = -up + d + stab;
+}
+
+__global__ void k_scalar_bface(DevMesh m, double Ds, int viscous, const double* __restrict__ bq,
+                               const double* __restrict__ q, const double* __restrict__ s,
+                               const double* __restrict__ sB, const int* __restrict__ sFixed,
+                               double* __restrict__ out, int FB) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= m.B) return;
+  const int B = m.B, F = m.F, N = m.N;
+  const int ci = m.bcell[b];
+  const double ms = m.bmagSf[b];
+  const double S[3] = {m.bSf[b], m.bSf[B + b], m.bSf[2 * B + b]};
+  const double n[3] = {m.bnf[b], m.bnf[B + b], m.bnf[2 * B + b]};
+  const double rb = bq[Q_RHO * B + b];
+  const double Ub[3] = {bq[Q_UX * B + b], bq[Q_UY * B + b], bq[Q_UZ * B + b]};
+  const double sb = sB[b];
+  const double rS = rb * sb;
+  const double coefR = sqrt(fmax(VSMALL, rb) / fmax(VSMALL, rb));
+  double roeU[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) roeU[k] = (coefR * Ub[k] + Ub[k]) / (coefR + 1.0);
+  double lam = fabs(dot3(roeU, n) - 0.0);
+  const double eps = 0.05 * lam;
+  if (lam < eps) lam = (lam * lam + eps * eps) / (2.0 * eps);
+  const double un = dot3(Ub, n);
+  double ph = -0.5 * ms * lam * (rS - rS);
+  ph += 0.5 * ms * (rb * un * sb + rb * un * sb);
+  ph -= 0.5 * ms * 0.0 * (rS + rS);
+  double lap = 0.0;
+  if (viscous) lap = (Ds * ms) * ((sb - s[ci]) * m.bdc[b]);
+  out[F + b] = ph - lap;
+  // dissipation |U_b.n| and rho_B (U_B . S_B) valueInternalCoeffs / rho_I
+  const double vic = sFixed[m.bpatch[b]] ? 0.0 : 1.0;
+  const double flux = rb * (dot3(Ub, S) - 0.0 * ms) * vic;
+  out[3 * FB + F + b] = 0.5 * ms * fabs(un - 0.0) + flux * (1.0 / q[Q_RHO * N + ci]);
+}
+
+__global__ void __launch_bounds__(128) k_scalar_rows(DevMesh m, CellResParams D, const double* __restrict__ face,
+                                                     int FB, const double* __restrict__ rhoS,
+                                                     const double* __restrict__ rhoS0,
+                                                     const double* __restrict__ rhoS00, const double* __restrict__ rPDT,
+                                                     double* __restrict__ src, double* __restrict__ blk,
+                                                     double* __restrict__ dg, double* __restrict__ rD,
+                                                     int* __restrict__ status) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.N) return;
+  const int F = m.F;
+  double dv = 0.0, diag = 0.0;
+  for (int e = m.cptr[c]; e < m.cptr[c + 1]; ++e) {
+    const int code = m.cface[e];
+    const int f = code >= 0 ? code : ~code;
+    dv = code >= 0 ? dv + face[f] : dv - face[f];
+    diag += code >= 0 ? face[3 * FB + f] : face[4 * FB + f];
+  }
+  for (int e = m.bptr[c]; e < m.bptr[c + 1]; ++e) {
+    const int b = m.bface[e];
+    dv += face[F + b];
+    diag += face[3 * FB + F + b];
+  }
+  const double Vc = m.V[c];
+  double r = -(dv / Vc);
+  double dgt, st;
+  ddt_matrix(D, Vc, rPDT[c], rhoS[c], rhoS0[c], rhoS00[c], dgt, st);
+  if (D.ddt != ICS_DDT_STEADY) r -= (dgt * rhoS[c] - st) / Vc;
+  src[c] = r * Vc;
+  diag += dgt;
+  // slots in face order: an owner-side face gives the upper coefficient
+  const int s = c >> 5, lane = c & 31;
+  const int base = m.slot_base[s];
+  for (int t = 0; t < m.nslot[c]; ++t) {
+    const int code = m.sface[(base + t) * 32 + lane];
+    const int f = code >= 0 ? code : ~code;
+    blk[(size_t)(base + t) * 32 + lane] = code >= 0 ? face[FB + f] : face[2 * FB + f];
+  }
+  dg[c] = diag;
+  const double r1 = 1.0 / fmax(1.0 / GREAT, fabs(diag));
+  if (!(r1 >= VSMALL)) atomicOr(status, 1);
+  rD[c] = r1;
+}
+
+__global__ void k_scalar_update(DevMesh m, const double* __restrict__ dx, const double* __restrict__ rho,
+                                double* __restrict__ rhoS, double* __restrict__ s) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.N) return;
+  rhoS[c] += dx[c];
+  s[c] = rhoS[c] / rho[c];
+}
+
+__global__ void k_scalar_bc(DevMesh m, const double* __restrict__ s, const int* __restrict__ sFixed,
+                            const double* __restrict__ sValue, double* __restrict__ sB) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= m.B) return;
+  const int pi = m.bpatch[b];
+  sB[b] = sFixed[pi] ? sValue[pi] : s[m.bcell[b]];
+}
+
+static CellResParams ddt_params(const Handle& h) {
+  CellResParams D;
+  D.ddt = h.cfg.c.ddt_scheme;
+  D.rDeltaT = D.coefft = D.coefft0 = D.coefft00 = 0;
+  D.serRatio = 1;
+  D.applySer = 0;
+  D.coMin = D.coMax = 0;
+  if (D.ddt != ICS_DDT_STEADY) {
+    D.rDeltaT = 1.0 / h.cfg.c.delta_t;
+    if (D.ddt == ICS_DDT_BACKWARD) {
+      const double dt = h.cfg.c.delta_t;
+      const double dt0 = h.timeIndex <= 1 ? GREAT : dt;
+      D.coefft = 1 + dt / (dt + dt0);
+      D.coefft00 = dt * dt / (dt0 * (dt + dt0));
+      D.coefft0 = D.coefft + D.coefft00;
+    }
+  }
+  return D;
+}
+
+void launch_scalar_assembly(Handle& h) {
+  const int N = h.m.N, F = h.m.F, B = h.m.B, FB = F + B;
+  const ResParams P = res_params(h);
+  // flow fields and reconstruction gradients at the current state
+  launch_fields(h);
+  launch_grad(h);
+  // s gradient for its reconstruction scheme, and a plain Gauss one for the
+  // laplacian's non-orthogonal correction
+  const int rs = h.reconS;
+  const int lim = rs == ICS_RECON_MUSCL_VENKATAKRISHNAN ? 2 : (rs == ICS_RECON_MUSCL_MINMOD ? 1 : 0);
+  if (rs != ICS_RECON_UPWIND) {
+    if (lim == 2)
+      ICS_LAUNCH(h, ICS_K_PASSIVE, k_grad<2, double><<<grid_for(N, 128), 128, 0, h.stream>>>(h.m, h.ss, h.ssB, 1u, h.sgrad));
+    else if (lim == 1)
+      ICS_LAUNCH(h, ICS_K_PASSIVE, k_grad<1, double><<<grid_for(N, 128), 128, 0, h.stream>>>(h.m, h.ss, h.ssB, 1u, h.sgrad));
+    else
+      ICS_LAUNCH(h, ICS_K_PASSIVE, k_grad<0, double><<<grid_for(N, 128), 128, 0, h.stream>>>(h.m, h.ss, h.ssB, 1u, h.sgrad));
+  }
+  const int viscous = h.cfg.c.viscous ? 1 : 0;
+  if (viscous)
+    ICS_LAUNCH(h, ICS_K_PASSIVE, k_grad<0, double><<<grid_for(N, 128), 128, 0, h.stream>>>(h.m, h.ss, h.ssB, 1u, h.sgradL));
+  if (F)
+    ICS_LAUNCH(h, ICS_K_PASSIVE, k_scalar_face<<<grid_for(F, 128), 128, 0, h.stream>>>(
+                                     h.m, P, rs, h.Ds, viscous, h.q, h.grad, h.ss, h.sgrad, h.sgradL, h.sface, FB));
+  if (B)
+    ICS_LAUNCH(h, ICS_K_PASSIVE, k_scalar_bface<<<grid_for(B, 128), 128, 0, h.stream>>>(
+                                     h.m, h.Ds, viscous, h.bq, h.q, h.ss, h.ssB, h.sFixed, h.sface, FB));
+  ICS_LAUNCH(h, ICS_K_PASSIVE, k_scalar_rows<<<grid_for(N, 128), 128, 0, h.stream>>>(
+                                   h.m, ddt_params(h), h.sface, FB, h.srhoS, h.srhoS0, h.srhoS00, h.rPDT, h.ssrc,
+                                   h.sblk, h.sdg, h.srD, &h.ks->status));
+  ICS_CUDA(cudaGetLastError());
+}
+
+void launch_scalar_update(Handle& h, const double* dx) {
+  ICS_LAUNCH(h, ICS_K_PASSIVE, k_scalar_update<<<grid_for(h.m.N, 256), 256, 0, h.stream>>>(h.m, dx, h.q, h.srhoS, h.ss));
+  if (h.m.B)
+    ICS_LAUNCH(h, ICS_K_PASSIVE, k_scalar_bc<<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, h.ss, h.sFixed, h.sValue, h.ssB));
+  ICS_CUDA(cudaGetLastError());
+}
+
+void launch_scalar_bc(Handle& h) {
+  if (h.m.B)
+    ICS_LAUNCH(h, ICS_K_PASSIVE, k_scalar_bc<<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, h.ss, h.sFixed, h.sValue, h.ssB));
+  ICS_CUDA(cudaGetLastError());
+}
+
 }  // namespace ics

@@ -240,6 +240,25 @@ int ics_begin_time_step(ics_handle h);
  * Rotating-frame (cylindrical) momentum sources are not provided.          */
 #define ICS_MAX_INSTANCES 16
 int ics_set_hb(ics_handle h, int32_t n_instances, const double* D);
+/* ---- passive scalar transport (dbnsFoam calculateScalarTransport.H) ----- */
+/* Enable the transported scalar s: initial cell values s [n_cells], per
+ * patch boundary condition patch_fixed[p] (1 fixedValue with patch_value[p],
+ * 0 zeroGradient), diffusivity D (used when the case is viscous: the
+ * laplacian(D, s) term and its Jacobian) and the reconstruct(s) scheme
+ * (ICS_RECON_*).  rhoS = rho s is formed from the current density.  Not
+ * available on Harmonic Balance handles.                                    */
+int ics_scalar_enable(ics_handle h, const double* s, const int32_t* patch_fixed, const double* patch_value,
+                      double D, int32_t recon_s);
+/* n_iterations solves of the scalar equation at the current flow state
+ * (dbnsFoam.C:126-133, after the pseudo iterations of a time step): Roe-type
+ * upwind flux of rho s with Harten's fix, implicit 1x1-block LDU matrix
+ * (convective, dissipation, boundary, viscous and dual-time terms), GMRES
+ * with the flow solver's settings, rhoS += increment, s = rhoS / rho.  perf
+ * receives the last solve's residuals (index 0).                            */
+int ics_scalar_transport(ics_handle h, int32_t n_iterations, ics_solver_perf* perf);
+/* Current s and rhoS [n_cells] (either may be NULL).                       */
+int ics_get_scalar(ics_handle h, double* s, double* rhoS);
+
 /* ---- differentiation of the residual (no counterpart in the reference,
  * whose Jacobian is the approximate one of ics_assemble_jacobian) --------- */
 /* Jacobian-vector product of the residual source R V (the vector
@@ -274,7 +293,7 @@ enum {
   ICS_K_FIELDS = 0, ICS_K_GRAD, ICS_K_FACE, ICS_K_BFACE, ICS_K_CELLRES, ICS_K_JAC_BOUNDARY, ICS_K_JAC_ROWS,
   ICS_K_JACOBI_INV, ICS_K_SPMV, ICS_K_LUSGS_FWD, ICS_K_LUSGS_REV, ICS_K_JACOBI, ICS_K_MGS, ICS_K_VECTOR,
   ICS_K_SCALAR, ICS_K_UPDATE, ICS_K_BC, ICS_K_BOUND, ICS_K_VISC, ICS_K_TANGENT, ICS_K_EXACT, ICS_K_OP0,
-  ICS_K_OP1, ICS_K_COUNT
+  ICS_K_OP1, ICS_K_PASSIVE, ICS_K_COUNT
 };
 /* Start (enable=1) or stop (0) recording a CUDA event pair around every
  * kernel launch on the handle's stream; starting clears previous records.  */

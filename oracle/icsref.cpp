@@ -141,6 +141,14 @@ struct Case {
     double residuals[5] = {0, 0, 0, 0, 0}, initResiduals[5] = {0, 0, 0, 0, 0};
   };
   std::vector<Control> ctl = std::vector<Control>(1);
+  // passive scalar transport (dbnsFoam calculateScalarTransport.H): s and the
+  // transported rhoS (with old time levels), boundary values, per-patch BC
+  bool scalarOn = false;
+  double Ds = 0;
+  int reconS = ICS_RECON_UPWIND;
+  std::vector<double> s, sB, rhoS, rhoS0, rhoS00;
+  std::vector<int> sFixed;
+  std::vector<double> sValue;
   std::string err;
 };
 
@@ -1753,6 +1761,293 @@ bool pseudoLoop(Case& c) {
   return more;
 }
 
+// ---------------------------------------------------------------------------
+// Passive scalar transport (dbnsFoam calculateScalarTransport.H:1-384): a
+// 1x0 coupled system for rhoS solved after the flow iterations
+// ---------------------------------------------------------------------------
+struct SMat {
+  std::vector<double> diag, lower, upper;
+};
+
+void scalarBoundary(Case& c) {
+  for (int b = 0; b < c.B; ++b) {
+    const int pi = c.bpatch[b];
+    c.sB[b] = c.sFixed[pi] ? c.sValue[pi] : c.s[c.bcell[b]];
+  }
+}
+
+void smatMul(const Case& c, const SMat& A, const double* x, double* y) {
+  for (int i = 0; i < c.N; ++i) y[i] = A.diag[i] * x[i];
+  for (int fi = 0; fi < c.F; ++fi) {
+    const int l = c.own[fi], u = c.nei[fi];
+    y[u] += A.lower[fi] * x[l];
+    y[l] += A.upper[fi] * x[u];
+  }
+}
+
+// lusgs.C:50-385 with one scalar equation, sequential in cell order
+int smatPrecondition(const Case& c, const SMat& A, double* r) {
+  if (c.cfg.preconditioner == ICS_PC_NONE) return ICS_OK;
+  if (c.cfg.preconditioner == ICS_PC_JACOBI) {
+    for (int i = 0; i < c.N; ++i) r[i] /= A.diag[i];
+    return ICS_OK;
+  }
+  std::vector<double> rD(c.N);
+  for (int i = 0; i < c.N; ++i) {
+    rD[i] = 1.0 / std::max(1.0 / GREAT, std::fabs(A.diag[i]));
+    if (rD[i] < VSMALL) return ICS_ERR_DIAG;
+  }
+  for (int ci = 0; ci < c.N; ++ci) {
+    const double d = rD[ci] * r[ci];
+    for (int fi : c.cellFaces[ci])
+      if (c.own[fi] == ci && c.nei[fi] > ci) r[c.nei[fi]] -= A.lower[fi] * d;
+  }
+  for (int ci = c.N - 1; ci >= 0; --ci) {
+    const double d = rD[ci] * r[ci];
+    r[ci] = d;
+    for (int fi : c.cellFaces[ci])
+      if (c.nei[fi] == ci && c.own[fi] < ci) r[c.own[fi]] -= A.upper[fi] * d;
+  }
+  return ICS_OK;
+}
+
+// gmres::solveDelta for the 1x0 system (norm factor, MGS, Givens, restart)
+int scalarGmres(Case& c, const SMat& A, const std::vector<double>& b, const std::vector<double>& w,
+                std::vector<double>& dx, ics_solver_perf& perf) {
+  const int N = c.N, m = c.cfg.n_directions;
+  std::memset(&perf, 0, sizeof(perf));
+  double avg = 0;
+  for (int i = 0; i < N; ++i) avg += w[i];
+  avg /= N;
+  std::vector<double> wmr(N), tmp(N), r(b);
+  for (int i = 0; i < N; ++i) wmr[i] = w[i] - avg;
+  smatMul(c, A, wmr.data(), tmp.data());
+  double nf = 0, sb = 0;
+  for (int i = 0; i < N; ++i) {
+    nf += std::fabs(tmp[i]) + std::fabs(b[i]);
+    sb += std::fabs(b[i]);
+  }
+  nf += VSMALL;
+  perf.init_res[0] = perf.final_res[0] = sb / nf;
+  dx.assign(N, 0.0);
+  std::vector<std::vector<double>> Vk(m, std::vector<double>(N));
+  std::vector<double> H(m * m, 0.0), yh(m, 0.0), bh(m + 1, 0.0), cs(m, 0.0), sn(m, 0.0);
+  auto givens = [](double h, double beta, double& cc, double& ss) {
+    if (beta == 0) {
+      cc = 1;
+      ss = 0;
+    } else if (std::fabs(beta) > std::fabs(h)) {
+      const double tau = -h / beta;
+      ss = 1.0 / std::sqrt(1.0 + sqr(tau));
+      cc = ss * tau;
+    } else {
+      const double tau = -beta / h;
+      cc = 1.0 / std::sqrt(1.0 + sqr(tau));
+      ss = cc * tau;
+    }
+  };
+  auto stop = [&]() {
+    if (perf.n_iterations < c.cfg.min_iter) return false;
+    const double rel = perf.final_res[0] / (perf.init_res[0] + ROOTVSMALL);
+    return perf.n_iterations >= c.cfg.max_iter || perf.final_res[0] < c.cfg.tolerance || rel < c.cfg.rel_tol;
+  };
+  int status = ICS_OK;
+  do {
+    int st = smatPrecondition(c, A, r.data());
+    if (st) {
+      c.err = "All diagonals of the scalar matrix are zero";
+      return st;
+    }
+    double beta = 0;
+    for (int q = 0; q < N; ++q) beta += sqr(r[q]);
+    beta = std::sqrt(beta);
+    if (!(beta > 0) || !std::isfinite(beta)) {
+      status = std::isfinite(beta) ? ICS_ERR_BREAKDOWN : ICS_ERR_NONFINITE;
+      perf.n_iterations++;
+      break;
+    }
+    std::fill(bh.begin(), bh.end(), 0.0);
+    bh[0] = beta;
+    for (int i = 0; i < m; ++i) {
+      for (int q = 0; q < N; ++q) Vk[i][q] = r[q] / beta;
+      smatMul(c, A, Vk[i].data(), r.data());
+      smatPrecondition(c, A, r.data());
+      for (int j = 0; j <= i; ++j) {
+        double sdot = 0;
+        for (int q = 0; q < N; ++q) sdot += r[q] * Vk[j][q];
+        H[j * m + i] = sdot;
+        for (int q = 0; q < N; ++q) r[q] -= H[j * m + i] * Vk[j][q];
+      }
+      beta = 0;
+      for (int q = 0; q < N; ++q) beta += sqr(r[q]);
+      beta = std::sqrt(beta);
+      for (int j = 0; j < i; ++j) {
+        const double Hji = H[j * m + i];
+        H[j * m + i] = cs[j] * Hji - sn[j] * H[(j + 1) * m + i];
+        H[(j + 1) * m + i] = sn[j] * Hji + cs[j] * H[(j + 1) * m + i];
+      }
+      givens(H[i * m + i], beta, cs[i], sn[i]);
+      const double bhi = bh[i];
+      bh[i] = cs[i] * bhi - sn[i] * bh[i + 1];
+      bh[i + 1] = sn[i] * bhi + cs[i] * bh[i + 1];
+      H[i * m + i] = cs[i] * H[i * m + i] - sn[i] * beta;
+    }
+    for (int i = m - 1; i >= 0; --i) {
+      double sum = bh[i];
+      for (int j = i + 1; j < m; ++j) sum -= H[i * m + j] * yh[j];
+      const double hii = H[i * m + i];
+      yh[i] = sum / (hii >= 0 ? hii + VSMALL : hii - VSMALL);
+    }
+    for (int i = 0; i < m; ++i)
+      for (int q = 0; q < N; ++q) dx[q] += yh[i] * Vk[i][q];
+    smatMul(c, A, dx.data(), r.data());
+    double sr = 0;
+    for (int q = 0; q < N; ++q) {
+      r[q] = b[q] - r[q];
+      sr += std::fabs(r[q]);
+    }
+    perf.final_res[0] = sr / nf;
+    perf.n_iterations++;
+  } while (!stop());
+  perf.converged = status == ICS_OK;
+  return status;
+}
+
+// one pass of calculateScalarTransport.H at the current flow state
+int scalarTransportStep(Case& c, ics_solver_perf& perf) {
+  const int N = c.N, F = c.F, B = c.B, NF = F + B;
+  const std::vector<double> rhoSPrev = c.rhoS;
+  VolS sF{c.s, c.sB};
+  VolS rF = fieldRho(c);
+  std::vector<double> s_l, s_r, rho_l, rho_r;
+  std::vector<V3> U_l, U_r;
+  reconstruct(c, sF, +1, c.reconS, s_l);
+  reconstruct(c, sF, -1, c.reconS, s_r);
+  reconstruct(c, rF, +1, c.cfg.recon_rho, rho_l);
+  reconstruct(c, rF, -1, c.cfg.recon_rho, rho_r);
+  reconstructU(c, +1, U_l);
+  reconstructU(c, -1, U_r);
+  // face flux phiSp: Roe-averaged upwinding with Harten's fix (lines 82-146)
+  std::vector<double> phiS(NF);
+  for (int fi = 0; fi < NF; ++fi) {
+    const double ms = magSfOf(c, fi);
+    const V3 n = SfOf(c, fi) / ms;
+    const double rS_l = rho_l[fi] * s_l[fi], rS_r = rho_r[fi] * s_r[fi];
+    const double coefR = std::sqrt(std::max(VSMALL, rho_r[fi]) / std::max(VSMALL, rho_l[fi]));
+    const V3 roeU = (coefR * U_r[fi] + U_l[fi]) / (coefR + 1.0);
+    const double uProj = dot(roeU, n) - 0.0;
+    double lam = std::fabs(uProj);
+    const double eps = 0.05 * lam;
+    if (lam < eps) lam = (sqr(lam) + sqr(eps)) / (2.0 * eps);
+    double ph = -0.5 * ms * lam * (rS_r - rS_l);
+    ph += 0.5 * ms * (rho_l[fi] * dot(U_l[fi], n) * s_l[fi] + rho_r[fi] * dot(U_r[fi], n) * s_r[fi]);
+    ph -= 0.5 * ms * 0.0 * (rS_l + rS_r);
+    phiS[fi] = ph;
+  }
+  // residual -div(phiSp) [+ laplacian(D, s)] [- physical ddt]
+  std::vector<double> div(N, 0.0), lap(N, 0.0);
+  for (int fi = 0; fi < F; ++fi) {
+    div[c.own[fi]] += phiS[fi];
+    div[c.nei[fi]] -= phiS[fi];
+  }
+  for (int b = 0; b < B; ++b) div[c.bcell[b]] += phiS[F + b];
+  const bool viscous = c.cfg.viscous != 0;
+  if (viscous) {
+    std::vector<V3> gs;
+    gaussGrad(c, sF, gs);
+    for (int fi = 0; fi < F; ++fi) {
+      const int o = c.own[fi], nb = c.nei[fi];
+      const double wf = c.w[fi];
+      const V3 d = c.C[nb] - c.C[o];
+      const V3 kcor = c.Sf[fi] / c.magSf[fi] - d * c.nodc[fi];
+      const V3 gf(wf * (gs[o].x - gs[nb].x) + gs[nb].x, wf * (gs[o].y - gs[nb].y) + gs[nb].y,
+                  wf * (gs[o].z - gs[nb].z) + gs[nb].z);
+      const double sn = c.nodc[fi] * (c.s[nb] - c.s[o]) + dot(kcor, gf);
+      const double lf = (c.Ds * c.magSf[fi]) * sn;
+      lap[o] += lf;
+      lap[nb] -= lf;
+    }
+    for (int b = 0; b < B; ++b) lap[c.bcell[b]] += (c.Ds * c.bmagSf[b]) * ((c.sB[b] - c.s[c.bcell[b]]) * c.bdc[b]);
+  }
+  const bool steady = c.cfg.ddt_scheme == ICS_DDT_STEADY;
+  const DdtCoeffs dd = ddtCoeffs(c);
+  std::vector<double> bsrc(N);
+  for (int i = 0; i < N; ++i) {
+    const double Vc = c.V[i];
+    double r = -(div[i] / Vc);
+    if (viscous) r += lap[i] / Vc;
+    if (!steady) {
+      double dg, sr;
+      ddtMatrix(c, dd, i, c.rhoS[i], c.rhoS0[i], c.rhoS00[i], dg, sr);
+      r -= (dg * c.rhoS[i] - sr) / Vc;
+    }
+    bsrc[i] = r * Vc;
+  }
+  // Jacobian (lines 197-343)
+  SMat A;
+  A.diag.assign(N, 0.0);
+  A.lower.assign(F, 0.0);
+  A.upper.assign(F, 0.0);
+  for (int fi = 0; fi < F; ++fi) {
+    const V3 n = c.Sf[fi] / c.magSf[fi];
+    const double up = 0.5 * c.magSf[fi] * dot(U_r[fi], n);
+    const double lo = -0.5 * c.magSf[fi] * dot(U_l[fi], n);
+    A.upper[fi] += up;
+    A.lower[fi] += lo;
+    A.diag[c.own[fi]] -= lo;
+    A.diag[c.nei[fi]] -= up;
+  }
+  // dissipation with lambdaConv = |interpolate(U).n| (internal and boundary faces)
+  for (int fi = 0; fi < F; ++fi) {
+    const int o = c.own[fi], nb = c.nei[fi];
+    const double wf = c.w[fi];
+    const V3 Uf(wf * (c.U[o].x - c.U[nb].x) + c.U[nb].x, wf * (c.U[o].y - c.U[nb].y) + c.U[nb].y,
+                wf * (c.U[o].z - c.U[nb].z) + c.U[nb].z);
+    const double lc = std::fabs(dot(Uf, c.Sf[fi] / c.magSf[fi]) - 0.0);
+    const double d = 0.5 * c.magSf[fi] * lc;
+    A.upper[fi] -= d;
+    A.lower[fi] -= d;
+    A.diag[o] += d;
+    A.diag[nb] += d;
+  }
+  for (int b = 0; b < B; ++b) {
+    const double lc = std::fabs(dot(c.UB[b], c.bSf[b] / c.bmagSf[b]) - 0.0);
+    A.diag[c.bcell[b]] += 0.5 * c.bmagSf[b] * lc;
+  }
+  // geometric boundaries: rho_B (U_B . S_B) valueInternalCoeffs / rho_I
+  for (int b = 0; b < B; ++b) {
+    const int ci = c.bcell[b];
+    const double vic = c.sFixed[c.bpatch[b]] ? 0.0 : 1.0;
+    const double flux = rhoBof(c, b) * (dot(c.UB[b], c.bSf[b]) - 0.0 * c.bmagSf[b]) * vic;
+    A.diag[ci] += flux * (1.0 / c.rho[ci]);
+  }
+  if (viscous) {
+    for (int fi = 0; fi < F; ++fi) {
+      const int o = c.own[fi], nb = c.nei[fi];
+      const double rhof = c.w[fi] * (c.rho[o] - c.rho[nb]) + c.rho[nb];
+      const double stab = 0.5 * (c.Ds / rhof) * c.magSf[fi] * c.dc[fi];
+      A.upper[fi] -= stab;
+      A.lower[fi] -= stab;
+      A.diag[o] += stab;
+      A.diag[nb] += stab;
+    }
+  }
+  for (int i = 0; i < N; ++i) {
+    double dg, sr;
+    ddtMatrix(c, dd, i, c.rhoS[i], c.rhoS0[i], c.rhoS00[i], dg, sr);
+    A.diag[i] += dg;
+  }
+  std::vector<double> dx;
+  const int st = scalarGmres(c, A, bsrc, rhoSPrev, dx, perf);
+  if (st && st != ICS_ERR_BREAKDOWN) return st;
+  for (int i = 0; i < N; ++i) {
+    c.rhoS[i] += dx[i];
+    c.s[i] = c.rhoS[i] / c.rho[i];
+  }
+  scalarBoundary(c);
+  return ICS_OK;
+}
+
 }  // namespace
 
 struct ics_handle_s : Case {};
@@ -2175,6 +2470,10 @@ int icsref_begin_time_step(ics_handle h) {
     c.rhoU00 = c.rhoU0;
     c.rhoE00 = c.rhoE0;
   }
+  if (c.scalarOn) {
+    c.rhoS00 = c.timeIndex == 0 ? c.rhoS : c.rhoS0;
+    c.rhoS0 = c.rhoS;
+  }
   c.timeIndex++;
   if (!steady) {
     c.initResValid = false;
@@ -2205,6 +2504,59 @@ int icsref_set_hb(ics_handle h, int32_t n, const double* D) {
   c.ctl.assign(n, Case::Control());
   c.initResValid = c.prevResValid = false;
   c.haveMatrix = c.haveIncrement = false;
+  return ICS_OK;
+}
+
+int icsref_scalar_enable(ics_handle h, const double* s, const int32_t* patch_fixed, const double* patch_value,
+                         double D, int32_t recon) {
+  if (!h || !s || recon < 0 || recon > ICS_RECON_MUSCL_MINMOD || D < 0) return ICS_ERR_ARG;
+  Case& c = *h;
+  if (c.nInst > 1) {
+    c.err = "scalar transport is not provided for Harmonic Balance handles";
+    return ICS_ERR_ARG;
+  }
+  const int P = (int)c.patches.size();
+  c.sFixed.assign(P, 0);
+  c.sValue.assign(P, 0.0);
+  for (int p = 0; p < P; ++p) {
+    c.sFixed[p] = patch_fixed ? (patch_fixed[p] != 0) : 0;
+    c.sValue[p] = patch_value ? patch_value[p] : 0.0;
+  }
+  c.s.assign(s, s + c.N);
+  c.sB.assign(c.B, 0.0);
+  c.rhoS.resize(c.N);
+  for (int i = 0; i < c.N; ++i) c.rhoS[i] = c.rho[i] * c.s[i];
+  c.rhoS0 = c.rhoS;
+  c.rhoS00 = c.rhoS;
+  c.Ds = D;
+  c.reconS = recon;
+  scalarBoundary(c);
+  c.scalarOn = true;
+  return ICS_OK;
+}
+
+int icsref_scalar_transport(ics_handle h, int32_t n_iterations, ics_solver_perf* perf) {
+  if (!h || n_iterations < 0) return ICS_ERR_ARG;
+  Case& c = *h;
+  if (!c.scalarOn) {
+    c.err = "scalar transport is not enabled";
+    return ICS_ERR_STATE;
+  }
+  ics_solver_perf pf{};
+  for (int it = 0; it < n_iterations; ++it) {
+    const int st = scalarTransportStep(c, pf);
+    if (st) return st;
+  }
+  if (perf) *perf = pf;
+  return ICS_OK;
+}
+
+int icsref_get_scalar(ics_handle h, double* s, double* rhoS) {
+  if (!h) return ICS_ERR_ARG;
+  Case& c = *h;
+  if (!c.scalarOn) return ICS_ERR_STATE;
+  if (s) std::memcpy(s, c.s.data(), sizeof(double) * c.N);
+  if (rhoS) std::memcpy(rhoS, c.rhoS.data(), sizeof(double) * c.N);
   return ICS_OK;
 }
 

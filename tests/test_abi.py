@@ -68,3 +68,25 @@ def test_gpu_binding_requires_built_library(monkeypatch, tmp_path):
     monkeypatch.setattr(gpu, "library_path", lambda: str(tmp_path / "missing.so"))
     with pytest.raises(RuntimeError):
         gpu.binding()
+
+
+def test_cuda_library_has_no_unresolved_symbols_of_its_own():
+    """Every symbol the library needs comes from libc/libstdc++/libm/pthread
+    (versioned) or is weak: none of our own functions is left undefined."""
+    import shutil
+    import subprocess
+
+    from icsfoam_gb300 import _build
+
+    if not shutil.which("nm"):
+        pytest.skip("nm not available")
+    out = subprocess.run(["nm", "-D", "--undefined-only", _build.build_gpu()], capture_output=True, text=True,
+                         check=True).stdout
+    bad = []
+    for line in out.splitlines():
+        parts = line.split()
+        if len(parts) < 2 or parts[0] == "w":
+            continue
+        if "@" not in parts[-1]:
+            bad.append(parts[-1])
+    assert not bad, bad

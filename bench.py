@@ -20,7 +20,7 @@ host buffers, the roofline of the dominant kernel, SM clocks sampled during
 the timed region, and the CPU oracle timed on a bounded sample.
 
 ``--impl reference`` times the CPU oracle (the reference algorithm restated
-in C++) on a 64x16x16 sample of the same workload.
+in C++) on 64x16x16 samples of the same workload, one process per host core.
 """
 
 import argparse
@@ -377,6 +377,27 @@ def run_batch(n_cases=64, steps=5, warmup=2, seed=2):
             "sequential_cell_iters_per_s": total * steps / seq, "speedup": seq / conc}
 
 
+def run_viscous_box(n=96, steps=10, warmup=3):
+    """The viscous randomised box (Sutherland, isothermal wall, RCM numbering), mixed precision."""
+    from icsfoam_gb300 import cases, gpu
+
+    b = gpu.binding()
+    w = cases.random_box(n)
+    h = gpu.open_case(w.mesh, cases.make_config(b, w.settings, precision=1))
+    h.set_primitive(w.p, w.U, w.T)
+    for _ in range(warmup):
+        h.pseudo_loop()
+        h.pseudo_iteration()
+    h.timer_start()
+    for _ in range(steps):
+        h.pseudo_loop()
+        h.pseudo_iteration()
+    ms = h.timer_stop()
+    h.close()
+    return {"workload": w.name, "cells": w.mesh.n_cells, "ms_per_iter": round(ms / steps, 3),
+            "cell_iters_per_s": w.mesh.n_cells * steps / (ms / 1000.0)}
+
+
 def run_diff(nx=120, ny=64, nz=64, reps=5):
     """Residual derivatives on the swept bump: forward-mode JVP, exact Jacobian assembly by
     coloured JVPs, and the transpose product (VJP)."""
@@ -410,57 +431,72 @@ def run_diff(nx=120, ny=64, nz=64, reps=5):
             "note": "jvp/vjp ms include the host<->device copy of the [N,5] vectors"}
 
 
-def cpu_sample(seconds, warm=1):
-    """The oracle (reference algorithm, FP64, sequential) on a 64x16x16 sample."""
+def _oracle_worker(args):
+    """One oracle process: its own 64x16x16 sample, warm-up, barrier, timed iterations."""
+    steps, warmup, seconds, barrier, seed = args
+    sys.path.insert(0, ROOT)
     import oracle
     from icsfoam_gb300 import cases
 
     w = cases.bump_channel(64, 16, 16, ordering_mode="colour")
     h = oracle.open_case(w.mesh, cases.make_config(oracle.binding(), w.settings))
     h.set_primitive(w.p, w.U, w.T)
-    for _ in range(warm):
+    for _ in range(warmup):
         h.pseudo_loop()
         h.pseudo_iteration()
+    barrier.wait()
     t0 = time.perf_counter()
     it = 0
     while True:
         h.pseudo_loop()
         h.pseudo_iteration()
         it += 1
-        if time.perf_counter() - t0 >= seconds:
+        if (steps and it >= steps) or (seconds and time.perf_counter() - t0 >= seconds):
             break
-    dt = time.perf_counter() - t0
-    return {"value": w.mesh.n_cells * it / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": "bump channel 64x16x16 (16,384 cells), same schemes/settings, %d pseudo iterations "
-                      "after %d warm-up, FP64 oracle, 1 thread" % (it, warm)}
+    return w.mesh.n_cells * it, time.perf_counter() - t0, it
+
+
+def oracle_throughput(steps=0, warmup=1, seconds=0.0, procs=None):
+    """The oracle (reference algorithm, FP64) on every host core: one independent
+    64x16x16 sample per process, started together; cell-iters/s = all cells x
+    iterations / the slowest process's time (the reference's own parallel runs
+    would split one mesh with halo exchanges, so this is an upper bound)."""
+    import multiprocessing as mp
+
+    procs = procs or os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    mgr = ctx.Manager()
+    barrier = mgr.Barrier(procs)
+    with ctx.Pool(procs) as pool:
+        res = pool.map(_oracle_worker, [(steps, warmup, seconds, barrier, k) for k in range(procs)])
+    work = sum(r[0] for r in res)
+    dt = max(r[1] for r in res)
+    its = min(r[2] for r in res)
+    return work / dt, dt, procs, its
+
+
+def cpu_sample(seconds, warm=1):
+    """The oracle on all host cores for about ``seconds`` (bounded sample)."""
+    v, dt, procs, its = oracle_throughput(seconds=seconds, warmup=warm)
+    return {"value": v, "unit": UNIT, "cores": procs, "kind": "port",
+            "sample": "bump channel 64x16x16 (16,384 cells) per process, same schemes/settings, %d processes "
+                      "(one per host core) of >= %d pseudo iterations after %d warm-up, FP64 oracle"
+                      % (procs, its, warm)}
 
 
 def reference_arm(args, dist):
     if dist.rank != 0:
         return
-    import oracle
-    from icsfoam_gb300 import cases
-
-    w = cases.bump_channel(64, 16, 16, ordering_mode="colour")
-    h = oracle.open_case(w.mesh, cases.make_config(oracle.binding(), w.settings))
-    h.set_primitive(w.p, w.U, w.T)
-    for _ in range(args.warmup):
-        h.pseudo_loop()
-        h.pseudo_iteration()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        h.pseudo_loop()
-        h.pseudo_iteration()
-    dt = time.perf_counter() - t0
-    v = w.mesh.n_cells * args.steps / dt
-    sample = ("bump channel 64x16x16 (16,384 cells) standing in for 256x64x64; HLLC MUSCL/Venkatakrishnan, "
-              "GMRES(8)+LU-SGS; FP64 oracle, 1 thread")
+    v, dt, procs, its = oracle_throughput(steps=args.steps, warmup=args.warmup)
+    sample = ("bump channel 64x16x16 (16,384 cells) standing in for 256x64x64, one independent sample per host "
+              "core (%d processes); HLLC MUSCL/Venkatakrishnan, GMRES(8)+LU-SGS; FP64 oracle" % procs)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": "bump_channel_64x16x16_sample_of_256x64x64", "cells": w.mesh.n_cells},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+            "config": {"workload": "bump_channel_64x16x16_sample_of_256x64x64", "cells_per_process": 16384,
+                       "processes": procs},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": procs, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -504,6 +540,7 @@ def main():
         extra["harmonic_balance"] = run_hb_sweep()
         extra["batch_independent_cases"] = run_batch()
         extra["derivatives"] = run_diff()
+        extra["viscous_box"] = run_viscous_box()
     # roofline of the dominant kernel class of the mixed leg
     from icsfoam_gb300 import ordering  # noqa: F401
 

@@ -94,7 +94,7 @@ void free_all(Handle& h) {
   void* ptrs[] = {m.own, m.nei, m.Sf, m.magSf, m.w, m.nodc, m.dOwn, m.dNei, m.dCC, m.nf, m.bnf, m.C, m.V,
                   m.bcell, m.bpatch, m.bSf, m.bmagSf, m.bdOwn, m.bdc, m.patches, m.cptr, m.cface, m.bptr,
                   m.bface, m.slot_base, m.scol, m.sface, m.nlow, m.nslot, m.fl_cells, m.rl_cells, m.fl_lptr,
-                  m.rl_lptr, h.W, h.W0, h.W00, h.Wprev, h.prim, h.pB, h.TB, h.UB, h.phiB, h.pseudoCo, h.rPDT,
+                  m.rl_lptr, m.sweep_flag, m.sweep_ticket, h.W, h.W0, h.W00, h.Wprev, h.prim, h.pB, h.TB, h.UB, h.phiB, h.pseudoCo, h.rPDT,
                   h.ddtCoeff, h.q, h.bq, h.clin, h.grad, h.fflux, h.frec, h.flam, h.bjac, h.src, h.vcell,
                   h.fvisc, h.vsf2, m.dc, m.Dhb, h.tW, h.tprim, h.tq, h.tgrad, h.tflux, h.tvc, h.tfv, h.tv,
                   h.ss, h.ssB, h.srhoS, h.srhoS0, h.srhoS00, h.sgrad, h.sgradL, h.sface, h.sblk, h.sdg, h.srD,
@@ -392,6 +392,8 @@ void build_mesh(Handle& h, const ics_mesh_desc* d) {
   m.fl_cells = upload(fcells);
   m.rl_cells = upload(rcells);
   m.fl_lptr = upload(m.fl_ptr);
+  m.sweep_flag = dalloc<int>((size_t)N);
+  m.sweep_ticket = dalloc<unsigned int>(2);
   m.rl_lptr = upload(m.rl_ptr);
 }
 
@@ -893,12 +895,19 @@ int ics_precondition(ics_handle hh, double* r) {
       return ICS_ERR_STATE;
     }
     const size_t n5 = 5ull * h.m.N;
+    ICS_CUDA(cudaMemsetAsync(&h.ks->status, 0, sizeof(int), h.stream));
     ICS_CUDA(cudaMemcpyAsync(h.scratch, r, n5 * sizeof(double), cudaMemcpyHostToDevice, h.stream));
     to_vec(h, h.scratch, h.kw);
     precondition(h, h.kw);
     from_vec(h, h.kw, h.scratch);
     ICS_CUDA(cudaMemcpyAsync(r, h.scratch, n5 * sizeof(double), cudaMemcpyDeviceToHost, h.stream));
+    int st = 0;
+    ICS_CUDA(cudaMemcpyAsync(&st, &h.ks->status, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
     ICS_CUDA(cudaStreamSynchronize(h.stream));
+    if (st & 8) {
+      h.err = "a sync-free LU-SGS sweep gave up waiting";
+      return ICS_ERR_TIMEOUT;
+    }
     return ICS_OK;
   });
 }

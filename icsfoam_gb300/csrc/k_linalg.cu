@@ -420,6 +420,104 @@ __global__ void __launch_bounds__(1024) k_lusgs_block(DevMesh m, const TB* __res
   }
 }
 
+// ----------------------------------------------- sync-free LU-SGS sweeps
+// One launch per sweep for schedules with many levels (RCM / natural
+// numbering): blocks draw consecutive tickets in level order (order[]), so a
+// row only ever waits for rows with smaller tickets, whose blocks started
+// earlier and are resident or done -- no deadlock.  A row spins (bounded) on
+// its neighbours' done flags, reads their values through L2 (ld.cg: L1 is not
+// coherent between SMs), writes its own value, fences, and raises its flag.
+// The arithmetic per row is that of lusgs_fwd_row / lusgs_rev_row, so the
+// result equals the level-by-level sweep bit for bit.  A wait that exceeds
+// the bound sets status bit 8 and returns (the host reports ICS_ERR_TIMEOUT).
+constexpr int SWEEP_SPIN_LIMIT = 1 << 22;
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" : : "l"(p), "r"(v) : "memory");
+}
+
+// acquire-poll a neighbour's done flag: busy for a while, then with a short
+// sleep; bounded (status bit 8 and false after SWEEP_SPIN_LIMIT polls)
+template <typename TV>
+__device__ __forceinline__ bool wait_flag(const int* flags, int j, int* status) {
+  int it = 0;
+  while (ld_acquire(flags + j) == 0) {
+    if (++it > SWEEP_SPIN_LIMIT) {
+      atomicOr(status, 8);
+      return false;
+    }
+    if (it > 64) __nanosleep(32);
+  }
+  return true;
+}
+
+template <typename TB, typename TV, bool FWD, bool SCALE>
+__global__ void __launch_bounds__(128) k_lusgs_sweep(DevMesh m, const TB* __restrict__ blk,
+                                                     const TB* __restrict__ rD, TV* r, const int* __restrict__ order,
+                                                     int count, int* flags, unsigned int* ticket, int* status) {
+  __shared__ int base;
+  if (threadIdx.x == 0) base = (int)atomicAdd(ticket, blockDim.x);
+  __syncthreads();
+  const int i = base + threadIdx.x;
+  if (i >= count) return;
+  const int c = order[i];
+  const int s = c >> 5, lane = c & 31;
+  const int sb = m.slot_base[s];
+  const int nl = m.nlow[c], ns = m.nslot[c];
+  TV acc[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) acc[k] = __ldcg(r + 5 * c + k);
+  if (FWD) {
+#pragma unroll 1
+    for (int t = 0; t < nl; ++t) {
+      const int col = m.scol[(sb + t) * 32 + lane];
+      if (!wait_flag<TV>(flags, col, status)) return;
+      const TV rj = TV(rD[col]);
+      TV dj[5];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) dj[k] = rj * __ldcg(r + 5 * col + k);
+      const TB* Bk = blk + (size_t)(sb + t) * 25 * 32 + lane;
+#pragma unroll
+      for (int a = 0; a < 5; ++a) {
+        TV v = TV(0);
+#pragma unroll
+        for (int b = 0; b < 5; ++b) v += TV(Bk[(5 * a + b) * 32]) * dj[b];
+        acc[a] -= v;
+      }
+    }
+  } else {
+#pragma unroll 1
+    for (int t = ns - 1; t >= nl; --t) {
+      const int col = m.scol[(sb + t) * 32 + lane];
+      if (!wait_flag<TV>(flags, col, status)) return;
+      TV dj[5];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) dj[k] = __ldcg(r + 5 * col + k);
+      const TB* Bk = blk + (size_t)(sb + t) * 25 * 32 + lane;
+#pragma unroll
+      for (int a = 0; a < 5; ++a) {
+        TV v = TV(0);
+#pragma unroll
+        for (int b = 0; b < 5; ++b) v += TV(Bk[(5 * a + b) * 32]) * dj[b];
+        acc[a] -= v;
+      }
+    }
+  }
+  if (SCALE || !FWD) {
+    const TV rc = TV(rD[c]);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) acc[k] = rc * acc[k];
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) r[5 * c + k] = acc[k];
+  st_release(flags + c, 1);  // orders the row's stores before the flag
+}
+
 template <typename TB, typename TV>
 __global__ void k_jacobi_apply(int N, const TB* __restrict__ inv, TV* __restrict__ r) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -722,6 +820,19 @@ static void lusgs_t(Handle& h, TV* r) {
   // When the last forward level holds exactly the rows of the first reverse
   // level (rows without upper neighbours, e.g. the last colour), the two are
   // fused: r' = r - L d*, then delta = rD r' in the same pass.
+  // many levels on a large mesh: one sync-free launch per sweep
+  if (m.nfl > 2 && (long)m.N >= 2048L * m.nfl) {
+    cudaStream_t st = h.stream;
+    int* status = &h.ks->status;
+    ICS_CUDA(cudaMemsetAsync(m.sweep_flag, 0, (size_t)m.N * sizeof(int), st));
+    ICS_CUDA(cudaMemsetAsync(m.sweep_ticket, 0, 2 * sizeof(unsigned int), st));
+    ICS_LAUNCH(h, ICS_K_LUSGS_FWD, k_lusgs_sweep<TB, TV, true, false><<<grid_for(m.N, 128), 128, 0, st>>>(
+                                       m, blk, rD, r, m.fl_cells, m.N, m.sweep_flag, m.sweep_ticket, status));
+    ICS_CUDA(cudaMemsetAsync(m.sweep_flag, 0, (size_t)m.N * sizeof(int), st));
+    ICS_LAUNCH(h, ICS_K_LUSGS_REV, k_lusgs_sweep<TB, TV, false, true><<<grid_for(m.N, 128), 128, 0, st>>>(
+                                       m, blk, rD, r, m.rl_cells, m.N, m.sweep_flag, m.sweep_ticket + 1, status));
+    return;
+  }
   const bool blockFwd = (long)m.N < 2048L * m.nfl;
   const bool fuse = !blockFwd && m.fuse_last;
   if (!blockFwd) {
@@ -1099,7 +1210,8 @@ static int gmres_t(Handle& h, ResIO& p) {
     ICS_CUDA(cudaMemcpyAsync(&h.ksHost->status, &ks->status, sizeof(int), cudaMemcpyDeviceToHost, st));
     ICS_CUDA(cudaStreamSynchronize(st));
     if (h.ksHost->status) {
-      status = (h.ksHost->status & 4) ? ICS_ERR_NONFINITE : ICS_ERR_BREAKDOWN;
+      status = (h.ksHost->status & 8) ? ICS_ERR_TIMEOUT
+                                      : ((h.ksHost->status & 4) ? ICS_ERR_NONFINITE : ICS_ERR_BREAKDOWN);
       p.nIter++;
       break;
     }

@@ -446,12 +446,16 @@ __device__ __forceinline__ void st_release(int* p, int v) {
 template <typename TV>
 __device__ __forceinline__ bool wait_flag(const int* flags, int j, int* status) {
   int it = 0;
+  unsigned ns = 32;
   while (ld_acquire(flags + j) == 0) {
     if (++it > SWEEP_SPIN_LIMIT) {
       atomicOr(status, 8);
       return false;
     }
-    if (it > 64) __nanosleep(32);
+    // exponential back-off: rows many levels ahead stop loading the memory
+    // system that the rows being finished need
+    __nanosleep(ns);
+    if (ns < 1024) ns <<= 1;
   }
   return true;
 }
@@ -469,43 +473,71 @@ __global__ void __launch_bounds__(128) k_lusgs_sweep(DevMesh m, const TB* __rest
   const int s = c >> 5, lane = c & 31;
   const int sb = m.slot_base[s];
   const int nl = m.nlow[c], ns = m.nslot[c];
+  // the neighbours of this sweep: slots [0, nl) forward, [nl, ns) backward
+  const int nn = FWD ? nl : ns - nl;
+  auto slot = [&](int p) { return FWD ? p : ns - 1 - p; };
+  // everything that does not depend on the neighbours' results (columns,
+  // blocks, their rD) is loaded before the first wait; an acquire load keeps
+  // later loads behind it, so these would otherwise sit on the critical path
+  constexpr int PF = 3;
+  int colp[PF];
+  TB bp[PF][25];
+  TV rdp[PF];
+#pragma unroll
+  for (int p = 0; p < PF; ++p) {
+    if (p < nn) {
+      const int t = slot(p);
+      colp[p] = m.scol[(sb + t) * 32 + lane];
+      const TB* Bk = blk + (size_t)(sb + t) * 25 * 32 + lane;
+#pragma unroll
+      for (int q = 0; q < 25; ++q) bp[p][q] = Bk[q * 32];
+      rdp[p] = FWD ? TV(rD[colp[p]]) : TV(1);
+    }
+  }
   TV acc[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) acc[k] = __ldcg(r + 5 * c + k);
-  if (FWD) {
-#pragma unroll 1
-    for (int t = 0; t < nl; ++t) {
-      const int col = m.scol[(sb + t) * 32 + lane];
-      if (!wait_flag<TV>(flags, col, status)) return;
-      const TV rj = TV(rD[col]);
+  // all prefetched neighbours ready first: their value loads then overlap
+#pragma unroll
+  for (int p = 0; p < PF; ++p)
+    if (p < nn && !wait_flag<TV>(flags, colp[p], status)) return;
+  TV rv[PF][5];
+#pragma unroll
+  for (int p = 0; p < PF; ++p)
+    if (p < nn)
+#pragma unroll
+      for (int k = 0; k < 5; ++k) rv[p][k] = __ldcg(r + 5 * colp[p] + k);
+#pragma unroll
+  for (int p = 0; p < PF; ++p) {
+    if (p < nn) {
       TV dj[5];
 #pragma unroll
-      for (int k = 0; k < 5; ++k) dj[k] = rj * __ldcg(r + 5 * col + k);
-      const TB* Bk = blk + (size_t)(sb + t) * 25 * 32 + lane;
+      for (int k = 0; k < 5; ++k) dj[k] = rdp[p] * rv[p][k];
 #pragma unroll
       for (int a = 0; a < 5; ++a) {
         TV v = TV(0);
 #pragma unroll
-        for (int b = 0; b < 5; ++b) v += TV(Bk[(5 * a + b) * 32]) * dj[b];
+        for (int b2 = 0; b2 < 5; ++b2) v += TV(bp[p][5 * a + b2]) * dj[b2];
         acc[a] -= v;
       }
     }
-  } else {
+  }
 #pragma unroll 1
-    for (int t = ns - 1; t >= nl; --t) {
-      const int col = m.scol[(sb + t) * 32 + lane];
-      if (!wait_flag<TV>(flags, col, status)) return;
-      TV dj[5];
+  for (int p = PF; p < nn; ++p) {  // rows with more neighbours than prefetched
+    const int t = slot(p);
+    const int col = m.scol[(sb + t) * 32 + lane];
+    if (!wait_flag<TV>(flags, col, status)) return;
+    const TV rj = FWD ? TV(rD[col]) : TV(1);
+    TV dj[5];
 #pragma unroll
-      for (int k = 0; k < 5; ++k) dj[k] = __ldcg(r + 5 * col + k);
-      const TB* Bk = blk + (size_t)(sb + t) * 25 * 32 + lane;
+    for (int k = 0; k < 5; ++k) dj[k] = rj * __ldcg(r + 5 * col + k);
+    const TB* Bk = blk + (size_t)(sb + t) * 25 * 32 + lane;
 #pragma unroll
-      for (int a = 0; a < 5; ++a) {
-        TV v = TV(0);
+    for (int a = 0; a < 5; ++a) {
+      TV v = TV(0);
 #pragma unroll
-        for (int b = 0; b < 5; ++b) v += TV(Bk[(5 * a + b) * 32]) * dj[b];
-        acc[a] -= v;
-      }
+      for (int b2 = 0; b2 < 5; ++b2) v += TV(Bk[(5 * a + b2) * 32]) * dj[b2];
+      acc[a] -= v;
     }
   }
   if (SCALE || !FWD) {

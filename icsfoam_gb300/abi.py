@@ -148,6 +148,14 @@ _MEASURE["linear_residual_noalloc"] = (C.c_int, [_P, _P, _P, _P])
 # independent cases iterated concurrently (CUDA library only)
 _MEASURE["pseudo_iteration_batch"] = (C.c_int, [_P, C.c_int32, _P, _P])
 
+# bounded-wait probe (CUDA library only)
+_MEASURE["test_sweep_timeout"] = (C.c_int, [_P, C.c_int32, C.c_int32])
+
+# checkpoint / resume (CUDA library only)
+_MEASURE["checkpoint_size"] = (C.c_int, [_P, C.POINTER(C.c_int64)])
+_MEASURE["save_checkpoint"] = (C.c_int, [_P, _P, C.c_int64])
+_MEASURE["load_checkpoint"] = (C.c_int, [_P, _P, C.c_int64])
+
 # differentiation of the residual (CUDA library only)
 _MEASURE["jvp"] = (C.c_int, [_P, _P, _P, C.c_int32])
 _MEASURE["vjp"] = (C.c_int, [_P, _P, _P, C.c_int32])
@@ -426,6 +434,22 @@ class CaseHandle:
         ms = C.c_double()
         self._check(self.b.fn["timer_stop"](self.h, C.byref(ms)), "timer_stop")
         return float(ms.value)
+
+    def test_sweep_timeout(self, skip_row: int, spin_limit: int) -> int:
+        """Status of the bounded-wait probe (ICS_ERR_TIMEOUT expected when rows depend on skip_row)."""
+        return int(self.b.fn["test_sweep_timeout"](self.h, int(skip_row), int(spin_limit)))
+
+    # ------------------------------------------------- checkpoint / resume
+    def save_checkpoint(self) -> bytes:
+        n = C.c_int64()
+        self._check(self.b.fn["checkpoint_size"](self.h, C.byref(n)), "checkpoint_size")
+        buf = C.create_string_buffer(n.value)
+        self._check(self.b.fn["save_checkpoint"](self.h, buf, n.value), "save_checkpoint")
+        return buf.raw
+
+    def load_checkpoint(self, data: bytes):
+        buf = C.create_string_buffer(data, len(data))
+        self._check(self.b.fn["load_checkpoint"](self.h, buf, len(data)), "load_checkpoint")
 
     # ------------------------------------------------------ passive scalar
     def scalar_enable(self, s, patch_fixed=None, patch_value=None, D=0.0, recon=0):

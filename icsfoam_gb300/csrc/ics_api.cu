@@ -19,6 +19,8 @@
 #include <thread>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "ics_internal.cuh"
 
 using namespace ics;
@@ -440,7 +442,15 @@ double residual_norm(const std::vector<double>& r) {
   return std::sqrt(s);
 }
 
+// NVTX range around a phase of the pseudo iteration (visible in Nsight
+// Systems timelines; a no-op without a tool attached)
+struct Range {
+  explicit Range(const char* name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+};
+
 int do_residual(Handle& h, double* host_src) {
+  Range rg("ics residual");
   // SER (setCoAndDeltaT.H:3-37) from the last two linear-solver initial residuals
   double ratio = 1.0;
   bool apply = false;
@@ -485,6 +495,7 @@ int do_residual(Handle& h, double* host_src) {
 }
 
 int do_jacobian(Handle& h) {
+  Range rg("ics jacobian");
   if (!h.haveFlux) {
     h.err = "assemble_jacobian needs a residual evaluation first";
     return ICS_ERR_STATE;
@@ -504,6 +515,7 @@ int do_jacobian(Handle& h) {
 }
 
 int do_solve(Handle& h, ics_solver_perf* perf) {
+  Range rg("ics gmres");
   if (!h.haveMatrix) {
     h.err = "solve_increment needs an assembled Jacobian";
     return ICS_ERR_STATE;
@@ -521,6 +533,7 @@ int do_solve(Handle& h, ics_solver_perf* perf) {
 }
 
 int do_update(Handle& h, ics_iter_stats* s) {
+  Range rg("ics update");
   if (!h.haveIncrement) {
     h.err = "update_fields needs a solved increment";
     return ICS_ERR_STATE;
@@ -929,6 +942,7 @@ int ics_update_fields(ics_handle hh, ics_iter_stats* stats) {
 
 int ics_pseudo_iteration(ics_handle hh, ics_iter_stats* stats) {
   return guard(hh, [&](Handle& h) {
+    Range rg("ics pseudo iteration");
     ics_iter_stats s;
     std::memset(&s, 0, sizeof(s));
     int r = do_residual(h, nullptr);
@@ -1063,6 +1077,188 @@ int ics_timer_stop(ics_handle hh, double* ms) {
   });
 }
 
+// failure-detection probe ------------------------------------------------------
+int ics_test_sweep_timeout(ics_handle hh, int32_t skip_row, int32_t spin_limit) {
+  if (!hh || spin_limit < 1) return ICS_ERR_ARG;
+  return guard(hh, [&](Handle& h) {
+    const int N = h.m.N;
+    if (!h.haveMatrix) {
+      h.err = "test_sweep_timeout needs an assembled Jacobian";
+      return ICS_ERR_STATE;
+    }
+    if (skip_row < 0 || skip_row >= N) return ICS_ERR_ARG;
+    // the forward level order without skip_row
+    std::vector<int> order(N);
+    ICS_CUDA(cudaMemcpy(order.data(), h.m.fl_cells, N * sizeof(int), cudaMemcpyDeviceToHost));
+    order.erase(std::remove(order.begin(), order.end(), (int)skip_row), order.end());
+    if ((int)order.size() != N - 1) return ICS_ERR_ARG;
+    ICS_CUDA(cudaMemcpy(h.ibuf, order.data(), (N - 1) * sizeof(int), cudaMemcpyHostToDevice));
+    ICS_CUDA(cudaMemsetAsync(&h.ks->status, 0, sizeof(int), h.stream));
+    sweep_probe(h, h.ibuf, N - 1, spin_limit);
+    int st = 0;
+    ICS_CUDA(cudaMemcpyAsync(&st, &h.ks->status, sizeof(int), cudaMemcpyDeviceToHost, h.stream));
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    if (st & 8) {
+      h.err = "a sync-free sweep wait gave up (as the probe intends)";
+      return ICS_ERR_TIMEOUT;
+    }
+    return ICS_OK;
+  });
+}
+
+// checkpoint / resume ----------------------------------------------------------
+// Raw binary: a fixed header, then the arrays in a fixed order.  Everything
+// the next pseudo iteration reads is included (state, old time levels,
+// primitives, boundary values, pseudo Courant numbers, SER and pseudotime
+// control state, the passive scalar), so a resumed run continues bit for bit.
+namespace {
+struct CkptHeader {
+  char magic[8];
+  int32_t version, N, F, B, nInst, scalarOn, timeIndex, initResValid, prevResValid, nres;
+  double lastRhoL2;
+};
+constexpr int32_t CKPT_VERSION = 1;
+
+struct CkptIO {
+  Handle& h;
+  char* out;
+  const char* in;
+  size_t pos = 0;
+  void bytes(void* host, size_t n) {
+    if (out) std::memcpy(out + pos, host, n);
+    if (in) std::memcpy(host, in + pos, n);
+    pos += n;
+  }
+  void dev(double* d, size_t n) {
+    const size_t nb = n * sizeof(double);
+    if (out) ICS_CUDA(cudaMemcpy(out + pos, d, nb, cudaMemcpyDeviceToHost));
+    if (in) ICS_CUDA(cudaMemcpy(d, in + pos, nb, cudaMemcpyHostToDevice));
+    pos += nb;
+  }
+};
+
+size_t ckpt_walk(Handle& h, CkptHeader& hd, char* out, const char* in) {
+  CkptIO io{h, out, in};
+  io.bytes(&hd, sizeof(hd));
+  const size_t N = h.m.N, B = h.m.B;
+  io.dev(h.W, 5 * N);
+  io.dev(h.W0, 5 * N);
+  io.dev(h.W00, 5 * N);
+  io.dev(h.prim, 5 * N);
+  io.dev(h.pB, B);
+  io.dev(h.TB, B);
+  io.dev(h.UB, 3 * B);
+  io.dev(h.phiB, B);
+  io.dev(h.pseudoCo, N);
+  const size_t nres = 5 * (size_t)h.m.nInst;
+  if (in) {
+    h.initRes.resize(nres);
+    h.prevRes.resize(nres);
+  }
+  std::vector<double> pad(nres, 0.0);
+  io.bytes(h.initRes.size() == nres ? h.initRes.data() : pad.data(), nres * sizeof(double));
+  io.bytes(h.prevRes.size() == nres ? h.prevRes.data() : pad.data(), nres * sizeof(double));
+  for (auto& q : h.ctl) {
+    int32_t v[3] = {q.corr, q.converged ? 1 : 0, q.firstIteration ? 1 : 0};
+    io.bytes(v, sizeof(v));
+    if (in) {
+      q.corr = v[0];
+      q.converged = v[1] != 0;
+      q.firstIteration = v[2] != 0;
+    }
+    io.bytes(q.residuals, sizeof(q.residuals));
+    io.bytes(q.initResiduals, sizeof(q.initResiduals));
+  }
+  if (h.scalarOn) {
+    io.dev(h.ss, N);
+    io.dev(h.ssB, B);
+    io.dev(h.srhoS, N);
+    io.dev(h.srhoS0, N);
+    io.dev(h.srhoS00, N);
+  }
+  return io.pos;
+}
+
+CkptHeader ckpt_header(const Handle& h) {
+  CkptHeader hd;
+  std::memset(&hd, 0, sizeof(hd));
+  std::memcpy(hd.magic, "ICSCKPT", 7);
+  hd.version = CKPT_VERSION;
+  hd.N = h.m.N;
+  hd.F = h.m.F;
+  hd.B = h.m.B;
+  hd.nInst = h.m.nInst;
+  hd.scalarOn = h.scalarOn ? 1 : 0;
+  hd.timeIndex = h.timeIndex;
+  hd.initResValid = h.initResValid ? 1 : 0;
+  hd.prevResValid = h.prevResValid ? 1 : 0;
+  hd.nres = 5 * h.m.nInst;
+  hd.lastRhoL2 = h.lastRhoL2;
+  return hd;
+}
+}  // namespace
+
+int ics_checkpoint_size(ics_handle hh, int64_t* bytes) {
+  if (!hh || !bytes) return ICS_ERR_ARG;
+  return guard(hh, [&](Handle& h) {
+    CkptHeader hd = ckpt_header(h);
+    // a dry walk counts the bytes
+    size_t n = sizeof(hd);
+    const size_t N = h.m.N, B = h.m.B;
+    n += sizeof(double) * (20 * N + 6 * B + N);
+    n += 2 * sizeof(double) * 5 * h.m.nInst;
+    n += h.ctl.size() * (3 * sizeof(int32_t) + 10 * sizeof(double));
+    if (h.scalarOn) n += sizeof(double) * (4 * N + B);
+    *bytes = (int64_t)n;
+    return ICS_OK;
+  });
+}
+
+int ics_save_checkpoint(ics_handle hh, void* buf, int64_t bytes) {
+  if (!hh || !buf) return ICS_ERR_ARG;
+  return guard(hh, [&](Handle& h) {
+    int64_t need = 0;
+    ics_checkpoint_size(hh, &need);
+    if (bytes < need) {
+      h.err = "checkpoint buffer too small";
+      return ICS_ERR_ARG;
+    }
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    CkptHeader hd = ckpt_header(h);
+    ckpt_walk(h, hd, (char*)buf, nullptr);
+    return ICS_OK;
+  });
+}
+
+int ics_load_checkpoint(ics_handle hh, const void* buf, int64_t bytes) {
+  if (!hh || !buf || bytes < (int64_t)sizeof(CkptHeader)) return ICS_ERR_ARG;
+  return guard(hh, [&](Handle& h) {
+    CkptHeader hd;
+    std::memcpy(&hd, buf, sizeof(hd));
+    const CkptHeader mine = ckpt_header(h);
+    if (std::memcmp(hd.magic, mine.magic, 8) != 0 || hd.version != CKPT_VERSION || hd.N != mine.N ||
+        hd.F != mine.F || hd.B != mine.B || hd.nInst != mine.nInst || hd.scalarOn != mine.scalarOn) {
+      h.err = "checkpoint does not match this handle (mesh, instances or scalar transport)";
+      return ICS_ERR_ARG;
+    }
+    int64_t need = 0;
+    ics_checkpoint_size(hh, &need);
+    if (bytes < need) {
+      h.err = "checkpoint truncated";
+      return ICS_ERR_ARG;
+    }
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    CkptHeader tmp = hd;
+    ckpt_walk(h, tmp, nullptr, (const char*)buf);
+    h.timeIndex = hd.timeIndex;
+    h.initResValid = hd.initResValid != 0;
+    h.prevResValid = hd.prevResValid != 0;
+    h.lastRhoL2 = hd.lastRhoL2;
+    h.haveFlux = h.haveMatrix = h.haveIncrement = h.haveExact = false;
+    return ICS_OK;
+  });
+}
+
 // passive scalar transport ---------------------------------------------------
 __global__ void k_scalar_init(int N, const double* __restrict__ s, const double* __restrict__ W,
                               double* __restrict__ rhoS) {
@@ -1128,6 +1324,7 @@ int ics_scalar_transport(ics_handle hh, int32_t n_iterations, ics_solver_perf* p
       return ICS_ERR_STATE;
     }
     ensure_workspace(h);
+    Range rg("ics scalar transport");
     ics_solver_perf pf;
     std::memset(&pf, 0, sizeof(pf));
     double* dx = (double*)h.kx;
@@ -1201,6 +1398,7 @@ int ics_jvp(ics_handle hh, const double* v, double* Jv, int32_t device) {
   if (!v || !Jv) return ICS_ERR_ARG;
   return guard(hh, [&](Handle& h) {
     ensure_tangent(h);
+    Range rg("ics jvp");
     double* tv = h.tv;
     double* out = h.tv + 5ull * h.m.N;
     stage_in(h, v, tv, device);
@@ -1239,6 +1437,7 @@ int ics_vjp(ics_handle hh, const double* u, double* JTu, int32_t device) {
   if (!u || !JTu) return ICS_ERR_ARG;
   return guard(hh, [&](Handle& h) {
     ensure_tangent(h);
+    Range rg("ics vjp");
     if (!h.haveExact) assemble_exact(h);
     double* tu = h.tv;
     double* out = h.tv + 5ull * h.m.N;

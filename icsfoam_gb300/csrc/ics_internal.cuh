@@ -290,6 +290,7 @@ int precondition(Handle& h, void* r);
 // fills *perf (maximum over instances) and initRes (per instance, [5*J + k])
 int gmres_solve(Handle& h, ics_solver_perf* perf, std::vector<double>& initRes);
 void to_vec(Handle& h, const double* src, void* dst);   // FP64 -> Krylov type
+void sweep_probe(Handle& h, const int* order, int count, int spin_limit);
 void from_vec(Handle& h, const void* src, double* dst); // Krylov type -> FP64
 
 inline int prec(const Handle& h) { return h.cfg.c.precision; }

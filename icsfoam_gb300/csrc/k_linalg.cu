@@ -444,11 +444,11 @@ __device__ __forceinline__ void st_release(int* p, int v) {
 // acquire-poll a neighbour's done flag: busy for a while, then with a short
 // sleep; bounded (status bit 8 and false after SWEEP_SPIN_LIMIT polls)
 template <typename TV>
-__device__ __forceinline__ bool wait_flag(const int* flags, int j, int* status) {
+__device__ __forceinline__ bool wait_flag(const int* flags, int j, int* status, int limit) {
   int it = 0;
   unsigned ns = 32;
   while (ld_acquire(flags + j) == 0) {
-    if (++it > SWEEP_SPIN_LIMIT) {
+    if (++it > limit) {
       atomicOr(status, 8);
       return false;
     }
@@ -463,7 +463,8 @@ __device__ __forceinline__ bool wait_flag(const int* flags, int j, int* status) 
 template <typename TB, typename TV, bool FWD, bool SCALE>
 __global__ void __launch_bounds__(128) k_lusgs_sweep(DevMesh m, const TB* __restrict__ blk,
                                                      const TB* __restrict__ rD, TV* r, const int* __restrict__ order,
-                                                     int count, int* flags, unsigned int* ticket, int* status) {
+                                                     int count, int* flags, unsigned int* ticket, int* status,
+                                                     int spin_limit) {
   __shared__ int base;
   if (threadIdx.x == 0) base = (int)atomicAdd(ticket, blockDim.x);
   __syncthreads();
@@ -500,7 +501,7 @@ __global__ void __launch_bounds__(128) k_lusgs_sweep(DevMesh m, const TB* __rest
   // all prefetched neighbours ready first: their value loads then overlap
 #pragma unroll
   for (int p = 0; p < PF; ++p)
-    if (p < nn && !wait_flag<TV>(flags, colp[p], status)) return;
+    if (p < nn && !wait_flag<TV>(flags, colp[p], status, spin_limit)) return;
   TV rv[PF][5];
 #pragma unroll
   for (int p = 0; p < PF; ++p)
@@ -526,7 +527,7 @@ __global__ void __launch_bounds__(128) k_lusgs_sweep(DevMesh m, const TB* __rest
   for (int p = PF; p < nn; ++p) {  // rows with more neighbours than prefetched
     const int t = slot(p);
     const int col = m.scol[(sb + t) * 32 + lane];
-    if (!wait_flag<TV>(flags, col, status)) return;
+    if (!wait_flag<TV>(flags, col, status, spin_limit)) return;
     const TV rj = FWD ? TV(rD[col]) : TV(1);
     TV dj[5];
 #pragma unroll
@@ -859,10 +860,12 @@ static void lusgs_t(Handle& h, TV* r) {
     ICS_CUDA(cudaMemsetAsync(m.sweep_flag, 0, (size_t)m.N * sizeof(int), st));
     ICS_CUDA(cudaMemsetAsync(m.sweep_ticket, 0, 2 * sizeof(unsigned int), st));
     ICS_LAUNCH(h, ICS_K_LUSGS_FWD, k_lusgs_sweep<TB, TV, true, false><<<grid_for(m.N, 128), 128, 0, st>>>(
-                                       m, blk, rD, r, m.fl_cells, m.N, m.sweep_flag, m.sweep_ticket, status));
+                                       m, blk, rD, r, m.fl_cells, m.N, m.sweep_flag, m.sweep_ticket, status,
+                                       SWEEP_SPIN_LIMIT));
     ICS_CUDA(cudaMemsetAsync(m.sweep_flag, 0, (size_t)m.N * sizeof(int), st));
     ICS_LAUNCH(h, ICS_K_LUSGS_REV, k_lusgs_sweep<TB, TV, false, true><<<grid_for(m.N, 128), 128, 0, st>>>(
-                                       m, blk, rD, r, m.rl_cells, m.N, m.sweep_flag, m.sweep_ticket + 1, status));
+                                       m, blk, rD, r, m.rl_cells, m.N, m.sweep_flag, m.sweep_ticket + 1, status,
+                                       SWEEP_SPIN_LIMIT));
     return;
   }
   const bool blockFwd = (long)m.N < 2048L * m.nfl;
@@ -962,6 +965,29 @@ static void precondition_t(Handle& h, TV* r) {
     lusgs_t<TB, TV>(h, r);
   else if (h.cfg.c.preconditioner == ICS_PC_JACOBI)
     ICS_LAUNCH(h, ICS_K_JACOBI, k_jacobi_apply<TB, TV><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m.N, (const TB*)h.dginv, r));
+}
+
+// One sync-free forward sweep over `order` (count rows) with a given wait
+// bound; used to exercise the bounded waits (a row left out of the order
+// never raises its flag, so its dependents must give up and report).
+template <typename TB, typename TV>
+static void sweep_probe_t(Handle& h, const int* order, int count, int spin_limit) {
+  const DevMesh& m = h.m;
+  cudaStream_t st = h.stream;
+  ICS_CUDA(cudaMemsetAsync(m.sweep_flag, 0, (size_t)m.N * sizeof(int), st));
+  ICS_CUDA(cudaMemsetAsync(m.sweep_ticket, 0, 2 * sizeof(unsigned int), st));
+  ICS_CUDA(cudaMemsetAsync(h.kw, 0, 5ull * m.N * sizeof(TV), st));
+  ICS_LAUNCH(h, ICS_K_LUSGS_FWD, k_lusgs_sweep<TB, TV, true, false><<<grid_for(count, 128), 128, 0, st>>>(
+                                     m, (const TB*)h.blk, (const TB*)h.rD, (TV*)h.kw, order, count, m.sweep_flag,
+                                     m.sweep_ticket, &h.ks->status, spin_limit));
+  ICS_CUDA(cudaGetLastError());
+}
+
+void sweep_probe(Handle& h, const int* order, int count, int spin_limit) {
+  if (prec(h) == ICS_PREC_MIXED)
+    sweep_probe_t<float, float>(h, order, count, spin_limit);
+  else
+    sweep_probe_t<double, double>(h, order, count, spin_limit);
 }
 
 void spmv(Handle& h, const void* x, void* y) {

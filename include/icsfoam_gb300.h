@@ -259,6 +259,28 @@ int ics_scalar_transport(ics_handle h, int32_t n_iterations, ics_solver_perf* pe
 /* Current s and rhoS [n_cells] (either may be NULL).                       */
 int ics_get_scalar(ics_handle h, double* s, double* rhoS);
 
+/* ---- failure detection (host-injected) ----------------------------------- */
+/* Probe of the bounded device waits: one sync-free forward LU-SGS sweep on the
+ * assembled Jacobian with row skip_row left out of the schedule, so its flag
+ * is never raised; the rows that depend on it give up after spin_limit polls.
+ * Returns ICS_ERR_TIMEOUT when the waits report as designed (ICS_OK when no
+ * row depends on skip_row); the context stays usable.                       */
+int ics_test_sweep_timeout(ics_handle h, int32_t skip_row, int32_t spin_limit);
+
+/* ---- checkpoint / resume (the reference writes OpenFOAM time directories
+ * and a pseudotimeState dictionary, pseudotimeControl.C:59-63,84-89) ------- */
+/* Bytes of a checkpoint of this handle.                                    */
+int ics_checkpoint_size(ics_handle h, int64_t* bytes);
+/* Everything the next pseudo iteration reads -- conservative state, old time
+ * levels, primitives, boundary values, pseudo Courant numbers, SER and
+ * pseudotime-control state, passive scalar -- into a host buffer (raw binary
+ * with a header).  A handle created with the same mesh and configuration
+ * resumes from it bit for bit.                                              */
+int ics_save_checkpoint(ics_handle h, void* buf, int64_t bytes);
+/* Restore a checkpoint; ICS_ERR_ARG when it belongs to another mesh size,
+ * instance count or scalar-transport setting.                              */
+int ics_load_checkpoint(ics_handle h, const void* buf, int64_t bytes);
+
 /* ---- differentiation of the residual (no counterpart in the reference,
  * whose Jacobian is the approximate one of ics_assemble_jacobian) --------- */
 /* Jacobian-vector product of the residual source R V (the vector

@@ -157,3 +157,60 @@ def test_batch_of_independent_cases_equals_sequential_runs(gpu_binding):
         assert np.array_equal(a.get_state()["W"], b.get_state()["W"])
     with pytest.raises(abi.IcsError):
         abi.pseudo_iteration_batch([bat[0], bat[0]])
+
+
+@pytest.mark.parametrize("unsteady,scalar", [(False, False), (True, True)])
+def test_checkpoint_resume_is_bit_exact(gpu_binding, unsteady, scalar):
+    """Save after a few iterations, continue; a fresh handle loading the
+    checkpoint continues to the identical state."""
+    w = cases.bump_channel(24, 8, 4, ordering_mode="colour")
+    over = dict(ddt_scheme=2, delta_t=1e-4, n_pseudo_corr=3) if unsteady else {}
+
+    def fresh():
+        h = open_case(gpu_binding, w, **over)
+        if scalar:
+            h.scalar_enable(np.full(w.mesh.n_cells, 0.2), D=0.0, recon=3)
+        return h
+
+    def run(h, n):
+        for _ in range(n):
+            if unsteady and not h.pseudo_loop():
+                h.begin_time_step()
+            elif not unsteady:
+                h.pseudo_loop()
+            h.pseudo_iteration()
+            if scalar:
+                h.scalar_transport(1)
+
+    a = fresh()
+    if unsteady:
+        a.begin_time_step()
+    run(a, 4)
+    ck = a.save_checkpoint()
+    run(a, 5)
+    b = fresh()
+    b.load_checkpoint(ck)
+    run(b, 5)
+    assert np.array_equal(a.get_state()["W"], b.get_state()["W"])
+    assert np.array_equal(a.get_boundary_state()["p"], b.get_boundary_state()["p"])
+    if scalar:
+        assert np.array_equal(a.get_scalar()[0], b.get_scalar()[0])
+    other = open_case(gpu_binding, cases.bump_channel(8, 4, 2, ordering_mode="colour"))
+    with pytest.raises(abi.IcsError) as e:
+        other.load_checkpoint(ck)
+    assert e.value.status == abi.ICS_ERR_ARG
+
+
+def test_bounded_sweep_wait_reports_timeout(gpu_binding):
+    """A row left out of a sync-free sweep never raises its flag: the rows that
+    wait on it give up after a short bound and the status says so; nothing
+    faults and the context keeps working."""
+    w = cases.bump_channel(24, 8, 4, ordering_mode="natural")
+    h = open_case(gpu_binding, w)
+    h.residual()
+    h.assemble_jacobian()
+    assert h.test_sweep_timeout(0, 1000) == abi.ICS_ERR_TIMEOUT  # cell 0 has upper neighbours
+    assert h.test_sweep_timeout(w.mesh.n_cells - 1, 1000) == abi.ICS_OK  # nobody depends on the last
+    h.pseudo_loop()
+    h.pseudo_iteration()
+    assert np.all(np.isfinite(h.get_state()["W"]))

@@ -1117,7 +1117,7 @@ struct CkptHeader {
   int32_t version, N, F, B, nInst, scalarOn, timeIndex, initResValid, prevResValid, nres;
   double lastRhoL2;
 };
-constexpr int32_t CKPT_VERSION = 1;
+constexpr int32_t CKPT_VERSION = 2;
 
 struct CkptIO {
   Handle& h;
@@ -1150,6 +1150,7 @@ size_t ckpt_walk(Handle& h, CkptHeader& hd, char* out, const char* in) {
   io.dev(h.UB, 3 * B);
   io.dev(h.phiB, B);
   io.dev(h.pseudoCo, N);
+  io.dev(h.rPDT, N);  // the dual-time residual term rounds with the previous 1/dtau
   const size_t nres = 5 * (size_t)h.m.nInst;
   if (in) {
     h.initRes.resize(nres);
@@ -1205,7 +1206,7 @@ int ics_checkpoint_size(ics_handle hh, int64_t* bytes) {
     // a dry walk counts the bytes
     size_t n = sizeof(hd);
     const size_t N = h.m.N, B = h.m.B;
-    n += sizeof(double) * (20 * N + 6 * B + N);
+    n += sizeof(double) * (20 * N + 6 * B + 2 * N);
     n += 2 * sizeof(double) * 5 * h.m.nInst;
     n += h.ctl.size() * (3 * sizeof(int32_t) + 10 * sizeof(double));
     if (h.scalarOn) n += sizeof(double) * (4 * N + B);

@@ -272,7 +272,8 @@ int ics_test_sweep_timeout(ics_handle h, int32_t skip_row, int32_t spin_limit);
 /* Bytes of a checkpoint of this handle.                                    */
 int ics_checkpoint_size(ics_handle h, int64_t* bytes);
 /* Everything the next pseudo iteration reads -- conservative state, old time
- * levels, primitives, boundary values, pseudo Courant numbers, SER and
+ * levels, primitives, boundary values, pseudo Courant numbers and the last
+ * local pseudo time steps, SER and
  * pseudotime-control state, passive scalar -- into a host buffer (raw binary
  * with a header).  A handle created with the same mesh and configuration
  * resumes from it bit for bit.                                              */

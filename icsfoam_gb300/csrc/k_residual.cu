@@ -116,22 +116,19 @@ __global__ void __launch_bounds__(128) k_grad(DevMesh m, const Real* __restrict_
     const int o = m.own[f], nb = m.nei[f];
     const int other = isOwn ? nb : o;
     const double wf = m.w[f];
-    const double S0 = m.Sf[f], S1 = m.Sf[F + f], S2 = m.Sf[2 * F + f];
+    // the owner adds S sf, the neighbour subtracts it: fold the sign into S
+    // (exact) so each component is one multiply-add whichever side this is
+    const double sg = isOwn ? 1.0 : -1.0;
+    const double S0 = sg * m.Sf[f], S1 = sg * m.Sf[F + f], S2 = sg * m.Sf[2 * F + f];
 #pragma unroll
     for (int k = 0; k < NQ; ++k) {
       if (!((mask >> k) & 1)) continue;
       const Real qo = q[k * N + other];
       const Real qown = isOwn ? qc[k] : qo, qnei = isOwn ? qo : qc[k];
       const Real sf = wf * (qown - qnei) + qnei;
-      if (isOwn) {
-        g[k][0] = g[k][0] + S0 * sf;
-        g[k][1] = g[k][1] + S1 * sf;
-        g[k][2] = g[k][2] + S2 * sf;
-      } else {
-        g[k][0] = g[k][0] - S0 * sf;
-        g[k][1] = g[k][1] - S1 * sf;
-        g[k][2] = g[k][2] - S2 * sf;
-      }
+      g[k][0] = g[k][0] + S0 * sf;
+      g[k][1] = g[k][1] + S1 * sf;
+      g[k][2] = g[k][2] + S2 * sf;
       if (LIMITED) {
         qmax[k] = fmax(qmax[k], qo);
         qmin[k] = fmin(qmin[k], qo);

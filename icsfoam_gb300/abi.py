@@ -128,6 +128,7 @@ _FUNCS = {
     "begin_time_step": (C.c_int, [_P]),
     "pseudo_loop": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "set_hb": (C.c_int, [_P, C.c_int32, _P]),
+    "set_mrf": (C.c_int, [_P, _P, _P, _P, _P, C.c_int32]),
     "scalar_enable": (C.c_int, [_P, _P, _P, _P, C.c_double, C.c_int32]),
     "scalar_transport": (C.c_int, [_P, C.c_int32, C.POINTER(SolverPerf)]),
     "get_scalar": (C.c_int, [_P, _P, _P]),
@@ -403,6 +404,24 @@ class CaseHandle:
     def set_hb(self, n_instances: int, D):
         D = np.ascontiguousarray(D, np.float64).reshape(n_instances, n_instances)
         self._check(self.b.fn["set_hb"](self.h, int(n_instances), _ptr(D)), "set_hb")
+
+    def set_mrf(self, fields=None, mode: int = 0):
+        """Moving reference frames from ``mrf.frame_fields`` (None: off).
+
+        ``fields`` = (omega [N,3], face_velocity [F+B], boundary_U [B,3],
+        included [B]); mode 0 = dbnsFoam, 1 = the HB solver's re-assignment
+        after every update.
+        """
+        if fields is None:
+            self._check(self.b.fn["set_mrf"](self.h, None, None, None, None, 0), "set_mrf")
+            return
+        om, fv, bu, inc = fields
+        om = np.ascontiguousarray(om, np.float64).reshape(self.N, 3)
+        fv = np.ascontiguousarray(fv, np.float64).reshape(-1)
+        bu = np.ascontiguousarray(bu, np.float64).reshape(-1, 3)
+        inc = np.ascontiguousarray(inc, np.int32).reshape(-1)
+        self._keep_mrf = (om, fv, bu, inc)
+        self._check(self.b.fn["set_mrf"](self.h, _ptr(om), _ptr(fv), _ptr(bu), _ptr(inc), int(mode)), "set_mrf")
 
     def pseudo_loop(self) -> bool:
         more = C.c_int32()

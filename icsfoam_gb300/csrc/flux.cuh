@@ -9,8 +9,10 @@
 //             switches with x >= 0 -> 1)
 //   Roe     : roeFluxScheme.C:41-409 (P |Lambda| P^-1 dissipation with the
 //             Harten entropy fix)
-// The MRF face velocity is zero (no MRF zones on the hot path), kept as an
-// explicit "- 0.0" only where it changes nothing.
+// um is the MRF face velocity (frame velocity . n, zero outside MRF zones):
+// it makes the normal velocities relative and adds the pressure work where
+// each scheme adds it (ausmPlusUpFluxScheme.C:101-102,293; hllcFluxScheme.C:
+// 157-161,217-218; roeFluxScheme.C:362-363,406-408).
 #pragma once
 
 #include "dual.cuh"
@@ -45,9 +47,9 @@ __device__ __forceinline__ double negd(const Real& s) {
 // out: phi, phiUx, phiUy, phiUz, phiE
 template <typename Real>
 __device__ __forceinline__ void flux_ausm(const FStateT<Real>& L, const FStateT<Real>& R, const double S[3],
-                                          double magS, int lowMach, Real out[5]) {
-  const Real unL = dot3(L.U, S) / magS;
-  const Real unR = dot3(R.U, S) / magS;
+                                          double magS, int lowMach, double um, Real out[5]) {
+  const Real unL = dot3(L.U, S) / magS - um;
+  const Real unR = dot3(R.U, S) / magS - um;
   const Real cl = sq(L.c) / fmax(L.c, unL);
   const Real cr = sq(R.c) / fmax(R.c, -unR);
   const Real cf = fmin(cl, cr);
@@ -89,21 +91,21 @@ __device__ __forceinline__ void flux_ausm(const FStateT<Real>& L, const FStateT<
   out[1] = rhoa * up.U[0] * magS + p12 * S[0];
   out[2] = rhoa * up.U[1] * magS + p12 * S[1];
   out[3] = rhoa * up.U[2] * magS + p12 * S[2];
-  out[4] = rhoa * up.H * magS + p12 * 0.0 * magS;
+  out[4] = rhoa * up.H * magS + p12 * um * magS;
 }
 
 template <typename Real>
 __device__ __forceinline__ void flux_hllc(const FStateT<Real>& L, const FStateT<Real>& R, const double n[3],
-                                          double magS, double gInterp, Real out[5]) {
+                                          double magS, double gInterp, double um, Real out[5]) {
   const Real coefR = sqrt(fmax(VSMALL, R.rho) / fmax(VSMALL, L.rho));
   const Real icr = 1.0 / (coefR + 1.0);  // one FP64 reciprocal for the four Roe averages
   Real uAvg[3];
   for (int k = 0; k < 3; ++k) uAvg[k] = (coefR * R.U[k] + L.U[k]) * icr;
   const Real HAvg = (coefR * R.H + L.H) * icr;
   const Real cAvg = sqrt(fabs((gInterp - 1.0) * (HAvg - 0.5 * dot3(uAvg, uAvg))));
-  const Real uMag_l = dot3(L.U, n) - 0.0;
-  const Real uMag_r = dot3(R.U, n) - 0.0;
-  const Real uMagAvg = dot3(uAvg, n) - 0.0;
+  const Real uMag_l = dot3(L.U, n) - um;
+  const Real uMag_r = dot3(R.U, n) - um;
+  const Real uMagAvg = dot3(uAvg, n) - um;
   const Real Sl = fmin(uMag_l - L.c, uMagAvg - cAvg);
   const Real Sr = fmax(uMag_r + R.c, uMagAvg + cAvg);
   const Real rl = L.rho, rr = R.rho, pl = L.p, pr = R.p;
@@ -132,8 +134,8 @@ __device__ __forceinline__ void flux_hllc(const FStateT<Real>& L, const FStateT<
   }
   const Real rhoEStar_l = il * ((Sl - uMag_l) * (rl * L.E) - pl * uMag_l + pStar_l * Sm);
   const Real rhoEStar_r = ir * ((Sr - uMag_r) * (rr * R.E) - pr * uMag_r + pStar_r * Sm);
-  const Real fEl = Sm * (rhoEStar_l + pStar_l) + pStar_l * 0.0;
-  const Real fEr = Sm * (rhoEStar_r + pStar_r) + pStar_r * 0.0;
+  const Real fEl = Sm * (rhoEStar_l + pStar_l) + pStar_l * um;
+  const Real fEr = Sm * (rhoEStar_r + pStar_r) + pStar_r * um;
   out[4] = (coefSl * rl * L.H * uMag_l + coefSlm * fEl + coefSmr * fEr + coefSr * rr * R.H * uMag_r) * magS;
 }
 
@@ -146,7 +148,7 @@ __device__ __forceinline__ void cross3(const A* a, const B* b, C* c) {
 
 template <typename Real>
 __device__ __forceinline__ void flux_roe(const FStateT<Real>& L, const FStateT<Real>& R, const double n[3],
-                                         double magS, double gI, double eps, Real out[5]) {
+                                         double magS, double gI, double eps, double um, Real out[5]) {
   const Real coefR = sqrt(fmax(VSMALL, R.rho) / fmax(VSMALL, L.rho));
   const Real rD = coefR * L.rho;
   Real rU[3];
@@ -155,7 +157,7 @@ __device__ __forceinline__ void flux_roe(const FStateT<Real>& L, const FStateT<R
   const Real rH = (coefR * R.H + L.H) * icr;
   const Real rC = sqrt(fabs((gI - 1.0) * (rH - 0.5 * dot3(rU, rU))));
   const Real uMag_l = dot3(L.U, n), uMag_r = dot3(R.U, n);
-  const Real uProj = dot3(rU, n) - 0.0;
+  const Real uProj = dot3(rU, n) - um;
   const double a1 = gI - 1;
   const Real theta = 0.5 * a1 * dot3(rU, rU);
   const Real c2 = sq(rC);
@@ -250,6 +252,12 @@ __device__ __forceinline__ void flux_roe(const FStateT<Real>& L, const FStateT<R
   ph += 0.5 * magS * (rn_l + rn_r);
   for (int k = 0; k < 3; ++k) pU[k] += 0.5 * magS * (rn_l * L.U[k] + rn_r * R.U[k] + n[k] * (L.p + R.p));
   pE += 0.5 * magS * (rn_l * L.H + rn_r * R.H);
+  if (um != 0.0) {  // the frame's share of the central flux (roeFluxScheme.C:406-408)
+    const double hm = 0.5 * magS * um;
+    ph -= hm * (L.rho + R.rho);
+    for (int k = 0; k < 3; ++k) pU[k] -= hm * (L.rho * L.U[k] + R.rho * R.U[k]);
+    pE -= hm * (L.rho * L.E + R.rho * R.E);
+  }
   out[0] = ph;
   out[1] = pU[0];
   out[2] = pU[1];

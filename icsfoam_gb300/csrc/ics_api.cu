@@ -98,7 +98,7 @@ void free_all(Handle& h) {
                   m.bface, m.slot_base, m.scol, m.sface, m.nlow, m.nslot, m.fl_cells, m.rl_cells, m.fl_lptr,
                   m.rl_lptr, m.sweep_flag, m.sweep_ticket, h.W, h.W0, h.W00, h.Wprev, h.prim, h.pB, h.TB, h.UB, h.phiB, h.pseudoCo, h.rPDT,
                   h.ddtCoeff, h.q, h.bq, h.clin, h.grad, h.fflux, h.frec, h.flam, h.bjac, h.src, h.vcell,
-                  h.fvisc, h.vsf2, m.dc, m.Dhb, h.tW, h.tprim, h.tq, h.tgrad, h.tflux, h.tvc, h.tfv, h.tv,
+                  h.fvisc, h.vsf2, m.dc, m.Dhb, m.mrfU, m.mrfOm, m.mrfBU, m.mrfBIn, h.tW, h.tprim, h.tq, h.tgrad, h.tflux, h.tvc, h.tfv, h.tv,
                   h.ss, h.ssB, h.srhoS, h.srhoS0, h.srhoS00, h.sgrad, h.sgradL, h.sface, h.sblk, h.sdg, h.srD,
                   h.ssrc, h.sFixed, h.sValue,
                   h.blk, h.dg,
@@ -1001,6 +1001,8 @@ int ics_begin_time_step(ics_handle hh) {
                                cudaMemcpyDeviceToDevice, h.stream));
       ICS_CUDA(cudaMemcpyAsync(h.srhoS0, h.srhoS, N * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
     }
+    // dbnsFoam outerLoop.H:6: the frame velocity on the zones' boundary faces
+    launch_mrf_bc(h);
     h.timeIndex++;
     h.haveExact = false;
     if (!steady) {
@@ -1495,6 +1497,58 @@ int ics_set_hb(ics_handle hh, int32_t n, const double* D) {
     h.haveMatrix = h.haveIncrement = false;
     free_exact(h);   // the stencil gains the instance partners
     drop_graphs(h);  // the captured cycle's reduction grids depend on n
+    return ICS_OK;
+  });
+}
+
+int ics_set_mrf(ics_handle hh, const double* omega, const double* face_velocity, const double* boundary_U,
+                const int32_t* included, int32_t mode) {
+  if (!hh) return ICS_ERR_ARG;
+  Handle& h0 = hh->h;
+  const int N = h0.m.N, F = h0.m.F, B = h0.m.B;
+  if (omega) {
+    if (!face_velocity || (B > 0 && (!boundary_U || !included)) ||
+        (mode != ICS_MRF_OUTER_LOOP && mode != ICS_MRF_EVERY_UPDATE)) {
+      h0.err = "MRF zones need omega, face_velocity, boundary_U, included and a known mode";
+      return ICS_ERR_ARG;
+    }
+    bool ok = true;
+    for (long i = 0; i < 3L * N && ok; ++i) ok = std::isfinite(omega[i]);
+    for (long i = 0; i < (long)F + B && ok; ++i) ok = std::isfinite(face_velocity[i]);
+    for (long i = 0; i < 3L * B && ok; ++i) ok = std::isfinite(boundary_U[i]);
+    for (long i = 0; i < B && ok; ++i) ok = included[i] == 0 || included[i] == 1;
+    if (!ok) {
+      h0.err = "non-finite MRF field or an included flag other than 0/1";
+      return ICS_ERR_ARG;
+    }
+  }
+  return guard(hh, [&](Handle& h) {
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    DevMesh& m = h.m;
+    void* old[] = {m.mrfU, m.mrfOm, m.mrfBU, m.mrfBIn};
+    for (void* p : old) dfree(p);
+    m.mrfU = m.mrfOm = m.mrfBU = nullptr;
+    m.mrfBIn = nullptr;
+    m.mrfEvery = 0;
+    h.haveExact = false;
+    h.haveFlux = h.haveMatrix = h.haveIncrement = false;
+    drop_graphs(h);
+    if (!omega) return ICS_OK;
+    std::vector<double> om(3ull * N), bu(3ull * B);
+    for (int i = 0; i < N; ++i)
+      for (int k = 0; k < 3; ++k) om[(size_t)k * N + i] = omega[3 * i + k];
+    for (int b = 0; b < B; ++b)
+      for (int k = 0; k < 3; ++k) bu[(size_t)k * B + b] = boundary_U[3 * b + k];
+    m.mrfOm = upload(om);
+    m.mrfU = upload(std::vector<double>(face_velocity, face_velocity + F + B));
+    if (B > 0) {
+      m.mrfBU = upload(bu);
+      m.mrfBIn = upload(std::vector<int>(included, included + B));
+    }
+    m.mrfEvery = mode == ICS_MRF_EVERY_UPDATE;
+    // createFields.H:262-263: the boundary velocity is assigned at once
+    launch_mrf_bc(h);
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
     return ICS_OK;
   });
 }

@@ -110,6 +110,15 @@ struct DevMesh {
   // coupled through the spectral operator Dhb [nInst][nInst]
   int nInst = 1, Nc = 0;
   double* Dhb = nullptr;
+  // moving reference frames (all nullptr without MRF zones): frame velocity
+  // . n per internal then boundary face [F+B], rotation vector per cell
+  // [3][N], frame velocity of the boundary faces [3][B] and where it is
+  // assigned [B]; mrfEvery re-assigns it after every boundary update
+  double* mrfU = nullptr;
+  double* mrfOm = nullptr;
+  double* mrfBU = nullptr;
+  int* mrfBIn = nullptr;
+  int mrfEvery = 0;
 };
 
 struct Cfg {
@@ -264,6 +273,7 @@ void launch_residual(Handle& h, double serRatio, bool applySer);
 void launch_jacobian(Handle& h);
 void launch_update(Handle& h, int* boundedDev);
 void launch_bc(Handle& h);
+void launch_mrf_bc(Handle& h);
 void launch_set_primitive(Handle& h);
 void launch_derive_primitive(Handle& h);
 void launch_bound_local_timestep(Handle& h);

@@ -92,7 +92,8 @@ __global__ void k_jac_boundary(DevMesh m, double R, double Cv, double gamma, con
   const double TBb = TB[b], pBb = pB[b];
   const double rhoB = (1.0 / (R * TBb)) * pBb;
   const double UB[3] = {UBv[b], UBv[B + b], UBv[2 * B + b]};
-  const double UrelBdotSf = dot3(UB, SfB) - 0.0 * bm;
+  const double umb = m.mrfU ? m.mrfU[m.F + b] : 0.0;  // MRF frame velocity (convectiveFluxScheme.C:94)
+  const double UrelBdotSf = dot3(UB, SfB) - umb * bm;
   const double rhoEB = rhoB * (Cv * TBb + 0.5 * dot3(UB, UB));
   double SuV[3], dCdU[3], dMdp[3], dMdT[3], dEdU[3], dMdUDiag[3];
   double dMdU[3][3];
@@ -190,6 +191,15 @@ __global__ void __launch_bounds__(128) k_jac_rows(DevMesh m, double gamma, const
     const T mhs = T(-0.5) * magS;
     const T d = T(0.5) * magS * T(flam[f]);
     const T sv = vsf2 ? T(vsf2[f]) : T(0);
+    // MRF: -div(w, u_MRF |S|) on the diagonal entries (convectiveFluxScheme.C:477-481,
+    // blockFvOperatorsTemplates.C:148-197): upper -= phi (1-w), lower += phi w,
+    // and the matching negative column sums on the diagonal
+    T moff = T(0), mdg = T(0);
+    if (m.mrfU) {
+      const double phm = m.mrfU[f] * m.magSf[f], wf = m.w[f];
+      moff = isOwn ? T(-(phm * (1.0 - wf))) : T(phm * wf);
+      mdg = isOwn ? T(-(phm * wf)) : T(phm * (1.0 - wf));
+    }
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
 #pragma unroll
@@ -207,6 +217,8 @@ __global__ void __launch_bounds__(128) k_jac_rows(DevMesh m, double gamma, const
           diag[k] -= up;
         }
         if (i == j) {
+          off += moff;
+          diag[k] += mdg;
           off -= d;
           diag[k] += d;
           off -= sv;
@@ -225,6 +237,19 @@ __global__ void __launch_bounds__(128) k_jac_rows(DevMesh m, double gamma, const
   const T dc = T(ddtCoeff[c] * m.V[c]);
 #pragma unroll
   for (int q = 0; q < 5; ++q) diag[6 * q] += dc;
+  if (m.mrfOm) {
+    // MRF source block: skew(omega) V on the momentum diagonal block
+    // (convectiveFluxScheme.C:131-137)
+    const int N = m.N;
+    const double Vc = m.V[c];
+    const double ox = m.mrfOm[c] * Vc, oy = m.mrfOm[N + c] * Vc, oz = m.mrfOm[2 * N + c] * Vc;
+    diag[5 * 1 + 2] -= T(oz);
+    diag[5 * 1 + 3] += T(oy);
+    diag[5 * 2 + 1] += T(oz);
+    diag[5 * 2 + 3] -= T(ox);
+    diag[5 * 3 + 1] -= T(oy);
+    diag[5 * 3 + 2] += T(ox);
+  }
   if (m.nInst > 1) {
     // Harmonic Balance diagonal V D_JJ on every equation (HBZone.C:435-518)
     const int J = c / m.Nc;

@@ -283,7 +283,9 @@ __device__ __forceinline__ Real reconstruct(const DevMesh& m, int scheme, int k,
                  d[2 * F + f] * grad[(3 * k + 2) * N + c]);
 }
 
-template <typename Real = double>
+// MRF = true reads the frame face velocity (moving reference frames); the
+// default instance has it as the constant zero, so it costs nothing there
+template <typename Real = double, bool MRF = false>
 __global__ void __launch_bounds__(128) k_face(DevMesh m, ResParams P, const Real* __restrict__ q,
                                               const Real* __restrict__ grad, const double* __restrict__ clin,
                                               const double* __restrict__ nf, Real* __restrict__ fflux,
@@ -309,13 +311,14 @@ __global__ void __launch_bounds__(128) k_face(DevMesh m, ResParams P, const Real
   const double S[3] = {m.Sf[f], m.Sf[F + f], m.Sf[2 * F + f]};
   const double n[3] = {nf[f], nf[F + f], nf[2 * F + f]};
   const double magS = m.magSf[f];
+  const double um = MRF ? m.mrfU[f] : 0.0;
   Real out[5];
   if (P.scheme == ICS_FLUX_AUSMPLUSUP)
-    flux_ausm(L, R, S, magS, P.lowMach, out);
+    flux_ausm(L, R, S, magS, P.lowMach, um, out);
   else if (P.scheme == ICS_FLUX_HLLC)
-    flux_hllc(L, R, n, magS, P.gamma, out);
+    flux_hllc(L, R, n, magS, P.gamma, um, out);
   else
-    flux_roe(L, R, n, magS, P.gamma, P.entropyFix, out);
+    flux_roe(L, R, n, magS, P.gamma, P.entropyFix, um, out);
 #pragma unroll
   for (int k = 0; k < 5; ++k) fflux[k * FB + f] = out[k];
   if constexpr (is_fp64<Real>) {  // the tangent needs only the fluxes
@@ -336,7 +339,7 @@ __global__ void __launch_bounds__(128) k_face(DevMesh m, ResParams P, const Real
       const double a = q[(Q_UX + k) * N + o], b = q[(Q_UX + k) * N + nb];
       ui[k] = wf * (a - b) + b;
     }
-    flam[f] = ci + fabs(dot3(ui, n) - 0.0);
+    flam[f] = ci + fabs(dot3(ui, n) - um);
   }
 }
 
@@ -353,17 +356,18 @@ __global__ void k_bface(DevMesh m, ResParams P, const double* __restrict__ bq, c
   const double S[3] = {m.bSf[b], m.bSf[B + b], m.bSf[2 * B + b]};
   const double n[3] = {bnf[b], bnf[B + b], bnf[2 * B + b]};
   const double magS = m.bmagSf[b];
+  const double um = m.mrfU ? m.mrfU[F + b] : 0.0;
   double out[5];
   if (P.scheme == ICS_FLUX_AUSMPLUSUP)
-    flux_ausm(L, L, S, magS, P.lowMach, out);
+    flux_ausm(L, L, S, magS, P.lowMach, um, out);
   else if (P.scheme == ICS_FLUX_HLLC)
-    flux_hllc(L, L, n, magS, P.gamma, out);
+    flux_hllc(L, L, n, magS, P.gamma, um, out);
   else
-    flux_roe(L, L, n, magS, P.gamma, P.entropyFix, out);
+    flux_roe(L, L, n, magS, P.gamma, P.entropyFix, um, out);
 #pragma unroll
   for (int k = 0; k < 5; ++k) fflux[k * FB + F + b] = out[k];
   phiB[b] = out[0];
-  flam[F + b] = bclin[b] + fabs(dot3(L.U, n) - 0.0);
+  flam[F + b] = bclin[b] + fabs(dot3(L.U, n) - um);
 }
 
 // ------------------------------------------------------------ cell residual
@@ -442,7 +446,8 @@ __global__ void __launch_bounds__(128) k_cellres(DevMesh m, CellResParams D, con
       const double U0 = prim[2 * N + c], U1 = prim[3 * N + c], U2 = prim[4 * N + c];
       const double bm = m.bmagSf[b];
       const double un = U0 * (m.bSf[b] / bm) + U1 * (m.bSf[B + b] / bm) + U2 * (m.bSf[2 * B + b] / bm);
-      const double pl = 0.5 * m.bdc[b] * (clin[c] + fabs(un - 0.0));
+      const double umb = m.mrfU ? m.mrfU[F + b] : 0.0;
+      const double pl = 0.5 * m.bdc[b] * (clin[c] + fabs(un - umb));
       rmax = fmax(rmax, pl);
     }
   }
@@ -486,6 +491,17 @@ __global__ void __launch_bounds__(128) k_cellres(DevMesh m, CellResParams D, con
   } else {
 #pragma unroll
     for (int k = 0; k < 5; ++k) src[5 * c + k] = r[k] * Vc;
+  }
+  if (m.mrfOm) {
+    // MRF source -(omega x rho U) V on the momentum equations
+    // (convectiveFluxScheme.C:123-129), rho U = rho_ * U_
+    const double om[3] = {m.mrfOm[c], m.mrfOm[N + c], m.mrfOm[2 * N + c]};
+    const double rho = W[5 * c];
+    const double rU[3] = {rho * prim[2 * N + c], rho * prim[3 * N + c], rho * prim[4 * N + c]};
+    double cr[3];
+    cross3(om, rU, cr);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) src[5 * c + 1 + k] -= cr[k] * Vc;
   }
   double co = pseudoCo[c];
   if (D.applySer) {
@@ -570,9 +586,14 @@ void launch_grad(Handle& h) { launch_grad_t<double>(h, h.q, h.grad, ICS_K_GRAD);
 void launch_face_flux(Handle& h) {
   const int FB = h.m.F + h.m.B;
   const ResParams P = res_params(h);
-  if (h.m.F > 0)
-    ICS_LAUNCH(h, ICS_K_FACE, k_face<<<grid_for(h.m.F, 128), 128, 0, h.stream>>>(h.m, P, h.q, h.grad, h.clin, h.m.nf, h.fflux,
-                                                        h.frec, h.flam, FB));
+  if (h.m.F > 0) {
+    if (h.m.mrfU)
+      ICS_LAUNCH(h, ICS_K_FACE, (k_face<double, true><<<grid_for(h.m.F, 128), 128, 0, h.stream>>>(
+                                    h.m, P, h.q, h.grad, h.clin, h.m.nf, h.fflux, h.frec, h.flam, FB)));
+    else
+      ICS_LAUNCH(h, ICS_K_FACE, k_face<<<grid_for(h.m.F, 128), 128, 0, h.stream>>>(h.m, P, h.q, h.grad, h.clin, h.m.nf, h.fflux,
+                                                          h.frec, h.flam, FB));
+  }
   if (h.m.B > 0)
     ICS_LAUNCH(h, ICS_K_BFACE, k_bface<<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, P, h.bq, h.clin + h.m.N, h.m.bnf, h.fflux,
                                                          h.flam, h.phiB, FB));
@@ -660,6 +681,15 @@ __global__ void __launch_bounds__(128) k_src_tangent(DevMesh m, double dgPhys, c
   const double Vc = m.V[c];
 #pragma unroll
   for (int k = 0; k < 5; ++k) r[k] -= dgPhys * Vc * v[5 * c + k];
+  if (m.mrfOm) {  // the MRF source is linear in rho U
+    const int N = m.N;
+    const double om[3] = {m.mrfOm[c], m.mrfOm[N + c], m.mrfOm[2 * N + c]};
+    const double vU[3] = {v[5 * c + 1], v[5 * c + 2], v[5 * c + 3]};
+    double cr[3];
+    cross3(om, vU, cr);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r[1 + k] -= cr[k] * Vc;
+  }
   if (m.nInst > 1) {
     const int J = c / m.Nc, cl = c - J * m.Nc;
     for (int K = 0; K < m.nInst; ++K) {
@@ -692,10 +722,15 @@ void launch_residual_tangent(Handle& h, const double* v, double* out) {
                                                                                       nullptr, P, tq, nullptr, nullptr,
                                                                                       nullptr));
   launch_grad_t<Dual>(h, tq, tgrad, ICS_K_TANGENT);
-  if (h.m.F > 0)
-    ICS_LAUNCH(h, ICS_K_TANGENT, k_face<Dual><<<grid_for(h.m.F, 128), 128, 0, h.stream>>>(h.m, P, tq, tgrad, nullptr,
-                                                                                          h.m.nf, tflux, nullptr,
-                                                                                          nullptr, FB));
+  if (h.m.F > 0) {
+    if (h.m.mrfU)
+      ICS_LAUNCH(h, ICS_K_TANGENT, (k_face<Dual, true><<<grid_for(h.m.F, 128), 128, 0, h.stream>>>(
+                                       h.m, P, tq, tgrad, nullptr, h.m.nf, tflux, nullptr, nullptr, FB)));
+    else
+      ICS_LAUNCH(h, ICS_K_TANGENT, k_face<Dual><<<grid_for(h.m.F, 128), 128, 0, h.stream>>>(h.m, P, tq, tgrad, nullptr,
+                                                                                            h.m.nf, tflux, nullptr,
+                                                                                            nullptr, FB));
+  }
   Dual* tfv = nullptr;
   if (h.cfg.c.viscous) {
     tfv = (Dual*)h.tfv;
@@ -748,14 +783,15 @@ __global__ void __launch_bounds__(128) k_scalar_face(DevMesh m, ResParams P, int
   double roeU[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) roeU[k] = (coefR * Ur[k] + Ul[k]) / (coefR + 1.0);
-  const double uProj = dot3(roeU, n) - 0.0;
+  const double um = m.mrfU ? m.mrfU[f] : 0.0;
+  const double uProj = dot3(roeU, n) - um;
   double lam = fabs(uProj);
   const double eps = 0.05 * lam;
   if (lam < eps) lam = (lam * lam + eps * eps) / (2.0 * eps);
   const double unl = dot3(Ul, n), unr = dot3(Ur, n);
   double ph = -0.5 * ms * lam * (rSr - rSl);
   ph += 0.5 * ms * (rl * unl * sl + rr * unr * sr);
-  ph -= 0.5 * ms * 0.0 * (rSl + rSr);
+  ph -= 0.5 * ms * um * (rSl + rSr);
   const double wf = m.w[f];
   // LF dissipation with the linearly interpolated cell velocity
   double Uf[3];
@@ -764,7 +800,7 @@ __global__ void __launch_bounds__(128) k_scalar_face(DevMesh m, ResParams P, int
     const double a = q[(Q_UX + k) * N + o], b = q[(Q_UX + k) * N + nb];
     Uf[k] = wf * (a - b) + b;
   }
-  const double d = 0.5 * ms * fabs(dot3(Uf, n) - 0.0);
+  const double d = 0.5 * ms * fabs(dot3(Uf, n) - um);
   double stab = 0.0, lap = 0.0;
   if (viscous) {
     const double nodc = m.nodc[f];
@@ -778,7 +814,12 @@ __global__ void __launch_bounds__(128) k_scalar_face(DevMesh m, ResParams P, int
     const double rhof = wf * (q[Q_RHO * N + o] - q[Q_RHO * N + nb]) + q[Q_RHO * N + nb];
     stab = 0.5 * (Ds / rhof) * ms * m.dc[f];
   }
-  const double up = 0.5 * ms * unr, lo = -0.5 * ms * unl;
+  double up = 0.5 * ms * unr, lo = -0.5 * ms * unl;
+  if (um != 0.0) {  // -div(w, u_MRF |S|) (calculateScalarTransport.H:217-219)
+    const double phm = um * ms;
+    up -= phm * (1.0 - wf);
+    lo -= -phm * wf;
+  }
   out[f] = ph - lap;
   out[FB + f] = up - d - stab;
   out[2 * FB + f] = lo - d - stab;
@@ -805,20 +846,21 @@ __global__ void k_scalar_bface(DevMesh m, double Ds, int viscous, const double* 
   double roeU[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) roeU[k] = (coefR * Ub[k] + Ub[k]) / (coefR + 1.0);
-  double lam = fabs(dot3(roeU, n) - 0.0);
+  const double um = m.mrfU ? m.mrfU[F + b] : 0.0;
+  double lam = fabs(dot3(roeU, n) - um);
   const double eps = 0.05 * lam;
   if (lam < eps) lam = (lam * lam + eps * eps) / (2.0 * eps);
   const double un = dot3(Ub, n);
   double ph = -0.5 * ms * lam * (rS - rS);
   ph += 0.5 * ms * (rb * un * sb + rb * un * sb);
-  ph -= 0.5 * ms * 0.0 * (rS + rS);
+  ph -= 0.5 * ms * um * (rS + rS);
   double lap = 0.0;
   if (viscous) lap = (Ds * ms) * ((sb - s[ci]) * m.bdc[b]);
   out[F + b] = ph - lap;
   // dissipation |U_b.n| and rho_B (U_B . S_B) valueInternalCoeffs / rho_I
   const double vic = sFixed[m.bpatch[b]] ? 0.0 : 1.0;
-  const double flux = rb * (dot3(Ub, S) - 0.0 * ms) * vic;
-  out[3 * FB + F + b] = 0.5 * ms * fabs(un - 0.0) + flux * (1.0 / q[Q_RHO * N + ci]);
+  const double flux = rb * (dot3(Ub, S) - um * ms) * vic;
+  out[3 * FB + F + b] = 0.5 * ms * fabs(un - um) + flux * (1.0 / q[Q_RHO * N + ci]);
 }
 
 __global__ void __launch_bounds__(128) k_scalar_rows(DevMesh m, CellResParams D, const double* __restrict__ face,

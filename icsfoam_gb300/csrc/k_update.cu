@@ -110,6 +110,12 @@ __global__ void k_bc(DevMesh m, const double* __restrict__ prim, double* __restr
     }
     default: break;
   }
+  // MRF: fixed-value patches keep the frame velocity that
+  // correctBoundaryVelocity assigned them; in the every-update mode every
+  // included face is re-assigned before T is evaluated (HB updateFields.H:86-88)
+  if (m.mrfBIn && m.mrfBIn[b] &&
+      (m.mrfEvery || pt.kind == ICS_PATCH_FIXED || pt.kind == ICS_PATCH_ISOTHERMAL_WALL))
+    for (int k = 0; k < 3; ++k) U[k] = m.mrfBU[k * B + b];
   // T
   double T = TB[b];
   switch (pt.kind) {
@@ -221,6 +227,21 @@ void launch_update(Handle& h, int* boundedDev) {
   const int useTMax = c.T_max < GREAT ? 1 : 0;
   ICS_LAUNCH(h, ICS_K_UPDATE, k_update<<<grid_for(h.m.N, 256), 256, 0, h.stream>>>(h.m.N, h.W, h.dW, h.prim, c.R, h.cfg.Cv, c.rho_min, eMin, eMax,
                                                         useTMax, boundedDev));
+  ICS_CUDA(cudaGetLastError());
+}
+
+// MRFCoupledZone::correctBoundaryVelocity (MRFCoupledZone.C:594-619): the
+// frame velocity on the included boundary faces
+__global__ void k_mrf_bc(DevMesh m, double* __restrict__ UB) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= m.B || !m.mrfBIn[b]) return;
+  const int B = m.B;
+  for (int k = 0; k < 3; ++k) UB[k * B + b] = m.mrfBU[k * B + b];
+}
+
+void launch_mrf_bc(Handle& h) {
+  if (!h.m.B || !h.m.mrfBIn) return;
+  ICS_LAUNCH(h, ICS_K_BC, k_mrf_bc<<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, h.UB));
   ICS_CUDA(cudaGetLastError());
 }
 

@@ -30,6 +30,12 @@ zeroGradient / noSlip|fixedValue 0 / fixedValue ISOTHERMAL_WALL
 ``inletOutlet`` is taken as zeroGradient (outflow).  Other combinations,
 non-uniform boundary values, cyclic and processor patches and binary files
 raise ``ValueError``.  Only ASCII format is read.
+
+Moving reference frames: when ``constant/MRFProperties`` or
+``constant/MRFTranslatingProperties`` exists, its zones are built on the
+cell zones of ``constant/polyMesh/cellZones`` (in the returned, possibly
+renumbered, cell order) and returned as ``dicts["mrf_zones"]`` = (rotating,
+translating), ready for ``mrf.frame_fields``; ``write_mrf`` writes them.
 """
 
 from __future__ import annotations
@@ -307,6 +313,37 @@ def mesh_from_polymesh(points, faces, owner, neighbour, boundary: List[Dict], pa
     return M._finish(points, fp_int, own, nei, entries, plist)
 
 
+def read_cell_zones(path: str) -> Dict[str, np.ndarray]:
+    """constant/polyMesh/cellZones: {name: cell labels}."""
+    _, body = _header_and_body(_read(path))
+    n, inner = _list_body(body)
+    zones: Dict[str, np.ndarray] = {}
+    pos = 0
+    for m in re.finditer(r"(\S+)\s*\{", inner):
+        if m.start() < pos:
+            continue
+        depth, i = 1, m.end()
+        while depth and i < len(inner):
+            depth += {"{": 1, "}": -1}.get(inner[i], 0)
+            i += 1
+        block = inner[m.end():i - 1]
+        pos = i
+        lab = re.search(r"cellLabels\s+List<label>\s*(\d+)\s*(\{\s*(-?\d+)\s*\}|\(([^)]*)\))", block)
+        if not lab:
+            raise ValueError("%s: zone %s has no cellLabels" % (path, m.group(1)))
+        cnt = int(lab.group(1))
+        if lab.group(3) is not None:
+            v = np.full(cnt, int(lab.group(3)), np.int64)
+        else:
+            v = np.array(lab.group(4).split(), dtype=np.int64)
+        if v.size != cnt:
+            raise ValueError("%s: zone %s: expected %d labels" % (path, m.group(1), cnt))
+        zones[m.group(1)] = v
+    if len(zones) != n:
+        raise ValueError("%s: expected %d zones" % (path, n))
+    return zones
+
+
 def _time_dir(path: str, time: str) -> str:
     for cand in (time, time + ".orig"):
         d = os.path.join(path, cand)
@@ -339,15 +376,25 @@ def load_case(path: str, time: str = "0", ordering_mode: Optional[str] = None):
     p = np.broadcast_to(p_in.reshape(-1), (N,)).copy() if p_in.ndim == 1 else p_in[:, 0].copy()
     T = np.broadcast_to(T_in.reshape(-1), (N,)).copy() if T_in.ndim == 1 else T_in[:, 0].copy()
     U = np.broadcast_to(U_in, (N, 3)).copy()
+    old_to_new = np.arange(N)
     if ordering_mode:
         perm = ordering.permutation(mesh, ordering_mode)
         mesh = M.renumber(mesh, perm)
         p, U, T = p[perm], U[perm], T[perm]
+        old_to_new = np.empty(N, np.int64)
+        old_to_new[perm] = np.arange(N)
     dicts = {}
     for name, sub in (("fvSchemes", "system"), ("fvSolution", "system"), ("controlDict", "system"),
-                      ("thermophysicalProperties", "constant")):
+                      ("thermophysicalProperties", "constant"), ("MRFProperties", "constant"),
+                      ("MRFTranslatingProperties", "constant")):
         f = os.path.join(path, sub, name)
         dicts[name] = parse_dict(_header_and_body(_read(f))[1]) if os.path.exists(f) else {}
+    if dicts["MRFProperties"] or dicts["MRFTranslatingProperties"]:
+        from . import mrf as MRF
+        zf = os.path.join(pm, "cellZones")
+        cz = read_cell_zones(zf) if os.path.exists(zf) else {}
+        cz = {k: old_to_new[v] for k, v in cz.items()}
+        dicts["mrf_zones"] = MRF.zones_from_dicts(dicts["MRFProperties"], dicts["MRFTranslatingProperties"], cz)
     settings = settings_from_dicts(dicts)
     return mesh, {"p": p, "U": U, "T": T}, settings, dicts
 
@@ -507,3 +554,36 @@ def write_case(path: str, mesh: M.Mesh, p: np.ndarray, U: np.ndarray, T: np.ndar
     field("p", "volScalarField", p, 0, lambda v: "%.17g" % v)
     field("U", "volVectorField", U, 1, lambda v: "(%.17g %.17g %.17g)" % tuple(v))
     field("T", "volScalarField", T, 2, lambda v: "%.17g" % v)
+
+
+def write_mrf(path: str, mesh: M.Mesh, rotating=(), translating=()):
+    """Write the zones as constant/polyMesh/cellZones (one zone per MRF zone,
+    named zone0, zone1, ...) and constant/MRFProperties /
+    constant/MRFTranslatingProperties (one sub-dictionary per zone)."""
+    zones = list(rotating) + list(translating)
+    blocks = []
+    for i, z in enumerate(zones):
+        c = np.asarray(z.cells)
+        lab = np.nonzero(c)[0] if c.dtype == bool else np.sort(c.astype(np.int64))
+        blocks.append("zone%d\n{\n    type cellZone;\n    cellLabels List<label> %d\n(\n%s\n)\n;\n}"
+                      % (i, len(lab), "\n".join(str(int(x)) for x in lab)))
+    _write(os.path.join(path, "constant", "polyMesh", "cellZones"), "regIOobject", "constant/polyMesh",
+           "cellZones", "\n%d\n(\n%s\n)\n" % (len(zones), "\n".join(blocks)))
+    vec = lambda v: "(%.17g %.17g %.17g)" % tuple(v)
+    names = lambda ps: "(%s)" % " ".join(ps)
+    rot = []
+    for i, z in enumerate(rotating):
+        rot.append("zone%d\n{\n    cellZone zone%d;\n    active %s;\n    nonRotatingPatches %s;\n"
+                   "    origin %s;\n    axis %s;\n    omega %.17g;\n}" % (i, i, "yes" if z.active else "no",
+                                                                       names(z.non_rotating_patches),
+                                                                       vec(z.origin), vec(z.axis), z.omega))
+    _write(os.path.join(path, "constant", "MRFProperties"), "dictionary", "constant", "MRFProperties",
+           "\n" + "\n".join(rot) + "\n")
+    tra = []
+    for j, z in enumerate(translating):
+        i = len(rotating) + j
+        tra.append("zone%d\n{\n    cellZone zone%d;\n    active %s;\n    nonMovingPatches %s;\n"
+                   "    frameVelocity %s;\n}" % (i, i, "yes" if z.active else "no", names(z.non_moving_patches),
+                                                  vec(z.frame_velocity)))
+    _write(os.path.join(path, "constant", "MRFTranslatingProperties"), "dictionary", "constant",
+           "MRFTranslatingProperties", "\n" + "\n".join(tra) + "\n")

@@ -240,6 +240,31 @@ int ics_begin_time_step(ics_handle h);
  * Rotating-frame (cylindrical) momentum sources are not provided.          */
 #define ICS_MAX_INSTANCES 16
 int ics_set_hb(ics_handle h, int32_t n_instances, const double* D);
+/* Moving reference frames (MRF zones): replaces the convectiveFluxScheme
+ * fields MRFOmega / MRFFaceVelocity (convectiveFluxScheme.H:77-81,192-199)
+ * and MRFCoupledZoneList::correctBoundaryVelocity as dbnsFoam sets them up
+ * (outerLoop.H:6-21, createFields.H:262-266).  Arrays are in the handle's
+ * cell / face numbering:
+ *   omega[3*N]         rotation vector of each cell (zero outside zones)
+ *   face_velocity[F+B] frame velocity . n of each internal then boundary
+ *                      face (MRFZoneList::faceU() & Sf/|Sf|)
+ *   boundary_U[3*B]    frame velocity of each boundary face
+ *   included[B]        1 where correctBoundaryVelocity assigns boundary_U
+ * The face velocity enters every flux scheme (relative normal velocities,
+ * pressure work p u_MRF |S|), the wave speed of the local time step and of
+ * the LF dissipation, the boundary Jacobian (U_rel . S) and the Jacobian
+ * term -div(w, u_MRF |S|); omega adds the source -(omega x rho U) V and its
+ * skew block to the diagonal (addMRFSource, convectiveFluxScheme.C:123-139).
+ * The boundary velocity is assigned at every ics_begin_time_step and kept by
+ * fixed-value patches (fixed, isothermal wall) through every update; with
+ * mode ICS_MRF_EVERY_UPDATE (dbnsFullyImplicitHBFoam updateFields.H:88) it
+ * is also re-assigned on every included face after each update.
+ * omega == NULL switches the zones off.  The passive scalar uses the same
+ * face velocity (calculateScalarTransport.H:96-145,217-290).                 */
+#define ICS_MRF_OUTER_LOOP 0
+#define ICS_MRF_EVERY_UPDATE 1
+int ics_set_mrf(ics_handle h, const double* omega, const double* face_velocity, const double* boundary_U,
+                const int32_t* included, int32_t mode);
 /* ---- passive scalar transport (dbnsFoam calculateScalarTransport.H) ----- */
 /* Enable the transported scalar s: initial cell values s [n_cells], per
  * patch boundary condition patch_fixed[p] (1 fixedValue with patch_value[p],

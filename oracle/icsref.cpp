@@ -149,8 +149,26 @@ struct Case {
   std::vector<double> s, sB, rhoS, rhoS0, rhoS00;
   std::vector<int> sFixed;
   std::vector<double> sValue;
+  // moving reference frames (dbnsFoam outerLoop.H:6-21): frame velocity . n
+  // per internal then boundary face, rotation vector per cell, frame velocity
+  // of the boundary faces that correctBoundaryVelocity assigns
+  bool mrfOn = false;
+  int mrfEvery = 0;
+  std::vector<double> mrfU;
+  std::vector<V3> mrfOm, mrfBU;
+  std::vector<int> mrfBIn;
   std::string err;
 };
+
+// MRF face velocity of face fi (internal then boundary), zero without zones
+inline double umOf(const Case& c, int fi) { return c.mrfOn ? c.mrfU[fi] : 0.0; }
+
+// MRFCoupledZone::correctBoundaryVelocity (MRFCoupledZone.C:594-619)
+void mrfBoundaryVelocity(Case& c) {
+  if (!c.mrfOn) return;
+  for (int b = 0; b < c.B; ++b)
+    if (c.mrfBIn[b]) c.UB[b] = c.mrfBU[b];
+}
 
 // ---------------------------------------------------------------------------
 // Thermo: perfectGas + hConst + sensibleInternalEnergy, Tref = 0
@@ -345,8 +363,8 @@ void calcFluxAUSM(Case& c) {
   for (int fi = 0; fi < NF; ++fi) {
     un_L[fi] = dot(U_L[fi], SfOf(c, fi)) / magSfOf(c, fi);
     un_R[fi] = dot(U_R[fi], SfOf(c, fi)) / magSfOf(c, fi);
-    un_L[fi] -= 0.0;  // MRF face velocity (zero without MRF zones)
-    un_R[fi] -= 0.0;
+    un_L[fi] -= umOf(c, fi);  // MRF face velocity (ausmPlusUpFluxScheme.C:101-102)
+    un_R[fi] -= umOf(c, fi);
   }
   VolS E = fieldE(c);
   VolS H = fieldH(c, E);
@@ -418,7 +436,7 @@ void calcFluxAUSM(Case& c) {
     const double ms = magSfOf(c, fi);
     c.phi[fi] = rhoa * ms;
     c.phiU[fi] = rhoaU * ms + p12 * SfOf(c, fi);
-    c.phiE[fi] = rhoah * ms + p12 * 0.0 * ms;
+    c.phiE[fi] = rhoah * ms + p12 * umOf(c, fi) * ms;
   }
 }
 
@@ -454,9 +472,10 @@ void calcFluxHLLC(Case& c) {
     const V3 uAvg = (coefR * U_r[fi] + U_l[fi]) / (coefR + 1.0);
     const double HAvg = (coefR * H_r[fi] + H_l[fi]) / (coefR + 1.0);
     const double cAvg = std::sqrt(std::fabs((gInterp - 1.0) * (HAvg - 0.5 * magSqr(uAvg))));
-    const double uMag_l = dot(U_l[fi], n) - 0.0;
-    const double uMag_r = dot(U_r[fi], n) - 0.0;
-    const double uMagAvg = dot(uAvg, n) - 0.0;
+    const double um = umOf(c, fi);  // hllcFluxScheme.C:157-161
+    const double uMag_l = dot(U_l[fi], n) - um;
+    const double uMag_r = dot(U_r[fi], n) - um;
+    const double uMagAvg = dot(uAvg, n) - um;
     const double Sl = std::min(uMag_l - c_l[fi], uMagAvg - cAvg);
     const double Sr = std::max(uMag_r + c_r[fi], uMagAvg + cAvg);
     const double rl = rho_l[fi], rr = rho_r[fi], pl = p_l[fi], pr = p_r[fi];
@@ -481,8 +500,8 @@ void calcFluxHLLC(Case& c) {
                  ms;
     const double rhoEStar_l = 1.0 / (Sl - Sm) * ((Sl - uMag_l) * (rl * E_l[fi]) - pl * uMag_l + pStar_l * Sm);
     const double rhoEStar_r = 1.0 / (Sr - Sm) * ((Sr - uMag_r) * (rr * E_r[fi]) - pr * uMag_r + pStar_r * Sm);
-    const double fluxRhoEStar_l = Sm * (rhoEStar_l + pStar_l) + pStar_l * 0.0;
-    const double fluxRhoEStar_r = Sm * (rhoEStar_r + pStar_r) + pStar_r * 0.0;
+    const double fluxRhoEStar_l = Sm * (rhoEStar_l + pStar_l) + pStar_l * um;
+    const double fluxRhoEStar_r = Sm * (rhoEStar_r + pStar_r) + pStar_r * um;
     c.phiE[fi] = (coefSl * rl * H_l[fi] * uMag_l + coefSlm * fluxRhoEStar_l + coefSmr * fluxRhoEStar_r +
                   coefSr * rr * H_r[fi] * uMag_r) *
                  ms;
@@ -517,7 +536,8 @@ void calcFluxRoe(Case& c) {
     const double rH = (coefR * H_r[fi] + H_l[fi]) / (coefR + 1.0);
     const double rC = std::sqrt(std::fabs((gI - 1.0) * (rH - 0.5 * magSqr(rU))));
     const double uMag_l = dot(U_l[fi], n), uMag_r = dot(U_r[fi], n);
-    const double uProj = dot(rU, n) - 0.0;
+    const double um = umOf(c, fi);  // roeFluxScheme.C:362-363
+    const double uProj = dot(rU, n) - um;
     const V3 rhoU_l = rho_l[fi] * U_l[fi], rhoU_r = rho_r[fi] * U_r[fi];
     const double rhoE_l = rho_l[fi] * E_l[fi], rhoE_r = rho_r[fi] * E_r[fi];
     // getRoeDissipation: P |Lambda| P^-1 assembled in conservative variables
@@ -610,7 +630,11 @@ void calcFluxRoe(Case& c) {
     ph += 0.5 * ms * (rn_l + rn_r);
     pU = pU + 0.5 * ms * (rn_l * U_l[fi] + rn_r * U_r[fi] + n * (p_l[fi] + p_r[fi]));
     pE += 0.5 * ms * (rn_l * H_l[fi] + rn_r * H_r[fi]);
-    ph -= 0.5 * ms * 0.0 * (rho_l[fi] + rho_r[fi]);
+    if (um != 0.0) {  // roeFluxScheme.C:406-408
+      ph -= 0.5 * ms * um * (rho_l[fi] + rho_r[fi]);
+      pU = pU - 0.5 * ms * um * (rhoU_l + rhoU_r);
+      pE -= 0.5 * ms * um * (rhoE_l + rhoE_r);
+    }
     c.phi[fi] = ph;
     c.phiU[fi] = pU;
     c.phiE[fi] = pE;
@@ -918,6 +942,13 @@ void residualSource(Case& c) {
       }
       for (int k = 0; k < 5; ++k) c.src[5 * i + k] = c.src[5 * i + k] + hb[k];
     }
+    if (c.mrfOn) {
+      // addMRFSource: -(omega x rho U) V with rhoU = rho_ * U_ (convectiveFluxScheme.C:123-129)
+      const V3 rU = c.rho[i] * c.U[i];
+      const V3 o = c.mrfOm[i];
+      const V3 cr(o.y * rU.z - o.z * rU.y, o.z * rU.x - o.x * rU.z, o.x * rU.y - o.y * rU.x);
+      for (int k = 0; k < 3; ++k) c.src[5 * i + 1 + k] -= cr[k] * Vc;
+    }
   }
   c.lastRhoL2 = std::sqrt(l2);
 }
@@ -937,7 +968,7 @@ void waveSpeed(const Case& c, std::vector<double>& lam) {
   for (int fi = 0; fi < c.F + c.B; ++fi) {
     const V3 n = SfOf(c, fi) / magSfOf(c, fi);
     const V3 uf(ui[0][fi], ui[1][fi], ui[2][fi]);
-    lam[fi] = ci[fi] + std::fabs(dot(uf, n) - 0.0);
+    lam[fi] = ci[fi] + std::fabs(dot(uf, n) - umOf(c, fi));
   }
 }
 
@@ -982,7 +1013,7 @@ void setCoAndDeltaT(Case& c) {
     if (!pt.is_wall) continue;
     const int o = c.bcell[b];
     const double cc = std::sqrt(c.gamma / psiOf(c, c.T[o]));
-    const double pl = 0.5 * c.bdc[b] * (cc + std::fabs(dot(c.U[o], c.bSf[b] / c.bmagSf[b]) - 0.0));
+    const double pl = 0.5 * c.bdc[b] * (cc + std::fabs(dot(c.U[o], c.bSf[b] / c.bmagSf[b]) - umOf(c, c.F + b)));
     c.rPseudoDeltaT[o] = std::max(c.rPseudoDeltaT[o], pl);
   }
   for (int i = 0; i < c.N; ++i) c.rPseudoDeltaT[i] /= c.pseudoCo[i];
@@ -1052,7 +1083,22 @@ void assembleJacobian(Case& c) {
       c.diag[c.nei[fi]].a[k] -= up;
     }
   }
-  // addDissipationJacobian: lambda = interp(c) + |interp(U).n|, subtracted
+  // MRF: -div(w, u_MRF |S|) on rho, rhoU (x I), rhoE (convectiveFluxScheme.C:477-481;
+  // fvj::div of a face flux, blockFvOperatorsTemplates.C:148-197)
+  if (c.mrfOn) {
+    for (int fi = 0; fi < c.F; ++fi) {
+      const double phm = c.mrfU[fi] * c.magSf[fi];
+      const double up = phm * (1 - c.w[fi]), lo = -phm * c.w[fi];
+      for (int q = 0; q < 5; ++q) {
+        const int k = diagIdx[q];
+        c.upper[fi].a[k] -= up;
+        c.lower[fi].a[k] -= lo;
+        c.diag[c.own[fi]].a[k] -= -lo;
+        c.diag[c.nei[fi]].a[k] -= -up;
+      }
+    }
+  }
+  // addDissipationJacobian: lambda = interp(c) + |interp(U).n - u_MRF|, subtracted
   std::vector<double> lam;
   waveSpeed(c, lam);
   for (int fi = 0; fi < c.F; ++fi) {
@@ -1092,7 +1138,7 @@ void assembleJacobian(Case& c) {
     const V3 SfB = c.bSf[b];
     const double rhoB = rhoBof(c, b);
     const V3 UB = c.UB[b];
-    const double UrelBdotSf = dot(UB, SfB) - 0.0 * c.bmagSf[b];
+    const double UrelBdotSf = dot(UB, SfB) - umOf(c, c.F + b) * c.bmagSf[b];
     const double pB = c.pB[b], TB = c.TB[b];
     const double rhoEB = rhoB * (heOf(c, TB) + 0.5 * magSqr(UB));
     const double cvB = c.Cv;
@@ -1165,6 +1211,20 @@ void assembleJacobian(Case& c) {
   for (int i = 0; i < c.N; ++i) {
     const double dc = c.ddtCoeff[i] * c.V[i];
     for (int q = 0; q < 5; ++q) c.diag[i].a[diagIdx[q]] += dc;
+  }
+  // addMRFSource: skew(omega) V on the momentum block (convectiveFluxScheme.C:131-137)
+  if (c.mrfOn) {
+    for (int i = 0; i < c.N; ++i) {
+      const V3 o = c.mrfOm[i];
+      const double Vc = c.V[i];
+      B5& D = c.diag[i];
+      D(1, 2) -= o.z * Vc;
+      D(1, 3) += o.y * Vc;
+      D(2, 1) += o.z * Vc;
+      D(2, 3) -= o.x * Vc;
+      D(3, 1) -= o.y * Vc;
+      D(3, 2) += o.x * Vc;
+    }
   }
   // viscousFluxScheme::createViscousJacobian, LaxFriedrichJacobian:
   // minus laplacian(0.5 lambda_v, 1) on rho, rhoU (x I), rhoE (viscousFluxScheme.C:234-247)
@@ -1612,6 +1672,15 @@ void correctBoundaryConditions(Case& c, const std::vector<double>& psiB) {
       }
     }
   }
+  // MRF: a fixedValue patch keeps the frame velocity correctBoundaryVelocity
+  // gave it; the HB solver re-assigns every included face here
+  // (dbnsFullyImplicitHBFoam updateFields.H:86-88)
+  if (c.mrfOn)
+    for (int b = 0; b < c.B; ++b) {
+      const int kind = c.patches[c.bpatch[b]].kind;
+      if (c.mrfBIn[b] && (c.mrfEvery || kind == ICS_PATCH_FIXED || kind == ICS_PATCH_ISOTHERMAL_WALL))
+        c.UB[b] = c.mrfBU[b];
+    }
   // T
   for (int b = 0; b < c.B; ++b) {
     const Patch& pt = c.patches[c.bpatch[b]];
@@ -1935,13 +2004,14 @@ int scalarTransportStep(Case& c, ics_solver_perf& perf) {
     const double rS_l = rho_l[fi] * s_l[fi], rS_r = rho_r[fi] * s_r[fi];
     const double coefR = std::sqrt(std::max(VSMALL, rho_r[fi]) / std::max(VSMALL, rho_l[fi]));
     const V3 roeU = (coefR * U_r[fi] + U_l[fi]) / (coefR + 1.0);
-    const double uProj = dot(roeU, n) - 0.0;
+    const double um = umOf(c, fi);
+    const double uProj = dot(roeU, n) - um;
     double lam = std::fabs(uProj);
     const double eps = 0.05 * lam;
     if (lam < eps) lam = (sqr(lam) + sqr(eps)) / (2.0 * eps);
     double ph = -0.5 * ms * lam * (rS_r - rS_l);
     ph += 0.5 * ms * (rho_l[fi] * dot(U_l[fi], n) * s_l[fi] + rho_r[fi] * dot(U_r[fi], n) * s_r[fi]);
-    ph -= 0.5 * ms * 0.0 * (rS_l + rS_r);
+    ph -= 0.5 * ms * um * (rS_l + rS_r);
     phiS[fi] = ph;
   }
   // residual -div(phiSp) [+ laplacian(D, s)] [- physical ddt]
@@ -1997,13 +2067,23 @@ int scalarTransportStep(Case& c, ics_solver_perf& perf) {
     A.diag[c.own[fi]] -= lo;
     A.diag[c.nei[fi]] -= up;
   }
-  // dissipation with lambdaConv = |interpolate(U).n| (internal and boundary faces)
+  // MRF: -div(w, u_MRF |S|) (lines 217-219)
+  if (c.mrfOn)
+    for (int fi = 0; fi < F; ++fi) {
+      const double phm = c.mrfU[fi] * c.magSf[fi];
+      const double up = phm * (1 - c.w[fi]), lo = -phm * c.w[fi];
+      A.upper[fi] -= up;
+      A.lower[fi] -= lo;
+      A.diag[c.own[fi]] -= -lo;
+      A.diag[c.nei[fi]] -= -up;
+    }
+  // dissipation with lambdaConv = |interpolate(U).n - u_MRF| (internal and boundary faces)
   for (int fi = 0; fi < F; ++fi) {
     const int o = c.own[fi], nb = c.nei[fi];
     const double wf = c.w[fi];
     const V3 Uf(wf * (c.U[o].x - c.U[nb].x) + c.U[nb].x, wf * (c.U[o].y - c.U[nb].y) + c.U[nb].y,
                 wf * (c.U[o].z - c.U[nb].z) + c.U[nb].z);
-    const double lc = std::fabs(dot(Uf, c.Sf[fi] / c.magSf[fi]) - 0.0);
+    const double lc = std::fabs(dot(Uf, c.Sf[fi] / c.magSf[fi]) - umOf(c, fi));
     const double d = 0.5 * c.magSf[fi] * lc;
     A.upper[fi] -= d;
     A.lower[fi] -= d;
@@ -2011,14 +2091,14 @@ int scalarTransportStep(Case& c, ics_solver_perf& perf) {
     A.diag[nb] += d;
   }
   for (int b = 0; b < B; ++b) {
-    const double lc = std::fabs(dot(c.UB[b], c.bSf[b] / c.bmagSf[b]) - 0.0);
+    const double lc = std::fabs(dot(c.UB[b], c.bSf[b] / c.bmagSf[b]) - umOf(c, F + b));
     A.diag[c.bcell[b]] += 0.5 * c.bmagSf[b] * lc;
   }
   // geometric boundaries: rho_B (U_B . S_B) valueInternalCoeffs / rho_I
   for (int b = 0; b < B; ++b) {
     const int ci = c.bcell[b];
     const double vic = c.sFixed[c.bpatch[b]] ? 0.0 : 1.0;
-    const double flux = rhoBof(c, b) * (dot(c.UB[b], c.bSf[b]) - 0.0 * c.bmagSf[b]) * vic;
+    const double flux = rhoBof(c, b) * (dot(c.UB[b], c.bSf[b]) - umOf(c, F + b) * c.bmagSf[b]) * vic;
     A.diag[ci] += flux * (1.0 / c.rho[ci]);
   }
   if (viscous) {
@@ -2474,12 +2554,43 @@ int icsref_begin_time_step(ics_handle h) {
     c.rhoS00 = c.timeIndex == 0 ? c.rhoS : c.rhoS0;
     c.rhoS0 = c.rhoS;
   }
+  mrfBoundaryVelocity(c);  // outerLoop.H:6
   c.timeIndex++;
   if (!steady) {
     c.initResValid = false;
     c.prevResValid = false;
   }
   if (c.cfg.reset_pseudo) std::fill(c.pseudoCo.begin(), c.pseudoCo.end(), c.cfg.pseudo_co_num);
+  return ICS_OK;
+}
+
+// MRF zones (the same arrays as ics_set_mrf); omega == NULL switches them off
+int icsref_set_mrf(ics_handle h, const double* omega, const double* face_velocity, const double* boundary_U,
+                   const int32_t* included, int32_t mode) {
+  if (!h) return ICS_ERR_ARG;
+  Case& c = *h;
+  c.mrfOn = false;
+  c.mrfU.clear();
+  c.mrfOm.clear();
+  c.mrfBU.clear();
+  c.mrfBIn.clear();
+  c.haveMatrix = c.haveIncrement = false;
+  if (!omega) return ICS_OK;
+  if (!face_velocity || (c.B > 0 && (!boundary_U || !included)) ||
+      (mode != ICS_MRF_OUTER_LOOP && mode != ICS_MRF_EVERY_UPDATE))
+    return ICS_ERR_ARG;
+  c.mrfU.assign(face_velocity, face_velocity + c.F + c.B);
+  c.mrfOm.resize(c.N);
+  for (int i = 0; i < c.N; ++i) c.mrfOm[i] = V3(omega[3 * i], omega[3 * i + 1], omega[3 * i + 2]);
+  c.mrfBU.resize(c.B);
+  c.mrfBIn.resize(c.B);
+  for (int b = 0; b < c.B; ++b) {
+    c.mrfBU[b] = V3(boundary_U[3 * b], boundary_U[3 * b + 1], boundary_U[3 * b + 2]);
+    c.mrfBIn[b] = included[b];
+  }
+  c.mrfEvery = mode == ICS_MRF_EVERY_UPDATE;
+  c.mrfOn = true;
+  mrfBoundaryVelocity(c);  // createFields.H:262-263
   return ICS_OK;
 }
 

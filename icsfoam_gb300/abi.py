@@ -47,7 +47,7 @@ class IcsError(RuntimeError):
 
 class PatchDesc(C.Structure):
     _fields_ = [("kind", C.c_int32), ("is_wall", C.c_int32), ("p", C.c_double), ("T", C.c_double),
-                ("U", C.c_double * 3), ("p0", C.c_double), ("T0", C.c_double)]
+                ("U", C.c_double * 3), ("p0", C.c_double), ("T0", C.c_double), ("rotation", C.c_double * 9)]
 
 
 class MeshDesc(C.Structure):
@@ -60,6 +60,8 @@ class MeshDesc(C.Structure):
         ("b_cell", C.c_void_p), ("b_patch", C.c_void_p), ("b_Sf", C.c_void_p), ("b_Cf", C.c_void_p),
         ("b_delta_coeffs", C.c_void_p), ("patches", C.POINTER(PatchDesc)),
         ("solution_d", C.c_int32 * 3),
+        ("b_partner", C.c_void_p), ("b_weights", C.c_void_p), ("b_nbr_d", C.c_void_p),
+        ("b_nonorth_delta_coeffs", C.c_void_p),
     ]
 
 
@@ -263,7 +265,15 @@ class CaseHandle:
             for k in range(3):
                 pats[i].U[k] = p.U[k]
             pats[i].p0, pats[i].T0 = p.p0, p.T0
+            R = p.rotation if p.rotation is not None else (1, 0, 0, 0, 1, 0, 0, 0, 1)
+            for k in range(9):
+                pats[i].rotation[k] = R[k]
         self._keep.append(pats)
+        if mesh.b_partner is not None and np.any(mesh.b_partner >= 0):
+            desc.b_partner = keep(mesh.b_partner, np.int32)
+            desc.b_weights = keep(mesh.b_weights, np.float64)
+            desc.b_nbr_d = keep(mesh.b_nbr_d, np.float64)
+            desc.b_nonorth_delta_coeffs = keep(mesh.b_nonorth_delta_coeffs, np.float64)
         desc.patches = pats
         for k in range(3):
             desc.solution_d[k] = mesh.solution_d[k]

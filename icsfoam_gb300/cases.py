@@ -237,17 +237,20 @@ def hb_bump_channel(nx: int = 64, ny: int = 16, nz: int = 4, frequency: float = 
 def annular_sector(nr: int = 32, nt: int = 64, nz: int = 128, r0: float = 0.5, r1: float = 0.6,
                    sector_deg: float = 20.0, length: float = 0.2, mach: float = 0.4, omega: float = 300.0,
                    p0: float = 1.0e5, T0: float = 300.0, ordering_mode: str = "colour", flux: str = "HLLC",
-                   second_order: bool = True) -> Workload:
-    """Axial flow through an annular sector r in [r0, r1], |theta| <= sector/2,
-    z in [0, length]: total-pressure inlet (z = 0), static-pressure outlet,
-    slip hub and shroud walls; the sector's side planes are slip planes (a
-    rotational cyclic pair in a turbomachinery sector).  The cells with z in
-    [length/3, 2 length/3] form a zone rotating at ``omega`` rad/s about the
-    z axis (an MRFProperties zone with its nonRotatingPatches empty).
-    Cell index order: i radial, j circumferential, k axial."""
+                   second_order: bool = True, sides: str = "cyclic", theta0_deg: Optional[float] = None) -> Workload:
+    """Axial flow through an annular sector r in [r0, r1], theta in
+    [theta0, theta0 + sector] (theta0 = -sector/2 by default), z in [0,
+    length]: total-pressure inlet (z = 0), static-pressure outlet, slip hub
+    and shroud walls; the sector's side planes are a rotational cyclic pair
+    (``sides="cyclic"``: "sideA" at theta0 couples to "sideB" rotated by
+    -sector about z) or slip planes (``sides="slip"``, patch "sides").  The
+    cells with z in [length/3, 2 length/3] form a zone rotating at ``omega``
+    rad/s about the z axis (an MRFProperties zone; the cyclic sides are its
+    coupled patches).  Cell index order: i radial, j circumferential, k axial."""
     from . import mrf as MRF
     rs = np.linspace(r0, r1, nr + 1)
-    th = np.radians(np.linspace(-0.5 * sector_deg, 0.5 * sector_deg, nt + 1))
+    t0 = -0.5 * sector_deg if theta0_deg is None else theta0_deg
+    th = np.radians(np.linspace(t0, t0 + sector_deg, nt + 1))
     zs = np.linspace(0.0, length, nz + 1)
     g = np.zeros((nr + 1, nt + 1, nz + 1, 3))
     g[..., 0] = rs[:, None, None] * np.cos(th)[None, :, None]
@@ -260,8 +263,13 @@ def annular_sector(nr: int = 32, nt: int = 64, nz: int = 128, r0: float = 0.5, r
     outlet = M.Patch("outlet", M.PATCH_PRESSURE_OUTLET, p=p_static)
     hub = M.Patch("hub", M.PATCH_SLIP, is_wall=True)
     shroud = M.Patch("shroud", M.PATCH_SLIP, is_wall=True)
-    side = M.Patch("sides", M.PATCH_SLIP)
-    sides = {"xmin": hub, "xmax": shroud, "ymin": side, "ymax": side, "zmin": inlet, "zmax": outlet}
+    if sides == "cyclic":
+        sa, sb = M.cyclic_pair("sideA", "sideB", (0.0, 0.0, 1.0), -sector_deg)
+        coupled = ("sideA", "sideB")
+    else:
+        sa = sb = M.Patch("sides", M.PATCH_SLIP)
+        coupled = ()
+    sides = {"xmin": hub, "xmax": shroud, "ymin": sa, "ymax": sb, "zmin": inlet, "zmax": outlet}
     mesh = M.hex_mesh(g, sides)
     mesh = ordering.apply(mesh, ordering_mode)
     N = mesh.n_cells
@@ -270,13 +278,14 @@ def annular_sector(nr: int = 32, nt: int = 64, nz: int = 128, r0: float = 0.5, r
     U[:, 2] = mach * c
     zc = mesh.C[:, 2]
     rotor = (zc > length / 3.0) & (zc < 2.0 * length / 3.0)
-    zone = MRF.RotatingZone(cells=rotor, origin=(0.0, 0.0, 0.0), axis=(0.0, 0.0, 1.0), omega=omega)
+    zone = MRF.RotatingZone(cells=rotor, origin=(0.0, 0.0, 0.0), axis=(0.0, 0.0, 1.0), omega=omega,
+                            coupled_patches=coupled)
     rec = 3 if second_order else 0
     settings = dict(thermo_settings(), flux_scheme={"AUSMPlusUp": 0, "HLLC": 1, "ROE": 2}[flux],
                     recon_rho=rec, recon_U=rec, recon_T=rec, ddt_scheme=0, pseudo_co_num=1.0,
                     pseudo_co_num_max=200.0, n_directions=8, max_iter=5, tolerance=1e-12, rel_tol=1e-2,
                     pseudo_tol=1e-30, pseudo_tol_rel=1e-30)
-    return Workload("annulus_%dx%dx%d" % (nr, nt, nz), mesh, np.full(N, p_static), U, np.full(N, T_static),
+    return Workload("annulus_%dx%dx%d%s" % (nr, nt, nz, "" if sides == "cyclic" else "_slip"), mesh, np.full(N, p_static), U, np.full(N, T_static),
                     settings, mrf=([zone], []))
 
 

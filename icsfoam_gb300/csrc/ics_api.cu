@@ -98,7 +98,8 @@ void free_all(Handle& h) {
                   m.bface, m.slot_base, m.scol, m.sface, m.nlow, m.nslot, m.fl_cells, m.rl_cells, m.fl_lptr,
                   m.rl_lptr, m.sweep_flag, m.sweep_ticket, h.W, h.W0, h.W00, h.Wprev, h.prim, h.pB, h.TB, h.UB, h.phiB, h.pseudoCo, h.rPDT,
                   h.ddtCoeff, h.q, h.bq, h.clin, h.grad, h.fflux, h.frec, h.flam, h.bjac, h.src, h.vcell,
-                  h.fvisc, h.vsf2, m.dc, m.Dhb, m.mrfU, m.mrfOm, m.mrfBU, m.mrfBIn, h.tW, h.tprim, h.tq, h.tgrad, h.tflux, h.tvc, h.tfv, h.tv,
+                  h.fvisc, h.vsf2, m.dc, m.Dhb, m.mrfU, m.mrfOm, m.mrfBU, m.mrfBIn, m.bpartner, m.bw, m.bdelta, m.bdNei,
+                  m.bnodc, m.cyc_face, m.cyc_row, m.cyc_ptr, h.cblk, h.cfrec, h.tW, h.tprim, h.tq, h.tgrad, h.tflux, h.tvc, h.tfv, h.tv,
                   h.ss, h.ssB, h.srhoS, h.srhoS0, h.srhoS00, h.sgrad, h.sgradL, h.sface, h.sblk, h.sdg, h.srD,
                   h.ssrc, h.sFixed, h.sValue,
                   h.blk, h.dg,
@@ -279,10 +280,59 @@ void build_mesh(Handle& h, const ics_mesh_desc* d) {
     for (int k = 0; k < 3; ++k) pts[p].U[k] = q.U[k];
     pts[p].p0 = q.p0;
     pts[p].T0 = q.T0;
-    if (q.kind < 0 || q.kind > ICS_PATCH_ISOTHERMAL_WALL) throw std::string("unknown patch kind");
+    for (int k = 0; k < 9; ++k) pts[p].R[k] = q.rotation[k];
+    if (q.kind < 0 || q.kind > ICS_PATCH_CYCLIC) throw std::string("unknown patch kind");
   }
   m.patches = upload(pts);
   m.npatches = d->n_patches;
+  // coupled (cyclic) faces
+  {
+    std::vector<int> cycFaces;
+    for (int b = 0; b < B; ++b)
+      if (d->patches[d->b_patch[b]].kind == ICS_PATCH_CYCLIC) cycFaces.push_back(b);
+    if (!cycFaces.empty()) {
+      if (!d->b_partner || !d->b_weights || !d->b_nbr_d)
+        throw std::string("cyclic patches need b_partner, b_weights and b_nbr_d");
+      std::vector<int> partner(B, -1);
+      std::vector<double> w(B, 1.0), delta(3 * (size_t)B, 0.0), nbrd(3 * (size_t)B, 0.0), nodc(B);
+      for (int b = 0; b < B; ++b) nodc[b] = d->b_nonorth_delta_coeffs ? d->b_nonorth_delta_coeffs[b] : d->b_delta_coeffs[b];
+      for (int b : cycFaces) {
+        const int pc = d->b_partner[b];
+        if (pc < 0 || pc >= N) throw std::string("cyclic face partner cell out of range");
+        const double wb = d->b_weights[b];
+        if (!(wb > 0.0 && wb < 1.0)) throw std::string("cyclic face weight outside (0, 1)");
+        partner[b] = pc;
+        w[b] = wb;
+        for (int k = 0; k < 3; ++k) {
+          const double nd = d->b_nbr_d[3 * b + k];
+          nbrd[(size_t)k * B + b] = nd;
+          delta[(size_t)k * B + b] = bdOwn[(size_t)k * B + b] - nd;
+        }
+      }
+      // grouped by the owning cell for the row-owner coupling product
+      std::stable_sort(cycFaces.begin(), cycFaces.end(),
+                       [&](int a, int b2) { return d->b_cell[a] < d->b_cell[b2]; });
+      std::vector<int> rows, ptr(1, 0);
+      for (size_t i = 0; i < cycFaces.size(); ++i) {
+        const int c = d->b_cell[cycFaces[i]];
+        if (rows.empty() || rows.back() != c) {
+          if (!rows.empty()) ptr.push_back((int)i);
+          rows.push_back(c);
+        }
+      }
+      ptr.push_back((int)cycFaces.size());
+      m.bpartner = upload(partner);
+      m.bw = upload(w);
+      m.bdelta = upload(delta);
+      m.bdNei = upload(nbrd);
+      m.bnodc = upload(nodc);
+      m.ncyc = (int)cycFaces.size();
+      m.ncrow = (int)rows.size();
+      m.cyc_face = upload(cycFaces);
+      m.cyc_row = upload(rows);
+      m.cyc_ptr = upload(ptr);
+    }
+  }
   // cell -> faces CSR in face order
   std::vector<int> cnt(N + 1, 0);
   for (int f = 0; f < F; ++f) {
@@ -420,6 +470,10 @@ void alloc_state(Handle& h) {
   h.fflux = dalloc<double>(5ull * (F + B));
   h.frec = dalloc<double>(8ull * F);
   h.flam = dalloc<double>((size_t)F + B);
+  if (h.m.ncyc) {
+    h.cfrec = dalloc<double>(8ull * h.m.ncyc);
+    h.cblk = dalloc<double>(25ull * h.m.ncyc);  // FP64 size; FP32 blocks use half
+  }
   h.bjac = dalloc<double>(25ull * B);
   h.src = dalloc<double>(5ull * N);
   h.dW = dalloc<double>(5ull * N);
@@ -665,6 +719,7 @@ int ics_create(const ics_mesh_desc* mesh, const ics_config* cfg, ics_handle* out
   st = guard(hh, [&](Handle& hd) {
     ICS_CUDA(cudaStreamCreateWithFlags(&hd.stream, cudaStreamNonBlocking));
     build_mesh(hd, mesh);
+    if (hd.m.ncyc > 0 && cfg->viscous) throw std::string("viscous terms across cyclic patches are not built");
     alloc_state(hd);
     ensure_workspace(hd);
     std::vector<double> co(hd.m.N, cfg->pseudo_co_num);
@@ -697,6 +752,10 @@ int ics_set_config(ics_handle hh, const ics_config* cfg) {
   }
   if (hh->h.m.nInst > 1 && (cfg->ddt_scheme != ICS_DDT_STEADY || cfg->solver != ICS_SOLVER_GMRES)) {
     hh->h.err = "Harmonic Balance needs steadyState ddt and the GMRES solver";
+    return ICS_ERR_ARG;
+  }
+  if (hh->h.m.ncyc > 0 && cfg->viscous) {
+    hh->h.err = "viscous terms across cyclic patches are not built";
     return ICS_ERR_ARG;
   }
   return guard(hh, [&](Handle& h) {
@@ -1274,6 +1333,10 @@ int ics_scalar_enable(ics_handle hh, const double* s, const int32_t* patch_fixed
   if (!hh || !s || recon < 0 || recon > ICS_RECON_MUSCL_MINMOD || !(D >= 0)) return ICS_ERR_ARG;
   if (hh->h.m.nInst > 1) {
     hh->h.err = "scalar transport is not provided for Harmonic Balance handles";
+    return ICS_ERR_ARG;
+  }
+  if (hh->h.m.ncyc > 0) {
+    hh->h.err = "scalar transport across cyclic patches is not built";
     return ICS_ERR_ARG;
   }
   return guard(hh, [&](Handle& h) {

@@ -56,6 +56,7 @@ struct KrylovScalars {
 struct Patch {
   int kind, is_wall;
   double p, T, U[3], p0, T0;
+  double R[9];  // cyclic: partner-side vectors into this patch's frame
 };
 
 struct DevMesh {
@@ -114,6 +115,20 @@ struct DevMesh {
   // . n per internal then boundary face [F+B], rotation vector per cell
   // [3][N], frame velocity of the boundary faces [3][B] and where it is
   // assigned [B]; mrfEvery re-assigns it after every boundary update
+  // coupled (cyclic) boundary faces: partner cell [B] (-1 elsewhere),
+  // weights [B], delta (partner centre seen from this side minus C) [3][B],
+  // partner-side displacement Cf - C - delta [3][B], nonOrthDeltaCoeffs [B];
+  // the cyclic faces grouped by cell (cyc_face, in increasing cell order) and
+  // the rows that own them (cyc_row with cyc_ptr into cyc_face)
+  int* bpartner = nullptr;
+  double* bw = nullptr;
+  double* bdelta = nullptr;
+  double* bdNei = nullptr;
+  double* bnodc = nullptr;
+  int ncyc = 0, ncrow = 0;
+  int* cyc_face = nullptr;
+  int* cyc_row = nullptr;
+  int* cyc_ptr = nullptr;
   double* mrfU = nullptr;
   double* mrfOm = nullptr;
   double* mrfBU = nullptr;
@@ -153,6 +168,8 @@ struct Handle {
   double* fflux = nullptr;  // [5][F+B]
   double* frec = nullptr;   // [8][F]: ULx,ULy,ULz,URx,URy,URz,EL,ER
   double* flam = nullptr;   // [F+B]
+  double* cfrec = nullptr;  // [8][ncyc]: the reconstructed states of the cyclic faces (as frec)
+  void* cblk = nullptr;     // [ncyc][25] cyclic coupling blocks (partner rotation folded in)
   double* bjac = nullptr;   // [25][B] boundary Jacobian diag contribution
   double* src = nullptr;    // [N][5] source = R*V
   // viscous terms (allocated when the case is viscous)

@@ -109,11 +109,23 @@ void build_exact_pattern(Handle& h) {
     ICS_CUDA(cudaMemcpy(own.data(), h.m.own, F * sizeof(int), cudaMemcpyDeviceToHost));
     ICS_CUDA(cudaMemcpy(nei.data(), h.m.nei, F * sizeof(int), cudaMemcpyDeviceToHost));
   }
-  std::vector<int> aptr(N + 1, 0), adj(2 * (size_t)F);
+  // cyclic faces couple their cell with the partner cell (each pair of
+  // faces gives both directions)
+  std::vector<int> cyc(h.m.ncyc), bcell, bpart;
+  if (h.m.ncyc) {
+    const int B = h.m.B;
+    bcell.resize(B);
+    bpart.resize(B);
+    ICS_CUDA(cudaMemcpy(cyc.data(), h.m.cyc_face, h.m.ncyc * sizeof(int), cudaMemcpyDeviceToHost));
+    ICS_CUDA(cudaMemcpy(bcell.data(), h.m.bcell, B * sizeof(int), cudaMemcpyDeviceToHost));
+    ICS_CUDA(cudaMemcpy(bpart.data(), h.m.bpartner, B * sizeof(int), cudaMemcpyDeviceToHost));
+  }
+  std::vector<int> aptr(N + 1, 0), adj(2 * (size_t)F + cyc.size());
   for (int f = 0; f < F; ++f) {
     aptr[own[f] + 1]++;
     aptr[nei[f] + 1]++;
   }
+  for (int b : cyc) aptr[bcell[b] + 1]++;
   for (int c = 0; c < N; ++c) aptr[c + 1] += aptr[c];
   {
     std::vector<int> fill(aptr.begin(), aptr.end() - 1);
@@ -121,6 +133,7 @@ void build_exact_pattern(Handle& h) {
       adj[fill[own[f]]++] = nei[f];
       adj[fill[nei[f]]++] = own[f];
     }
+    for (int b : cyc) adj[fill[bcell[b]]++] = bpart[b];
   }
   const int nI = h.m.nInst, Nc = h.m.Nc;
   std::vector<int> ptr(N + 1, 0), col;

@@ -60,6 +60,7 @@ __global__ void k_jac_boundary(DevMesh m, double R, double Cv, double gamma, con
                                double* __restrict__ bjac) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= m.B) return;
+  if (m.bpartner && m.bpartner[b] >= 0) return;  // cyclic faces: k_jac_cyclic
   const int B = m.B, N = m.N;
   const Patch pt = m.patches[m.bpatch[b]];
   const int ci = m.bcell[b];
@@ -146,6 +147,65 @@ __global__ void k_jac_boundary(DevMesh m, double R, double Cv, double gamma, con
   const double d = 0.5 * bm * flam[m.F + b];
   for (int q = 0; q < 5; ++q) D[6 * q] += d;
   for (int k = 0; k < 25; ++k) bjac[k * B + b] = D[k];
+}
+
+// Cyclic faces: the coupled part of insertBlock (diag += 0.5|S| A_L, the
+// interface block 0.5|S| A_R), of -div(w, u_MRF |S|) (diag -= phi w, the
+// interface -= phi (1-w)) and of insertDissipationBlock (diag += 0.5|S|
+// lambda, the interface -= the same) -- no boundary-condition terms on a
+// coupled patch (blockFvMatrix.C:211-326, convectiveFluxScheme.C:219-232).
+// The interface block multiplies the partner's unknowns with their momentum
+// rotated into this side's frame (Amul: patchNeighbourField of psi,
+// blockFvMatrix.C:386-407), so the stored block is U_f diag(1, R, 1).
+template <typename T>
+__global__ void k_jac_cyclic(DevMesh m, double gamma, const double* __restrict__ cfrec,
+                             const double* __restrict__ flam, double* __restrict__ bjac, T* __restrict__ cblk) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m.ncyc) return;
+  const int B = m.B, nc = m.ncyc;
+  const int b = m.cyc_face[i];
+  const double* R = m.patches[m.bpatch[b]].R;
+  const double n[3] = {m.bnf[b], m.bnf[B + b], m.bnf[2 * B + b]};
+  const double UL[3] = {cfrec[i], cfrec[nc + i], cfrec[2 * nc + i]};
+  const double UR[3] = {cfrec[3 * nc + i], cfrec[4 * nc + i], cfrec[5 * nc + i]};
+  EulerJ<double> AL, AR;
+  AL.init(gamma, UL, cfrec[6 * nc + i], n);
+  AR.init(gamma, UR, cfrec[7 * nc + i], n);
+  const double magS = m.bmagSf[b];
+  const double hs = 0.5 * magS;
+  const double d = 0.5 * magS * flam[m.F + b];
+  double phm = 0.0;
+  if (m.mrfU) phm = m.mrfU[m.F + b] * magS;
+  const double wb = m.bw[b];
+  double D[25], U[25];
+#pragma unroll
+  for (int r = 0; r < 5; ++r)
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      const int k = 5 * r + c;
+      double dg = -(-0.5 * magS * AL.entry(r, c));
+      double up = hs * AR.entry(r, c);
+      if (r == c) {
+        dg -= phm * wb;
+        up -= phm * (1.0 - wb);
+        dg += d;
+        up -= d;
+      }
+      D[k] = dg;
+      U[k] = up;
+    }
+#pragma unroll
+  for (int k = 0; k < 25; ++k) bjac[k * B + b] = D[k];
+  T* out = cblk + (size_t)i * 25;
+#pragma unroll
+  for (int r = 0; r < 5; ++r) {
+    out[5 * r] = T(U[5 * r]);
+    out[5 * r + 4] = T(U[5 * r + 4]);
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      out[5 * r + 1 + c] =
+          T(U[5 * r + 1] * R[c] + U[5 * r + 2] * R[3 + c] + U[5 * r + 3] * R[6 + c]);
+  }
 }
 
 // Row assembly.  T = block storage/compute type.
@@ -319,6 +379,14 @@ void launch_jacobian(Handle& h) {
     ICS_LAUNCH(h, ICS_K_JAC_BOUNDARY, k_jac_boundary<<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, h.cfg.c.R, h.cfg.Cv, h.cfg.gamma, h.W, h.prim,
                                                                 h.pB, h.TB, h.UB, h.phiB, h.flam, h.bjac));
   int* status = &h.ks->status;
+  if (h.m.ncyc > 0) {
+    if (prec(h) == ICS_PREC_MIXED)
+      ICS_LAUNCH(h, ICS_K_JAC_BOUNDARY, k_jac_cyclic<float><<<grid_for(h.m.ncyc, 128), 128, 0, h.stream>>>(
+                                            h.m, h.cfg.gamma, h.cfrec, h.flam, h.bjac, (float*)h.cblk));
+    else
+      ICS_LAUNCH(h, ICS_K_JAC_BOUNDARY, k_jac_cyclic<double><<<grid_for(h.m.ncyc, 128), 128, 0, h.stream>>>(
+                                            h.m, h.cfg.gamma, h.cfrec, h.flam, h.bjac, (double*)h.cblk));
+  }
   if (prec(h) == ICS_PREC_MIXED) {
     ICS_LAUNCH(h, ICS_K_JAC_ROWS, k_jac_rows<float><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, h.cfg.gamma, h.frec, h.flam, h.bjac,
                                                                    h.ddtCoeff, (float*)h.blk, (float*)h.dg,

@@ -166,6 +166,36 @@ __global__ void __launch_bounds__(128) k_spmv(DevMesh m, const TB* __restrict__ 
   for (int k = 0; k < 5; ++k) y[5 * c + k] = acc[k];
 }
 
+// Cyclic couplings (the interface part of Amul, blockFvMatrix.C:386-407):
+// y_c += sum over the cyclic faces of c of B_f x_partner, B_f holding the
+// partner's rotation; one thread per row that owns cyclic faces, after k_spmv.
+template <typename TB, typename TV>
+__global__ void __launch_bounds__(128) k_cyc_mv(DevMesh m, const TB* __restrict__ cblk, const TV* __restrict__ x,
+                                                TV* __restrict__ y) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= m.ncrow) return;
+  const int c = m.cyc_row[r];
+  TV acc[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) acc[k] = y[5 * c + k];
+  for (int e = m.cyc_ptr[r]; e < m.cyc_ptr[r + 1]; ++e) {
+    const int pc = m.bpartner[m.cyc_face[e]];
+    const TB* Bk = cblk + (size_t)e * 25;
+    TV xj[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) xj[k] = x[5 * pc + k];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      TV a = TV(0);
+#pragma unroll
+      for (int j = 0; j < 5; ++j) a += TV(Bk[5 * i + j]) * xj[j];
+      acc[i] += a;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 5; ++k) y[5 * c + k] = acc[k];
+}
+
 // ------------------------------------- fused A x + LU-SGS (two-level schedule)
 // On a schedule of two levels where the first holds the rows without lower
 // neighbours and the second the rows without upper neighbours (the
@@ -832,6 +862,8 @@ __global__ void __launch_bounds__(RB) k_sumsq(int N, const double* __restrict__ 
 template <typename TB, typename TV>
 static void spmv_t(Handle& h, const TV* x, TV* y) {
   ICS_LAUNCH(h, ICS_K_SPMV, k_spmv<TB, TV><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, (const TB*)h.blk, (const TB*)h.dg, x, y));
+  if (h.m.ncrow > 0)
+    ICS_LAUNCH(h, ICS_K_SPMV, k_cyc_mv<TB, TV><<<grid_for(h.m.ncrow, 128), 128, 0, h.stream>>>(h.m, (const TB*)h.cblk, x, y));
 }
 
 
@@ -906,8 +938,9 @@ static void lusgs_t(Handle& h, TV* r) {
 template <typename TB, typename TV>
 static bool fused_op_available(const Handle& h) {
   const DevMesh& m = h.m;
+  // (the fused passes carry no cyclic couplings: those meshes take spmv_t)
   return h.cfg.c.preconditioner == ICS_PC_LUSGS && m.nfl == 2 && m.nrl == 2 && m.fuse_last &&
-         (long)m.N >= 2048L * m.nfl;
+         (long)m.N >= 2048L * m.nfl && m.ncyc == 0;
 }
 
 // vout != nullptr: x is unnormalised; v = x / beta is stored in vout and

@@ -134,6 +134,10 @@ extern "C" int ics_linear_residual_noalloc(ics_handle hh, const double* x, doubl
     h.err = "linear_residual_noalloc: Harmonic Balance coupling is not provided";
     return ICS_ERR_ARG;
   }
+  if (h.m.ncyc > 0) {
+    h.err = "linear_residual_noalloc: cyclic couplings are not provided";
+    return ICS_ERR_ARG;
+  }
   if ((long)h.m.N > NOALLOC_MAX_CELLS) {
     char buf[160];
     std::snprintf(buf, sizeof(buf), "linear_residual_noalloc: %d cells exceed the fixed scratch capacity of %ld cells",

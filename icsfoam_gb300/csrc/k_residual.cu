@@ -139,6 +139,27 @@ __global__ void __launch_bounds__(128) k_grad(DevMesh m, const Real* __restrict_
   for (int e = b0; e < b1; ++e) {
     const int b = m.bface[e];
     const double S0 = m.bSf[b], S1 = m.bSf[B + b], S2 = m.bSf[2 * B + b];
+    const int pc = m.bpartner ? m.bpartner[b] : -1;
+    if (pc >= 0) {
+      // cyclic face: linear interpolation with the partner cell, whose value
+      // also bounds the limiter (gaussGrad / cellLimitedGrad on a coupled
+      // patch; a scalar field's neighbour values are not rotated)
+      const double wb = m.bw[b];
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) {
+        if (!((mask >> k) & 1)) continue;
+        const Real qn = q[k * N + pc];
+        const Real sf = wb * (qc[k] - qn) + qn;
+        g[k][0] = g[k][0] + S0 * sf;
+        g[k][1] = g[k][1] + S1 * sf;
+        g[k][2] = g[k][2] + S2 * sf;
+        if (LIMITED) {
+          qmax[k] = fmax(qmax[k], qn);
+          qmin[k] = fmin(qmin[k], qn);
+        }
+      }
+      continue;
+    }
 #pragma unroll
     for (int k = 0; k < NQ; ++k) {
       if (!((mask >> k) & 1)) continue;
@@ -348,6 +369,7 @@ __global__ void k_bface(DevMesh m, ResParams P, const double* __restrict__ bq, c
                         double* __restrict__ phiB, int FB) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= m.B) return;
+  if (m.bpartner && m.bpartner[b] >= 0) return;  // cyclic faces: k_cface
   const int B = m.B, F = m.F;
   double qb[NQ];
 #pragma unroll
@@ -368,6 +390,116 @@ __global__ void k_bface(DevMesh m, ResParams P, const double* __restrict__ bq, c
   for (int k = 0; k < 5; ++k) fflux[k * FB + F + b] = out[k];
   phiB[b] = out[0];
   flam[F + b] = bclin[b] + fabs(dot3(L.U, n) - um);
+}
+
+// Reconstruction on a cyclic face between this side's cell o and the
+// partner cell pc: linearUpwind / limitedScheme on a coupled patch.  The
+// partner's value enters as it is (the fields reconstructed here are scalar
+// fields, U component by component); its gradient vector is rotated into
+// this side's frame (patchNeighbourField of the gradient); the partner side
+// extrapolates along Cf - C - delta, the TVD ratio uses delta.
+template <typename Real>
+__device__ __forceinline__ Real reconstruct_cyc(const DevMesh& m, int scheme, int k, int b, int o, int pc,
+                                                const Real& qo, const Real& qn, const Real* __restrict__ grad,
+                                                const double* R, double dir) {
+  const int N = m.N, B = m.B;
+  const double wUp = dir > 0 ? 1.0 : 0.0;
+  if (scheme == ICS_RECON_UPWIND) return wUp * (qo - qn) + qn;
+  Real g0, g1, g2;
+  if (dir > 0) {
+    g0 = grad[(3 * k) * N + o];
+    g1 = grad[(3 * k + 1) * N + o];
+    g2 = grad[(3 * k + 2) * N + o];
+  } else {
+    const Real a0 = grad[(3 * k) * N + pc], a1 = grad[(3 * k + 1) * N + pc], a2 = grad[(3 * k + 2) * N + pc];
+    g0 = R[0] * a0 + R[1] * a1 + R[2] * a2;
+    g1 = R[3] * a0 + R[4] * a1 + R[5] * a2;
+    g2 = R[6] * a0 + R[7] * a1 + R[8] * a2;
+  }
+  if (scheme == ICS_RECON_VANLEER || scheme == ICS_RECON_MINMOD) {
+    const Real gradf = qn - qo;
+    const Real gradcf = m.bdelta[b] * g0 + m.bdelta[B + b] * g1 + m.bdelta[2 * B + b] * g2;
+    Real r;
+    if (fabs(gradcf) >= 1000 * fabs(gradf))
+      r = 2 * 1000 * (gradcf >= 0 ? 1.0 : -1.0) * (gradf >= 0 ? 1.0 : -1.0) - 1.0;
+    else
+      r = 2 * (gradcf / gradf) - 1;
+    Real lim;
+    if (scheme == ICS_RECON_VANLEER)
+      lim = (r + fabs(r)) / (1 + fabs(r));
+    else
+      lim = fmax(fmin(fmin(r, 1.0), 2.0), 0.0);
+    const Real wgt = lim * m.bw[b] + (1.0 - lim) * wUp;
+    return wgt * (qo - qn) + qn;
+  }
+  const double* d = dir > 0 ? m.bdOwn : m.bdNei;
+  const Real base = wUp * (qo - qn) + qn;
+  return base + (d[b] * g0 + d[B + b] * g1 + d[2 * B + b] * g2);
+}
+
+// Flux through the cyclic faces (one thread per face of the list); writes
+// the face flux, the boundary mass flux, the wave speed with the coupled
+// linear interpolation (velocity rotated: fvc::interpolate of a vector
+// field) and the reconstructed states for the Jacobian.
+template <typename Real = double, bool MRF = false>
+__global__ void __launch_bounds__(128) k_cface(DevMesh m, ResParams P, const Real* __restrict__ q,
+                                               const Real* __restrict__ grad, const double* __restrict__ clin,
+                                               Real* __restrict__ fflux, double* __restrict__ cfrec,
+                                               double* __restrict__ flam, double* __restrict__ phiB, int FB) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m.ncyc) return;
+  const int N = m.N, F = m.F, B = m.B, nc = m.ncyc;
+  const int b = m.cyc_face[i];
+  const int o = m.bcell[b], pc = m.bpartner[b];
+  const double* R = m.patches[m.bpatch[b]].R;
+  Real qL[NQ], qR[NQ];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    if (P.scheme == ICS_FLUX_ROE && k == Q_C) {
+      qL[k] = qR[k] = 0.0;
+      continue;
+    }
+    const Real qo = q[k * N + o], qn = q[k * N + pc];
+    const int sch = recon_of(P, k);
+    qL[k] = reconstruct_cyc(m, sch, k, b, o, pc, qo, qn, grad, R, +1.0);
+    qR[k] = reconstruct_cyc(m, sch, k, b, o, pc, qo, qn, grad, R, -1.0);
+  }
+  FStateT<Real> L{qL[Q_RHO], qL[Q_P], {qL[Q_UX], qL[Q_UY], qL[Q_UZ]}, qL[Q_E], qL[Q_H], qL[Q_C]};
+  FStateT<Real> Rs{qR[Q_RHO], qR[Q_P], {qR[Q_UX], qR[Q_UY], qR[Q_UZ]}, qR[Q_E], qR[Q_H], qR[Q_C]};
+  const double S[3] = {m.bSf[b], m.bSf[B + b], m.bSf[2 * B + b]};
+  const double n[3] = {m.bnf[b], m.bnf[B + b], m.bnf[2 * B + b]};
+  const double magS = m.bmagSf[b];
+  const double um = MRF ? m.mrfU[F + b] : 0.0;
+  Real out[5];
+  if (P.scheme == ICS_FLUX_AUSMPLUSUP)
+    flux_ausm(L, Rs, S, magS, P.lowMach, um, out);
+  else if (P.scheme == ICS_FLUX_HLLC)
+    flux_hllc(L, Rs, n, magS, P.gamma, um, out);
+  else
+    flux_roe(L, Rs, n, magS, P.gamma, P.entropyFix, um, out);
+#pragma unroll
+  for (int k = 0; k < 5; ++k) fflux[k * FB + F + b] = out[k];
+  if constexpr (is_fp64<Real>) {
+    phiB[b] = out[0];
+    cfrec[0 * nc + i] = qL[Q_UX];
+    cfrec[1 * nc + i] = qL[Q_UY];
+    cfrec[2 * nc + i] = qL[Q_UZ];
+    cfrec[3 * nc + i] = qR[Q_UX];
+    cfrec[4 * nc + i] = qR[Q_UY];
+    cfrec[5 * nc + i] = qR[Q_UZ];
+    cfrec[6 * nc + i] = qL[Q_E];
+    cfrec[7 * nc + i] = qR[Q_E];
+    const double wb = m.bw[b];
+    const double ci = wb * (clin[o] - clin[pc]) + clin[pc];
+    const double Up[3] = {q[Q_UX * N + pc], q[Q_UY * N + pc], q[Q_UZ * N + pc]};
+    double ui[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double rp = R[3 * k] * Up[0] + R[3 * k + 1] * Up[1] + R[3 * k + 2] * Up[2];
+      ui[k] = wb * (q[(Q_UX + k) * N + o] - rp) + rp;
+    }
+    flam[F + b] = ci + fabs(dot3(ui, n) - um);
+  }
 }
 
 // ------------------------------------------------------------ cell residual
@@ -442,7 +574,10 @@ __global__ void __launch_bounds__(128) k_cellres(DevMesh m, CellResParams D, con
     const int b = m.bface[e];
 #pragma unroll
     for (int k = 0; k < 5; ++k) dv[k] += fflux[k * FB + F + b];
-    if (m.patches[m.bpatch[b]].is_wall) {
+    if (m.bpartner && m.bpartner[b] >= 0) {
+      // coupled face: nonOrthDeltaCoeffs lambda as for an internal face (setCoAndDeltaT.H:73-87)
+      rmax = fmax(rmax, m.bnodc[b] * flam[F + b]);
+    } else if (m.patches[m.bpatch[b]].is_wall) {
       const double U0 = prim[2 * N + c], U1 = prim[3 * N + c], U2 = prim[4 * N + c];
       const double bm = m.bmagSf[b];
       const double un = U0 * (m.bSf[b] / bm) + U1 * (m.bSf[B + b] / bm) + U2 * (m.bSf[2 * B + b] / bm);
@@ -597,6 +732,14 @@ void launch_face_flux(Handle& h) {
   if (h.m.B > 0)
     ICS_LAUNCH(h, ICS_K_BFACE, k_bface<<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, P, h.bq, h.clin + h.m.N, h.m.bnf, h.fflux,
                                                          h.flam, h.phiB, FB));
+  if (h.m.ncyc > 0) {
+    if (h.m.mrfU)
+      ICS_LAUNCH(h, ICS_K_BFACE, (k_cface<double, true><<<grid_for(h.m.ncyc, 128), 128, 0, h.stream>>>(
+                                     h.m, P, h.q, h.grad, h.clin, h.fflux, h.cfrec, h.flam, h.phiB, FB)));
+    else
+      ICS_LAUNCH(h, ICS_K_BFACE, (k_cface<double, false><<<grid_for(h.m.ncyc, 128), 128, 0, h.stream>>>(
+                                     h.m, P, h.q, h.grad, h.clin, h.fflux, h.cfrec, h.flam, h.phiB, FB)));
+  }
   ICS_CUDA(cudaGetLastError());
 }
 
@@ -655,6 +798,13 @@ __global__ void __launch_bounds__(128) k_src_tangent(DevMesh m, double dgPhys, c
       dv[k] = code >= 0 ? dv[k] + t : dv[k] - t;
     }
   }
+  if (m.bpartner)
+    for (int e = m.bptr[c]; e < m.bptr[c + 1]; ++e) {
+      const int b = m.bface[e];
+      if (m.bpartner[b] < 0) continue;
+#pragma unroll
+      for (int k = 0; k < 5; ++k) dv[k] += fflux[k * FB + m.F + b].d;
+    }
   double r[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) r[k] = -dv[k];
@@ -730,6 +880,14 @@ void launch_residual_tangent(Handle& h, const double* v, double* out) {
       ICS_LAUNCH(h, ICS_K_TANGENT, k_face<Dual><<<grid_for(h.m.F, 128), 128, 0, h.stream>>>(h.m, P, tq, tgrad, nullptr,
                                                                                             h.m.nf, tflux, nullptr,
                                                                                             nullptr, FB));
+  }
+  if (h.m.ncyc > 0) {  // the cyclic faces depend on the cells of both sides
+    if (h.m.mrfU)
+      ICS_LAUNCH(h, ICS_K_TANGENT, (k_cface<Dual, true><<<grid_for(h.m.ncyc, 128), 128, 0, h.stream>>>(
+                                       h.m, P, tq, tgrad, nullptr, tflux, nullptr, nullptr, nullptr, FB)));
+    else
+      ICS_LAUNCH(h, ICS_K_TANGENT, (k_cface<Dual, false><<<grid_for(h.m.ncyc, 128), 128, 0, h.stream>>>(
+                                       h.m, P, tq, tgrad, nullptr, tflux, nullptr, nullptr, nullptr, FB)));
   }
   Dual* tfv = nullptr;
   if (h.cfg.c.viscous) {

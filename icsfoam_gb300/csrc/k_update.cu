@@ -60,6 +60,25 @@ __global__ void k_bc(DevMesh m, const double* __restrict__ prim, double* __restr
   const int B = m.B, N = m.N;
   const Patch pt = m.patches[m.bpatch[b]];
   const int ci = m.bcell[b];
+  if (m.bpartner && m.bpartner[b] >= 0) {
+    // coupled patch: weighted mean of this side's cell and the partner's,
+    // the partner's velocity rotated into this side's frame
+    // (coupledFvPatchField::evaluate with cyclic patchNeighbourField)
+    const int pc = m.bpartner[b];
+    const double wb = m.bw[b];
+    const double* Rm = pt.R;
+    pB[b] = wb * (prim[ci] - prim[pc]) + prim[pc];
+    const double Un[3] = {prim[2 * N + pc], prim[3 * N + pc], prim[4 * N + pc]};
+    for (int k = 0; k < 3; ++k) {
+      const double up = Rm[3 * k] * Un[0] + Rm[3 * k + 1] * Un[1] + Rm[3 * k + 2] * Un[2];
+      UB[k * B + b] = wb * (prim[(2 + k) * N + ci] - up) + up;
+    }
+    double T = wb * (prim[N + ci] - prim[N + pc]) + prim[N + pc];
+    T = fmax(T, TMin);
+    if (useTMax) T = fmax(T, TMax);
+    TB[b] = T;
+    return;
+  }
   const double psiB = 1.0 / (R * TB[b]);
   const double gM1ByG = (gamma - 1.0) / gamma;
   const double Uc[3] = {prim[2 * N + ci], prim[3 * N + ci], prim[4 * N + ci]};

@@ -127,11 +127,18 @@ def stack_instances(mesh: M.Mesh, n: int, patch_for: Callable[[M.Patch, int], M.
     st.b_cell = off(mesh.b_cell, N)
     st.b_Sf, st.b_Cf, st.b_delta_coeffs = rep(mesh.b_Sf), rep(mesh.b_Cf), rep(mesh.b_delta_coeffs)
     st.b_patch = off(mesh.b_patch, P)
+    if mesh.b_partner is not None:
+        st.b_partner = np.concatenate([np.where(mesh.b_partner >= 0, mesh.b_partner + J * N, -1)
+                                       for J in range(n)]).astype(np.int32)
+        st.b_weights, st.b_nbr_d = rep(mesh.b_weights), rep(mesh.b_nbr_d)
+        st.b_nonorth_delta_coeffs = rep(mesh.b_nonorth_delta_coeffs)
     pats: List[M.Patch] = []
     for J in range(n):
         for p in mesh.patches:
             q = copy.copy(p)
             q.name = "%s_%d" % (p.name, J)
+            if q.partner is not None:
+                q.partner = "%s_%d" % (p.partner, J)
             pats.append(patch_for(q, J) if patch_for else q)
     st.patches = pats
     st.cell_ijk = rep(mesh.cell_ijk) if mesh.cell_ijk is not None else None

@@ -36,6 +36,7 @@ PATCH_FIXED = 3            # U, p, T fixedValue
 PATCH_PRESSURE_OUTLET = 4  # p fixedValue, U/T zeroGradient
 PATCH_TOTAL_INLET = 5      # totalPressure / totalTemperature / pressureInletOutletVelocity
 PATCH_ISOTHERMAL_WALL = 6  # U fixed 0, T fixed, p zeroGradient
+PATCH_CYCLIC = 7           # coupled to a partner patch, face i <-> face i (rotational or parallel)
 PATCH_EMPTY = 0            # no finite-volume faces
 
 PATCH_NAMES = {
@@ -45,6 +46,7 @@ PATCH_NAMES = {
     "pressureOutlet": PATCH_PRESSURE_OUTLET,
     "totalInlet": PATCH_TOTAL_INLET,
     "isothermalWall": PATCH_ISOTHERMAL_WALL,
+    "cyclic": PATCH_CYCLIC,
     "empty": PATCH_EMPTY,
 }
 
@@ -58,6 +60,12 @@ class Patch:
 
     ``is_wall`` marks OpenFOAM ``wall``-type patches, which the local pseudo
     time step treats specially (``setCoAndDeltaT.H:88-136``).
+
+    A cyclic patch (``kind == PATCH_CYCLIC``) names its ``partner`` patch;
+    face i of the two is one coupled face.  ``rotation`` (row-major 3x3)
+    maps vectors of the partner's side into this patch's frame (OpenFOAM
+    cyclic forwardT; the identity for a parallel cyclic), ``centre`` is the
+    point it rotates about (used to check the face pairing).
     """
 
     name: str
@@ -68,6 +76,33 @@ class Patch:
     U: Tuple[float, float, float] = (0.0, 0.0, 0.0)
     p0: float = 0.0
     T0: float = 0.0
+    partner: Optional[str] = None
+    rotation: Optional[Tuple[float, ...]] = None
+    centre: Tuple[float, float, float] = (0.0, 0.0, 0.0)
+    separation: Tuple[float, float, float] = (0.0, 0.0, 0.0)
+
+
+def rotation_matrix(axis, angle_deg: float) -> np.ndarray:
+    """Right-handed rotation by ``angle_deg`` about ``axis`` (Rodrigues)."""
+    a = np.asarray(axis, np.float64)
+    a = a / np.linalg.norm(a)
+    t = np.radians(angle_deg)
+    K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+    return np.eye(3) + np.sin(t) * K + (1.0 - np.cos(t)) * (K @ K)
+
+
+def cyclic_pair(name_a: str, name_b: str, axis=(0.0, 0.0, 1.0), angle_deg: float = 0.0,
+                centre=(0.0, 0.0, 0.0), separation=(0.0, 0.0, 0.0)) -> Tuple[Patch, Patch]:
+    """Two coupled patches: rotating patch b's geometry by ``angle_deg`` about
+    ``axis`` through ``centre`` and shifting it by ``separation`` lands it on
+    patch a (a rotational cyclic, or a translational one at 0 degrees)."""
+    R = rotation_matrix(axis, angle_deg)
+    sep = np.asarray(separation, np.float64)
+    a = Patch(name_a, PATCH_CYCLIC, partner=name_b, rotation=tuple(R.ravel()), centre=tuple(centre),
+              separation=tuple(sep))
+    b = Patch(name_b, PATCH_CYCLIC, partner=name_a, rotation=tuple(R.T.ravel()), centre=tuple(centre),
+              separation=tuple(-(R.T @ sep)))
+    return a, b
 
 
 @dataclasses.dataclass
@@ -99,6 +134,13 @@ class Mesh:
     face_points: Optional[np.ndarray] = None     # (F, 4) internal faces
     b_face_points: Optional[np.ndarray] = None   # (B, 4)
     cell_ijk: Optional[np.ndarray] = None        # (N, 3) generator index
+    # coupled (cyclic) boundary faces: the partner patch's cell of the paired
+    # face (-1 elsewhere), linear weight, the vector from the partner cell's
+    # centre (in this side's frame) to the face centre, nonOrthDeltaCoeffs
+    b_partner: Optional[np.ndarray] = None       # (B,) int32
+    b_weights: Optional[np.ndarray] = None       # (B,)
+    b_nbr_d: Optional[np.ndarray] = None         # (B, 3)
+    b_nonorth_delta_coeffs: Optional[np.ndarray] = None  # (B,)
 
     @property
     def n_faces(self) -> int:
@@ -344,6 +386,7 @@ def _finish(pts, fp_int, own, nei, entries, patch_list, dims=None, cell_ijk=None
         for d in range(3):
             if emax[d] > 0.5:
                 sol[d] = -1
+    cyc = cyclic_geometry(fv_patches, b_patch, b_cell, bSf, bCf, C)
     m = Mesh(
         n_cells=n_cells,
         owner=own.astype(np.int32), neighbour=nei.astype(np.int32),
@@ -355,6 +398,11 @@ def _finish(pts, fp_int, own, nei, entries, patch_list, dims=None, cell_ijk=None
         patches=fv_patches, solution_d=tuple(sol),
         points=pts, face_points=fp_int, b_face_points=b_fp,
     )
+    m.b_partner, m.b_weights, m.b_nbr_d, cyc_dc, cyc_nodc = cyc
+    m.b_nonorth_delta_coeffs = m.b_delta_coeffs.copy()
+    sel = m.b_partner >= 0
+    m.b_delta_coeffs[sel] = cyc_dc[sel]
+    m.b_nonorth_delta_coeffs[sel] = cyc_nodc[sel]
     m._empty = (e_fp, e_cell)  # kept for renumbering
     if cell_ijk is not None:
         m.cell_ijk = cell_ijk
@@ -363,6 +411,62 @@ def _finish(pts, fp_int, own, nei, entries, patch_list, dims=None, cell_ijk=None
         c = np.arange(n_cells)
         m.cell_ijk = np.stack([c % nx, (c // nx) % ny, c // (nx * ny)], axis=1).astype(np.int32)
     return m
+
+
+def cyclic_geometry(patches: List[Patch], b_patch, b_cell, bSf, bCf, C):
+    """Coupled-face data of cyclic patches (OpenFOAM cyclicFvPatch):
+
+    * partner cell: owner of face i of the partner patch;
+    * weights w = dn / (d + dn), d = n . (Cf - C_own) on this side and dn the
+      same on the partner side (cyclicFvPatch::makeWeights);
+    * delta = (Cf - C_own) - R (Cf_nbr - C_nbr) (cyclicFvPatch::delta), so the
+      partner centre seen from this side is C_own + delta; deltaCoeffs =
+      1/|delta|, nonOrthDeltaCoeffs = 1/max(n . delta, 0.05 |delta|);
+    * nbr_d = Cf - (C_own + delta): the partner-side displacement that
+      linearUpwind extrapolates along.
+    Face pairing is checked: R (Cf_nbr - centre) + centre + separation must
+    land on Cf.
+    """
+    B = len(b_patch)
+    partner = np.full(B, -1, np.int32)
+    w = np.ones(B)
+    nbr_d = np.zeros((B, 3))
+    dc = np.zeros(B)
+    nodc = np.zeros(B)
+    names = [p.name for p in patches]
+    for pi, p in enumerate(patches):
+        if p.kind != PATCH_CYCLIC:
+            continue
+        if p.partner not in names:
+            raise ValueError("cyclic patch %s: partner %r not found" % (p.name, p.partner))
+        qi = names.index(p.partner)
+        q = patches[qi]
+        if q.kind != PATCH_CYCLIC or q.partner != p.name:
+            raise ValueError("cyclic patches %s and %s do not name each other" % (p.name, q.name))
+        fa = np.nonzero(b_patch == pi)[0]
+        fb = np.nonzero(b_patch == qi)[0]
+        if len(fa) != len(fb):
+            raise ValueError("cyclic patches %s and %s differ in size" % (p.name, q.name))
+        R = np.asarray(p.rotation if p.rotation is not None else np.eye(3).ravel(), np.float64).reshape(3, 3)
+        ctr = np.asarray(p.centre, np.float64)
+        mapped = (bCf[fb] - ctr) @ R.T + ctr + np.asarray(p.separation, np.float64)
+        scale = max(1.0, np.abs(bCf).max())
+        if len(fa) and np.abs(mapped - bCf[fa]).max() > 1e-8 * scale:
+            raise ValueError("cyclic patches %s and %s: faces do not pair under the rotation" % (p.name, q.name))
+        na = bSf[fa] / np.linalg.norm(bSf[fa], axis=1)[:, None]
+        nb = bSf[fb] / np.linalg.norm(bSf[fb], axis=1)[:, None]
+        da = bCf[fa] - C[b_cell[fa]]
+        db = bCf[fb] - C[b_cell[fb]]
+        di = np.einsum("ij,ij->i", na, da)
+        dni = np.einsum("ij,ij->i", nb, db)
+        partner[fa] = b_cell[fb]
+        w[fa] = dni / (di + dni)
+        delta = da - db @ R.T
+        nbr_d[fa] = da - delta
+        md = np.linalg.norm(delta, axis=1)
+        dc[fa] = 1.0 / md
+        nodc[fa] = 1.0 / np.maximum(np.einsum("ij,ij->i", na, delta), 0.05 * md)
+    return partner, w, nbr_d, dc, nodc
 
 
 def renumber(mesh: Mesh, new_to_old: np.ndarray) -> Mesh:

@@ -73,7 +73,9 @@ enum {
   ICS_PATCH_PRESSURE_OUTLET = 4, /* p fixedValue, U, T zeroGradient                  */
   ICS_PATCH_TOTAL_INLET = 5,     /* totalPressure, totalTemperature,
                                     pressureInletOutletVelocity                      */
-  ICS_PATCH_ISOTHERMAL_WALL = 6  /* U = 0, T fixed, p zeroGradient                   */
+  ICS_PATCH_ISOTHERMAL_WALL = 6, /* U = 0, T fixed, p zeroGradient                   */
+  ICS_PATCH_CYCLIC = 7           /* coupled to a partner patch (OpenFOAM cyclic, parallel
+                                    or rotational): face i of the one is face i of the other */
 };
 
 typedef struct {
@@ -82,6 +84,8 @@ typedef struct {
   double p, T;      /* fixed static pressure / temperature                 */
   double U[3];      /* fixed velocity                                      */
   double p0, T0;    /* total pressure / temperature (ICS_PATCH_TOTAL_INLET) */
+  double rotation[9]; /* ICS_PATCH_CYCLIC: row-major R taking the partner side's
+                         vectors into this patch's frame (cyclic forwardT)  */
 } ics_patch_desc;
 
 /* Mesh in OpenFOAM LDU convention (owner < neighbour, upper-triangular
@@ -104,6 +108,13 @@ typedef struct {
   const double* b_delta_coeffs;       /* [n_bfaces]                         */
   const ics_patch_desc* patches;      /* [n_patches]                        */
   int32_t solution_d[3];              /* +1 solved, -1 empty direction      */
+  /* coupled (cyclic) boundary faces, OpenFOAM cyclicFvPatch; all may be NULL
+   * when no patch is ICS_PATCH_CYCLIC                                       */
+  const int32_t* b_partner;             /* [n_bfaces] the paired face's cell (-1: not cyclic) */
+  const double* b_weights;              /* [n_bfaces] coupled linear weights  */
+  const double* b_nbr_d;                /* [n_bfaces][3] face centre minus the partner
+                                           cell centre seen from this side (Cf - C - delta) */
+  const double* b_nonorth_delta_coeffs; /* [n_bfaces]; NULL: b_delta_coeffs  */
 } ics_mesh_desc;
 
 /* Dictionary entries of fvSchemes / fvSolution / thermophysicalProperties

@@ -87,6 +87,7 @@ struct B5 {
 struct Patch {
   int kind, is_wall;
   double p, T, U[3], p0, T0;
+  double R[9];  // cyclic: partner-side vectors into this patch's frame
 };
 
 struct Case {
@@ -149,6 +150,15 @@ struct Case {
   std::vector<double> s, sB, rhoS, rhoS0, rhoS00;
   std::vector<int> sFixed;
   std::vector<double> sValue;
+  // coupled (cyclic) boundary faces: partner cell (-1 elsewhere), linear
+  // weight, delta (partner centre seen from this side minus C), partner-side
+  // displacement Cf - C - delta, nonOrthDeltaCoeffs, and the interface
+  // blocks of the last Jacobian (blockFvMatrix interfacesUpper)
+  bool hasCyc = false;
+  std::vector<int> bpartner;
+  std::vector<double> bw, bnodc;
+  std::vector<V3> bdelta, bnbrd;
+  std::vector<B5> iface;
   // moving reference frames (dbnsFoam outerLoop.H:6-21): frame velocity . n
   // per internal then boundary face, rotation vector per cell, frame velocity
   // of the boundary faces that correctBoundaryVelocity assigns
@@ -159,6 +169,14 @@ struct Case {
   std::vector<int> mrfBIn;
   std::string err;
 };
+
+// cyclic boundary face b, and R v with the rotation of its patch
+inline bool isCyc(const Case& c, int b) { return c.hasCyc && c.bpartner[b] >= 0; }
+inline V3 rotP(const Case& c, int b, const V3& v) {
+  const double* R = c.patches[c.bpatch[b]].R;
+  return V3(R[0] * v.x + R[1] * v.y + R[2] * v.z, R[3] * v.x + R[4] * v.y + R[5] * v.z,
+            R[6] * v.x + R[7] * v.y + R[8] * v.z);
+}
 
 // MRF face velocity of face fi (internal then boundary), zero without zones
 inline double umOf(const Case& c, int fi) { return c.mrfOn ? c.mrfU[fi] : 0.0; }
@@ -195,6 +213,11 @@ void gaussGrad(const Case& c, const VolS& f, std::vector<V3>& g) {
   }
   for (int b = 0; b < c.B; ++b) {
     const int o = c.bcell[b];
+    if (isCyc(c, b)) {  // linear interpolation with the partner (coupled patch)
+      const int pc = c.bpartner[b];
+      g[o] = g[o] + c.bSf[b] * (c.bw[b] * (f.in[o] - f.in[pc]) + f.in[pc]);
+      continue;
+    }
     g[o] = g[o] + c.bSf[b] * f.bf[b];
   }
   for (int i = 0; i < c.N; ++i) g[i] = g[i] / c.V[i];
@@ -213,8 +236,9 @@ void cellLimitedGrad(const Case& c, const VolS& f, bool venkat, std::vector<V3>&
   }
   for (int b = 0; b < c.B; ++b) {
     const int o = c.bcell[b];
-    maxV[o] = std::max(maxV[o], f.bf[b]);
-    minV[o] = std::min(minV[o], f.bf[b]);
+    const double v = isCyc(c, b) ? f.in[c.bpartner[b]] : f.bf[b];  // coupled: the neighbour cell
+    maxV[o] = std::max(maxV[o], v);
+    minV[o] = std::min(minV[o], v);
   }
   for (int i = 0; i < c.N; ++i) {
     maxV[i] -= f.in[i];
@@ -249,51 +273,74 @@ void interpLinear(const Case& c, const VolS& f, std::vector<double>& out) {
     const int o = c.own[fi], n = c.nei[fi];
     out[fi] = c.w[fi] * (f.in[o] - f.in[n]) + f.in[n];
   }
-  for (int b = 0; b < c.B; ++b) out[c.F + b] = f.bf[b];
+  for (int b = 0; b < c.B; ++b) {
+    const int pc = isCyc(c, b) ? c.bpartner[b] : -1;
+    out[c.F + b] = pc >= 0 ? c.bw[b] * (f.in[c.bcell[b]] - f.in[pc]) + f.in[pc] : f.bf[b];
+  }
 }
 
 // fvc::interpolate(vf, dir, "reconstruct(..)") for the configured scheme.
 void reconstruct(const Case& c, const VolS& f, double dir, int scheme, std::vector<double>& out) {
   out.resize(c.F + c.B);
   const double wUp = pos0(dir);
-  if (scheme == ICS_RECON_UPWIND) {
-    for (int fi = 0; fi < c.F; ++fi) {
-      const int o = c.own[fi], n = c.nei[fi];
-      out[fi] = wUp * (f.in[o] - f.in[n]) + f.in[n];
-    }
-  } else if (scheme == ICS_RECON_VANLEER || scheme == ICS_RECON_MINMOD) {
-    std::vector<V3> g;
+  const bool tvd = scheme == ICS_RECON_VANLEER || scheme == ICS_RECON_MINMOD;
+  std::vector<V3> g;
+  if (tvd)
     gaussGrad(c, f, g);
-    for (int fi = 0; fi < c.F; ++fi) {
-      const int o = c.own[fi], n = c.nei[fi];
-      const double phiP = f.in[o], phiN = f.in[n];
-      const V3 d = c.C[n] - c.C[o];
-      const double gradf = phiN - phiP;
-      const double gradcf = dir > 0 ? dot(d, g[o]) : dot(d, g[n]);
-      double r;
-      if (std::fabs(gradcf) >= 1000 * std::fabs(gradf))
-        r = 2 * 1000 * sgn(gradcf) * sgn(gradf) - 1;
-      else
-        r = 2 * (gradcf / gradf) - 1;
-      double lim;
-      if (scheme == ICS_RECON_VANLEER)
-        lim = (r + std::fabs(r)) / (1 + std::fabs(r));
-      else
-        lim = std::max(std::min(std::min(r, 1.0), 2.0), 0.0);
-      const double wgt = lim * c.w[fi] + (1.0 - lim) * wUp;
-      out[fi] = wgt * (phiP - phiN) + phiN;
-    }
-  } else {  // MUSCL: linearUpwind + cellLimited gradient
-    std::vector<V3> g;
+  else if (scheme != ICS_RECON_UPWIND)
     cellLimitedGrad(c, f, scheme == ICS_RECON_MUSCL_VENKATAKRISHNAN, g);
-    for (int fi = 0; fi < c.F; ++fi) {
-      const int o = c.own[fi], n = c.nei[fi];
+  // TVD limitedScheme weight of a face with upwind-side gradient gu
+  auto tvdValue = [&](double phiP, double phiN, const V3& d, const V3& gu, double cdw) {
+    const double gradf = phiN - phiP;
+    const double gradcf = dot(d, gu);
+    double r;
+    if (std::fabs(gradcf) >= 1000 * std::fabs(gradf))
+      r = 2 * 1000 * sgn(gradcf) * sgn(gradf) - 1;
+    else
+      r = 2 * (gradcf / gradf) - 1;
+    double lim;
+    if (scheme == ICS_RECON_VANLEER)
+      lim = (r + std::fabs(r)) / (1 + std::fabs(r));
+    else
+      lim = std::max(std::min(std::min(r, 1.0), 2.0), 0.0);
+    const double wgt = lim * cdw + (1.0 - lim) * wUp;
+    return wgt * (phiP - phiN) + phiN;
+  };
+  for (int fi = 0; fi < c.F; ++fi) {
+    const int o = c.own[fi], n = c.nei[fi];
+    const double phiP = f.in[o], phiN = f.in[n];
+    if (scheme == ICS_RECON_UPWIND) {
+      out[fi] = wUp * (phiP - phiN) + phiN;
+    } else if (tvd) {
+      out[fi] = tvdValue(phiP, phiN, c.C[n] - c.C[o], dir > 0 ? g[o] : g[n], c.w[fi]);
+    } else {  // MUSCL: linearUpwind + cellLimited gradient
       const int up = dir > 0 ? o : n;
-      const double base = wUp * (f.in[o] - f.in[n]) + f.in[n];
+      const double base = wUp * (phiP - phiN) + phiN;
       out[fi] = base + dot(c.Cf[fi] - c.C[up], g[up]);
     }
   }
-  for (int b = 0; b < c.B; ++b) out[c.F + b] = f.bf[b];
+  for (int b = 0; b < c.B; ++b) {
+    out[c.F + b] = f.bf[b];
+    if (!isCyc(c, b)) continue;
+    // coupled face: this side's cell o and the partner pc; the partner's
+    // value as it is (a scalar field), its gradient rotated into this side's
+    // frame; the TVD ratio uses delta, linearUpwind extrapolates the partner
+    // side along Cf - C - delta (limitedScheme / linearUpwind on coupled patches)
+    const int o = c.bcell[b], pc = c.bpartner[b];
+    const double phiP = f.in[o], phiN = f.in[pc];
+    if (scheme == ICS_RECON_UPWIND) {
+      out[c.F + b] = wUp * (phiP - phiN) + phiN;
+      continue;
+    }
+    const V3 gu = dir > 0 ? g[o] : rotP(c, b, g[pc]);
+    if (tvd) {
+      out[c.F + b] = tvdValue(phiP, phiN, c.bdelta[b], gu, c.bw[b]);
+    } else {
+      const double base = wUp * (phiP - phiN) + phiN;
+      const V3 d = dir > 0 ? c.bCf[b] - c.C[o] : c.bnbrd[b];
+      out[c.F + b] = base + dot(d, gu);
+    }
+  }
 }
 
 // component fields of U (internal + boundary)
@@ -967,7 +1014,14 @@ void waveSpeed(const Case& c, std::vector<double>& lam) {
   lam.resize(c.F + c.B);
   for (int fi = 0; fi < c.F + c.B; ++fi) {
     const V3 n = SfOf(c, fi) / magSfOf(c, fi);
-    const V3 uf(ui[0][fi], ui[1][fi], ui[2][fi]);
+    V3 uf(ui[0][fi], ui[1][fi], ui[2][fi]);
+    const int b = fi - c.F;
+    if (b >= 0 && isCyc(c, b)) {  // fvc::interpolate(U) on a coupled patch: the partner's U rotated
+      const V3 up = rotP(c, b, c.U[c.bpartner[b]]);
+      const V3 uo = c.U[c.bcell[b]];
+      const double w = c.bw[b];
+      uf = V3(w * (uo.x - up.x) + up.x, w * (uo.y - up.y) + up.y, w * (uo.z - up.z) + up.z);
+    }
     lam[fi] = ci[fi] + std::fabs(dot(uf, n) - umOf(c, fi));
   }
 }
@@ -1010,6 +1064,11 @@ void setCoAndDeltaT(Case& c) {
   }
   for (int b = 0; b < c.B; ++b) {
     const Patch& pt = c.patches[c.bpatch[b]];
+    if (isCyc(c, b)) {  // coupled: nonOrthDeltaCoeffs lambda (setCoAndDeltaT.H:73-87)
+      const int o = c.bcell[b];
+      c.rPseudoDeltaT[o] = std::max(c.rPseudoDeltaT[o], c.bnodc[b] * lam[c.F + b]);
+      continue;
+    }
     if (!pt.is_wall) continue;
     const int o = c.bcell[b];
     const double cc = std::sqrt(c.gamma / psiOf(c, c.T[o]));
@@ -1098,6 +1157,33 @@ void assembleJacobian(Case& c) {
       }
     }
   }
+  // coupled (cyclic) faces: insertBlock's interface block 0.5|S| A_R with
+  // diag += 0.5|S| A_L; -div(w, u_MRF |S|): interface -= phi (1-w), diag -= phi w
+  // (blockFvMatrix.C:241-262, blockFvOperatorsTemplates.C:176-195)
+  if (c.hasCyc) {
+    c.iface.assign(c.B, B5());
+    for (int b = 0; b < c.B; ++b) {
+      if (!isCyc(c, b)) continue;
+      const int fi = c.F + b, o = c.bcell[b];
+      const V3 n = c.bSf[b] / c.bmagSf[b];
+      const B5 AL = eulerJacobian(g, U_l[fi], E_l[fi], n);
+      const B5 AR = eulerJacobian(g, U_r[fi], E_r[fi], n);
+      for (int k = 0; k < 25; ++k) {
+        const double up = 0.5 * c.bmagSf[b] * AR.a[k];
+        const double lo = -0.5 * c.bmagSf[b] * AL.a[k];
+        c.iface[b].a[k] += up;
+        c.diag[o].a[k] -= lo;
+      }
+      if (c.mrfOn) {
+        const double phm = c.mrfU[fi] * c.bmagSf[b];
+        const double up = phm * (1 - c.bw[b]), lo = -phm * c.bw[b];
+        for (int q = 0; q < 5; ++q) {
+          c.iface[b].a[diagIdx[q]] -= up;
+          c.diag[o].a[diagIdx[q]] -= -lo;
+        }
+      }
+    }
+  }
   // addDissipationJacobian: lambda = interp(c) + |interp(U).n - u_MRF|, subtracted
   std::vector<double> lam;
   waveSpeed(c, lam);
@@ -1114,11 +1200,14 @@ void assembleJacobian(Case& c) {
   for (int b = 0; b < c.B; ++b) {
     const double d = 0.5 * c.bmagSf[b] * lam[c.F + b];
     for (int q = 0; q < 5; ++q) c.diag[c.bcell[b]].a[diagIdx[q]] += d;
+    if (isCyc(c, b))
+      for (int q = 0; q < 5; ++q) c.iface[b].a[diagIdx[q]] -= d;
   }
   // addBoundaryTerms (boundaryJacobian :47-120, :219-355)
   for (int b = 0; b < c.B; ++b) {
     const Patch& pt = c.patches[c.bpatch[b]];
     const int ci = c.bcell[b];
+    if (isCyc(c, b)) continue;  // physical patches only
     // valueInternalCoeffs
     double pV = 1, tV = 1;
     V3 uV(1, 1, 1);
@@ -1285,6 +1374,17 @@ void matrixMul(const Case& c, const double* x, double* y) {
         const double* xk = x + 5 * (K * c.Nc + cl);
         for (int k = 0; k < 5; ++k) y[5 * i + k] += d * xk[k];
       }
+    }
+  }
+  // cyclic interfaces (blockFvMatrix::Amul, blockFvMatrix.C:386-407): the
+  // partner's unknowns with the momentum rotated into this side's frame
+  if (c.hasCyc && (int)c.iface.size() == c.B) {
+    for (int b = 0; b < c.B; ++b) {
+      if (!isCyc(c, b)) continue;
+      const int o = c.bcell[b], pc = c.bpartner[b];
+      const V3 xu = rotP(c, b, V3(x[5 * pc + 1], x[5 * pc + 2], x[5 * pc + 3]));
+      const double xt[5] = {x[5 * pc], xu.x, xu.y, xu.z, x[5 * pc + 4]};
+      bmv(c.iface[b], xt, y + 5 * o, 1.0);
     }
   }
 }
@@ -1641,6 +1741,11 @@ void correctBoundaryConditions(Case& c, const std::vector<double>& psiB) {
                                    1.0 / gM1ByG);
         break;
       }
+      case ICS_PATCH_CYCLIC: {  // coupledFvPatchField::evaluate
+        const int pc = c.bpartner[b];
+        c.pB[b] = c.bw[b] * (c.p[ci] - c.p[pc]) + c.p[pc];
+        break;
+      }
     }
   }
   // U
@@ -1670,6 +1775,12 @@ void correctBoundaryConditions(Case& c, const std::vector<double>& psiB) {
         c.UB[b] = out;
         break;
       }
+      case ICS_PATCH_CYCLIC: {  // the partner's velocity rotated into this side's frame
+        const V3 up = rotP(c, b, c.U[c.bpartner[b]]);
+        const double w = c.bw[b];
+        c.UB[b] = V3(w * (c.U[ci].x - up.x) + up.x, w * (c.U[ci].y - up.y) + up.y, w * (c.U[ci].z - up.z) + up.z);
+        break;
+      }
     }
   }
   // MRF: a fixedValue patch keeps the frame velocity correctBoundaryVelocity
@@ -1694,6 +1805,11 @@ void correctBoundaryConditions(Case& c, const std::vector<double>& psiB) {
       case ICS_PATCH_TOTAL_INLET: {
         const double gM1ByG = (g - 1.0) / g;
         c.TB[b] = pt.T0 / (1.0 + 0.5 * psiB[b] * gM1ByG * (1.0 - pos0(c.phiB[b])) * magSqr(c.UB[b]));
+        break;
+      }
+      case ICS_PATCH_CYCLIC: {
+        const int pc = c.bpartner[b];
+        c.TB[b] = c.bw[b] * (c.T[ci] - c.T[pc]) + c.T[pc];
         break;
       }
     }
@@ -2180,6 +2296,10 @@ void icsref_default_config(ics_config* c) {
 
 int icsref_set_config(ics_handle h, const ics_config* cfg) {
   if (!h || !cfg) return ICS_ERR_ARG;
+  if (h->hasCyc && cfg->viscous) {
+    h->err = "viscous terms across cyclic patches are not built";
+    return ICS_ERR_ARG;
+  }
   if (cfg->flux_scheme < 0 || cfg->flux_scheme > 2) {
     h->err = "Unknown convectiveFluxScheme";
     return ICS_ERR_SCHEME;
@@ -2259,7 +2379,28 @@ int icsref_create(const ics_mesh_desc* m, const ics_config* cfg, ics_handle* out
     for (int k = 0; k < 3; ++k) q.U[k] = d.U[k];
     q.p0 = d.p0;
     q.T0 = d.T0;
+    for (int k = 0; k < 9; ++k) q.R[k] = d.rotation[k];
+    if (d.kind == ICS_PATCH_CYCLIC) c.hasCyc = true;
     c.patches.push_back(q);
+  }
+  if (c.hasCyc) {
+    if (!m->b_partner || !m->b_weights || !m->b_nbr_d || cfg->viscous) {
+      delete h;
+      return ICS_ERR_ARG;
+    }
+    c.bpartner.assign(c.B, -1);
+    c.bw.assign(c.B, 1.0);
+    c.bnodc.resize(c.B);
+    c.bdelta.assign(c.B, V3());
+    c.bnbrd.assign(c.B, V3());
+    for (int b = 0; b < c.B; ++b) {
+      c.bnodc[b] = m->b_nonorth_delta_coeffs ? m->b_nonorth_delta_coeffs[b] : m->b_delta_coeffs[b];
+      if (c.patches[c.bpatch[b]].kind != ICS_PATCH_CYCLIC) continue;
+      c.bpartner[b] = m->b_partner[b];
+      c.bw[b] = m->b_weights[b];
+      c.bnbrd[b] = V3(m->b_nbr_d[3 * b], m->b_nbr_d[3 * b + 1], m->b_nbr_d[3 * b + 2]);
+      c.bdelta[b] = (c.bCf[b] - c.C[c.bcell[b]]) - c.bnbrd[b];
+    }
   }
   for (int k = 0; k < 3; ++k) c.solD[k] = m->solution_d[k];
   c.cellFaces.assign(c.N, {});
@@ -2622,6 +2763,7 @@ int icsref_scalar_enable(ics_handle h, const double* s, const int32_t* patch_fix
                          double D, int32_t recon) {
   if (!h || !s || recon < 0 || recon > ICS_RECON_MUSCL_MINMOD || D < 0) return ICS_ERR_ARG;
   Case& c = *h;
+  if (c.hasCyc) return ICS_ERR_ARG;  // scalar transport across cyclic patches is not built
   if (c.nInst > 1) {
     c.err = "scalar transport is not provided for Harmonic Balance handles";
     return ICS_ERR_ARG;

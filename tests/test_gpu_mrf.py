@@ -28,7 +28,7 @@ FLUXES = ["AUSMPlusUp", "HLLC", "ROE"]
 
 
 def sector(flux="HLLC", **kw):
-    return perturb(cases.annular_sector(6, 8, 9, ordering_mode="colour", flux=flux, **kw))
+    return perturb(cases.annular_sector(6, 8, 9, ordering_mode="colour", flux=flux, sides="slip", **kw))
 
 
 def open_case(b, w, mode=0, fields=None, **over):

@@ -23,7 +23,7 @@ from icsfoam_gb300 import foam_case
 
 @pytest.fixture(scope="module")
 def sector():
-    return cases.annular_sector(6, 8, 9, ordering_mode="natural")
+    return cases.annular_sector(6, 8, 9, ordering_mode="natural", sides="slip")
 
 
 def test_frame_fields_closure_and_patches(sector):
@@ -120,7 +120,7 @@ def _open(b, w, fields):
 
 
 def test_oracle_source_and_skew_block_are_the_omega_terms(oracle_binding):
-    w = cases.annular_sector(6, 8, 9, ordering_mode="natural")
+    w = cases.annular_sector(6, 8, 9, ordering_mode="natural", sides="slip")
     rng = np.random.default_rng(0)
     w.U = w.U + rng.uniform(-20, 20, w.U.shape)
     om, fv, bU, inc = MRF.frame_fields(w.mesh, *w.mrf)
@@ -149,7 +149,7 @@ def test_oracle_source_and_skew_block_are_the_omega_terms(oracle_binding):
 def test_oracle_boundary_assignment_sequence(oracle_binding):
     """Slip faces get the frame velocity at each time step and lose it at
     the next boundary update; an isothermal wall keeps it."""
-    w = cases.annular_sector(6, 8, 9, ordering_mode="natural")
+    w = cases.annular_sector(6, 8, 9, ordering_mode="natural", sides="slip")
     names = [p.name for p in w.mesh.patches]
     w.mesh.patches[names.index("hub")].kind = M.PATCH_ISOTHERMAL_WALL
     w.mesh.patches[names.index("hub")].T = 280.0
@@ -174,7 +174,7 @@ def test_case_files_round_trip(tmp_path):
     a renumbering."""
     from test_foam_case import write_dicts
 
-    w = cases.annular_sector(4, 6, 9, ordering_mode="natural")
+    w = cases.annular_sector(4, 6, 9, ordering_mode="natural", sides="slip")
     rot = w.mrf[0][0]
     rot.non_rotating_patches = ("hub",)
     tra = MRF.TranslatingZone(np.nonzero(w.mesh.C[:, 2] < 0.05)[0], (1.0, 0.0, 2.0), ("inlet",))

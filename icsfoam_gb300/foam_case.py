@@ -25,11 +25,12 @@ fixedValue / zeroGradient|inletOutlet|pIOV /    PRESSURE_OUTLET
 totalPressure / pressureInletOutletVelocity /   TOTAL_INLET (p0, T0)
    totalTemperature
 zeroGradient / noSlip|fixedValue 0 / fixedValue ISOTHERMAL_WALL
+cyclic / cyclic / cyclic (cyclic polyPatch)     CYCLIC (neighbourPatch, transform)
 ==============================================  ==========================
 
 ``inletOutlet`` is taken as zeroGradient (outflow).  Other combinations,
-non-uniform boundary values, cyclic and processor patches and binary files
-raise ``ValueError``.  Only ASCII format is read.
+non-uniform boundary values, cyclicAMI and processor patches and binary
+files raise ``ValueError``.  Only ASCII format is read.
 
 Moving reference frames: when ``constant/MRFProperties`` or
 ``constant/MRFTranslatingProperties`` exists, its zones are built on the
@@ -210,7 +211,7 @@ def read_boundary(path: str) -> List[Dict]:
         if not isinstance(e, dict):
             continue
         out.append({"name": name, "type": e.get("type", "patch"), "nFaces": int(e["nFaces"]),
-                    "startFace": int(e["startFace"])})
+                    "startFace": int(e["startFace"]), "dict": e})
     if len(out) != n:
         raise ValueError("%s: expected %d patches" % (path, n))
     return out
@@ -267,13 +268,30 @@ def _uval(e: Dict, key: str, n_comp: int):
     return v
 
 
-def patch_from_bcs(name: str, ptype: str, bp: Dict, bU: Dict, bT: Dict) -> M.Patch:
-    """Fold the p, U, T boundary conditions of one patch into a patch kind."""
+def patch_from_bcs(name: str, ptype: str, bp: Dict, bU: Dict, bT: Dict, bdict: Optional[Dict] = None) -> M.Patch:
+    """Fold the p, U, T boundary conditions of one patch into a patch kind.
+
+    A ``cyclic`` polyPatch (with cyclic p, U, T) becomes a coupled patch; its
+    transform (``bdict``: neighbourPatch, transform translational /
+    rotational, separationVector or rotationAxis / rotationCentre /
+    rotationAngle) is resolved against the face geometry by
+    ``mesh_from_polymesh``.
+    """
     tp, tU, tT = bp.get("type"), bU.get("type"), bT.get("type")
     is_wall = ptype == "wall"
     if ptype == "empty" or "empty" in (tp, tU, tT):
         return M.Patch(name, M.PATCH_EMPTY)
-    if ptype in ("cyclic", "cyclicAMI", "processor") or "cyclic" in (tp, tU, tT):
+    if ptype == "cyclic":
+        if any(t not in (None, "cyclic") for t in (tp, tU, tT)):
+            raise ValueError("patch %s: a cyclic patch needs cyclic p, U and T" % name)
+        d = bdict or {}
+        if "neighbourPatch" not in d:
+            raise ValueError("patch %s: cyclic without neighbourPatch" % name)
+        q = M.Patch(name, M.PATCH_CYCLIC, partner=d["neighbourPatch"])
+        q.transform = d  # resolved in mesh_from_polymesh
+        q.match_tolerance = float(d.get("matchTolerance", 1e-4))
+        return q
+    if ptype in ("cyclicAMI", "processor") or "cyclic" in (tp, tU, tT):
         raise ValueError("patch %s: %s patches are not supported" % (name, ptype))
     if tp == "fixedValue" and tU == "fixedValue" and tT == "fixedValue":
         U = _uval(bU, "value", 3)
@@ -299,7 +317,55 @@ def patch_from_bcs(name: str, ptype: str, bp: Dict, bU: Dict, bT: Dict) -> M.Pat
 
 
 # ------------------------------------------------------------------ mesh
+def _vec3(s) -> np.ndarray:
+    v = np.array(str(s).replace("(", " ").replace(")", " ").split(), dtype=np.float64)
+    if v.size != 3:
+        raise ValueError("expected a vector, got %r" % s)
+    return v
+
+
+def _resolve_cyclic(patches: List[M.Patch], centres: Dict[str, np.ndarray]):
+    """Rotation and separation of each cyclic pair from its transform entry
+    (OpenFOAM cyclicTransform): translational - separationVector (this patch
+    to its neighbour); rotational - rotationAxis, rotationCentre and
+    rotationAngle, the sign that maps the neighbour's face centres onto this
+    patch's being taken; no transform - the translation between the patch
+    centroids.  The face pairing is checked again when the mesh is built."""
+    by = {p.name: p for p in patches}
+    for p in patches:
+        if p.kind != M.PATCH_CYCLIC:
+            continue
+        d = getattr(p, "transform", {}) or {}
+        ca, cb = centres[p.name], centres[p.partner]
+        kind = d.get("transform", "")
+        if kind == "rotational":
+            axis = _vec3(d["rotationAxis"])
+            ctr = _vec3(d.get("rotationCentre", "(0 0 0)"))
+            ang = float(d["rotationAngle"])
+            best = None
+            for a in (ang, -ang):
+                R = M.rotation_matrix(axis, a)
+                err = np.abs((cb - ctr) @ R.T + ctr - ca).max() if len(ca) else 0.0
+                if best is None or err < best[0]:
+                    best = (err, R)
+            p.rotation, p.centre, p.separation = tuple(best[1].ravel()), tuple(ctr), (0.0, 0.0, 0.0)
+        else:
+            if kind == "translational":
+                sep = -_vec3(d["separationVector"])
+            else:
+                sep = (ca.mean(axis=0) - cb.mean(axis=0)) if len(ca) else np.zeros(3)
+            p.rotation, p.separation = tuple(np.eye(3).ravel()), tuple(sep)
+        if by[p.partner].partner != p.name:
+            raise ValueError("cyclic patches %s and %s do not name each other" % (p.name, p.partner))
+
+
 def mesh_from_polymesh(points, faces, owner, neighbour, boundary: List[Dict], patches: List[M.Patch]) -> M.Mesh:
+    centres = {}
+    for b, p in zip(boundary, patches):
+        if p.kind == M.PATCH_CYCLIC:
+            sl = slice(b["startFace"], b["startFace"] + b["nFaces"])
+            centres[p.name] = M.face_centres_and_areas(points, faces[sl])[0] if b["nFaces"] else np.zeros((0, 3))
+    _resolve_cyclic(patches, centres)
     nInt = len(neighbour)
     own = owner[:nInt].astype(np.int64)
     nei = neighbour.astype(np.int64)
@@ -370,7 +436,7 @@ def load_case(path: str, time: str = "0", ordering_mode: Optional[str] = None):
     U_in, U_b = read_field(os.path.join(tdir, "U"), 3)
     T_in, T_b = read_field(os.path.join(tdir, "T"), 1)
     patches = [patch_from_bcs(b["name"], b["type"], p_b.get(b["name"], {}), U_b.get(b["name"], {}),
-                              T_b.get(b["name"], {})) for b in boundary]
+                              T_b.get(b["name"], {}), b["dict"]) for b in boundary]
     mesh = mesh_from_polymesh(points, faces, owner, neighbour, boundary, patches)
     N = mesh.n_cells
     p = np.broadcast_to(p_in.reshape(-1), (N,)).copy() if p_in.ndim == 1 else p_in[:, 0].copy()
@@ -474,6 +540,20 @@ def _faces_text(faces) -> List[str]:
     return ["%d(%s)" % (len(f), " ".join(str(int(x)) for x in f)) for f in faces]
 
 
+def _transform_text(patch: M.Patch) -> str:
+    """The cyclicTransform entries of a coupled patch (axis-angle from R)."""
+    R = np.asarray(patch.rotation if patch.rotation is not None else np.eye(3).ravel(), np.float64).reshape(3, 3)
+    ang = np.degrees(np.arccos(np.clip((np.trace(R) - 1.0) / 2.0, -1.0, 1.0)))
+    if ang < 1e-12:
+        sep = -np.asarray(patch.separation, np.float64)
+        return "\n        transform translational;\n        separationVector (%.17g %.17g %.17g);" % tuple(sep)
+    ax = np.array([R[2, 1] - R[1, 2], R[0, 2] - R[2, 0], R[1, 0] - R[0, 1]])
+    ax = ax / np.linalg.norm(ax)
+    return ("\n        transform rotational;\n        rotationAxis (%.17g %.17g %.17g);"
+            "\n        rotationCentre (%.17g %.17g %.17g);\n        rotationAngle %.17g;"
+            % (tuple(ax) + tuple(patch.centre) + (ang,)))
+
+
 def write_case(path: str, mesh: M.Mesh, p: np.ndarray, U: np.ndarray, T: np.ndarray):
     """Write ``mesh`` and the cell fields as an ASCII case (polyMesh + 0/{p,U,T}).
 
@@ -512,8 +592,12 @@ def write_case(path: str, mesh: M.Mesh, p: np.ndarray, U: np.ndarray, T: np.ndar
     bl = []
     for patch, n, st in boundary:
         ptype = "empty" if patch.kind == M.PATCH_EMPTY else ("wall" if patch.is_wall else "patch")
-        bl.append("    %s\n    {\n        type %s;\n        nFaces %d;\n        startFace %d;\n    }"
-                  % (patch.name, ptype, n, st))
+        extra = ""
+        if patch.kind == M.PATCH_CYCLIC:
+            ptype = "cyclic"
+            extra = "\n        neighbourPatch %s;" % patch.partner + _transform_text(patch)
+        bl.append("    %s\n    {\n        type %s;\n        nFaces %d;\n        startFace %d;%s\n    }"
+                  % (patch.name, ptype, n, st, extra))
     _write(os.path.join(pm, "boundary"), "polyBoundaryMesh", "constant/polyMesh", "boundary",
            "\n%d\n(\n%s\n)\n" % (len(boundary), "\n".join(bl)))
 
@@ -536,6 +620,8 @@ def write_case(path: str, mesh: M.Mesh, p: np.ndarray, U: np.ndarray, T: np.ndar
                     ("totalTemperature", "T0 uniform %.17g" % patch.T0))
         if k == M.PATCH_ISOTHERMAL_WALL:
             return ("zeroGradient", None), ("noSlip", None), ("fixedValue", "value uniform %.17g" % patch.T)
+        if k == M.PATCH_CYCLIC:
+            return ("cyclic", None), ("cyclic", None), ("cyclic", None)
         raise ValueError(patch.kind)
 
     def field(name, cls, values, idx, fmt):

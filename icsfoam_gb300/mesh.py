@@ -450,8 +450,9 @@ def cyclic_geometry(patches: List[Patch], b_patch, b_cell, bSf, bCf, C):
         R = np.asarray(p.rotation if p.rotation is not None else np.eye(3).ravel(), np.float64).reshape(3, 3)
         ctr = np.asarray(p.centre, np.float64)
         mapped = (bCf[fb] - ctr) @ R.T + ctr + np.asarray(p.separation, np.float64)
-        scale = max(1.0, np.abs(bCf).max())
-        if len(fa) and np.abs(mapped - bCf[fa]).max() > 1e-8 * scale:
+        # OpenFOAM's matchTolerance: a fraction of the face length scale
+        tol = getattr(p, "match_tolerance", 1e-4) * np.sqrt(np.linalg.norm(bSf[fa], axis=1))
+        if len(fa) and np.any(np.abs(mapped - bCf[fa]).max(axis=1) > tol):
             raise ValueError("cyclic patches %s and %s: faces do not pair under the rotation" % (p.name, q.name))
         na = bSf[fa] / np.linalg.norm(bSf[fa], axis=1)[:, None]
         nb = bSf[fb] / np.linalg.norm(bSf[fb], axis=1)[:, None]

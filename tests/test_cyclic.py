@@ -143,3 +143,52 @@ def test_cyclic_rejects_viscous_and_scalar(oracle_binding):
     h = _open(oracle_binding, w.mesh, w.settings, w.p, w.U, w.T)
     with pytest.raises(abi.IcsError):
         h.scalar_enable(np.zeros(w.mesh.n_cells))
+
+
+def test_cyclic_case_files_round_trip(tmp_path, oracle_binding):
+    """A rotational cyclic sector written as an OpenFOAM case (cyclic
+    polyPatches with their transform) and read back: same coupled geometry,
+    same residual."""
+    from test_foam_case import write_dicts
+
+    from icsfoam_gb300 import foam_case
+
+    w = cases.annular_sector(3, 5, 4, ordering_mode="natural")
+    foam_case.write_case(str(tmp_path), w.mesh, w.p, w.U, w.T)
+    write_dicts(str(tmp_path))
+    mesh, fields, settings, _ = foam_case.load_case(str(tmp_path))
+    for k in ("b_partner", "b_weights", "b_nbr_d", "b_delta_coeffs", "b_nonorth_delta_coeffs"):
+        assert np.allclose(getattr(mesh, k), getattr(w.mesh, k), rtol=1e-12, atol=1e-14), k
+    rot = {p.name: np.asarray(p.rotation) for p in mesh.patches if p.rotation is not None}
+    for p in w.mesh.patches:
+        if p.kind == M.PATCH_CYCLIC:
+            assert np.allclose(rot[p.name], p.rotation, atol=1e-14)
+    h1 = _open(oracle_binding, w.mesh, w.settings, w.p, w.U, w.T)
+    h2 = _open(oracle_binding, mesh, w.settings, fields["p"], fields["U"], fields["T"])
+    r1, r2 = h1.residual(), h2.residual()
+    assert np.abs(r1 - r2).max() <= 1e-11 * np.abs(r1).max()
+
+
+LS89 = __import__("os").path.join("/", "root", "reference", "tutorials", "VKI-LS89")
+
+
+@pytest.mark.skipif(not __import__("os").path.isdir(LS89), reason="reference tutorials not on this machine")
+def test_reads_the_reference_cascade_with_translational_cyclics(oracle_binding):
+    """The reference's VKI-LS89 turbine cascade (read in place, nothing
+    copied): its pitch-wise periodicity is a translational cyclic pair; the
+    pseudo iteration runs through the oracle (inviscid: viscous terms across
+    cyclic patches are not built)."""
+    from icsfoam_gb300 import foam_case
+
+    mesh, fields, settings, _ = foam_case.load_case(LS89)
+    names = [p.name for p in mesh.patches]
+    assert mesh.patches[names.index("Upper_periodicity")].kind == M.PATCH_CYCLIC
+    sel = mesh.b_partner >= 0
+    assert sel.sum() == 2 * 215
+    assert np.all((mesh.b_weights[sel] > 0) & (mesh.b_weights[sel] < 1))
+    st = dict(settings, viscous=0)
+    h = _open(oracle_binding, mesh, st, fields["p"], fields["U"], fields["T"])
+    h.begin_time_step()
+    s = h.pseudo_iteration()
+    assert np.isfinite(s.rho_l2_residual)
+    assert np.all(np.isfinite(h.get_state()["W"]))

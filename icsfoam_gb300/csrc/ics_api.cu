@@ -1335,8 +1335,8 @@ int ics_scalar_enable(ics_handle hh, const double* s, const int32_t* patch_fixed
     hh->h.err = "scalar transport is not provided for Harmonic Balance handles";
     return ICS_ERR_ARG;
   }
-  if (hh->h.m.ncyc > 0) {
-    hh->h.err = "scalar transport across cyclic patches is not built";
+  if (hh->h.m.ncyc > 0 && hh->h.cfg.c.viscous) {
+    hh->h.err = "the scalar's laplacian across cyclic patches is not built";
     return ICS_ERR_ARG;
   }
   return guard(hh, [&](Handle& h) {

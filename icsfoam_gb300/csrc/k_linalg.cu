@@ -1474,8 +1474,26 @@ __global__ void __launch_bounds__(RB) k_s_resid(int N, const double* __restrict_
   reduce_finish<1>(acc, partials, counter, out);
 }
 
+// scalar cyclic interfaces: y_c += sum over c's cyclic faces of a_f x_partner
+// (a_f in the upper slot of the scalar face coefficients)
+__global__ void k_s_cyc_mv(DevMesh m, const double* __restrict__ sface, int FB, const double* __restrict__ x,
+                           double* __restrict__ y) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= m.ncrow) return;
+  const int c = m.cyc_row[r];
+  double acc = y[c];
+  for (int e = m.cyc_ptr[r]; e < m.cyc_ptr[r + 1]; ++e) {
+    const int b = m.cyc_face[e];
+    acc += sface[FB + m.F + b] * x[m.bpartner[b]];
+  }
+  y[c] = acc;
+}
+
 static void s_spmv(Handle& h, const double* x, double* y) {
   ICS_LAUNCH(h, ICS_K_PASSIVE, k_s_spmv<<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, h.sblk, h.sdg, x, y));
+  if (h.m.ncrow)
+    ICS_LAUNCH(h, ICS_K_PASSIVE, k_s_cyc_mv<<<grid_for(h.m.ncrow, 128), 128, 0, h.stream>>>(h.m, h.sface, h.m.F + h.m.B,
+                                                                                            x, y));
 }
 
 static void s_precondition(Handle& h, double* r) {

@@ -991,6 +991,7 @@ __global__ void k_scalar_bface(DevMesh m, double Ds, int viscous, const double* 
                                double* __restrict__ out, int FB) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= m.B) return;
+  if (m.bpartner && m.bpartner[b] >= 0) return;  // cyclic faces: k_scalar_cface
   const int B = m.B, F = m.F, N = m.N;
   const int ci = m.bcell[b];
   const double ms = m.bmagSf[b];
@@ -1019,6 +1020,62 @@ __global__ void k_scalar_bface(DevMesh m, double Ds, int viscous, const double* 
   const double vic = sFixed[m.bpatch[b]] ? 0.0 : 1.0;
   const double flux = rb * (dot3(Ub, S) - um * ms) * vic;
   out[3 * FB + F + b] = 0.5 * ms * fabs(un - um) + flux * (1.0 / q[Q_RHO * N + ci]);
+}
+
+// Cyclic faces of the passive scalar: the face between this side's cell and
+// the partner (s, rho and the U components reconstructed as in k_cface), the
+// coupled half of insertBlock / the MRF divergence / the dissipation block,
+// the interface coefficient (no rotation: a scalar unknown) in the upper slot.
+__global__ void __launch_bounds__(128) k_scalar_cface(DevMesh m, ResParams P, int reconS,
+                                                      const double* __restrict__ q, const double* __restrict__ grad,
+                                                      const double* __restrict__ bq, const double* __restrict__ s,
+                                                      const double* __restrict__ sgrad, double* __restrict__ out,
+                                                      int FB) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m.ncyc) return;
+  const int N = m.N, F = m.F, B = m.B;
+  const int b = m.cyc_face[i];
+  const int o = m.bcell[b], pc = m.bpartner[b];
+  const double* R = m.patches[m.bpatch[b]].R;
+  const double sl = reconstruct_cyc(m, reconS, 0, b, o, pc, s[o], s[pc], sgrad, R, +1.0);
+  const double sr = reconstruct_cyc(m, reconS, 0, b, o, pc, s[o], s[pc], sgrad, R, -1.0);
+  const double qo = q[Q_RHO * N + o], qn = q[Q_RHO * N + pc];
+  const double rl = reconstruct_cyc(m, P.reconRho, Q_RHO, b, o, pc, qo, qn, grad, R, +1.0);
+  const double rr = reconstruct_cyc(m, P.reconRho, Q_RHO, b, o, pc, qo, qn, grad, R, -1.0);
+  double Ul[3], Ur[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int qk = Q_UX + k;
+    Ul[k] = reconstruct_cyc(m, P.reconU, qk, b, o, pc, q[qk * N + o], q[qk * N + pc], grad, R, +1.0);
+    Ur[k] = reconstruct_cyc(m, P.reconU, qk, b, o, pc, q[qk * N + o], q[qk * N + pc], grad, R, -1.0);
+  }
+  const double ms = m.bmagSf[b];
+  const double n[3] = {m.bnf[b], m.bnf[B + b], m.bnf[2 * B + b]};
+  const double rSl = rl * sl, rSr = rr * sr;
+  const double coefR = sqrt(fmax(VSMALL, rr) / fmax(VSMALL, rl));
+  double roeU[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) roeU[k] = (coefR * Ur[k] + Ul[k]) / (coefR + 1.0);
+  const double um = m.mrfU ? m.mrfU[F + b] : 0.0;
+  double lam = fabs(dot3(roeU, n) - um);
+  const double eps = 0.05 * lam;
+  if (lam < eps) lam = (lam * lam + eps * eps) / (2.0 * eps);
+  const double unl = dot3(Ul, n), unr = dot3(Ur, n);
+  double ph = -0.5 * ms * lam * (rSr - rSl);
+  ph += 0.5 * ms * (rl * unl * sl + rr * unr * sr);
+  ph -= 0.5 * ms * um * (rSl + rSr);
+  // LF dissipation with the coupled patch value of U (the rotated interpolate)
+  const double Ub[3] = {bq[Q_UX * B + b], bq[Q_UY * B + b], bq[Q_UZ * B + b]};
+  const double d = 0.5 * ms * fabs(dot3(Ub, n) - um);
+  double up = 0.5 * ms * unr, lo = -0.5 * ms * unl;
+  if (um != 0.0) {
+    const double phm = um * ms, wb = m.bw[b];
+    up -= phm * (1.0 - wb);
+    lo -= -phm * wb;
+  }
+  out[F + b] = ph;
+  out[FB + F + b] = up - d;
+  out[3 * FB + F + b] = -lo + d;
 }
 
 __global__ void __launch_bounds__(128) k_scalar_rows(DevMesh m, CellResParams D, const double* __restrict__ face,
@@ -1078,6 +1135,10 @@ __global__ void k_scalar_bc(DevMesh m, const double* __restrict__ s, const int* 
   if (b >= m.B) return;
   const int pi = m.bpatch[b];
   sB[b] = sFixed[pi] ? sValue[pi] : s[m.bcell[b]];
+  if (m.bpartner && m.bpartner[b] >= 0) {  // coupled evaluate
+    const int pc = m.bpartner[b];
+    sB[b] = m.bw[b] * (s[m.bcell[b]] - s[pc]) + s[pc];
+  }
 }
 
 static CellResParams ddt_params(const Handle& h) {
@@ -1127,6 +1188,9 @@ void launch_scalar_assembly(Handle& h) {
   if (B)
     ICS_LAUNCH(h, ICS_K_PASSIVE, k_scalar_bface<<<grid_for(B, 128), 128, 0, h.stream>>>(
                                      h.m, h.Ds, viscous, h.bq, h.q, h.ss, h.ssB, h.sFixed, h.sface, FB));
+  if (h.m.ncyc)
+    ICS_LAUNCH(h, ICS_K_PASSIVE, k_scalar_cface<<<grid_for(h.m.ncyc, 128), 128, 0, h.stream>>>(
+                                     h.m, P, rs, h.q, h.grad, h.bq, h.ss, h.sgrad, h.sface, FB));
   ICS_LAUNCH(h, ICS_K_PASSIVE, k_scalar_rows<<<grid_for(N, 128), 128, 0, h.stream>>>(
                                    h.m, ddt_params(h), h.sface, FB, h.srhoS, h.srhoS0, h.srhoS00, h.rPDT, h.ssrc,
                                    h.sblk, h.sdg, h.srD, &h.ks->status));

@@ -1952,12 +1952,17 @@ bool pseudoLoop(Case& c) {
 // ---------------------------------------------------------------------------
 struct SMat {
   std::vector<double> diag, lower, upper;
+  std::vector<double> iface;  // [B] coupled (cyclic) interface coefficients
 };
 
 void scalarBoundary(Case& c) {
   for (int b = 0; b < c.B; ++b) {
     const int pi = c.bpatch[b];
     c.sB[b] = c.sFixed[pi] ? c.sValue[pi] : c.s[c.bcell[b]];
+    if (isCyc(c, b)) {  // coupled evaluate
+      const int pc = c.bpartner[b];
+      c.sB[b] = c.bw[b] * (c.s[c.bcell[b]] - c.s[pc]) + c.s[pc];
+    }
   }
 }
 
@@ -1968,6 +1973,9 @@ void smatMul(const Case& c, const SMat& A, const double* x, double* y) {
     y[u] += A.lower[fi] * x[l];
     y[l] += A.upper[fi] * x[u];
   }
+  if (!A.iface.empty())
+    for (int b = 0; b < c.B; ++b)
+      if (isCyc(c, b)) y[c.bcell[b]] += A.iface[b] * x[c.bpartner[b]];
 }
 
 // lusgs.C:50-385 with one scalar equation, sequential in cell order
@@ -2183,6 +2191,24 @@ int scalarTransportStep(Case& c, ics_solver_perf& perf) {
     A.diag[c.own[fi]] -= lo;
     A.diag[c.nei[fi]] -= up;
   }
+  // coupled (cyclic) faces: interface 0.5|S| U_r.n, diagonal -(-0.5|S| U_l.n)
+  if (c.hasCyc) {
+    A.iface.assign(B, 0.0);
+    for (int b = 0; b < B; ++b) {
+      if (!isCyc(c, b)) continue;
+      const int fi = F + b;
+      const V3 n = c.bSf[b] / c.bmagSf[b];
+      const double up = 0.5 * c.bmagSf[b] * dot(U_r[fi], n);
+      const double lo = -0.5 * c.bmagSf[b] * dot(U_l[fi], n);
+      A.iface[b] += up;
+      A.diag[c.bcell[b]] -= lo;
+      if (c.mrfOn) {
+        const double phm = c.mrfU[fi] * c.bmagSf[b];
+        A.iface[b] -= phm * (1 - c.bw[b]);
+        A.diag[c.bcell[b]] -= phm * c.bw[b];
+      }
+    }
+  }
   // MRF: -div(w, u_MRF |S|) (lines 217-219)
   if (c.mrfOn)
     for (int fi = 0; fi < F; ++fi) {
@@ -2207,12 +2233,15 @@ int scalarTransportStep(Case& c, ics_solver_perf& perf) {
     A.diag[nb] += d;
   }
   for (int b = 0; b < B; ++b) {
+    // (on a coupled face U_B is the interpolate of U with the partner rotated)
     const double lc = std::fabs(dot(c.UB[b], c.bSf[b] / c.bmagSf[b]) - umOf(c, F + b));
     A.diag[c.bcell[b]] += 0.5 * c.bmagSf[b] * lc;
+    if (isCyc(c, b)) A.iface[b] -= 0.5 * c.bmagSf[b] * lc;
   }
   // geometric boundaries: rho_B (U_B . S_B) valueInternalCoeffs / rho_I
   for (int b = 0; b < B; ++b) {
     const int ci = c.bcell[b];
+    if (isCyc(c, b)) continue;
     const double vic = c.sFixed[c.bpatch[b]] ? 0.0 : 1.0;
     const double flux = rhoBof(c, b) * (dot(c.UB[b], c.bSf[b]) - umOf(c, F + b) * c.bmagSf[b]) * vic;
     A.diag[ci] += flux * (1.0 / c.rho[ci]);
@@ -2763,7 +2792,7 @@ int icsref_scalar_enable(ics_handle h, const double* s, const int32_t* patch_fix
                          double D, int32_t recon) {
   if (!h || !s || recon < 0 || recon > ICS_RECON_MUSCL_MINMOD || D < 0) return ICS_ERR_ARG;
   Case& c = *h;
-  if (c.hasCyc) return ICS_ERR_ARG;  // scalar transport across cyclic patches is not built
+  if (c.hasCyc && c.cfg.viscous) return ICS_ERR_ARG;  // laplacian across cyclic patches is not built
   if (c.nInst > 1) {
     c.err = "scalar transport is not provided for Harmonic Balance handles";
     return ICS_ERR_ARG;

@@ -136,13 +136,31 @@ def test_rotational_cyclic_equals_doubled_sector(oracle_binding, flux, recon):
     assert (np.abs(yb[rows] - ya) / sc).max() < 1e-10
 
 
-def test_cyclic_rejects_viscous_and_scalar(oracle_binding):
+def test_cyclic_rejects_viscous(oracle_binding):
     w = cases.annular_sector(3, 4, 4, ordering_mode="natural")
     with pytest.raises(abi.IcsError):
         abi.CaseHandle(oracle_binding, w.mesh, cases.make_config(oracle_binding, w.settings, viscous=1))
-    h = _open(oracle_binding, w.mesh, w.settings, w.p, w.U, w.T)
-    with pytest.raises(abi.IcsError):
-        h.scalar_enable(np.zeros(w.mesh.n_cells))
+
+
+@pytest.mark.parametrize("recon", [0, 3])
+def test_scalar_across_translational_cyclic_equals_doubled_span(oracle_binding, recon):
+    """Passive scalar: one transport step from a periodic s (block-Jacobi
+    preconditioning, which both domains share) gives the short domain's s in
+    the long one."""
+    ma, mb = _bump(3, 0.3), _bump(6, 0.6)
+    st = dict(cases.bump_channel(4, 2, 2).settings, preconditioner=2, max_iter=50, rel_tol=1e-12,
+              tolerance=1e-30)
+    out = []
+    for m in (ma, mb):
+        h = _open(oracle_binding, m, st, *_periodic_state(m, 0.3))
+        x, y, z = m.C.T
+        s0 = 0.5 + 0.3 * np.sin(2 * np.pi * z / 0.3 + 0.2) * np.cos(2 * x + 0.1) + 0.1 * y
+        fixed = np.array([p.name == "inlet" for p in m.patches], np.int32)
+        h.scalar_enable(s0, fixed, np.where(fixed == 1, 0.8, 0.0), recon=recon)
+        h.scalar_transport(1)
+        out.append(h.get_scalar()[0])
+    rows = _rows(ma, mb)
+    assert np.abs(out[1][rows] - out[0]).max() < 1e-10
 
 
 def test_cyclic_case_files_round_trip(tmp_path, oracle_binding):

@@ -158,10 +158,23 @@ def test_cyclic_tangent_and_exact_jacobian(gpu_binding, oracle_binding):
     assert abs(lhs - rhs) <= 1e-11 * (np.abs(u * jv).sum() + np.abs(jtu * v).sum())
 
 
-def test_cyclic_rejections(gpu_binding):
+def test_cyclic_rejects_viscous(gpu_binding):
     w = sector()
     with pytest.raises(abi.IcsError):
         abi.CaseHandle(gpu_binding, w.mesh, cases.make_config(gpu_binding, w.settings, viscous=1))
-    h = open_case(gpu_binding, w)
-    with pytest.raises(abi.IcsError):
-        h.scalar_enable(np.zeros(w.mesh.n_cells))
+
+
+@pytest.mark.parametrize("recon,mrf", [(3, False), (1, True)])
+def test_cyclic_passive_scalar(gpu_binding, oracle_binding, recon, mrf):
+    w = sector("HLLC")
+    hg, ho = open_case(gpu_binding, w, mrf=mrf), open_case(oracle_binding, w, mrf=mrf)
+    x, y, z = w.mesh.C.T
+    s0 = 0.5 + 0.4 * np.sin(40.0 * z + 0.3) * np.cos(30.0 * y + 0.1) + 0.2 * x
+    fixed = np.array([p.name == "inlet" for p in w.mesh.patches], np.int32)
+    for h in (hg, ho):
+        h.scalar_enable(s0, fixed, np.where(fixed == 1, 0.9, 0.0), D=0.0, recon=recon)
+        h.begin_time_step()
+        h.pseudo_iteration()
+    pg, po = hg.scalar_transport(3), ho.scalar_transport(3)
+    assert pg.n_iterations == po.n_iterations
+    assert np.abs(hg.get_scalar()[0] - ho.get_scalar()[0]).max() < 1e-10

@@ -525,7 +525,7 @@ int do_residual(Handle& h, double* host_src) {
     if (!h.vcell) {
       h.vcell = dalloc<double>(24ull * h.m.N);
       h.fvisc = dalloc<double>(8ull * (h.m.F + h.m.B));
-      h.vsf2 = dalloc<double>((size_t)h.m.F);
+      h.vsf2 = dalloc<double>((size_t)h.m.F + h.m.B);
     }
     launch_viscous(h);
   }
@@ -719,7 +719,6 @@ int ics_create(const ics_mesh_desc* mesh, const ics_config* cfg, ics_handle* out
   st = guard(hh, [&](Handle& hd) {
     ICS_CUDA(cudaStreamCreateWithFlags(&hd.stream, cudaStreamNonBlocking));
     build_mesh(hd, mesh);
-    if (hd.m.ncyc > 0 && cfg->viscous) throw std::string("viscous terms across cyclic patches are not built");
     alloc_state(hd);
     ensure_workspace(hd);
     std::vector<double> co(hd.m.N, cfg->pseudo_co_num);
@@ -754,10 +753,7 @@ int ics_set_config(ics_handle hh, const ics_config* cfg) {
     hh->h.err = "Harmonic Balance needs steadyState ddt and the GMRES solver";
     return ICS_ERR_ARG;
   }
-  if (hh->h.m.ncyc > 0 && cfg->viscous) {
-    hh->h.err = "viscous terms across cyclic patches are not built";
-    return ICS_ERR_ARG;
-  }
+
   return guard(hh, [&](Handle& h) {
     const bool structural = cfg->precision != h.cfg.c.precision || cfg->n_directions != h.cfg.c.n_directions;
     h.cfg.c = *cfg;

@@ -159,7 +159,8 @@ __global__ void k_jac_boundary(DevMesh m, double R, double Cv, double gamma, con
 // blockFvMatrix.C:386-407), so the stored block is U_f diag(1, R, 1).
 template <typename T>
 __global__ void k_jac_cyclic(DevMesh m, double gamma, const double* __restrict__ cfrec,
-                             const double* __restrict__ flam, double* __restrict__ bjac, T* __restrict__ cblk) {
+                             const double* __restrict__ flam, double* __restrict__ bjac, T* __restrict__ cblk,
+                             const double* __restrict__ vsf2) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m.ncyc) return;
   const int B = m.B, nc = m.ncyc;
@@ -177,6 +178,8 @@ __global__ void k_jac_cyclic(DevMesh m, double gamma, const double* __restrict__
   double phm = 0.0;
   if (m.mrfU) phm = m.mrfU[m.F + b] * magS;
   const double wb = m.bw[b];
+  // viscous LF: the coupled laplacian's diagonal and interface (viscousFluxScheme.C:234-247)
+  const double sv = vsf2 ? vsf2[m.F + b] : 0.0;
   double D[25], U[25];
 #pragma unroll
   for (int r = 0; r < 5; ++r)
@@ -190,6 +193,8 @@ __global__ void k_jac_cyclic(DevMesh m, double gamma, const double* __restrict__
         up -= phm * (1.0 - wb);
         dg += d;
         up -= d;
+        dg += sv;
+        up -= sv;
       }
       D[k] = dg;
       U[k] = up;
@@ -382,10 +387,12 @@ void launch_jacobian(Handle& h) {
   if (h.m.ncyc > 0) {
     if (prec(h) == ICS_PREC_MIXED)
       ICS_LAUNCH(h, ICS_K_JAC_BOUNDARY, k_jac_cyclic<float><<<grid_for(h.m.ncyc, 128), 128, 0, h.stream>>>(
-                                            h.m, h.cfg.gamma, h.cfrec, h.flam, h.bjac, (float*)h.cblk));
+                                            h.m, h.cfg.gamma, h.cfrec, h.flam, h.bjac, (float*)h.cblk,
+                                            h.cfg.c.viscous ? h.vsf2 : nullptr));
     else
       ICS_LAUNCH(h, ICS_K_JAC_BOUNDARY, k_jac_cyclic<double><<<grid_for(h.m.ncyc, 128), 128, 0, h.stream>>>(
-                                            h.m, h.cfg.gamma, h.cfrec, h.flam, h.bjac, (double*)h.cblk));
+                                            h.m, h.cfg.gamma, h.cfrec, h.flam, h.bjac, (double*)h.cblk,
+                                            h.cfg.c.viscous ? h.vsf2 : nullptr));
   }
   if (prec(h) == ICS_PREC_MIXED) {
     ICS_LAUNCH(h, ICS_K_JAC_ROWS, k_jac_rows<float><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, h.cfg.gamma, h.frec, h.flam, h.bjac,

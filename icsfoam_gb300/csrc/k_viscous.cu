@@ -67,6 +67,22 @@ __global__ void __launch_bounds__(128) k_visc_cell(DevMesh m, ViscParams P, cons
   for (int e = m.bptr[c]; e < m.bptr[c + 1]; ++e) {
     const int b = m.bface[e];
     const double S[3] = {m.bSf[b], m.bSf[B + b], m.bSf[2 * B + b]};
+    const int pc = m.bpartner ? m.bpartner[b] : -1;
+    if (pc >= 0) {
+      // coupled face: interpolate with the partner, its velocity rotated
+      const double* Rm = m.patches[m.bpatch[b]].R;
+      const double wb = m.bw[b];
+      const Real Un[3] = {prim[2 * N + pc], prim[3 * N + pc], prim[4 * N + pc]};
+      const Real en = W[5 * pc + 4] / W[5 * pc] - 0.5 * dot3(Un, Un);
+      for (int j = 0; j < 3; ++j) {
+        const Real up = Rm[3 * j] * Un[0] + Rm[3 * j + 1] * Un[1] + Rm[3 * j + 2] * Un[2];
+        const Real sf = wb * (Uc[j] - up) + up;
+        for (int i = 0; i < 3; ++i) g[3 * i + j] += S[i] * sf;
+      }
+      const Real sf = wb * (ec - en) + en;
+      for (int i = 0; i < 3; ++i) ge[i] += S[i] * sf;
+      continue;
+    }
     const double Ub[3] = {UB[b], UB[B + b], UB[2 * B + b]};
     const double eb = P.Cv * TB[b];
     for (int j = 0; j < 3; ++j)
@@ -142,6 +158,7 @@ __global__ void k_visc_bface(DevMesh m, ViscParams P, const Real* __restrict__ v
                              int FB) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= m.B) return;
+  if (m.bpartner && m.bpartner[b] >= 0) return;  // cyclic faces: k_visc_cface
   const int N = m.N, B = m.B, F = m.F;
   const int o = m.bcell[b];
   const double ms = m.bmagSf[b];
@@ -178,6 +195,72 @@ __global__ void k_visc_bface(DevMesh m, ViscParams P, const Real* __restrict__ v
   fv[7 * FB + F + b] = (alB * ms) * snE;
 }
 
+// Cyclic faces: the internal-face terms with the partner's vectors rotated
+// (R v) and its tensors rotated (R t R^T) into this side's frame, the
+// partner-side centre at C + delta (coupled snGrad and its non-orthogonal
+// correction), plus the LF coefficient of the coupled laplacian.
+template <typename Real = double>
+__global__ void __launch_bounds__(128) k_visc_cface(DevMesh m, const Real* __restrict__ vc,
+                                                    const Real* __restrict__ W, const Real* __restrict__ prim,
+                                                    Real* __restrict__ fv, double* __restrict__ sf2, int FB) {
+  const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i0 >= m.ncyc) return;
+  const int N = m.N, F = m.F, B = m.B;
+  const int b = m.cyc_face[i0];
+  const int o = m.bcell[b], pc = m.bpartner[b];
+  const double* Rm = m.patches[m.bpatch[b]].R;
+  const double wf = m.bw[b];
+  auto lin = [&](const Real& a, const Real& bb) { return wf * (a - bb) + bb; };
+  const Real muf = lin(vc[21 * N + o], vc[21 * N + pc]), alf = lin(vc[22 * N + o], vc[22 * N + pc]);
+  const double ms = m.bmagSf[b];
+  const double S[3] = {m.bSf[b], m.bSf[B + b], m.bSf[2 * B + b]};
+  const double nodc = m.bnodc[b];
+  double k[3];
+  for (int i = 0; i < 3; ++i) k[i] = m.bnf[i * B + b] - m.bdelta[i * B + b] * nodc;
+  Real gUf[9], tf[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      Real sg = 0, st = 0;
+      for (int kk = 0; kk < 3; ++kk)
+        for (int l = 0; l < 3; ++l) {
+          sg += Rm[3 * i + kk] * vc[(3 * kk + l) * N + pc] * Rm[3 * j + l];
+          st += Rm[3 * i + kk] * vc[(12 + 3 * kk + l) * N + pc] * Rm[3 * j + l];
+        }
+      gUf[3 * i + j] = lin(vc[(3 * i + j) * N + o], sg);
+      tf[3 * i + j] = lin(vc[(12 + 3 * i + j) * N + o], st);
+    }
+  const Real Un[3] = {prim[2 * N + pc], prim[3 * N + pc], prim[4 * N + pc]};
+  Real Uf[3], snU[3];
+  for (int j = 0; j < 3; ++j) {
+    const Real up = Rm[3 * j] * Un[0] + Rm[3 * j + 1] * Un[1] + Rm[3 * j + 2] * Un[2];
+    const Real uo = prim[(2 + j) * N + o];
+    Uf[j] = lin(uo, up);
+    const Real corr = k[0] * gUf[j] + k[1] * gUf[3 + j] + k[2] * gUf[6 + j];
+    snU[j] = nodc * (up - uo) + corr;
+  }
+  const Real ml = muf * ms;
+  for (int j = 0; j < 3; ++j) fv[j * FB + F + b] = ml * snU[j];
+  for (int j = 0; j < 3; ++j) fv[(3 + j) * FB + F + b] = S[0] * tf[j] + S[1] * tf[3 + j] + S[2] * tf[6 + j];
+  Real sig[3];
+  for (int i = 0; i < 3; ++i) {
+    Real s = 0;
+    for (int j = 0; j < 3; ++j) s += (muf * gUf[3 * i + j] + tf[3 * i + j]) * Uf[j];
+    sig[i] = s;
+  }
+  fv[6 * FB + F + b] = dot3(sig, S);
+  Real gef[3];
+  for (int i = 0; i < 3; ++i) {
+    const Real gp = Rm[3 * i] * vc[9 * N + pc] + Rm[3 * i + 1] * vc[10 * N + pc] + Rm[3 * i + 2] * vc[11 * N + pc];
+    gef[i] = lin(vc[(9 + i) * N + o], gp);
+  }
+  const Real snE = nodc * (vc[23 * N + pc] - vc[23 * N + o]) + dot3(k, gef);
+  fv[7 * FB + F + b] = (alf * ms) * snE;
+  if constexpr (std::is_same<Real, double>::value) {
+    const double rhof = lin(W[5 * o], W[5 * pc]);
+    sf2[F + b] = 0.5 * ((muf + alf) / rhof) * ms * m.bdc[b];
+  }
+}
+
 void launch_viscous(Handle& h) {
   if (!h.cfg.c.viscous) return;
   ViscParams P;
@@ -199,6 +282,9 @@ void launch_viscous(Handle& h) {
   if (h.m.B)
     ICS_LAUNCH(h, ICS_K_VISC, k_visc_bface<<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, P, h.vcell, h.prim, h.TB,
                                                                                         h.UB, h.fvisc, FB));
+  if (h.m.ncyc)
+    ICS_LAUNCH(h, ICS_K_VISC, k_visc_cface<<<grid_for(h.m.ncyc, 128), 128, 0, h.stream>>>(h.m, h.vcell, h.W, h.prim,
+                                                                                           h.fvisc, h.vsf2, FB));
   ICS_CUDA(cudaGetLastError());
 }
 
@@ -223,6 +309,9 @@ void launch_viscous_tangent(Handle& h, const Dual* W, const Dual* prim, Dual* vc
   if (h.m.B)
     ICS_LAUNCH(h, ICS_K_TANGENT, k_visc_bface<Dual><<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, P, vc, prim, h.TB,
                                                                                                 h.UB, fv, FB));
+  if (h.m.ncyc)
+    ICS_LAUNCH(h, ICS_K_TANGENT, k_visc_cface<Dual><<<grid_for(h.m.ncyc, 128), 128, 0, h.stream>>>(h.m, vc, W, prim, fv,
+                                                                                                   nullptr, FB));
   ICS_CUDA(cudaGetLastError());
 }
 

@@ -733,11 +733,32 @@ void gaussGradVec(const Case& c, const std::vector<V3>& in, const std::vector<V3
       }
     }
   }
-  for (int b = 0; b < c.B; ++b)
+  for (int b = 0; b < c.B; ++b) {
+    V3 fb = bf[b];
+    if (isCyc(c, b)) {  // coupled: interpolate with the partner's vector rotated
+      const V3 up = rotP(c, b, in[c.bpartner[b]]);
+      const V3& uo = in[c.bcell[b]];
+      for (int j = 0; j < 3; ++j) fb[j] = c.bw[b] * (uo[j] - up[j]) + up[j];
+    }
     for (int j = 0; j < 3; ++j)
-      for (int i = 0; i < 3; ++i) g[c.bcell[b]].a[3 * i + j] += c.bSf[b][i] * bf[b][j];
+      for (int i = 0; i < 3; ++i) g[c.bcell[b]].a[3 * i + j] += c.bSf[b][i] * fb[j];
+  }
   for (int k = 0; k < c.N; ++k)
     for (int q = 0; q < 9; ++q) g[k].a[q] /= c.V[k];
+}
+
+// R T R^T of a tensor with the rotation of boundary face b's patch
+inline T9 rotT(const Case& c, int b, const T9& t) {
+  const double* R = c.patches[c.bpatch[b]].R;
+  T9 o;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0;
+      for (int k = 0; k < 3; ++k)
+        for (int l = 0; l < 3; ++l) s += R[3 * i + k] * t.a[3 * k + l] * R[3 * j + l];
+      o.a[3 * i + j] = s;
+    }
+  return o;
 }
 
 struct Viscous {
@@ -829,10 +850,50 @@ void viscousFluxes(const Case& c, const Viscous& v, std::vector<V3>& lapU, std::
     const double lamv = (muf + alf) / rhof;
     sf2[fi] = 0.5 * lamv * ms * c.dc[fi];
   }
+  if (c.hasCyc) sf2.resize(c.F + c.B, 0.0);  // coupled faces keep their own coefficient
   for (int b = 0; b < c.B; ++b) {
     const int o = c.bcell[b];
     const double ms = c.bmagSf[b];
     const V3 n = c.bSf[b] / ms;
+    if (isCyc(c, b)) {
+      // coupled face: the internal-face formulas with the partner's vectors
+      // and tensors rotated into this side's frame (patchNeighbourField)
+      const int pc = c.bpartner[b];
+      const double wf = c.bw[b];
+      auto lin = [&](double a, double bb) { return wf * (a - bb) + bb; };
+      const double muf = lin(v.mu[o], v.mu[pc]), alf = lin(v.al[o], v.al[pc]);
+      const V3 kcor = n - c.bdelta[b] * c.bnodc[b];
+      const T9 gUp = rotT(c, b, v.gU[pc]), tp = rotT(c, b, v.tau[pc]);
+      T9 gUf, tf;
+      for (int q = 0; q < 9; ++q) {
+        gUf.a[q] = lin(v.gU[o].a[q], gUp.a[q]);
+        tf.a[q] = lin(v.tau[o].a[q], tp.a[q]);
+      }
+      const V3 Up = rotP(c, b, c.U[pc]);
+      V3 Uf, snUc;
+      for (int j = 0; j < 3; ++j) {
+        Uf[j] = lin(c.U[o][j], Up[j]);
+        const double corr = kcor.x * gUf.a[j] + kcor.y * gUf.a[3 + j] + kcor.z * gUf.a[6 + j];
+        snUc[j] = c.bnodc[b] * (Up[j] - c.U[o][j]) + corr;
+      }
+      lapU[c.F + b] = (muf * ms) * snUc;
+      for (int j = 0; j < 3; ++j)
+        divTau[c.F + b][j] = c.bSf[b].x * tf.a[j] + c.bSf[b].y * tf.a[3 + j] + c.bSf[b].z * tf.a[6 + j];
+      V3 sig;
+      for (int i = 0; i < 3; ++i) {
+        double s = 0;
+        for (int j = 0; j < 3; ++j) s += (muf * gUf.a[3 * i + j] + tf.a[3 * i + j]) * Uf[j];
+        sig[i] = s;
+      }
+      divSig[c.F + b] = dot(sig, c.bSf[b]);
+      const V3 gep = rotP(c, b, v.ge[pc]);
+      const V3 gef(lin(v.ge[o].x, gep.x), lin(v.ge[o].y, gep.y), lin(v.ge[o].z, gep.z));
+      const double snEc = c.bnodc[b] * (v.e[pc] - v.e[o]) + dot(kcor, gef);
+      lapE[c.F + b] = (alf * ms) * snEc;
+      const double rhof = lin(c.rho[o], c.rho[pc]);
+      sf2[c.F + b] = 0.5 * ((muf + alf) / rhof) * ms * c.bdc[b];
+      continue;
+    }
     V3 snU;
     for (int j = 0; j < 3; ++j) snU[j] = (c.UB[b][j] - c.U[o][j]) * c.bdc[b];
     const double snE = (v.eB[b] - v.e[o]) * c.bdc[b];
@@ -1317,7 +1378,7 @@ void assembleJacobian(Case& c) {
   }
   // viscousFluxScheme::createViscousJacobian, LaxFriedrichJacobian:
   // minus laplacian(0.5 lambda_v, 1) on rho, rhoU (x I), rhoE (viscousFluxScheme.C:234-247)
-  if (c.cfg.viscous && (int)c.viscSf2.size() == c.F) {
+  if (c.cfg.viscous && (int)c.viscSf2.size() >= c.F) {
     for (int fi = 0; fi < c.F; ++fi) {
       const double s = c.viscSf2[fi];
       for (int q = 0; q < 5; ++q) {
@@ -1328,6 +1389,16 @@ void assembleJacobian(Case& c) {
         c.diag[c.nei[fi]].a[k] += s;
       }
     }
+    // coupled faces: the laplacian's interface and diagonal (blockFvOperatorsTemplates.C:428-448)
+    if ((int)c.viscSf2.size() == c.F + c.B)
+      for (int b = 0; b < c.B; ++b) {
+        if (!isCyc(c, b)) continue;
+        const double s = c.viscSf2[c.F + b];
+        for (int q = 0; q < 5; ++q) {
+          c.iface[b].a[diagIdx[q]] -= s;
+          c.diag[c.bcell[b]].a[diagIdx[q]] += s;
+        }
+      }
   }
   // Harmonic Balance diagonal V D_JJ on every equation (HBZone.C:435-518)
   if (c.nInst > 1) {
@@ -2325,10 +2396,6 @@ void icsref_default_config(ics_config* c) {
 
 int icsref_set_config(ics_handle h, const ics_config* cfg) {
   if (!h || !cfg) return ICS_ERR_ARG;
-  if (h->hasCyc && cfg->viscous) {
-    h->err = "viscous terms across cyclic patches are not built";
-    return ICS_ERR_ARG;
-  }
   if (cfg->flux_scheme < 0 || cfg->flux_scheme > 2) {
     h->err = "Unknown convectiveFluxScheme";
     return ICS_ERR_SCHEME;
@@ -2413,7 +2480,7 @@ int icsref_create(const ics_mesh_desc* m, const ics_config* cfg, ics_handle* out
     c.patches.push_back(q);
   }
   if (c.hasCyc) {
-    if (!m->b_partner || !m->b_weights || !m->b_nbr_d || cfg->viscous) {
+    if (!m->b_partner || !m->b_weights || !m->b_nbr_d) {
       delete h;
       return ICS_ERR_ARG;
     }
@@ -2792,7 +2859,7 @@ int icsref_scalar_enable(ics_handle h, const double* s, const int32_t* patch_fix
                          double D, int32_t recon) {
   if (!h || !s || recon < 0 || recon > ICS_RECON_MUSCL_MINMOD || D < 0) return ICS_ERR_ARG;
   Case& c = *h;
-  if (c.hasCyc && c.cfg.viscous) return ICS_ERR_ARG;  // laplacian across cyclic patches is not built
+  if (c.hasCyc && c.cfg.viscous) return ICS_ERR_ARG;  // the scalar's laplacian across cyclic patches is not built
   if (c.nInst > 1) {
     c.err = "scalar transport is not provided for Harmonic Balance handles";
     return ICS_ERR_ARG;

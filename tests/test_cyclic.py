@@ -14,6 +14,9 @@ short one are ordinary internal faces.  Checked for
   here is axial (the components are frame-independent) with theta-periodic
   scalar fields; the Jacobian action is checked on a vector whose momentum
   is periodic in cylindrical components.
+* the viscous terms (Gauss gradients of U and e, laplacians with the
+  non-orthogonal correction, div(tauMC), div(sigmaDotU . S), the LF viscous
+  Jacobian) across both kinds of pair.
 """
 
 import numpy as np
@@ -73,10 +76,15 @@ def test_cyclic_geometry():
         M.hex_mesh(g, {"xmin": a, "xmax": b, "ymin": a, "ymax": b, "zmin": a, "zmax": b})
 
 
-@pytest.mark.parametrize("flux,recon", [("HLLC", 3), ("AUSMPlusUp", 3), ("ROE", 3), ("HLLC", 1), ("AUSMPlusUp", 0)])
-def test_translational_cyclic_equals_doubled_span(oracle_binding, flux, recon):
+VISCOUS = dict(viscous=1, sutherland=1, As=1.458e-6, Ts=110.4, Pr=0.72)
+
+
+@pytest.mark.parametrize("flux,recon,viscous", [("HLLC", 3, 0), ("AUSMPlusUp", 3, 0), ("ROE", 3, 0), ("HLLC", 1, 0),
+                                                ("AUSMPlusUp", 0, 0), ("AUSMPlusUp", 3, 1), ("HLLC", 1, 1)])
+def test_translational_cyclic_equals_doubled_span(oracle_binding, flux, recon, viscous):
     ma, mb = _bump(3, 0.3), _bump(6, 0.6)
-    st = dict(cases.bump_channel(4, 2, 2, flux=flux).settings, recon_rho=recon, recon_U=recon, recon_T=recon)
+    st = dict(cases.bump_channel(4, 2, 2, flux=flux).settings, recon_rho=recon, recon_U=recon, recon_T=recon,
+              **(VISCOUS if viscous else {}))
     ha = _open(oracle_binding, ma, st, *_periodic_state(ma, 0.3))
     hb = _open(oracle_binding, mb, st, *_periodic_state(mb, 0.3))
     rows = _rows(ma, mb)
@@ -106,11 +114,12 @@ def _sector_state(mesh):
     return p, U, T, r, th
 
 
-@pytest.mark.parametrize("flux,recon", [("HLLC", 3), ("ROE", 1), ("AUSMPlusUp", 3)])
-def test_rotational_cyclic_equals_doubled_sector(oracle_binding, flux, recon):
+@pytest.mark.parametrize("flux,recon,viscous", [("HLLC", 3, 0), ("ROE", 1, 0), ("AUSMPlusUp", 3, 0),
+                                                ("AUSMPlusUp", 3, 1)])
+def test_rotational_cyclic_equals_doubled_sector(oracle_binding, flux, recon, viscous):
     wa = cases.annular_sector(4, 6, 5, sector_deg=20.0, ordering_mode="natural", flux=flux)
     wb = cases.annular_sector(4, 12, 5, sector_deg=40.0, theta0_deg=-10.0, ordering_mode="natural", flux=flux)
-    st = dict(wa.settings, recon_rho=recon, recon_U=recon, recon_T=recon)
+    st = dict(wa.settings, recon_rho=recon, recon_U=recon, recon_T=recon, **(VISCOUS if viscous else {}))
     pa, Ua, Ta, _, _ = _sector_state(wa.mesh)
     pb, Ub, Tb, rb_, thb = _sector_state(wb.mesh)
     ha = _open(oracle_binding, wa.mesh, st, pa, Ua, Ta)
@@ -136,10 +145,11 @@ def test_rotational_cyclic_equals_doubled_sector(oracle_binding, flux, recon):
     assert (np.abs(yb[rows] - ya) / sc).max() < 1e-10
 
 
-def test_cyclic_rejects_viscous(oracle_binding):
+def test_cyclic_rejects_a_viscous_scalar(oracle_binding):
     w = cases.annular_sector(3, 4, 4, ordering_mode="natural")
+    h = _open(oracle_binding, w.mesh, dict(w.settings, **VISCOUS), w.p, w.U, w.T)
     with pytest.raises(abi.IcsError):
-        abi.CaseHandle(oracle_binding, w.mesh, cases.make_config(oracle_binding, w.settings, viscous=1))
+        h.scalar_enable(np.zeros(w.mesh.n_cells), D=1e-5)
 
 
 @pytest.mark.parametrize("recon", [0, 3])
@@ -193,9 +203,9 @@ LS89 = __import__("os").path.join("/", "root", "reference", "tutorials", "VKI-LS
 @pytest.mark.skipif(not __import__("os").path.isdir(LS89), reason="reference tutorials not on this machine")
 def test_reads_the_reference_cascade_with_translational_cyclics(oracle_binding):
     """The reference's VKI-LS89 turbine cascade (read in place, nothing
-    copied): its pitch-wise periodicity is a translational cyclic pair; the
-    pseudo iteration runs through the oracle (inviscid: viscous terms across
-    cyclic patches are not built)."""
+    copied): its pitch-wise periodicity is a translational cyclic pair; a
+    laminar viscous pseudo iteration (the case's constant mu; its turbulence
+    model is outside the path) runs through the oracle."""
     from icsfoam_gb300 import foam_case
 
     mesh, fields, settings, _ = foam_case.load_case(LS89)
@@ -204,8 +214,8 @@ def test_reads_the_reference_cascade_with_translational_cyclics(oracle_binding):
     sel = mesh.b_partner >= 0
     assert sel.sum() == 2 * 215
     assert np.all((mesh.b_weights[sel] > 0) & (mesh.b_weights[sel] < 1))
-    st = dict(settings, viscous=0)
-    h = _open(oracle_binding, mesh, st, fields["p"], fields["U"], fields["T"])
+    assert settings.get("viscous", 0) == 1
+    h = _open(oracle_binding, mesh, settings, fields["p"], fields["U"], fields["T"])
     h.begin_time_step()
     s = h.pseudo_iteration()
     assert np.isfinite(s.rho_l2_residual)

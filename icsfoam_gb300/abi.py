@@ -131,6 +131,7 @@ _FUNCS = {
     "pseudo_loop": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "set_hb": (C.c_int, [_P, C.c_int32, _P]),
     "set_mrf": (C.c_int, [_P, _P, _P, _P, _P, C.c_int32]),
+    "set_phase_lag": (C.c_int, [_P, _P, _P]),
     "scalar_enable": (C.c_int, [_P, _P, _P, _P, C.c_double, C.c_int32]),
     "scalar_transport": (C.c_int, [_P, C.c_int32, C.POINTER(SolverPerf)]),
     "get_scalar": (C.c_int, [_P, _P, _P]),
@@ -414,6 +415,18 @@ class CaseHandle:
     def set_hb(self, n_instances: int, D):
         D = np.ascontiguousarray(D, np.float64).reshape(n_instances, n_instances)
         self._check(self.b.fn["set_hb"](self.h, int(n_instances), _ptr(D)), "set_hb")
+
+    def set_phase_lag(self, setup=None):
+        """Phase-lag cyclic patches of an HB handle: ``hb.phase_lag_setup``'s
+        (mode, P), or None to switch phase lag off."""
+        if setup is None:
+            self._check(self.b.fn["set_phase_lag"](self.h, None, None), "set_phase_lag")
+            return
+        mode, P = setup
+        mode = np.ascontiguousarray(mode, np.int32)
+        P = np.ascontiguousarray(P, np.float64)
+        self._keep_plag = (mode, P)
+        self._check(self.b.fn["set_phase_lag"](self.h, _ptr(mode), _ptr(P)), "set_phase_lag")
 
     def set_mrf(self, fields=None, mode: int = 0):
         """Moving reference frames from ``mrf.frame_fields`` (None: off).

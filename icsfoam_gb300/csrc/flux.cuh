@@ -20,6 +20,58 @@
 
 namespace ics {
 
+// ------------------------------------------------ phase-lag cyclic neighbours
+// The neighbour value of instance J across a phase-lag cyclic face is
+// sum_K P_JK f_K(partner cell of instance K) for the fields the reference
+// phase-lags (phaseLagCyclicFvPatchField::patchNeighbourField: rho, p, the U
+// components, E, H and the sound speed); the others keep the plain cyclic
+// neighbour of their own instance.
+__device__ __forceinline__ int plag_mode(const DevMesh& m, int b) {
+  return m.plagMode ? m.plagMode[m.bpatch[b]] : 0;
+}
+template <typename Real, typename Fn>
+__device__ __forceinline__ Real plag_sum(const DevMesh& m, int b, int pc, Fn f) {
+  const int n = m.nInst, J = pc / m.Nc, cl = pc - J * m.Nc;
+  const double* P = m.plagP + ((size_t)m.bpatch[b] * n + J) * n;
+  Real s = Real(0.0);
+  for (int K = 0; K < n; ++K) s = s + P[K] * f(K * m.Nc + cl);
+  return s;
+}
+// the velocity from its component arrays: combined as it is (mode 1) or
+// combined and rotated into this side's frame (mode 2, cylindrical coordinates)
+template <typename Real>
+__device__ __forceinline__ void plag_vec(const DevMesh& m, int b, int pc, const Real* Ux, const Real* Uy,
+                                         const Real* Uz, Real v[3]) {
+  Real a[3];
+  a[0] = plag_sum<Real>(m, b, pc, [&](int c) { return Ux[c]; });
+  a[1] = plag_sum<Real>(m, b, pc, [&](int c) { return Uy[c]; });
+  a[2] = plag_sum<Real>(m, b, pc, [&](int c) { return Uz[c]; });
+  if (plag_mode(m, b) == 2) {
+    const double* R = m.patches[m.bpatch[b]].R;
+    for (int k = 0; k < 3; ++k) v[k] = R[3 * k] * a[0] + R[3 * k + 1] * a[1] + R[3 * k + 2] * a[2];
+  } else {
+    for (int k = 0; k < 3; ++k) v[k] = a[k];
+  }
+}
+// field k of the q layout [NQ][N]; the sound speed's neighbour is
+// sqrt(gamma/psi) of the instances (for AUSM+up's c* as well, as the reference)
+template <typename Real>
+__device__ __forceinline__ Real plag_q(const DevMesh& m, const Real* q, int k, int b, int pc) {
+  const int N = m.N;
+  if (k == Q_UX || k == Q_UY || k == Q_UZ) {
+    Real v[3];
+    plag_vec<Real>(m, b, pc, q + Q_UX * N, q + Q_UY * N, q + Q_UZ * N, v);
+    return v[k - Q_UX];
+  }
+  if (k == Q_C) {
+    const double g = m.plagGamma;
+    return plag_sum<Real>(m, b, pc, [&](int c) { return sqrt(g * (q[Q_P * N + c] / q[Q_RHO * N + c])); });
+  }
+  if (k == Q_H)
+    return plag_sum<Real>(m, b, pc, [&](int c) { return q[Q_E * N + c] + q[Q_P * N + c] / q[Q_RHO * N + c]; });
+  return plag_sum<Real>(m, b, pc, [&](int c) { return q[k * N + c]; });
+}
+
 // Face state; Real = double for the residual, Dual for its tangent
 template <typename Real>
 struct FStateT {

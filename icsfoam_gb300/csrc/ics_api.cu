@@ -98,7 +98,7 @@ void free_all(Handle& h) {
                   m.bface, m.slot_base, m.scol, m.sface, m.nlow, m.nslot, m.fl_cells, m.rl_cells, m.fl_lptr,
                   m.rl_lptr, m.sweep_flag, m.sweep_ticket, h.W, h.W0, h.W00, h.Wprev, h.prim, h.pB, h.TB, h.UB, h.phiB, h.pseudoCo, h.rPDT,
                   h.ddtCoeff, h.q, h.bq, h.clin, h.grad, h.fflux, h.frec, h.flam, h.bjac, h.src, h.vcell,
-                  h.fvisc, h.vsf2, m.dc, m.Dhb, m.mrfU, m.mrfOm, m.mrfBU, m.mrfBIn, m.bpartner, m.bw, m.bdelta, m.bdNei,
+                  h.fvisc, h.vsf2, m.dc, m.Dhb, m.mrfU, m.mrfOm, m.mrfBU, m.mrfBIn, m.plagMode, m.plagP, m.bpartner, m.bw, m.bdelta, m.bdNei,
                   m.bnodc, m.cyc_face, m.cyc_row, m.cyc_ptr, h.cblk, h.cfrec, h.tW, h.tprim, h.tq, h.tgrad, h.tflux, h.tvc, h.tfv, h.tv,
                   h.ss, h.ssB, h.srhoS, h.srhoS0, h.srhoS00, h.sgrad, h.sgradL, h.sface, h.sblk, h.sdg, h.srD,
                   h.ssrc, h.sFixed, h.sValue,
@@ -716,6 +716,7 @@ int ics_create(const ics_mesh_desc* mesh, const ics_config* cfg, ics_handle* out
   h.cfg.c = *cfg;
   h.cfg.Cv = cfg->Cp - cfg->R;
   h.cfg.gamma = cfg->Cp / h.cfg.Cv;
+  h.m.plagGamma = h.cfg.gamma;
   st = guard(hh, [&](Handle& hd) {
     ICS_CUDA(cudaStreamCreateWithFlags(&hd.stream, cudaStreamNonBlocking));
     build_mesh(hd, mesh);
@@ -759,6 +760,7 @@ int ics_set_config(ics_handle hh, const ics_config* cfg) {
     h.cfg.c = *cfg;
     h.cfg.Cv = cfg->Cp - cfg->R;
     h.cfg.gamma = cfg->Cp / h.cfg.Cv;
+    h.m.plagGamma = h.cfg.gamma;
     h.haveExact = false;
     if (structural) ensure_workspace(h);
     return ICS_OK;
@@ -1556,6 +1558,38 @@ int ics_set_hb(ics_handle hh, int32_t n, const double* D) {
     h.haveMatrix = h.haveIncrement = false;
     free_exact(h);   // the stencil gains the instance partners
     drop_graphs(h);  // the captured cycle's reduction grids depend on n
+    return ICS_OK;
+  });
+}
+
+int ics_set_phase_lag(ics_handle hh, const int32_t* mode, const double* P) {
+  if (!hh) return ICS_ERR_ARG;
+  Handle& h0 = hh->h;
+  const int np = h0.m.npatches, n = h0.m.nInst;
+  if (mode) {
+    if (n < 2 || !P) {
+      h0.err = "phase lag needs a Harmonic Balance handle and the operators";
+      return ICS_ERR_ARG;
+    }
+  }
+  return guard(hh, [&](Handle& h) {
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    std::vector<Patch> pts(np);
+    if (np) ICS_CUDA(cudaMemcpy(pts.data(), h.m.patches, np * sizeof(Patch), cudaMemcpyDeviceToHost));
+    if (mode)
+      for (int p = 0; p < np; ++p)
+        if (mode[p] < 0 || mode[p] > 2 || (mode[p] && pts[p].kind != ICS_PATCH_CYCLIC))
+          throw std::string("phase-lag modes must be 0, 1 or 2 and set on cyclic patches only");
+    dfree(h.m.plagMode);
+    dfree(h.m.plagP);
+    h.m.plagMode = nullptr;
+    h.m.plagP = nullptr;
+    h.haveFlux = h.haveMatrix = h.haveIncrement = false;
+    free_exact(h);  // the stencil gains the other instances' partners
+    drop_graphs(h);
+    if (!mode) return ICS_OK;
+    h.m.plagMode = upload(std::vector<int>(mode, mode + np));
+    h.m.plagP = upload(std::vector<double>(P, P + (size_t)np * n * n));
     return ICS_OK;
   });
 }

@@ -129,6 +129,12 @@ struct DevMesh {
   int* cyc_face = nullptr;
   int* cyc_row = nullptr;
   int* cyc_ptr = nullptr;
+  // phase-lag cyclic patches (Harmonic Balance): per patch 0 plain, 1 phase
+  // lag, 2 phase lag with cylindrical velocity; per patch the instances'
+  // operator P [npatches][nInst][nInst]; gamma for the sound-speed neighbour
+  int* plagMode = nullptr;
+  double* plagP = nullptr;
+  double plagGamma = 1.4;
   double* mrfU = nullptr;
   double* mrfOm = nullptr;
   double* mrfBU = nullptr;

@@ -136,6 +136,21 @@ void build_exact_pattern(Handle& h) {
     for (int b : cyc) adj[fill[bcell[b]]++] = bpart[b];
   }
   const int nI = h.m.nInst, Nc = h.m.Nc;
+  // cells with phase-lag cyclic faces -> their partners (CSR)
+  std::vector<int> plagPtr, plagCells;
+  if (h.m.plagMode && h.m.ncyc) {
+    std::vector<int> pm(h.m.npatches), bpatch(h.m.B);
+    ICS_CUDA(cudaMemcpy(pm.data(), h.m.plagMode, pm.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    ICS_CUDA(cudaMemcpy(bpatch.data(), h.m.bpatch, h.m.B * sizeof(int), cudaMemcpyDeviceToHost));
+    plagPtr.assign(N + 1, 0);
+    for (int b : cyc)
+      if (pm[bpatch[b]]) plagPtr[bcell[b] + 1]++;
+    for (int c = 0; c < N; ++c) plagPtr[c + 1] += plagPtr[c];
+    plagCells.resize(plagPtr[N]);
+    std::vector<int> fill(plagPtr.begin(), plagPtr.end() - 1);
+    for (int b : cyc)
+      if (pm[bpatch[b]]) plagCells[fill[bcell[b]]++] = bpart[b];
+  }
   std::vector<int> ptr(N + 1, 0), col;
   col.reserve((size_t)N * 27);
   std::vector<int> mark(N, -1), row;
@@ -156,6 +171,18 @@ void build_exact_pattern(Handle& h) {
     if (nI > 1) {
       const int cl = r % Nc;
       for (int K = 0; K < nI; ++K) add(K * Nc + cl);
+      // phase-lag faces: the partner cells of every instance, and theirs
+      // through the neighbours' gradients (rows within two hops)
+      if (!plagCells.empty()) {
+        auto addPl = [&](int c) {
+          for (int e = plagPtr[c]; e < plagPtr[c + 1]; ++e) {
+            const int cl2 = plagCells[e] % Nc;
+            for (int K = 0; K < nI; ++K) add(K * Nc + cl2);
+          }
+        };
+        addPl(r);
+        for (int a = aptr[r]; a < aptr[r + 1]; ++a) addPl(adj[a]);
+      }
     }
     std::sort(row.begin(), row.end());
     col.insert(col.end(), row.begin(), row.end());

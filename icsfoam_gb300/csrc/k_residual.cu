@@ -145,10 +145,11 @@ __global__ void __launch_bounds__(128) k_grad(DevMesh m, const Real* __restrict_
       // also bounds the limiter (gaussGrad / cellLimitedGrad on a coupled
       // patch; a scalar field's neighbour values are not rotated)
       const double wb = m.bw[b];
+      const bool plag = plag_mode(m, b) != 0;
 #pragma unroll
       for (int k = 0; k < NQ; ++k) {
         if (!((mask >> k) & 1)) continue;
-        const Real qn = q[k * N + pc];
+        const Real qn = plag ? plag_q(m, q, k, b, pc) : q[k * N + pc];
         const Real sf = wb * (qc[k] - qn) + qn;
         g[k][0] = g[k][0] + S0 * sf;
         g[k][1] = g[k][1] + S1 * sf;
@@ -459,7 +460,8 @@ __global__ void __launch_bounds__(128) k_cface(DevMesh m, ResParams P, const Rea
       qL[k] = qR[k] = 0.0;
       continue;
     }
-    const Real qo = q[k * N + o], qn = q[k * N + pc];
+    const Real qo = q[k * N + o];
+    const Real qn = plag_mode(m, b) ? plag_q(m, q, k, b, pc) : q[k * N + pc];
     const int sch = recon_of(P, k);
     qL[k] = reconstruct_cyc(m, sch, k, b, o, pc, qo, qn, grad, R, +1.0);
     qR[k] = reconstruct_cyc(m, sch, k, b, o, pc, qo, qn, grad, R, -1.0);
@@ -490,12 +492,21 @@ __global__ void __launch_bounds__(128) k_cface(DevMesh m, ResParams P, const Rea
     cfrec[6 * nc + i] = qL[Q_E];
     cfrec[7 * nc + i] = qR[Q_E];
     const double wb = m.bw[b];
-    const double ci = wb * (clin[o] - clin[pc]) + clin[pc];
-    const double Up[3] = {q[Q_UX * N + pc], q[Q_UY * N + pc], q[Q_UZ * N + pc]};
+    const bool plag = plag_mode(m, b) != 0;
+    const double cn = plag ? plag_q(m, q, Q_C, b, pc) : clin[pc];
+    const double ci = wb * (clin[o] - cn) + cn;
+    double rpv[3];
+    if (plag) {
+      plag_vec(m, b, pc, q + Q_UX * N, q + Q_UY * N, q + Q_UZ * N, rpv);
+    } else {
+      const double Up[3] = {q[Q_UX * N + pc], q[Q_UY * N + pc], q[Q_UZ * N + pc]};
+#pragma unroll
+      for (int k = 0; k < 3; ++k) rpv[k] = R[3 * k] * Up[0] + R[3 * k + 1] * Up[1] + R[3 * k + 2] * Up[2];
+    }
     double ui[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const double rp = R[3 * k] * Up[0] + R[3 * k + 1] * Up[1] + R[3 * k + 2] * Up[2];
+      const double rp = rpv[k];
       ui[k] = wb * (q[(Q_UX + k) * N + o] - rp) + rp;
     }
     flam[F + b] = ci + fabs(dot3(ui, n) - um);
@@ -1039,15 +1050,17 @@ __global__ void __launch_bounds__(128) k_scalar_cface(DevMesh m, ResParams P, in
   const double* R = m.patches[m.bpatch[b]].R;
   const double sl = reconstruct_cyc(m, reconS, 0, b, o, pc, s[o], s[pc], sgrad, R, +1.0);
   const double sr = reconstruct_cyc(m, reconS, 0, b, o, pc, s[o], s[pc], sgrad, R, -1.0);
-  const double qo = q[Q_RHO * N + o], qn = q[Q_RHO * N + pc];
+  const bool plag = plag_mode(m, b) != 0;
+  const double qo = q[Q_RHO * N + o], qn = plag ? plag_q(m, q, Q_RHO, b, pc) : q[Q_RHO * N + pc];
   const double rl = reconstruct_cyc(m, P.reconRho, Q_RHO, b, o, pc, qo, qn, grad, R, +1.0);
   const double rr = reconstruct_cyc(m, P.reconRho, Q_RHO, b, o, pc, qo, qn, grad, R, -1.0);
   double Ul[3], Ur[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const int qk = Q_UX + k;
-    Ul[k] = reconstruct_cyc(m, P.reconU, qk, b, o, pc, q[qk * N + o], q[qk * N + pc], grad, R, +1.0);
-    Ur[k] = reconstruct_cyc(m, P.reconU, qk, b, o, pc, q[qk * N + o], q[qk * N + pc], grad, R, -1.0);
+    const double un = plag ? plag_q(m, q, qk, b, pc) : q[qk * N + pc];
+    Ul[k] = reconstruct_cyc(m, P.reconU, qk, b, o, pc, q[qk * N + o], un, grad, R, +1.0);
+    Ur[k] = reconstruct_cyc(m, P.reconU, qk, b, o, pc, q[qk * N + o], un, grad, R, -1.0);
   }
   const double ms = m.bmagSf[b];
   const double n[3] = {m.bnf[b], m.bnf[B + b], m.bnf[2 * B + b]};

@@ -67,10 +67,19 @@ __global__ void k_bc(DevMesh m, const double* __restrict__ prim, double* __restr
     const int pc = m.bpartner[b];
     const double wb = m.bw[b];
     const double* Rm = pt.R;
-    pB[b] = wb * (prim[ci] - prim[pc]) + prim[pc];
-    const double Un[3] = {prim[2 * N + pc], prim[3 * N + pc], prim[4 * N + pc]};
+    // phase-lag cyclic (HB): p and U of the instances combined, T plain
+    const bool plag = plag_mode(m, b) != 0;
+    const double pn = plag ? plag_sum<double>(m, b, pc, [&](int c) { return prim[c]; }) : prim[pc];
+    pB[b] = wb * (prim[ci] - pn) + pn;
+    double upv[3];
+    if (plag) {
+      plag_vec(m, b, pc, prim + 2 * N, prim + 3 * N, prim + 4 * N, upv);
+    } else {
+      const double Un[3] = {prim[2 * N + pc], prim[3 * N + pc], prim[4 * N + pc]};
+      for (int k = 0; k < 3; ++k) upv[k] = Rm[3 * k] * Un[0] + Rm[3 * k + 1] * Un[1] + Rm[3 * k + 2] * Un[2];
+    }
     for (int k = 0; k < 3; ++k) {
-      const double up = Rm[3 * k] * Un[0] + Rm[3 * k + 1] * Un[1] + Rm[3 * k + 2] * Un[2];
+      const double up = upv[k];
       UB[k * B + b] = wb * (prim[(2 + k) * N + ci] - up) + up;
     }
     double T = wb * (prim[N + ci] - prim[N + pc]) + prim[N + pc];

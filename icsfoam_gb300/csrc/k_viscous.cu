@@ -74,8 +74,13 @@ __global__ void __launch_bounds__(128) k_visc_cell(DevMesh m, ViscParams P, cons
       const double wb = m.bw[b];
       const Real Un[3] = {prim[2 * N + pc], prim[3 * N + pc], prim[4 * N + pc]};
       const Real en = W[5 * pc + 4] / W[5 * pc] - 0.5 * dot3(Un, Un);
+      Real upv[3];
+      if (plag_mode(m, b))  // U phase-lagged across an HB phase-lag patch
+        plag_vec(m, b, pc, prim + 2 * N, prim + 3 * N, prim + 4 * N, upv);
+      else
+        for (int j = 0; j < 3; ++j) upv[j] = Rm[3 * j] * Un[0] + Rm[3 * j + 1] * Un[1] + Rm[3 * j + 2] * Un[2];
       for (int j = 0; j < 3; ++j) {
-        const Real up = Rm[3 * j] * Un[0] + Rm[3 * j + 1] * Un[1] + Rm[3 * j + 2] * Un[2];
+        const Real up = upv[j];
         const Real sf = wb * (Uc[j] - up) + up;
         for (int i = 0; i < 3; ++i) g[3 * i + j] += S[i] * sf;
       }
@@ -230,9 +235,14 @@ __global__ void __launch_bounds__(128) k_visc_cface(DevMesh m, const Real* __res
       tf[3 * i + j] = lin(vc[(12 + 3 * i + j) * N + o], st);
     }
   const Real Un[3] = {prim[2 * N + pc], prim[3 * N + pc], prim[4 * N + pc]};
+  Real upv[3];
+  if (plag_mode(m, b))
+    plag_vec(m, b, pc, prim + 2 * N, prim + 3 * N, prim + 4 * N, upv);
+  else
+    for (int j = 0; j < 3; ++j) upv[j] = Rm[3 * j] * Un[0] + Rm[3 * j + 1] * Un[1] + Rm[3 * j + 2] * Un[2];
   Real Uf[3], snU[3];
   for (int j = 0; j < 3; ++j) {
-    const Real up = Rm[3 * j] * Un[0] + Rm[3 * j + 1] * Un[1] + Rm[3 * j + 2] * Un[2];
+    const Real up = upv[j];
     const Real uo = prim[(2 + j) * N + o];
     Uf[j] = lin(uo, up);
     const Real corr = k[0] * gUf[j] + k[1] * gUf[3 + j] + k[2] * gUf[6 + j];

@@ -16,6 +16,11 @@ Restates (host side, tiny dense linear algebra):
   D = -(Im(E^-1) A Re(E) + Re(E^-1) A Im(E)).
 * ``reconstruct``     HBZone::reconstruct (HBZoneTemplates.C:327-405): the
   time history at any t from the instance snapshots (reconstructHBFoam).
+* ``phase_lag_operator`` phaseLagCyclicFvPatchField::phaseLaggedField
+  (phaseLagCyclicFvPatchFields.C): P = Re(E^-1 M E), M = diag(1, e^{i k
+  IBPA} (k = 1..H), e^{-i k IBPA}) -- the instances' values shifted by the
+  inter-blade phase angle; ``phase_lag_setup`` lays it out per patch of a
+  stacked mesh for ``CaseHandle.set_phase_lag``.
 
 The instances become one stacked mesh (``stack_instances``): instance J owns
 cells [J N, (J+1) N) and its own copy of every patch, so time-varying inlet
@@ -89,6 +94,39 @@ def hb_operator(omegas: np.ndarray, instants: np.ndarray) -> np.ndarray:
     A = np.diag(omegas)
     D = -(E1.imag @ A @ E.real + E1.real @ A @ E.imag)
     return np.ascontiguousarray(D)
+
+
+def phase_lag_operator(omegas: np.ndarray, instants: np.ndarray, ibpa: float) -> np.ndarray:
+    """P[J, K]: the neighbour value of instance J is sum_K P[J, K] f_K."""
+    E1 = e_inverse(omegas, instants)
+    E = np.linalg.pinv(E1)
+    nF = len(omegas)
+    nH = (nF - 1) // 2
+    Mx = np.zeros((nF, nF), complex)
+    Mx[0, 0] = 1.0
+    for k in range(1, nH + 1):
+        Mx[k, k] = np.exp(1j * k * ibpa)
+        Mx[nF - k, nF - k] = np.conj(Mx[k, k])
+    return np.ascontiguousarray((E1 @ (Mx @ E)).real)
+
+
+def phase_lag_setup(mesh: M.Mesh, n: int, omegas: np.ndarray, instants: np.ndarray, ibpa: float,
+                    cyl_coords: bool = False, patches: Sequence[str] = None):
+    """(mode [n_patches], P [n_patches, n, n]) of a stacked mesh: every cyclic
+    patch whose base name is in ``patches`` (all cyclic patches when None)
+    becomes phase-lagged; the owner of a pair (the lower patch index, as
+    cyclicPolyPatch::owner) takes +IBPA, its neighbour -IBPA."""
+    names = [p.name for p in mesh.patches]
+    mode = np.zeros(len(names), np.int32)
+    P = np.zeros((len(names), n, n))
+    for i, p in enumerate(mesh.patches):
+        base = p.name.rsplit("_", 1)[0]
+        if p.kind != M.PATCH_CYCLIC or (patches is not None and base not in patches):
+            continue
+        owner = i < names.index(p.partner)
+        mode[i] = 2 if cyl_coords else 1
+        P[i] = phase_lag_operator(omegas, instants, ibpa if owner else -ibpa)
+    return mode, np.ascontiguousarray(P)
 
 
 def reconstruction_weights(omegas: np.ndarray, instants: np.ndarray, t: float) -> np.ndarray:

@@ -272,6 +272,18 @@ int ics_set_hb(ics_handle h, int32_t n_instances, const double* D);
  * is also re-assigned on every included face after each update.
  * omega == NULL switches the zones off.  The passive scalar uses the same
  * face velocity (calculateScalarTransport.H:96-145,217-290).                 */
+/* Phase-lag cyclic patches of a Harmonic Balance handle (phaseLagCyclic,
+ * src/fields/fvPatchFields/constraint/phaseLagCyclic): mode[n_patches] is 0
+ * for a plain patch, 1 for a phase-lag cyclic patch, 2 for one whose velocity
+ * is combined in cylindrical components (cylCoords); P[n_patches][n][n] holds,
+ * for each phase-lag patch, Re(E^-1 M(IBPA) E) of its HB zone (M = diag(1,
+ * e^{i k IBPA}, ..., e^{-i k IBPA}); the neighbour patch uses -IBPA).  Across
+ * such a face the neighbour value of instance J of rho, p, the U components,
+ * E, H and the sound speed is sum_K P_JK f_K(partner cell of instance K)
+ * (phaseLagCyclicFvPatchField::patchNeighbourField); every other field and
+ * the Jacobian couplings keep the plain cyclic neighbour of instance J.
+ * mode == NULL switches phase lag off.                                      */
+int ics_set_phase_lag(ics_handle h, const int32_t* mode, const double* P);
 #define ICS_MRF_OUTER_LOOP 0
 #define ICS_MRF_EVERY_UPDATE 1
 int ics_set_mrf(ics_handle h, const double* omega, const double* face_velocity, const double* boundary_U,

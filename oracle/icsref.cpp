@@ -155,6 +155,11 @@ struct Case {
   // displacement Cf - C - delta, nonOrthDeltaCoeffs, and the interface
   // blocks of the last Jacobian (blockFvMatrix interfacesUpper)
   bool hasCyc = false;
+  // phase-lag cyclic patches of Harmonic Balance handles (phaseLagCyclic):
+  // per patch 0 = plain cyclic, 1 = phase lag, 2 = phase lag with the velocity
+  // combined in cylindrical components; the n x n operator Re(E^-1 M E) of each
+  std::vector<int> plagMode;
+  std::vector<double> plagP;
   std::vector<int> bpartner;
   std::vector<double> bw, bnodc;
   std::vector<V3> bdelta, bnbrd;
@@ -178,6 +183,45 @@ inline V3 rotP(const Case& c, int b, const V3& v) {
             R[6] * v.x + R[7] * v.y + R[8] * v.z);
 }
 
+// a vol field: internal values + boundary-face values
+struct VolS {
+  std::vector<double> in, bf;
+  std::vector<double> nb;  // phase-lagged neighbour values of the phase-lag cyclic faces (or empty)
+};
+
+// phase-lag cyclic face b (phaseLagCyclicFvPatchField::patchNeighbourField,
+// phaseLagCyclicFvPatchFields.C): the neighbour value of instance J of a
+// phase-lagged field is sum_K P_JK f_K(partner), P = Re(E^-1 M(+-IBPA) E)
+inline bool isPlag(const Case& c, int b) {
+  return isCyc(c, b) && !c.plagMode.empty() && c.plagMode[c.bpatch[b]] > 0;
+}
+template <typename Fn>
+double plagSum(const Case& c, int b, Fn f) {
+  const int n = c.nInst, pc = c.bpartner[b], J = pc / c.Nc, cl = pc % c.Nc;
+  const double* P = &c.plagP[((size_t)c.bpatch[b] * n + J) * n];
+  double s = 0;
+  for (int K = 0; K < n; ++K) s += P[K] * f(K * c.Nc + cl);
+  return s;
+}
+// the velocity: combined as it is (mode 1) or, with cylindrical coordinates,
+// combined and rotated into this side's frame (mode 2)
+inline V3 plagVec(const Case& c, int b, const std::vector<V3>& U) {
+  V3 v;
+  for (int k = 0; k < 3; ++k) v[k] = plagSum(c, b, [&](int q) { return U[q][k]; });
+  return c.plagMode[c.bpatch[b]] == 2 ? rotP(c, b, v) : v;
+}
+// neighbour value of a scalar field on cyclic face b
+inline double nbOf(const Case& c, const VolS& f, int b) {
+  return (!f.nb.empty() && isPlag(c, b)) ? f.nb[b] : f.in[c.bpartner[b]];
+}
+template <typename Fn>
+void setPlag(const Case& c, VolS& f, Fn cellValue) {
+  if (c.plagMode.empty()) return;
+  f.nb.assign(c.B, 0.0);
+  for (int b = 0; b < c.B; ++b)
+    if (isPlag(c, b)) f.nb[b] = plagSum(c, b, cellValue);
+}
+
 // MRF face velocity of face fi (internal then boundary), zero without zones
 inline double umOf(const Case& c, int fi) { return c.mrfOn ? c.mrfU[fi] : 0.0; }
 
@@ -197,9 +241,6 @@ inline double heOf(const Case& c, double T) { return c.Cv * T; }
 // ---------------------------------------------------------------------------
 // Field helpers: a vol field = internal values + boundary-face values
 // ---------------------------------------------------------------------------
-struct VolS {
-  std::vector<double> in, bf;
-};
 
 // Gauss linear gradient (OpenFOAM gaussGrad with linear interpolation)
 void gaussGrad(const Case& c, const VolS& f, std::vector<V3>& g) {
@@ -214,8 +255,8 @@ void gaussGrad(const Case& c, const VolS& f, std::vector<V3>& g) {
   for (int b = 0; b < c.B; ++b) {
     const int o = c.bcell[b];
     if (isCyc(c, b)) {  // linear interpolation with the partner (coupled patch)
-      const int pc = c.bpartner[b];
-      g[o] = g[o] + c.bSf[b] * (c.bw[b] * (f.in[o] - f.in[pc]) + f.in[pc]);
+      const double fn = nbOf(c, f, b);
+      g[o] = g[o] + c.bSf[b] * (c.bw[b] * (f.in[o] - fn) + fn);
       continue;
     }
     g[o] = g[o] + c.bSf[b] * f.bf[b];
@@ -236,7 +277,7 @@ void cellLimitedGrad(const Case& c, const VolS& f, bool venkat, std::vector<V3>&
   }
   for (int b = 0; b < c.B; ++b) {
     const int o = c.bcell[b];
-    const double v = isCyc(c, b) ? f.in[c.bpartner[b]] : f.bf[b];  // coupled: the neighbour cell
+    const double v = isCyc(c, b) ? nbOf(c, f, b) : f.bf[b];  // coupled: the neighbour cell
     maxV[o] = std::max(maxV[o], v);
     minV[o] = std::min(minV[o], v);
   }
@@ -274,8 +315,12 @@ void interpLinear(const Case& c, const VolS& f, std::vector<double>& out) {
     out[fi] = c.w[fi] * (f.in[o] - f.in[n]) + f.in[n];
   }
   for (int b = 0; b < c.B; ++b) {
-    const int pc = isCyc(c, b) ? c.bpartner[b] : -1;
-    out[c.F + b] = pc >= 0 ? c.bw[b] * (f.in[c.bcell[b]] - f.in[pc]) + f.in[pc] : f.bf[b];
+    if (isCyc(c, b)) {
+      const double fn = nbOf(c, f, b);
+      out[c.F + b] = c.bw[b] * (f.in[c.bcell[b]] - fn) + fn;
+    } else {
+      out[c.F + b] = f.bf[b];
+    }
   }
 }
 
@@ -327,7 +372,7 @@ void reconstruct(const Case& c, const VolS& f, double dir, int scheme, std::vect
     // frame; the TVD ratio uses delta, linearUpwind extrapolates the partner
     // side along Cf - C - delta (limitedScheme / linearUpwind on coupled patches)
     const int o = c.bcell[b], pc = c.bpartner[b];
-    const double phiP = f.in[o], phiN = f.in[pc];
+    const double phiP = f.in[o], phiN = nbOf(c, f, b);
     if (scheme == ICS_RECON_UPWIND) {
       out[c.F + b] = wUp * (phiP - phiN) + phiN;
       continue;
@@ -350,6 +395,11 @@ VolS Ucmpt(const Case& c, int k) {
   f.bf.resize(c.B);
   for (int i = 0; i < c.N; ++i) f.in[i] = c.U[i][k];
   for (int b = 0; b < c.B; ++b) f.bf[b] = c.UB[b][k];
+  if (!c.plagMode.empty()) {  // "U.component(k)"
+    f.nb.assign(c.B, 0.0);
+    for (int b = 0; b < c.B; ++b)
+      if (isPlag(c, b)) f.nb[b] = plagVec(c, b, c.U)[k];
+  }
   return f;
 }
 
@@ -372,6 +422,7 @@ VolS fieldE(const Case& c) {
   E.bf.resize(c.B);
   for (int i = 0; i < c.N; ++i) E.in[i] = heOf(c, c.T[i]) + 0.5 * magSqr(c.U[i]);
   for (int b = 0; b < c.B; ++b) E.bf[b] = heOf(c, c.TB[b]) + 0.5 * magSqr(c.UB[b]);
+  setPlag(c, E, [&](int q) { return heOf(c, c.T[q]) + 0.5 * magSqr(c.U[q]); });
   return E;
 }
 double rhoBof(const Case& c, int b) { return psiOf(c, c.TB[b]) * c.pB[b]; }
@@ -382,6 +433,7 @@ VolS fieldH(const Case& c, const VolS& E) {
   H.bf.resize(c.B);
   for (int i = 0; i < c.N; ++i) H.in[i] = std::max(E.in[i], SMALL) + std::max(c.p[i] / c.rho[i], SMALL);
   for (int b = 0; b < c.B; ++b) H.bf[b] = std::max(E.bf[b], SMALL) + std::max(c.pB[b] / rhoBof(c, b), SMALL);
+  setPlag(c, H, [&](int q) { return heOf(c, c.T[q]) + 0.5 * magSqr(c.U[q]) + c.p[q] / c.rho[q]; });
   return H;
 }
 VolS fieldRho(const Case& c) {
@@ -389,14 +441,19 @@ VolS fieldRho(const Case& c) {
   r.in = c.rho;
   r.bf.resize(c.B);
   for (int b = 0; b < c.B; ++b) r.bf[b] = rhoBof(c, b);
+  setPlag(c, r, [&](int q) { return c.rho[q]; });
   return r;
 }
 VolS fieldP(const Case& c) {
   VolS r;
   r.in = c.p;
   r.bf = c.pB;
+  setPlag(c, r, [&](int q) { return c.p[q]; });
   return r;
 }
+// the phase-lagged neighbour of a sound-speed field is sqrt(gamma/psi) of the
+// instances ("c" and "sqrt((gamma|thermo:psi))" alike)
+void setPlagC(const Case& c, VolS& f) { setPlag(c, f, [&](int q) { return std::sqrt(c.gamma / psiOf(c, c.T[q])); }); }
 
 // ---------------------------------------------------------------------------
 // Flux schemes
@@ -421,6 +478,7 @@ void calcFluxAUSM(Case& c) {
   const double g = c.gamma;
   for (int i = 0; i < c.N; ++i) cs.in[i] = std::sqrt(2.0 * (g - 1.0) / (g + 1.0) * H.in[i]);
   for (int b = 0; b < c.B; ++b) cs.bf[b] = std::sqrt(2.0 * (g - 1.0) / (g + 1.0) * H.bf[b]);
+  setPlagC(c, cs);
   std::vector<double> c_L, c_R;
   reconstruct(c, cs, +1, c.cfg.recon_T, c_L);
   reconstruct(c, cs, -1, c.cfg.recon_T, c_R);
@@ -503,6 +561,7 @@ void calcFluxHLLC(Case& c) {
   cs.bf.resize(c.B);
   for (int i = 0; i < c.N; ++i) cs.in[i] = std::max(std::sqrt(c.gamma / psiOf(c, c.T[i])), VSMALL);
   for (int b = 0; b < c.B; ++b) cs.bf[b] = std::max(std::sqrt(c.gamma / psiOf(c, c.TB[b])), VSMALL);
+  setPlagC(c, cs);
   reconstruct(c, cs, +1, c.cfg.recon_T, c_l);
   reconstruct(c, cs, -1, c.cfg.recon_T, c_r);
   VolS E = fieldE(c);
@@ -735,8 +794,8 @@ void gaussGradVec(const Case& c, const std::vector<V3>& in, const std::vector<V3
   }
   for (int b = 0; b < c.B; ++b) {
     V3 fb = bf[b];
-    if (isCyc(c, b)) {  // coupled: interpolate with the partner's vector rotated
-      const V3 up = rotP(c, b, in[c.bpartner[b]]);
+    if (isCyc(c, b)) {  // coupled: interpolate with the partner's vector rotated (U phase-lagged)
+      const V3 up = isPlag(c, b) ? plagVec(c, b, in) : rotP(c, b, in[c.bpartner[b]]);
       const V3& uo = in[c.bcell[b]];
       for (int j = 0; j < 3; ++j) fb[j] = c.bw[b] * (uo[j] - up[j]) + up[j];
     }
@@ -869,7 +928,7 @@ void viscousFluxes(const Case& c, const Viscous& v, std::vector<V3>& lapU, std::
         gUf.a[q] = lin(v.gU[o].a[q], gUp.a[q]);
         tf.a[q] = lin(v.tau[o].a[q], tp.a[q]);
       }
-      const V3 Up = rotP(c, b, c.U[pc]);
+      const V3 Up = isPlag(c, b) ? plagVec(c, b, c.U) : rotP(c, b, c.U[pc]);
       V3 Uf, snUc;
       for (int j = 0; j < 3; ++j) {
         Uf[j] = lin(c.U[o][j], Up[j]);
@@ -1068,6 +1127,7 @@ void waveSpeed(const Case& c, std::vector<double>& lam) {
   cs.bf.resize(c.B);
   for (int i = 0; i < c.N; ++i) cs.in[i] = std::sqrt(c.gamma / psiOf(c, c.T[i]));
   for (int b = 0; b < c.B; ++b) cs.bf[b] = std::sqrt(c.gamma / psiOf(c, c.TB[b]));
+  setPlagC(c, cs);
   std::vector<double> ci;
   interpLinear(c, cs, ci);
   std::vector<double> ui[3];
@@ -1078,7 +1138,7 @@ void waveSpeed(const Case& c, std::vector<double>& lam) {
     V3 uf(ui[0][fi], ui[1][fi], ui[2][fi]);
     const int b = fi - c.F;
     if (b >= 0 && isCyc(c, b)) {  // fvc::interpolate(U) on a coupled patch: the partner's U rotated
-      const V3 up = rotP(c, b, c.U[c.bpartner[b]]);
+      const V3 up = isPlag(c, b) ? plagVec(c, b, c.U) : rotP(c, b, c.U[c.bpartner[b]]);
       const V3 uo = c.U[c.bcell[b]];
       const double w = c.bw[b];
       uf = V3(w * (uo.x - up.x) + up.x, w * (uo.y - up.y) + up.y, w * (uo.z - up.z) + up.z);
@@ -1813,8 +1873,8 @@ void correctBoundaryConditions(Case& c, const std::vector<double>& psiB) {
         break;
       }
       case ICS_PATCH_CYCLIC: {  // coupledFvPatchField::evaluate
-        const int pc = c.bpartner[b];
-        c.pB[b] = c.bw[b] * (c.p[ci] - c.p[pc]) + c.p[pc];
+        const double pn = isPlag(c, b) ? plagSum(c, b, [&](int q) { return c.p[q]; }) : c.p[c.bpartner[b]];
+        c.pB[b] = c.bw[b] * (c.p[ci] - pn) + pn;
         break;
       }
     }
@@ -1847,7 +1907,7 @@ void correctBoundaryConditions(Case& c, const std::vector<double>& psiB) {
         break;
       }
       case ICS_PATCH_CYCLIC: {  // the partner's velocity rotated into this side's frame
-        const V3 up = rotP(c, b, c.U[c.bpartner[b]]);
+        const V3 up = isPlag(c, b) ? plagVec(c, b, c.U) : rotP(c, b, c.U[c.bpartner[b]]);
         const double w = c.bw[b];
         c.UB[b] = V3(w * (c.U[ci].x - up.x) + up.x, w * (c.U[ci].y - up.y) + up.y, w * (c.U[ci].z - up.z) + up.z);
         break;
@@ -2798,6 +2858,22 @@ int icsref_begin_time_step(ics_handle h) {
     c.prevResValid = false;
   }
   if (c.cfg.reset_pseudo) std::fill(c.pseudoCo.begin(), c.pseudoCo.end(), c.cfg.pseudo_co_num);
+  return ICS_OK;
+}
+
+// phase-lag cyclic patches (the same arrays as ics_set_phase_lag); mode == NULL switches them off
+int icsref_set_phase_lag(ics_handle h, const int32_t* mode, const double* P) {
+  if (!h) return ICS_ERR_ARG;
+  Case& c = *h;
+  c.plagMode.clear();
+  c.plagP.clear();
+  if (!mode) return ICS_OK;
+  const int np = (int)c.patches.size(), n = c.nInst;
+  if (n < 2 || !P) return ICS_ERR_ARG;
+  for (int p = 0; p < np; ++p)
+    if (mode[p] < 0 || mode[p] > 2 || (mode[p] && c.patches[p].kind != ICS_PATCH_CYCLIC)) return ICS_ERR_ARG;
+  c.plagMode.assign(mode, mode + np);
+  c.plagP.assign(P, P + (size_t)np * n * n);
   return ICS_OK;
 }
 

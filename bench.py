@@ -311,15 +311,16 @@ def run_e2e(w, steps, warmup):
             "host_buffers": "pinned"}
 
 
-def run_hb_sweep(instances=(3, 5, 7, 9), per=(64, 64, 64), steps=5, warmup=2):
-    """Harmonic Balance: 3/5/7/9 stacked instances of a 262,144-cell bump (oscillating back pressure,
-    2% at 5 kHz), mixed precision, one coupled GMRES per pseudo iteration."""
+def run_hb_sweep(instances=(3, 5, 7, 9), per=(32, 64, 128), steps=5, warmup=2):
+    """Harmonic Balance: 3/5/7/9 stacked instances of the 262,144-cell annular sector (rotational cyclic
+    sides, inlet total pressure oscillating 2% at 5 kHz), mixed precision, one coupled GMRES per pseudo
+    iteration."""
     from icsfoam_gb300 import cases, gpu
 
     b = gpu.binding()
     out = {}
     for n in instances:
-        w = cases.hb_bump_channel(*per, frequency=5000.0, harmonics=(n - 1) // 2, amplitude=0.02)
+        w = cases.hb_annular_sector(*per, frequency=5000.0, harmonics=(n - 1) // 2, amplitude=0.02)
         h = gpu.open_case(w.mesh, cases.make_config(b, w.settings, precision=1))
         h.set_hb(*w.hb)
         h.set_primitive(w.p, w.U, w.T)

@@ -15,7 +15,10 @@ here is generated from fixed seeds:
                      time-periodic outlet static pressure, 2H+1 stacked
                      instances and the spectral operator D.
 * ``annular_sector`` - axial flow through a 20-degree annular sector with a
-                     rotating (MRF) cell zone in its middle third.
+                     rotational cyclic side pair and a rotating (MRF) cell
+                     zone in its middle third; ``hb_annular_sector`` its
+                     Harmonic Balance version (oscillating inlet total
+                     pressure).
 
 Sizes are parameters; the headline sizes are 1000 cells, 256x64x64 and 200^3.
 """
@@ -269,8 +272,8 @@ def annular_sector(nr: int = 32, nt: int = 64, nz: int = 128, r0: float = 0.5, r
     else:
         sa = sb = M.Patch("sides", M.PATCH_SLIP)
         coupled = ()
-    sides = {"xmin": hub, "xmax": shroud, "ymin": sa, "ymax": sb, "zmin": inlet, "zmax": outlet}
-    mesh = M.hex_mesh(g, sides)
+    side_map = {"xmin": hub, "xmax": shroud, "ymin": sa, "ymax": sb, "zmin": inlet, "zmax": outlet}
+    mesh = M.hex_mesh(g, side_map)
     mesh = ordering.apply(mesh, ordering_mode)
     N = mesh.n_cells
     c = np.sqrt(GAMMA * R_GAS * T_static)
@@ -287,6 +290,28 @@ def annular_sector(nr: int = 32, nt: int = 64, nz: int = 128, r0: float = 0.5, r
                     pseudo_tol=1e-30, pseudo_tol_rel=1e-30)
     return Workload("annulus_%dx%dx%d%s" % (nr, nt, nz, "" if sides == "cyclic" else "_slip"), mesh, np.full(N, p_static), U, np.full(N, T_static),
                     settings, mrf=([zone], []))
+
+
+def hb_annular_sector(nr: int = 32, nt: int = 64, nz: int = 128, frequency: float = 5000.0, harmonics: int = 1,
+                      amplitude: float = 0.02, selected_period: Optional[float] = None, **kw) -> Workload:
+    """Harmonic Balance on the rotational-cyclic annular sector: the inlet
+    total pressure oscillates, p0 (1 + a sin(2 pi f t)); 2H+1 stacked
+    instances of ``annular_sector`` (the rotating zone is not applied)."""
+    from . import hb as HB
+    w = annular_sector(nr, nt, nz, **kw)
+    omegas = HB.omega_list([2.0 * np.pi * frequency], [harmonics])
+    n = 2 * harmonics + 1
+    t = HB.select_instants(omegas, n, selected_period)
+    D = HB.hb_operator(omegas, t)
+
+    def patch_for(q, J):
+        if q.kind == M.PATCH_TOTAL_INLET:
+            q.p0 = q.p0 * (1.0 + amplitude * np.sin(omegas[1] * t[J]))
+        return q
+
+    st = HB.stack_instances(w.mesh, n, patch_for)
+    rep = lambda a: np.concatenate([a] * n)
+    return Workload("hb%d_%s" % (n, w.name), st, rep(w.p), rep(w.U), rep(w.T), dict(w.settings), hb=(n, D))
 
 
 def make_config(binding, settings: Dict, **overrides):

@@ -86,6 +86,7 @@ class Config(C.Structure):
         ("reset_pseudo", C.c_int32),
         ("rho_min", C.c_double), ("T_min", C.c_double), ("T_max", C.c_double),
         ("n_sweeps", C.c_int32),
+        ("viscous_lf_jacobian", C.c_int32),
     ]
 
 

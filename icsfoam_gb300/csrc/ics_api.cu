@@ -98,7 +98,7 @@ void free_all(Handle& h) {
                   m.bface, m.slot_base, m.scol, m.sface, m.nlow, m.nslot, m.fl_cells, m.rl_cells, m.fl_lptr,
                   m.rl_lptr, m.sweep_flag, m.sweep_ticket, h.W, h.W0, h.W00, h.Wprev, h.prim, h.pB, h.TB, h.UB, h.phiB, h.pseudoCo, h.rPDT,
                   h.ddtCoeff, h.q, h.bq, h.clin, h.grad, h.fflux, h.frec, h.flam, h.bjac, h.src, h.vcell,
-                  h.fvisc, h.vsf2, m.dc, m.Dhb, m.mrfU, m.mrfOm, m.mrfBU, m.mrfBIn, m.plagMode, m.plagP, m.bpartner, m.bw, m.bdelta, m.bdNei,
+                  h.fvisc, h.vsf2, h.vjac, m.dc, m.Dhb, m.mrfU, m.mrfOm, m.mrfBU, m.mrfBIn, m.plagMode, m.plagP, m.bpartner, m.bw, m.bdelta, m.bdNei,
                   m.bnodc, m.cyc_face, m.cyc_row, m.cyc_ptr, h.cblk, h.cfrec, h.tW, h.tprim, h.tq, h.tgrad, h.tflux, h.tvc, h.tfv, h.tv,
                   h.ss, h.ssB, h.srhoS, h.srhoS0, h.srhoS00, h.sgrad, h.sgradL, h.sface, h.sblk, h.sdg, h.srD,
                   h.ssrc, h.sFixed, h.sValue,
@@ -144,6 +144,10 @@ int validate_config(const ics_config* c, std::string& err) {
       c->preconditioner > 2 || c->n_sweeps < 1) {
     err = "Unknown solver or preconditioner";
     return ICS_ERR_SCHEME;
+  }
+  if (c->viscous_lf_jacobian != 0 && c->viscous_lf_jacobian != 1) {
+    err = "viscous_lf_jacobian must be 0 or 1";
+    return ICS_ERR_ARG;
   }
   const int rs[3] = {c->recon_rho, c->recon_U, c->recon_T};
   for (int r : rs)
@@ -526,6 +530,7 @@ int do_residual(Handle& h, double* host_src) {
       h.vcell = dalloc<double>(24ull * h.m.N);
       h.fvisc = dalloc<double>(8ull * (h.m.F + h.m.B));
       h.vsf2 = dalloc<double>((size_t)h.m.F + h.m.B);
+      h.vjac = dalloc<double>(2ull * (h.m.F + h.m.B));
     }
     launch_viscous(h);
   }
@@ -696,6 +701,7 @@ void ics_default_config(ics_config* c) {
   c->T_min = SMALL;
   c->T_max = GREAT;
   c->n_sweeps = 1;
+  c->viscous_lf_jacobian = 1;
 }
 
 int ics_create(const ics_mesh_desc* mesh, const ics_config* cfg, ics_handle* out) {

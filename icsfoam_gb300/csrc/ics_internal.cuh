@@ -182,6 +182,8 @@ struct Handle {
   double* vcell = nullptr;  // [24][N] grad U, grad e, tauMC, mu, alphaEff, e
   double* fvisc = nullptr;  // [8][F+B] lapU, divTau, divSig, lapE face terms
   double* vsf2 = nullptr;   // [F] LF viscous Jacobian coefficient
+  double* vjac = nullptr;   // [2][F+B] non-LF viscous laplacian coefficients: internal and
+                            // coupled faces (mu_f|S|) dc, (alpha_f|S|) dc; boundary mu_b, alpha_b
   // Jacobian (FP64 or FP32 storage by precision)
   void* blk = nullptr;      // [nslots*25*32]
   void* dg = nullptr;       // [nslices*25*32]

@@ -51,13 +51,43 @@ struct EulerJ {
   }
 };
 
+// The five laplacian fields of the non-LF viscous Jacobian at one state
+// (viscousFluxScheme.C:259-267): -U/rho on momentum by rho and energy by rhoU,
+// 1/rho on momentum by rhoU (x I) and energy by rhoE, -E/rho + |U|^2/rho on
+// energy by rho, with E = he(T) + 0.5|U|^2.
+struct ViscLapField {
+  double mUr[3], ir, eR;
+  __device__ __forceinline__ void init(double rho, const double* U, double T, double Cv) {
+    const double u2 = dot3(U, U);
+    const double E = Cv * T + 0.5 * u2;
+    for (int k = 0; k < 3; ++k) mUr[k] = -U[k] / rho;
+    ir = 1.0 / rho;
+    eR = -E / rho + u2 / rho;
+  }
+  // entry (i, j) of the five laplacians for coefficients mg (mu) and ag (alphaEff)
+  __device__ __forceinline__ double entry(int i, int j, double mg, double ag) const {
+    if (i >= 1 && i <= 3) {
+      if (j == 0) return mUr[i - 1] * mg;
+      if (j == i) return ir * mg;
+      return 0.0;
+    }
+    if (i == 4) {
+      if (j == 0) return eR * ag;
+      if (j == 4) return ir * ag;
+      return mUr[j - 1] * ag;
+    }
+    return 0.0;
+  }
+};
+
 // Boundary diagonal contribution of one boundary face (addBoundaryTerms and
-// the boundary part of insertDissipationBlock), FP64, [25][B].
+// the boundary part of insertDissipationBlock), FP64, [25][B].  vj (non-LF
+// viscous Jacobian only): the patch mu and alphaEff, [2][F+B].
 __global__ void k_jac_boundary(DevMesh m, double R, double Cv, double gamma, const double* __restrict__ W,
                                const double* __restrict__ prim, const double* __restrict__ pB,
                                const double* __restrict__ TB, const double* __restrict__ UBv,
                                const double* __restrict__ phiB, const double* __restrict__ flam,
-                               double* __restrict__ bjac) {
+                               double* __restrict__ bjac, const double* __restrict__ vj) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= m.B) return;
   if (m.bpartner && m.bpartner[b] >= 0) return;  // cyclic faces: k_jac_cyclic
@@ -146,6 +176,42 @@ __global__ void k_jac_boundary(DevMesh m, double R, double Cv, double gamma, con
   // boundary dissipation 0.5 |S_b| lambda_b on the diagonal entries
   const double d = 0.5 * bm * flam[m.F + b];
   for (int q = 0; q < 5; ++q) D[6 * q] += d;
+  if (vj) {
+    // non-LF viscous boundary terms (viscousFluxScheme.C:41-86, 120-215):
+    // dMomFlux/dU = diag(-mu_b uGIC |S|), dEnergyFlux/dT = -alphaEff_b Cv TGIC |S|
+    // with gradientInternalCoeffs fixedValue -dc, zeroGradient 0, slip -dc |n_k|,
+    // pressureInletOutletVelocity -dc sqrt(|1 - n_k^2|) on inflow faces
+    const double dcb = m.bdc[b];
+    double uG[3] = {0.0, 0.0, 0.0}, tG = 0.0;
+    switch (pt.kind) {
+      case ICS_PATCH_SLIP:
+        for (int k = 0; k < 3; ++k) uG[k] = -dcb * fabs(nf[k]);
+        break;
+      case ICS_PATCH_FIXED:
+      case ICS_PATCH_ISOTHERMAL_WALL:
+        uG[0] = uG[1] = uG[2] = -dcb;
+        tG = -dcb;
+        break;
+      case ICS_PATCH_TOTAL_INLET:
+        if (phiB[b] < 0)
+          for (int k = 0; k < 3; ++k) uG[k] = -dcb * sqrt(fabs(1.0 - nf[k] * nf[k]));
+        tG = -dcb;
+        break;
+      default: break;
+    }
+    const int FB = m.F + B;
+    const double muB = vj[m.F + b], alB = vj[FB + m.F + b];
+    const double EI = Cv * prim[N + ci] + 0.5 * magU2;
+    const double dEvdT = -alB * Cv * tG * bm;
+    for (int i = 0; i < 3; ++i) {
+      const double dMv = -muB * uG[i] * bm;
+      D[5 * (1 + i)] += dMv * dUdRho[i];
+      D[6 * (1 + i)] += dMv * dUdRhoU;
+      D[21 + i] += dEvdT * dTdRhoU[i];
+    }
+    D[20] += dEvdT * (-1.0 / (Cv * rhoI) * (EI - magU2));
+    D[24] += dEvdT * dTdRhoE;
+  }
   for (int k = 0; k < 25; ++k) bjac[k * B + b] = D[k];
 }
 
@@ -157,10 +223,17 @@ __global__ void k_jac_boundary(DevMesh m, double R, double Cv, double gamma, con
 // The interface block multiplies the partner's unknowns with their momentum
 // rotated into this side's frame (Amul: patchNeighbourField of psi,
 // blockFvMatrix.C:386-407), so the stored block is U_f diag(1, R, 1).
+// vsf2: the LF viscous coefficient; vj with W, prim and the boundary state:
+// the non-LF viscous laplacians, whose interface takes the fields at the
+// coupled patch value and whose diagonal takes them at the owner cell
+// (blockFvOperatorsTemplates.C:428-448).
 template <typename T>
 __global__ void k_jac_cyclic(DevMesh m, double gamma, const double* __restrict__ cfrec,
                              const double* __restrict__ flam, double* __restrict__ bjac, T* __restrict__ cblk,
-                             const double* __restrict__ vsf2) {
+                             const double* __restrict__ vsf2, const double* __restrict__ vj,
+                             const double* __restrict__ W, const double* __restrict__ prim,
+                             const double* __restrict__ pB, const double* __restrict__ TB,
+                             const double* __restrict__ UBv, double Rgas, double Cv) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m.ncyc) return;
   const int B = m.B, nc = m.ncyc;
@@ -199,6 +272,22 @@ __global__ void k_jac_cyclic(DevMesh m, double gamma, const double* __restrict__
       D[k] = dg;
       U[k] = up;
     }
+  if (vj) {
+    const int N = m.N, FB = m.F + B, o = m.bcell[b];
+    const double mg = vj[m.F + b], ag = vj[FB + m.F + b];
+    ViscLapField fo, fb;
+    const double Uo[3] = {prim[2 * N + o], prim[3 * N + o], prim[4 * N + o]};
+    const double Ub[3] = {UBv[b], UBv[B + b], UBv[2 * B + b]};
+    fo.init(W[5 * o], Uo, prim[N + o], Cv);
+    fb.init((1.0 / (Rgas * TB[b])) * pB[b], Ub, TB[b], Cv);
+#pragma unroll
+    for (int r = 0; r < 5; ++r)
+#pragma unroll
+      for (int c = 0; c < 5; ++c) {
+        D[5 * r + c] += fo.entry(r, c, mg, ag);
+        U[5 * r + c] -= fb.entry(r, c, mg, ag);
+      }
+  }
 #pragma unroll
   for (int k = 0; k < 25; ++k) bjac[k * B + b] = D[k];
   T* out = cblk + (size_t)i * 25;
@@ -213,19 +302,31 @@ __global__ void k_jac_cyclic(DevMesh m, double gamma, const double* __restrict__
   }
 }
 
-// Row assembly.  T = block storage/compute type.
-template <typename T>
+// Row assembly.  T = block storage/compute type; VJ: the non-LF viscous
+// laplacians (vj, W, prim, Cv used only then).
+template <typename T, bool VJ>
 __global__ void __launch_bounds__(128) k_jac_rows(DevMesh m, double gamma, const double* __restrict__ frec,
                                                   const double* __restrict__ flam, const double* __restrict__ bjac,
                                                   const double* __restrict__ ddtCoeff, T* __restrict__ blk,
                                                   T* __restrict__ dg, T* __restrict__ rD, int* __restrict__ status,
-                                                  const double* __restrict__ vsf2) {
-  // vsf2 (viscous cases): LF viscous coefficient 0.5 lambda_v |S| deltaCoeffs,
-  // subtracted from the off-diagonal and added to the diagonal entries
-  // (viscousFluxScheme.C:234-247); nullptr for inviscid cases
+                                                  const double* __restrict__ vsf2, const double* __restrict__ vj,
+                                                  const double* __restrict__ W, const double* __restrict__ prim,
+                                                  double Cv) {
+  // vsf2 (viscous cases, LaxFriedrichJacobian): LF viscous coefficient
+  // 0.5 lambda_v |S| deltaCoeffs, subtracted from the off-diagonal and added
+  // to the diagonal entries (viscousFluxScheme.C:234-247); nullptr otherwise.
+  // VJ: each face adds the five laplacians at this cell to the diagonal and
+  // minus those at the other cell to the off-diagonal block
+  // (viscousFluxScheme.C:259-267, blockFvOperatorsTemplates.C:386-420).
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.N) return;
   const int F = m.F, B = m.B;
+  ViscLapField vfc;
+  if constexpr (VJ) {
+    const int N = m.N;
+    const double Uc[3] = {prim[2 * N + c], prim[3 * N + c], prim[4 * N + c]};
+    vfc.init(W[5 * c], Uc, prim[N + c], Cv);
+  }
   const int s = c >> 5, lane = c & 31;
   T diag[25];
 #pragma unroll
@@ -259,6 +360,15 @@ __global__ void __launch_bounds__(128) k_jac_rows(DevMesh m, double gamma, const
     // MRF: -div(w, u_MRF |S|) on the diagonal entries (convectiveFluxScheme.C:477-481,
     // blockFvOperatorsTemplates.C:148-197): upper -= phi (1-w), lower += phi w,
     // and the matching negative column sums on the diagonal
+    ViscLapField vfx;
+    double mg = 0.0, ag = 0.0;
+    if constexpr (VJ) {
+      const int N = m.N, x = isOwn ? m.nei[f] : m.own[f];
+      const double Ux[3] = {prim[2 * N + x], prim[3 * N + x], prim[4 * N + x]};
+      vfx.init(W[5 * x], Ux, prim[N + x], Cv);
+      mg = vj[f];
+      ag = vj[F + B + f];
+    }
     T moff = T(0), mdg = T(0);
     if (m.mrfU) {
       const double phm = m.mrfU[f] * m.magSf[f], wf = m.w[f];
@@ -288,6 +398,10 @@ __global__ void __launch_bounds__(128) k_jac_rows(DevMesh m, double gamma, const
           diag[k] += d;
           off -= sv;
           diag[k] += sv;
+        }
+        if constexpr (VJ) {
+          off -= T(vfx.entry(i, j, mg, ag));
+          diag[k] += T(vfc.entry(i, j, mg, ag));
         }
         out[k * 32] = off;
       }
@@ -380,31 +494,45 @@ __global__ void k_jacobi_inverse(int N, const T* __restrict__ dg, T* __restrict_
 }
 
 void launch_jacobian(Handle& h) {
+  // viscous Jacobian: LF coefficient (vsf2) or the non-LF laplacians (vj)
+  const bool visc = h.cfg.c.viscous != 0, lf = h.cfg.c.viscous_lf_jacobian != 0;
+  const double* vsf2 = visc && lf ? h.vsf2 : nullptr;
+  const double* vj = visc && !lf ? h.vjac : nullptr;
   if (h.m.B > 0)
     ICS_LAUNCH(h, ICS_K_JAC_BOUNDARY, k_jac_boundary<<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, h.cfg.c.R, h.cfg.Cv, h.cfg.gamma, h.W, h.prim,
-                                                                h.pB, h.TB, h.UB, h.phiB, h.flam, h.bjac));
+                                                                h.pB, h.TB, h.UB, h.phiB, h.flam, h.bjac, vj));
   int* status = &h.ks->status;
   if (h.m.ncyc > 0) {
     if (prec(h) == ICS_PREC_MIXED)
       ICS_LAUNCH(h, ICS_K_JAC_BOUNDARY, k_jac_cyclic<float><<<grid_for(h.m.ncyc, 128), 128, 0, h.stream>>>(
-                                            h.m, h.cfg.gamma, h.cfrec, h.flam, h.bjac, (float*)h.cblk,
-                                            h.cfg.c.viscous ? h.vsf2 : nullptr));
+                                            h.m, h.cfg.gamma, h.cfrec, h.flam, h.bjac, (float*)h.cblk, vsf2, vj,
+                                            h.W, h.prim, h.pB, h.TB, h.UB, h.cfg.c.R, h.cfg.Cv));
     else
       ICS_LAUNCH(h, ICS_K_JAC_BOUNDARY, k_jac_cyclic<double><<<grid_for(h.m.ncyc, 128), 128, 0, h.stream>>>(
-                                            h.m, h.cfg.gamma, h.cfrec, h.flam, h.bjac, (double*)h.cblk,
-                                            h.cfg.c.viscous ? h.vsf2 : nullptr));
+                                            h.m, h.cfg.gamma, h.cfrec, h.flam, h.bjac, (double*)h.cblk, vsf2, vj,
+                                            h.W, h.prim, h.pB, h.TB, h.UB, h.cfg.c.R, h.cfg.Cv));
   }
   if (prec(h) == ICS_PREC_MIXED) {
-    ICS_LAUNCH(h, ICS_K_JAC_ROWS, k_jac_rows<float><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, h.cfg.gamma, h.frec, h.flam, h.bjac,
-                                                                   h.ddtCoeff, (float*)h.blk, (float*)h.dg,
-                                                                   (float*)h.rD, status, h.cfg.c.viscous ? h.vsf2 : nullptr));
+    if (vj)
+      ICS_LAUNCH(h, ICS_K_JAC_ROWS, k_jac_rows<float, true><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(
+                                        h.m, h.cfg.gamma, h.frec, h.flam, h.bjac, h.ddtCoeff, (float*)h.blk,
+                                        (float*)h.dg, (float*)h.rD, status, vsf2, vj, h.W, h.prim, h.cfg.Cv));
+    else
+      ICS_LAUNCH(h, ICS_K_JAC_ROWS, k_jac_rows<float, false><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(
+                                        h.m, h.cfg.gamma, h.frec, h.flam, h.bjac, h.ddtCoeff, (float*)h.blk,
+                                        (float*)h.dg, (float*)h.rD, status, vsf2, nullptr, nullptr, nullptr, 0.0));
     if (h.cfg.c.preconditioner == ICS_PC_JACOBI || h.cfg.c.solver == ICS_SOLVER_SMOOTH)
       ICS_LAUNCH(h, ICS_K_JACOBI_INV, k_jacobi_inverse<float><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m.N, (float*)h.dg, (float*)h.dginv,
                                                                           status));
   } else {
-    ICS_LAUNCH(h, ICS_K_JAC_ROWS, k_jac_rows<double><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, h.cfg.gamma, h.frec, h.flam, h.bjac,
-                                                                    h.ddtCoeff, (double*)h.blk, (double*)h.dg,
-                                                                    (double*)h.rD, status, h.cfg.c.viscous ? h.vsf2 : nullptr));
+    if (vj)
+      ICS_LAUNCH(h, ICS_K_JAC_ROWS, k_jac_rows<double, true><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(
+                                        h.m, h.cfg.gamma, h.frec, h.flam, h.bjac, h.ddtCoeff, (double*)h.blk,
+                                        (double*)h.dg, (double*)h.rD, status, vsf2, vj, h.W, h.prim, h.cfg.Cv));
+    else
+      ICS_LAUNCH(h, ICS_K_JAC_ROWS, k_jac_rows<double, false><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(
+                                        h.m, h.cfg.gamma, h.frec, h.flam, h.bjac, h.ddtCoeff, (double*)h.blk,
+                                        (double*)h.dg, (double*)h.rD, status, vsf2, nullptr, nullptr, nullptr, 0.0));
     if (h.cfg.c.preconditioner == ICS_PC_JACOBI || h.cfg.c.solver == ICS_SOLVER_SMOOTH)
       ICS_LAUNCH(h, ICS_K_JACOBI_INV, k_jacobi_inverse<double><<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m.N, (double*)h.dg, (double*)h.dginv,
                                                                            status));

@@ -112,7 +112,8 @@ __global__ void __launch_bounds__(128) k_visc_cell(DevMesh m, ViscParams P, cons
 template <typename Real = double>
 __global__ void __launch_bounds__(128) k_visc_face(DevMesh m, const Real* __restrict__ vc,
                                                    const Real* __restrict__ W, const Real* __restrict__ prim,
-                                                   Real* __restrict__ fv, double* __restrict__ sf2, int FB) {
+                                                   Real* __restrict__ fv, double* __restrict__ sf2,
+                                                   double* __restrict__ vj, int FB) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.F) return;
   const int N = m.N, F = m.F;
@@ -154,13 +155,17 @@ __global__ void __launch_bounds__(128) k_visc_face(DevMesh m, const Real* __rest
     const double rhof = wf * (W[5 * o] - W[5 * n]) + W[5 * n];
     const double lamv = (muf + alf) / rhof;
     sf2[f] = 0.5 * lamv * ms * m.dc[f];
+    if (vj) {  // laplacian coefficients of the non-LF Jacobian (blockFvOperatorsTemplates.C:398-399)
+      vj[f] = muf * ms * m.dc[f];
+      vj[FB + f] = alf * ms * m.dc[f];
+    }
   }
 }
 
 template <typename Real = double>
 __global__ void k_visc_bface(DevMesh m, ViscParams P, const Real* __restrict__ vc, const Real* __restrict__ prim,
                              const double* __restrict__ TB, const double* __restrict__ UBv, Real* __restrict__ fv,
-                             int FB) {
+                             double* __restrict__ vj, int FB) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= m.B) return;
   if (m.bpartner && m.bpartner[b] >= 0) return;  // cyclic faces: k_visc_cface
@@ -198,6 +203,10 @@ __global__ void k_visc_bface(DevMesh m, ViscParams P, const Real* __restrict__ v
   }
   fv[6 * FB + F + b] = dot3(sig, S);
   fv[7 * FB + F + b] = (alB * ms) * snE;
+  if (vj) {  // patch mu and alphaEff for the non-LF boundary terms (viscousFluxScheme.C:57-58)
+    vj[F + b] = muB;
+    vj[FB + F + b] = alB;
+  }
 }
 
 // Cyclic faces: the internal-face terms with the partner's vectors rotated
@@ -207,7 +216,8 @@ __global__ void k_visc_bface(DevMesh m, ViscParams P, const Real* __restrict__ v
 template <typename Real = double>
 __global__ void __launch_bounds__(128) k_visc_cface(DevMesh m, const Real* __restrict__ vc,
                                                     const Real* __restrict__ W, const Real* __restrict__ prim,
-                                                    Real* __restrict__ fv, double* __restrict__ sf2, int FB) {
+                                                    Real* __restrict__ fv, double* __restrict__ sf2,
+                                                    double* __restrict__ vj, int FB) {
   const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
   if (i0 >= m.ncyc) return;
   const int N = m.N, F = m.F, B = m.B;
@@ -268,6 +278,10 @@ __global__ void __launch_bounds__(128) k_visc_cface(DevMesh m, const Real* __res
   if constexpr (std::is_same<Real, double>::value) {
     const double rhof = lin(W[5 * o], W[5 * pc]);
     sf2[F + b] = 0.5 * ((muf + alf) / rhof) * ms * m.bdc[b];
+    if (vj) {
+      vj[F + b] = muf * ms * m.bdc[b];
+      vj[FB + F + b] = alf * ms * m.bdc[b];
+    }
   }
 }
 
@@ -284,17 +298,18 @@ void launch_viscous(Handle& h) {
   P.Ts = h.cfg.c.Ts;
   P.sutherland = h.cfg.c.sutherland;
   const int FB = h.m.F + h.m.B;
+  double* vj = h.vjac;  // written in both Jacobian modes: the mode may change between residual and assembly
   ICS_LAUNCH(h, ICS_K_VISC, k_visc_cell<<<grid_for(h.m.N, 128), 128, 0, h.stream>>>(h.m, P, h.W, h.prim, h.TB, h.UB,
                                                                                      h.vcell));
   if (h.m.F)
     ICS_LAUNCH(h, ICS_K_VISC, k_visc_face<<<grid_for(h.m.F, 128), 128, 0, h.stream>>>(h.m, h.vcell, h.W, h.prim,
-                                                                                       h.fvisc, h.vsf2, FB));
+                                                                                       h.fvisc, h.vsf2, vj, FB));
   if (h.m.B)
     ICS_LAUNCH(h, ICS_K_VISC, k_visc_bface<<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, P, h.vcell, h.prim, h.TB,
-                                                                                        h.UB, h.fvisc, FB));
+                                                                                        h.UB, h.fvisc, vj, FB));
   if (h.m.ncyc)
     ICS_LAUNCH(h, ICS_K_VISC, k_visc_cface<<<grid_for(h.m.ncyc, 128), 128, 0, h.stream>>>(h.m, h.vcell, h.W, h.prim,
-                                                                                           h.fvisc, h.vsf2, FB));
+                                                                                           h.fvisc, h.vsf2, vj, FB));
   ICS_CUDA(cudaGetLastError());
 }
 
@@ -315,13 +330,13 @@ void launch_viscous_tangent(Handle& h, const Dual* W, const Dual* prim, Dual* vc
                                                                                              h.UB, vc));
   if (h.m.F)
     ICS_LAUNCH(h, ICS_K_TANGENT, k_visc_face<Dual><<<grid_for(h.m.F, 128), 128, 0, h.stream>>>(h.m, vc, W, prim, fv,
-                                                                                               nullptr, FB));
+                                                                                               nullptr, nullptr, FB));
   if (h.m.B)
     ICS_LAUNCH(h, ICS_K_TANGENT, k_visc_bface<Dual><<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, P, vc, prim, h.TB,
-                                                                                                h.UB, fv, FB));
+                                                                                                h.UB, fv, nullptr, FB));
   if (h.m.ncyc)
     ICS_LAUNCH(h, ICS_K_TANGENT, k_visc_cface<Dual><<<grid_for(h.m.ncyc, 128), 128, 0, h.stream>>>(h.m, vc, W, prim, fv,
-                                                                                                   nullptr, FB));
+                                                                                                   nullptr, nullptr, FB));
   ICS_CUDA(cudaGetLastError());
 }
 

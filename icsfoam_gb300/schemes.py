@@ -75,6 +75,8 @@ def config_from_dicts(binding: abi.Binding, fvSchemes: Dict, fvSolution: Dict, t
     cfg.flux_scheme = _FLUX[name]
     cfg.low_mach_ausm = _switch(cfs.get("lowMachAusm", True))
     cfg.entropy_fix_coeff = float(cfs.get("entropyFixCoeff", 0.05))
+    # viscousFluxScheme { LaxFriedrichJacobian true; } (viscousFluxScheme.C:107)
+    cfg.viscous_lf_jacobian = _switch(fvSchemes.get("viscousFluxScheme", {}).get("LaxFriedrichJacobian", True))
     ddt = fvSchemes.get("ddtSchemes", {}).get("default", "dualTime rPseudoDeltaT steadyState").split()
     if len(ddt) < 3 or ddt[0] != "dualTime" or ddt[-1] not in _DDT:
         raise ValueError("ddtSchemes default must be 'dualTime rPseudoDeltaT <steadyState|Euler|backward>'")

@@ -149,6 +149,13 @@ typedef struct {
   double rho_min, T_min, T_max;
   /* smoothSolverCoupled: Jacobi sweeps per stop test (nSweeps)            */
   int32_t n_sweeps;
+  /* viscousFluxScheme: LaxFriedrichJacobian (viscousFluxScheme.C:107).
+   * 1 (default): the viscous Jacobian is the scalar laplacian of
+   * 0.5 (mu+alphaEff)/rho on every equation.  0: the laplacians of mu and
+   * alphaEff acting on the conserved variables through -U/rho, 1/rho,
+   * (|U|^2-E)/rho, plus the boundary terms of the physical patches
+   * (viscousFluxScheme.C:120-215, 249-267).                               */
+  int32_t viscous_lf_jacobian;
 } ics_config;
 
 /* residualsIO (residualsIO.H:54-315): L1 residuals normalised per equation. */

@@ -116,6 +116,10 @@ struct Case {
   std::vector<double> pseudoCo, rPseudoDeltaT, ddtCoeff;
   // LF viscous Jacobian coefficient per internal face (from the last residual)
   std::vector<double> viscSf2;
+  // laplacian coefficients of the non-LF viscous Jacobian (F+B): internal and
+  // coupled faces (mu_f |S|) deltaCoeffs and (alphaEff_f |S|) deltaCoeffs,
+  // physical boundary faces the patch values mu_b and alphaEff_b
+  std::vector<double> viscMuG, viscAlG;
   // fluxes of the last calcFlux (F+B)
   std::vector<double> phi, phiE;
   std::vector<V3> phiU;
@@ -863,10 +867,16 @@ void viscousFields(const Case& c, Viscous& v) {
 // Viscous face fluxes out of the owner: momentum (laplacian(mu,U) + div(tauMC))
 // and energy (div(sigmaDotU . S) + laplacian(alphaEff, e)), each term kept
 // separate as in residualsUpdate.H, plus the LF viscous Jacobian coefficient
-// sf2 = 0.5 lambda_v |S| deltaCoeffs (viscousFluxScheme.C:234-247).
+// sf2 = 0.5 lambda_v |S| deltaCoeffs (viscousFluxScheme.C:234-247) and the
+// coefficients of the non-LF laplacians, muG = (mu_f |S|) deltaCoeffs and
+// alG = (alphaEff_f |S|) deltaCoeffs (blockFvOperatorsTemplates.C:398-399),
+// mu_b and alphaEff_b on physical boundary faces (viscousFluxScheme.C:57-58).
 void viscousFluxes(const Case& c, const Viscous& v, std::vector<V3>& lapU, std::vector<V3>& divTau,
-                   std::vector<double>& divSig, std::vector<double>& lapE, std::vector<double>& sf2) {
+                   std::vector<double>& divSig, std::vector<double>& lapE, std::vector<double>& sf2,
+                   std::vector<double>& muG, std::vector<double>& alG) {
   const int NF = c.F + c.B;
+  muG.assign(NF, 0.0);
+  alG.assign(NF, 0.0);
   lapU.assign(NF, V3());
   divTau.assign(NF, V3());
   divSig.assign(NF, 0.0);
@@ -908,6 +918,8 @@ void viscousFluxes(const Case& c, const Viscous& v, std::vector<V3>& lapU, std::
     const double rhof = lin(c.rho[o], c.rho[n]);
     const double lamv = (muf + alf) / rhof;
     sf2[fi] = 0.5 * lamv * ms * c.dc[fi];
+    muG[fi] = muf * ms * c.dc[fi];
+    alG[fi] = alf * ms * c.dc[fi];
   }
   if (c.hasCyc) sf2.resize(c.F + c.B, 0.0);  // coupled faces keep their own coefficient
   for (int b = 0; b < c.B; ++b) {
@@ -951,8 +963,12 @@ void viscousFluxes(const Case& c, const Viscous& v, std::vector<V3>& lapU, std::
       lapE[c.F + b] = (alf * ms) * snEc;
       const double rhof = lin(c.rho[o], c.rho[pc]);
       sf2[c.F + b] = 0.5 * ((muf + alf) / rhof) * ms * c.bdc[b];
+      muG[c.F + b] = muf * ms * c.bdc[b];
+      alG[c.F + b] = alf * ms * c.bdc[b];
       continue;
     }
+    muG[c.F + b] = v.muB[b];
+    alG[c.F + b] = v.alB[b];
     V3 snU;
     for (int j = 0; j < 3; ++j) snU[j] = (c.UB[b][j] - c.U[o][j]) * c.bdc[b];
     const double snE = (v.eB[b] - v.e[o]) * c.bdc[b];
@@ -1041,7 +1057,7 @@ void residualSource(Case& c) {
     viscousFields(c, v);
     std::vector<V3> lapU, divTau;
     std::vector<double> divSig, lapE;
-    viscousFluxes(c, v, lapU, divTau, divSig, lapE, c.viscSf2);
+    viscousFluxes(c, v, lapU, divTau, divSig, lapE, c.viscSf2, c.viscMuG, c.viscAlG);
     dLapU.assign(c.N, V3());
     dTau.assign(c.N, V3());
     dSig.assign(c.N, 0.0);
@@ -1436,9 +1452,105 @@ void assembleJacobian(Case& c) {
       D(3, 2) += o.x * Vc;
     }
   }
+  // viscousFluxScheme::createViscousJacobian without LaxFriedrichJacobian
+  // (viscousFluxScheme.C:249-273): minus the laplacians of mu and alphaEff
+  // acting through -U/rho, 1/rho (x I), -E/rho + |U|^2/rho, -U/rho, 1/rho, with
+  // E = he(T) + 0.5 |U|^2.  A laplacian of coefficient s and field vf gives
+  // upper = vf[nei] s, lower = vf[own] s, diag -= the lower of its own faces
+  // (blockFvOperatorsTemplates.C:386-448): so each face adds vf[cell] s to the
+  // diagonal of each of its cells and -vf[other] s to the off-diagonal
+  // block; a coupled face the interface -vf_b s with vf_b the patch value
+  // and vf[cell] s on the diagonal.  Physical patches add the boundary
+  // terms of addBoundaryTerms (viscousFluxScheme.C:41-86, 120-215).
+  if (c.cfg.viscous && !c.cfg.viscous_lf_jacobian && (int)c.viscMuG.size() == c.F + c.B) {
+    // the five laplacian fields at a cell (or patch) state: -U/rho, 1/rho, -E/rho + |U|^2/rho
+    struct VF {
+      V3 mUr;
+      double ir, eR;
+    };
+    auto vfOf = [&](double rho, const V3& U, double T) {
+      VF r;
+      const double E = heOf(c, T) + 0.5 * magSqr(U);
+      r.mUr = V3(-U.x / rho, -U.y / rho, -U.z / rho);
+      r.ir = 1.0 / rho;
+      r.eR = -E / rho + magSqr(U) / rho;
+      return r;
+    };
+    // add vf s to block A (sign +1) or subtract (-1): the five laplacians' entries
+    auto addLap = [&](B5& A, const VF& f, double mg, double ag, double sign) {
+      for (int i = 0; i < 3; ++i) {
+        A(1 + i, 0) += sign * (f.mUr[i] * mg);
+        A(1 + i, 1 + i) += sign * (f.ir * mg);
+        A(4, 1 + i) += sign * (f.mUr[i] * ag);
+      }
+      A(4, 0) += sign * (f.eR * ag);
+      A(4, 4) += sign * (f.ir * ag);
+    };
+    std::vector<VF> cell(c.N);
+    for (int i = 0; i < c.N; ++i) cell[i] = vfOf(c.rho[i], c.U[i], c.T[i]);
+    for (int fi = 0; fi < c.F; ++fi) {
+      const int o = c.own[fi], n = c.nei[fi];
+      const double mg = c.viscMuG[fi], ag = c.viscAlG[fi];
+      addLap(c.upper[fi], cell[n], mg, ag, -1.0);
+      addLap(c.lower[fi], cell[o], mg, ag, -1.0);
+      addLap(c.diag[o], cell[o], mg, ag, 1.0);
+      addLap(c.diag[n], cell[n], mg, ag, 1.0);
+    }
+    for (int b = 0; b < c.B; ++b) {
+      const int o = c.bcell[b];
+      const Patch& pt = c.patches[c.bpatch[b]];
+      if (isCyc(c, b)) {
+        const double mg = c.viscMuG[c.F + b], ag = c.viscAlG[c.F + b];
+        addLap(c.iface[b], vfOf(rhoBof(c, b), c.UB[b], c.TB[b]), mg, ag, -1.0);
+        addLap(c.diag[o], cell[o], mg, ag, 1.0);
+        continue;
+      }
+      if (pt.kind == ICS_PATCH_EMPTY) continue;
+      // gradientInternalCoeffs of U and T: fixedValue -deltaCoeffs, zeroGradient 0,
+      // slip -deltaCoeffs |n_k| (basicSymmetry snGradTransformDiag),
+      // pressureInletOutletVelocity -deltaCoeffs sqrt(|1 - n_k^2|) on inflow faces
+      // (directionMixed with valueFraction I - n n), 0 on outflow
+      const double dcb = c.bdc[b];
+      const V3 nf = c.bSf[b] / c.bmagSf[b];
+      V3 uG;
+      double tG = 0.0;
+      switch (pt.kind) {
+        case ICS_PATCH_SLIP: uG = V3(-dcb * std::fabs(nf.x), -dcb * std::fabs(nf.y), -dcb * std::fabs(nf.z)); break;
+        case ICS_PATCH_FIXED:
+        case ICS_PATCH_ISOTHERMAL_WALL:
+          uG = V3(-dcb, -dcb, -dcb);
+          tG = -dcb;
+          break;
+        case ICS_PATCH_TOTAL_INLET:
+          if (c.phiB[b] < 0)
+            uG = V3(-dcb * std::sqrt(std::fabs(1.0 - nf.x * nf.x)), -dcb * std::sqrt(std::fabs(1.0 - nf.y * nf.y)),
+                    -dcb * std::sqrt(std::fabs(1.0 - nf.z * nf.z)));
+          tG = -dcb;
+          break;
+        default: break;
+      }
+      const double muB = c.viscMuG[c.F + b], alB = c.viscAlG[c.F + b];
+      const double ms = c.bmagSf[b];
+      const V3 dMdU(-muB * uG.x * ms, -muB * uG.y * ms, -muB * uG.z * ms);
+      const double dEdT = -alB * c.Cv * tG * ms;
+      const double rhoI = c.rho[o];
+      const V3 UI = c.U[o];
+      const double EI = heOf(c, c.T[o]) + 0.5 * magSqr(UI);
+      const double cvI = c.Cv;
+      const double dTdRho = -1.0 / (cvI * rhoI) * (EI - magSqr(UI));
+      B5& D = c.diag[o];
+      for (int i = 0; i < 3; ++i) {
+        D(1 + i, 0) += dMdU[i] * (-UI[i] / rhoI);
+        D(1 + i, 1 + i) += dMdU[i] * (1.0 / rhoI);
+        D(4, 1 + i) += dEdT * (-UI[i] / (cvI * rhoI));
+      }
+      D(4, 0) += dEdT * dTdRho;
+      D(4, 4) += dEdT * (1.0 / (cvI * rhoI));
+    }
+  }
   // viscousFluxScheme::createViscousJacobian, LaxFriedrichJacobian:
   // minus laplacian(0.5 lambda_v, 1) on rho, rhoU (x I), rhoE (viscousFluxScheme.C:234-247)
-  if (c.cfg.viscous && (int)c.viscSf2.size() >= c.F) {
+  if (c.cfg.viscous && c.cfg.viscous_lf_jacobian && (int)c.viscSf2.size() >= c.F) {
     for (int fi = 0; fi < c.F; ++fi) {
       const double s = c.viscSf2[fi];
       for (int q = 0; q < 5; ++q) {
@@ -2452,6 +2564,7 @@ void icsref_default_config(ics_config* c) {
   c->T_min = SMALL;
   c->T_max = GREAT;
   c->n_sweeps = 1;
+  c->viscous_lf_jacobian = 1;
 }
 
 int icsref_set_config(ics_handle h, const ics_config* cfg) {
@@ -2465,6 +2578,7 @@ int icsref_set_config(ics_handle h, const ics_config* cfg) {
     h->err = "Unknown solver or preconditioner";
     return ICS_ERR_SCHEME;
   }
+  if (cfg->viscous_lf_jacobian != 0 && cfg->viscous_lf_jacobian != 1) return ICS_ERR_ARG;
   if (cfg->n_directions < 1 || cfg->n_directions > 64) return ICS_ERR_ARG;
   if (h->nInst > 1 && (cfg->ddt_scheme != ICS_DDT_STEADY || cfg->solver != ICS_SOLVER_GMRES)) {
     h->err = "Harmonic Balance needs steadyState ddt and the GMRES solver";

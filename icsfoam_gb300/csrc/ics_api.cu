@@ -96,7 +96,7 @@ void free_all(Handle& h) {
   void* ptrs[] = {m.own, m.nei, m.Sf, m.magSf, m.w, m.nodc, m.dOwn, m.dNei, m.dCC, m.nf, m.bnf, m.C, m.V,
                   m.bcell, m.bpatch, m.bSf, m.bmagSf, m.bdOwn, m.bdc, m.patches, m.cptr, m.cface, m.bptr,
                   m.bface, m.slot_base, m.scol, m.sface, m.nlow, m.nslot, m.fl_cells, m.rl_cells, m.fl_lptr,
-                  m.rl_lptr, m.sweep_flag, m.sweep_ticket, h.W, h.W0, h.W00, h.Wprev, h.prim, h.pB, h.TB, h.UB, h.phiB, h.pseudoCo, h.rPDT,
+                  m.rl_lptr, m.sweep_pad, m.sweep_ticket, h.W, h.W0, h.W00, h.Wprev, h.prim, h.pB, h.TB, h.UB, h.phiB, h.pseudoCo, h.rPDT,
                   h.ddtCoeff, h.q, h.bq, h.clin, h.grad, h.fflux, h.frec, h.flam, h.bjac, h.src, h.vcell,
                   h.fvisc, h.vsf2, h.vjac, m.dc, m.Dhb, m.mrfU, m.mrfOm, m.mrfBU, m.mrfBIn, m.plagMode, m.plagP, m.bpartner, m.bw, m.bdelta, m.bdNei,
                   m.bnodc, m.cyc_face, m.cyc_row, m.cyc_ptr, h.cblk, h.cfrec, h.tW, h.tprim, h.tq, h.tgrad, h.tflux, h.tvc, h.tfv, h.tv,
@@ -448,7 +448,8 @@ void build_mesh(Handle& h, const ics_mesh_desc* d) {
   m.fl_cells = upload(fcells);
   m.rl_cells = upload(rcells);
   m.fl_lptr = upload(m.fl_ptr);
-  m.sweep_flag = dalloc<int>((size_t)N);
+  // outputs of the sync-free sweeps (the schedules with many levels only)
+  if (m.nfl > 2 && (long)N >= 2048L * m.nfl) m.sweep_pad = dalloc<double>(16ull * N);
   m.sweep_ticket = dalloc<unsigned int>(2);
   m.rl_lptr = upload(m.rl_ptr);
 }
@@ -1152,6 +1153,7 @@ int ics_test_sweep_timeout(ics_handle hh, int32_t skip_row, int32_t spin_limit) 
       return ICS_ERR_STATE;
     }
     if (skip_row < 0 || skip_row >= N) return ICS_ERR_ARG;
+    if (!h.m.sweep_pad) h.m.sweep_pad = dalloc<double>(16ull * N);  // schedules with few levels
     // the forward level order without skip_row
     std::vector<int> order(N);
     ICS_CUDA(cudaMemcpy(order.data(), h.m.fl_cells, N * sizeof(int), cudaMemcpyDeviceToHost));

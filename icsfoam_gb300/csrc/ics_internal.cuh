@@ -104,7 +104,7 @@ struct DevMesh {
   int* rl_cells = nullptr;           // cells by reverse level
   int* fl_lptr = nullptr;            // device copies of the level pointers
   int* rl_lptr = nullptr;
-  int* sweep_flag = nullptr;         // [N] done flags of the sync-free sweeps (0 / 1)
+  void* sweep_pad = nullptr;         // [2][8N] FP64-sized outputs of the sync-free sweeps
   unsigned int* sweep_ticket = nullptr;  // [2] row tickets of the sync-free sweeps
   bool fuse_last = false;            // last forward level == first reverse level (same rows)
   // Harmonic Balance: nInst stacked instances of Nc cells (instance-major),

@@ -456,47 +456,68 @@ __global__ void __launch_bounds__(1024) k_lusgs_block(DevMesh m, const TB* __res
 // One launch per sweep for schedules with many levels (RCM / natural
 // numbering): blocks draw consecutive tickets in level order (order[]), so a
 // row only ever waits for rows with smaller tickets, whose blocks started
-// earlier and are resident or done -- no deadlock.  A row spins (bounded) on
-// its neighbours' done flags, reads their values through L2 (ld.cg: L1 is not
-// coherent between SMs), writes its own value, fences, and raises its flag.
-// The arithmetic per row is that of lusgs_fwd_row / lusgs_rev_row, so the
-// result equals the level-by-level sweep bit for bit.  A wait that exceeds
-// the bound sets status bit 8 and returns (the host reports ICS_ERR_TIMEOUT).
+// earlier and are resident or done -- no deadlock.  The sweep writes its rows
+// into a padded output array (8 words per row, 32 B for FP32) that starts
+// filled with a sentinel (all bits set, a NaN that GPU arithmetic never
+// produces: its NaNs are the canonical 0x7fff.. ones), and a row's result
+// words are their own done flags: a row polls its neighbours' five words
+// with relaxed loads until none is the sentinel.  One L2 round trip per
+// poll brings both the readiness and the values, the writer needs no fence,
+// and the polls of all prefetched neighbours are issued together.  The
+// arithmetic per row is that of lusgs_fwd_row / lusgs_rev_row, so the result
+// equals the level-by-level sweep bit for bit.  A wait that exceeds the
+// bound sets status bit 8, publishes zeros (so that its dependents do not
+// wait in turn) and returns; waiting rows that see bit 8 give up too (the
+// host reports ICS_ERR_TIMEOUT).
 constexpr int SWEEP_SPIN_LIMIT = 1 << 22;
+constexpr int SWEEP_PAD = 8;  // words per row of the sweep outputs
 
-__device__ __forceinline__ int ld_acquire(const int* p) {
+__device__ __forceinline__ int ld_relaxed_int(const int* p) {
   int v;
-  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ void st_release(int* p, int v) {
-  asm volatile("st.release.gpu.global.b32 [%0], %1;" : : "l"(p), "r"(v) : "memory");
+__device__ __forceinline__ void ld_relaxed5(const float* p, float* v) {
+  asm volatile("ld.relaxed.gpu.global.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3])
+               : "l"(p)
+               : "memory");
+  asm volatile("ld.relaxed.gpu.global.f32 %0, [%1];" : "=f"(v[4]) : "l"(p + 4) : "memory");
 }
-
-// acquire-poll a neighbour's done flag: busy for a while, then with a short
-// sleep; bounded (status bit 8 and false after SWEEP_SPIN_LIMIT polls)
+__device__ __forceinline__ void ld_relaxed5(const double* p, double* v) {
+  asm volatile("ld.relaxed.gpu.global.v2.f64 {%0, %1}, [%2];" : "=d"(v[0]), "=d"(v[1]) : "l"(p) : "memory");
+  asm volatile("ld.relaxed.gpu.global.v2.f64 {%0, %1}, [%2];" : "=d"(v[2]), "=d"(v[3]) : "l"(p + 2) : "memory");
+  asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v[4]) : "l"(p + 4) : "memory");
+}
+__device__ __forceinline__ void st_relaxed5(float* p, const float* v) {
+  asm volatile("st.relaxed.gpu.global.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(v[0]), "f"(v[1]), "f"(v[2]),
+               "f"(v[3])
+               : "memory");
+  asm volatile("st.relaxed.gpu.global.f32 [%0], %1;" ::"l"(p + 4), "f"(v[4]) : "memory");
+}
+__device__ __forceinline__ void st_relaxed5(double* p, const double* v) {
+  asm volatile("st.relaxed.gpu.global.v2.f64 [%0], {%1, %2};" ::"l"(p), "d"(v[0]), "d"(v[1]) : "memory");
+  asm volatile("st.relaxed.gpu.global.v2.f64 [%0], {%1, %2};" ::"l"(p + 2), "d"(v[2]), "d"(v[3]) : "memory");
+  asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p + 4), "d"(v[4]) : "memory");
+}
+__device__ __forceinline__ bool sweep_word_set(float v) { return __float_as_uint(v) != 0xffffffffu; }
+__device__ __forceinline__ bool sweep_word_set(double v) {
+  return (unsigned long long)__double_as_longlong(v) != ~0ull;
+}
 template <typename TV>
-__device__ __forceinline__ bool wait_flag(const int* flags, int j, int* status, int limit) {
-  int it = 0;
-  unsigned ns = 32;
-  while (ld_acquire(flags + j) == 0) {
-    if (++it > limit) {
-      atomicOr(status, 8);
-      return false;
-    }
-    // exponential back-off: rows many levels ahead stop loading the memory
-    // system that the rows being finished need
-    __nanosleep(ns);
-    if (ns < 1024) ns <<= 1;
-  }
-  return true;
+__device__ __forceinline__ bool sweep_ready(const TV* v) {
+  return sweep_word_set(v[0]) && sweep_word_set(v[1]) && sweep_word_set(v[2]) && sweep_word_set(v[3]) &&
+         sweep_word_set(v[4]);
 }
 
-template <typename TB, typename TV, bool FWD, bool SCALE>
+// FWD: in = the right-hand side r (5 words per row), out = the forward
+// result; !FWD: in = the forward result (padded), out = the reverse result,
+// also written to r (5 words per row).  `out` holds the sentinel on entry.
+template <typename TB, typename TV, bool FWD>
 __global__ void __launch_bounds__(128) k_lusgs_sweep(DevMesh m, const TB* __restrict__ blk,
-                                                     const TB* __restrict__ rD, TV* r, const int* __restrict__ order,
-                                                     int count, int* flags, unsigned int* ticket, int* status,
-                                                     int spin_limit) {
+                                                     const TB* __restrict__ rD, const TV* in, TV* out, TV* r,
+                                                     const int* __restrict__ order, int count, unsigned int* ticket,
+                                                     int* status, int spin_limit) {
   __shared__ int base;
   if (threadIdx.x == 0) base = (int)atomicAdd(ticket, blockDim.x);
   __syncthreads();
@@ -510,8 +531,7 @@ __global__ void __launch_bounds__(128) k_lusgs_sweep(DevMesh m, const TB* __rest
   const int nn = FWD ? nl : ns - nl;
   auto slot = [&](int p) { return FWD ? p : ns - 1 - p; };
   // everything that does not depend on the neighbours' results (columns,
-  // blocks, their rD) is loaded before the first wait; an acquire load keeps
-  // later loads behind it, so these would otherwise sit on the critical path
+  // blocks, their rD) is loaded before the first poll
   constexpr int PF = 3;
   int colp[PF];
   TB bp[PF][25];
@@ -529,17 +549,36 @@ __global__ void __launch_bounds__(128) k_lusgs_sweep(DevMesh m, const TB* __rest
   }
   TV acc[5];
 #pragma unroll
-  for (int k = 0; k < 5; ++k) acc[k] = __ldcg(r + 5 * c + k);
-  // all prefetched neighbours ready first: their value loads then overlap
-#pragma unroll
-  for (int p = 0; p < PF; ++p)
-    if (p < nn && !wait_flag<TV>(flags, colp[p], status, spin_limit)) return;
+  for (int k = 0; k < 5; ++k) acc[k] = FWD ? __ldcg(in + 5 * c + k) : __ldcg(in + SWEEP_PAD * c + k);
+  TV* mine = out + (size_t)SWEEP_PAD * c;
+  // poll the prefetched neighbours together: (bounded; gives up on bit 8)
   TV rv[PF][5];
+  unsigned pending = 0;
 #pragma unroll
   for (int p = 0; p < PF; ++p)
-    if (p < nn)
+    if (p < nn) pending |= 1u << p;
+  {
+    int it = 0;
+    unsigned ns_ = 32;
+    while (true) {
 #pragma unroll
-      for (int k = 0; k < 5; ++k) rv[p][k] = __ldcg(r + 5 * colp[p] + k);
+      for (int p = 0; p < PF; ++p)
+        if (pending & (1u << p)) {
+          ld_relaxed5(out + (size_t)SWEEP_PAD * colp[p], rv[p]);
+          if (sweep_ready(rv[p])) pending &= ~(1u << p);
+        }
+      if (!pending) break;
+      ++it;
+      if (it > spin_limit || ((it & 63) == 0 && (ld_relaxed_int(status) & 8))) {
+        if (it > spin_limit) atomicOr(status, 8);
+        const TV z[5] = {TV(0), TV(0), TV(0), TV(0), TV(0)};
+        st_relaxed5(mine, z);
+        return;
+      }
+      __nanosleep(ns_);
+      if (ns_ < 256) ns_ <<= 1;
+    }
+  }
 #pragma unroll
   for (int p = 0; p < PF; ++p) {
     if (p < nn) {
@@ -559,11 +598,26 @@ __global__ void __launch_bounds__(128) k_lusgs_sweep(DevMesh m, const TB* __rest
   for (int p = PF; p < nn; ++p) {  // rows with more neighbours than prefetched
     const int t = slot(p);
     const int col = m.scol[(sb + t) * 32 + lane];
-    if (!wait_flag<TV>(flags, col, status, spin_limit)) return;
+    TV rj5[5];
+    int it = 0;
+    unsigned ns_ = 32;
+    while (true) {
+      ld_relaxed5(out + (size_t)SWEEP_PAD * col, rj5);
+      if (sweep_ready(rj5)) break;
+      ++it;
+      if (it > spin_limit || ((it & 63) == 0 && (ld_relaxed_int(status) & 8))) {
+        if (it > spin_limit) atomicOr(status, 8);
+        const TV z[5] = {TV(0), TV(0), TV(0), TV(0), TV(0)};
+        st_relaxed5(mine, z);
+        return;
+      }
+      __nanosleep(ns_);
+      if (ns_ < 256) ns_ <<= 1;
+    }
     const TV rj = FWD ? TV(rD[col]) : TV(1);
     TV dj[5];
 #pragma unroll
-    for (int k = 0; k < 5; ++k) dj[k] = rj * __ldcg(r + 5 * col + k);
+    for (int k = 0; k < 5; ++k) dj[k] = rj * rj5[k];
     const TB* Bk = blk + (size_t)(sb + t) * 25 * 32 + lane;
 #pragma unroll
     for (int a = 0; a < 5; ++a) {
@@ -573,14 +627,14 @@ __global__ void __launch_bounds__(128) k_lusgs_sweep(DevMesh m, const TB* __rest
       acc[a] -= v;
     }
   }
-  if (SCALE || !FWD) {
+  if (!FWD) {
     const TV rc = TV(rD[c]);
 #pragma unroll
     for (int k = 0; k < 5; ++k) acc[k] = rc * acc[k];
-  }
 #pragma unroll
-  for (int k = 0; k < 5; ++k) r[5 * c + k] = acc[k];
-  st_release(flags + c, 1);  // orders the row's stores before the flag
+    for (int k = 0; k < 5; ++k) r[5 * c + k] = acc[k];
+  }
+  st_relaxed5(mine, acc);
 }
 
 template <typename TB, typename TV>
@@ -891,14 +945,16 @@ static void lusgs_t(Handle& h, TV* r) {
   if (m.nfl > 2 && (long)m.N >= 2048L * m.nfl) {
     cudaStream_t st = h.stream;
     int* status = &h.ks->status;
-    ICS_CUDA(cudaMemsetAsync(m.sweep_flag, 0, (size_t)m.N * sizeof(int), st));
+    TV* fwd = (TV*)m.sweep_pad;
+    TV* rev = fwd + (size_t)SWEEP_PAD * m.N;
+    const size_t padBytes = (size_t)SWEEP_PAD * m.N * sizeof(TV);
+    ICS_CUDA(cudaMemsetAsync(fwd, 0xff, 2 * padBytes, st));  // the sentinel in both outputs
     ICS_CUDA(cudaMemsetAsync(m.sweep_ticket, 0, 2 * sizeof(unsigned int), st));
-    ICS_LAUNCH(h, ICS_K_LUSGS_FWD, k_lusgs_sweep<TB, TV, true, false><<<grid_for(m.N, 128), 128, 0, st>>>(
-                                       m, blk, rD, r, m.fl_cells, m.N, m.sweep_flag, m.sweep_ticket, status,
+    ICS_LAUNCH(h, ICS_K_LUSGS_FWD, k_lusgs_sweep<TB, TV, true><<<grid_for(m.N, 128), 128, 0, st>>>(
+                                       m, blk, rD, r, fwd, nullptr, m.fl_cells, m.N, m.sweep_ticket, status,
                                        SWEEP_SPIN_LIMIT));
-    ICS_CUDA(cudaMemsetAsync(m.sweep_flag, 0, (size_t)m.N * sizeof(int), st));
-    ICS_LAUNCH(h, ICS_K_LUSGS_REV, k_lusgs_sweep<TB, TV, false, true><<<grid_for(m.N, 128), 128, 0, st>>>(
-                                       m, blk, rD, r, m.rl_cells, m.N, m.sweep_flag, m.sweep_ticket + 1, status,
+    ICS_LAUNCH(h, ICS_K_LUSGS_REV, k_lusgs_sweep<TB, TV, false><<<grid_for(m.N, 128), 128, 0, st>>>(
+                                       m, blk, rD, fwd, rev, r, m.rl_cells, m.N, m.sweep_ticket + 1, status,
                                        SWEEP_SPIN_LIMIT));
     return;
   }
@@ -1004,17 +1060,18 @@ static void precondition_t(Handle& h, TV* r) {
 
 // One sync-free forward sweep over `order` (count rows) with a given wait
 // bound; used to exercise the bounded waits (a row left out of the order
-// never raises its flag, so its dependents must give up and report).
+// never writes its result, so its dependents must give up and report).
 template <typename TB, typename TV>
 static void sweep_probe_t(Handle& h, const int* order, int count, int spin_limit) {
   const DevMesh& m = h.m;
   cudaStream_t st = h.stream;
-  ICS_CUDA(cudaMemsetAsync(m.sweep_flag, 0, (size_t)m.N * sizeof(int), st));
+  TV* fwd = (TV*)m.sweep_pad;
+  ICS_CUDA(cudaMemsetAsync(fwd, 0xff, (size_t)SWEEP_PAD * m.N * sizeof(TV), st));
   ICS_CUDA(cudaMemsetAsync(m.sweep_ticket, 0, 2 * sizeof(unsigned int), st));
   ICS_CUDA(cudaMemsetAsync(h.kw, 0, 5ull * m.N * sizeof(TV), st));
-  ICS_LAUNCH(h, ICS_K_LUSGS_FWD, k_lusgs_sweep<TB, TV, true, false><<<grid_for(count, 128), 128, 0, st>>>(
-                                     m, (const TB*)h.blk, (const TB*)h.rD, (TV*)h.kw, order, count, m.sweep_flag,
-                                     m.sweep_ticket, &h.ks->status, spin_limit));
+  ICS_LAUNCH(h, ICS_K_LUSGS_FWD, k_lusgs_sweep<TB, TV, true><<<grid_for(count, 128), 128, 0, st>>>(
+                                     m, (const TB*)h.blk, (const TB*)h.rD, (const TV*)h.kw, fwd, nullptr, order,
+                                     count, m.sweep_ticket, &h.ks->status, spin_limit));
   ICS_CUDA(cudaGetLastError());
 }
 

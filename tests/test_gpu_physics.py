@@ -202,7 +202,7 @@ def test_checkpoint_resume_is_bit_exact(gpu_binding, unsteady, scalar):
 
 
 def test_bounded_sweep_wait_reports_timeout(gpu_binding):
-    """A row left out of a sync-free sweep never raises its flag: the rows that
+    """A row left out of a sync-free sweep never writes its result: the rows that
     wait on it give up after a short bound and the status says so; nothing
     faults and the context keeps working."""
     w = cases.bump_channel(24, 8, 4, ordering_mode="natural")

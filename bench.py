@@ -144,9 +144,15 @@ class ClockSampler:
 
 # ---------------------------------------------------------- algorithmic bytes
 def kernel_bytes(kind, N, F, B, nslots, mixed, nlev):
-    """Compulsory DRAM bytes of one launch of a kernel class (each array once)."""
+    """Compulsory DRAM bytes of one launch of a kernel class (each array once).
+
+    Off-diagonal slots hold ow words: 8 in FP32 storage (the factored block:
+    scaled normal, side velocity and energy, identity multiple), 25 in FP64;
+    diagonal blocks hold 25.
+    """
     pb = 4 if mixed else 8   # block entries
     pv = 4 if mixed else 8   # Krylov vectors
+    ow = 8 if mixed else 25  # words per off-diagonal slot
     if kind == "face":       # MUSCL face flux: gathered cell fields + face geometry + outputs
         return 264 * N + 232 * F
     if kind == "grad":
@@ -154,18 +160,18 @@ def kernel_bytes(kind, N, F, B, nslots, mixed, nlev):
     if kind == "cellres":
         return 136 * N + 64 * F
     if kind == "jac_rows":
-        return (112 + 50 * pb) * F + (25 * pb + 16 + pb) * N
+        return (112 + 2 * ow * pb) * F + (25 * pb + 16 + pb) * N
     if kind == "spmv":
-        return 25 * pb * N + 50 * pb * F + 8 * F + 10 * pv * N
+        return 25 * pb * N + 2 * ow * pb * F + 8 * F + 10 * pv * N
     if kind in ("lusgs_fwd", "lusgs_rev"):
         # colour-blocked 2-level schedule: one launch per sweep (forward level 0 has no lower
         # neighbours; the last forward level is fused with the first reverse one), reading all F
-        # blocks of its triangle, rD and r of its N/2 rows, the neighbours' deltas, writing deltas
-        return 25 * pb * F + pb * N / 2 + 3 * 5 * pv * N / 2 + 4 * F
+        # slots of its triangle, rD and r of its N/2 rows, the neighbours' deltas, writing deltas
+        return ow * pb * F + pb * N / 2 + 3 * 5 * pv * N / 2 + 4 * F
     if kind == "op0":   # fused operator, pass 1: (A x) on the level-0 half of the rows
-        return 25 * pb * N / 2 + 25 * pb * F + 5 * pv * N + 5 * pv * N / 2 + 4 * F
+        return 25 * pb * N / 2 + ow * pb * F + 5 * pv * N + 5 * pv * N / 2 + 4 * F
     if kind == "op1":   # pass 2: (A x) + forward sweep + first reverse on the other half
-        return 25 * pb * N / 2 + 25 * pb * F + 10 * pv * N + pb * N + 4 * F
+        return 25 * pb * N / 2 + ow * pb * F + 10 * pv * N + pb * N + 4 * F
     if kind == "mgs":
         return 20 * pv * N
     return None

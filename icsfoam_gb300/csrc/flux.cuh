@@ -64,7 +64,7 @@ __device__ __forceinline__ Real plag_q(const DevMesh& m, const Real* q, int k, i
     return v[k - Q_UX];
   }
   if (k == Q_C) {
-    const double g = m.plagGamma;
+    const double g = m.gamma;
     return plag_sum<Real>(m, b, pc, [&](int c) { return sqrt(g * (q[Q_P * N + c] / q[Q_RHO * N + c])); });
   }
   if (k == Q_H)

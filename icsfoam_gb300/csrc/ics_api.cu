@@ -21,6 +21,7 @@
 
 #include <nvtx3/nvToolsExt.h>
 
+#include "blocks.cuh"
 #include "ics_internal.cuh"
 
 using namespace ics;
@@ -99,7 +100,7 @@ void free_all(Handle& h) {
                   m.rl_lptr, m.sweep_pad, m.sweep_ticket, h.W, h.W0, h.W00, h.Wprev, h.prim, h.pB, h.TB, h.UB, h.phiB, h.pseudoCo, h.rPDT,
                   h.ddtCoeff, h.q, h.bq, h.clin, h.grad, h.fflux, h.frec, h.flam, h.bjac, h.src, h.vcell,
                   h.fvisc, h.vsf2, h.vjac, m.dc, m.Dhb, m.mrfU, m.mrfOm, m.mrfBU, m.mrfBIn, m.plagMode, m.plagP, m.bpartner, m.bw, m.bdelta, m.bdNei,
-                  m.bnodc, m.cyc_face, m.cyc_row, m.cyc_ptr, h.cblk, h.cfrec, h.tW, h.tprim, h.tq, h.tgrad, h.tflux, h.tvc, h.tfv, h.tv,
+                  m.bnodc, m.cyc_face, m.cyc_row, m.cyc_ptr, h.cblk, h.vjslotbuf, h.vjcellbuf, h.cfrec, h.tW, h.tprim, h.tq, h.tgrad, h.tflux, h.tvc, h.tfv, h.tv,
                   h.ss, h.ssB, h.srhoS, h.srhoS0, h.srhoS00, h.sgrad, h.sgradL, h.sface, h.sblk, h.sdg, h.srD,
                   h.ssrc, h.sFixed, h.sValue,
                   h.blk, h.dg,
@@ -189,7 +190,8 @@ void ensure_workspace(Handle& h) {
   if (h.kvPrec != p) {
     void* ptrs[] = {h.blk, h.dg, h.dginv, h.rD, h.kw, h.kx, h.kb, h.kt, h.kv};
     for (void* q : ptrs) dfree(q);
-    h.blk = dalloc<char>((size_t)h.m.nslots * 25 * 32 * eb);
+    // off-diagonal slots: factored in FP32, full in FP64 (blocks.cuh)
+    h.blk = dalloc<char>((size_t)h.m.nslots * slot_words(p == ICS_PREC_MIXED) * 32 * eb);
     h.dg = dalloc<char>((size_t)h.m.nslices * 25 * 32 * eb);
     h.dginv = dalloc<char>((size_t)h.m.nslices * 25 * 32 * eb);
     h.rD = dalloc<char>((size_t)h.m.N * eb);
@@ -723,7 +725,7 @@ int ics_create(const ics_mesh_desc* mesh, const ics_config* cfg, ics_handle* out
   h.cfg.c = *cfg;
   h.cfg.Cv = cfg->Cp - cfg->R;
   h.cfg.gamma = cfg->Cp / h.cfg.Cv;
-  h.m.plagGamma = h.cfg.gamma;
+  h.m.gamma = h.cfg.gamma;
   st = guard(hh, [&](Handle& hd) {
     ICS_CUDA(cudaStreamCreateWithFlags(&hd.stream, cudaStreamNonBlocking));
     build_mesh(hd, mesh);
@@ -767,7 +769,7 @@ int ics_set_config(ics_handle hh, const ics_config* cfg) {
     h.cfg.c = *cfg;
     h.cfg.Cv = cfg->Cp - cfg->R;
     h.cfg.gamma = cfg->Cp / h.cfg.Cv;
-    h.m.plagGamma = h.cfg.gamma;
+    h.m.gamma = h.cfg.gamma;
     h.haveExact = false;
     if (structural) ensure_workspace(h);
     return ICS_OK;
@@ -920,8 +922,16 @@ int ics_get_jacobian(ics_handle hh, double* diag, double* lower, double* upper) 
     const DevMesh& m = h.m;
     const bool mixed = h.jacPrecision == ICS_PREC_MIXED;
     const size_t eb = mixed ? 4 : 8;
-    std::vector<char> blk((size_t)m.nslots * 25 * 32 * eb), dg((size_t)m.nslices * 25 * 32 * eb);
-    ICS_CUDA(cudaMemcpy(blk.data(), h.blk, blk.size(), cudaMemcpyDeviceToHost));
+    // the off-diagonal slots are stored factored: expand them on the device
+    std::vector<double> blk((size_t)m.nslots * 25 * 32);
+    std::vector<char> dg((size_t)m.nslices * 25 * 32 * eb);
+    double* tmp = nullptr;
+    ICS_CUDA(cudaMalloc(&tmp, blk.size() * sizeof(double)));
+    launch_expand_slots(h, tmp);
+    cudaError_t e1 = cudaMemcpyAsync(blk.data(), tmp, blk.size() * sizeof(double), cudaMemcpyDeviceToHost, h.stream);
+    if (e1 == cudaSuccess) e1 = cudaStreamSynchronize(h.stream);  // the handle's stream does not block
+    cudaFree(tmp);
+    ICS_CUDA(e1);
     ICS_CUDA(cudaMemcpy(dg.data(), h.dg, dg.size(), cudaMemcpyDeviceToHost));
     std::vector<int> sb(m.nslices + 1), sface((size_t)m.nslots * 32), nsl(m.N);
     ICS_CUDA(cudaMemcpy(sb.data(), m.slot_base, sb.size() * sizeof(int), cudaMemcpyDeviceToHost));
@@ -939,7 +949,7 @@ int ics_get_jacobian(ics_handle hh, double* diag, double* lower, double* upper) 
         const int f = code >= 0 ? code : ~code;
         double* dst = code >= 0 ? upper : lower;  // owner row holds upper_f
         if (!dst) continue;
-        for (int k = 0; k < 25; ++k) dst[25 * f + k] = get(blk, ((size_t)(sb[s] + t) * 25 + k) * 32 + lane);
+        for (int k = 0; k < 25; ++k) dst[25 * f + k] = blk[((size_t)(sb[s] + t) * 25 + k) * 32 + lane];
       }
     }
     return ICS_OK;

@@ -131,10 +131,16 @@ struct DevMesh {
   int* cyc_ptr = nullptr;
   // phase-lag cyclic patches (Harmonic Balance): per patch 0 plain, 1 phase
   // lag, 2 phase lag with cylindrical velocity; per patch the instances'
-  // operator P [npatches][nInst][nInst]; gamma for the sound-speed neighbour
+  // operator P [npatches][nInst][nInst]
   int* plagMode = nullptr;
   double* plagP = nullptr;
-  double plagGamma = 1.4;
+  // ratio of specific heats (the phase-lagged sound speed, the factored
+  // off-diagonal blocks)
+  double gamma = 1.4;
+  // non-LF viscous parts of the off-diagonal blocks (blocks.cuh), block
+  // storage type; nullptr unless that Jacobian mode is assembled
+  const void* vjslot = nullptr;
+  const void* vjcell = nullptr;
   double* mrfU = nullptr;
   double* mrfOm = nullptr;
   double* mrfBU = nullptr;
@@ -176,6 +182,8 @@ struct Handle {
   double* flam = nullptr;   // [F+B]
   double* cfrec = nullptr;  // [8][ncyc]: the reconstructed states of the cyclic faces (as frec)
   void* cblk = nullptr;     // [ncyc][25] cyclic coupling blocks (partner rotation folded in)
+  void* vjslotbuf = nullptr;  // non-LF viscous block parts (FP64-sized): [nslots][2][32]
+  void* vjcellbuf = nullptr;  // and [5][N]
   double* bjac = nullptr;   // [25][B] boundary Jacobian diag contribution
   double* src = nullptr;    // [N][5] source = R*V
   // viscous terms (allocated when the case is viscous)
@@ -296,6 +304,8 @@ void launch_grad(Handle& h);
 void launch_face_flux(Handle& h);
 void launch_residual(Handle& h, double serRatio, bool applySer);
 void launch_jacobian(Handle& h);
+// the off-diagonal slots expanded to 25 FP64 entries, [nslots][25][32]
+void launch_expand_slots(Handle& h, double* out);
 void launch_update(Handle& h, int* boundedDev);
 void launch_bc(Handle& h);
 void launch_mrf_bc(Handle& h);

@@ -7,15 +7,17 @@
 //     lower_f = -0.5|S| A(W_L) - 0.5|S| lambda I  (row nei, column own)
 // and the diagonal is the negative column sum of the off-diagonal blocks
 // (LduMatrix::negSumDiag), plus the boundary dissipation, the boundary
-// Jacobian and the temporal term.  Each cell therefore evaluates A(W_L) and
-// A(W_R) of its faces (both sides of a face evaluate both Jacobians); in
-// mixed precision this block arithmetic runs in FP32.
+// Jacobian and the temporal term.  The off-diagonal slot is stored factored
+// (blocks.cuh: the side's state, the signed scaled normal and the identity
+// multiple); the diagonal needs the other side's Jacobian, which the cell
+// evaluates entry by entry.  In mixed precision this arithmetic runs in FP32.
 //
 // Reference: convectiveFluxScheme::addFluxTerms (convectiveFluxScheme.C:374-484),
 // addDissipationJacobian (:487-534), addBoundaryTerms with boundaryJacobian
 // (:47-120, :219-355), addTemporalTerms (:358-369); blockFvMatrix::insertBlock
 // and insertDissipationBlock (blockFvMatrix.C:211-326); LU-SGS scalar
 // diagonal (lusgs.C:50-127).
+#include "blocks.cuh"
 #include "flux.cuh"
 #include "ics_internal.cuh"
 
@@ -318,6 +320,9 @@ __global__ void __launch_bounds__(128) k_jac_rows(DevMesh m, double gamma, const
   // VJ: each face adds the five laplacians at this cell to the diagonal and
   // minus those at the other cell to the off-diagonal block
   // (viscousFluxScheme.C:259-267, blockFvOperatorsTemplates.C:386-420).
+  // Off-diagonal slots are stored factored (blocks.cuh): s = +-0.5|S| n,
+  // the side's (U, E) and c0 = the identity multiple; with VJ the slot's two
+  // laplacian coefficients go to vjslot and this cell's five fields to vjcell.
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.N) return;
   const int F = m.F, B = m.B;
@@ -326,6 +331,10 @@ __global__ void __launch_bounds__(128) k_jac_rows(DevMesh m, double gamma, const
     const int N = m.N;
     const double Uc[3] = {prim[2 * N + c], prim[3 * N + c], prim[4 * N + c]};
     vfc.init(W[5 * c], Uc, prim[N + c], Cv);
+    T* vc = (T*)m.vjcell;
+    for (int k = 0; k < 3; ++k) vc[k * N + c] = T(vfc.mUr[k]);
+    vc[3 * N + c] = T(vfc.ir);
+    vc[4 * N + c] = T(vfc.eR);
   }
   const int s = c >> 5, lane = c & 31;
   T diag[25];
@@ -337,10 +346,13 @@ __global__ void __launch_bounds__(128) k_jac_rows(DevMesh m, double gamma, const
   const int ns = m.nslot[c];
   for (int t = 0; t < width; ++t) {
     const int idx = (base + t) * 32 + lane;
-    T* out = blk + (size_t)(base + t) * 25 * 32 + lane;
+    constexpr int SW = SlotBlock<T>::W;  // 8 factored (FP32) or 25 full (FP64) words
+    T* out = blk + (size_t)(base + t) * SW * 32 + lane;
+    T* vout = VJ ? (T*)m.vjslot + (size_t)(base + t) * 2 * 32 + lane : nullptr;
     if (t >= ns) {
 #pragma unroll
-      for (int k = 0; k < 25; ++k) out[k * 32] = T(0);
+      for (int k = 0; k < SW; ++k) out[k * 32] = T(0);
+      if constexpr (VJ) vout[0] = vout[32] = T(0);
       continue;
     }
     const int code = m.sface[idx];
@@ -349,9 +361,10 @@ __global__ void __launch_bounds__(128) k_jac_rows(DevMesh m, double gamma, const
     const T nn[3] = {T(m.nf[f]), T(m.nf[F + f]), T(m.nf[2 * F + f])};
     const T UL[3] = {T(frec[f]), T(frec[F + f]), T(frec[2 * F + f])};
     const T UR[3] = {T(frec[3 * F + f]), T(frec[4 * F + f]), T(frec[5 * F + f])};
-    EulerJ<T> AL, AR;
-    AL.init(g, UL, T(frec[6 * F + f]), nn);
-    AR.init(g, UR, T(frec[7 * F + f]), nn);
+    // the diagonal takes minus the other orientation's block: -lower_f in
+    // the owner's row (A(W_L), -0.5|S|), -upper_f in the neighbour's row
+    EulerJ<T> Ad;
+    Ad.init(g, isOwn ? UL : UR, T(frec[(isOwn ? 6 : 7) * F + f]), nn);
     const T magS = T(m.magSf[f]);
     const T hs = T(0.5) * magS;
     const T mhs = T(-0.5) * magS;
@@ -360,14 +373,12 @@ __global__ void __launch_bounds__(128) k_jac_rows(DevMesh m, double gamma, const
     // MRF: -div(w, u_MRF |S|) on the diagonal entries (convectiveFluxScheme.C:477-481,
     // blockFvOperatorsTemplates.C:148-197): upper -= phi (1-w), lower += phi w,
     // and the matching negative column sums on the diagonal
-    ViscLapField vfx;
     double mg = 0.0, ag = 0.0;
     if constexpr (VJ) {
-      const int N = m.N, x = isOwn ? m.nei[f] : m.own[f];
-      const double Ux[3] = {prim[2 * N + x], prim[3 * N + x], prim[4 * N + x]};
-      vfx.init(W[5 * x], Ux, prim[N + x], Cv);
       mg = vj[f];
       ag = vj[F + B + f];
+      vout[0] = T(mg);
+      vout[32] = T(ag);
     }
     T moff = T(0), mdg = T(0);
     if (m.mrfU) {
@@ -375,35 +386,48 @@ __global__ void __launch_bounds__(128) k_jac_rows(DevMesh m, double gamma, const
       moff = isOwn ? T(-(phm * (1.0 - wf))) : T(phm * wf);
       mdg = isOwn ? T(-(phm * wf)) : T(phm * (1.0 - wf));
     }
+    // row own: this slot is upper_f = A(U_R, 0.5|S| n) + c0 I and the
+    // diagonal gains -lower_f; row nei: lower_f = A(U_L, -0.5|S| n) + c0 I
+    const T sg = isOwn ? hs : mhs;
+    const T* Us = isOwn ? UR : UL;
+    const T Es = T(frec[(isOwn ? 7 : 6) * F + f]);
+    if constexpr (SW == 8) {
+      out[0] = sg * nn[0];
+      out[32] = sg * nn[1];
+      out[64] = sg * nn[2];
+      out[96] = Us[0];
+      out[128] = Us[1];
+      out[160] = Us[2];
+      out[192] = Es;
+      out[224] = ((moff - d) - sv);
+    } else {
+      EulerJ<T> As;
+      As.init(g, Us, Es, nn);
+#pragma unroll
+      for (int i = 0; i < 5; ++i)
+#pragma unroll
+        for (int j = 0; j < 5; ++j) {
+          T off = sg * As.entry(i, j);
+          if (i == j) {
+            off += moff;
+            off -= d;
+            off -= sv;
+          }
+          out[(5 * i + j) * 32] = off;
+        }
+    }
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
 #pragma unroll
       for (int j = 0; j < 5; ++j) {
         const int k = 5 * i + j;
-        const T lo = mhs * AL.entry(i, j);
-        const T up = hs * AR.entry(i, j);
-        T off;
-        if (isOwn) {
-          // row own: this slot is upper_f; diagonal gains -lower_f
-          off = up;
-          diag[k] -= lo;
-        } else {
-          off = lo;
-          diag[k] -= up;
-        }
+        diag[k] -= (isOwn ? mhs : hs) * Ad.entry(i, j);
         if (i == j) {
-          off += moff;
           diag[k] += mdg;
-          off -= d;
           diag[k] += d;
-          off -= sv;
           diag[k] += sv;
         }
-        if constexpr (VJ) {
-          off -= T(vfx.entry(i, j, mg, ag));
-          diag[k] += T(vfc.entry(i, j, mg, ag));
-        }
-        out[k * 32] = off;
+        if constexpr (VJ) diag[k] += T(vfc.entry(i, j, mg, ag));
       }
     }
   }
@@ -493,11 +517,49 @@ __global__ void k_jacobi_inverse(int N, const T* __restrict__ dg, T* __restrict_
     for (int j = 0; j < 5; ++j) dst[(5 * i + j) * 32] = T(a[i][5 + j]);
 }
 
+// every slot's 25 entries (A(U, E, s) + c0 I minus the non-LF viscous part)
+template <typename TB>
+__global__ void k_expand_slots(DevMesh m, const TB* __restrict__ blk, double* __restrict__ out) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;  // slot * 32 + lane
+  if (i >= (long)m.nslots * 32) return;
+  const size_t slot = (size_t)(i / 32);
+  const int lane = (int)(i % 32);
+  SlotBlock<TB> Bk;
+  Bk.load(blk, slot, lane);
+  const int col = m.scol[i];
+  const bool vj = m.vjslot && col >= 0 && col < m.N;  // padding slots have no column
+  for (int k = 0; k < 25; ++k) {
+    double e = Bk.entry(m.gamma, k / 5, k % 5);
+    if (vj) e -= vj_entry<TB>(m, slot, lane, col, k / 5, k % 5);
+    out[(slot * 25 + k) * 32 + lane] = e;
+  }
+}
+
+void launch_expand_slots(Handle& h, double* out) {
+  const long n = (long)h.m.nslots * 32;
+  if (h.jacPrecision == ICS_PREC_MIXED)
+    k_expand_slots<float><<<grid_for(n, 128), 128, 0, h.stream>>>(h.m, (const float*)h.blk, out);
+  else
+    k_expand_slots<double><<<grid_for(n, 128), 128, 0, h.stream>>>(h.m, (const double*)h.blk, out);
+  ICS_CUDA(cudaGetLastError());
+}
+
 void launch_jacobian(Handle& h) {
   // viscous Jacobian: LF coefficient (vsf2) or the non-LF laplacians (vj)
   const bool visc = h.cfg.c.viscous != 0, lf = h.cfg.c.viscous_lf_jacobian != 0;
   const double* vsf2 = visc && lf ? h.vsf2 : nullptr;
   const double* vj = visc && !lf ? h.vjac : nullptr;
+  // the non-LF viscous parts of the off-diagonal blocks (blocks.cuh)
+  if (vj) {
+    if (!h.vjslotbuf) {  // FP64-sized: serves both precisions
+      ICS_CUDA(cudaMalloc(&h.vjslotbuf, (size_t)h.m.nslots * 2 * 32 * sizeof(double)));
+      ICS_CUDA(cudaMalloc(&h.vjcellbuf, 5ull * h.m.N * sizeof(double)));
+    }
+    h.m.vjslot = h.vjslotbuf;
+    h.m.vjcell = h.vjcellbuf;
+  } else {
+    h.m.vjslot = h.m.vjcell = nullptr;
+  }
   if (h.m.B > 0)
     ICS_LAUNCH(h, ICS_K_JAC_BOUNDARY, k_jac_boundary<<<grid_for(h.m.B, 128), 128, 0, h.stream>>>(h.m, h.cfg.c.R, h.cfg.Cv, h.cfg.gamma, h.W, h.prim,
                                                                 h.pB, h.TB, h.UB, h.phiB, h.flam, h.bjac, vj));

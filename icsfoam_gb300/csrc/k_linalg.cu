@@ -16,6 +16,7 @@
 //             the L1 residuals for the stop test (coupledMatrixSolver.C:198-221).
 #include <cmath>
 
+#include "blocks.cuh"
 #include "ics_internal.cuh"
 
 namespace ics {
@@ -135,20 +136,19 @@ __global__ void __launch_bounds__(128) k_spmv(DevMesh m, const TB* __restrict__ 
   }
   const int base = m.slot_base[s];
   const int ns = m.nslot[c];
+  const TV g = TV(m.gamma);
 #pragma unroll 1
   for (int t = 0; t < ns; ++t) {
     const int col = m.scol[(base + t) * 32 + lane];
-    TV xj[5];
+    TV xj[5], y[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) xj[k] = x[5 * col + k];
-    const TB* Bk = blk + (size_t)(base + t) * 25 * 32 + lane;
+    SlotBlock<TB> Bk;
+    Bk.load(blk, base + t, lane);
+    Bk.mv(g, xj, y);
+    if (m.vjslot) vj_sub<TB>(m, base + t, lane, col, xj, y);
 #pragma unroll
-    for (int i = 0; i < 5; ++i) {
-      TV a = TV(0);
-#pragma unroll
-      for (int j = 0; j < 5; ++j) a += TV(Bk[(5 * i + j) * 32]) * xj[j];
-      acc[i] += a;
-    }
+    for (int i = 0; i < 5; ++i) acc[i] += y[i];
   }
   if (m.nInst > 1) {
     // Harmonic Balance coupling blocks V D_JK I with the other instances
@@ -246,20 +246,19 @@ __global__ void __launch_bounds__(128, MINB) k_op_level0(DevMesh m, const TB* __
   }
   const int base = m.slot_base[s];
   const int ns = m.nslot[c];
+  const TV g = TV(m.gamma);
 #pragma unroll UNR
   for (int t = 0; t < ns; ++t) {
     const int col = m.scol[(base + t) * 32 + lane];
-    TV xj[5];
+    TV xj[5], y[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) xj[k] = ldx<SCALED>(x, 5 * (size_t)col + k, beta);
-    const TB* Bk = blk + (size_t)(base + t) * 25 * 32 + lane;
+    SlotBlock<TB> Bk;
+    Bk.load(blk, base + t, lane);
+    Bk.mv(g, xj, y);
+    if (m.vjslot) vj_sub<TB>(m, base + t, lane, col, xj, y);
 #pragma unroll
-    for (int r = 0; r < 5; ++r) {
-      TV a = TV(0);
-#pragma unroll
-      for (int j = 0; j < 5; ++j) a += TV(Bk[(5 * r + j) * 32]) * xj[j];
-      acc[r] += a;
-    }
+    for (int r = 0; r < 5; ++r) acc[r] += y[r];
   }
   if (m.nInst > 1) {
     const int J = c / m.Nc, cl = c - J * m.Nc;
@@ -306,28 +305,28 @@ __global__ void __launch_bounds__(128, MINB) k_op_level1(DevMesh m, const TB* __
   }
   const int base = m.slot_base[s];
   const int ns = m.nslot[c];  // all lower: these rows have no upper neighbours
+  const TV g = TV(m.gamma);
 #pragma unroll UNR
   for (int t = 0; t < ns; ++t) {
     const int col = m.scol[(base + t) * 32 + lane];
     const TV rj = TV(rD[col]);
-    TV xj[5], dj[5];
+    TV xj[5], dj[5], ya[5], yb[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
       xj[k] = ldx<SCALED>(x, 5 * (size_t)col + k, beta);
       dj[k] = rj * w[5 * col + k];
     }
-    const TB* Bk = blk + (size_t)(base + t) * 25 * 32 + lane;
+    SlotBlock<TB> Bk;
+    Bk.load(blk, base + t, lane);
+    Bk.mv2(g, xj, ya, dj, yb);
+    if (m.vjslot) {
+      vj_sub<TB>(m, base + t, lane, col, xj, ya);
+      vj_sub<TB>(m, base + t, lane, col, dj, yb);
+    }
 #pragma unroll
     for (int r = 0; r < 5; ++r) {
-      TV a = TV(0), b = TV(0);
-#pragma unroll
-      for (int j = 0; j < 5; ++j) {
-        const TV e = TV(Bk[(5 * r + j) * 32]);
-        a += e * xj[j];
-        b += e * dj[j];
-      }
-      acc[r] += a;
-      fw[r] += b;
+      acc[r] += ya[r];
+      fw[r] += yb[r];
     }
   }
   if (m.nInst > 1) {
@@ -358,21 +357,20 @@ __device__ __forceinline__ void lusgs_fwd_row(const DevMesh& m, const TB* __rest
   TV acc[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) acc[k] = r[5 * c + k];
+  const TV g = TV(m.gamma);
 #pragma unroll 1
   for (int t = 0; t < nl; ++t) {
     const int col = m.scol[(base + t) * 32 + lane];
     const TV rj = TV(rD[col]);
-    TV dj[5];
+    TV dj[5], y[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) dj[k] = rj * r[5 * col + k];
-    const TB* Bk = blk + (size_t)(base + t) * 25 * 32 + lane;
+    SlotBlock<TB> Bk;
+    Bk.load(blk, base + t, lane);
+    Bk.mv(g, dj, y);
+    if (m.vjslot) vj_sub<TB>(m, base + t, lane, col, dj, y);
 #pragma unroll
-    for (int i = 0; i < 5; ++i) {
-      TV a = TV(0);
-#pragma unroll
-      for (int j = 0; j < 5; ++j) a += TV(Bk[(5 * i + j) * 32]) * dj[j];
-      acc[i] -= a;
-    }
+    for (int i = 0; i < 5; ++i) acc[i] -= y[i];
   }
   if (SCALE) {
     const TV rc = TV(rD[c]);
@@ -395,20 +393,19 @@ __device__ __forceinline__ void lusgs_rev_row(const DevMesh& m, const TB* __rest
   for (int k = 0; k < 5; ++k) acc[k] = r[5 * c + k];
   // two slots in flight: their column loads and the dependent gathers overlap
   // (2% on the reverse sweep; the order of the updates is unchanged)
+  const TV g = TV(m.gamma);
 #pragma unroll 2
   for (int t = ns - 1; t >= nl; --t) {
     const int col = m.scol[(base + t) * 32 + lane];
-    TV dj[5];
+    TV dj[5], y[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) dj[k] = r[5 * col + k];
-    const TB* Bk = blk + (size_t)(base + t) * 25 * 32 + lane;
+    SlotBlock<TB> Bk;
+    Bk.load(blk, base + t, lane);
+    Bk.mv(g, dj, y);
+    if (m.vjslot) vj_sub<TB>(m, base + t, lane, col, dj, y);
 #pragma unroll
-    for (int i = 0; i < 5; ++i) {
-      TV a = TV(0);
-#pragma unroll
-      for (int j = 0; j < 5; ++j) a += TV(Bk[(5 * i + j) * 32]) * dj[j];
-      acc[i] -= a;
-    }
+    for (int i = 0; i < 5; ++i) acc[i] -= y[i];
   }
   const TV rc = TV(rD[c]);
 #pragma unroll
@@ -538,19 +535,18 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_lusgs_sweep(DevMesh m, const 
   // blocks, their rD) is loaded before the first poll
   constexpr int PF = 3;
   int colp[PF];
-  TB bp[PF][25];
+  SlotBlock<TB> bp[PF];
   TV rdp[PF];
 #pragma unroll
   for (int p = 0; p < PF; ++p) {
     if (p < nn) {
       const int t = slot(p);
       colp[p] = m.scol[(sb + t) * 32 + lane];
-      const TB* Bk = blk + (size_t)(sb + t) * 25 * 32 + lane;
-#pragma unroll
-      for (int q = 0; q < 25; ++q) bp[p][q] = Bk[q * 32];
+      bp[p].load(blk, sb + t, lane);
       rdp[p] = FWD ? TV(rD[colp[p]]) : TV(1);
     }
   }
+  const TV g = TV(m.gamma);
   TV acc[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) acc[k] = FWD ? __ldcg(in + 5 * c + k) : __ldcg(in + SWEEP_PAD * c + k);
@@ -586,16 +582,13 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_lusgs_sweep(DevMesh m, const 
 #pragma unroll
   for (int p = 0; p < PF; ++p) {
     if (p < nn) {
-      TV dj[5];
+      TV dj[5], y[5];
 #pragma unroll
       for (int k = 0; k < 5; ++k) dj[k] = rdp[p] * rv[p][k];
+      bp[p].mv(g, dj, y);
+      if (m.vjslot) vj_sub<TB>(m, sb + slot(p), lane, colp[p], dj, y);
 #pragma unroll
-      for (int a = 0; a < 5; ++a) {
-        TV v = TV(0);
-#pragma unroll
-        for (int b2 = 0; b2 < 5; ++b2) v += TV(bp[p][5 * a + b2]) * dj[b2];
-        acc[a] -= v;
-      }
+      for (int a = 0; a < 5; ++a) acc[a] -= y[a];
     }
   }
 #pragma unroll 1
@@ -619,17 +612,15 @@ __global__ void __launch_bounds__(SWEEP_THREADS) k_lusgs_sweep(DevMesh m, const 
       if (ns_ < 256) ns_ <<= 1;
     }
     const TV rj = FWD ? TV(rD[col]) : TV(1);
-    TV dj[5];
+    TV dj[5], y[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) dj[k] = rj * rj5[k];
-    const TB* Bk = blk + (size_t)(sb + t) * 25 * 32 + lane;
+    SlotBlock<TB> Bk;
+    Bk.load(blk, sb + t, lane);
+    Bk.mv(g, dj, y);
+    if (m.vjslot) vj_sub<TB>(m, sb + t, lane, col, dj, y);
 #pragma unroll
-    for (int a = 0; a < 5; ++a) {
-      TV v = TV(0);
-#pragma unroll
-      for (int b2 = 0; b2 < 5; ++b2) v += TV(Bk[(5 * a + b2) * 32]) * dj[b2];
-      acc[a] -= v;
-    }
+    for (int a = 0; a < 5; ++a) acc[a] -= y[a];
   }
   if (!FWD) {
     const TV rc = TV(rD[c]);
@@ -1026,23 +1017,25 @@ static bool fused_op_t(Handle& h, const TV* x, TV* w, TV* vout = nullptr) {
   int s0, n0, s1, n1;
   level(0, &c0, &s0, &n0);
   level(1, &c1, &s1, &n1);
-  // slot loops: no unrolling for the fused product (fewer live registers,
-  // measured 20% faster than the compiler's default), two for the plain one
+  // slot loops not unrolled; FP32: at least 8 blocks of 128 per SM (64
+  // registers), with the factored slots 4-7% faster per pass than two slots
+  // in flight or the compiler's register choice (72-80); FP64 would spill
+  constexpr int OPB = sizeof(TB) == 4 ? 8 : 1;
   const KrylovScalars* ks = h.ks;
   if (n0) {
     if (vout)
-      ICS_LAUNCH(h, ICS_K_OP0, k_op_level0<TB, TV, 1, 2, true><<<grid_for(n0, 128), 128, 0, h.stream>>>(
+      ICS_LAUNCH(h, ICS_K_OP0, k_op_level0<TB, TV, OPB, 1, true><<<grid_for(n0, 128), 128, 0, h.stream>>>(
                                    m, blk, dg, x, w, c0, s0, n0, ks, vout));
     else
-      ICS_LAUNCH(h, ICS_K_OP0, k_op_level0<TB, TV, 1, 2><<<grid_for(n0, 128), 128, 0, h.stream>>>(
+      ICS_LAUNCH(h, ICS_K_OP0, k_op_level0<TB, TV, OPB, 1><<<grid_for(n0, 128), 128, 0, h.stream>>>(
                                    m, blk, dg, x, w, c0, s0, n0, nullptr, nullptr));
   }
   if (n1) {
     if (vout)
-      ICS_LAUNCH(h, ICS_K_OP1, k_op_level1<TB, TV, 1, 1, true><<<grid_for(n1, 128), 128, 0, h.stream>>>(
+      ICS_LAUNCH(h, ICS_K_OP1, k_op_level1<TB, TV, OPB, 1, true><<<grid_for(n1, 128), 128, 0, h.stream>>>(
                                    m, blk, dg, rD, x, w, c1, s1, n1, ks, vout));
     else
-      ICS_LAUNCH(h, ICS_K_OP1, k_op_level1<TB, TV, 1, 1><<<grid_for(n1, 128), 128, 0, h.stream>>>(
+      ICS_LAUNCH(h, ICS_K_OP1, k_op_level1<TB, TV, OPB, 1><<<grid_for(n1, 128), 128, 0, h.stream>>>(
                                    m, blk, dg, rD, x, w, c1, s1, n1, nullptr, nullptr));
   }
   // reverse level 1 = forward level 0 rows
@@ -1210,16 +1203,18 @@ __global__ void __launch_bounds__(128) k_jacobi_sweep(DevMesh m, const TB* __res
   const int s = c >> 5, lane = c & 31;
   TV acc[5] = {TV(0), TV(0), TV(0), TV(0), TV(0)};
   const int base = m.slot_base[s];
+  const TV g = TV(m.gamma);
   for (int t = 0; t < m.nslot[c]; ++t) {
     const int col = m.scol[(base + t) * 32 + lane];
-    const TB* Bk = blk + (size_t)(base + t) * 25 * 32 + lane;
+    TV xj[5], y[5];
 #pragma unroll
-    for (int i = 0; i < 5; ++i) {
-      TV a = TV(0);
+    for (int k = 0; k < 5; ++k) xj[k] = xo[5 * col + k];
+    SlotBlock<TB> Bk;
+    Bk.load(blk, base + t, lane);
+    Bk.mv(g, xj, y);
+    if (m.vjslot) vj_sub<TB>(m, base + t, lane, col, xj, y);
 #pragma unroll
-      for (int j = 0; j < 5; ++j) a += TV(Bk[(5 * i + j) * 32]) * xo[5 * col + j];
-      acc[i] += a;
-    }
+    for (int i = 0; i < 5; ++i) acc[i] += y[i];
   }
   TV r[5];
 #pragma unroll
@@ -1337,7 +1332,9 @@ static int gmres_t(Handle& h, ResIO& p) {
     ICS_LAUNCH(h, ICS_K_VECTOR,
                k_resid<TV><<<inst_grid(h), RB, 0, st>>>(h.m.Nc, h.src, t, w, h.partials, h.counter, ks->res));
   };
-  const int key = h.cfg.c.preconditioner * 100000 + prec(h) * 1000 + m;
+  // the captured launches hold DevMesh by value: the non-LF viscous block
+  // parts (m.vjslot) are part of the key
+  const int key = (h.m.vjslot ? 10000000 : 0) + h.cfg.c.preconditioner * 100000 + prec(h) * 1000 + m;
   const bool useGraph = !h.prof;  // per-launch event timing needs direct launches
   if (useGraph && h.cycleKey != key) {
     drop_graphs(h);

@@ -26,6 +26,7 @@
 #include <cstdio>
 #include <mutex>
 
+#include "blocks.cuh"
 #include "ics_internal.cuh"
 
 // identical to the definition in ics_api.cu (one handle type for the ABI)
@@ -69,14 +70,15 @@ __global__ void __launch_bounds__(NOALLOC_THREADS)
     const int ns = m.nslot[c];
     for (int t = 0; t < ns; ++t) {
       const int col = m.scol[(base + t) * 32 + lane];
-      const TB* Bk = blk + (size_t)(base + t) * 25 * 32 + lane;
+      double xj[5], yo[5];
 #pragma unroll
-      for (int i = 0; i < 5; ++i) {
-        double a = 0.0;
+      for (int k = 0; k < 5; ++k) xj[k] = x[5 * col + k];
+      SlotBlock<TB> Bk;
+      Bk.load(blk, base + t, lane);
+      Bk.mv(m.gamma, xj, yo);
+      if (m.vjslot) vj_sub<TB>(m, base + t, lane, col, xj, yo);
 #pragma unroll
-        for (int j = 0; j < 5; ++j) a += double(Bk[(5 * i + j) * 32]) * x[5 * col + j];
-        y[i] += a;
-      }
+      for (int i = 0; i < 5; ++i) y[i] += yo[i];
     }
 #pragma unroll
     for (int k = 0; k < 5; ++k) {

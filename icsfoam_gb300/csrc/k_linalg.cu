@@ -82,6 +82,12 @@ __device__ __forceinline__ bool reduce_finish(double (&v)[NV], double* __restric
 
 constexpr int RB = 256;  // threads per reduction block
 
+// MGS steps stream 3 Krylov vectors of which two are L2-resident, so they are
+// bound by latency and the reduction tail rather than by HBM: 4 blocks per SM
+// (608 on 152 SMs) measured 11% faster than 8 per SM (sweep of 304-1216).
+constexpr int MGS_BLOCKS = 608;
+constexpr int MGS_CHUNKS = 2;
+
 // 16-byte vector of the Krylov element type
 template <typename TV>
 struct V16;
@@ -706,7 +712,7 @@ __device__ __forceinline__ void dev_hess(KrylovScalars* ks, int i, int m) {
 // post = 1: the finishing thread also starts the cycle (dev_beta0);
 // post = 2: it also performs the Hessenberg update of direction i.
 template <typename TV>
-__global__ void __launch_bounds__(RB) k_mgs(long n, TV* __restrict__ w, const TV* __restrict__ vprev,
+__global__ void __launch_bounds__(RB, 4) k_mgs(long n, TV* __restrict__ w, const TV* __restrict__ vprev,
                                             const double* __restrict__ hprev, const TV* __restrict__ vnext,
                                             const int* __restrict__ status, double* __restrict__ partials,
                                             unsigned int* __restrict__ counter, double* __restrict__ out,
@@ -722,8 +728,29 @@ __global__ void __launch_bounds__(RB) k_mgs(long n, TV* __restrict__ w, const TV
     const VT* o4 = reinterpret_cast<const VT*>(vnext);
     const long stride = (long)gridDim.x * blockDim.x;
     TV tacc = TV(0);
-#pragma unroll 4
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nv; i += stride) {
+    // MGS_CHUNKS 16-byte chunks per thread and iteration, every load issued
+    // before the first use: the compiler's unrolled loop kept one chunk in
+    // flight at 32 registers (ncu: long-scoreboard stalls, 50% warps active);
+    // two chunks at <= 64 registers measured 6% faster per step
+    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    for (; i + (MGS_CHUNKS - 1) * stride < nv; i += MGS_CHUNKS * stride) {
+      VT x[MGS_CHUNKS], pv[MGS_CHUNKS], ov[MGS_CHUNKS];
+#pragma unroll
+      for (int u = 0; u < MGS_CHUNKS; ++u) {
+        x[u] = w4[i + u * stride];
+        if (vprev) pv[u] = p4[i + u * stride];
+        if (vnext) ov[u] = o4[i + u * stride];
+      }
+#pragma unroll
+      for (int u = 0; u < MGS_CHUNKS; ++u) {
+        if (vprev) {
+          axpy16(x[u], h, pv[u]);
+          w4[i + u * stride] = x[u];
+        }
+        tacc += dot16(x[u], vnext ? ov[u] : x[u]);
+      }
+    }
+    for (; i < nv; i += stride) {
       VT x = w4[i];
       if (vprev) {
         axpy16(x, h, p4[i]);
@@ -1269,10 +1296,6 @@ static int smooth_t(Handle& h, ResIO& p) {
   return finite ? ICS_OK : ICS_ERR_NONFINITE;
 }
 
-// MGS steps stream 3 Krylov vectors of which two are L2-resident, so they are
-// bound by latency and the reduction tail rather than by HBM: 4 blocks per SM
-// (608 on 152 SMs) measured 11% faster than 8 per SM (sweep of 304-1216).
-constexpr int MGS_BLOCKS = 608;
 
 template <typename TB, typename TV>
 static int gmres_t(Handle& h, ResIO& p) {

@@ -766,12 +766,15 @@ int ics_set_config(ics_handle hh, const ics_config* cfg) {
 
   return guard(hh, [&](Handle& h) {
     const bool structural = cfg->precision != h.cfg.c.precision || cfg->n_directions != h.cfg.c.n_directions;
+    // the Jacobian storage depends on the precision (factored FP32 / full FP64 slots)
+    const bool precChange = cfg->precision != h.cfg.c.precision;
     h.cfg.c = *cfg;
     h.cfg.Cv = cfg->Cp - cfg->R;
     h.cfg.gamma = cfg->Cp / h.cfg.Cv;
     h.m.gamma = h.cfg.gamma;
     h.haveExact = false;
     if (structural) ensure_workspace(h);
+    if (precChange) h.haveMatrix = false;  // reassembled by the next iteration
     return ICS_OK;
   });
 }

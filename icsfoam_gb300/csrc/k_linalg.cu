@@ -461,8 +461,10 @@ __global__ void __launch_bounds__(1024) k_lusgs_block(DevMesh m, const TB* __res
 // row only ever waits for rows with smaller tickets, whose blocks started
 // earlier and are resident or done -- no deadlock.  The sweep writes its rows
 // into a padded output array (8 words per row, 32 B for FP32) that starts
-// filled with a sentinel (all bits set, a NaN that GPU arithmetic never
-// produces: its NaNs are the canonical 0x7fff.. ones), and a row's result
+// filled with a sentinel (all bits set: a NaN with the sign bit, which GPU
+// arithmetic does not produce from finite operands -- a result that matched
+// it, from a NaN already in the input, would make its dependents give up
+// at the bound and report, never hang), and a row's result
 // words are their own done flags: a row polls its neighbours' five words
 // with relaxed loads until none is the sentinel.  One L2 round trip per
 // poll brings both the readiness and the values, the writer needs no fence,

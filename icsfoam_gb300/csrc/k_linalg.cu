@@ -1048,7 +1048,8 @@ static bool fused_op_t(Handle& h, const TV* x, TV* w, TV* vout = nullptr) {
   level(1, &c1, &s1, &n1);
   // slot loops not unrolled; FP32: at least 8 blocks of 128 per SM (64
   // registers), with the factored slots 4-7% faster per pass than two slots
-  // in flight or the compiler's register choice (72-80); FP64 would spill
+  // in flight or the compiler's register choice (72-80), and 10 or 12 blocks
+  // (51 / 40 registers, the latter spilling) were not faster; FP64 would spill
   constexpr int OPB = sizeof(TB) == 4 ? 8 : 1;
   const KrylovScalars* ks = h.ks;
   if (n0) {

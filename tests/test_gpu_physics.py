@@ -214,3 +214,24 @@ def test_bounded_sweep_wait_reports_timeout(gpu_binding):
     h.pseudo_loop()
     h.pseudo_iteration()
     assert np.all(np.isfinite(h.get_state()["W"]))
+
+
+def test_precision_change_needs_a_new_jacobian(gpu_binding):
+    """The Jacobian's slot storage depends on the precision (25 FP64 entries,
+    8 factored FP32 words): switching precision drops the assembled matrix,
+    and the re-assembled FP32 one acts like the FP64 one."""
+    w = cases.bump_channel(16, 6, 3, ordering_mode="colour")
+    h = open_case(gpu_binding, w)
+    h.residual()
+    h.assemble_jacobian()
+    x = np.random.default_rng(3).standard_normal((w.mesh.n_cells, 5))
+    y64 = h.matrix_mul(x)
+    h.set_config(cases.make_config(gpu_binding, w.settings, precision=1))
+    with pytest.raises(abi.IcsError):
+        h.matrix_mul(x)
+    h.residual()
+    h.assemble_jacobian()
+    y32 = h.matrix_mul(x)
+    scale = np.abs(y64).max(axis=0)
+    scale[1:4] = scale[1:4].max()
+    assert (np.abs(y32 - y64) / scale).max() < 1e-5

@@ -727,6 +727,7 @@ int ics_create(const ics_mesh_desc* mesh, const ics_config* cfg, ics_handle* out
   h.cfg.gamma = cfg->Cp / h.cfg.Cv;
   h.m.gamma = h.cfg.gamma;
   st = guard(hh, [&](Handle& hd) {
+    ICS_CUDA(cudaGetDevice(&hd.device));
     ICS_CUDA(cudaStreamCreateWithFlags(&hd.stream, cudaStreamNonBlocking));
     build_mesh(hd, mesh);
     alloc_state(hd);
@@ -766,15 +767,18 @@ int ics_set_config(ics_handle hh, const ics_config* cfg) {
 
   return guard(hh, [&](Handle& h) {
     const bool structural = cfg->precision != h.cfg.c.precision || cfg->n_directions != h.cfg.c.n_directions;
-    // the Jacobian storage depends on the precision (factored FP32 / full FP64 slots)
+    // the Jacobian storage depends on the precision (factored FP32 / full FP64 slots),
+    // and the factored FP32 slots apply gamma when they are used, so a new gamma
+    // would meet diagonal blocks assembled under the old one
     const bool precChange = cfg->precision != h.cfg.c.precision;
+    const bool gammaChange = cfg->Cp != h.cfg.c.Cp || cfg->R != h.cfg.c.R;
     h.cfg.c = *cfg;
     h.cfg.Cv = cfg->Cp - cfg->R;
     h.cfg.gamma = cfg->Cp / h.cfg.Cv;
     h.m.gamma = h.cfg.gamma;
     h.haveExact = false;
     if (structural) ensure_workspace(h);
-    if (precChange) h.haveMatrix = false;  // reassembled by the next iteration
+    if (precChange || gammaChange) h.haveMatrix = false;  // reassembled by the next iteration
     return ICS_OK;
   });
 }

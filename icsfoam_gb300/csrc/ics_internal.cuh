@@ -157,6 +157,7 @@ struct Handle {
   DevMesh m;
   Cfg cfg;
   cudaStream_t stream = nullptr;
+  int device = 0;  // the CUDA device current at ics_create (owns the stream and every buffer)
   std::string err;
   // state
   double* W = nullptr;      // [N][5]

@@ -3,25 +3,31 @@
 // This is the allocation-free variant of the GMRES residual step (the
 // unpreconditioned residual and its L1 sums that gmres::solveDelta computes
 // after each restart cycle).  It exists for callers that must not call
-// cudaMalloc/cudaFree once they are running: code executing while a CUDA
-// graph is being captured (allocation is not capturable), real-time or
-// embedded drivers that forbid device allocation after start-up, and hosts
-// that own all device memory through their own pool (for example a CFD code
-// that hands us its buffers).  Such a caller passes device buffers for the
-// input x, the output r and the five L1 sums; the only scratch this kernel
-// needs (per-block partial sums and a completion counter) lives in the
-// file-scope device array below, which every GPU that loads this library
-// holds until the process exits.
+// cudaMalloc/cudaFree once they are running: real-time or embedded drivers
+// that forbid device allocation after start-up (an allocation can block on
+// the driver or fail under memory pressure in the middle of a time step), and
+// hosts that own all device memory through their own pool (for example a CFD
+// code that hands us its buffers and accounts for every byte on the device).
+// Such a caller passes device buffers for the input x, the output r and the
+// five L1 sums; the only scratch this kernel needs (per-block partial sums
+// and a completion counter) lives in the file-scope device array below,
+// which every GPU that loads this library holds until the process exits.
 //
 // Limits and caveats:
 //   * one 256-thread block per 256 cells and 5 partial sums per block, so
 //     the array caps the case at NOALLOC_MAX_CELLS = 2,097,152 cells (320 KiB
-//     of partials); larger handles are rejected with ICS_ERR_ARG.
+//     of partials); larger handles are rejected with ICS_ERR_ARG, and so are
+//     Harmonic Balance and cyclic handles (A here has neither coupling).
 //   * every call shares the array: calls that overlap on the GPU (two
 //     streams, two host threads) race on it.  Calls on one stream are safe;
 //     each call clears the counter before it launches.
+//   * the call runs on the handle's stream and on the handle's device (made
+//     current for the call, then restored) and synchronises that stream
+//     before it returns, so r and l1 are complete on return.  x must be
+//     complete before the call: a caller that wrote it on another stream
+//     synchronises that stream (or the device) first.
 //   * the first call on a device resolves the array's device address with
-//     cudaGetSymbolAddress; make that first call before any stream capture.
+//     cudaGetSymbolAddress, with that device current.
 #include <cmath>
 #include <cstdio>
 #include <mutex>
@@ -147,12 +153,25 @@ extern "C" int ics_linear_residual_noalloc(ics_handle hh, const double* x, doubl
     h.err = buf;
     return ICS_ERR_ARG;
   }
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= 256) {
-    h.err = "linear_residual_noalloc: no current CUDA device";
+  const int dev = h.device;
+  if (dev < 0 || dev >= 256) {
+    h.err = "linear_residual_noalloc: device index out of range";
     return ICS_ERR_CUDA;
   }
+  // the handle's stream and buffers belong to h.device: make it current for the call
+  int prevDev = -1;
+  cudaError_t e = cudaGetDevice(&prevDev);
+  if (e == cudaSuccess && prevDev != dev) e = cudaSetDevice(dev);
+  if (e != cudaSuccess) {
+    h.err = std::string("linear_residual_noalloc: ") + cudaGetErrorString(e);
+    return ICS_ERR_CUDA;
+  }
+  struct Restore {
+    int prev, dev;
+    ~Restore() {
+      if (prev >= 0 && prev != dev) cudaSetDevice(prev);
+    }
+  } restore{prevDev, dev};
   double* scratch = nullptr;
   {
     // set-up once per device, with that device current

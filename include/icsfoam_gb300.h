@@ -388,16 +388,20 @@ int ics_timer_stop(ics_handle h, double* ms);
 /* ---- allocation-free entry point (no counterpart in the reference) ------ */
 /* r = b - A x and the five per-equation L1 sums of r, with A the handle's
  * assembled Jacobian and b its last residual source, for callers that must
- * not allocate device memory while running (code inside a CUDA graph
- * capture, real-time drivers that allocate only at start-up, hosts that own
- * every device buffer).  x, r ([n_cells][5]) and l1 ([5]) are caller-owned
- * DEVICE pointers; nothing is allocated or freed.  The only scratch is a
- * fixed file-scope device array sized for at most 2,097,152 cells: larger
- * handles return ICS_ERR_ARG, and so do Harmonic Balance handles (A here
- * has no instance coupling).  The first call on a device looks up that
- * array's address (cudaGetSymbolAddress), so make it before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race.
- * Runs on the handle's stream and synchronises it before returning.        */
+ * not allocate device memory while running: real-time drivers that allocate
+ * only at start-up (an allocation mid-run can stall on the driver or fail
+ * under memory pressure) and hosts that own every device buffer through
+ * their own pool.  x, r ([n_cells][5]) and l1 ([5]) are caller-owned DEVICE
+ * pointers; nothing is allocated or freed.  The only scratch is a fixed
+ * file-scope device array sized for at most 2,097,152 cells: larger handles
+ * return ICS_ERR_ARG, and so do Harmonic Balance and cyclic handles (A here
+ * has neither coupling).  All calls share that array: calls that overlap on
+ * the GPU race; calls on one stream are safe.  The call runs on the handle's
+ * stream, with the handle's device made current for its duration, and
+ * synchronises that stream before returning, so r and l1 are complete on
+ * return; x must already be complete (a caller that wrote it on another
+ * stream synchronises that stream first).  The first call on a device looks
+ * up the array's address (cudaGetSymbolAddress) with that device current.   */
 int ics_linear_residual_noalloc(ics_handle h, const double* x, double* r, double* l1);
 
 #ifdef __cplusplus

@@ -235,3 +235,22 @@ def test_precision_change_needs_a_new_jacobian(gpu_binding):
     scale = np.abs(y64).max(axis=0)
     scale[1:4] = scale[1:4].max()
     assert (np.abs(y32 - y64) / scale).max() < 1e-5
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_gamma_change_needs_a_new_jacobian(gpu_binding, precision):
+    """The factored FP32 slots apply gamma when they are used: a new Cp or R
+    would mix it with diagonal blocks assembled under the old one, so a change
+    of either drops the assembled matrix (in both precisions)."""
+    w = cases.bump_channel(16, 6, 3, ordering_mode="colour")
+    h = open_case(gpu_binding, w, precision=precision)
+    h.residual()
+    h.assemble_jacobian()
+    x = np.random.default_rng(4).standard_normal((w.mesh.n_cells, 5))
+    h.matrix_mul(x)
+    h.set_config(cases.make_config(gpu_binding, w.settings, precision=precision, Cp=1040.0))
+    with pytest.raises(abi.IcsError):
+        h.matrix_mul(x)
+    h.residual()
+    h.assemble_jacobian()
+    assert np.all(np.isfinite(h.matrix_mul(x)))

@@ -87,6 +87,7 @@ class Config(C.Structure):
         ("rho_min", C.c_double), ("T_min", C.c_double), ("T_max", C.c_double),
         ("n_sweeps", C.c_int32),
         ("viscous_lf_jacobian", C.c_int32),
+        ("limiter_coeff", C.c_double),
     ]
 
 

@@ -168,6 +168,33 @@ __device__ __forceinline__ void flux_hllc(const FStateT<Real>& L, const FStateT<
   const double coefSm = pos0d(Sm);
   const double coefSlm = (1.0 - coefSl) * coefSm;
   const double coefSmr = (1.0 - coefSm) * (1.0 - coefSr);
+  if ((coefSl != 0.0) + (coefSlm != 0.0) + (coefSmr != 0.0) + (coefSr != 0.0) == 1) {
+    // The usual case: exactly one wave region has a non-zero switch, and the
+    // switched sum below reduces to that region's flux (x + 0 = x, 1 x = x),
+    // so only that flux is evaluated: the plain flux of one side (Sl >= 0 or
+    // Sr < 0) or one side's star flux.  The two states are selected, not
+    // blended, so this costs no FP64 work.
+    const bool left = coefSl != 0.0 || coefSlm != 0.0;
+    const FStateT<Real>& X = left ? L : R;
+    const Real uX = left ? uMag_l : uMag_r;
+    if (coefSl != 0.0 || coefSr != 0.0) {
+      out[0] = X.rho * uX * magS;
+      for (int k = 0; k < 3; ++k) out[1 + k] = (X.rho * uX * X.U[k] + X.p * n[k]) * magS;
+      out[4] = X.rho * X.H * uX * magS;
+      return;
+    }
+    const Real SX = left ? Sl : Sr;
+    const Real iX = 1.0 / (SX - Sm);
+    out[0] = Sm * iX * ((SX - uX) * X.rho) * magS;
+    const Real pStar = X.rho * (uX - SX) * (uX - Sm) + X.p;
+    for (int k = 0; k < 3; ++k) {
+      const Real rus = iX * ((SX - uX) * X.rho * X.U[k] + (pStar - X.p) * n[k]);
+      out[1 + k] = (Sm * rus + pStar * n[k]) * magS;
+    }
+    const Real rhoEStar = iX * ((SX - uX) * (X.rho * X.E) - X.p * uX + pStar * Sm);
+    out[4] = (Sm * (rhoEStar + pStar) + pStar * um) * magS;
+    return;
+  }
   // one reciprocal per wave pair, shared by the mass, momentum and energy star fluxes
   const Real il = 1.0 / (Sl - Sm), ir = 1.0 / (Sr - Sm);
   const Real fluxRhoStar_l = Sm * il * ((Sl - uMag_l) * rl);

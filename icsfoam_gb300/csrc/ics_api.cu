@@ -150,6 +150,10 @@ int validate_config(const ics_config* c, std::string& err) {
     err = "viscous_lf_jacobian must be 0 or 1";
     return ICS_ERR_ARG;
   }
+  if (!(c->limiter_coeff > 0.0 && c->limiter_coeff <= 1.0)) {
+    err = "cellLimited coefficient k must be in (0, 1]";
+    return ICS_ERR_ARG;
+  }
   const int rs[3] = {c->recon_rho, c->recon_U, c->recon_T};
   for (int r : rs)
     if (r < 0 || r > 4) {
@@ -705,6 +709,7 @@ void ics_default_config(ics_config* c) {
   c->T_max = GREAT;
   c->n_sweeps = 1;
   c->viscous_lf_jacobian = 1;
+  c->limiter_coeff = 1.0;
 }
 
 int ics_create(const ics_mesh_desc* mesh, const ics_config* cfg, ics_handle* out) {
@@ -726,6 +731,7 @@ int ics_create(const ics_mesh_desc* mesh, const ics_config* cfg, ics_handle* out
   h.cfg.Cv = cfg->Cp - cfg->R;
   h.cfg.gamma = cfg->Cp / h.cfg.Cv;
   h.m.gamma = h.cfg.gamma;
+  h.m.limWiden = 1.0 / cfg->limiter_coeff - 1.0;
   st = guard(hh, [&](Handle& hd) {
     ICS_CUDA(cudaGetDevice(&hd.device));
     ICS_CUDA(cudaStreamCreateWithFlags(&hd.stream, cudaStreamNonBlocking));
@@ -776,6 +782,7 @@ int ics_set_config(ics_handle hh, const ics_config* cfg) {
     h.cfg.Cv = cfg->Cp - cfg->R;
     h.cfg.gamma = cfg->Cp / h.cfg.Cv;
     h.m.gamma = h.cfg.gamma;
+    h.m.limWiden = 1.0 / cfg->limiter_coeff - 1.0;
     h.haveExact = false;
     if (structural) ensure_workspace(h);
     if (precChange || gammaChange) h.haveMatrix = false;  // reassembled by the next iteration

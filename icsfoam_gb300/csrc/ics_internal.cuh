@@ -137,6 +137,8 @@ struct DevMesh {
   // ratio of specific heats (the phase-lagged sound speed, the factored
   // off-diagonal blocks)
   double gamma = 1.4;
+  // cellLimited coefficient k as the widening factor 1/k - 1 of the bounds
+  double limWiden = 0.0;
   // non-LF viscous parts of the off-diagonal blocks (blocks.cuh), block
   // storage type; nullptr unless that Jacobian mode is assembled
   const void* vjslot = nullptr;

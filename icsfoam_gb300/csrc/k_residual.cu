@@ -21,25 +21,9 @@
 // cellLimited<Venkatakrishnan|minmod> Gauss linear gradients.
 #include <type_traits>
 
-#include "flux.cuh"
-#include "ics_internal.cuh"
+#include "residual.cuh"
 
 namespace ics {
-
-template <typename Real>
-constexpr bool is_fp64 = std::is_same<Real, double>::value;
-
-struct ResParams {
-  double R, Cv, gamma, cstarFac;
-  int scheme, reconRho, reconU, reconT, lowMach;
-  double entropyFix;
-};
-
-__device__ __forceinline__ int recon_of(const ResParams& P, int q) {
-  if (q == Q_RHO || q == Q_P) return P.reconRho;
-  if (q == Q_UX || q == Q_UY || q == Q_UZ) return P.reconU;
-  return P.reconT;
-}
 
 // ------------------------------------------------------------------ fields
 // Real = double: cells and boundary faces; Real = Dual: the cells' tangents
@@ -130,8 +114,8 @@ __global__ void __launch_bounds__(128) k_grad(DevMesh m, const Real* __restrict_
       g[k][1] = g[k][1] + S1 * sf;
       g[k][2] = g[k][2] + S2 * sf;
       if (LIMITED) {
-        qmax[k] = fmax(qmax[k], qo);
-        qmin[k] = fmin(qmin[k], qo);
+        qmax[k] = omax(qmax[k], qo);
+        qmin[k] = omin(qmin[k], qo);
       }
     }
   }
@@ -155,8 +139,8 @@ __global__ void __launch_bounds__(128) k_grad(DevMesh m, const Real* __restrict_
         g[k][1] = g[k][1] + S1 * sf;
         g[k][2] = g[k][2] + S2 * sf;
         if (LIMITED) {
-          qmax[k] = fmax(qmax[k], qn);
-          qmin[k] = fmin(qmin[k], qn);
+          qmax[k] = omax(qmax[k], qn);
+          qmin[k] = omin(qmin[k], qn);
         }
       }
       continue;
@@ -169,8 +153,8 @@ __global__ void __launch_bounds__(128) k_grad(DevMesh m, const Real* __restrict_
       g[k][1] = g[k][1] + S1 * v;
       g[k][2] = g[k][2] + S2 * v;
       if (LIMITED) {
-        qmax[k] = fmax(qmax[k], v);
-        qmin[k] = fmin(qmin[k], v);
+        qmax[k] = omax(qmax[k], Real(v));
+        qmin[k] = omin(qmin[k], Real(v));
       }
     }
   }
@@ -196,12 +180,18 @@ __global__ void __launch_bounds__(128) k_grad(DevMesh m, const Real* __restrict_
       eneg[k] = 0.0;
       qmax[k] -= qc[k];
       qmin[k] -= qc[k];
+      if (m.limWiden > 0.0) {  // cellLimited coefficient k < 1
+        const Real wd = m.limWiden * (qmax[k] - qmin[k]);
+        qmax[k] = qmax[k] + wd;
+        qmin[k] = qmin[k] - wd;
+      }
     }
+    // comparisons and extrema through the integer image of the doubles (okey)
     auto faceExtrap = [&](int k, const Real& ex) {
-      if (ex > SMALL)
-        epos[k] = fmax(epos[k], ex);
-      else if (ex < -SMALL)
-        eneg[k] = fmin(eneg[k], ex);
+      if (ogt(ex, SMALL))
+        epos[k] = omax(epos[k], ex);
+      else if (olt(ex, -SMALL))
+        eneg[k] = omin(eneg[k], ex);
       else
         small |= 1u << k;
     };
@@ -272,39 +262,6 @@ __global__ void __launch_bounds__(128) k_grad(DevMesh m, const Real* __restrict_
 }
 
 // ------------------------------------------------------------ face fluxes
-// reconstruct field k on face f for direction dir (+1 owner side, -1 neighbour side)
-template <typename Real>
-__device__ __forceinline__ Real reconstruct(const DevMesh& m, int scheme, int k, int f, int o, int nb, const Real& qo,
-                                            const Real& qn, const Real* __restrict__ grad, double dir) {
-  const int N = m.N, F = m.F;
-  const double wUp = dir > 0 ? 1.0 : 0.0;
-  if (scheme == ICS_RECON_UPWIND) return wUp * (qo - qn) + qn;
-  if (scheme == ICS_RECON_VANLEER || scheme == ICS_RECON_MINMOD) {
-    const int c = dir > 0 ? o : nb;
-    const double d0 = m.dCC[f], d1 = m.dCC[F + f], d2 = m.dCC[2 * F + f];
-    const Real gradf = qn - qo;
-    const Real gradcf = d0 * grad[(3 * k) * N + c] + d1 * grad[(3 * k + 1) * N + c] + d2 * grad[(3 * k + 2) * N + c];
-    Real r;
-    if (fabs(gradcf) >= 1000 * fabs(gradf))
-      r = 2 * 1000 * (gradcf >= 0 ? 1.0 : -1.0) * (gradf >= 0 ? 1.0 : -1.0) - 1.0;
-    else
-      r = 2 * (gradcf / gradf) - 1;
-    Real lim;
-    if (scheme == ICS_RECON_VANLEER)
-      lim = (r + fabs(r)) / (1 + fabs(r));
-    else
-      lim = fmax(fmin(fmin(r, 1.0), 2.0), 0.0);
-    const Real wgt = lim * m.w[f] + (1.0 - lim) * wUp;
-    return wgt * (qo - qn) + qn;
-  }
-  // MUSCL: upwind value + limited-gradient extrapolation
-  const int c = dir > 0 ? o : nb;
-  const double* d = dir > 0 ? m.dOwn : m.dNei;
-  const Real base = wUp * (qo - qn) + qn;
-  return base + (d[f] * grad[(3 * k) * N + c] + d[F + f] * grad[(3 * k + 1) * N + c] +
-                 d[2 * F + f] * grad[(3 * k + 2) * N + c]);
-}
-
 // MRF = true reads the frame face velocity (moving reference frames); the
 // default instance has it as the constant zero, so it costs nothing there
 template <typename Real = double, bool MRF = false>
@@ -663,7 +620,7 @@ __global__ void __launch_bounds__(128) k_cellres(DevMesh m, CellResParams D, con
 }
 
 // ------------------------------------------------------------------ launch
-static ResParams res_params(const Handle& h) {
+ResParams res_params(const Handle& h) {
   ResParams P;
   P.R = h.cfg.c.R;
   P.Cv = h.cfg.Cv;
@@ -685,7 +642,7 @@ void launch_fields(Handle& h) {
   ICS_CUDA(cudaGetLastError());
 }
 
-static unsigned grad_mask(const Handle& h, int* limited) {
+unsigned grad_mask(const Handle& h, int* limited) {
   unsigned mask = 0;
   int lim = 0;
   const int rs[3] = {h.cfg.c.recon_rho, h.cfg.c.recon_U, h.cfg.c.recon_T};

@@ -65,6 +65,22 @@ def reconstruction_scheme(entry: str, grad_entry: Optional[str]) -> int:
     raise ValueError("Unknown interpolation scheme %r" % kind)
 
 
+def cell_limited_coeff(grad_entry: Optional[str]) -> float:
+    """The coefficient k of ``cellLimited<limiter> Gauss linear k`` (OpenFOAM
+    cellLimitedGrad: k in [0, 1]; 1 when omitted).  k = 0 (no limiting) is
+    not provided."""
+    words = (grad_entry or "").split()
+    if len(words) >= 4 and words[1] == "Gauss":
+        k = float(words[3])
+    elif len(words) >= 2 and words[1] != "Gauss":
+        k = float(words[-1])
+    else:
+        k = 1.0
+    if not 0.0 < k <= 1.0:
+        raise ValueError("cellLimited coefficient must be in (0, 1], got %g" % k)
+    return k
+
+
 def config_from_dicts(binding: abi.Binding, fvSchemes: Dict, fvSolution: Dict, thermo: Optional[Dict] = None):
     """Build an ics_config from fvSchemes / fvSolution / thermophysical entries."""
     cfg = binding.default_config()
@@ -83,11 +99,18 @@ def config_from_dicts(binding: abi.Binding, fvSchemes: Dict, fvSolution: Dict, t
     cfg.ddt_scheme = _DDT[ddt[-1]]
     interp = fvSchemes.get("interpolationSchemes", {})
     grads = fvSchemes.get("gradSchemes", {})
+    coeffs = set()
     for field, attr in (("rho", "recon_rho"), ("U", "recon_U"), ("T", "recon_T")):
         entry = interp.get("reconstruct(%s)" % field, "upwind")
         gname = entry.split()[1] if len(entry.split()) > 1 else None
         gentry = grads.get(gname, grads.get("default")) if gname else None
         setattr(cfg, attr, reconstruction_scheme(entry, gentry))
+        if entry.split()[0] == "linearUpwind":
+            coeffs.add(cell_limited_coeff(gentry))
+    if len(coeffs) > 1:
+        raise ValueError("different cellLimited coefficients per reconstructed field are not provided: %s"
+                         % sorted(coeffs))
+    cfg.limiter_coeff = coeffs.pop() if coeffs else 1.0
     fs = fvSolution.get("flowSolver", {})
     sname = _strip_gpu(fs.get("solver", "GMRES"))
     if sname not in abi.SOLVER:

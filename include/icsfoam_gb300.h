@@ -156,6 +156,12 @@ typedef struct {
    * (|U|^2-E)/rho, plus the boundary terms of the physical patches
    * (viscousFluxScheme.C:120-215, 249-267).                               */
   int32_t viscous_lf_jacobian;
+  /* gradSchemes cellLimited<limiter> Gauss linear k: the coefficient k in
+   * (0, 1] of the cellLimited gradients of linearUpwind reconstruction.
+   * k < 1 widens each cell's bounds by (1/k - 1)(max - min) of its
+   * neighbourhood before the limiter (OpenFOAM cellLimitedGrad); 1 is the
+   * plain limiter.                                                          */
+  double limiter_coeff;
 } ics_config;
 
 /* residualsIO (residualsIO.H:54-315): L1 residuals normalised per equation. */

@@ -289,6 +289,16 @@ void cellLimitedGrad(const Case& c, const VolS& f, bool venkat, std::vector<V3>&
     maxV[i] -= f.in[i];
     minV[i] -= f.in[i];
   }
+  // the coefficient k of "cellLimited<..> Gauss linear k": for k < 1 the
+  // bounds widen by (1/k - 1)(max - min) (cellLimitedGrad::calcGrad)
+  if (c.cfg.limiter_coeff < 1.0) {
+    const double widen = 1.0 / c.cfg.limiter_coeff - 1.0;
+    for (int i = 0; i < c.N; ++i) {
+      const double d = widen * (maxV[i] - minV[i]);
+      maxV[i] += d;
+      minV[i] -= d;
+    }
+  }
   std::vector<double> lim(c.N, 1.0);
   auto limitFace = [&](double& l, double maxD, double minD, double extrap) {
     double r = 1;
@@ -2565,6 +2575,7 @@ void icsref_default_config(ics_config* c) {
   c->T_max = GREAT;
   c->n_sweeps = 1;
   c->viscous_lf_jacobian = 1;
+  c->limiter_coeff = 1.0;
 }
 
 int icsref_set_config(ics_handle h, const ics_config* cfg) {
@@ -2579,6 +2590,7 @@ int icsref_set_config(ics_handle h, const ics_config* cfg) {
     return ICS_ERR_SCHEME;
   }
   if (cfg->viscous_lf_jacobian != 0 && cfg->viscous_lf_jacobian != 1) return ICS_ERR_ARG;
+  if (!(cfg->limiter_coeff > 0.0 && cfg->limiter_coeff <= 1.0)) return ICS_ERR_ARG;
   if (cfg->n_directions < 1 || cfg->n_directions > 64) return ICS_ERR_ARG;
   if (h->nInst > 1 && (cfg->ddt_scheme != ICS_DDT_STEADY || cfg->solver != ICS_SOLVER_GMRES)) {
     h->err = "Harmonic Balance needs steadyState ddt and the GMRES solver";

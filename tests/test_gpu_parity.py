@@ -28,6 +28,8 @@ WORKLOADS = {
 
 EXTRA = {
     "bump_hllc_vanleer_natural": dict(recon_rho=1, recon_U=1, recon_T=1),
+    # cellLimited<Venkatakrishnan> Gauss linear 0.5
+    "bump_hllc_muscl_k05_natural": dict(limiter_coeff=0.5),
 }
 
 
@@ -79,7 +81,7 @@ def perturb(w, seed=3, amp=0.02):
     return w
 
 
-CASES = list(WORKLOADS) + ["bump_hllc_vanleer_natural"]
+CASES = list(WORKLOADS) + list(EXTRA)
 
 
 def make(name):

@@ -376,3 +376,39 @@ def test_dictionary_selection_and_errors(oracle_binding):
     bad2 = dict(fvSolution, flowSolver={"solver": "BiCG"})
     with pytest.raises(ValueError):
         schemes.config_from_dicts(oracle_binding, fvSchemes, bad2)
+    # the cellLimited coefficient k (gradSchemes "cellLimited<..> Gauss linear k")
+    assert cfg.limiter_coeff == 1.0
+    half = dict(fvSchemes, gradSchemes={"default": "cellLimited<Venkatakrishnan> Gauss linear 0.5"})
+    assert schemes.config_from_dicts(oracle_binding, half, fvSolution).limiter_coeff == 0.5
+    mixed_k = dict(fvSchemes, gradSchemes={"default": "cellLimited<Venkatakrishnan> Gauss linear 0.5",
+                                           "grad(U)": "cellLimited<Venkatakrishnan> Gauss linear 1"})
+    with pytest.raises(ValueError):
+        schemes.config_from_dicts(oracle_binding, mixed_k, fvSolution)
+    zero_k = dict(fvSchemes, gradSchemes={"default": "cellLimited<Venkatakrishnan> Gauss linear 0"})
+    with pytest.raises(ValueError):
+        schemes.config_from_dicts(oracle_binding, zero_k, fvSolution)
+
+
+def test_cell_limited_coefficient_widens_the_bounds(oracle_binding):
+    """cellLimited's coefficient k < 1 widens each cell's bounds by
+    (1/k - 1)(max - min) before the limiter: k = 1 is the default limiter,
+    and as k shrinks the limited gradients (so the residual) move towards the
+    unlimited Gauss gradients."""
+    w = cases.bump_channel(16, 6, 3, ordering_mode="colour")
+    rng = np.random.default_rng(5)
+    p = w.p * (1.0 + 0.05 * rng.standard_normal(w.mesh.n_cells))
+
+    def res(k, pp):
+        h = abi.CaseHandle(oracle_binding, w.mesh, cases.make_config(oracle_binding, w.settings, limiter_coeff=k))
+        h.set_primitive(pp, w.U, w.T)
+        return h.residual()
+
+    r1 = res(1.0, p)
+    h = abi.CaseHandle(oracle_binding, w.mesh, cases.make_config(oracle_binding, w.settings))
+    h.set_primitive(p, w.U, w.T)
+    rdef = h.residual()
+    assert np.array_equal(r1, rdef)
+    r5, r_small, r_tiny = res(0.5, p), res(1e-6, p), res(1e-9, p)
+    assert not np.allclose(r5, r1)
+    # k -> 0: the limiter tends to 1 wherever the neighbourhood is not flat
+    assert np.abs(r_small - r_tiny).max() < 1e-4 * np.abs(r_tiny).max()

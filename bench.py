@@ -49,9 +49,15 @@ def parse():
     ap.add_argument("--ny", type=int, default=64)
     ap.add_argument("--nz", type=int, default=64)
     ap.add_argument("--to-solution", type=int, default=1, help="also run to the 1e-8 drop")
-    ap.add_argument("--solution-cap-s", type=float, default=30.0)
+    ap.add_argument("--solution-cap-s", type=float, default=90.0,
+                    help="time cap of the mixed-precision leg to 1e-8 (the FP64 leg gets 2.5x)")
+    ap.add_argument("--plateau-cap-s", type=float, default=15.0,
+                    help="seconds of the configured Venkatakrishnan limiter (mixed) recording its plateau")
+    ap.add_argument("--viscous-solution", type=int, default=0,
+                    help="only run the 200^3 viscous box (8M cells) to 1e-8 in both precisions")
     ap.add_argument("--e2e-steps", type=int, default=10)
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0,
+                    help="timed seconds of the CPU baseline (at least one full-mesh iteration per core)")
     ap.add_argument("--profile", type=int, default=1, help="per-kernel CUDA events in the timed region")
     ap.add_argument("--extras", type=int, default=1,
                     help="also time the Harmonic Balance sweep, the batch of independent cases and the "
@@ -177,6 +183,27 @@ def kernel_bytes(kind, N, F, B, nslots, mixed, nlev):
     return None
 
 
+# What bounds each kernel class: the FP64 pipe (GB300 runs FP64 at ~1.3
+# TFLOP/s) or HBM.  The residual's face and gradient kernels and the
+# dual-number / reverse-mode derivative kernels are FP64-ALU bound in both
+# precisions; the Jacobian row assembly is FP64-ALU bound when it writes
+# FP64 blocks; the Krylov passes are HBM bound.
+FP64_BOUND = {"face", "grad", "bface", "tangent", "adjoint", "exact"}
+
+
+def kernel_bound(kind, mixed):
+    if kind in FP64_BOUND or (kind == "jac_rows" and not mixed):
+        return "fp64"
+    return "hbm"
+
+
+# FP64 flops of one unit of work (a face for "face", a cell for "grad"),
+# HLLC + MUSCL / cellLimited<Venkatakrishnan>: counted by ncu from the
+# executed DFMA (2 flops), DADD and DMUL instructions of one launch
+# (profiles/fp64_face_grad_bump_128x64x64.md), divided by the faces / cells
+FP64_FLOPS_PER_UNIT = {"face": 319.8, "grad": 1013.2}
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -210,6 +237,7 @@ def run_timed(w, prec, steps, warmup, dist, profile):
     b = gpu.binding()
     h = gpu.open_case(w.mesh, cases.make_config(b, w.settings, precision=prec))
     h.set_primitive(w.p, w.U, w.T)
+    fp64_rate = h.measure_fp64_rate()
     for _ in range(warmup):
         h.pseudo_loop()
         h.pseudo_iteration()
@@ -246,7 +274,7 @@ def run_timed(w, prec, steps, warmup, dist, profile):
         kern = h.profile_read()
         h.close()
     return {"ms": ms, "launches": launches, "kernels": kern, "clocks": ck,
-            "last_rho_l2": last.rho_l2_residual if last else None}
+            "last_rho_l2": last.rho_l2_residual if last else None, "fp64_rate": fp64_rate}
 
 
 def run_to_solution(w, prec, cap_s, target=1e-8, max_iters=20000, from_peak=False, **over):
@@ -279,7 +307,45 @@ def run_to_solution(w, prec, cap_s, target=1e-8, max_iters=20000, from_peak=Fals
     state = h.get_state()["W"]
     h.close()
     return {"iterations": it, "seconds": dt, "drop": drop, "min_drop": best, "reached": drop <= target,
-            "cell_iters_per_s": w.mesh.n_cells * it / dt, "history": hist[-5:]}, state
+            "cell_iters_per_s": w.mesh.n_cells * it / dt,
+            "history": hist[::max(1, len(hist) // 12)] + hist[-1:]}, state
+
+
+# Reference dictionary settings under which the pseudo-time iteration of the
+# workloads reaches a 1e-8 drop of the rho residual.  With the configured
+# cellLimited<Venkatakrishnan> gradients the reference algorithm (the oracle
+# as much as this GPU path) stalls: OpenFOAM's Venkatakrishnan limiter has no
+# smoothing parameter, is below 1 for every finite ratio, and the face that
+# sets a cell's limiter keeps switching, so the residual plateaus at a
+# 1e-7..1e-5 drop on the bump channel and ~1e-3 on the viscous box.  The
+# cellLimited<minmod> gradients (gradSchemes "cellLimited<minmod> Gauss
+# linear 1", same linearUpwind reconstruction) equal 1 wherever the ratio
+# is >= 1, so the limiter stops switching and both precisions converge.
+SOLUTION_SETTINGS = {"recon_rho": 4, "recon_U": 4, "recon_T": 4}
+SOLUTION_SCHEME = "linearUpwind + cellLimited<minmod> Gauss linear 1"
+
+
+def run_solution_pair(w, cap_s, settings, plateau_cap_s=0.0, from_peak=False):
+    """Mixed precision and FP64 to a 1e-8 drop under `settings`: iterations,
+    seconds, sustained cell-iters/s, and the converged fields' difference;
+    with plateau_cap_s > 0 also the configured reconstruction (mixed) for that
+    long, to record where it stalls."""
+    import numpy as np
+
+    def rel(a, b):
+        scale = np.abs(b).max(axis=0)
+        scale[1:4] = scale[1:4].max()
+        return float((np.abs(a - b) / scale).max())
+
+    sm, Wm = run_to_solution(w, 1, cap_s, from_peak=from_peak, **settings)
+    sd, Wd = run_to_solution(w, 0, 2.5 * cap_s, from_peak=from_peak, **settings)
+    out = {"scheme": SOLUTION_SCHEME, "mixed": sm, "fp64": sd,
+           "mixed_speedup_to_1e-8": (sd["seconds"] / sm["seconds"]) if sm["reached"] and sd["reached"] else None,
+           "converged_field_max_rel_diff": rel(Wm, Wd)}
+    if plateau_cap_s > 0:
+        pm, _ = run_to_solution(w, 1, plateau_cap_s, from_peak=from_peak)
+        out["configured_venkatakrishnan_mixed"] = pm
+    return out
 
 
 def run_e2e(w, steps, warmup):
@@ -479,13 +545,13 @@ def run_diff(nx=120, ny=64, nz=64, reps=5):
 
 
 def _oracle_worker(args):
-    """One oracle process: its own 64x16x16 sample, warm-up, barrier, timed iterations."""
-    steps, warmup, seconds, barrier, seed = args
+    """One oracle process on its own copy of the mesh: warm-up, barrier, timed iterations."""
+    dims, steps, warmup, seconds, barrier = args
     sys.path.insert(0, ROOT)
     import oracle
     from icsfoam_gb300 import cases
 
-    w = cases.bump_channel(64, 16, 16, ordering_mode="colour")
+    w = cases.bump_channel(*dims, ordering_mode="colour")
     h = oracle.open_case(w.mesh, cases.make_config(oracle.binding(), w.settings))
     h.set_primitive(w.p, w.U, w.T)
     for _ in range(warmup):
@@ -503,11 +569,14 @@ def _oracle_worker(args):
     return w.mesh.n_cells * it, time.perf_counter() - t0, it
 
 
-def oracle_throughput(steps=0, warmup=1, seconds=0.0, procs=None):
-    """The oracle (reference algorithm, FP64) on every host core: one independent
-    64x16x16 sample per process, started together; cell-iters/s = all cells x
-    iterations / the slowest process's time (the reference's own parallel runs
-    would split one mesh with halo exchanges, so this is an upper bound)."""
+def oracle_throughput(dims, steps=0, warmup=1, seconds=0.0, procs=None):
+    """The oracle (the reference algorithm, FP64, single-threaded as each MPI
+    rank of the reference is) on every host core, each process iterating its
+    own copy of the whole mesh, started together: cell-iters/s = all cells x
+    iterations / the slowest process's time.  The reference's own parallel
+    run would split the mesh into as many subdomains with halo exchanges and
+    allreduces (and block-Jacobi LU-SGS across them), so this aggregate is an
+    upper bound of what the host cores deliver on the workload."""
     import multiprocessing as mp
 
     procs = procs or os.cpu_count() or 1
@@ -515,35 +584,42 @@ def oracle_throughput(steps=0, warmup=1, seconds=0.0, procs=None):
     mgr = ctx.Manager()
     barrier = mgr.Barrier(procs)
     with ctx.Pool(procs) as pool:
-        res = pool.map(_oracle_worker, [(steps, warmup, seconds, barrier, k) for k in range(procs)])
+        res = pool.map(_oracle_worker, [(dims, steps, warmup, seconds, barrier) for _ in range(procs)])
     work = sum(r[0] for r in res)
     dt = max(r[1] for r in res)
     its = min(r[2] for r in res)
     return work / dt, dt, procs, its
 
 
-def cpu_sample(seconds, warm=1):
+def _reference_sample(dims, procs, its, warm):
+    return ("bump channel %dx%dx%d (the timed workload itself), one copy per host core (%d processes, "
+            "single-threaded each) of >= %d pseudo iterations after %d warm-up; HLLC MUSCL/Venkatakrishnan, "
+            "GMRES(8)+LU-SGS, FP64 oracle; aggregate of independent full-mesh runs = an upper bound of a "
+            "%d-subdomain decomposed run" % (dims + (procs, its, warm, procs)))
+
+
+def cpu_sample(dims, seconds, warm=1):
     """The oracle on all host cores for about ``seconds`` (bounded sample)."""
-    v, dt, procs, its = oracle_throughput(seconds=seconds, warmup=warm)
+    v, dt, procs, its = oracle_throughput(dims, seconds=seconds, warmup=warm)
     return {"value": v, "unit": UNIT, "cores": procs, "kind": "port",
-            "sample": "bump channel 64x16x16 (16,384 cells) per process, same schemes/settings, %d processes "
-                      "(one per host core) of >= %d pseudo iterations after %d warm-up, FP64 oracle"
-                      % (procs, its, warm)}
+            "sample": _reference_sample(dims, procs, its, warm)}
 
 
 def reference_arm(args, dist):
     if dist.rank != 0:
         return
-    v, dt, procs, its = oracle_throughput(steps=args.steps, warmup=args.warmup)
-    sample = ("bump channel 64x16x16 (16,384 cells) standing in for 256x64x64, one independent sample per host "
-              "core (%d processes); HLLC MUSCL/Venkatakrishnan, GMRES(8)+LU-SGS; FP64 oracle" % procs)
+    dims = (args.nx, args.ny, args.nz)
+    v, dt, procs, its = oracle_throughput(dims, steps=args.steps, warmup=args.warmup)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic",
-            "config": {"workload": "bump_channel_64x16x16_sample_of_256x64x64", "cells_per_process": 16384,
-                       "processes": procs},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": procs, "kind": "port", "sample": sample},
+            "data": "synthetic (generated bump-channel mesh, uniform M=0.675 initial state)",
+            "config": {"workload": "bump_channel_%dx%dx%d" % dims, "cells": args.nx * args.ny * args.nz,
+                       "processes": procs, "flux": "HLLC",
+                       "reconstruction": "MUSCL + cellLimited<Venkatakrishnan>", "solver": "GMRES(8)+LU-SGS",
+                       "ordering": "colour-blocked"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": procs, "kind": "port",
+                             "sample": _reference_sample(dims, procs, its, args.warmup)},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -559,6 +635,13 @@ def main():
         os.environ["CUDA_VISIBLE_DEVICES"] = str(dist.local)
     from icsfoam_gb300 import cases
 
+    if args.viscous_solution:
+        # the randomised viscous box at its configured size and numbering (RCM)
+        w = cases.random_box(200)
+        res = run_solution_pair(w, args.solution_cap_s, SOLUTION_SETTINGS, from_peak=True)
+        print(json.dumps({"workload": w.name, "cells": w.mesh.n_cells, "ordering": "rcm", **res}), flush=True)
+        dist.close()
+        return
     t0 = time.time()
     w = cases.bump_channel(args.nx, args.ny, args.nz, ordering_mode="colour")
     mesh_s = time.time() - t0
@@ -569,31 +652,8 @@ def main():
     value64 = N * args.steps * dist.world / (fp64["ms"] / 1000.0)
     extra = {}
     if dist.rank == 0 and args.to_solution:
-        import numpy as np
-
-        from icsfoam_gb300 import cases as _cases
-
-        def rel(a, b):
-            scale = np.abs(b).max(axis=0)
-            scale[1:4] = scale[1:4].max()
-            return float((np.abs(a - b) / scale).max())
-
-        sm, Wm = run_to_solution(w, 1, args.solution_cap_s)
-        sd, Wd = run_to_solution(w, 0, args.solution_cap_s)
-        # first-order reconstruction converges without limiter chatter: time to
-        # the 1e-8 drop in both precisions and the converged fields' difference
-        wf = _cases.bump_channel(128, 32, 32, ordering_mode="colour", second_order=False)
-        fm, Wfm = run_to_solution(wf, 1, 2 * args.solution_cap_s)
-        fd, Wfd = run_to_solution(wf, 0, 2 * args.solution_cap_s)
-        extra["to_solution"] = {
-            "mixed": sm, "fp64": sd,
-            "mixed_vs_fp64_field_max_rel_diff_at_cap": rel(Wm, Wd),
-            "note": "second-order MUSCL with OpenFOAM's cellLimited<Venkatakrishnan> (no smoothing) stalls "
-                    "at a 1e-6..1e-5 drop on this case (limiter chatter); min_drop records the plateau",
-            "first_order_bump_128x32x32": {
-                "mixed": fm, "fp64": fd,
-                "mixed_speedup_to_1e-8": fd["seconds"] / fm["seconds"] if fm["reached"] and fd["reached"] else None,
-                "converged_field_max_rel_diff": rel(Wfm, Wfd)}}
+        extra["to_solution"] = run_solution_pair(w, args.solution_cap_s, SOLUTION_SETTINGS,
+                                                 plateau_cap_s=args.plateau_cap_s)
     e2e = run_e2e(w, args.steps, args.warmup) if dist.rank == 0 else None
     if dist.rank == 0 and args.extras:
         extra["harmonic_balance"] = run_hb_sweep()
@@ -606,29 +666,54 @@ def main():
 
     nslots = None
     roof = None
+    fp64_roof = None
     kern_table = {}
     if mixed["kernels"]:
         peak, peak_kind = load_peaks()
         traffic = load_traffic()
+        fp64_peak = mixed["fp64_rate"]
         nlev = 2
         tot = sum(v[0] for v in mixed["kernels"].values())
         dom = max(mixed["kernels"].items(), key=lambda kv: kv[1][0])
         for k, (ms, n) in mixed["kernels"].items():
             if n:
                 kern_table[k] = {"ms_total": round(ms, 3), "launches": n, "share": round(ms / tot, 4),
-                                 "ms_per_launch": round(ms / n, 5)}
+                                 "ms_per_launch": round(ms / n, 5), "bound": kernel_bound(k, True)}
                 byts = kernel_bytes(k, N, F, B, nslots, True, nlev)
                 if byts:
                     kern_table[k]["GBps"] = round(byts / (ms / n / 1000.0) / 1e9, 1)
-        name, (ms, n) = dom
+                if k in FP64_FLOPS_PER_UNIT:
+                    units = F if k == "face" else N
+                    kern_table[k]["fp64_GFLOPs"] = round(FP64_FLOPS_PER_UNIT[k] * units / (ms / n / 1000.0) / 1e9, 1)
+        # the HBM roofline of the dominant HBM-bound kernel class; the
+        # FP64-bound classes get theirs against the measured FP64 FMA rate
+        hbm = [(k, v) for k, v in mixed["kernels"].items() if v[1] and kernel_bound(k, True) == "hbm"
+               and kernel_bytes(k, N, F, B, nslots, True, nlev)]
+        name, (ms, n) = max(hbm, key=lambda kv: kv[1][0])
         byts = kernel_bytes(name, N, F, B, nslots, True, nlev)
-        if byts:
-            ach = byts / (ms / n / 1000.0) / 1e9
-            tr = traffic.get((name, "mixed"))
-            roof = {"kernel": name, "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
-                    "frac": round(ach / peak, 4), "peak_source": peak_kind,
-                    "algorithmic_bytes_per_launch": int(byts),
-                    "traffic": (tr[1] * N / tr[0]) if tr else None}
+        ach = byts / (ms / n / 1000.0) / 1e9
+        tr = traffic.get((name, "mixed"))
+        roof = {"kernel": name, "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(ach / peak, 4), "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": int(byts),
+                "traffic": (tr[1] * N / tr[0]) if tr else None,
+                "share_of_step": round(ms / tot, 4),
+                "dominant_kernel_overall": {"kernel": dom[0], "bound": kernel_bound(dom[0], True),
+                                            "share_of_step": round(dom[1][0] / tot, 4)}}
+        fp64_roof = {}
+        for k in FP64_FLOPS_PER_UNIT:
+            if k in mixed["kernels"] and mixed["kernels"][k][1]:
+                ms_k, n_k = mixed["kernels"][k]
+                units = F if k == "face" else N
+                ach64 = FP64_FLOPS_PER_UNIT[k] * units / (ms_k / n_k / 1000.0) / 1e9
+                trk = traffic.get((k, "fp64"))
+                fp64_roof[k] = {"bound": "fp64", "achieved": round(ach64, 1), "peak": round(fp64_peak, 1),
+                                "unit": "GFLOP/s", "frac": round(ach64 / fp64_peak, 4) if fp64_peak else None,
+                                "peak_source": "measured FP64 FMA microkernel (ics_measure_fp64_rate)",
+                                "flops_per_launch": int(FP64_FLOPS_PER_UNIT[k] * units),
+                                "hbm_GBps": kern_table[k].get("GBps"),
+                                "traffic": (trk[1] * N / trk[0]) if trk else None,
+                                "share_of_step": round(ms_k / tot, 4)}
     fp64_table = {}
     if fp64["kernels"]:
         for k, (ms, n) in fp64["kernels"].items():
@@ -637,7 +722,7 @@ def main():
                 byts = kernel_bytes(k, N, F, B, nslots, False, 2)
                 if byts:
                     fp64_table[k]["GBps"] = round(byts / (ms / n / 1000.0) / 1e9, 1)
-    cpu = cpu_sample(args.cpu_seconds) if dist.rank == 0 else None
+    cpu = cpu_sample((args.nx, args.ny, args.nz), args.cpu_seconds) if dist.rank == 0 else None
     if dist.rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
@@ -652,7 +737,7 @@ def main():
             "fp64": {"value": value64, "unit": UNIT, "ms_per_step": fp64["ms"] / args.steps,
                      "kernels": fp64_table},
             "mixed_over_fp64": value / value64,
-            "kernels": kern_table, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "kernels": kern_table, "roofline": roof, "fp64_roofline": fp64_roof, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": mixed["launches"], "clocks": mixed["clocks"], "mesh_build_s": round(mesh_s, 1),
         }
         line.update(extra)

@@ -105,6 +105,16 @@ class IterStats(C.Structure):
                 ("bounded_cells", C.c_int32), ("status", C.c_int32)]
 
 
+class KrylovOpts(C.Structure):
+    _fields_ = [("n_directions", C.c_int32), ("max_cycles", C.c_int32), ("rel_tol", C.c_double),
+                ("precision", C.c_int32), ("preconditioner", C.c_int32), ("pseudo_time", C.c_int32)]
+
+
+class KrylovResult(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("cycles", C.c_int32), ("rel_residual", C.c_double),
+                ("converged", C.c_int32)]
+
+
 # exported functions: name -> (restype, argtypes)
 _P = C.c_void_p
 _FUNCS = {
@@ -146,6 +156,7 @@ _MEASURE = {
     "launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "timer_start": (C.c_int, [_P]),
     "timer_stop": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "measure_fp64_rate": (C.c_int, [_P, C.POINTER(C.c_double)]),
 }
 
 # allocation-free linear residual (CUDA library only; arguments are device pointers)
@@ -165,12 +176,16 @@ _MEASURE["load_checkpoint"] = (C.c_int, [_P, _P, C.c_int64])
 # differentiation of the residual (CUDA library only)
 _MEASURE["jvp"] = (C.c_int, [_P, _P, _P, C.c_int32])
 _MEASURE["vjp"] = (C.c_int, [_P, _P, _P, C.c_int32])
+_MEASURE["vjp_recompute"] = (C.c_int, [_P, _P, _P, C.c_int32])
+_MEASURE["adjoint_solve"] = (C.c_int, [_P, _P, _P, C.POINTER(KrylovOpts), C.POINTER(KrylovResult)])
+_MEASURE["tangent_solve"] = (C.c_int, [_P, _P, _P, C.POINTER(KrylovOpts), C.POINTER(KrylovResult)])
+_MEASURE["pressure_force"] = (C.c_int, [_P, C.c_int32, _P, C.POINTER(C.c_double), _P])
 _MEASURE["assemble_exact_jacobian"] = (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int32)])
 _MEASURE["get_exact_jacobian"] = (C.c_int, [_P, _P, _P, _P])
 
 KERNEL_CLASSES = ("fields", "grad", "face", "bface", "cellres", "jac_boundary", "jac_rows", "jacobi_inv", "spmv",
                   "lusgs_fwd", "lusgs_rev", "jacobi", "mgs", "vector", "scalar", "update", "bc", "bound", "visc",
-                  "tangent", "exact", "op0", "op1", "passive")
+                  "tangent", "exact", "op0", "op1", "passive", "adjoint")
 
 EXPORTED = tuple(_FUNCS) + tuple(_MEASURE)
 
@@ -471,6 +486,12 @@ class CaseHandle:
         self._check(self.b.fn["launch_count"](self.h, C.byref(n)), "launch_count")
         return int(n.value)
 
+    def measure_fp64_rate(self) -> float:
+        """Measured FP64 FMA rate of the handle's GPU in GFLOP/s."""
+        v = C.c_double()
+        self._check(self.b.fn["measure_fp64_rate"](self.h, C.byref(v)), "measure_fp64_rate")
+        return v.value
+
     def timer_start(self):
         self._check(self.b.fn["timer_start"](self.h), "timer_start")
 
@@ -532,6 +553,40 @@ class CaseHandle:
 
     def jvp_device(self, v_dev: int, out_dev: int):
         self._check(self.b.fn["jvp"](self.h, v_dev, out_dev, 1), "jvp")
+
+    def vjp_recompute(self, u: np.ndarray) -> np.ndarray:
+        """(d(R V)/dW)^T u by reverse mode (no stored Jacobian)."""
+        u = np.ascontiguousarray(u, np.float64).reshape(self.N, 5)
+        out = np.empty((self.N, 5))
+        self._check(self.b.fn["vjp_recompute"](self.h, _ptr(u), _ptr(out), 0), "vjp_recompute")
+        return out
+
+    def _krylov(self, fn, rhs, n_directions=30, max_cycles=20, rel_tol=1e-8, precision=0, preconditioner=1,
+                pseudo_time=0):
+        rhs = np.ascontiguousarray(rhs, np.float64).reshape(self.N, 5)
+        sol = np.empty((self.N, 5))
+        o = KrylovOpts(n_directions, max_cycles, rel_tol, precision, preconditioner, pseudo_time)
+        r = KrylovResult()
+        self._check(self.b.fn[fn](self.h, _ptr(rhs), _ptr(sol), C.byref(o), C.byref(r)), fn)
+        return sol, r
+
+    def adjoint_solve(self, g, **opts):
+        """Solve A^T psi = g, A = pseudo_time V/dtau - d(R V)/dW; returns (psi, KrylovResult)."""
+        return self._krylov("adjoint_solve", g, **opts)
+
+    def tangent_solve(self, b, **opts):
+        """Solve A x = b, A = pseudo_time V/dtau - d(R V)/dW (matrix-free Newton-Krylov);
+        returns (x, KrylovResult)."""
+        return self._krylov("tangent_solve", b, **opts)
+
+    def pressure_force(self, patch: int, direction=(1.0, 0.0, 0.0), gradient=True):
+        """(J, dJ/dW or None): the patch's integrated pressure force along direction."""
+        d = np.ascontiguousarray(direction, np.float64)
+        J = C.c_double()
+        g = np.empty((self.N, 5)) if gradient else None
+        self._check(self.b.fn["pressure_force"](self.h, int(patch), _ptr(d), C.byref(J), _ptr(g)),
+                    "pressure_force")
+        return J.value, g
 
     def vjp_device(self, u_dev: int, out_dev: int):
         self._check(self.b.fn["vjp"](self.h, u_dev, out_dev, 1), "vjp")

@@ -194,7 +194,8 @@ def swept_bump(nx: int = 240, ny: int = 128, nz: int = 128, thickness: float = 0
     inlet = M.Patch("inlet", M.PATCH_TOTAL_INLET, p0=p0, T0=T0)
     outlet = M.Patch("outlet", M.PATCH_PRESSURE_OUTLET, p=p_static)
     wall = M.Patch("walls", M.PATCH_SLIP, is_wall=True)
-    sides = {"xmin": inlet, "xmax": outlet, "ymin": wall, "ymax": wall, "zmin": wall, "zmax": wall}
+    bump = M.Patch("bump", M.PATCH_SLIP, is_wall=True)  # the lower wall carrying the swept bump
+    sides = {"xmin": inlet, "xmax": outlet, "ymin": bump, "ymax": wall, "zmin": wall, "zmax": wall}
     mesh = M.hex_mesh(g, sides)
     mesh = ordering.apply(mesh, ordering_mode)
     N = mesh.n_cells

@@ -101,6 +101,7 @@ void free_all(Handle& h) {
                   h.ddtCoeff, h.q, h.bq, h.clin, h.grad, h.fflux, h.frec, h.flam, h.bjac, h.src, h.vcell,
                   h.fvisc, h.vsf2, h.vjac, m.dc, m.Dhb, m.mrfU, m.mrfOm, m.mrfBU, m.mrfBIn, m.plagMode, m.plagP, m.bpartner, m.bw, m.bdelta, m.bdNei,
                   m.bnodc, m.cyc_face, m.cyc_row, m.cyc_ptr, h.cblk, h.vjslotbuf, h.vjcellbuf, h.cfrec, h.tW, h.tprim, h.tq, h.tgrad, h.tflux, h.tvc, h.tfv, h.tv,
+                  h.aF, h.aQ, h.aG, h.aSrc, h.aVal,
                   h.ss, h.ssB, h.srhoS, h.srhoS0, h.srhoS00, h.sgrad, h.sgradL, h.sface, h.sblk, h.sdg, h.srD,
                   h.ssrc, h.sFixed, h.sValue,
                   h.blk, h.dg,
@@ -1540,6 +1541,78 @@ int ics_vjp(ics_handle hh, const double* u, double* JTu, int32_t device) {
     stage_in(h, u, tu, device);
     exact_vjp(h, tu, out);
     stage_out(h, out, JTu, device);
+    return ICS_OK;
+  });
+}
+
+int ics_vjp_recompute(ics_handle hh, const double* u, double* JTu, int32_t device) {
+  if (!u || !JTu) return ICS_ERR_ARG;
+  return guard(hh, [&](Handle& h) {
+    const std::string why = residual_vjp_unsupported(h);
+    if (!why.empty()) {
+      h.err = why;
+      return ICS_ERR_ARG;
+    }
+    ensure_tangent(h);
+    Range rg("ics vjp_recompute");
+    double* tu = h.tv;
+    double* out = h.tv + 5ull * h.m.N;
+    stage_in(h, u, tu, device);
+    launch_residual_vjp(h, tu, out);
+    stage_out(h, out, JTu, device);
+    return ICS_OK;
+  });
+}
+
+namespace {
+// one matrix-free Krylov solve with host right-hand side and solution
+using KrylovSolve = int (*)(Handle&, const double*, double*, const ics_krylov_opts&, ics_krylov_result*);
+int krylov_entry(ics_handle hh, const double* rhs, double* sol, const ics_krylov_opts* opts,
+                 ics_krylov_result* result, KrylovSolve solve, const char* name) {
+  if (!rhs || !sol || !opts) return ICS_ERR_ARG;
+  return guard(hh, [&](Handle& h) {
+    ensure_tangent(h);
+    Range rg(name);
+    double* d = h.tv;
+    double* x = h.tv + 5ull * h.m.N;
+    stage_in(h, rhs, d, 0);
+    ics_krylov_result r{};
+    const int st = solve(h, d, x, *opts, &r);
+    if (result) *result = r;
+    stage_out(h, x, sol, 0);
+    return st;
+  });
+}
+}  // namespace
+
+int ics_adjoint_solve(ics_handle hh, const double* g, double* psi, const ics_krylov_opts* opts,
+                      ics_krylov_result* result) {
+  return krylov_entry(hh, g, psi, opts, result, adjoint_solve, "ics adjoint_solve");
+}
+
+int ics_tangent_solve(ics_handle hh, const double* b, double* x, const ics_krylov_opts* opts,
+                      ics_krylov_result* result) {
+  return krylov_entry(hh, b, x, opts, result, tangent_solve, "ics tangent_solve");
+}
+
+int ics_pressure_force(ics_handle hh, int32_t patch, const double dir[3], double* J, double* dJdW) {
+  if (!dir || !J) return ICS_ERR_ARG;
+  return guard(hh, [&](Handle& h) {
+    if (patch < 0 || patch >= h.m.npatches) {
+      h.err = "pressure_force: no such patch";
+      return ICS_ERR_ARG;
+    }
+    std::vector<Patch> ps(h.m.npatches);
+    ICS_CUDA(cudaMemcpy(ps.data(), h.m.patches, ps.size() * sizeof(Patch), cudaMemcpyDeviceToHost));
+    const int k = ps[patch].kind;
+    if (k != ICS_PATCH_SLIP && k != ICS_PATCH_ZERO_GRADIENT && k != ICS_PATCH_ISOTHERMAL_WALL) {
+      h.err = "pressure_force: the patch's pressure is not zeroGradient";
+      return ICS_ERR_ARG;
+    }
+    ensure_tangent(h);
+    double* d = dJdW ? h.tv : nullptr;
+    *J = pressure_force(h, patch, dir, d);
+    if (dJdW) stage_out(h, d, dJdW, 0);
     return ICS_OK;
   });
 }

@@ -239,6 +239,15 @@ struct Handle {
   void* tvc = nullptr;
   void* tfv = nullptr;
   double* tv = nullptr;   // [10N] direction and product staging
+  // reverse-mode residual derivative workspace (allocated on first use):
+  // adjoints of the reconstructed face states [16][F], of the cell fields
+  // [NQ][N] and unlimited gradients [3 NQ][N], and the limiter bounds'
+  // source cells and adjoints [2 NQ][N]
+  double* aF = nullptr;
+  double* aQ = nullptr;
+  double* aG = nullptr;
+  int* aSrc = nullptr;
+  double* aVal = nullptr;
   // exact Jacobian of the residual source: stencil CSR (two face hops plus
   // Harmonic Balance partners), transpose positions, colouring, blocks
   int* xptr = nullptr;
@@ -319,6 +328,16 @@ void launch_viscous(Handle& h);
 // Jacobian-vector product of the residual source: out = d(R V)/dW v at the
 // current state with the boundary values held fixed (v, out device [N][5])
 void launch_residual_tangent(Handle& h, const double* v, double* out);
+// its transpose by reverse mode (out = (d(R V)/dW)^T u, device [N][5]),
+// recomputing the fields and limited gradients; the empty string when the
+// configuration is covered, else why not
+void launch_residual_vjp(Handle& h, const double* u, double* out);
+std::string residual_vjp_unsupported(const Handle& h);
+// matrix-free Krylov solves (device FP64 [N][5] right-hand side and solution)
+// and the patch pressure force with its gradient (device [N][5] or nullptr)
+int adjoint_solve(Handle& h, const double* g, double* psi, const ics_krylov_opts& o, ics_krylov_result* res);
+int tangent_solve(Handle& h, const double* b, double* x, const ics_krylov_opts& o, ics_krylov_result* res);
+double pressure_force(Handle& h, int patch, const double dir[3], double* dJdW_dev);
 // passive scalar: face terms + matrix rows at the current flow state, the
 // scalar GMRES solve (increment in dx, device [N]) and the state update
 void launch_scalar_assembly(Handle& h);

@@ -948,10 +948,10 @@ static void spmv_t(Handle& h, const TV* x, TV* y) {
 
 
 template <typename TB, typename TV>
-static void lusgs_t(Handle& h, TV* r) {
+static void lusgs_t(Handle& h, TV* r, const TB* blkIn = nullptr, const TB* rDIn = nullptr) {
   const DevMesh& m = h.m;
-  const TB* blk = (const TB*)h.blk;
-  const TB* rD = (const TB*)h.rD;
+  const TB* blk = blkIn ? blkIn : (const TB*)h.blk;
+  const TB* rD = rDIn ? rDIn : (const TB*)h.rD;
   // forward sweep, then reverse sweep; many small levels run in one CTA
   if ((long)m.N < 2048L * m.nfl) {
     ICS_LAUNCH(h, ICS_K_LUSGS_FWD, k_lusgs_block<TB, TV, true><<<1, 1024, 0, h.stream>>>(m, blk, rD, r, m.fl_cells, m.fl_lptr, m.nfl));
@@ -1099,6 +1099,18 @@ static void sweep_probe_t(Handle& h, const int* order, int count, int spin_limit
   ICS_LAUNCH(h, ICS_K_LUSGS_FWD, k_lusgs_sweep<TB, TV, true><<<grid_for(count, SWEEP_THREADS), SWEEP_THREADS, 0, st>>>(
                                      m, (const TB*)h.blk, (const TB*)h.rD, (const TV*)h.kw, fwd, nullptr, order,
                                      count, m.sweep_ticket, &h.ks->status, spin_limit));
+  ICS_CUDA(cudaGetLastError());
+}
+
+// LU-SGS sweeps on an FP64 vector with the given off-diagonal slots (factored
+// FP32 or 25-entry FP64 storage) and scalar diagonal: the preconditioner of
+// the matrix-free Krylov solves (k_krylov.cu), which transposes the blocks
+// for the adjoint system
+void lusgs_with(Handle& h, const void* blk, const void* rD, bool fp32, double* r) {
+  if (fp32)
+    lusgs_t<float, double>(h, r, (const float*)blk, (const float*)rD);
+  else
+    lusgs_t<double, double>(h, r, (const double*)blk, (const double*)rD);
   ICS_CUDA(cudaGetLastError());
 }
 

@@ -367,6 +367,62 @@ int ics_get_exact_jacobian(ics_handle h, int32_t* row_ptr, int32_t* cols, double
 /* Vector-Jacobian product JTu = (d(R V)/dW)^T u with the exact Jacobian,
  * assembled first when the state changed.  Pointers as in ics_jvp.         */
 int ics_vjp(ics_handle h, const double* u, double* JTu, int32_t device);
+/* The same vector-Jacobian product by reverse mode, storing no Jacobian:
+ * the face and cell maps of the residual are transposed in reverse order and
+ * the fields, Gauss gradients and cellLimited limiters are recomputed from
+ * the state in the backward pass (the flux's local partial derivatives by
+ * dual numbers through the same flux function).  Equal to ics_vjp up to
+ * round-off, and the exact transpose of ics_jvp's map.  Covers the inviscid
+ * residual with upwind or linearUpwind (MUSCL) reconstruction, all three
+ * flux schemes, the physical ddt, MRF zones and Harmonic Balance; returns
+ * ICS_ERR_ARG for viscous cases, cyclic patches and the TVD limitedScheme
+ * reconstructions.  Pointers as in ics_jvp.                                 */
+int ics_vjp_recompute(ics_handle h, const double* u, double* JTu, int32_t device);
+/* ---- Krylov solves with the exact residual derivative (no counterpart in
+ * the reference, whose linear solves use the approximate Jacobian) ------- */
+typedef struct {
+  int32_t n_directions;   /* Krylov dimension (restart length), 1..64            */
+  int32_t max_cycles;     /* restart cycles at most                               */
+  double rel_tol;         /* stop when ||rhs - A x||_2 <= rel_tol ||rhs||_2        */
+  int32_t precision;      /* ICS_PREC_FP64: FP64 Krylov basis; ICS_PREC_MIXED:
+                             FP32 basis (operator and preconditioner stay FP64)   */
+  int32_t preconditioner; /* ICS_PC_NONE, or ICS_PC_LUSGS: the LU-SGS of the
+                             approximate Jacobian of the last ics_assemble_jacobian
+                             (transposed for the adjoint system)                  */
+  int32_t pseudo_time;    /* 1: add the local pseudo-time diagonal V / dtau of the
+                             last ics_residual to the operator (the implicit
+                             pseudo-time step), 0: the steady operator           */
+} ics_krylov_opts;
+typedef struct {
+  int32_t iterations;     /* operator applications                                */
+  int32_t cycles;         /* restart cycles                                       */
+  double rel_residual;    /* final ||rhs - A x||_2 / ||rhs||_2 (recomputed)        */
+  int32_t converged;
+} ics_krylov_result;
+/* The operator of both solves is A = s V / dtau - d(R V)/dW (s = the option
+ * pseudo_time): the exact form of the matrix the reference assembles
+ * approximately (its Jacobian of -R V plus the pseudo-time diagonal, which
+ * ics_solve_increment solves with), so the approximate Jacobian's LU-SGS is a
+ * consistent preconditioner.
+ * Adjoint system A^T psi = g at the current state, by restarted
+ * right-preconditioned GMRES whose operator is ics_vjp_recompute's reverse
+ * chain (no Jacobian stored).  g and psi are host [n_cells][5].  Coverage as
+ * ics_vjp_recompute; the LU-SGS preconditioner needs no cyclic patches.     */
+int ics_adjoint_solve(ics_handle h, const double* g, double* psi, const ics_krylov_opts* opts,
+                      ics_krylov_result* result);
+/* Tangent (Newton) system A x = b at the current state with the forward-mode
+ * product of ics_jvp in the operator: with pseudo_time = 1 and b the residual
+ * source R V this is the pseudo-time Newton step of ics_solve_increment with
+ * the exact Jacobian (matrix-free Newton-Krylov), preconditioned by the
+ * reference's approximate one.                                              */
+int ics_tangent_solve(ics_handle h, const double* b, double* x, const ics_krylov_opts* opts,
+                      ics_krylov_result* result);
+/* Integrated pressure force of one patch along dir: J = sum over its faces of
+ * p (S . dir), with p the pressure of each face's cell (the patch's pressure
+ * must be zeroGradient: slip, zeroGradient or isothermal wall patches), and,
+ * when dJdW is not NULL, dJ/dW [n_cells][5] (host), the right-hand side of
+ * the adjoint system of that functional.                                    */
+int ics_pressure_force(ics_handle h, int32_t patch, const double dir[3], double* J, double* dJdW);
 /* pseudotimeControl::loop() (pseudotimeControl.C:159-241): returns 1 in
  * *more while the pseudo loop should run another iteration.                 */
 int ics_pseudo_loop(ics_handle h, int32_t* more);
@@ -377,7 +433,7 @@ enum {
   ICS_K_FIELDS = 0, ICS_K_GRAD, ICS_K_FACE, ICS_K_BFACE, ICS_K_CELLRES, ICS_K_JAC_BOUNDARY, ICS_K_JAC_ROWS,
   ICS_K_JACOBI_INV, ICS_K_SPMV, ICS_K_LUSGS_FWD, ICS_K_LUSGS_REV, ICS_K_JACOBI, ICS_K_MGS, ICS_K_VECTOR,
   ICS_K_SCALAR, ICS_K_UPDATE, ICS_K_BC, ICS_K_BOUND, ICS_K_VISC, ICS_K_TANGENT, ICS_K_EXACT, ICS_K_OP0,
-  ICS_K_OP1, ICS_K_PASSIVE, ICS_K_COUNT
+  ICS_K_OP1, ICS_K_PASSIVE, ICS_K_ADJOINT, ICS_K_COUNT
 };
 /* Start (enable=1) or stop (0) recording a CUDA event pair around every
  * kernel launch on the handle's stream; starting clears previous records.  */
@@ -390,6 +446,12 @@ int ics_launch_count(ics_handle h, int64_t* launches);
  * a second one, synchronises and returns the elapsed milliseconds.          */
 int ics_timer_start(ics_handle h);
 int ics_timer_stop(ics_handle h, double* ms);
+
+/* FP64 fused multiply-add rate (GFLOP/s, an FMA = 2 flops) of the handle's
+ * GPU, measured with CUDA events on the handle's stream by a kernel of
+ * independent FMA chains on every SM: the peak against which the FP64-bound
+ * residual kernels (face fluxes, gradients) are reported.                   */
+int ics_measure_fp64_rate(ics_handle h, double* gflops);
 
 /* ---- allocation-free entry point (no counterpart in the reference) ------ */
 /* r = b - A x and the five per-equation L1 sums of r, with A the handle's

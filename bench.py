@@ -53,6 +53,8 @@ def parse():
                     help="time cap of the mixed-precision leg to 1e-8 (the FP64 leg gets 2.5x)")
     ap.add_argument("--plateau-cap-s", type=float, default=15.0,
                     help="seconds of the configured Venkatakrishnan limiter (mixed) recording its plateau")
+    ap.add_argument("--convergence-study", type=int, default=0,
+                    help="only record the GPU and oracle rho residual histories of the reduced workloads")
     ap.add_argument("--viscous-solution", type=int, default=0,
                     help="only run the 200^3 viscous box (8M cells) to 1e-8 in both precisions")
     ap.add_argument("--e2e-steps", type=int, default=10)
@@ -348,6 +350,78 @@ def run_solution_pair(w, cap_s, settings, plateau_cap_s=0.0, from_peak=False):
     return out
 
 
+def _history_worker(args):
+    """The oracle's rho L2 history of one reduced workload (CPU process)."""
+    name, settings, iters, every = args
+    sys.path.insert(0, ROOT)
+    import oracle
+    from icsfoam_gb300 import cases
+
+    w = _study_workload(name)
+    h = oracle.open_case(w.mesh, cases.make_config(oracle.binding(), w.settings, **settings))
+    h.set_primitive(w.p, w.U, w.T)
+    hist = []
+    for it in range(iters):
+        h.pseudo_loop()
+        s = h.pseudo_iteration()
+        if it % every == 0 or it == iters - 1:
+            hist.append((it, s.rho_l2_residual))
+    return hist
+
+
+def _study_workload(name):
+    from icsfoam_gb300 import cases
+
+    if name == "bump_64x16x16":
+        return cases.bump_channel(64, 16, 16, ordering_mode="colour")
+    return cases.random_box(24)
+
+
+def run_convergence_study(iters=1500, every=50):
+    """rho L2 histories of the reduced bump channel (64x16x16) and viscous box
+    (24^3) under the configured cellLimited<Venkatakrishnan> gradients and
+    under cellLimited<minmod>, from the GPU (FP64) and from the oracle run at
+    the same time on host cores: both stall with Venkatakrishnan at the same
+    level, both converge with minmod."""
+    import multiprocessing as mp
+
+    from icsfoam_gb300 import cases, gpu
+
+    runs = [(name, label, settings) for name in ("bump_64x16x16", "random_box_24")
+            for label, settings in (("venkatakrishnan", {}), ("minmod", SOLUTION_SETTINGS))]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(len(runs)) as pool:
+        pending = pool.map_async(_history_worker, [(n, st, iters, every) for n, _, st in runs])
+        b = gpu.binding()
+        gpu_hist = []
+        for name, label, settings in runs:
+            w = _study_workload(name)
+            h = gpu.open_case(w.mesh, cases.make_config(b, w.settings, **settings))
+            h.set_primitive(w.p, w.U, w.T)
+            hist = []
+            for it in range(iters):
+                h.pseudo_loop()
+                s = h.pseudo_iteration()
+                if it % every == 0 or it == iters - 1:
+                    hist.append((it, s.rho_l2_residual))
+            h.close()
+            gpu_hist.append(hist)
+        ora_hist = pending.get()
+    out = {}
+    for (name, label, _), hg, ho in zip(runs, gpu_hist, ora_hist):
+        g = [r for _, r in hg]
+        o = [r for _, r in ho]
+        peak_g, peak_o = max(g), max(o)
+        out["%s_%s" % (name, label)] = {
+            "iterations": iters,
+            "gpu_min_drop_from_peak": min(g[g.index(peak_g):]) / peak_g,
+            "oracle_min_drop_from_peak": min(o[o.index(peak_o):]) / peak_o,
+            "gpu_last_drop": g[-1] / peak_g, "oracle_last_drop": o[-1] / peak_o,
+            "history": [(it, rg, ro) for (it, rg), (_, ro) in zip(hg, ho)],
+        }
+    return out
+
+
 def run_e2e(w, steps, warmup):
     """Through the C ABI with pinned host buffers: state H2D, one pseudo iteration, state D2H per step.
 
@@ -635,6 +709,10 @@ def main():
         os.environ["CUDA_VISIBLE_DEVICES"] = str(dist.local)
     from icsfoam_gb300 import cases
 
+    if args.convergence_study:
+        print(json.dumps({"convergence_study": run_convergence_study(args.convergence_study)}), flush=True)
+        dist.close()
+        return
     if args.viscous_solution:
         # the randomised viscous box at its configured size and numbering (RCM)
         w = cases.random_box(200)

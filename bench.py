@@ -249,9 +249,11 @@ def run_timed(w, prec, steps, warmup, dist, profile):
     l0 = h.launch_count()
     h.timer_start()
     last = None
+    cycles = 0
     for _ in range(steps):
         h.pseudo_loop()
         last = h.pseudo_iteration()
+        cycles += last.perf.n_iterations
     ms = h.timer_stop()
     launches = h.launch_count() - l0
     ck = clocks.stop()
@@ -276,7 +278,8 @@ def run_timed(w, prec, steps, warmup, dist, profile):
         kern = h.profile_read()
         h.close()
     return {"ms": ms, "launches": launches, "kernels": kern, "clocks": ck,
-            "last_rho_l2": last.rho_l2_residual if last else None, "fp64_rate": fp64_rate}
+            "last_rho_l2": last.rho_l2_residual if last else None, "fp64_rate": fp64_rate,
+            "gmres_cycles_per_iter": cycles / max(steps, 1)}
 
 
 def run_to_solution(w, prec, cap_s, target=1e-8, max_iters=20000, from_peak=False, **over):
@@ -294,10 +297,12 @@ def run_to_solution(w, prec, cap_s, target=1e-8, max_iters=20000, from_peak=Fals
     drop = 1.0
     best = 1.0
     hist = []
+    cycles = 0
     while it < max_iters:
         h.pseudo_loop()
         s = h.pseudo_iteration()
         it += 1
+        cycles += s.perf.n_iterations
         r0 = max(r0 or 0.0, s.rho_l2_residual) if from_peak else (r0 or s.rho_l2_residual)
         drop = s.rho_l2_residual / r0
         best = min(best, drop)
@@ -309,7 +314,7 @@ def run_to_solution(w, prec, cap_s, target=1e-8, max_iters=20000, from_peak=Fals
     state = h.get_state()["W"]
     h.close()
     return {"iterations": it, "seconds": dt, "drop": drop, "min_drop": best, "reached": drop <= target,
-            "cell_iters_per_s": w.mesh.n_cells * it / dt,
+            "cell_iters_per_s": w.mesh.n_cells * it / dt, "gmres_cycles_per_iter": cycles / max(it, 1),
             "history": hist[::max(1, len(hist) // 12)] + hist[-1:]}, state
 
 
@@ -487,8 +492,9 @@ def run_hb_sweep(instances=(3, 5, 7, 9), per=(32, 64, 128), steps=5, warmup=2):
 
 
 def run_batch(n_cases=64, steps=5, warmup=2, seed=2):
-    """64 independent bump cases, N ~ U[2000, 50000]: one pseudo iteration of all of them per step,
-    concurrently (ics_pseudo_iteration_batch) and one after another (the reference's way)."""
+    """64 independent shock-tube cases (Sod, AUSM+up, backward dual-time ddt), N ~ U[2000, 50000]
+    (seeded): one pseudo iteration of all of them per step, concurrently (ics_pseudo_iteration_batch)
+    and one after another (the reference's way)."""
     import numpy as np
 
     from icsfoam_gb300 import abi, cases, gpu
@@ -498,10 +504,10 @@ def run_batch(n_cases=64, steps=5, warmup=2, seed=2):
     sizes = rng.integers(2000, 50001, n_cases)
     hs, total = [], 0
     for n in sizes:
-        k = max(2, int(round((n / 4.0) ** (1.0 / 3.0))))
-        w = cases.bump_channel(4 * k, k, k, ordering_mode="colour")
+        w = cases.shock_tube(int(n), ordering_mode="colour")
         h = gpu.open_case(w.mesh, cases.make_config(b, w.settings, precision=1))
         h.set_primitive(w.p, w.U, w.T)
+        h.begin_time_step()
         hs.append(h)
         total += w.mesh.n_cells
     for _ in range(warmup):
@@ -522,7 +528,8 @@ def run_batch(n_cases=64, steps=5, warmup=2, seed=2):
     seq = time.perf_counter() - t0
     for h in hs:
         h.close()
-    return {"cases": n_cases, "cells": int(total), "concurrent_cell_iters_per_s": total * steps / conc,
+    return {"cases": n_cases, "kind": "Sod shock tubes, 1D, colour-blocked", "cells": int(total),
+            "concurrent_cell_iters_per_s": total * steps / conc,
             "sequential_cell_iters_per_s": total * steps / seq, "speedup": seq / conc}
 
 
@@ -813,7 +820,8 @@ def main():
                        "ordering": "colour-blocked", "parallelism": "replicas" if dist.world > 1 else "1 GPU",
                        "l2": "working set >> 129 MB L2; no flush needed"},
             "fp64": {"value": value64, "unit": UNIT, "ms_per_step": fp64["ms"] / args.steps,
-                     "kernels": fp64_table},
+                     "gmres_cycles_per_iter": fp64["gmres_cycles_per_iter"], "kernels": fp64_table},
+            "gmres_cycles_per_iter": mixed["gmres_cycles_per_iter"],
             "mixed_over_fp64": value / value64,
             "kernels": kern_table, "roofline": roof, "fp64_roofline": fp64_roof, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": mixed["launches"], "clocks": mixed["clocks"], "mesh_build_s": round(mesh_s, 1),

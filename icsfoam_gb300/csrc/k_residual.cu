@@ -264,8 +264,10 @@ __global__ void __launch_bounds__(128) k_grad(DevMesh m, const Real* __restrict_
 // ------------------------------------------------------------ face fluxes
 // MRF = true reads the frame face velocity (moving reference frames); the
 // default instance has it as the constant zero, so it costs nothing there
+// FP64 residual: three blocks per SM (168 registers) keep more warps in
+// flight for the FP64 pipe; the dual-number tangent keeps its registers
 template <typename Real = double, bool MRF = false>
-__global__ void __launch_bounds__(128) k_face(DevMesh m, ResParams P, const Real* __restrict__ q,
+__global__ void __launch_bounds__(128, is_fp64<Real> ? 3 : 1) k_face(DevMesh m, ResParams P, const Real* __restrict__ q,
                                               const Real* __restrict__ grad, const double* __restrict__ clin,
                                               const double* __restrict__ nf, Real* __restrict__ fflux,
                                               double* __restrict__ frec, double* __restrict__ flam, int FB) {

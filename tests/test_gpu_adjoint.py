@@ -81,11 +81,11 @@ def test_vjp_recompute_refuses_what_it_does_not_cover(gpu_binding):
         h2.vjp_recompute(np.ones((w2.mesh.n_cells, 5)))
 
 
-def _swept(b, n=(24, 12, 8), iterations=3, precision=0):
+def _swept(b, n=(24, 12, 8), iterations=3, precision=0, **over):
     """The swept bump after some pseudo iterations, with its approximate
     Jacobian assembled at that state (the preconditioner)."""
     w = cases.swept_bump(*n)
-    h = abi.CaseHandle(b, w.mesh, cases.make_config(b, w.settings, precision=precision))
+    h = abi.CaseHandle(b, w.mesh, cases.make_config(b, w.settings, precision=precision, **over))
     h.set_primitive(w.p, w.U, w.T)
     for _ in range(iterations):
         h.pseudo_loop()
@@ -121,17 +121,25 @@ def _residuals(h, psi, x, g, b, pseudo_time):
     return r_a, r_t
 
 
-@pytest.mark.parametrize("pseudo_time,precision,iterations", [(1, 0, 3), (1, 1, 3), (0, 0, 200), (0, 1, 200)])
-def test_adjoint_and_tangent_solves_are_dual(gpu_binding, pseudo_time, precision, iterations):
+FIRST_ORDER = {"recon_rho": 0, "recon_U": 0, "recon_T": 0}
+
+
+@pytest.mark.parametrize("pseudo_time,precision,iterations,over", [(1, 0, 3, {}), (1, 1, 3, {}),
+                                                                   (0, 0, 400, FIRST_ORDER),
+                                                                   (0, 1, 400, FIRST_ORDER)])
+def test_adjoint_and_tangent_solves_are_dual(gpu_binding, pseudo_time, precision, iterations, over):
     """A^T psi = g (reverse-mode operator) and A x = b (forward-mode operator,
     matrix-free Newton-Krylov), right-preconditioned by the approximate
     Jacobian's LU-SGS (transposed for the adjoint), solved to 1e-8 with an
-    FP64 or FP32 Krylov basis: with the pseudo-time diagonal early in the run,
-    and for the steady operator on a state iterated towards convergence.  The
+    FP64 or FP32 Krylov basis: with the pseudo-time diagonal early in the run
+    (second order), and for the steady operator on a converged state (first
+    order: with the cellLimited limiters the pseudo-time iteration of this
+    case stalls, and the steady linearisation at a stalled state is not well
+    conditioned for this preconditioner).  The
     true residuals meet the tolerance and <g, x> = <psi, b> holds to the
     bound the two residuals allow, which needs the two operators to be each
     other's transpose."""
-    w, h, bump = _swept(gpu_binding, iterations=iterations)
+    w, h, bump = _swept(gpu_binding, iterations=iterations, **over)
     _, g = h.pressure_force(bump, (1.0, 0.0, 0.0))
     W = h.get_state()["W"]
     b = direction(W, 30) * 1e-3

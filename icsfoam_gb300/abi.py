@@ -142,6 +142,7 @@ _FUNCS = {
     "begin_time_step": (C.c_int, [_P]),
     "pseudo_loop": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "set_hb": (C.c_int, [_P, C.c_int32, _P]),
+    "set_hb_zone": (C.c_int, [_P, _P, C.c_int32, _P, _P]),
     "set_mrf": (C.c_int, [_P, _P, _P, _P, _P, C.c_int32]),
     "set_phase_lag": (C.c_int, [_P, _P, _P]),
     "scalar_enable": (C.c_int, [_P, _P, _P, _P, C.c_double, C.c_int32]),
@@ -432,6 +433,16 @@ class CaseHandle:
     def set_hb(self, n_instances: int, D):
         D = np.ascontiguousarray(D, np.float64).reshape(n_instances, n_instances)
         self._check(self.b.fn["set_hb"](self.h, int(n_instances), _ptr(D)), "set_hb")
+
+    def set_hb_zone(self, zone=None, cyl_coords=False, axis=(0.0, 0.0, 1.0), origin=(0.0, 0.0, 0.0)):
+        """HB zone (per-instance cell flags or None for every cell) and cylCoords."""
+        z = None if zone is None else np.ascontiguousarray(zone, np.int32)
+        a = np.ascontiguousarray(axis, np.float64)
+        o = np.ascontiguousarray(origin, np.float64)
+        if z is not None:
+            self._keep.append(z)
+        self._check(self.b.fn["set_hb_zone"](self.h, _ptr(z), int(bool(cyl_coords)), _ptr(a), _ptr(o)),
+                    "set_hb_zone")
 
     def set_phase_lag(self, setup=None):
         """Phase-lag cyclic patches of an HB handle: ``hb.phase_lag_setup``'s

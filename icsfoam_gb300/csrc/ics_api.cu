@@ -101,7 +101,7 @@ void free_all(Handle& h) {
                   h.ddtCoeff, h.q, h.bq, h.clin, h.grad, h.fflux, h.frec, h.flam, h.bjac, h.src, h.vcell,
                   h.fvisc, h.vsf2, h.vjac, m.dc, m.Dhb, m.mrfU, m.mrfOm, m.mrfBU, m.mrfBIn, m.plagMode, m.plagP, m.bpartner, m.bw, m.bdelta, m.bdNei,
                   m.bnodc, m.cyc_face, m.cyc_row, m.cyc_ptr, h.cblk, h.vjslotbuf, h.vjcellbuf, h.cfrec, h.tW, h.tprim, h.tq, h.tgrad, h.tflux, h.tvc, h.tfv, h.tv,
-                  h.aF, h.aQ, h.aG, h.aSrc, h.aVal,
+                  h.aF, h.aQ, h.aG, h.aSrc, h.aVal, h.hbZoneBuf,
                   h.ss, h.ssB, h.srhoS, h.srhoS0, h.srhoS00, h.sgrad, h.sgradL, h.sface, h.sblk, h.sdg, h.srD,
                   h.ssrc, h.sFixed, h.sValue,
                   h.blk, h.dg,
@@ -1658,11 +1658,63 @@ int ics_set_hb(ics_handle hh, int32_t n, const double* D) {
     }
     h.m.nInst = n;
     h.m.Nc = h.m.N / n;
+    // a new instance count starts without a zone (every cell) and Cartesian
+    if (h.hbZoneBuf) ICS_CUDA(cudaFree(h.hbZoneBuf));
+    h.hbZoneBuf = nullptr;
+    h.m.hbZone = nullptr;
+    h.m.hbCyl = 0;
     h.ctl.assign(n, Handle::Control());
     h.initResValid = h.prevResValid = false;
     h.haveMatrix = h.haveIncrement = false;
     free_exact(h);   // the stencil gains the instance partners
     drop_graphs(h);  // the captured cycle's reduction grids depend on n
+    return ICS_OK;
+  });
+}
+
+int ics_set_hb_zone(ics_handle hh, const int32_t* zone, int32_t cyl_coords, const double axis[3],
+                    const double origin[3]) {
+  if (!hh) return ICS_ERR_ARG;
+  Handle& h0 = hh->h;
+  if (h0.m.nInst < 2) {
+    h0.err = "set_hb_zone needs a Harmonic Balance handle";
+    return ICS_ERR_ARG;
+  }
+  double a[3] = {0, 0, 1}, o[3] = {0, 0, 0};
+  if (cyl_coords) {
+    if (!axis || !origin) {
+      h0.err = "cylCoords needs the rotation axis and origin";
+      return ICS_ERR_ARG;
+    }
+    const double ma = std::sqrt(axis[0] * axis[0] + axis[1] * axis[1] + axis[2] * axis[2]);
+    if (!(ma > 0)) {
+      h0.err = "zero rotation axis";
+      return ICS_ERR_ARG;
+    }
+    for (int k = 0; k < 3; ++k) {
+      a[k] = axis[k] / ma;
+      o[k] = origin[k];
+    }
+  }
+  return guard(hh, [&](Handle& h) {
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    if (h.hbZoneBuf) ICS_CUDA(cudaFree(h.hbZoneBuf));
+    h.hbZoneBuf = nullptr;
+    h.m.hbZone = nullptr;
+    if (zone) {
+      std::vector<unsigned char> mask(h.m.N);
+      for (int c = 0; c < h.m.N; ++c) mask[c] = zone[c % h.m.Nc] != 0;
+      h.hbZoneBuf = dalloc<unsigned char>(h.m.N);
+      ICS_CUDA(cudaMemcpy(h.hbZoneBuf, mask.data(), h.m.N, cudaMemcpyHostToDevice));
+      h.m.hbZone = h.hbZoneBuf;
+    }
+    h.m.hbCyl = cyl_coords ? 1 : 0;
+    for (int k = 0; k < 3; ++k) {
+      h.m.hbAxis[k] = a[k];
+      h.m.hbOrigin[k] = o[k];
+    }
+    h.haveMatrix = h.haveIncrement = h.haveExact = false;
+    drop_graphs(h);  // the captured launches hold DevMesh by value
     return ICS_OK;
   });
 }

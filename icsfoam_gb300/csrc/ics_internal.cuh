@@ -111,6 +111,13 @@ struct DevMesh {
   // coupled through the spectral operator Dhb [nInst][nInst]
   int nInst = 1, Nc = 0;
   double* Dhb = nullptr;
+  // HB zone (HBZone cellZone): cells of the stacked mesh that carry the
+  // spectral source and couplings (nullptr: every cell); hbCyl combines the
+  // instances' momentum in cylindrical components about hbAxis through
+  // hbOrigin (HBZone cylCoords)
+  const unsigned char* hbZone = nullptr;
+  int hbCyl = 0;
+  double hbAxis[3] = {0, 0, 1}, hbOrigin[3] = {0, 0, 0};
   // moving reference frames (all nullptr without MRF zones): frame velocity
   // . n per internal then boundary face [F+B], rotation vector per cell
   // [3][N], frame velocity of the boundary faces [3][B] and where it is
@@ -248,6 +255,7 @@ struct Handle {
   double* aG = nullptr;
   int* aSrc = nullptr;
   double* aVal = nullptr;
+  unsigned char* hbZoneBuf = nullptr;  // owner of m.hbZone
   // exact Jacobian of the residual source: stencil CSR (two face hops plus
   // Harmonic Balance partners), transpose positions, colouring, blocks
   int* xptr = nullptr;

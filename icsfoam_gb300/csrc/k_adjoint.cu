@@ -378,15 +378,7 @@ __global__ void __launch_bounds__(128) k_adj_cell(DevMesh m, ResParams P, unsign
 #pragma unroll
     for (int k = 0; k < 3; ++k) r[1 + k] -= cr[k] * Vc;
   }
-  if (m.nInst > 1) {  // -V_c sum_J D_JK u_(J,c) into instance K
-    const int K = c / m.Nc, cl = c - K * m.Nc;
-    for (int J = 0; J < m.nInst; ++J) {
-      const double d = Vc * m.Dhb[J * m.nInst + K];
-      const double* uj = u + 5 * ((size_t)J * m.Nc + cl);
-#pragma unroll
-      for (int k = 0; k < 5; ++k) r[k] -= d * uj[k];
-    }
-  }
+  if (m.nInst > 1) hb_apply_transpose(m, c, -Vc, u, r);  // -V_c sum_J D_JK u_(J,c) into instance K
 #pragma unroll
   for (int k = 0; k < 5; ++k) out[5 * c + k] = r[k];
 }

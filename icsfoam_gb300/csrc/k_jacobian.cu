@@ -19,6 +19,7 @@
 // diagonal (lusgs.C:50-127).
 #include "blocks.cuh"
 #include "flux.cuh"
+#include "hb.cuh"
 #include "ics_internal.cuh"
 
 namespace ics {
@@ -453,8 +454,9 @@ __global__ void __launch_bounds__(128) k_jac_rows(DevMesh m, double gamma, const
     diag[5 * 3 + 1] -= T(oy);
     diag[5 * 3 + 2] += T(ox);
   }
-  if (m.nInst > 1) {
-    // Harmonic Balance diagonal V D_JJ on every equation (HBZone.C:435-518)
+  if (m.nInst > 1 && hb_in_zone(m, c)) {
+    // Harmonic Balance diagonal V D_JJ on every equation, in the HB zone
+    // (HBZone.C:435-518: Cartesian, cylCoords or not)
     const int J = c / m.Nc;
     const T hd = T(m.V[c] * m.Dhb[J * m.nInst + J]);
 #pragma unroll

@@ -17,6 +17,7 @@
 #include <cmath>
 
 #include "blocks.cuh"
+#include "hb.cuh"
 #include "ics_internal.cuh"
 
 namespace ics {
@@ -156,7 +157,7 @@ __global__ void __launch_bounds__(128) k_spmv(DevMesh m, const TB* __restrict__ 
 #pragma unroll
     for (int i = 0; i < 5; ++i) acc[i] += y[i];
   }
-  if (m.nInst > 1) {
+  if (m.nInst > 1 && hb_in_zone(m, c)) {
     // Harmonic Balance coupling blocks V D_JK I with the other instances
     const int J = c / m.Nc, cl = c - J * m.Nc;
     const double Vc = m.V[c];
@@ -279,7 +280,7 @@ __global__ void __launch_bounds__(128, MINB) k_op_level0(DevMesh m, const TB* __
 #pragma unroll
     for (int r = 0; r < 5; ++r) acc[r] += y[r];
   }
-  if (m.nInst > 1) {
+  if (m.nInst > 1 && hb_in_zone(m, c)) {
     const int J = c / m.Nc, cl = c - J * m.Nc;
     const double Vc = m.V[c];
     for (int K = 0; K < m.nInst; ++K) {
@@ -372,7 +373,7 @@ __global__ void __launch_bounds__(128, MINB) k_op_level1(DevMesh m, const TB* __
       fw[r] += yb[r];
     }
   }
-  if (m.nInst > 1) {
+  if (m.nInst > 1 && hb_in_zone(m, c)) {
     const int J = c / m.Nc, cl = c - J * m.Nc;
     const double Vc = m.V[c];
     for (int K = 0; K < m.nInst; ++K) {

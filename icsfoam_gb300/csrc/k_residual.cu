@@ -582,15 +582,10 @@ __global__ void __launch_bounds__(128) k_cellres(DevMesh m, CellResParams D, con
   }
   if (m.nInst > 1) {
     // Harmonic Balance source -V sum_K D_JK W_K of this cell's instance J
-    // (HBZoneTemplates.C:39-92), added to R*V (HB residualsUpdate.H:72-74)
-    const int J = c / m.Nc, cl = c - J * m.Nc;
+    // (HBZoneTemplates.C:39-92, HBZone.C:520-652 in its zone and with
+    // cylCoords), added to R*V (HB residualsUpdate.H:72-74)
     double hb[5] = {0, 0, 0, 0, 0};
-    for (int K = 0; K < m.nInst; ++K) {
-      const double d = m.Dhb[J * m.nInst + K];
-      const double* wk = W + 5 * ((size_t)K * m.Nc + cl);
-#pragma unroll
-      for (int k = 0; k < 5; ++k) hb[k] -= Vc * d * wk[k];
-    }
+    hb_apply(m, c, -Vc, W, hb);
 #pragma unroll
     for (int k = 0; k < 5; ++k) src[5 * c + k] = r[k] * Vc + hb[k];
   } else {
@@ -810,15 +805,7 @@ __global__ void __launch_bounds__(128) k_src_tangent(DevMesh m, double dgPhys, c
 #pragma unroll
     for (int k = 0; k < 3; ++k) r[1 + k] -= cr[k] * Vc;
   }
-  if (m.nInst > 1) {
-    const int J = c / m.Nc, cl = c - J * m.Nc;
-    for (int K = 0; K < m.nInst; ++K) {
-      const double d = Vc * m.Dhb[J * m.nInst + K];
-      const double* vk = v + 5 * ((size_t)K * m.Nc + cl);
-#pragma unroll
-      for (int k = 0; k < 5; ++k) r[k] -= d * vk[k];
-    }
-  }
+  if (m.nInst > 1) hb_apply(m, c, -Vc, v, r);  // the HB source is linear in W
 #pragma unroll
   for (int k = 0; k < 5; ++k) out[5 * c + k] = r[k];
 }

@@ -7,6 +7,7 @@
 #include <type_traits>
 
 #include "flux.cuh"
+#include "hb.cuh"
 #include "ics_internal.cuh"
 
 namespace ics {

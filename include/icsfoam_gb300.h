@@ -261,9 +261,20 @@ int ics_begin_time_step(ics_handle h);
  * instances) and every instance keeps its own pseudotimeControl state
  * (ics_pseudo_loop answers 1 while any instance is not finished).  Needs
  * steadyState ddt and the GMRES solver; n_instances = 1 switches HB off.
- * Rotating-frame (cylindrical) momentum sources are not provided.          */
+ * Zones and cylindrical momentum sources: ics_set_hb_zone.                */
 #define ICS_MAX_INSTANCES 16
 int ics_set_hb(ics_handle h, int32_t n_instances, const double* D);
+/* The HB zone of an HB handle (HBZone.C:100-165, 359-652): zone[n] (n =
+ * n_cells / n_instances, the same cells in every instance; NULL: every cell)
+ * marks the cells that carry the spectral source -V sum_K D_JK W_K and the
+ * Jacobian's V D_JK couplings; the others carry neither (a cellZone).  With
+ * cyl_coords the source combines each instance's momentum in cylindrical
+ * components (radial, circumferential, axial about axis through origin, at
+ * that instance's cell centre) and turns the sum back into Cartesian
+ * components at the cell's own centre (HBZone cylCoords); the Jacobian's
+ * couplings stay Cartesian, as the reference's addBlock.                    */
+int ics_set_hb_zone(ics_handle h, const int32_t* zone, int32_t cyl_coords, const double axis[3],
+                    const double origin[3]);
 /* Moving reference frames (MRF zones): replaces the convectiveFluxScheme
  * fields MRFOmega / MRFFaceVelocity (convectiveFluxScheme.H:77-81,192-199)
  * and MRFCoupledZoneList::correctBoundaryVelocity as dbnsFoam sets them up

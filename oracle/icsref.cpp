@@ -134,6 +134,10 @@ struct Case {
   // Harmonic Balance: nInst stacked instances of Nc cells, operator Dhb
   int nInst = 1, Nc = 0;
   std::vector<double> Dhb;
+  // HB zone (HBZone cellZone; empty: every cell) and cylCoords about axis / origin
+  std::vector<unsigned char> hbZone;
+  bool hbCyl = false;
+  V3 hbAxis = V3(0, 0, 1), hbOrigin = V3();
   // residual bookkeeping (setCoAndDeltaT.H, pseudotimeControl), one entry per
   // equation and instance: [5*J + k], k = rho, rhoUx, rhoUy, rhoUz, rhoE
   bool initResValid = false, prevResValid = false;
@@ -228,6 +232,19 @@ void setPlag(const Case& c, VolS& f, Fn cellValue) {
 
 // MRF face velocity of face fi (internal then boundary), zero without zones
 inline double umOf(const Case& c, int fi) { return c.mrfOn ? c.mrfU[fi] : 0.0; }
+
+// HBZone cellZone membership of cell i (every cell without a zone)
+inline bool hbInZone(const Case& c, int i) { return c.hbZone.empty() || c.hbZone[i]; }
+
+// radial and circumferential unit vectors of the HB zone's cylindrical frame
+// at the centre of cell i (HBZone.C:560-582)
+inline void hbFrame(const Case& c, int i, V3& rh, V3& th) {
+  V3 r = c.C[i] - c.hbOrigin;
+  r = r - c.hbAxis * dot(c.hbAxis, r);
+  rh = r / std::sqrt(dot(r, r));
+  th = V3(c.hbAxis.y * rh.z - c.hbAxis.z * rh.y, c.hbAxis.z * rh.x - c.hbAxis.x * rh.z,
+          c.hbAxis.x * rh.y - c.hbAxis.y * rh.x);
+}
 
 // MRFCoupledZone::correctBoundaryVelocity (MRFCoupledZone.C:594-619)
 void mrfBoundaryVelocity(Case& c) {
@@ -1123,15 +1140,36 @@ void residualSource(Case& c) {
     c.src[5 * i + 2] = rU.y * Vc;
     c.src[5 * i + 3] = rU.z * Vc;
     c.src[5 * i + 4] = rE * Vc;
-    if (c.nInst > 1) {
+    if (c.nInst > 1 && hbInZone(c, i)) {
       // Harmonic Balance source -V sum_K D_JK W_K (HBZoneTemplates.C:39-92),
-      // added to R*V (HB residualsUpdate.H:72-74)
+      // added to R*V (HB residualsUpdate.H:72-74); in the HB zone only, and
+      // with cylCoords the momentum combined in cylindrical components at
+      // each instance's cell centre (HBZone.C:520-652)
       const int J = i / c.Nc, cl = i % c.Nc;
       double hb[5] = {0, 0, 0, 0, 0};
+      V3 cyl;
       for (int K = 0; K < c.nInst; ++K) {
         const int j = K * c.Nc + cl;
-        const double wv[5] = {c.rho[j], c.rhoU[j].x, c.rhoU[j].y, c.rhoU[j].z, c.rhoE[j]};
-        for (int k = 0; k < 5; ++k) hb[k] -= Vc * c.Dhb[J * c.nInst + K] * wv[k];
+        const double d = Vc * c.Dhb[J * c.nInst + K];
+        hb[0] -= d * c.rho[j];
+        hb[4] -= d * c.rhoE[j];
+        if (c.hbCyl) {
+          V3 rh, th;
+          hbFrame(c, j, rh, th);
+          cyl = cyl + V3(dot(c.rhoU[j], rh), dot(c.rhoU[j], th), dot(c.rhoU[j], c.hbAxis)) * d;
+        } else {
+          hb[1] -= d * c.rhoU[j].x;
+          hb[2] -= d * c.rhoU[j].y;
+          hb[3] -= d * c.rhoU[j].z;
+        }
+      }
+      if (c.hbCyl) {
+        V3 rh, th;
+        hbFrame(c, i, rh, th);
+        const V3 cart = rh * cyl.x + th * cyl.y + c.hbAxis * cyl.z;
+        hb[1] -= cart.x;
+        hb[2] -= cart.y;
+        hb[3] -= cart.z;
       }
       for (int k = 0; k < 5; ++k) c.src[5 * i + k] = c.src[5 * i + k] + hb[k];
     }
@@ -1585,6 +1623,7 @@ void assembleJacobian(Case& c) {
   // Harmonic Balance diagonal V D_JJ on every equation (HBZone.C:435-518)
   if (c.nInst > 1) {
     for (int i = 0; i < c.N; ++i) {
+      if (!hbInZone(c, i)) continue;
       const int J = i / c.Nc;
       const double d = c.V[i] * c.Dhb[J * c.nInst + J];
       for (int q = 0; q < 5; ++q) c.diag[i].a[diagIdx[q]] += d;
@@ -1620,6 +1659,7 @@ void matrixMul(const Case& c, const double* x, double* y) {
   // on every equation (dbnsFullyImplicitHBFoam outerLoop.H, HB.addBlock)
   if (c.nInst > 1) {
     for (int i = 0; i < c.N; ++i) {
+      if (!hbInZone(c, i)) continue;
       const int J = i / c.Nc, cl = i % c.Nc;
       for (int K = 0; K < c.nInst; ++K) {
         if (K == J) continue;
@@ -3051,8 +3091,33 @@ int icsref_set_hb(ics_handle h, int32_t n, const double* D) {
   c.nInst = n;
   c.Nc = c.N / n;
   c.Dhb.assign(n > 1 ? D : nullptr, n > 1 ? D + n * n : nullptr);
+  c.hbZone.clear();
+  c.hbCyl = false;
   c.ctl.assign(n, Case::Control());
   c.initResValid = c.prevResValid = false;
+  c.haveMatrix = c.haveIncrement = false;
+  return ICS_OK;
+}
+
+int icsref_set_hb_zone(ics_handle h, const int32_t* zone, int32_t cyl_coords, const double axis[3],
+                       const double origin[3]) {
+  if (!h) return ICS_ERR_ARG;
+  Case& c = *h;
+  if (c.nInst < 2) return ICS_ERR_ARG;
+  c.hbZone.clear();
+  if (zone) {
+    c.hbZone.resize(c.N);
+    for (int i = 0; i < c.N; ++i) c.hbZone[i] = zone[i % c.Nc] != 0;
+  }
+  c.hbCyl = cyl_coords != 0;
+  if (c.hbCyl) {
+    if (!axis || !origin) return ICS_ERR_ARG;
+    const V3 a(axis[0], axis[1], axis[2]);
+    const double ma = std::sqrt(dot(a, a));
+    if (!(ma > 0)) return ICS_ERR_ARG;
+    c.hbAxis = a / ma;
+    c.hbOrigin = V3(origin[0], origin[1], origin[2]);
+  }
   c.haveMatrix = c.haveIncrement = false;
   return ICS_OK;
 }

@@ -169,3 +169,93 @@ def test_reconstruction_recovers_band_limited_history(H, selected):
         assert np.allclose(HB.reconstruct(om, t, snaps, tt), f(tt), atol=1e-10)
     # at an instant the weights select that snapshot
     assert np.allclose(HB.reconstruction_weights(om, t, t[1]), np.eye(2 * H + 1)[1], atol=1e-10)
+
+
+def _zone_case():
+    """HB annular sector (slip sides) whose instance meshes are rotated about
+    the axis by different angles, so that the cylindrical frames of the
+    instances differ; zone: the upstream half of the cells."""
+    w = cases.hb_annular_sector(4, 6, 6, harmonics=1, sides="slip")
+    m = w.mesh
+    n, D = w.hb
+    Nc = m.n_cells // n
+    rng = np.random.default_rng(8)
+    w.p = w.p * (1 + 0.02 * rng.uniform(-1, 1, m.n_cells))
+    w.U = w.U + 5.0 * rng.uniform(-1, 1, (m.n_cells, 3))
+
+    def rot(a):
+        c, s = np.cos(a), np.sin(a)
+        return np.array([[c, -s, 0.0], [s, c, 0.0], [0.0, 0.0, 1.0]])
+
+    inst_f = m.owner // Nc
+    inst_b = m.b_cell // Nc
+    for K in range(n):
+        R = rot(0.05 * K)
+        m.C[K * Nc:(K + 1) * Nc] = m.C[K * Nc:(K + 1) * Nc] @ R.T
+        for a in (m.Sf, m.Cf):
+            a[inst_f == K] = a[inst_f == K] @ R.T
+        for a in (m.b_Sf, m.b_Cf):
+            a[inst_b == K] = a[inst_b == K] @ R.T
+        w.U[K * Nc:(K + 1) * Nc] = w.U[K * Nc:(K + 1) * Nc] @ R.T
+    zone = (m.C[:Nc, 2] < 0.1).astype(np.int32)
+    return w, zone
+
+
+def test_hb_zone_and_cylindrical_source(oracle_binding):
+    """The HB zone carries the source and couplings, the other cells neither;
+    every cell as the zone is the default; with identical instance frames the
+    cylindrical combination equals the Cartesian one; with rotated instances
+    it differs only in the momentum source, and the Jacobian stays Cartesian
+    (HBZone.C:435-519)."""
+    w, zone = _zone_case()
+    n, D = w.hb
+    Nc = w.mesh.n_cells // n
+
+    def opened(zone_=None, cyl=False, Dm=D):
+        h = abi.CaseHandle(oracle_binding, w.mesh, cases.make_config(oracle_binding, w.settings))
+        h.set_hb(n, Dm)
+        h.set_primitive(w.p, w.U, w.T)
+        if zone_ is not None or cyl:
+            h.set_hb_zone(zone_, cyl, (0.0, 0.0, 1.0), (0.0, 0.0, 0.0))
+        return h
+
+    base = opened()
+    r0 = base.residual()
+    base.assemble_jacobian()
+    x = np.random.default_rng(2).standard_normal((w.mesh.n_cells, 5))
+    y0 = base.matrix_mul(x)
+    every = opened(np.ones(Nc, np.int32))
+    assert np.array_equal(every.residual(), r0)
+    every.assemble_jacobian()
+    assert np.array_equal(every.matrix_mul(x), y0)
+    # outside the zone: the residual and matrix action of uncoupled instances
+    zoned = opened(zone)
+    free = opened(Dm=np.zeros_like(D))
+    rz, rf = zoned.residual(), free.residual()
+    out = np.tile(zone == 0, n)
+    assert np.array_equal(rz[out], rf[out]) and np.array_equal(rz[~out], r0[~out])
+    zoned.assemble_jacobian()
+    free.assemble_jacobian()
+    yz, yf = zoned.matrix_mul(x), free.matrix_mul(x)
+    assert np.allclose(yz[out], yf[out], rtol=1e-14, atol=0) and np.allclose(yz[~out], y0[~out], rtol=1e-14, atol=0)
+    # cylindrical components: only the momentum source changes, the matrix does not
+    cyl = opened(cyl=True)
+    rc = cyl.residual()
+    assert np.array_equal(rc[:, [0, 4]], r0[:, [0, 4]])
+    assert not np.allclose(rc[:, 1:4], r0[:, 1:4], rtol=1e-9, atol=0)
+    cyl.assemble_jacobian()
+    assert np.allclose(cyl.matrix_mul(x), y0, rtol=1e-14, atol=1e-300)
+    # identical instance meshes: the cylindrical frames agree and the two
+    # combinations give the same source up to round-off
+    w2 = cases.hb_annular_sector(4, 6, 6, harmonics=1, sides="slip")
+    w2.U = w.U
+    res = []
+    for c in (False, True):
+        h = abi.CaseHandle(oracle_binding, w2.mesh, cases.make_config(oracle_binding, w2.settings))
+        h.set_hb(*w2.hb)
+        h.set_primitive(w.p, w.U, w.T)
+        if c:
+            h.set_hb_zone(None, True, (0.0, 0.0, 1.0), (0.0, 0.0, 0.0))
+        res.append(h.residual())
+    scale = np.abs(res[0]).max(axis=0)
+    assert np.max(np.abs(res[1] - res[0]) / scale) < 1e-12

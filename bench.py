@@ -319,17 +319,18 @@ def run_to_solution(w, prec, cap_s, target=1e-8, max_iters=20000, from_peak=Fals
 
 
 # Reference dictionary settings under which the pseudo-time iteration of the
-# workloads reaches a 1e-8 drop of the rho residual.  With the configured
+# bump channel reaches a 1e-8 drop of the rho residual.  With the configured
 # cellLimited<Venkatakrishnan> gradients the reference algorithm (the oracle
 # as much as this GPU path) stalls: OpenFOAM's Venkatakrishnan limiter has no
-# smoothing parameter, is below 1 for every finite ratio, and the face that
-# sets a cell's limiter keeps switching, so the residual plateaus at a
-# 1e-7..1e-5 drop on the bump channel and ~1e-3 on the viscous box.  The
-# cellLimited<minmod> gradients (gradSchemes "cellLimited<minmod> Gauss
-# linear 1", same linearUpwind reconstruction) equal 1 wherever the ratio
-# is >= 1, so the limiter stops switching and both precisions converge.
-SOLUTION_SETTINGS = {"recon_rho": 4, "recon_U": 4, "recon_T": 4}
-SOLUTION_SCHEME = "linearUpwind + cellLimited<minmod> Gauss linear 1"
+# smoothing parameter and is below 1 for every finite ratio, so the face that
+# sets a cell's limiter keeps switching and the residual plateaus (1e-7..1e-5
+# on the 64x16x16 channel for the oracle, ~1e-3 on the 256x64x64 one).  The
+# cellLimited<minmod> gradients converge on the 64x16x16 channel but stall at
+# ~4e-4 on 256x64x64; the TVD vanLeer limitedScheme of the reference's
+# tutorials (interpolationSchemes "reconstruct(rho) vanLeer", same for U, T)
+# converges on both, and is what the time to 1e-8 is measured with.
+SOLUTION_SETTINGS = {"recon_rho": 1, "recon_U": 1, "recon_T": 1}
+SOLUTION_SCHEME = "vanLeer (TVD limitedScheme, Gauss linear gradient)"
 
 
 def run_solution_pair(w, cap_s, settings, plateau_cap_s=0.0, from_peak=False):
@@ -384,16 +385,18 @@ def _study_workload(name):
 
 def run_convergence_study(iters=1500, every=50):
     """rho L2 histories of the reduced bump channel (64x16x16) and viscous box
-    (24^3) under the configured cellLimited<Venkatakrishnan> gradients and
-    under cellLimited<minmod>, from the GPU (FP64) and from the oracle run at
-    the same time on host cores: both stall with Venkatakrishnan at the same
-    level, both converge with minmod."""
+    (24^3) under the configured cellLimited<Venkatakrishnan> gradients, under
+    cellLimited<minmod> and under the vanLeer limitedScheme, from the GPU
+    (FP64) and from the oracle run at the same time on host cores: the two
+    stall together where the algorithm stalls and converge together where it
+    converges."""
     import multiprocessing as mp
 
     from icsfoam_gb300 import cases, gpu
 
     runs = [(name, label, settings) for name in ("bump_64x16x16", "random_box_24")
-            for label, settings in (("venkatakrishnan", {}), ("minmod", SOLUTION_SETTINGS))]
+            for label, settings in (("venkatakrishnan", {}), ("minmod", {"recon_rho": 4, "recon_U": 4, "recon_T": 4}),
+                                    ("vanleer", SOLUTION_SETTINGS))]
     ctx = mp.get_context("spawn")
     with ctx.Pool(len(runs)) as pool:
         pending = pool.map_async(_history_worker, [(n, st, iters, every) for n, _, st in runs])

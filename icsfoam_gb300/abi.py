@@ -105,6 +105,14 @@ class IterStats(C.Structure):
                 ("bounded_cells", C.c_int32), ("status", C.c_int32)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("face_block", C.c_int32), ("grad_block", C.c_int32), ("mgs_blocks", C.c_int32),
+                ("fused_operator", C.c_int32), ("from_cache", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class KrylovOpts(C.Structure):
     _fields_ = [("n_directions", C.c_int32), ("max_cycles", C.c_int32), ("rel_tol", C.c_double),
                 ("precision", C.c_int32), ("preconditioner", C.c_int32), ("pseudo_time", C.c_int32)]
@@ -158,6 +166,7 @@ _MEASURE = {
     "timer_start": (C.c_int, [_P]),
     "timer_stop": (C.c_int, [_P, C.POINTER(C.c_double)]),
     "measure_fp64_rate": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "autotune": (C.c_int, [_P, C.POINTER(Tuning)]),
 }
 
 # allocation-free linear residual (CUDA library only; arguments are device pointers)
@@ -496,6 +505,12 @@ class CaseHandle:
         n = C.c_int64()
         self._check(self.b.fn["launch_count"](self.h, C.byref(n)), "launch_count")
         return int(n.value)
+
+    def autotune(self) -> dict:
+        """Time the launch choices on this state and keep the fastest (see ics_autotune)."""
+        t = Tuning()
+        self._check(self.b.fn["autotune"](self.h, C.byref(t)), "autotune")
+        return t.as_dict()
 
     def measure_fp64_rate(self) -> float:
         """Measured FP64 FMA rate of the handle's GPU in GFLOP/s."""

@@ -12,6 +12,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <map>
+#include <mutex>
 #include <cstring>
 #include <new>
 #include <atomic>
@@ -1541,6 +1543,56 @@ int ics_vjp(ics_handle hh, const double* u, double* JTu, int32_t device) {
     stage_in(h, u, tu, device);
     exact_vjp(h, tu, out);
     stage_out(h, out, JTu, device);
+    return ICS_OK;
+  });
+}
+
+namespace {
+// autotuner choices per (device, cells, faces, slots, levels, precision, scheme, limiter)
+std::mutex g_tune_mu;
+std::map<std::vector<long long>, ics_tuning> g_tune_cache;
+std::vector<long long> tune_key(const Handle& h) {
+  int lim = 0;
+  grad_mask(h, &lim);
+  return {h.device, h.m.N, h.m.F, h.m.nslots, h.m.nfl, h.m.nrl, prec(h), h.cfg.c.flux_scheme, lim,
+          h.cfg.c.preconditioner, h.cfg.c.n_directions};
+}
+}  // namespace
+
+int ics_autotune(ics_handle hh, ics_tuning* out) {
+  return guard(hh, [&](Handle& h) {
+    if (!h.haveMatrix || !h.haveFlux) {
+      h.err = "autotune needs a residual and an assembled Jacobian";
+      return ICS_ERR_STATE;
+    }
+    const auto key = tune_key(h);
+    ics_tuning t{};
+    {
+      std::lock_guard<std::mutex> lock(g_tune_mu);
+      auto it = g_tune_cache.find(key);
+      if (it != g_tune_cache.end()) t = it->second, t.from_cache = 1;
+    }
+    if (!t.from_cache) {
+      std::vector<std::pair<std::string, double>> log;
+      autotune_residual(h, log);
+      autotune_linalg(h, log);
+      t.face_block = h.tuneFaceBs;
+      t.grad_block = h.tuneGradBs;
+      t.mgs_blocks = h.tuneMgsBlocks;
+      t.fused_operator = h.tuneFused;
+      std::lock_guard<std::mutex> lock(g_tune_mu);
+      g_tune_cache[key] = t;
+    }
+    h.tuneFaceBs = t.face_block;
+    h.tuneGradBs = t.grad_block;
+    h.tuneMgsBlocks = t.mgs_blocks;
+    h.tuneFused = t.fused_operator;
+    drop_graphs(h);  // the captured cycle holds the old launch shapes
+    // the timing runs overwrote the Krylov workspace and the face fields
+    // of this state; the next iteration recomputes both
+    h.haveIncrement = false;
+    ICS_CUDA(cudaStreamSynchronize(h.stream));
+    if (out) *out = t;
     return ICS_OK;
   });
 }

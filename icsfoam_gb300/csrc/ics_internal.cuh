@@ -256,6 +256,9 @@ struct Handle {
   int* aSrc = nullptr;
   double* aVal = nullptr;
   unsigned char* hbZoneBuf = nullptr;  // owner of m.hbZone
+  // launch choices, set by the autotuner (ics_autotune) or left at the
+  // defaults that the hand sweeps picked
+  int tuneFaceBs = 128, tuneGradBs = 128, tuneMgsBlocks = 608, tuneFused = 1;
   // exact Jacobian of the residual source: stencil CSR (two face hops plus
   // Harmonic Balance partners), transpose positions, colouring, blocks
   int* xptr = nullptr;
@@ -364,6 +367,13 @@ void spmv(Handle& h, const void* x, void* y);
 int precondition(Handle& h, void* r);
 // fills *perf (maximum over instances) and initRes (per instance, [5*J + k])
 int gmres_solve(Handle& h, ics_solver_perf* perf, std::vector<double>& initRes);
+// the autotuner's measurements on the handle's assembled system (ms per
+// candidate) for the Krylov side and the residual side; they set the tune*
+// fields to the fastest candidates
+void autotune_linalg(Handle& h, std::vector<std::pair<std::string, double>>& log);
+void autotune_residual(Handle& h, std::vector<std::pair<std::string, double>>& log);
+// fields with a reconstruction gradient (bit k = q field k) and the MUSCL limiter kind
+unsigned grad_mask(const Handle& h, int* limited);
 void to_vec(Handle& h, const double* src, void* dst);   // FP64 -> Krylov type
 void sweep_probe(Handle& h, const int* order, int count, int spin_limit);
 void from_vec(Handle& h, const void* src, double* dst); // Krylov type -> FP64

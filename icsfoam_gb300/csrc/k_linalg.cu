@@ -14,6 +14,7 @@
 //             grid and a last-block-done tree, so results are reproducible
 //             run to run.  One host synchronisation per restart cycle reads
 //             the L1 residuals for the stop test (coupledMatrixSolver.C:198-221).
+#include <algorithm>
 #include <cmath>
 
 #include "blocks.cuh"
@@ -85,8 +86,8 @@ constexpr int RB = 256;  // threads per reduction block
 
 // MGS steps stream 3 Krylov vectors of which two are L2-resident, so they are
 // bound by latency and the reduction tail rather than by HBM: 4 blocks per SM
-// (608 on 152 SMs) measured 11% faster than 8 per SM (sweep of 304-1216).
-constexpr int MGS_BLOCKS = 608;
+// (608 on 152 SMs) measured 11% faster than 8 per SM (sweep of 304-1216);
+// the default of Handle::tuneMgsBlocks, which the autotuner may change.
 constexpr int MGS_CHUNKS = 2;
 
 // 16-byte vector of the Krylov element type
@@ -1071,7 +1072,7 @@ template <typename TB, typename TV>
 static bool fused_op_available(const Handle& h) {
   const DevMesh& m = h.m;
   // (the fused passes carry no cyclic couplings: those meshes take spmv_t)
-  return h.cfg.c.preconditioner == ICS_PC_LUSGS && m.nfl == 2 && m.nrl == 2 && m.fuse_last &&
+  return h.tuneFused && h.cfg.c.preconditioner == ICS_PC_LUSGS && m.nfl == 2 && m.nrl == 2 && m.fuse_last &&
          (long)m.N >= 2048L * m.nfl && m.ncyc == 0;
 }
 
@@ -1385,7 +1386,7 @@ static int gmres_t(Handle& h, ResIO& p) {
   auto cycle = [&]() {
     precondition_t<TB, TV>(h, w);
     ICS_LAUNCH(h, ICS_K_MGS,
-               k_mgs<TV><<<MGS_BLOCKS, RB, 0, st>>>(n5, w, nullptr, nullptr, nullptr, &ks->status, h.partials,
+               k_mgs<TV><<<h.tuneMgsBlocks, RB, 0, st>>>(n5, w, nullptr, nullptr, nullptr, &ks->status, h.partials,
                                                        h.counter, red, ks, 1, 0, m));
     // with the fused operator the step's normalisation is folded into it and
     // the unnormalised vector alternates between two buffers (w, t); the
@@ -1407,11 +1408,11 @@ static int gmres_t(Handle& h, ResIO& p) {
         const TV* vprev = j > 0 ? V + (size_t)(j - 1) * vs : nullptr;
         const double* hprev = j > 0 ? &ks->H[(j - 1) * m + i] : nullptr;
         ICS_LAUNCH(h, ICS_K_MGS,
-                   k_mgs<TV><<<MGS_BLOCKS, RB, 0, st>>>(n5, wc, vprev, hprev, V + (size_t)j * vs, &ks->status,
+                   k_mgs<TV><<<h.tuneMgsBlocks, RB, 0, st>>>(n5, wc, vprev, hprev, V + (size_t)j * vs, &ks->status,
                                                            h.partials, h.counter, &ks->H[j * m + i], ks, 0, i, m));
       }
       ICS_LAUNCH(h, ICS_K_MGS,
-                 k_mgs<TV><<<MGS_BLOCKS, RB, 0, st>>>(n5, wc, vi, &ks->H[i * m + i], nullptr, &ks->status,
+                 k_mgs<TV><<<h.tuneMgsBlocks, RB, 0, st>>>(n5, wc, vi, &ks->H[i * m + i], nullptr, &ks->status,
                                                          h.partials, h.counter, &red[1], ks, 2, i, m));
     }
     ICS_LAUNCH(h, ICS_K_SCALAR, k_backsub<<<1, 1, 0, st>>>(ks, m));
@@ -1487,6 +1488,77 @@ int gmres_solve(Handle& h, ics_solver_perf* perf, std::vector<double>& initRes) 
   perf->converged = st == ICS_OK;
   initRes = r.init;
   return st;
+}
+
+// ------------------------------------------------------------ autotuner
+// Times the Krylov-side launch choices on the handle's assembled system with
+// CUDA events on its stream (median of three runs each, after a warm-up):
+// the MGS step's grid, and the fused LU-SGS operator against SpMV plus
+// separate sweeps.  Sets the fastest; the arithmetic of every choice is the
+// same up to the order of the sums.
+template <typename TB, typename TV>
+static void autotune_linalg_t(Handle& h, std::vector<std::pair<std::string, double>>& log) {
+  cudaStream_t st = h.stream;
+  const long n5 = 5L * h.m.N;
+  TV* V = (TV*)h.kv;
+  TV* w = (TV*)h.kw;
+  TV* t = (TV*)h.kt;
+  cudaEvent_t e0, e1;
+  ICS_CUDA(cudaEventCreate(&e0));
+  ICS_CUDA(cudaEventCreate(&e1));
+  auto timed = [&](auto&& fn) {
+    fn();
+    double best[3];
+    for (int r = 0; r < 3; ++r) {
+      ICS_CUDA(cudaEventRecord(e0, st));
+      fn();
+      ICS_CUDA(cudaEventRecord(e1, st));
+      ICS_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      ICS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      best[r] = ms;
+    }
+    std::sort(best, best + 3);
+    return best[1];
+  };
+  // operands: w = b, v_0 = b (a step of the cycle's Gram-Schmidt)
+  to_vec(h, h.src, w);
+  to_vec(h, h.src, V);
+  KrylovScalars* ks = h.ks;
+  const int m = h.cfg.c.n_directions;
+  int bestBlocks = h.tuneMgsBlocks;
+  double bestMs = 1e300;
+  for (int blocks : {152, 304, 456, 608}) {
+    const double ms = timed([&]() {
+      k_mgs<TV><<<blocks, RB, 0, st>>>(n5, w, nullptr, nullptr, V, &ks->status, h.partials, h.counter,
+                                        &ks->H[0], ks, 0, 0, m);
+    });
+    log.emplace_back("mgs_blocks_" + std::to_string(blocks), ms);
+    if (ms < bestMs) bestMs = ms, bestBlocks = blocks;
+  }
+  h.tuneMgsBlocks = bestBlocks;
+  ICS_CUDA(cudaMemsetAsync(&ks->status, 0, sizeof(int), st));
+  h.tuneFused = 1;
+  if (fused_op_available<TB, TV>(h)) {
+    const double fused = timed([&]() { fused_op_t<TB, TV>(h, V, w); });
+    const double split = timed([&]() {
+      spmv_t<TB, TV>(h, V, t);
+      precondition_t<TB, TV>(h, t);
+    });
+    log.emplace_back("operator_fused", fused);
+    log.emplace_back("operator_spmv_then_lusgs", split);
+    h.tuneFused = fused <= split ? 1 : 0;
+  }
+  ICS_CUDA(cudaEventDestroy(e0));
+  ICS_CUDA(cudaEventDestroy(e1));
+  ICS_CUDA(cudaGetLastError());
+}
+
+void autotune_linalg(Handle& h, std::vector<std::pair<std::string, double>>& log) {
+  if (prec(h) == ICS_PREC_MIXED)
+    autotune_linalg_t<float, float>(h, log);
+  else
+    autotune_linalg_t<double, double>(h, log);
 }
 
 // sum of a device array (deterministic fixed-order reduction)
@@ -1706,7 +1778,7 @@ int scalar_gmres(Handle& h, double* dx, ics_solver_perf* perf) {
   int status = ICS_OK;
   while (true) {
     s_precondition(h, w);
-    ICS_LAUNCH(h, ICS_K_MGS, k_mgs<double><<<MGS_BLOCKS, RB, 0, st>>>(N, w, nullptr, nullptr, nullptr, &ks->status,
+    ICS_LAUNCH(h, ICS_K_MGS, k_mgs<double><<<h.tuneMgsBlocks, RB, 0, st>>>(N, w, nullptr, nullptr, nullptr, &ks->status,
                                                                        h.partials, h.counter, red, ks, 1, 0, m));
     for (int i = 0; i < m; ++i) {
       double* vi = V + (size_t)i * vs;
@@ -1717,10 +1789,10 @@ int scalar_gmres(Handle& h, double* dx, ics_solver_perf* perf) {
         const double* vprev = j > 0 ? V + (size_t)(j - 1) * vs : nullptr;
         const double* hprev = j > 0 ? &ks->H[(j - 1) * m + i] : nullptr;
         ICS_LAUNCH(h, ICS_K_MGS,
-                   k_mgs<double><<<MGS_BLOCKS, RB, 0, st>>>(N, w, vprev, hprev, V + (size_t)j * vs, &ks->status,
+                   k_mgs<double><<<h.tuneMgsBlocks, RB, 0, st>>>(N, w, vprev, hprev, V + (size_t)j * vs, &ks->status,
                                                             h.partials, h.counter, &ks->H[j * m + i], ks, 0, i, m));
       }
-      ICS_LAUNCH(h, ICS_K_MGS, k_mgs<double><<<MGS_BLOCKS, RB, 0, st>>>(N, w, vi, &ks->H[i * m + i], nullptr,
+      ICS_LAUNCH(h, ICS_K_MGS, k_mgs<double><<<h.tuneMgsBlocks, RB, 0, st>>>(N, w, vi, &ks->H[i * m + i], nullptr,
                                                                          &ks->status, h.partials, h.counter, &red[1],
                                                                          ks, 2, i, m));
     }

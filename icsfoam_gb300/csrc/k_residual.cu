@@ -671,7 +671,7 @@ static void launch_grad_t(Handle& h, const Real* q, Real* grad, int kind) {
     if (isMuscl && rs[g] != (limited == 2 ? ICS_RECON_MUSCL_VENKATAKRISHNAN : ICS_RECON_MUSCL_MINMOD))
       throw std::string("MUSCL groups must share one gradient limiter");
   }
-  const int bs = 128;
+  const int bs = h.tuneGradBs;
   if (limited == 2)
     ICS_LAUNCH(h, kind, k_grad<2, Real><<<grid_for(h.m.N, bs), bs, 0, h.stream>>>(h.m, q, h.bq, mask, grad));
   else if (limited == 1)
@@ -683,15 +683,59 @@ static void launch_grad_t(Handle& h, const Real* q, Real* grad, int kind) {
 
 void launch_grad(Handle& h) { launch_grad_t<double>(h, h.q, h.grad, ICS_K_GRAD); }
 
+// The residual-side launch choices of the autotuner: threads per block of
+// the face-flux and gradient kernels (64 or 128; both kernels are FP64-pipe
+// bound and their occupancy is set by registers), timed with CUDA events on
+// the handle's stream at its current state.
+void autotune_residual(Handle& h, std::vector<std::pair<std::string, double>>& log) {
+  cudaEvent_t e0, e1;
+  ICS_CUDA(cudaEventCreate(&e0));
+  ICS_CUDA(cudaEventCreate(&e1));
+  auto timed = [&](auto&& fn) {
+    fn();
+    float best = 1e30f;
+    for (int r = 0; r < 3; ++r) {
+      ICS_CUDA(cudaEventRecord(e0, h.stream));
+      fn();
+      ICS_CUDA(cudaEventRecord(e1, h.stream));
+      ICS_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      ICS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      best = ms < best ? ms : best;
+    }
+    return (double)best;
+  };
+  launch_fields(h);
+  int bestG = h.tuneGradBs, bestF = h.tuneFaceBs;
+  double tg = 1e300, tf = 1e300;
+  for (int bs : {64, 128}) {
+    h.tuneGradBs = bs;
+    const double ms = timed([&]() { launch_grad(h); });
+    log.emplace_back("grad_block_" + std::to_string(bs), ms);
+    if (ms < tg) tg = ms, bestG = bs;
+  }
+  h.tuneGradBs = bestG;
+  launch_grad(h);
+  for (int bs : {64, 128}) {
+    h.tuneFaceBs = bs;
+    const double ms = timed([&]() { launch_face_flux(h); });
+    log.emplace_back("face_block_" + std::to_string(bs), ms);
+    if (ms < tf) tf = ms, bestF = bs;
+  }
+  h.tuneFaceBs = bestF;
+  ICS_CUDA(cudaEventDestroy(e0));
+  ICS_CUDA(cudaEventDestroy(e1));
+}
+
 void launch_face_flux(Handle& h) {
   const int FB = h.m.F + h.m.B;
   const ResParams P = res_params(h);
   if (h.m.F > 0) {
     if (h.m.mrfU)
-      ICS_LAUNCH(h, ICS_K_FACE, (k_face<double, true><<<grid_for(h.m.F, 128), 128, 0, h.stream>>>(
+      ICS_LAUNCH(h, ICS_K_FACE, (k_face<double, true><<<grid_for(h.m.F, h.tuneFaceBs), h.tuneFaceBs, 0, h.stream>>>(
                                     h.m, P, h.q, h.grad, h.clin, h.m.nf, h.fflux, h.frec, h.flam, FB)));
     else
-      ICS_LAUNCH(h, ICS_K_FACE, k_face<<<grid_for(h.m.F, 128), 128, 0, h.stream>>>(h.m, P, h.q, h.grad, h.clin, h.m.nf, h.fflux,
+      ICS_LAUNCH(h, ICS_K_FACE, k_face<<<grid_for(h.m.F, h.tuneFaceBs), h.tuneFaceBs, 0, h.stream>>>(h.m, P, h.q, h.grad, h.clin, h.m.nf, h.fflux,
                                                           h.frec, h.flam, FB));
   }
   if (h.m.B > 0)

@@ -458,6 +458,23 @@ int ics_launch_count(ics_handle h, int64_t* launches);
 int ics_timer_start(ics_handle h);
 int ics_timer_stop(ics_handle h, double* ms);
 
+/* Launch choices picked by the autotuner (no counterpart in the reference). */
+typedef struct {
+  int32_t face_block;      /* threads per block of the face-flux kernel (64 / 128)       */
+  int32_t grad_block;      /* threads per block of the gradient kernel (64 / 128)        */
+  int32_t mgs_blocks;      /* grid of the Gram-Schmidt steps (152 / 304 / 456 / 608)      */
+  int32_t fused_operator;  /* 1: fused M^-1 A passes on two-level schedules, 0: SpMV then
+                              LU-SGS sweeps                                              */
+  int32_t from_cache;      /* 1: taken from an earlier tuning of a case of the same shape */
+} ics_tuning;
+/* Time each candidate launch choice on the handle's current state and
+ * assembled Jacobian (CUDA events on its stream) and keep the fastest, for
+ * this handle and -- cached per device, mesh shape, precision and scheme --
+ * for later handles of the same shape, which take the cached choice without
+ * timing.  Needs ics_residual and ics_assemble_jacobian first.  Every choice
+ * computes the same result up to the order of floating-point sums.        */
+int ics_autotune(ics_handle h, ics_tuning* out);
+
 /* FP64 fused multiply-add rate (GFLOP/s, an FMA = 2 flops) of the handle's
  * GPU, measured with CUDA events on the handle's stream by a kernel of
  * independent FMA chains on every SM: the peak against which the FP64-bound

@@ -254,3 +254,31 @@ def test_gamma_change_needs_a_new_jacobian(gpu_binding, precision):
     h.residual()
     h.assemble_jacobian()
     assert np.all(np.isfinite(h.matrix_mul(x)))
+
+
+def test_autotune_keeps_the_results_and_caches_the_choice(gpu_binding):
+    """ics_autotune times its launch choices and keeps the fastest; every
+    choice gives the same pseudo iterations up to round-off, and a second
+    handle of the same shape takes the cached choice."""
+    w = cases.bump_channel(48, 16, 16, ordering_mode="colour")
+    ref = open_case(gpu_binding, w, precision=1)
+    tuned = open_case(gpu_binding, w, precision=1)
+    tuned.residual()
+    tuned.assemble_jacobian()
+    t = tuned.autotune()
+    assert t["face_block"] in (64, 128) and t["grad_block"] in (64, 128)
+    assert t["mgs_blocks"] in (152, 304, 456, 608) and t["fused_operator"] in (0, 1) and not t["from_cache"]
+    for _ in range(3):
+        ref.pseudo_loop()
+        ref.pseudo_iteration()
+        tuned.pseudo_loop()
+        tuned.pseudo_iteration()
+    Wr, Wt = ref.get_state()["W"], tuned.get_state()["W"]
+    scale = np.abs(Wr).max(axis=0)
+    assert (np.abs(Wt - Wr) / scale).max() < 1e-6
+    other = open_case(gpu_binding, w, precision=1)
+    other.residual()
+    other.assemble_jacobian()
+    t2 = other.autotune()
+    assert t2["from_cache"] and {k: t2[k] for k in t2 if k != "from_cache"} == \
+        {k: t[k] for k in t if k != "from_cache"}

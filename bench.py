@@ -53,6 +53,8 @@ def parse():
                     help="time cap of the mixed-precision leg to 1e-8 (the FP64 leg gets 2.5x)")
     ap.add_argument("--plateau-cap-s", type=float, default=15.0,
                     help="seconds of the configured Venkatakrishnan limiter (mixed) recording its plateau")
+    ap.add_argument("--adjoint", type=int, default=0,
+                    help="only the reverse-mode VJP and the adjoint solve on the 240x128x128 swept bump")
     ap.add_argument("--convergence-study", type=int, default=0,
                     help="only record the GPU and oracle rho residual histories of the reduced workloads")
     ap.add_argument("--viscous-solution", type=int, default=0,
@@ -623,9 +625,48 @@ def run_diff(nx=120, ny=64, nz=64, reps=5):
         h.vjp(v)
     vjp_ms = h.timer_stop() / reps
     h.close()
-    return {"workload": w.name, "cells": N, "jvp_ms": round(jvp_ms, 3), "exact_jacobian_s": round(asm_s, 3),
-            "colours": ncol, "stencil_blocks": nnz, "vjp_ms": round(vjp_ms, 3),
-            "note": "jvp/vjp ms include the host<->device copy of the [N,5] vectors"}
+    out = {"workload": w.name, "cells": N, "jvp_ms": round(jvp_ms, 3), "exact_jacobian_s": round(asm_s, 3),
+           "colours": ncol, "stencil_blocks": nnz, "vjp_ms": round(vjp_ms, 3),
+           "note": "jvp/vjp ms include the host<->device copy of the [N,5] vectors"}
+    out.update(run_adjoint(w, reps=reps))
+    return out
+
+
+def run_adjoint(w, iterations=20, reps=5, rel_tol=1e-8):
+    """The reverse-mode VJP (gradients recomputed, no stored Jacobian) and the
+    adjoint of the bump's x pressure force after some pseudo iterations:
+    (V/dtau - d(R V)/dW)^T psi = dJ/dW to rel_tol, FP64 operator and FP32
+    Krylov basis, transposed LU-SGS of the approximate Jacobian."""
+    import numpy as np
+
+    from icsfoam_gb300 import cases, gpu
+
+    b = gpu.binding()
+    h = gpu.open_case(w.mesh, cases.make_config(b, w.settings))
+    h.set_primitive(w.p, w.U, w.T)
+    for _ in range(iterations):
+        h.pseudo_loop()
+        h.pseudo_iteration()
+    h.residual()
+    h.assemble_jacobian()
+    N = w.mesh.n_cells
+    u = np.random.default_rng(1).standard_normal((N, 5))
+    h.vjp_recompute(u)
+    h.timer_start()
+    for _ in range(reps):
+        h.vjp_recompute(u)
+    rev_ms = h.timer_stop() / reps
+    bump = [p.name for p in w.mesh.patches].index("bump")
+    force, g = h.pressure_force(bump, (1.0, 0.0, 0.0))
+    t0 = time.perf_counter()
+    psi, r = h.adjoint_solve(g, n_directions=40, max_cycles=100, rel_tol=rel_tol, precision=1, pseudo_time=1)
+    adj_s = time.perf_counter() - t0
+    h.close()
+    return {"vjp_recompute_ms": round(rev_ms, 3), "pressure_force_x": force,
+            "adjoint": {"operator": "V/dtau - d(R V)/dW (reverse mode), FP32 Krylov basis, transposed LU-SGS",
+                        "iterations": r.iterations, "cycles": r.cycles, "rel_residual": r.rel_residual,
+                        "converged": bool(r.converged), "seconds": round(adj_s, 3),
+                        "ms_per_iteration": round(1000 * adj_s / max(r.iterations, 1), 3)}}
 
 
 def _oracle_worker(args):
@@ -719,6 +760,11 @@ def main():
         os.environ["CUDA_VISIBLE_DEVICES"] = str(dist.local)
     from icsfoam_gb300 import cases
 
+    if args.adjoint:
+        w = cases.swept_bump(240, 128, 128)
+        print(json.dumps({"workload": w.name, "cells": w.mesh.n_cells, **run_adjoint(w)}), flush=True)
+        dist.close()
+        return
     if args.convergence_study:
         print(json.dumps({"convergence_study": run_convergence_study(args.convergence_study)}), flush=True)
         dist.close()

@@ -103,7 +103,7 @@ void free_all(Handle& h) {
                   h.ddtCoeff, h.q, h.bq, h.clin, h.grad, h.fflux, h.frec, h.flam, h.bjac, h.src, h.vcell,
                   h.fvisc, h.vsf2, h.vjac, m.dc, m.Dhb, m.mrfU, m.mrfOm, m.mrfBU, m.mrfBIn, m.plagMode, m.plagP, m.bpartner, m.bw, m.bdelta, m.bdNei,
                   m.bnodc, m.cyc_face, m.cyc_row, m.cyc_ptr, h.cblk, h.vjslotbuf, h.vjcellbuf, h.cfrec, h.tW, h.tprim, h.tq, h.tgrad, h.tflux, h.tvc, h.tfv, h.tv,
-                  h.aF, h.aQ, h.aG, h.aSrc, h.aVal, h.hbZoneBuf,
+                  h.aF, h.aS, h.aQ, h.aG, h.aSrc, h.aVal, h.hbZoneBuf,
                   h.ss, h.ssB, h.srhoS, h.srhoS0, h.srhoS00, h.sgrad, h.sgradL, h.sface, h.sblk, h.sdg, h.srD,
                   h.ssrc, h.sFixed, h.sValue,
                   h.blk, h.dg,

@@ -251,6 +251,7 @@ struct Handle {
   // [NQ][N] and unlimited gradients [3 NQ][N], and the limiter bounds'
   // source cells and adjoints [2 NQ][N]
   double* aF = nullptr;
+  double* aS = nullptr;   // [16][F] adjoints of the TVD gradient projections
   double* aQ = nullptr;
   double* aG = nullptr;
   int* aSrc = nullptr;

@@ -30,8 +30,11 @@
 // Every branch (limiter selection, flux region) is decided on the values as
 // the forward pass decides it, so this is the transpose of ics_jvp's linear
 // map exactly (to round-off).  Boundary values are held fixed, as there.
-// Not provided (the entry point returns ICS_ERR_ARG): viscous terms, cyclic
-// patches and the TVD limitedScheme reconstructions (vanLeer, Minmod).
+// For the TVD limitedScheme reconstructions (vanLeer, Minmod) the face value
+// depends on both cells and on the upwind cell's unlimited gradient: the face
+// kernel transposes it there and hands on the adjoint of the gradient's
+// projection.  Not provided (the entry point returns ICS_ERR_ARG): viscous
+// terms and cyclic patches.
 #include "residual.cuh"
 
 namespace ics {
@@ -65,7 +68,7 @@ __device__ __forceinline__ void cell_q(const Real W[5], const ResParams& P, Real
 template <bool MRF>
 __global__ void __launch_bounds__(128) k_adj_face(DevMesh m, ResParams P, const double* __restrict__ q,
                                                   const double* __restrict__ grad, const double* __restrict__ u,
-                                                  double* __restrict__ aF) {
+                                                  double* __restrict__ aF, double* __restrict__ aS) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= m.F) return;
   const int N = m.N, F = m.F;
@@ -89,10 +92,11 @@ __global__ void __launch_bounds__(128) k_adj_face(DevMesh m, ResParams P, const 
   const double S[3] = {m.Sf[f], m.Sf[F + f], m.Sf[2 * F + f]};
   const double magS = m.magSf[f];
   const double um = MRF ? m.mrfU[f] : 0.0;
+  double qb[2 * NQ];
 #pragma unroll 1
   for (int j = 0; j < 2 * NQ; ++j) {
     if (P.scheme == ICS_FLUX_ROE && (j % NQ) == Q_C) {
-      aF[(size_t)j * F + f] = 0.0;
+      qb[j] = 0.0;
       continue;
     }
     Dual x[2 * NQ];
@@ -111,7 +115,41 @@ __global__ void __launch_bounds__(128) k_adj_face(DevMesh m, ResParams P, const 
     double a = 0.0;
 #pragma unroll
     for (int i = 0; i < 5; ++i) a += Fb[i] * out[i].d;
-    aF[(size_t)j * F + f] = a;
+    qb[j] = a;
+  }
+  // the reconstructions' transpose: adjoints reaching the owner's and the
+  // neighbour's value (aF[k], aF[NQ + k]); for the TVD limitedSchemes, whose
+  // face value depends on both cells and on the upwind cell's gradient
+  // projected on C_nei - C_own, also the adjoints of those projections of
+  // the left and right values (aS[k], aS[NQ + k])
+#pragma unroll 1
+  for (int k = 0; k < NQ; ++k) {
+    const int sch = recon_of(P, k);
+    double ao = qb[k], an = qb[NQ + k], sl = 0.0, sr = 0.0;
+    const bool used = !(P.scheme == ICS_FLUX_ROE && k == Q_C);  // Roe reconstructs no sound speed
+    if (used && (sch == ICS_RECON_VANLEER || sch == ICS_RECON_MINMOD)) {
+      const double qo = q[k * N + o], qn = q[k * N + nb];
+      const double d0 = m.dCC[f], d1 = m.dCC[F + f], d2 = m.dCC[2 * F + f];
+      const double gl = d0 * grad[(3 * k) * N + o] + d1 * grad[(3 * k + 1) * N + o] + d2 * grad[(3 * k + 2) * N + o];
+      const double gr = d0 * grad[(3 * k) * N + nb] + d1 * grad[(3 * k + 1) * N + nb] +
+                        d2 * grad[(3 * k + 2) * N + nb];
+      const double wf = m.w[f];
+      double dl[3], dr[3];  // d(value)/d(qo, qn, projected gradient)
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const Dual xo(qo, i == 0 ? 1.0 : 0.0), xn(qn, i == 1 ? 1.0 : 0.0);
+        dl[i] = tvd_face(sch, wf, 1.0, xo, xn, Dual(gl, i == 2 ? 1.0 : 0.0)).d;
+        dr[i] = tvd_face(sch, wf, 0.0, xo, xn, Dual(gr, i == 2 ? 1.0 : 0.0)).d;
+      }
+      ao = qb[k] * dl[0] + qb[NQ + k] * dr[0];
+      an = qb[k] * dl[1] + qb[NQ + k] * dr[1];
+      sl = qb[k] * dl[2];
+      sr = qb[NQ + k] * dr[2];
+    }
+    aF[(size_t)k * F + f] = ao;
+    aF[(size_t)(NQ + k) * F + f] = an;
+    aS[(size_t)k * F + f] = sl;
+    aS[(size_t)(NQ + k) * F + f] = sr;
   }
 }
 
@@ -122,8 +160,9 @@ __global__ void __launch_bounds__(128) k_adj_face(DevMesh m, ResParams P, const 
 // (max: slot k, min: slot NQ + k) the neighbour cell that attained it
 // (aSrc, -1 for none) and the adjoint it receives (aVal).
 template <int LIMITED>
-__global__ void __launch_bounds__(128) k_adj_lim(DevMesh m, unsigned mask, const double* __restrict__ q,
-                                                 const double* __restrict__ bq, const double* __restrict__ aF,
+__global__ void __launch_bounds__(128) k_adj_lim(DevMesh m, unsigned mask, unsigned tvd,
+                                                 const double* __restrict__ q, const double* __restrict__ bq,
+                                                 const double* __restrict__ aF, const double* __restrict__ aS,
                                                  double* __restrict__ aQ, double* __restrict__ aG,
                                                  int* __restrict__ aSrc, double* __restrict__ aVal) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -141,7 +180,12 @@ __global__ void __launch_bounds__(128) k_adj_lim(DevMesh m, unsigned mask, const
       const int f = isOwn ? code : ~code;
       const double a = aF[(size_t)(isOwn ? k : NQ + k) * F + f];
       qd += a;
-      if (hasGrad) {
+      if (hasGrad && ((tvd >> k) & 1)) {  // TVD: the upwind gradient's projection on C_nei - C_own
+        const double sa = aS[(size_t)(isOwn ? k : NQ + k) * F + f];
+        gb[0] += sa * m.dCC[f];
+        gb[1] += sa * m.dCC[F + f];
+        gb[2] += sa * m.dCC[2 * F + f];
+      } else if (hasGrad) {  // linearUpwind: the extrapolation d . g from the cell to the face
         const double* d = isOwn ? m.dOwn : m.dNei;
         gb[0] += a * d[f];
         gb[1] += a * d[F + f];
@@ -394,6 +438,7 @@ static void ensure_adjoint(Handle& h) {
     return p;
   };
   h.aF = (double*)dal(2 * NQ * F * sizeof(double));
+  h.aS = (double*)dal(2 * NQ * F * sizeof(double));
   h.aQ = (double*)dal(NQ * N * sizeof(double));
   h.aG = (double*)dal(3 * NQ * N * sizeof(double));
   h.aSrc = (int*)dal(2 * NQ * N * sizeof(int));
@@ -403,10 +448,6 @@ static void ensure_adjoint(Handle& h) {
 std::string residual_vjp_unsupported(const Handle& h) {
   if (h.cfg.c.viscous) return "the reverse-mode residual derivative does not cover viscous terms";
   if (h.m.ncyc > 0) return "the reverse-mode residual derivative does not cover cyclic patches";
-  const int rs[3] = {h.cfg.c.recon_rho, h.cfg.c.recon_U, h.cfg.c.recon_T};
-  for (int r : rs)
-    if (r == ICS_RECON_VANLEER || r == ICS_RECON_MINMOD)
-      return "the reverse-mode residual derivative covers upwind and linearUpwind (MUSCL) reconstruction only";
   return "";
 }
 
@@ -420,24 +461,31 @@ void launch_residual_vjp(Handle& h, const double* u, double* out) {
   launch_grad(h);
   int limited = 0;
   const unsigned mask = grad_mask(h, &limited);
+  // fields reconstructed by a TVD limitedScheme (their gradient is unlimited)
+  unsigned tvd = 0;
+  for (int k = 0; k < NQ; ++k) {
+    const int sch = k == Q_RHO || k == Q_P ? h.cfg.c.recon_rho
+                                           : (k >= Q_UX && k <= Q_UZ ? h.cfg.c.recon_U : h.cfg.c.recon_T);
+    if (sch == ICS_RECON_VANLEER || sch == ICS_RECON_MINMOD) tvd |= 1u << k;
+  }
   if (h.m.F > 0) {
     if (h.m.mrfU)
       ICS_LAUNCH(h, ICS_K_ADJOINT, (k_adj_face<true><<<grid_for(h.m.F, 128), 128, 0, h.stream>>>(
-                                       h.m, P, h.q, h.grad, u, h.aF)));
+                                       h.m, P, h.q, h.grad, u, h.aF, h.aS)));
     else
       ICS_LAUNCH(h, ICS_K_ADJOINT, (k_adj_face<false><<<grid_for(h.m.F, 128), 128, 0, h.stream>>>(
-                                       h.m, P, h.q, h.grad, u, h.aF)));
+                                       h.m, P, h.q, h.grad, u, h.aF, h.aS)));
   }
   const int N = h.m.N;
   if (limited == 2)
     ICS_LAUNCH(h, ICS_K_ADJOINT, k_adj_lim<2><<<grid_for(N, 128), 128, 0, h.stream>>>(
-                                     h.m, mask, h.q, h.bq, h.aF, h.aQ, h.aG, h.aSrc, h.aVal));
+                                     h.m, mask, tvd, h.q, h.bq, h.aF, h.aS, h.aQ, h.aG, h.aSrc, h.aVal));
   else if (limited == 1)
     ICS_LAUNCH(h, ICS_K_ADJOINT, k_adj_lim<1><<<grid_for(N, 128), 128, 0, h.stream>>>(
-                                     h.m, mask, h.q, h.bq, h.aF, h.aQ, h.aG, h.aSrc, h.aVal));
+                                     h.m, mask, tvd, h.q, h.bq, h.aF, h.aS, h.aQ, h.aG, h.aSrc, h.aVal));
   else
     ICS_LAUNCH(h, ICS_K_ADJOINT, k_adj_lim<0><<<grid_for(N, 128), 128, 0, h.stream>>>(
-                                     h.m, mask, h.q, h.bq, h.aF, h.aQ, h.aG, h.aSrc, h.aVal));
+                                     h.m, mask, tvd, h.q, h.bq, h.aF, h.aS, h.aQ, h.aG, h.aSrc, h.aVal));
   double dgPhys = 0.0;
   if (h.cfg.c.ddt_scheme == ICS_DDT_EULER) dgPhys = 1.0 / h.cfg.c.delta_t;
   if (h.cfg.c.ddt_scheme == ICS_DDT_BACKWARD) {

@@ -27,6 +27,26 @@ __device__ __forceinline__ int recon_of(const ResParams& P, int q) {
   return P.reconT;
 }
 
+// TVD limitedScheme face value from the two cell values and the upwind
+// cell's gradient projected on C_nei - C_own (NVD/TVD r with vanLeer or Minmod)
+template <typename Real, typename GT>
+__device__ __forceinline__ Real tvd_face(int scheme, double wf, double wUp, const Real& qo, const Real& qn,
+                                         const GT& gradcf) {
+  const Real gradf = qn - qo;
+  Real r;
+  if (fabs(gradcf) >= 1000 * fabs(gradf))
+    r = 2 * 1000 * (gradcf >= 0 ? 1.0 : -1.0) * (gradf >= 0 ? 1.0 : -1.0) - 1.0;
+  else
+    r = 2 * (gradcf / gradf) - 1;
+  Real lim;
+  if (scheme == ICS_RECON_VANLEER)
+    lim = (r + fabs(r)) / (1 + fabs(r));
+  else
+    lim = fmax(fmin(fmin(r, 1.0), 2.0), 0.0);
+  const Real wgt = lim * wf + (1.0 - lim) * wUp;
+  return wgt * (qo - qn) + qn;
+}
+
 // reconstruct field k on face f for direction dir (+1 owner side, -1 neighbour side)
 template <typename Real>
 __device__ __forceinline__ Real reconstruct(const DevMesh& m, int scheme, int k, int f, int o, int nb, const Real& qo,
@@ -37,20 +57,8 @@ __device__ __forceinline__ Real reconstruct(const DevMesh& m, int scheme, int k,
   if (scheme == ICS_RECON_VANLEER || scheme == ICS_RECON_MINMOD) {
     const int c = dir > 0 ? o : nb;
     const double d0 = m.dCC[f], d1 = m.dCC[F + f], d2 = m.dCC[2 * F + f];
-    const Real gradf = qn - qo;
     const Real gradcf = d0 * grad[(3 * k) * N + c] + d1 * grad[(3 * k + 1) * N + c] + d2 * grad[(3 * k + 2) * N + c];
-    Real r;
-    if (fabs(gradcf) >= 1000 * fabs(gradf))
-      r = 2 * 1000 * (gradcf >= 0 ? 1.0 : -1.0) * (gradf >= 0 ? 1.0 : -1.0) - 1.0;
-    else
-      r = 2 * (gradcf / gradf) - 1;
-    Real lim;
-    if (scheme == ICS_RECON_VANLEER)
-      lim = (r + fabs(r)) / (1 + fabs(r));
-    else
-      lim = fmax(fmin(fmin(r, 1.0), 2.0), 0.0);
-    const Real wgt = lim * m.w[f] + (1.0 - lim) * wUp;
-    return wgt * (qo - qn) + qn;
+    return tvd_face(scheme, m.w[f], wUp, qo, qn, gradcf);
   }
   // MUSCL: upwind value + limited-gradient extrapolation; the neighbour
   // side's upwind value 0 (qo - qn) + qn is qn itself

@@ -384,10 +384,10 @@ int ics_vjp(ics_handle h, const double* u, double* JTu, int32_t device);
  * the state in the backward pass (the flux's local partial derivatives by
  * dual numbers through the same flux function).  Equal to ics_vjp up to
  * round-off, and the exact transpose of ics_jvp's map.  Covers the inviscid
- * residual with upwind or linearUpwind (MUSCL) reconstruction, all three
- * flux schemes, the physical ddt, MRF zones and Harmonic Balance; returns
- * ICS_ERR_ARG for viscous cases, cyclic patches and the TVD limitedScheme
- * reconstructions.  Pointers as in ics_jvp.                                 */
+ * residual with every reconstruction (upwind, the TVD limitedSchemes,
+ * linearUpwind with cellLimited gradients), all three flux schemes, the
+ * physical ddt, MRF zones and Harmonic Balance (zones, cylCoords); returns
+ * ICS_ERR_ARG for viscous cases and cyclic patches.  Pointers as in ics_jvp. */
 int ics_vjp_recompute(ics_handle h, const double* u, double* JTu, int32_t device);
 /* ---- Krylov solves with the exact residual derivative (no counterpart in
  * the reference, whose linear solves use the approximate Jacobian) ------- */

@@ -522,46 +522,101 @@ def run_hb_sweep(instances=(3, 5, 7, 9), per=(32, 64, 128), steps=5, warmup=2):
     return out
 
 
-def run_batch(n_cases=64, steps=5, warmup=2, seed=2):
-    """64 independent shock-tube cases (Sod, AUSM+up, backward dual-time ddt), N ~ U[2000, 50000]
-    (seeded): one pseudo iteration of all of them per step, concurrently (ics_pseudo_iteration_batch)
-    and one after another (the reference's way)."""
+def run_batch(n_cases=64, steps=3, seed=2, precision=1):
+    """64 independent shock-tube cases (Sod, AUSM+up, backward dual-time ddt, pseudo CFL 50,
+    GMRES(8)+LU-SGS), N ~ U[2000, 50000] (seeded), `steps` physical time steps, each case
+    pseudo-iterating until its own pseudotimeControl completes; three ways: one after another
+    (the reference's way), handles iterated concurrently from host threads
+    (ics_pseudo_iteration_batch), and all cases stacked in one handle (ics_set_cases: one
+    launch sequence per pseudo iteration for every case).  cell-iters/s counts each case's own
+    pseudo iterations (identical in the three runs, which the leg checks); a warm-up time step
+    first, on fresh handles."""
     import numpy as np
 
     from icsfoam_gb300 import abi, cases, gpu
 
     b = gpu.binding()
-    rng = np.random.default_rng(seed)
-    sizes = rng.integers(2000, 50001, n_cases)
-    hs, total = [], 0
-    for n in sizes:
-        w = cases.shock_tube(int(n), ordering_mode="colour")
-        h = gpu.open_case(w.mesh, cases.make_config(b, w.settings, precision=1))
-        h.set_primitive(w.p, w.U, w.T)
-        h.begin_time_step()
-        hs.append(h)
-        total += w.mesh.n_cells
-    for _ in range(warmup):
-        for h in hs:
-            h.pseudo_loop()
-        abi.pseudo_iteration_batch(hs)
+    ws = cases.shock_tube_batch(n_cases, seed=seed)
+    cells = np.array([w.mesh.n_cells for w in ws])
+
+    def handles():
+        hs = []
+        for w in ws:
+            h = gpu.open_case(w.mesh, cases.make_config(b, w.settings, precision=precision))
+            h.set_primitive(w.p, w.U, w.T)
+            hs.append(h)
+        return hs
+
+    def sequential(hs, nsteps):
+        its = np.zeros(n_cases, int)
+        for k, h in enumerate(hs):
+            for _ in range(nsteps):
+                h.begin_time_step()
+                while h.pseudo_loop():
+                    h.pseudo_iteration()
+                    its[k] += 1
+        return its
+
+    def concurrent(hs, nsteps):
+        its = np.zeros(n_cases, int)
+        for _ in range(nsteps):
+            for h in hs:
+                h.begin_time_step()
+            live = list(range(n_cases))
+            while True:
+                live = [k for k in live if hs[k].pseudo_loop()]
+                if not live:
+                    break
+                abi.pseudo_iteration_batch([hs[k] for k in live])
+                its[live] += 1
+        return its
+
+    wst, start = cases.stack_cases(ws)
+    hst = gpu.open_case(wst.mesh, cases.make_config(b, wst.settings, precision=precision))
+    hst.set_cases(start)
+    hst.set_primitive(wst.p, wst.U, wst.T)
+
+    def stacked(nsteps):
+        its = np.zeros(n_cases, int)
+        for _ in range(nsteps):
+            hst.begin_time_step()
+            while hst.pseudo_loop():
+                live = ~hst.case_stats()["frozen"]
+                hst.pseudo_iteration()
+                its[live] += 1
+        return its
+
+    out = {"cases": n_cases, "kind": "Sod shock tubes, 1D, colour-blocked, AUSM+up first order, backward ddt",
+           "cells": int(cells.sum()), "time_steps": steps, "precision": "mixed" if precision else "fp64"}
+    stacked(1)  # warm-up: graph capture, first launches
     t0 = time.perf_counter()
-    for _ in range(steps):
-        for h in hs:
-            h.pseudo_loop()
-        abi.pseudo_iteration_batch(hs)
-    conc = time.perf_counter() - t0
+    its_st = stacked(steps)
+    t_st = time.perf_counter() - t0
+    hst.close()
+    hs = handles()
+    concurrent(hs, 1)
     t0 = time.perf_counter()
-    for _ in range(steps):
-        for h in hs:
-            h.pseudo_loop()
-            h.pseudo_iteration()
-    seq = time.perf_counter() - t0
+    its_co = concurrent(hs, steps)
+    t_co = time.perf_counter() - t0
     for h in hs:
         h.close()
-    return {"cases": n_cases, "kind": "Sod shock tubes, 1D, colour-blocked", "cells": int(total),
-            "concurrent_cell_iters_per_s": total * steps / conc,
-            "sequential_cell_iters_per_s": total * steps / seq, "speedup": seq / conc}
+    hs = handles()
+    sequential(hs, 1)
+    t0 = time.perf_counter()
+    its_se = sequential(hs, steps)
+    t_se = time.perf_counter() - t0
+    for h in hs:
+        h.close()
+    work = float((cells * its_st).sum())
+    out.update({
+        "pseudo_iterations_per_case": [int(its_st.min()), int(its_st.max())],
+        "same_iterations_all_modes": bool(np.array_equal(its_st, its_co) and np.array_equal(its_st, its_se)),
+        "stacked_cell_iters_per_s": work / t_st,
+        "concurrent_cell_iters_per_s": float((cells * its_co).sum()) / t_co,
+        "sequential_cell_iters_per_s": float((cells * its_se).sum()) / t_se,
+        "stacked_s": t_st, "concurrent_s": t_co, "sequential_s": t_se,
+        "stacked_over_sequential": t_se / t_st, "stacked_over_concurrent": t_co / t_st})
+    return out
 
 
 def run_viscous_box(n=96, steps=10, warmup=3):

@@ -175,6 +175,10 @@ _MEASURE["linear_residual_noalloc"] = (C.c_int, [_P, _P, _P, _P])
 # independent cases iterated concurrently (CUDA library only)
 _MEASURE["pseudo_iteration_batch"] = (C.c_int, [_P, C.c_int32, _P, _P])
 
+# independent cases stacked in one handle (CUDA library only)
+_MEASURE["set_cases"] = (C.c_int, [_P, C.c_int32, _P])
+_MEASURE["case_stats"] = (C.c_int, [_P, _P, _P, _P])
+
 # bounded-wait probe (CUDA library only)
 _MEASURE["test_sweep_timeout"] = (C.c_int, [_P, C.c_int32, C.c_int32])
 
@@ -438,6 +442,23 @@ class CaseHandle:
 
     def begin_time_step(self):
         self._check(self.b.fn["begin_time_step"](self.h), "begin_time_step")
+
+    def set_cases(self, case_start):
+        """Declare the handle's mesh a stack of independent cases: case k owns
+        cells case_start[k] .. case_start[k+1]-1 (see cases.stack_cases)."""
+        cs = np.ascontiguousarray(case_start, np.int32)
+        self._check(self.b.fn["set_cases"](self.h, len(cs) - 1, _ptr(cs)), "set_cases")
+        self.n_cases = len(cs) - 1
+
+    def case_stats(self):
+        """Per stacked case: rho L2 residual of the last residual, GMRES
+        restart cycles of the last solve, and whether the case is frozen."""
+        n = self.n_cases
+        l2 = np.zeros(n)
+        cyc = np.zeros(n, np.int32)
+        fr = np.zeros(n, np.int32)
+        self._check(self.b.fn["case_stats"](self.h, _ptr(l2), _ptr(cyc), _ptr(fr)), "case_stats")
+        return {"rho_l2": l2, "gmres_cycles": cyc, "frozen": fr.astype(bool)}
 
     def set_hb(self, n_instances: int, D):
         D = np.ascontiguousarray(D, np.float64).reshape(n_instances, n_instances)

@@ -320,3 +320,23 @@ def make_config(binding, settings: Dict, **overrides):
     for k, v in dict(settings, **overrides).items():
         setattr(cfg, k, v)
     return cfg
+
+
+def stack_cases(workloads) -> "tuple[Workload, np.ndarray]":
+    """Independent cases as one stacked workload (mesh.stack) with the case
+    offsets for CaseHandle.set_cases.  The cases share one solver
+    configuration: the first workload's settings."""
+    mesh, start = M.stack([w.mesh for w in workloads])
+    w0 = workloads[0]
+    cat = lambda f: np.concatenate([f(w) for w in workloads])
+    w = Workload("stack_%d" % len(workloads), mesh, cat(lambda w: w.p), cat(lambda w: w.U), cat(lambda w: w.T),
+                 dict(w0.settings))
+    return w, start
+
+
+def shock_tube_batch(n_cases: int = 64, seed: int = 2, low: int = 2000, high: int = 50000, ordering_mode="colour"):
+    """The many-small-cases batch: Sod shock tubes with cell counts drawn
+    uniformly from [low, high] (seeded), each over x in [-5, 5]."""
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(low, high + 1, n_cases)
+    return [shock_tube(int(n), ordering_mode=ordering_mode) for n in sizes]

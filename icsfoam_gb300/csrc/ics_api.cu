@@ -111,6 +111,7 @@ void free_all(Handle& h) {
                   h.ibuf};
   drop_graphs(h);
   free_exact(h);
+  free_cases(h);
   for (void* p : ptrs) dfree(p);
   for (cudaEvent_t e : h.evPool) cudaEventDestroy(e);
   if (h.tStart) cudaEventDestroy(h.tStart);
@@ -522,7 +523,23 @@ int do_residual(Handle& h, double* host_src) {
   // SER (setCoAndDeltaT.H:3-37) from the last two linear-solver initial residuals
   double ratio = 1.0;
   bool apply = false;
-  if (h.initResValid) {
+  if (h.cases.n) {
+    // per case, as its own handle would (frozen cases: none)
+    CaseSet& S = h.cases;
+    for (int k = 0; k < S.n; ++k) {
+      S.hser[k] = -1.0;
+      if (S.frozen[k] || !S.initValid[k]) continue;
+      const std::vector<double> in(&S.initRes[5 * k], &S.initRes[5 * k] + 5);
+      if (S.ctl[k].corr != 1 && S.prevValid[k]) {
+        const std::vector<double> pr(&S.prevRes[5 * k], &S.prevRes[5 * k] + 5);
+        double r = residual_norm(pr) / residual_norm(in);
+        S.hser[k] = std::max(std::min(r, h.cfg.c.pseudo_co_max_increase), h.cfg.c.pseudo_co_min_decrease);
+      }
+      std::copy(in.begin(), in.end(), &S.prevRes[5 * k]);
+      S.prevValid[k] = 1;
+    }
+    case_upload_ser(h);
+  } else if (h.initResValid) {
     const bool firstIter = h.ctl[0].corr == 1;
     if (!firstIter && h.prevResValid) {
       ratio = residual_norm(h.prevRes) / residual_norm(h.initRes);
@@ -547,6 +564,7 @@ int do_residual(Handle& h, double* host_src) {
   launch_residual(h, ratio, apply);
   h.haveFlux = true;
   h.lastRhoL2 = rho_l2(h);
+  if (h.cases.n) case_l2(h);
   if (host_src) {
     ICS_CUDA(cudaMemcpyAsync(host_src, h.src, 5ull * h.m.N * sizeof(double), cudaMemcpyDeviceToHost, h.stream));
     ICS_CUDA(cudaStreamSynchronize(h.stream));
@@ -592,6 +610,31 @@ int do_solve(Handle& h, ics_solver_perf* perf) {
   ensure_workspace(h);
   ICS_CUDA(cudaMemcpyAsync(h.Wprev, h.W, 5ull * h.m.N * sizeof(double), cudaMemcpyDeviceToDevice, h.stream));
   ics_solver_perf p;
+  if (h.cases.n) {
+    CaseSet& S = h.cases;
+    std::vector<int> cst;
+    int st = gmres_cases(h, cst);
+    std::memset(&p, 0, sizeof(p));
+    for (int k = 0; k < 5; ++k) p.init_res[k] = p.final_res[k] = -VGREAT;
+    bool conv = true;
+    for (int k = 0; k < S.n; ++k) {
+      if (S.frozen[k]) continue;
+      S.initValid[k] = 1;
+      std::memcpy(S.ctl[k].residuals, &S.initRes[5 * k], 5 * sizeof(double));
+      for (int j = 0; j < 5; ++j) {
+        p.init_res[j] = std::max(p.init_res[j], S.initRes[5 * k + j]);
+        p.final_res[j] = std::max(p.final_res[j], S.finRes[5 * k + j]);
+      }
+      p.n_iterations = std::max(p.n_iterations, S.cycles[k]);
+      if (cst[k] == ICS_ERR_NONFINITE && st == ICS_OK) st = ICS_ERR_NONFINITE;
+      conv = conv && cst[k] == ICS_OK;
+    }
+    p.converged = conv && st == ICS_OK;
+    h.haveIncrement = true;
+    if (perf) *perf = p;
+    if (st) h.err = st == ICS_ERR_TIMEOUT ? "LU-SGS sweep wait gave up" : "non-finite Krylov residual in a case";
+    return st;
+  }
   const int st = gmres_solve(h, &p, h.initRes);
   h.haveIncrement = true;
   h.initResValid = true;
@@ -771,6 +814,10 @@ int ics_set_config(ics_handle hh, const ics_config* cfg) {
   }
   if (hh->h.m.nInst > 1 && (cfg->ddt_scheme != ICS_DDT_STEADY || cfg->solver != ICS_SOLVER_GMRES)) {
     hh->h.err = "Harmonic Balance needs steadyState ddt and the GMRES solver";
+    return ICS_ERR_ARG;
+  }
+  if (hh->h.cases.n && cfg->solver != ICS_SOLVER_GMRES) {
+    hh->h.err = "stacked cases need the GMRES solver";
     return ICS_ERR_ARG;
   }
 
@@ -1051,6 +1098,29 @@ int ics_pseudo_iteration(ics_handle hh, ics_iter_stats* stats) {
   });
 }
 
+int ics_set_cases(ics_handle hh, int32_t n_cases, const int32_t* case_start) {
+  return guard(hh, [&](Handle& h) {
+    set_cases(h, n_cases, case_start);
+    return ICS_OK;
+  });
+}
+
+int ics_case_stats(ics_handle hh, double* rho_l2_out, int32_t* gmres_cycles, int32_t* frozen) {
+  return guard(hh, [&](Handle& h) {
+    const CaseSet& S = h.cases;
+    if (!S.n) {
+      h.err = "the handle holds no stacked cases";
+      return ICS_ERR_STATE;
+    }
+    for (int k = 0; k < S.n; ++k) {
+      if (rho_l2_out) rho_l2_out[k] = std::sqrt(S.hl2[k]);
+      if (gmres_cycles) gmres_cycles[k] = S.cycles[k];
+      if (frozen) frozen[k] = S.frozen[k];
+    }
+    return ICS_OK;
+  });
+}
+
 int ics_pseudo_iteration_batch(ics_handle* hs, int32_t n, ics_iter_stats* stats, int32_t* status) {
   if (!hs || n < 0) return ICS_ERR_ARG;
   for (int i = 0; i < n; ++i)
@@ -1099,7 +1169,10 @@ int ics_begin_time_step(ics_handle hh) {
     if (!steady) {
       h.initResValid = false;
       h.prevResValid = false;
+      std::fill(h.cases.initValid.begin(), h.cases.initValid.end(), 0);
+      std::fill(h.cases.prevValid.begin(), h.cases.prevValid.end(), 0);
     }
+    std::fill(h.cases.frozen.begin(), h.cases.frozen.end(), 0);
     if (h.cfg.c.reset_pseudo) {
       std::vector<double> co(h.m.N, h.cfg.c.pseudo_co_num);
       ICS_CUDA(cudaMemcpyAsync(h.pseudoCo, co.data(), co.size() * sizeof(double), cudaMemcpyHostToDevice, h.stream));
@@ -1312,6 +1385,10 @@ int ics_checkpoint_size(ics_handle hh, int64_t* bytes) {
 int ics_save_checkpoint(ics_handle hh, void* buf, int64_t bytes) {
   if (!hh || !buf) return ICS_ERR_ARG;
   return guard(hh, [&](Handle& h) {
+    if (h.cases.n) {
+      h.err = "checkpoints do not carry the per-case controls of stacked cases";
+      return ICS_ERR_ARG;
+    }
     int64_t need = 0;
     ics_checkpoint_size(hh, &need);
     if (bytes < need) {
@@ -1366,6 +1443,10 @@ int ics_scalar_enable(ics_handle hh, const double* s, const int32_t* patch_fixed
   if (!hh || !s || recon < 0 || recon > ICS_RECON_MUSCL_MINMOD || !(D >= 0)) return ICS_ERR_ARG;
   if (hh->h.m.nInst > 1) {
     hh->h.err = "scalar transport is not provided for Harmonic Balance handles";
+    return ICS_ERR_ARG;
+  }
+  if (hh->h.cases.n) {
+    hh->h.err = "stacked cases carry no passive scalar";
     return ICS_ERR_ARG;
   }
   if (hh->h.m.ncyc > 0 && hh->h.cfg.c.viscous) {
@@ -1674,6 +1755,20 @@ int ics_pseudo_loop(ics_handle hh, int32_t* more) {
   return guard(hh, [&](Handle& h) {
     // every instance's control advances (no short cut); more while any runs
     bool any = false;
+    if (h.cases.n) {
+      // stacked cases: a case whose loop completes stays frozen until all have
+      CaseSet& S = h.cases;
+      for (int k = 0; k < S.n; ++k) {
+        if (S.frozen[k]) continue;
+        if (pseudo_loop_one(h, S.ctl[k]))
+          any = true;
+        else
+          S.frozen[k] = 1;
+      }
+      if (!any) std::fill(S.frozen.begin(), S.frozen.end(), 0);
+      *more = any ? 1 : 0;
+      return ICS_OK;
+    }
     for (auto& q : h.ctl) any = pseudo_loop_one(h, q) || any;
     *more = any ? 1 : 0;
     return ICS_OK;
@@ -1689,6 +1784,10 @@ int ics_set_hb(ics_handle hh, int32_t n, const double* D) {
   }
   if (h0.m.N % n != 0) {
     h0.err = "cell count is not a multiple of the number of instances";
+    return ICS_ERR_ARG;
+  }
+  if (n > 1 && h0.cases.n) {
+    h0.err = "stacked cases are not combined with Harmonic Balance";
     return ICS_ERR_ARG;
   }
   if (n > 1 && (h0.cfg.c.ddt_scheme != ICS_DDT_STEADY || h0.cfg.c.solver != ICS_SOLVER_GMRES)) {

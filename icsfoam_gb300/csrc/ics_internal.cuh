@@ -155,6 +155,67 @@ struct DevMesh {
   double* mrfBU = nullptr;
   int* mrfBIn = nullptr;
   int mrfEvery = 0;
+  // independent cases stacked in one mesh (nullptr otherwise): case of each
+  // cell [N] and each case's SER factor [n_cases] (< 0: not applied)
+  const int* caseOf = nullptr;
+  const double* caseSer = nullptr;
+};
+
+// pseudotimeControl state (pseudotimeControl.C): the iteration count of the
+// current time step, convergence flags and the last / first residuals
+struct PseudoControl {
+  int corr = 0;
+  bool converged = false, firstIteration = true;
+  double residuals[5] = {0, 0, 0, 0, 0}, initResiduals[5] = {0, 0, 0, 0, 0};
+};
+
+// Device view of the stacked cases' per-case state (ics_set_cases): the
+// reduction segments (block b reduces cells segBeg[b] .. segEnd[b]-1 of case
+// segCase[b]; case k owns segments caseSeg[k] .. caseSeg[k+1]-1), and per
+// case its Krylov scalars with a Hessenberg of m x m.
+struct CaseDev {
+  int n = 0, m = 0;
+  const int* segCase = nullptr;
+  const int* segBeg = nullptr;
+  const int* segEnd = nullptr;
+  const int* caseSeg = nullptr;
+  const int* start = nullptr;     // [n+1] cells
+  const int* active = nullptr;    // [n] 1: the case takes part in this solve
+  double* partials = nullptr;     // [nseg][8]
+  unsigned int* counter = nullptr;  // [n]
+  double* H = nullptr;            // [n][m*m]
+  double* c = nullptr;            // [n][m]
+  double* s = nullptr;            // [n][m]
+  double* bh = nullptr;           // [n][m+1]
+  double* y = nullptr;            // [n][m]
+  double* beta = nullptr;         // [n]
+  double* red = nullptr;          // [n][2]
+  double* res = nullptr;          // [n][5] L1 residual sums
+  double* nfr = nullptr;          // [n][8] norm-factor and |b| sums
+  double* avg = nullptr;          // [n][5] averages of W
+  double* l2 = nullptr;           // [n] sums of (R_rho V)^2
+  int* status = nullptr;          // [n] breakdown / non-finite flags
+};
+
+struct CaseSet {
+  int n = 0, nseg = 0;
+  std::vector<int> start;          // host [n+1]
+  CaseDev d;
+  int* caseOf = nullptr;           // device [N]
+  double* ser = nullptr;           // device [n]
+  void* mem = nullptr;             // one device allocation behind d's arrays
+  // pinned host mirrors of res, nfr, l2, status, active
+  double* hres = nullptr;
+  double* hnfr = nullptr;
+  double* hl2 = nullptr;
+  int* hstatus = nullptr;
+  int* hactive = nullptr;
+  double* hser = nullptr;
+  // host bookkeeping per case (what a handle of its own keeps)
+  std::vector<PseudoControl> ctl;
+  std::vector<double> initRes, prevRes, finRes;  // [5n]
+  std::vector<char> initValid, prevValid, frozen;
+  std::vector<int> cycles;
 };
 
 struct Cfg {
@@ -227,11 +288,7 @@ struct Handle {
   bool initResValid = false, prevResValid = false;
   std::vector<double> initRes, prevRes;
   // one pseudotimeControl per instance (the HB solver loops while any runs)
-  struct Control {
-    int corr = 0;
-    bool converged = false, firstIteration = true;
-    double residuals[5] = {0, 0, 0, 0, 0}, initResiduals[5] = {0, 0, 0, 0, 0};
-  };
+  using Control = PseudoControl;
   std::vector<Control> ctl = std::vector<Control>(1);
   double lastRhoL2 = 0;
   // residual tangent (Jacobian-vector product) workspace of dual numbers
@@ -305,6 +362,8 @@ struct Handle {
   cudaGraphExec_t cycleExec = nullptr;
   int cycleKey = -1;
   long long cycleLaunches = 0;
+  // independent cases stacked in this handle (ics_set_cases); n == 0: off
+  CaseSet cases;
 };
 
 inline void drop_graphs(Handle& h) {
@@ -362,6 +421,17 @@ void free_exact(Handle& h);
 void assemble_exact(Handle& h);
 void exact_vjp(Handle& h, const double* u, double* y);
 void exact_jvp(Handle& h, const double* x, double* y);
+
+// independent cases stacked in one handle (k_cases.cu): set up the per-case
+// reductions and state, release them, one GMRES solve of every active case
+// (caseStatus [n]: ICS_OK, ICS_ERR_BREAKDOWN or ICS_ERR_NONFINITE per case;
+// the return value reports a sweep that gave up), the per-case rho L2 sums
+// of the last residual (host mirror) and the SER factors' upload
+void set_cases(Handle& h, int n, const int* start);
+void free_cases(Handle& h);
+int gmres_cases(Handle& h, std::vector<int>& caseStatus);
+void case_l2(Handle& h);
+void case_upload_ser(Handle& h);
 
 // linear algebra: precision-dispatched (mixed = FP32 blocks and vectors)
 void spmv(Handle& h, const void* x, void* y);

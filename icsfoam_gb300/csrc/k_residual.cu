@@ -604,8 +604,10 @@ __global__ void __launch_bounds__(128) k_cellres(DevMesh m, CellResParams D, con
     for (int k = 0; k < 3; ++k) src[5 * c + 1 + k] -= cr[k] * Vc;
   }
   double co = pseudoCo[c];
-  if (D.applySer) {
-    co *= D.serRatio;
+  // stacked independent cases: each case's own SER factor (< 0: none)
+  const double ser = m.caseSer ? m.caseSer[m.caseOf[c]] : D.serRatio;
+  if (m.caseSer ? ser >= 0.0 : D.applySer) {
+    co *= ser;
     co = fmax(fmin(co, D.coMax), D.coMin);
     pseudoCo[c] = co;
   }

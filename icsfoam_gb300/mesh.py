@@ -522,3 +522,42 @@ def cell_faces_csr(mesh: Mesh) -> Tuple[np.ndarray, np.ndarray]:
     np.add.at(ptr, cells + 1, 1)
     ptr = np.cumsum(ptr)
     return ptr.astype(np.int32), codes[order].astype(np.int32)
+
+
+def stack(meshes: Sequence[Mesh]) -> Tuple[Mesh, np.ndarray]:
+    """The disjoint union of independent meshes as one mesh (case-major cell
+    numbering: mesh k's cells follow those of meshes 0..k-1, each in its own
+    order) and the case offsets start[k] (n_cases + 1 entries).  Each mesh's
+    patches are kept as patches of their own, named ``<name>_<k>``; internal
+    faces keep each mesh's order, so the owner-ordered face list and every
+    cell's face order are those of the mesh alone."""
+    if not meshes:
+        raise ValueError("no meshes to stack")
+    sd = meshes[0].solution_d
+    if any(m.solution_d != sd for m in meshes):
+        raise ValueError("stacked meshes must share their solution directions")
+    if any(m.b_partner is not None and np.any(m.b_partner >= 0) for m in meshes):
+        raise ValueError("stacked meshes carry no cyclic patches")
+    start = np.zeros(len(meshes) + 1, np.int32)
+    start[1:] = np.cumsum([m.n_cells for m in meshes])
+    poff = np.cumsum([0] + [len(m.patches) for m in meshes])
+    cat = lambda f: np.concatenate([f(m) for m in meshes])
+    pats: List[Patch] = []
+    for k, m in enumerate(meshes):
+        for p in m.patches:
+            q = dataclasses.replace(p, name="%s_%d" % (p.name, k))
+            pats.append(q)
+    st = dataclasses.replace(
+        meshes[0],
+        n_cells=int(start[-1]),
+        owner=np.concatenate([m.owner + start[k] for k, m in enumerate(meshes)]).astype(np.int32),
+        neighbour=np.concatenate([m.neighbour + start[k] for k, m in enumerate(meshes)]).astype(np.int32),
+        Sf=cat(lambda m: m.Sf), Cf=cat(lambda m: m.Cf), weights=cat(lambda m: m.weights),
+        delta_coeffs=cat(lambda m: m.delta_coeffs), nonorth_delta_coeffs=cat(lambda m: m.nonorth_delta_coeffs),
+        C=cat(lambda m: m.C), V=cat(lambda m: m.V),
+        b_cell=np.concatenate([m.b_cell + start[k] for k, m in enumerate(meshes)]).astype(np.int32),
+        b_Sf=cat(lambda m: m.b_Sf), b_Cf=cat(lambda m: m.b_Cf), b_delta_coeffs=cat(lambda m: m.b_delta_coeffs),
+        b_patch=np.concatenate([m.b_patch + poff[k] for k, m in enumerate(meshes)]).astype(np.int32),
+        patches=pats, points=None, face_points=None, b_face_points=None, cell_ijk=None, b_partner=None,
+        b_weights=None, b_nbr_d=None, b_nonorth_delta_coeffs=None)
+    return st, start

@@ -249,6 +249,28 @@ int ics_pseudo_iteration(ics_handle h, ics_iter_stats* stats);
  * non-OK one.  The handles must be distinct.  (The reference runs such cases
  * one after another.)                                                        */
 int ics_pseudo_iteration_batch(ics_handle* handles, int32_t n, ics_iter_stats* stats, int32_t* status);
+/* Independent cases stacked in one handle (the many-small-cases batch as a
+ * leading dimension): the handle's mesh is the union of n_cases meshes whose
+ * cells case_start[k] .. case_start[k+1]-1 belong to case k (case_start
+ * [n_cases+1], increasing, from 0 to n_cells) and no internal face joins two
+ * cases.  Every kernel of a pseudo iteration then runs once over all cases,
+ * while each case keeps what a handle of its own would have: its GMRES
+ * (Hessenberg, Givens rotations, stop test coupledMatrixSolver.C:198-221 and
+ * norm factors gmres.C:812-850), its SER pseudo Courant number
+ * (setCoAndDeltaT.H:3-37) and its pseudotimeControl (pseudotimeControl.C:
+ * 159-241): ics_pseudo_loop reports more work while any case runs, and a case
+ * whose loop has completed is frozen (no update) until every case has
+ * completed, after which the next call starts the next time step for all.
+ * The dot products of case k reduce over segments that depend only on its own
+ * cell count, so a case's results do not depend on the other cases in the
+ * stack.  Call once, before the first residual.  Not with Harmonic Balance,
+ * cyclic patches or the block-Jacobi smoother solver (ICS_ERR_ARG).
+ * (CUDA library.)                                                            */
+int ics_set_cases(ics_handle h, int32_t n_cases, const int32_t* case_start);
+/* Per case of a stacked handle, each array [n_cases] and optional: the L2 norm
+ * of R_rho V of the last residual (dbnsFoam.C:136-138), the GMRES restart
+ * cycles of the last linear solve, and 1 while the case is frozen.         */
+int ics_case_stats(ics_handle h, double* rho_l2, int32_t* gmres_cycles, int32_t* frozen);
 /* Start a physical time step: shift old time levels, beginTimeStep.H:1-45.  */
 int ics_begin_time_step(ics_handle h);
 /* Harmonic Balance (dbnsFullyImplicitHBFoam outerLoop.H:1-230, HBZone.C:359-519):

@@ -150,33 +150,34 @@ def test_adjoint_and_tangent_solves_are_dual(gpu_binding, pseudo_time, precision
     assert abs(lhs - rhs) <= 2 * bound + 1e-12 * abs(lhs), (lhs, rhs, bound)
 
 
-def test_steady_adjoint_on_a_converged_state(gpu_binding):
-    """The steady operator (no pseudo-time diagonal) at a state the pseudo-time
-    iteration has converged (bump channel, vanLeer reconstruction, a 1e-8 drop
-    of the rho residual): the adjoint of the walls' x pressure force and a
-    tangent solve reach 1e-8, and their duality holds to the residual bound."""
-    w = _over(cases.bump_channel(24, 8, 4, ordering_mode="colour"), recon_rho=1, recon_U=1, recon_T=1)
+def test_steady_linearisation_at_convergence_is_singular(gpu_binding):
+    """Why the Krylov solves offer the pseudo-time operator: at a state the
+    pseudo-time iteration has converged (bump channel 12x4x2, first order, a
+    1e-9 drop of the rho residual) the steady linearisation -d(R V)/dW with
+    the boundary values held fixed (the JVP's operator), each variable scaled
+    by its largest magnitude, is numerically singular (smallest singular value
+    below 1e-10 of the largest) and has eigenvalues left of the imaginary
+    axis, so a Krylov solve of it from a generic right-hand side stalls."""
+    w = _over(cases.bump_channel(12, 4, 2, ordering_mode="colour"), recon_rho=0, recon_U=0, recon_T=0)
     h = abi.CaseHandle(gpu_binding, w.mesh, cases.make_config(gpu_binding, w.settings))
     h.set_primitive(w.p, w.U, w.T)
     r0 = None
-    for _ in range(3000):
+    for _ in range(2000):
         h.pseudo_loop()
         s = h.pseudo_iteration()
         r0 = r0 or s.rho_l2_residual
-        if s.rho_l2_residual < 1e-8 * r0:
+        if s.rho_l2_residual < 1e-9 * r0:
             break
-    assert s.rho_l2_residual < 1e-8 * r0
-    h.residual()
-    h.assemble_jacobian()
-    walls = [p.name for p in w.mesh.patches].index("walls")
-    _, g = h.pressure_force(walls, (1.0, 0.0, 0.0))
+    assert s.rho_l2_residual < 1e-9 * r0
     W = h.get_state()["W"]
-    b = direction(W, 31) * 1e-3
-    opts = dict(n_directions=60, max_cycles=60, rel_tol=1e-8, precision=1, pseudo_time=0)
-    psi, ra = h.adjoint_solve(g, **opts)
-    x, rt = h.tangent_solve(b, **opts)
-    assert ra.converged and rt.converged, (ra.rel_residual, ra.iterations, rt.rel_residual, rt.iterations)
-    r_a, r_t = _residuals(h, psi, x, g, b, 0)
-    lhs, rhs = float(np.sum(g * x)), float(np.sum(psi * b))
-    bound = np.linalg.norm(psi) * np.linalg.norm(r_t) + np.linalg.norm(r_a) * np.linalg.norm(x)
-    assert abs(lhs - rhs) <= 2 * bound + 1e-12 * abs(lhs), (lhs, rhs, bound)
+    n = W.size
+    A = np.zeros((n, n))
+    for j in range(n):
+        e = np.zeros(n)
+        e[j] = 1.0
+        A[:, j] = -h.jvp(e.reshape(W.shape)).ravel()
+    S = np.tile(np.abs(W).max(axis=0), W.shape[0])
+    As = A * S[None, :] / S[:, None]
+    sv = np.linalg.svd(As, compute_uv=False)
+    assert sv[-1] < 1e-10 * sv[0], (sv[-1], sv[0])
+    assert np.sum(np.linalg.eigvals(As).real < 0) >= 1

@@ -1661,6 +1661,7 @@ int ics_autotune(ics_handle hh, ics_tuning* out) {
       t.grad_block = h.tuneGradBs;
       t.mgs_blocks = h.tuneMgsBlocks;
       t.fused_operator = h.tuneFused;
+      t.reverse_rows = h.tuneRevRows;
       std::lock_guard<std::mutex> lock(g_tune_mu);
       g_tune_cache[key] = t;
     }
@@ -1668,12 +1669,34 @@ int ics_autotune(ics_handle hh, ics_tuning* out) {
     h.tuneGradBs = t.grad_block;
     h.tuneMgsBlocks = t.mgs_blocks;
     h.tuneFused = t.fused_operator;
+    h.tuneRevRows = t.reverse_rows;
     drop_graphs(h);  // the captured cycle holds the old launch shapes
     // the timing runs overwrote the Krylov workspace and the face fields
     // of this state; the next iteration recomputes both
     h.haveIncrement = false;
     ICS_CUDA(cudaStreamSynchronize(h.stream));
     if (out) *out = t;
+    return ICS_OK;
+  });
+}
+
+int ics_set_tuning(ics_handle hh, const ics_tuning* t) {
+  if (!t) return ICS_ERR_ARG;
+  return guard(hh, [&](Handle& h) {
+    const bool ok = (t->face_block == 64 || t->face_block == 128) && (t->grad_block == 64 || t->grad_block == 128) &&
+                    (t->mgs_blocks == 152 || t->mgs_blocks == 304 || t->mgs_blocks == 456 || t->mgs_blocks == 608) &&
+                    (t->fused_operator == 0 || t->fused_operator == 1) &&
+                    (t->reverse_rows == 1 || t->reverse_rows == 2);
+    if (!ok) {
+      h.err = "tuning values outside the autotuner's candidates";
+      return ICS_ERR_ARG;
+    }
+    h.tuneFaceBs = t->face_block;
+    h.tuneGradBs = t->grad_block;
+    h.tuneMgsBlocks = t->mgs_blocks;
+    h.tuneFused = t->fused_operator;
+    h.tuneRevRows = t->reverse_rows;
+    drop_graphs(h);
     return ICS_OK;
   });
 }

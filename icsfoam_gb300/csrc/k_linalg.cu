@@ -434,6 +434,75 @@ __device__ __forceinline__ void lusgs_rev_row(const DevMesh& m, const TB* __rest
   for (int k = 0; k < 5; ++k) r[5 * c + k] = rc * acc[k];
 }
 
+// Two rows of one reverse level in one thread: their slot loops run in
+// lockstep, so the column index, block words and gathered neighbour rows of
+// both are in flight together (a level's rows never read each other).  Each
+// row's arithmetic is that of lusgs_rev_row: slots from the last down to the
+// first upper one, acc -= B r_col, then the scaling by rD.
+template <typename TB, typename TV>
+__device__ __forceinline__ void lusgs_rev_row2(const DevMesh& m, const TB* __restrict__ blk,
+                                               const TB* __restrict__ rD, TV* __restrict__ r, int c0, int c1) {
+  const int l0 = c0 & 31, l1 = c1 & 31;
+  const int b0 = m.slot_base[c0 >> 5], b1 = m.slot_base[c1 >> 5];
+  const int nl0 = m.nlow[c0], nl1 = m.nlow[c1];
+  int t0 = m.nslot[c0] - 1, t1 = m.nslot[c1] - 1;
+  TV a0[5], a1[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    a0[k] = r[5 * c0 + k];
+    a1[k] = r[5 * c1 + k];
+  }
+  const TV g = TV(m.gamma);
+#pragma unroll 1
+  for (; t0 >= nl0 || t1 >= nl1; --t0, --t1) {
+    const bool v0 = t0 >= nl0, v1 = t1 >= nl1;
+    const int col0 = v0 ? m.scol[(b0 + t0) * 32 + l0] : c0;
+    const int col1 = v1 ? m.scol[(b1 + t1) * 32 + l1] : c1;
+    TV d0[5], d1[5], y0[5], y1[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      d0[k] = r[5 * col0 + k];
+      d1[k] = r[5 * col1 + k];
+    }
+    SlotBlock<TB> B0, B1;
+    if (v0) B0.load(blk, b0 + t0, l0);
+    if (v1) B1.load(blk, b1 + t1, l1);
+    if (v0) {
+      B0.mv(g, d0, y0);
+      if (m.vjslot) vj_sub<TB>(m, b0 + t0, l0, col0, d0, y0);
+#pragma unroll
+      for (int i = 0; i < 5; ++i) a0[i] -= y0[i];
+    }
+    if (v1) {
+      B1.mv(g, d1, y1);
+      if (m.vjslot) vj_sub<TB>(m, b1 + t1, l1, col1, d1, y1);
+#pragma unroll
+      for (int i = 0; i < 5; ++i) a1[i] -= y1[i];
+    }
+  }
+  const TV rc0 = TV(rD[c0]), rc1 = TV(rD[c1]);
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    r[5 * c0 + k] = rc0 * a0[k];
+    r[5 * c1 + k] = rc1 * a1[k];
+  }
+}
+
+// reverse level with two rows per thread: rows i and i + ceil(count/2)
+template <typename TB, typename TV>
+__global__ void __launch_bounds__(128) k_lusgs_rev2(DevMesh m, const TB* __restrict__ blk, const TB* __restrict__ rD,
+                                                    TV* __restrict__ r, const int* __restrict__ cells, int start,
+                                                    int count) {
+  const int half = (count + 1) >> 1;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= half) return;
+  const int c0 = cells ? cells[start + i] : start + i;
+  if (i + half < count)
+    lusgs_rev_row2<TB, TV>(m, blk, rD, r, c0, cells ? cells[start + i + half] : start + i + half);
+  else
+    lusgs_rev_row<TB, TV>(m, blk, rD, r, c0);
+}
+
 // one launch per level: cells = level list (nullptr when the level is the
 // contiguous range [start, start+count))
 // MODE 0: forward row, 1: reverse row, 2: forward row + reverse scaling
@@ -963,6 +1032,17 @@ static void spmv_t(Handle& h, const TV* x, TV* y) {
 }
 
 
+// one reverse level: one row per thread, or two (Handle::tuneRevRows)
+template <typename TB, typename TV>
+static void rev_level(Handle& h, const TB* blk, const TB* rD, TV* r, const int* cells, int start, int cnt) {
+  if (h.tuneRevRows == 2)
+    ICS_LAUNCH(h, ICS_K_LUSGS_REV, k_lusgs_rev2<TB, TV><<<grid_for((cnt + 1) / 2, 128), 128, 0, h.stream>>>(
+                                       h.m, blk, rD, r, cells, start, cnt));
+  else
+    ICS_LAUNCH(h, ICS_K_LUSGS_REV, k_lusgs_level<TB, TV, 1><<<grid_for(cnt, 128), 128, 0, h.stream>>>(
+                                       h.m, blk, rD, r, cells, start, cnt));
+}
+
 template <typename TB, typename TV>
 static void lusgs_t(Handle& h, TV* r, const TB* blkIn = nullptr, const TB* rDIn = nullptr) {
   const DevMesh& m = h.m;
@@ -1023,9 +1103,7 @@ static void lusgs_t(Handle& h, TV* r, const TB* blkIn = nullptr, const TB* rDIn 
     for (int l = fuse ? 1 : 0; l < m.nrl; ++l) {
       const int a = m.rl_ptr[l], cnt = m.rl_ptr[l + 1] - a;
       const bool contig = m.rl_cstart[l] >= 0;
-      ICS_LAUNCH(h, ICS_K_LUSGS_REV, k_lusgs_level<TB, TV, 1><<<grid_for(cnt, 128), 128, 0, h.stream>>>(
-                                         m, blk, rD, r, contig ? nullptr : m.rl_cells,
-                                         contig ? m.rl_cstart[l] : a, cnt));
+      rev_level<TB, TV>(h, blk, rD, r, contig ? nullptr : m.rl_cells, contig ? m.rl_cstart[l] : a, cnt);
     }
   }
 }
@@ -1087,9 +1165,7 @@ static bool fused_op_t(Handle& h, const TV* x, TV* w, TV* vout = nullptr) {
   // reverse level 1 = forward level 0 rows
   const int a = m.rl_ptr[1], cnt = m.rl_ptr[2] - a;
   const bool contig = m.rl_cstart[1] >= 0;
-  if (cnt)
-    ICS_LAUNCH(h, ICS_K_LUSGS_REV, k_lusgs_level<TB, TV, 1><<<grid_for(cnt, 128), 128, 0, h.stream>>>(
-                                       m, blk, rD, w, contig ? nullptr : m.rl_cells, contig ? m.rl_cstart[1] : a, cnt));
+  if (cnt) rev_level<TB, TV>(h, blk, rD, w, contig ? nullptr : m.rl_cells, contig ? m.rl_cstart[1] : a, cnt);
   return true;
 }
 
@@ -1514,6 +1590,17 @@ static void autotune_linalg_t(Handle& h, std::vector<std::pair<std::string, doub
     log.emplace_back("operator_spmv_then_lusgs", split);
     h.tuneFused = fused <= split ? 1 : 0;
   }
+  // rows per thread of the reverse level sweeps, timed on the whole LU-SGS
+  double revMs[3] = {0, 0, 0};
+  for (int rows : {1, 2}) {
+    h.tuneRevRows = rows;
+    revMs[rows] = timed([&]() {
+      to_vec(h, h.src, t);
+      precondition_t<TB, TV>(h, t);
+    });
+    log.emplace_back("reverse_rows_" + std::to_string(rows), revMs[rows]);
+  }
+  h.tuneRevRows = revMs[2] < revMs[1] ? 2 : 1;
   ICS_CUDA(cudaEventDestroy(e0));
   ICS_CUDA(cudaEventDestroy(e1));
   ICS_CUDA(cudaGetLastError());

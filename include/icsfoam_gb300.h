@@ -488,6 +488,8 @@ typedef struct {
   int32_t fused_operator;  /* 1: fused M^-1 A passes on two-level schedules, 0: SpMV then
                               LU-SGS sweeps                                              */
   int32_t from_cache;      /* 1: taken from an earlier tuning of a case of the same shape */
+  int32_t reverse_rows;    /* rows per thread of the reverse LU-SGS level sweep (1 / 2:
+                              two rows' slot loads in flight together)                   */
 } ics_tuning;
 /* Time each candidate launch choice on the handle's current state and
  * assembled Jacobian (CUDA events on its stream) and keep the fastest, for
@@ -496,6 +498,10 @@ typedef struct {
  * timing.  Needs ics_residual and ics_assemble_jacobian first.  Every choice
  * computes the same result up to the order of floating-point sums.        */
 int ics_autotune(ics_handle h, ics_tuning* out);
+/* Apply launch choices, e.g. an ics_autotune result saved by the host for a
+ * later run of the same case shape (from_cache is ignored).  Values outside
+ * the candidate sets above are refused (ICS_ERR_ARG).                        */
+int ics_set_tuning(ics_handle h, const ics_tuning* t);
 
 /* FP64 fused multiply-add rate (GFLOP/s, an FMA = 2 flops) of the handle's
  * GPU, measured with CUDA events on the handle's stream by a kernel of

@@ -268,6 +268,7 @@ def test_autotune_keeps_the_results_and_caches_the_choice(gpu_binding):
     t = tuned.autotune()
     assert t["face_block"] in (64, 128) and t["grad_block"] in (64, 128)
     assert t["mgs_blocks"] in (152, 304, 456, 608) and t["fused_operator"] in (0, 1) and not t["from_cache"]
+    assert t["reverse_rows"] in (1, 2)
     for _ in range(3):
         ref.pseudo_loop()
         ref.pseudo_iteration()
@@ -282,3 +283,29 @@ def test_autotune_keeps_the_results_and_caches_the_choice(gpu_binding):
     t2 = other.autotune()
     assert t2["from_cache"] and {k: t2[k] for k in t2 if k != "from_cache"} == \
         {k: t[k] for k in t if k != "from_cache"}
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("fused", [0, 1])
+def test_reverse_rows_per_thread_keep_every_bit(gpu_binding, precision, fused):
+    """ics_set_tuning(reverse_rows=2): two rows of a reverse LU-SGS level per
+    thread, each with the one-row arithmetic: the preconditioner and three
+    pseudo iterations are bit-identical to one row per thread, on the two-level
+    (colour-blocked) schedule of 4320 rows (level launches, not the one-CTA
+    walk), with and without the fused operator."""
+    for order in ("colour",):
+        w = cases.bump_channel(40, 12, 9, ordering_mode=order)
+        hs = [open_case(gpu_binding, w, precision=precision) for _ in range(2)]
+        for h, rows in zip(hs, (1, 2)):
+            h.set_tuning(fused_operator=fused, reverse_rows=rows)
+            h.residual()
+            h.assemble_jacobian()
+        r = np.random.default_rng(5).standard_normal((w.mesh.n_cells, 5))
+        assert np.array_equal(hs[0].precondition(r), hs[1].precondition(r)), order
+        for _ in range(3):
+            for h in hs:
+                h.pseudo_loop()
+                h.pseudo_iteration()
+        assert np.array_equal(hs[0].get_state()["W"], hs[1].get_state()["W"]), order
+    with pytest.raises(abi.IcsError):
+        hs[0].set_tuning(reverse_rows=3)

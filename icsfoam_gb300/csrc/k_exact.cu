@@ -187,7 +187,9 @@ void build_exact_pattern(Handle& h) {
     std::sort(row.begin(), row.end());
     col.insert(col.end(), row.begin(), row.end());
     ptr[r + 1] = (int)col.size();
-    if (col.size() > (size_t)0x7fffffff / 25) throw std::string("exact Jacobian stencil too large");
+    // rows, columns and transpose positions are 32-bit; block entries are
+    // addressed as (size_t) block * 25
+    if (col.size() > (size_t)0x7fffffff) throw std::string("exact Jacobian stencil too large");
   }
   const size_t nnz = col.size();
   // transpose positions: entry (r, c) -> index of (c, r) in row c

@@ -19,7 +19,7 @@ import pytest
 
 from icsfoam_gb300 import abi, cases
 
-from test_gpu_parity import relerr  # noqa: E402
+from test_gpu_parity import perturb, relerr  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
@@ -32,8 +32,13 @@ def _tubes(sizes):
 
 
 def _bumps():
-    return [cases.bump_channel(8, 4, 2, ordering_mode="colour"), cases.bump_channel(12, 6, 3, ordering_mode="colour"),
-            cases.bump_channel(10, 4, 2, ordering_mode="colour")]
+    # perturbed states (as the parity tests use): from the uniform start the
+    # y and z momentum residuals are round-off, and the GMRES stop test's
+    # relative criterion divides them by round-off initial residuals, so a
+    # different summation order changes the number of restart cycles
+    return [perturb(cases.bump_channel(8, 4, 2, ordering_mode="colour"), seed=1),
+            perturb(cases.bump_channel(12, 6, 3, ordering_mode="colour"), seed=2),
+            perturb(cases.bump_channel(10, 4, 2, ordering_mode="colour"), seed=3)]
 
 
 def _open(b, w, precision=0):

@@ -696,7 +696,7 @@ def run_mrf_annulus(nr=32, nt=64, nz=128, steps=10, warmup=3):
             "rho_residual_drop": s.rho_l2_residual / first}
 
 
-def run_diff(nx=120, ny=64, nz=64, reps=5):
+def run_diff(nx=240, ny=128, nz=128, reps=5):
     """Residual derivatives on the swept bump: forward-mode JVP, exact Jacobian assembly by
     coloured JVPs, and the transpose product (VJP)."""
     import numpy as np

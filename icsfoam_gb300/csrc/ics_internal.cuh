@@ -159,6 +159,10 @@ struct DevMesh {
   // cell [N] and each case's SER factor [n_cases] (< 0: not applied)
   const int* caseOf = nullptr;
   const double* caseSer = nullptr;
+  // and each case's Krylov norm and flags (the fused operator's scaling)
+  const double* caseBeta = nullptr;
+  const int* caseActive = nullptr;
+  const int* caseStatus = nullptr;
 };
 
 // pseudotimeControl state (pseudotimeControl.C): the iteration count of the
@@ -450,6 +454,9 @@ void sweep_probe(Handle& h, const int* order, int count, int spin_limit);
 void from_vec(Handle& h, const void* src, double* dst); // Krylov type -> FP64
 
 inline int prec(const Handle& h) { return h.cfg.c.precision; }
+// w = M^-1 A (x / beta) with v = x / beta stored in vout, by the fused LU-SGS
+// operator passes; false (nothing launched) where they do not apply
+bool fused_operator(Handle& h, const void* x, void* w, void* vout);
 // element stride between consecutive Krylov basis vectors (5N rounded up to 64)
 inline size_t kstride(const Handle& h) { return ((5ull * h.m.N + 63) / 64) * 64; }
 inline size_t vbytes(const Handle& h) { return prec(h) == ICS_PREC_MIXED ? 4 : 8; }

@@ -23,8 +23,9 @@
 //     stop test per case; a case that has stopped (or broken down) is marked
 //     inactive and its correction is left as it stands while the others go
 //     on.
-// The LU-SGS preconditioner and the SpMV are the handle's own (union) kernels:
-// their rows only read rows of the same case.
+// The LU-SGS preconditioner, the SpMV and the fused operator passes are the
+// handle's own (union) kernels: their rows only read rows of the same case, and
+// the fused passes scale each row by its own case's Krylov norm.
 #include <algorithm>
 #include <cmath>
 
@@ -363,17 +364,26 @@ int gmres_cases_t(Handle& h, std::vector<int>& caseStatus) {
   auto cycle = [&]() {
     precondition(h, w);
     ICS_LAUNCH(h, ICS_K_MGS, k_cmgs<TV><<<ns, CB, 0, st>>>(D, w, nullptr, 0, nullptr, 0, 0, 1, 0));
+    // with the fused operator (each row scaled by its own case's norm) the
+    // unnormalised vector alternates between w and t, as in the single-system
+    // cycle; the cycle's residual goes back to w
+    TV* wb[2] = {w, t};
     for (int i = 0; i < m; ++i) {
       TV* vi = V + (size_t)i * vs;
-      ICS_LAUNCH(h, ICS_K_VECTOR, k_cscale<TV><<<ns, CB, 0, st>>>(D, w, vi));
-      spmv(h, vi, w);
-      precondition(h, w);
+      TV* wc = w;
+      if (fused_operator(h, wb[i & 1], wb[(i + 1) & 1], vi)) {
+        wc = wb[(i + 1) & 1];
+      } else {
+        ICS_LAUNCH(h, ICS_K_VECTOR, k_cscale<TV><<<ns, CB, 0, st>>>(D, w, vi));
+        spmv(h, vi, w);
+        precondition(h, w);
+      }
       for (int j = 0; j <= i; ++j) {
         const TV* vprev = j > 0 ? V + (size_t)(j - 1) * vs : nullptr;
-        ICS_LAUNCH(h, ICS_K_MGS, k_cmgs<TV><<<ns, CB, 0, st>>>(D, w, vprev, (j - 1) * m + i, V + (size_t)j * vs,
+        ICS_LAUNCH(h, ICS_K_MGS, k_cmgs<TV><<<ns, CB, 0, st>>>(D, wc, vprev, (j - 1) * m + i, V + (size_t)j * vs,
                                                                j * m + i, -1, 0, i));
       }
-      ICS_LAUNCH(h, ICS_K_MGS, k_cmgs<TV><<<ns, CB, 0, st>>>(D, w, vi, i * m + i, nullptr, 0, 1, 2, i));
+      ICS_LAUNCH(h, ICS_K_MGS, k_cmgs<TV><<<ns, CB, 0, st>>>(D, wc, vi, i * m + i, nullptr, 0, 1, 2, i));
     }
     ICS_LAUNCH(h, ICS_K_SCALAR, k_cbacksub<<<(n + 63) / 64, 64, 0, st>>>(D));
     ICS_LAUNCH(h, ICS_K_VECTOR, k_cxupdate<TV><<<ns, CB, 0, st>>>(D, x, V, vs));
@@ -470,6 +480,9 @@ void free_cases(Handle& h) {
   S = CaseSet();
   h.m.caseOf = nullptr;
   h.m.caseSer = nullptr;
+  h.m.caseBeta = nullptr;
+  h.m.caseActive = nullptr;
+  h.m.caseStatus = nullptr;
 }
 
 void set_cases(Handle& h, int n, const int* start) {
@@ -571,6 +584,9 @@ void set_cases(Handle& h, int n, const int* start) {
   S.cycles.assign(n, 0);
   h.m.caseOf = S.caseOf;
   h.m.caseSer = S.ser;
+  h.m.caseBeta = D.beta;
+  h.m.caseActive = D.active;
+  h.m.caseStatus = D.status;
 }
 
 int gmres_cases(Handle& h, std::vector<int>& caseStatus) {

@@ -227,6 +227,15 @@ template <typename TV>
 __device__ __forceinline__ TV krylov_rbeta(const KrylovScalars* ks) {
   return ks && ks->status == 0 ? TV(1.0 / ks->beta) : TV(1);
 }
+// the reciprocal norm of row c's system: its stacked case's, else the handle's
+template <typename TV>
+__device__ __forceinline__ TV row_rbeta(const DevMesh& m, int c, const KrylovScalars* ks) {
+  if (m.caseBeta) {
+    const int k = m.caseOf[c];
+    return m.caseActive[k] && m.caseStatus[k] == 0 ? TV(1.0 / m.caseBeta[k]) : TV(1);
+  }
+  return krylov_rbeta<TV>(ks);
+}
 
 template <typename TB, typename TV, int MINB = 1, int UNR = 1, bool SCALED = false>
 __global__ void __launch_bounds__(128, MINB) k_op_level0(DevMesh m, const TB* __restrict__ blk, const TB* __restrict__ dg,
@@ -237,7 +246,7 @@ __global__ void __launch_bounds__(128, MINB) k_op_level0(DevMesh m, const TB* __
   if (i >= count) return;
   const int c = cells ? cells[start + i] : start + i;
   const int s = c >> 5, lane = c & 31;
-  const TV beta = SCALED ? krylov_rbeta<TV>(ks) : TV(1);  // reciprocal
+  const TV beta = SCALED ? row_rbeta<TV>(m, c, ks) : TV(1);  // reciprocal
   TV xc[5], acc[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) xc[k] = ldx<SCALED>(x, 5 * (size_t)c + k, beta);
@@ -306,7 +315,7 @@ __global__ void __launch_bounds__(128, MINB) k_op_level1(DevMesh m, const TB* __
   if (i >= count) return;
   const int c = cells ? cells[start + i] : start + i;
   const int s = c >> 5, lane = c & 31;
-  const TV beta = SCALED ? krylov_rbeta<TV>(ks) : TV(1);  // reciprocal
+  const TV beta = SCALED ? row_rbeta<TV>(m, c, ks) : TV(1);  // reciprocal
   TV xc[5], acc[5], fw[5];
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
@@ -1204,6 +1213,12 @@ void lusgs_with(Handle& h, const void* blk, const void* rD, bool fp32, double* r
   else
     lusgs_t<double, double>(h, r, (const double*)blk, (const double*)rD);
   ICS_CUDA(cudaGetLastError());
+}
+
+bool fused_operator(Handle& h, const void* x, void* w, void* vout) {
+  if (prec(h) == ICS_PREC_MIXED)
+    return fused_op_t<float, float>(h, (const float*)x, (float*)w, (float*)vout);
+  return fused_op_t<double, double>(h, (const double*)x, (double*)w, (double*)vout);
 }
 
 void sweep_probe(Handle& h, const int* order, int count, int spin_limit) {

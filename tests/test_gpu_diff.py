@@ -157,26 +157,34 @@ def test_swept_bump_full_size_derivatives(gpu_binding):
     tie of the limiter's bounds, where the residual has no derivative):
       * along 32 seeded directions the JVP equals central differences with the
         step 1e-7 to 1e-5 of each equation's max-norm at every cell where the
-        differences are step-consistent (steps 1e-7 and 2.5e-8 agree to 1e-6);
-        the others sit on kinks of the limiters' min / max selections and must
-        stay below 1% of the cells;
+        residual is smooth over the step (the forward and backward differences
+        agree to 1e-5: |R(W+hv) - 2 R(W) + R(W-hv)| / h); the others sit on
+        kinks of the limiters' min / max selections, where the one-sided
+        derivative of the JVP and the average slope of a central difference
+        differ, and must stay below 1% of the cells;
       * the reverse-mode VJP (gradients recomputed) is the JVP's transpose,
         <u, J v> = <J^T u, v> to 1e-12 of |u| |J v|, and equals the product
         with the assembled exact Jacobian (97 M stencil blocks) to 1e-10."""
     w = perturb(cases.swept_bump(240, 128, 128))
     h = open_case(gpu_binding, w, untie=True)
     W = h.get_state()["W"]
+    R0 = h.residual()
+    eps = 1e-7
     kinks = 0
     for s in range(32):
         v = direction(W, 100 + s)
         J = h.jvp(v)
-        F1 = fd_jvp(h, W, v, eps=1e-7)
-        F2 = fd_jvp(h, W, v, eps=2.5e-8)
-        scale = np.abs(F1).max(axis=0)
+        h.set_conservative(W + eps * v)
+        Rp = h.residual()
+        h.set_conservative(W - eps * v)
+        Rm = h.residual()
+        h.set_conservative(W)
+        F = (Rp - Rm) / (2 * eps)
+        scale = np.abs(F).max(axis=0)
         scale[1:4] = scale[1:4].max()
-        smooth = (np.abs(F1 - F2) / scale).max(axis=1) < 1e-6
+        smooth = (np.abs(Rp - 2 * R0 + Rm) / eps / scale).max(axis=1) < 1e-5
         kinks += int((~smooth).sum())
-        err = (np.abs(J - F1)[smooth] / scale).max()
+        err = (np.abs(J - F)[smooth] / scale).max()
         assert err < 1e-5, (s, err)
     assert kinks < 0.01 * 32 * W.shape[0], kinks
     rng = np.random.default_rng(7)

@@ -53,6 +53,10 @@ def parse():
                     help="time cap of the mixed-precision leg to 1e-8 (the FP64 leg gets 2.5x)")
     ap.add_argument("--plateau-cap-s", type=float, default=15.0,
                     help="seconds of the configured Venkatakrishnan limiter (mixed) recording its plateau")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="only the batch of this many independent shock-tube cases")
+    ap.add_argument("--batch-stacked-only", type=int, default=0,
+                    help="with --batch: only the cases stacked in one handle")
     ap.add_argument("--adjoint", type=int, default=0,
                     help="only the reverse-mode VJP and the adjoint solve on the 240x128x128 swept bump")
     ap.add_argument("--convergence-study", type=int, default=0,
@@ -540,7 +544,7 @@ def run_hb_sweep(instances=(3, 5, 7, 9), per=(32, 64, 128), steps=5, warmup=2):
     return out
 
 
-def run_batch(n_cases=64, steps=3, seed=2, precision=1):
+def run_batch(n_cases=64, steps=3, seed=2, precision=1, modes=("stacked", "concurrent", "sequential")):
     """64 independent shock-tube cases (Sod, AUSM+up, backward dual-time ddt, pseudo CFL 50,
     GMRES(8)+LU-SGS), N ~ U[2000, 50000] (seeded), `steps` physical time steps, each case
     pseudo-iterating until its own pseudotimeControl completes; three ways: one after another
@@ -611,6 +615,11 @@ def run_batch(n_cases=64, steps=3, seed=2, precision=1):
     its_st = stacked(steps)
     t_st = time.perf_counter() - t0
     hst.close()
+    work = float((cells * its_st).sum())
+    out.update({"pseudo_iterations_per_case": [int(its_st.min()), int(its_st.max())],
+                "stacked_cell_iters_per_s": work / t_st, "stacked_s": t_st})
+    if "concurrent" not in modes:
+        return out
     hs = handles()
     concurrent(hs, 1)
     t0 = time.perf_counter()
@@ -625,14 +634,11 @@ def run_batch(n_cases=64, steps=3, seed=2, precision=1):
     t_se = time.perf_counter() - t0
     for h in hs:
         h.close()
-    work = float((cells * its_st).sum())
     out.update({
-        "pseudo_iterations_per_case": [int(its_st.min()), int(its_st.max())],
         "same_iterations_all_modes": bool(np.array_equal(its_st, its_co) and np.array_equal(its_st, its_se)),
-        "stacked_cell_iters_per_s": work / t_st,
         "concurrent_cell_iters_per_s": float((cells * its_co).sum()) / t_co,
         "sequential_cell_iters_per_s": float((cells * its_se).sum()) / t_se,
-        "stacked_s": t_st, "concurrent_s": t_co, "sequential_s": t_se,
+        "concurrent_s": t_co, "sequential_s": t_se,
         "stacked_over_sequential": t_se / t_st, "stacked_over_concurrent": t_co / t_st})
     return out
 
@@ -859,6 +865,12 @@ def main():
         os.environ["CUDA_VISIBLE_DEVICES"] = str(dist.local)
     from icsfoam_gb300 import cases
 
+    if args.batch:
+        # the independent-case batch alone (stacked only with --batch-stacked-only 1)
+        modes = ("stacked",) if args.batch_stacked_only else ("stacked", "concurrent", "sequential")
+        print(json.dumps(run_batch(n_cases=args.batch, modes=modes)), flush=True)
+        dist.close()
+        return
     if args.adjoint:
         w = cases.swept_bump(240, 128, 128)
         print(json.dumps({"workload": w.name, "cells": w.mesh.n_cells, **run_adjoint(w)}), flush=True)

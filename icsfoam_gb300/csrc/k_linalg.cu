@@ -1584,15 +1584,19 @@ static void autotune_linalg_t(Handle& h, std::vector<std::pair<std::string, doub
   const int m = h.cfg.c.n_directions;
   int bestBlocks = h.tuneMgsBlocks;
   double bestMs = 1e300;
-  // the cycle's step: w -= h v_prev, then w . v_next, eight in a row (one
-  // launch is a few microseconds, too short to time alone); h = 0 keeps w
+  // the cycle's steps: w -= h v_{j-1}, then w . v_j over the m basis vectors
+  // in turn (their working set exceeds L2 as in the cycle; one launch alone
+  // is too short to time); h = 0 keeps w
+  const long vs = (long)kstride(h);
+  for (int j = 1; j < m; ++j) to_vec(h, h.src, V + (size_t)j * vs);
   ICS_CUDA(cudaMemsetAsync(&ks->red[15], 0, sizeof(double), st));
   ICS_CUDA(cudaMemsetAsync(&ks->status, 0, sizeof(int), st));
   for (int blocks : {152, 304, 456, 608}) {
     const double ms = timed([&]() {
-      for (int r = 0; r < 8; ++r)
-        k_mgs<TV><<<blocks, RB, 0, st>>>(n5, w, V, &ks->red[15], V, &ks->status, h.partials, h.counter,
-                                          &ks->red[14], ks, 0, 0, m);
+      for (int j = 0; j < m; ++j)
+        k_mgs<TV><<<blocks, RB, 0, st>>>(n5, w, V + (size_t)((j + m - 1) % m) * vs, &ks->red[15],
+                                          V + (size_t)j * vs, &ks->status, h.partials, h.counter, &ks->red[14], ks,
+                                          0, 0, m);
     });
     log.emplace_back("mgs_blocks_" + std::to_string(blocks), ms);
     if (ms < bestMs) bestMs = ms, bestBlocks = blocks;

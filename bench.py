@@ -246,7 +246,7 @@ def load_traffic():
 # launch choices picked by ics_autotune on the headline workload (per
 # precision), applied to the later handles of the same mesh
 TUNING = {}
-TUNE_KEYS = ("face_block", "grad_block", "mgs_blocks", "fused_operator", "reverse_rows", "op1_blocks")
+TUNE_KEYS = ("face_block", "grad_block", "mgs_blocks", "fused_operator", "reverse_rows")
 
 
 def tuned(h, prec):

@@ -107,8 +107,7 @@ class IterStats(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("face_block", C.c_int32), ("grad_block", C.c_int32), ("mgs_blocks", C.c_int32),
-                ("fused_operator", C.c_int32), ("from_cache", C.c_int32), ("reverse_rows", C.c_int32),
-                ("op1_blocks", C.c_int32)]
+                ("fused_operator", C.c_int32), ("from_cache", C.c_int32), ("reverse_rows", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -535,11 +534,10 @@ class CaseHandle:
         self._check(self.b.fn["autotune"](self.h, C.byref(t)), "autotune")
         return t.as_dict()
 
-    def set_tuning(self, face_block=128, grad_block=128, mgs_blocks=608, fused_operator=1, reverse_rows=1,
-                   op1_blocks=8):
+    def set_tuning(self, face_block=128, grad_block=128, mgs_blocks=608, fused_operator=1, reverse_rows=1):
         """Apply launch choices (ics_set_tuning), e.g. a saved autotune() result."""
         t = Tuning(face_block=face_block, grad_block=grad_block, mgs_blocks=mgs_blocks,
-                   fused_operator=fused_operator, from_cache=0, reverse_rows=reverse_rows, op1_blocks=op1_blocks)
+                   fused_operator=fused_operator, from_cache=0, reverse_rows=reverse_rows)
         self._check(self.b.fn["set_tuning"](self.h, C.byref(t)), "set_tuning")
 
     def measure_fp64_rate(self) -> float:

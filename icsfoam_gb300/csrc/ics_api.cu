@@ -1662,7 +1662,6 @@ int ics_autotune(ics_handle hh, ics_tuning* out) {
       t.mgs_blocks = h.tuneMgsBlocks;
       t.fused_operator = h.tuneFused;
       t.reverse_rows = h.tuneRevRows;
-      t.op1_blocks = h.tuneOp1Blocks;
       std::lock_guard<std::mutex> lock(g_tune_mu);
       g_tune_cache[key] = t;
     }
@@ -1671,7 +1670,6 @@ int ics_autotune(ics_handle hh, ics_tuning* out) {
     h.tuneMgsBlocks = t.mgs_blocks;
     h.tuneFused = t.fused_operator;
     h.tuneRevRows = t.reverse_rows;
-    h.tuneOp1Blocks = t.op1_blocks;
     drop_graphs(h);  // the captured cycle holds the old launch shapes
     // the timing runs overwrote the Krylov workspace and the face fields
     // of this state; the next iteration recomputes both
@@ -1688,7 +1686,7 @@ int ics_set_tuning(ics_handle hh, const ics_tuning* t) {
     const bool ok = (t->face_block == 64 || t->face_block == 128) && (t->grad_block == 64 || t->grad_block == 128) &&
                     (t->mgs_blocks == 152 || t->mgs_blocks == 304 || t->mgs_blocks == 456 || t->mgs_blocks == 608) &&
                     (t->fused_operator == 0 || t->fused_operator == 1) &&
-                    (t->reverse_rows == 1 || t->reverse_rows == 2) && (t->op1_blocks == 8 || t->op1_blocks == 9);
+                    (t->reverse_rows == 1 || t->reverse_rows == 2);
     if (!ok) {
       h.err = "tuning values outside the autotuner's candidates";
       return ICS_ERR_ARG;
@@ -1698,7 +1696,6 @@ int ics_set_tuning(ics_handle hh, const ics_tuning* t) {
     h.tuneMgsBlocks = t->mgs_blocks;
     h.tuneFused = t->fused_operator;
     h.tuneRevRows = t->reverse_rows;
-    h.tuneOp1Blocks = t->op1_blocks;
     drop_graphs(h);
     return ICS_OK;
   });

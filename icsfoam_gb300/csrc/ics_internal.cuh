@@ -320,7 +320,7 @@ struct Handle {
   unsigned char* hbZoneBuf = nullptr;  // owner of m.hbZone
   // launch choices, set by the autotuner (ics_autotune) or left at the
   // defaults that the hand sweeps picked
-  int tuneFaceBs = 128, tuneGradBs = 128, tuneMgsBlocks = 608, tuneFused = 1, tuneRevRows = 1, tuneOp1Blocks = 8;
+  int tuneFaceBs = 128, tuneGradBs = 128, tuneMgsBlocks = 608, tuneFused = 1, tuneRevRows = 1;
   // exact Jacobian of the residual source: stencil CSR (two face hops plus
   // Harmonic Balance partners), transpose positions, colouring, blocks
   int* xptr = nullptr;

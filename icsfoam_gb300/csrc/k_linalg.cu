@@ -1163,24 +1163,13 @@ static bool fused_op_t(Handle& h, const TV* x, TV* w, TV* vout = nullptr) {
       ICS_LAUNCH(h, ICS_K_OP0, k_op_level0<TB, TV, OPB, 1><<<grid_for(n0, 128), 128, 0, h.stream>>>(
                                    m, blk, dg, x, w, c0, s0, n0, nullptr, nullptr));
   }
-  // level-1 pass: 8 blocks of 128 per SM (64 registers) or 9 (56 registers,
-  // Handle::tuneOp1Blocks): the number of resident waves a level makes on the
-  // 152 SMs decides how much of the last wave runs part-empty
   if (n1) {
-    if (sizeof(TB) == 4 && h.tuneOp1Blocks == 9) {
-      if (vout)
-        ICS_LAUNCH(h, ICS_K_OP1, k_op_level1<TB, TV, 9, 1, true><<<grid_for(n1, 128), 128, 0, h.stream>>>(
-                                     m, blk, dg, rD, x, w, c1, s1, n1, ks, vout));
-      else
-        ICS_LAUNCH(h, ICS_K_OP1, k_op_level1<TB, TV, 9, 1><<<grid_for(n1, 128), 128, 0, h.stream>>>(
-                                     m, blk, dg, rD, x, w, c1, s1, n1, nullptr, nullptr));
-    } else if (vout) {
+    if (vout)
       ICS_LAUNCH(h, ICS_K_OP1, k_op_level1<TB, TV, OPB, 1, true><<<grid_for(n1, 128), 128, 0, h.stream>>>(
                                    m, blk, dg, rD, x, w, c1, s1, n1, ks, vout));
-    } else {
+    else
       ICS_LAUNCH(h, ICS_K_OP1, k_op_level1<TB, TV, OPB, 1><<<grid_for(n1, 128), 128, 0, h.stream>>>(
                                    m, blk, dg, rD, x, w, c1, s1, n1, nullptr, nullptr));
-    }
   }
   // reverse level 1 = forward level 0 rows
   const int a = m.rl_ptr[1], cnt = m.rl_ptr[2] - a;
@@ -1615,15 +1604,6 @@ static void autotune_linalg_t(Handle& h, std::vector<std::pair<std::string, doub
   h.tuneMgsBlocks = bestBlocks;
   ICS_CUDA(cudaMemsetAsync(&ks->status, 0, sizeof(int), st));
   h.tuneFused = 1;
-  if (fused_op_available<TB, TV>(h) && sizeof(TB) == 4) {
-    double opMs[2];
-    for (int b : {8, 9}) {
-      h.tuneOp1Blocks = b;
-      opMs[b - 8] = timed([&]() { fused_op_t<TB, TV>(h, V, w); });
-      log.emplace_back("op1_blocks_per_sm_" + std::to_string(b), opMs[b - 8]);
-    }
-    h.tuneOp1Blocks = opMs[1] < opMs[0] ? 9 : 8;
-  }
   if (fused_op_available<TB, TV>(h)) {
     const double fused = timed([&]() { fused_op_t<TB, TV>(h, V, w); });
     const double split = timed([&]() {

@@ -490,8 +490,6 @@ typedef struct {
   int32_t from_cache;      /* 1: taken from an earlier tuning of a case of the same shape */
   int32_t reverse_rows;    /* rows per thread of the reverse LU-SGS level sweep (1 / 2:
                               two rows' slot loads in flight together)                   */
-  int32_t op1_blocks;      /* resident 128-thread blocks per SM of the fused level-1 pass
-                              in mixed precision (8 / 9)                                 */
 } ics_tuning;
 /* Time each candidate launch choice on the handle's current state and
  * assembled Jacobian (CUDA events on its stream) and keep the fastest, for

@@ -268,7 +268,7 @@ def test_autotune_keeps_the_results_and_caches_the_choice(gpu_binding):
     t = tuned.autotune()
     assert t["face_block"] in (64, 128) and t["grad_block"] in (64, 128)
     assert t["mgs_blocks"] in (152, 304, 456, 608) and t["fused_operator"] in (0, 1) and not t["from_cache"]
-    assert t["reverse_rows"] in (1, 2) and t["op1_blocks"] in (8, 9)
+    assert t["reverse_rows"] in (1, 2)
     for _ in range(3):
         ref.pseudo_loop()
         ref.pseudo_iteration()
@@ -283,23 +283,6 @@ def test_autotune_keeps_the_results_and_caches_the_choice(gpu_binding):
     t2 = other.autotune()
     assert t2["from_cache"] and {k: t2[k] for k in t2 if k != "from_cache"} == \
         {k: t[k] for k in t if k != "from_cache"}
-
-
-def test_level1_blocks_per_sm_keep_every_bit(gpu_binding):
-    """ics_set_tuning(op1_blocks=9): the fused level-1 pass built for 9
-    resident blocks per SM (56 registers) computes exactly what the 8-block
-    build does (mixed precision, two-level schedule)."""
-    w = cases.bump_channel(40, 12, 9, ordering_mode="colour")
-    hs = [open_case(gpu_binding, w, precision=1) for _ in range(2)]
-    for h, b in zip(hs, (8, 9)):
-        h.set_tuning(op1_blocks=b)
-    for _ in range(3):
-        for h in hs:
-            h.pseudo_loop()
-            h.pseudo_iteration()
-    assert np.array_equal(hs[0].get_state()["W"], hs[1].get_state()["W"])
-    with pytest.raises(abi.IcsError):
-        hs[0].set_tuning(op1_blocks=10)
 
 
 @pytest.mark.parametrize("precision", [0, 1])

@@ -1405,6 +1405,10 @@ int ics_save_checkpoint(ics_handle hh, void* buf, int64_t bytes) {
 int ics_load_checkpoint(ics_handle hh, const void* buf, int64_t bytes) {
   if (!hh || !buf || bytes < (int64_t)sizeof(CkptHeader)) return ICS_ERR_ARG;
   return guard(hh, [&](Handle& h) {
+    if (h.cases.n) {
+      h.err = "checkpoints do not carry the per-case controls of stacked cases";
+      return ICS_ERR_ARG;
+    }
     CkptHeader hd;
     std::memcpy(&hd, buf, sizeof(hd));
     const CkptHeader mine = ckpt_header(h);

@@ -264,7 +264,8 @@ int ics_pseudo_iteration_batch(ics_handle* handles, int32_t n, ics_iter_stats* s
  * The dot products of case k reduce over segments that depend only on its own
  * cell count, so a case's results do not depend on the other cases in the
  * stack.  Call once, before the first residual.  Not with Harmonic Balance,
- * cyclic patches or the block-Jacobi smoother solver (ICS_ERR_ARG).
+ * cyclic patches, the block-Jacobi smoother solver, the passive scalar or
+ * checkpoints (ICS_ERR_ARG).
  * (CUDA library.)                                                            */
 int ics_set_cases(ics_handle h, int32_t n_cases, const int32_t* case_start);
 /* Per case of a stacked handle, each array [n_cases] and optional: the L2 norm

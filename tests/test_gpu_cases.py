@@ -144,3 +144,11 @@ def test_invalid_stacks_are_refused(gpu_binding):
         h.scalar_enable(np.full(w.mesh.n_cells, 0.1), D=0.0, recon=0)
     with pytest.raises(abi.IcsError):
         h.save_checkpoint()
+    plain = _open(gpu_binding, cases.shock_tube(100, ordering_mode="colour"))
+    plain.set_primitive(*(np.ones(100) * 1e5, np.zeros((100, 3)), np.ones(100) * 300.0))
+    blob = plain.save_checkpoint()
+    w2, start2 = cases.stack_cases(_tubes((40, 60)))
+    h2 = _open(gpu_binding, w2)
+    h2.set_cases(start2)
+    with pytest.raises(abi.IcsError):
+        h2.load_checkpoint(blob)

@@ -897,7 +897,9 @@ def main():
     value = N * args.steps * dist.world / (mixed["ms"] / 1000.0)
     value64 = N * args.steps * dist.world / (fp64["ms"] / 1000.0)
     extra = {}
-    if dist.rank == 0 and args.to_solution:
+    # the long single-GPU legs run only in a 1-GPU run: a scaling run holds all
+    # N GPUs while rank 0 would run them
+    if dist.rank == 0 and args.to_solution and dist.world == 1:
         # first-order reconstruction reaches 1e-8 in both precisions; the
         # second-order vanLeer one stalls at ~1.3e-8 on this mesh (milestones
         # to 2e-8); the configured Venkatakrishnan limiter's plateau recorded
@@ -905,7 +907,7 @@ def main():
         second = run_solution_pair(w, args.solution_cap_s, SOLUTION_SETTINGS, plateau_cap_s=args.plateau_cap_s)
         extra["to_solution"] = {"first_order": first, "second_order": second}
     e2e = run_e2e(w, args.steps, args.warmup) if dist.rank == 0 else None
-    if dist.rank == 0 and args.extras:
+    if dist.rank == 0 and args.extras and dist.world == 1:
         extra["harmonic_balance"] = run_hb_sweep()
         extra["batch_independent_cases"] = run_batch()
         extra["derivatives"] = run_diff()
@@ -972,7 +974,8 @@ def main():
                 byts = kernel_bytes(k, N, F, B, nslots, False, 2)
                 if byts:
                     fp64_table[k]["GBps"] = round(byts / (ms / n / 1000.0) / 1e9, 1)
-    cpu = cpu_sample((args.nx, args.ny, args.nz), args.cpu_seconds) if dist.rank == 0 else None
+    # the CPU baseline: rank 0 of a 1-GPU run only
+    cpu = cpu_sample((args.nx, args.ny, args.nz), args.cpu_seconds) if dist.rank == 0 and dist.world == 1 else None
     if dist.rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,

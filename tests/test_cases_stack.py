@@ -58,3 +58,19 @@ def test_stacked_residual_matvec_and_lusgs_are_the_cases(oracle_binding):
         assert relerr(r[sl], rk) < 1e-14
         assert relerr(y[sl], h.matrix_mul(x[sl])) < 1e-14
         assert relerr(z[sl], h.precondition(x[sl])) < 1e-14
+
+
+def test_stack_refuses_cyclic_and_mixed_dimensions():
+    import pytest
+
+    from icsfoam_gb300 import mesh as M
+
+    tube = cases.shock_tube(20).mesh        # 1-D: y and z empty
+    bump = cases.bump_channel(4, 2, 2).mesh  # 3-D
+    with pytest.raises(ValueError):
+        M.stack([tube, bump])
+    sector = cases.annular_sector(2, 4, 4, sides="cyclic").mesh
+    with pytest.raises(ValueError):
+        M.stack([sector, sector])
+    with pytest.raises(ValueError):
+        M.stack([])

@@ -53,6 +53,8 @@ def parse():
                     help="time cap of the mixed-precision leg to 1e-8 (the FP64 leg gets 2.5x)")
     ap.add_argument("--plateau-cap-s", type=float, default=15.0,
                     help="seconds of the configured Venkatakrishnan limiter (mixed) recording its plateau")
+    ap.add_argument("--study-box-first", type=int, default=0,
+                    help="with --convergence-study: only the viscous box of this size, first order")
     ap.add_argument("--batch", type=int, default=0,
                     help="only the batch of this many independent shock-tube cases")
     ap.add_argument("--batch-stacked-only", type=int, default=0,
@@ -430,10 +432,10 @@ def _study_workload(name):
 
     if name == "bump_64x16x16":
         return cases.bump_channel(64, 16, 16, ordering_mode="colour")
-    return cases.random_box(24)
+    return cases.random_box(int(name.rsplit("_", 1)[1]))
 
 
-def run_convergence_study(iters=1500, every=50):
+def run_convergence_study(iters=1500, every=50, runs=None):
     """rho L2 histories of the reduced bump channel (64x16x16) and viscous box
     (24^3) under the configured cellLimited<Venkatakrishnan> gradients, under
     cellLimited<minmod> and under the vanLeer limitedScheme, from the GPU
@@ -444,9 +446,11 @@ def run_convergence_study(iters=1500, every=50):
 
     from icsfoam_gb300 import cases, gpu
 
-    runs = [(name, label, settings) for name in ("bump_64x16x16", "random_box_24")
-            for label, settings in (("venkatakrishnan", {}), ("minmod", {"recon_rho": 4, "recon_U": 4, "recon_T": 4}),
-                                    ("vanleer", SOLUTION_SETTINGS))]
+    if runs is None:
+        runs = [(name, label, settings) for name in ("bump_64x16x16", "random_box_24")
+                for label, settings in (("venkatakrishnan", {}),
+                                        ("minmod", {"recon_rho": 4, "recon_U": 4, "recon_T": 4}),
+                                        ("vanleer", SOLUTION_SETTINGS))]
     ctx = mp.get_context("spawn")
     with ctx.Pool(len(runs)) as pool:
         pending = pool.map_async(_history_worker, [(n, st, iters, every) for n, _, st in runs])
@@ -877,7 +881,11 @@ def main():
         dist.close()
         return
     if args.convergence_study:
-        print(json.dumps({"convergence_study": run_convergence_study(args.convergence_study)}), flush=True)
+        runs = None
+        if args.study_box_first:
+            # the viscous box with first-order reconstruction, GPU and oracle in lockstep
+            runs = [("random_box_%d" % args.study_box_first, "first_order", FIRST_ORDER_SETTINGS)]
+        print(json.dumps({"convergence_study": run_convergence_study(args.convergence_study, runs=runs)}), flush=True)
         dist.close()
         return
     if args.viscous_solution:
